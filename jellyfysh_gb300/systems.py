@@ -1,0 +1,99 @@
+"""Seeded synthetic initial states of the benchmark and parity systems.
+
+The reference draws random positions without overlap rejection and gives every atom the same charge
+(``input_output_handler/input_handler/random_node_creator/atom_random_node_creator.py:56-67``), so the states
+here are generated directly: random sequential addition for hard spheres and point charges with a hard core,
+simple-cubic and face-centred-cubic lattices with uniform jitter for dense systems.  All generators take a
+``numpy.random.Generator`` and return float64 arrays of shape ``(n, 3)`` with every coordinate in ``[0, L)``.
+"""
+import math
+from typing import Optional
+
+import numpy as np
+
+
+def _wrap(positions: np.ndarray, system_length: float) -> np.ndarray:
+    positions = np.mod(positions, system_length)
+    positions[positions >= system_length] = 0.0
+    return positions
+
+
+def random_sequential_addition(n: int, radius: float, system_length: float, rng: np.random.Generator,
+                               max_trials: int = 10_000_000) -> np.ndarray:
+    """Uniform trial points; a trial closer than ``2 * radius`` (minimum image) to a placed sphere is rejected."""
+    diameter_sq = (2.0 * radius) ** 2
+    placed = np.zeros((n, 3), dtype=np.float64)
+    count = 0
+    trials = 0
+    batch = 256
+    while count < n:
+        candidates = rng.uniform(0.0, system_length, size=(batch, 3))
+        for candidate in candidates:
+            trials += 1
+            if trials > max_trials:
+                raise RuntimeError("random sequential addition did not place %d spheres" % n)
+            if count:
+                separation = placed[:count] - candidate
+                separation -= system_length * np.round(separation / system_length)
+                if np.min(np.einsum("ij,ij->i", separation, separation)) < diameter_sq:
+                    continue
+            placed[count] = candidate
+            count += 1
+            if count == n:
+                break
+    return _wrap(placed, system_length)
+
+
+def simple_cubic_jitter(n: int, system_length: float, jitter: float, rng: np.random.Generator) -> np.ndarray:
+    """First ``n`` sites (lexicographic order) of an ``m^3`` simple-cubic lattice, ``m = ceil(n^(1/3))``, plus a
+    uniform jitter in ``[-jitter, jitter]`` per coordinate."""
+    m = int(math.ceil(round(n ** (1.0 / 3.0), 9)))
+    while m ** 3 < n:
+        m += 1
+    spacing = system_length / m
+    grid = np.stack(np.meshgrid(np.arange(m), np.arange(m), np.arange(m), indexing="ij"), axis=-1).reshape(-1, 3)
+    sites = (grid[:n].astype(np.float64) + 0.5) * spacing
+    sites += rng.uniform(-jitter, jitter, size=sites.shape)
+    return _wrap(sites, system_length)
+
+
+def fcc_jitter(n: int, system_length: float, jitter_fraction: float, rng: np.random.Generator) -> np.ndarray:
+    """First ``n`` sites of a face-centred-cubic lattice of ``k^3`` cubic cells, ``k = ceil((n/4)^(1/3))``, plus a
+    uniform jitter of ``+-jitter_fraction`` of the nearest-neighbour spacing per coordinate."""
+    k = max(1, int(math.ceil(round((n / 4.0) ** (1.0 / 3.0), 9))))
+    while 4 * k ** 3 < n:
+        k += 1
+    a = system_length / k
+    basis = np.array([[0.0, 0.0, 0.0], [0.5, 0.5, 0.0], [0.5, 0.0, 0.5], [0.0, 0.5, 0.5]])
+    grid = np.stack(np.meshgrid(np.arange(k), np.arange(k), np.arange(k), indexing="ij"), axis=-1).reshape(-1, 3)
+    sites = (grid[:, None, :] + basis[None, :, :]).reshape(-1, 3)[:n] * a + 0.25 * a
+    spacing = a / math.sqrt(2.0)
+    sites = sites + rng.uniform(-jitter_fraction * spacing, jitter_fraction * spacing, size=sites.shape)
+    return _wrap(sites, system_length)
+
+
+def alternating_charges(n: int) -> np.ndarray:
+    """Charges +1, -1, +1, ... (``n/2`` of each sign for even ``n``)."""
+    charges = np.ones(n, dtype=np.float64)
+    charges[1::2] = -1.0
+    return charges
+
+
+def hard_sphere_box(n: int, packing_fraction: float, radius: float = 1.0) -> float:
+    """Side of the cubic box holding ``n`` spheres of ``radius`` at ``packing_fraction``."""
+    return (n * 4.0 / 3.0 * math.pi * radius ** 3 / packing_fraction) ** (1.0 / 3.0)
+
+
+def lennard_jones_box(n: int, density: float, sigma: float = 1.0) -> float:
+    return (n / density) ** (1.0 / 3.0) * sigma
+
+
+def min_image_min_distance(positions: np.ndarray, system_length: float, limit: Optional[int] = None) -> float:
+    """Smallest minimum-image pair distance (for checks of generated states)."""
+    p = positions if limit is None else positions[:limit]
+    best = math.inf
+    for i in range(len(p) - 1):
+        s = p[i + 1:] - p[i]
+        s -= system_length * np.round(s / system_length)
+        best = min(best, float(np.sqrt(np.min(np.einsum("ij,ij->i", s, s)))))
+    return best

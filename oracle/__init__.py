@@ -1,0 +1,303 @@
+"""CPU oracle of the ECMC event-time path: ctypes front end of ``oracle/jf_oracle.c``.
+
+TEST INFRASTRUCTURE ONLY.  This package is the checker of the GPU product.  Only ``tests/``,
+``__graft_entry__.smoke()`` and the CPU-baseline leg of ``bench.py`` import it; the product package
+``jellyfysh_gb300`` never does.
+
+The C library restates JeLLyFysh's arithmetic with CPython 3.12 float semantics; see the header of
+``jf_oracle.c`` for the file-by-file map onto the reference.
+"""
+import ctypes
+import math
+from typing import Optional, Sequence
+
+import numpy as np
+
+from .build_oracle import build as _build
+
+EV_PAIR, EV_BOUNDED, EV_HARDCORE, EV_CELL_BOUNDING, EV_CELL_VETO, EV_BOUNDARY, EV_END_OF_CHAIN, EV_STOP = range(8)
+POT_HARD_SPHERE, POT_LENNARD_JONES, POT_COULOMB = range(3)
+FAR_NONE, FAR_CELL_VETO, FAR_CELL_BOUNDING = range(3)
+RNG_PAIR, RNG_THIN, RNG_VETO_TIME, RNG_VETO_CHOICE, RNG_VETO_UNIFORM, RNG_NEW_ACTIVE = range(6)
+
+STATUS_NAMES = {0: "ok", 1: "ValueError", 2: "AssertionError", 3: "ZeroDivisionError", 4: "complex result",
+                5: "bad configuration", 6: "allocation failure", 7: "cell index out of range"}
+
+
+class OracleError(RuntimeError):
+    pass
+
+
+class JfoSystem(ctypes.Structure):
+    _fields_ = [("n", ctypes.c_int), ("system_length", ctypes.c_double), ("cells_per_side", ctypes.c_int),
+                ("neighbor_layers", ctypes.c_int), ("max_occupants", ctypes.c_int), ("beta", ctypes.c_double),
+                ("chain_time", ctypes.c_double), ("speed", ctypes.c_double), ("initial_direction", ctypes.c_int),
+                ("initial_active", ctypes.c_int), ("potential", ctypes.c_int), ("hs_radius", ctypes.c_double),
+                ("lj_prefactor", ctypes.c_double), ("lj_sigma", ctypes.c_double),
+                ("coulomb_prefactor", ctypes.c_double), ("bound_prefactor", ctypes.c_double),
+                ("ewald_alpha", ctypes.c_double), ("fourier_cutoff", ctypes.c_int),
+                ("position_cutoff", ctypes.c_int), ("far", ctypes.c_int), ("estimator_points", ctypes.c_int),
+                ("estimator_prefactor", ctypes.c_double), ("rng_key", ctypes.c_uint64)]
+
+
+EVENT_DTYPE = np.dtype([("kind", np.int32), ("moved", np.int32), ("target", np.int32), ("new_active", np.int32),
+                        ("new_direction", np.int32), ("accepted", np.int32), ("time_q", np.float64),
+                        ("time_r", np.float64), ("x", np.float64), ("y", np.float64), ("z", np.float64)])
+
+_LIB = None
+_D = ctypes.c_double
+_PD = ctypes.POINTER(ctypes.c_double)
+
+
+def lib() -> ctypes.CDLL:
+    global _LIB
+    if _LIB is None:
+        handle = ctypes.CDLL(_build())
+        handle.jfo_py_mod.restype = _D
+        handle.jfo_py_mod.argtypes = [_D, _D]
+        handle.jfo_py_divmod.argtypes = [_D, _D, _PD, _PD]
+        handle.jfo_py_sum.restype = _D
+        handle.jfo_py_sum.argtypes = [_PD, ctypes.c_int]
+        handle.jfo_time_add.argtypes = [_D, _D, _D, _PD, _PD]
+        handle.jfo_time_sub.restype = _D
+        handle.jfo_time_sub.argtypes = [_D, _D, _D, _D]
+        handle.jfo_chain_key.restype = ctypes.c_uint64
+        handle.jfo_chain_key.argtypes = [ctypes.c_uint64, ctypes.c_uint64]
+        handle.jfo_draw.restype = ctypes.c_uint64
+        handle.jfo_draw.argtypes = [ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint32, ctypes.c_uint32]
+        handle.jfo_uniform.restype = _D
+        handle.jfo_uniform.argtypes = [ctypes.c_uint64]
+        handle.jfo_log.restype = _D
+        handle.jfo_log.argtypes = [_D]
+        handle.jfo_expovariate.restype = _D
+        handle.jfo_expovariate.argtypes = [ctypes.c_uint64, _D]
+        handle.jfo_randbelow.restype = ctypes.c_uint32
+        handle.jfo_randbelow.argtypes = [ctypes.c_uint64, ctypes.c_uint32]
+        handle.jfo_hs_displacement.argtypes = [_D, _PD, _PD, _PD]
+        handle.jfo_ip_displacement.argtypes = [_D, _D, _PD, _PD, _D, _D, _D, _PD]
+        handle.jfo_ip_derivative.argtypes = [_D, _D, _PD, _PD, _D, _D, _PD]
+        handle.jfo_lj_displacement.argtypes = [_D, _D, _PD, _PD, _D, _PD]
+        handle.jfo_lj_derivative.argtypes = [_D, _D, _PD, _PD, _PD]
+        handle.jfo_dep_displacement.argtypes = [_D, ctypes.c_int, _D, _PD, _PD, _D, _PD]
+        handle.jfo_dep_derivative.argtypes = [_D, ctypes.c_int, _D, _PD, _PD, _PD]
+        handle.jfo_ipcb_displacement.argtypes = [_D, _D, _PD, _PD, _D, _D, _D, _PD]
+        handle.jfo_ipcb_derivative.argtypes = [_D, _PD, _PD, _D, _D, _PD]
+        handle.jfo_mic_x_derivative.restype = _D
+        handle.jfo_mic_x_derivative.argtypes = [_D, ctypes.c_int, ctypes.c_int, _D, _D, _D, _D]
+        handle.jfo_mic_derivative.argtypes = [_D, ctypes.c_int, ctypes.c_int, _D, _D, _PD, _PD, _D, _D, _PD]
+        handle.jfo_cell_bounds.argtypes = [_D, ctypes.c_int, _PD, _PD]
+        handle.jfo_chain_create.restype = ctypes.c_void_p
+        handle.jfo_chain_create.argtypes = [ctypes.POINTER(JfoSystem), _PD, _PD, ctypes.POINTER(ctypes.c_int)]
+        handle.jfo_chain_destroy.argtypes = [ctypes.c_void_p]
+        handle.jfo_chain_run.restype = ctypes.c_int64
+        handle.jfo_chain_run.argtypes = [ctypes.c_void_p, ctypes.c_int64, _D, _D, ctypes.c_void_p,
+                                         ctypes.POINTER(ctypes.c_int)]
+        handle.jfo_chain_positions.argtypes = [ctypes.c_void_p, _PD]
+        handle.jfo_chain_state.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int64),
+                                           ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int), _PD, _PD]
+        handle.jfo_chain_bounds.restype = ctypes.c_int
+        handle.jfo_chain_bounds.argtypes = [ctypes.c_void_p, _PD, ctypes.c_int]
+        handle.jfo_chain_walker.restype = ctypes.c_int
+        handle.jfo_chain_walker.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
+                                            ctypes.POINTER(ctypes.c_int32), _PD, ctypes.c_int, _PD]
+        _LIB = handle
+    return _LIB
+
+
+def _vec(values: Sequence[float]):
+    return (ctypes.c_double * 3)(*[float(v) for v in values])
+
+
+def _call(fn, *args) -> float:
+    out = ctypes.c_double()
+    status = fn(*args, ctypes.byref(out))
+    if status != 0:
+        raise OracleError(STATUS_NAMES.get(status, str(status)))
+    return out.value
+
+
+# ---- primitives ---------------------------------------------------------------------------------
+def py_mod(x: float, y: float) -> float:
+    return lib().jfo_py_mod(x, y)
+
+
+def py_divmod(x: float, y: float):
+    q, r = ctypes.c_double(), ctypes.c_double()
+    lib().jfo_py_divmod(x, y, ctypes.byref(q), ctypes.byref(r))
+    return q.value, r.value
+
+
+def py_sum(values: Sequence[float]) -> float:
+    array = (ctypes.c_double * len(values))(*values)
+    return lib().jfo_py_sum(array, len(values))
+
+
+def time_add(q: float, r: float, dt: float):
+    oq, orr = ctypes.c_double(), ctypes.c_double()
+    lib().jfo_time_add(q, r, dt, ctypes.byref(oq), ctypes.byref(orr))
+    return oq.value, orr.value
+
+
+def chain_key(seed: int, chain: int) -> int:
+    return lib().jfo_chain_key(seed, chain)
+
+
+def draw(key: int, event: int, kind: int, target: int) -> int:
+    return lib().jfo_draw(key, event, kind, target)
+
+
+def uniform(bits: int) -> float:
+    return lib().jfo_uniform(bits)
+
+
+def log(x: float) -> float:
+    return lib().jfo_log(x)
+
+
+def expovariate(bits: int, beta: float) -> float:
+    return lib().jfo_expovariate(bits, beta)
+
+
+def randbelow(bits: int, n: int) -> int:
+    return lib().jfo_randbelow(bits, n)
+
+
+# ---- potentials (reference argument order: velocity, separation, [charges], [potential_change]) ----
+def hs_displacement(radius, velocity, separation) -> float:
+    return _call(lib().jfo_hs_displacement, radius, _vec(velocity), _vec(separation))
+
+
+def ip_displacement(power, prefactor, velocity, separation, charge_one, charge_two, potential_change) -> float:
+    return _call(lib().jfo_ip_displacement, power, prefactor, _vec(velocity), _vec(separation), charge_one,
+                 charge_two, potential_change)
+
+
+def ip_derivative(power, prefactor, velocity, separation, charge_one, charge_two) -> float:
+    return _call(lib().jfo_ip_derivative, power, prefactor, _vec(velocity), _vec(separation), charge_one,
+                 charge_two)
+
+
+def lj_displacement(prefactor, sigma, velocity, separation, potential_change) -> float:
+    return _call(lib().jfo_lj_displacement, prefactor, sigma, _vec(velocity), _vec(separation), potential_change)
+
+
+def lj_derivative(prefactor, sigma, velocity, separation) -> float:
+    return _call(lib().jfo_lj_derivative, prefactor, sigma, _vec(velocity), _vec(separation))
+
+
+def dep_displacement(r0, power, prefactor, velocity, separation, potential_change) -> float:
+    return _call(lib().jfo_dep_displacement, r0, int(power), prefactor, _vec(velocity), _vec(separation),
+                 potential_change)
+
+
+def dep_derivative(r0, power, prefactor, velocity, separation) -> float:
+    return _call(lib().jfo_dep_derivative, r0, int(power), prefactor, _vec(velocity), _vec(separation))
+
+
+def ipcb_displacement(prefactor, system_length, velocity, separation, charge_one, charge_two,
+                      potential_change) -> float:
+    return _call(lib().jfo_ipcb_displacement, prefactor, system_length, _vec(velocity), _vec(separation),
+                 charge_one, charge_two, potential_change)
+
+
+def ipcb_derivative(prefactor, velocity, separation, charge_one, charge_two) -> float:
+    return _call(lib().jfo_ipcb_derivative, prefactor, _vec(velocity), _vec(separation), charge_one, charge_two)
+
+
+def mic_derivative(alpha, fourier_cutoff, position_cutoff, prefactor, system_length, velocity, separation,
+                   charge_one, charge_two) -> float:
+    return _call(lib().jfo_mic_derivative, alpha, fourier_cutoff, position_cutoff, prefactor, system_length,
+                 _vec(velocity), _vec(separation), charge_one, charge_two)
+
+
+def mic_x_derivative(alpha, fourier_cutoff, position_cutoff, system_length, sx, sy, sz) -> float:
+    return lib().jfo_mic_x_derivative(alpha, fourier_cutoff, position_cutoff, system_length, sx, sy, sz)
+
+
+def cell_bounds(system_length: float, cells_per_side: int):
+    lo = (ctypes.c_double * cells_per_side)()
+    hi = (ctypes.c_double * cells_per_side)()
+    lib().jfo_cell_bounds(system_length, cells_per_side, lo, hi)
+    return list(lo), list(hi)
+
+
+# ---- chains -------------------------------------------------------------------------------------
+SYSTEM_DEFAULTS = dict(neighbor_layers=1, max_occupants=1, beta=1.0, chain_time=1.0, speed=1.0,
+                       initial_direction=0, initial_active=0, potential=POT_HARD_SPHERE, hs_radius=0.0,
+                       lj_prefactor=1.0, lj_sigma=1.0, coulomb_prefactor=1.0, bound_prefactor=1.5837,
+                       ewald_alpha=3.45, fourier_cutoff=6, position_cutoff=2, far=FAR_NONE, estimator_points=10,
+                       estimator_prefactor=1.5, rng_key=0)
+
+
+def make_system(**kwargs) -> JfoSystem:
+    values = dict(SYSTEM_DEFAULTS)
+    values.update(kwargs)
+    return JfoSystem(**values)
+
+
+class Chain:
+    """One ECMC chain run by the oracle (single thread; ctypes releases the GIL during runs)."""
+
+    def __init__(self, system: JfoSystem, positions: np.ndarray, charges: Optional[np.ndarray] = None):
+        positions = np.ascontiguousarray(positions, dtype=np.float64).reshape(-1, 3)
+        assert positions.shape[0] == system.n
+        self.system = system
+        self._positions_in = positions
+        charge_pointer = None
+        if charges is not None:
+            self._charges_in = np.ascontiguousarray(charges, dtype=np.float64)
+            charge_pointer = self._charges_in.ctypes.data_as(_PD)
+        status = ctypes.c_int()
+        self._handle = lib().jfo_chain_create(ctypes.byref(system), positions.ctypes.data_as(_PD), charge_pointer,
+                                              ctypes.byref(status))
+        if not self._handle:
+            raise OracleError("chain creation failed: " + STATUS_NAMES.get(status.value, str(status.value)))
+
+    def __del__(self):
+        handle = getattr(self, "_handle", None)
+        if handle:
+            lib().jfo_chain_destroy(handle)
+            self._handle = None
+
+    def run(self, max_events: int, stop_time: Optional[float] = None, record: bool = True):
+        """Advance by at most ``max_events`` events; returns the event log (or the count)."""
+        stop_q, stop_r = (math.inf, math.inf) if stop_time is None else divmod(stop_time, 1.0)
+        log_array = np.zeros(max_events if record else 0, dtype=EVENT_DTYPE)
+        status = ctypes.c_int()
+        done = lib().jfo_chain_run(self._handle, max_events, stop_q, stop_r,
+                                   log_array.ctypes.data if record else None, ctypes.byref(status))
+        if status.value != 0:
+            raise OracleError("chain run stopped after %d events: %s"
+                              % (done, STATUS_NAMES.get(status.value, str(status.value))))
+        return log_array[:done] if record else done
+
+    def positions(self) -> np.ndarray:
+        out = np.zeros((self.system.n, 3), dtype=np.float64)
+        lib().jfo_chain_positions(self._handle, out.ctypes.data_as(_PD))
+        return out
+
+    def state(self):
+        event, active, direction = ctypes.c_int64(), ctypes.c_int(), ctypes.c_int()
+        q, r = ctypes.c_double(), ctypes.c_double()
+        lib().jfo_chain_state(self._handle, ctypes.byref(event), ctypes.byref(active), ctypes.byref(direction),
+                              ctypes.byref(q), ctypes.byref(r))
+        return dict(events=event.value, active=active.value, direction=direction.value, time_q=q.value,
+                    time_r=r.value)
+
+    def bounds(self) -> np.ndarray:
+        need = -lib().jfo_chain_bounds(self._handle, None, 0)
+        if need <= 0:
+            return np.zeros((0,))
+        out = np.zeros(need, dtype=np.float64)
+        lib().jfo_chain_bounds(self._handle, out.ctypes.data_as(_PD), need)
+        cells = need // 6
+        return out.reshape(2, cells, 3)
+
+    def walker(self, direction: int, which: int = 0):
+        size = -lib().jfo_chain_walker(self._handle, direction, which, None, None, 0, None)
+        cells = np.zeros((size, 2), dtype=np.int32)
+        rates = np.zeros(size, dtype=np.float64)
+        total = ctypes.c_double()
+        lib().jfo_chain_walker(self._handle, direction, which, cells.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)),
+                               rates.ctypes.data_as(_PD), size, ctypes.byref(total))
+        return cells, rates, total.value
