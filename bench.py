@@ -1,0 +1,357 @@
+"""Benchmark of the GB300 event-time engine: events/s of batched Lennard-Jones ECMC chains.
+
+Workload (one step = every chain advances ``--events`` events):
+    4096 independent chains of N = 1024 Lennard-Jones atoms (epsilon = sigma = 1, density 0.8, beta = 1/1.2),
+    periodic cube L = (1024 / 0.8)^(1/3), 12^3 cells with 3 neighbour layers (nearby cells cover 2.5 sigma),
+    far field by the cell-bounding potential (InnerPointEstimator bounds, prefactor 1.5, 10 points per side),
+    chain time 2 sigma with directions +x -> +y -> +z, seeded simple-cubic lattice plus +-0.05 sigma jitter.
+    Mixed precision: FP32 screening of every candidate, FP64 re-solve of the near-winners (the event times are the
+    FP64 ones).  The working set (positions, FP32 mirror, occupancy: ~210 MB) is larger than the 126 MB L2.
+
+Arms:
+    default            the GPU engine (value = device-timed events/s; e2e = through ChainBatch with host buffers)
+    --impl reference   the CPU oracle (a C restatement of the reference's event loop) on all host threads
+
+Multi-GPU: one process per GPU under torchrun; every rank runs its own 4096 chains (independent replicas, no
+collective on the data path), value = all ranks' events / max-over-ranks time.
+"""
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "events/s on 1 GB300, batched mixed-precision vs plain FP64 at <=1e-9 rel err"
+WORKLOAD = dict(workload="lennard_jones_chains_4096x1024_cell_bounding", chains=4096, n=1024, density=0.8,
+                beta=1.0 / 1.2, cells_per_side=12, neighbor_layers=3, chain_time=2.0, far="cell_bounding",
+                jitter=0.05, estimator_points=10, estimator_prefactor=1.5)
+CELLS = WORKLOAD["cells_per_side"] ** 3
+# measured DRAM traffic of the chain kernel per committed event (ncu dram__bytes_read.sum + write.sum of one launch
+# of this workload divided by its events; see profiles/chains_kernel_lennard_jones_4096x1024.md); None if unknown
+NCU_TRAFFIC_PER_EVENT = None
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    p.add_argument("--events", type=int, default=128, help="events per chain and step")
+    p.add_argument("--chains", type=int, default=WORKLOAD["chains"])
+    p.add_argument("--block-warps", type=int, default=0, help="warps per block (0 = autotune)")
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-fp64", action="store_true")
+    return p.parse_args()
+
+
+def make_workload(chains, seed_offset=0):
+    from jellyfysh_gb300 import ChainSpec, systems
+    n = WORKLOAD["n"]
+    length = systems.lennard_jones_box(n, WORKLOAD["density"])
+    rng = np.random.default_rng(1234 + seed_offset)
+    specs, positions = [], []
+    for c in range(chains):
+        specs.append(ChainSpec(n=n, system_length=length, cells_per_side=WORKLOAD["cells_per_side"],
+                               potential="lennard_jones", far=WORKLOAD["far"],
+                               neighbor_layers=WORKLOAD["neighbor_layers"], beta=WORKLOAD["beta"],
+                               chain_time=WORKLOAD["chain_time"], estimator_points=WORKLOAD["estimator_points"],
+                               estimator_prefactor=WORKLOAD["estimator_prefactor"],
+                               initial_active=int(rng.integers(n)), initial_direction=int(rng.integers(3))))
+        positions.append(systems.simple_cubic_jitter(n, length, WORKLOAD["jitter"], rng))
+    return specs, positions, length
+
+
+class ClockSampler:
+    """nvidia-smi samples of the SM clock and throttle reasons during the timed region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.QUERY,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, sm_max, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                sm_max = max(sm_max, float(parts[2]))
+            except ValueError:
+                continue
+            for name, flag in zip(names, parts[5:9]):
+                if flag.lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": sm_max, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as handle:
+            data = json.load(handle)
+        return float(data["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def cpu_reference_sample(threads, events_per_chain, chains_per_thread=1):
+    """The oracle (C restatement of the reference's event loop) on host threads; returns events/s."""
+    import concurrent.futures
+    import oracle
+    specs, positions, length = make_workload(threads * chains_per_thread, seed_offset=99)
+    systems = []
+    for c, spec in enumerate(specs):
+        systems.append(oracle.make_system(
+            n=spec.n, system_length=spec.system_length, cells_per_side=spec.cells_per_side,
+            neighbor_layers=spec.neighbor_layers, max_occupants=1, beta=spec.beta, chain_time=spec.chain_time,
+            initial_active=spec.initial_active, initial_direction=spec.initial_direction,
+            potential=oracle.POT_LENNARD_JONES, far=oracle.FAR_CELL_BOUNDING,
+            estimator_points=spec.estimator_points, estimator_prefactor=spec.estimator_prefactor,
+            rng_key=oracle.chain_key(99, c)))
+    with concurrent.futures.ThreadPoolExecutor(max_workers=threads) as pool:
+        chains = list(pool.map(lambda i: oracle.Chain(systems[i], positions[i]), range(len(systems))))
+        start = time.perf_counter()
+        done = list(pool.map(lambda ch: ch.run(events_per_chain, record=False), chains))
+        elapsed = time.perf_counter() - start
+    return sum(done) / elapsed, sum(done), elapsed
+
+
+def reference_arm(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    events = 60
+    values = []
+    for _ in range(args.warmup):
+        cpu_reference_sample(threads, 10)
+    total_events, total_time = 0, 0.0
+    for _ in range(args.steps):
+        rate, done, elapsed = cpu_reference_sample(threads, events)
+        values.append(rate)
+        total_events += done
+        total_time += elapsed
+    value = total_events / total_time
+    config = dict(WORKLOAD)
+    config["sample"] = "%d chains x %d events per step" % (threads, events)
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "events/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * total_time / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic: seeded simple-cubic lattice + uniform jitter", "config": config,
+            "cpu_baseline": {"value": value, "unit": "events/s", "cores": threads, "kind": "port",
+                             "sample": config["sample"]},
+            "e2e": {"value": value, "unit": "events/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def autotune(batch, events):
+    """Pick warps per block of the mixed kernel by a short timed sweep."""
+    import torch
+    best, best_time = 4, math.inf
+    for warps in (1, 2, 4, 8):
+        batch.set_block_warps(warps)
+        torch.cuda.synchronize()
+        start = time.perf_counter()
+        batch.run(events, mode="mixed")
+        elapsed = time.perf_counter() - start
+        if elapsed < best_time:
+            best, best_time = warps, elapsed
+    batch.set_block_warps(best)
+    return best
+
+
+def gpu_arm(args):
+    import torch
+    import torch.distributed as dist
+    from jellyfysh_gb300 import ChainBatch
+    from jellyfysh_gb300.chains import STATE_DTYPE
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    device = torch.device("cuda", local)
+    specs, positions, length = make_workload(args.chains, seed_offset=rank)
+    batch = ChainBatch(specs, positions, seed=1000 + rank, device="cuda:%d" % local)
+    stream = torch.cuda.current_stream(device)
+    warps = args.block_warps or autotune(batch, 8)
+    batch.set_block_warps(warps)
+    for _ in range(args.warmup):
+        batch.run(args.events, mode="mixed")
+    batch.check_status()
+    state0 = batch.state()
+    launches0 = batch.launch_count()
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize(device)
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    with ClockSampler(local) as clocks:
+        begin = torch.cuda.Event(enable_timing=True)
+        finish = torch.cuda.Event(enable_timing=True)
+        begin.record(stream)
+        for s in range(args.steps):
+            starts[s].record(stream)
+            batch.run(args.events, mode="mixed", sync=False)
+            ends[s].record(stream)
+        finish.record(stream)
+        torch.cuda.synchronize(device)
+    elapsed_ms = begin.elapsed_time(finish)
+    launches = batch.launch_count() - launches0
+    kernel_ms = [a.elapsed_time(b) for a, b in zip(starts, ends)]
+    batch.check_status()
+    state1 = batch.state()
+    events_done = int(state1["events"].sum() - state0["events"].sum())
+    candidates = int(state1["candidates"].sum() - state0["candidates"].sum())
+    refined = int(state1["refined"].sum() - state0["refined"].sum())
+    fallbacks = int(state1["refine_fallbacks"].sum() - state0["refine_fallbacks"].sum())
+    elapsed_t = torch.tensor([elapsed_ms], dtype=torch.float64, device=device)
+    events_t = torch.tensor([events_done], dtype=torch.float64, device=device)
+    if world > 1:
+        dist.all_reduce(elapsed_t, op=dist.ReduceOp.MAX)
+        dist.all_reduce(events_t, op=dist.ReduceOp.SUM)
+    total_ms = float(elapsed_t.item())
+    value = float(events_t.item()) / (total_ms / 1000.0)
+
+    # end to end through ChainBatch with host buffers: H2D of the chain state, the run, D2H of the results
+    host = [t.cpu().pin_memory() for t in batch.state_tensors()]
+    results = [batch.positions_dev, batch.state_dev]
+    host_results = [t.cpu().pin_memory() for t in results]
+    h2d = sum(t.numel() * t.element_size() for t in host)
+    d2h = sum(t.numel() * t.element_size() for t in host_results)
+    e2e_steps = max(2, args.steps // 2)
+    state_before = batch.state()
+    torch.cuda.synchronize(device)
+    e_begin = torch.cuda.Event(enable_timing=True)
+    e_end = torch.cuda.Event(enable_timing=True)
+    e_begin.record(stream)
+    for _ in range(e2e_steps):
+        for dst, src in zip(batch.state_tensors(), host):
+            dst.copy_(src, non_blocking=True)
+        batch.run(args.events, mode="mixed", sync=False)
+        for dst, src in zip(host_results, results):
+            dst.copy_(src, non_blocking=True)
+    e_end.record(stream)
+    torch.cuda.synchronize(device)
+    e2e_ms = e_begin.elapsed_time(e_end)
+    e2e_events = e2e_steps * sum(1 for _ in specs) * args.events
+    e2e_value = e2e_events / (e2e_ms / 1000.0)
+    del state_before
+
+    # plain FP64, one chain per launch (the baseline of the mixed-precision batching)
+    fp64 = None
+    if not args.no_fp64:
+        fp64_chains, fp64_events = 8, 16
+        torch.cuda.synchronize(device)
+        f_begin = torch.cuda.Event(enable_timing=True)
+        f_end = torch.cuda.Event(enable_timing=True)
+        s_before = batch.state()
+        f_begin.record(stream)
+        for c in range(fp64_chains):
+            batch.run(fp64_events, mode="exact", first=c, count=1, sync=False)
+        f_end.record(stream)
+        torch.cuda.synchronize(device)
+        f_ms = f_begin.elapsed_time(f_end)
+        s_after = batch.state()
+        f_done = int(s_after["events"][:fp64_chains].sum() - s_before["events"][:fp64_chains].sum())
+        fp64 = {"value": f_done / (f_ms / 1000.0), "unit": "events/s",
+                "sample": "%d chains x %d events, one launch per chain" % (fp64_chains, fp64_events),
+                "speedup_of_batched_mixed": value / (f_done / (f_ms / 1000.0))}
+
+    if rank != 0:
+        if world > 1:
+            dist.barrier()
+            dist.destroy_process_group()
+        return
+
+    # roofline of the chain kernel: algorithmic bytes per event (cell scan of every cell, FP32 neighbour
+    # positions and identifiers of the pair candidates, active position write, cell index and time)
+    events_per_launch = args.chains * args.events
+    nb = candidates / max(events_done, 1)
+    bytes_per_event = 4 * CELLS + 12 * nb + 4 * nb + 32
+    kernel_s = float(np.mean(kernel_ms)) / 1000.0
+    achieved = bytes_per_event * events_per_launch / kernel_s / 1e9
+    peak, peak_kind = measured_peaks()
+    traffic = None if NCU_TRAFFIC_PER_EVENT is None else NCU_TRAFFIC_PER_EVENT * events_per_launch
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": traffic, "peak_source": peak_kind, "bytes_per_event": bytes_per_event,
+                "neighbours_per_event": nb, "refined_per_event": refined / max(events_done, 1),
+                "fallback_events": fallbacks, "kernel": "jf::chains_kernel<1>"}
+    cpu = None
+    if not args.no_cpu_baseline and world == 1:
+        threads = os.cpu_count() or 1
+        rate, done, elapsed = cpu_reference_sample(threads, 40)
+        cpu = {"value": rate, "unit": "events/s", "cores": threads, "kind": "port",
+               "sample": "%d chains x 40 events of the same workload, one chain per thread (%.1f s)"
+                         % (threads, elapsed)}
+    config = dict(WORKLOAD)
+    config.update(chains=args.chains, events_per_chain_per_step=args.events, block_warps=warps,
+                  l2="inputs larger than L2 (working set %.0f MB)" % (sum(
+                      t.numel() * t.element_size() for t in batch.state_tensors()) / 1e6),
+                  parallelism="replicas" if world > 1 else "single GPU")
+    line = {"metric": METRIC, "value": value, "unit": "events/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
+            "data": "synthetic: seeded simple-cubic lattice + uniform jitter", "config": config,
+            "e2e": {"value": e2e_value, "unit": "events/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+            "roofline": roofline, "cpu_baseline": cpu, "gpu_launches": launches, "clocks": clocks.summary(),
+            "fp64_one_chain_per_launch": fp64}
+    print(json.dumps(line))
+    if world > 1:
+        dist.barrier()
+        dist.destroy_process_group()
+    batch.close()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        reference_arm(args)
+    else:
+        gpu_arm(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,232 @@
+/*
+ * jfgpu.h -- C ABI of the GB300 event-time engine for event-chain Monte Carlo (libjfgpu.so).
+ *
+ * Plain pointers and sizes only.  Arrays named "device" live in GPU memory owned by the caller (for example
+ * PyTorch tensors); the library owns only engines (contexts) and the lookup tables inside them.  Every function
+ * returns JFGPU_OK (0) or a nonzero error code and never aborts; per-element and per-chain results carry the
+ * status codes of the reference's exceptions (JFGPU_STATUS_*).  Streams are cudaStream_t passed as void*
+ * (NULL = the legacy default stream).
+ *
+ * Reference interfaces replaced (paths relative to the JeLLyFysh source tree):
+ *   jfgpu_*_displacement / jfgpu_*_derivative
+ *       Potential.displacement / Potential.derivative          jellyfysh/potential/potential.py:153-253
+ *       (hard_sphere_potential.py:65-99, inverse_power_potential.py:71-179, lennard_jones_potential.py:63-135,
+ *        displaced_even_power_potential.py:73-142, abstracts.py:212-530,
+ *        inverse_power_coulomb_bounding_potential.c:53-139 via .py:111-140,
+ *        merged_image_coulomb_potential.c:205-274 via .py:128-154, cell_bounding_potential.py:155-238)
+ *   jfgpu_engine_create
+ *       construct_* / destroy_* contexts                        merged_image_coulomb_potential.c:77-156
+ *       CellBoundingPotential.initialize, CellVetoEventHandler.initialize (estimator scans, Walker tables)
+ *                                                               cell_bounding_potential.py:70-126,
+ *                                                               cell_veto_event_handler.py:93-160, walker.py:53-103
+ *   jfgpu_chains_init / jfgpu_chains_run
+ *       SingleProcessMediator.run with the event handlers, the heap scheduler, the tree state handler and the
+ *       single-active cell occupancy of the path              jellyfysh/mediator/single_process_mediator.py:91-156,
+ *       two_leaf_unit_event_handler.py:98-154, two_leaf_unit_bounding_potential_event_handler.py:112-168,
+ *       two_leaf_unit_cell_bounding_potential_event_handler.py:137-211, cell_veto_event_handler.py:162-238,
+ *       leaf_unit_cell_veto_event_handler.py:117-149, cell_boundary_event_handler.py:98-173,
+ *       single_independent_active_periodic_direction_end_of_chain_event_handler.py:151-237,
+ *       scheduler/heap_scheduler/heap.c:156-304, activator/internal_state/single_active_cell_occupancy.py:95-237
+ */
+#ifndef JFGPU_H
+#define JFGPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- return codes ---- */
+#define JFGPU_OK 0
+#define JFGPU_ERROR_CUDA 1
+#define JFGPU_ERROR_ARGUMENT 2
+#define JFGPU_ERROR_ALLOCATION 3
+#define JFGPU_ERROR_TABLE 4
+
+/* ---- per-element / per-chain status (the reference's exceptions) ---- */
+#define JFGPU_STATUS_OK 0
+#define JFGPU_STATUS_VALUE_ERROR 1     /* math.sqrt of a negative number */
+#define JFGPU_STATUS_ASSERTION 2       /* a failed assert of the reference */
+#define JFGPU_STATUS_ZERO_DIVISION 3   /* ZeroDivisionError of a float division */
+#define JFGPU_STATUS_COMPLEX 4         /* negative ** fractional */
+#define JFGPU_STATUS_CELL_RANGE 7      /* position outside the cell list */
+#define JFGPU_STATUS_EVENT_CAP 8       /* the refinement set of a mixed-precision event overflowed twice */
+
+/* ---- potentials ---- */
+#define JFGPU_POT_HARD_SPHERE 0
+#define JFGPU_POT_LENNARD_JONES 1
+#define JFGPU_POT_COULOMB 2            /* merged-image Coulomb bounded by the inverse-power Coulomb bound */
+
+/* ---- far fields ---- */
+#define JFGPU_FAR_NONE 0
+#define JFGPU_FAR_CELL_VETO 1
+#define JFGPU_FAR_CELL_BOUNDING 2
+
+/* ---- run modes ---- */
+#define JFGPU_MODE_EXACT 0             /* every candidate solved in FP64 with the reference's arithmetic */
+#define JFGPU_MODE_MIXED 1             /* FP32 screening of all candidates, FP64 re-solve of the near-winners */
+
+/* ---- event kinds of the event log ---- */
+#define JFGPU_EV_PAIR 0
+#define JFGPU_EV_BOUNDED 1
+#define JFGPU_EV_HARDCORE 2
+#define JFGPU_EV_CELL_BOUNDING 3
+#define JFGPU_EV_CELL_VETO 4
+#define JFGPU_EV_BOUNDARY 5
+#define JFGPU_EV_END_OF_CHAIN 6
+
+/* ======================================================================================================
+ * Potentials: batched displacement / derivative.  velocity and separation are device arrays [n][3];
+ * charges are device arrays [n][2] (charge of the active unit, charge of the target unit);
+ * potential_change is a device array [n]; out [n] receives the time displacement (inf = no event) or the
+ * time derivative; status [n] receives JFGPU_STATUS_* per element.
+ * ==================================================================================================== */
+int jfgpu_hard_sphere_displacement(double radius, const double *velocity, const double *separation, int64_t n,
+                                   double *out, int32_t *status, void *stream);
+int jfgpu_inverse_power_displacement(double power, double prefactor, const double *velocity,
+                                     const double *separation, const double *charges,
+                                     const double *potential_change, int64_t n, double *out, int32_t *status,
+                                     void *stream);
+int jfgpu_inverse_power_derivative(double power, double prefactor, const double *velocity, const double *separation,
+                                   const double *charges, int64_t n, double *out, int32_t *status, void *stream);
+int jfgpu_lennard_jones_displacement(double prefactor, double characteristic_length, const double *velocity,
+                                     const double *separation, const double *potential_change, int64_t n,
+                                     double *out, int32_t *status, void *stream);
+int jfgpu_lennard_jones_derivative(double prefactor, double characteristic_length, const double *velocity,
+                                   const double *separation, int64_t n, double *out, int32_t *status,
+                                   void *stream);
+int jfgpu_displaced_even_power_displacement(double equilibrium_separation, int32_t power, double prefactor,
+                                            const double *velocity, const double *separation,
+                                            const double *potential_change, int64_t n, double *out,
+                                            int32_t *status, void *stream);
+int jfgpu_displaced_even_power_derivative(double equilibrium_separation, int32_t power, double prefactor,
+                                          const double *velocity, const double *separation, int64_t n,
+                                          double *out, int32_t *status, void *stream);
+int jfgpu_coulomb_bound_displacement(double prefactor, double system_length, const double *velocity,
+                                     const double *separation, const double *charges,
+                                     const double *potential_change, int64_t n, double *out, int32_t *status,
+                                     void *stream);
+int jfgpu_coulomb_bound_derivative(double prefactor, const double *velocity, const double *separation,
+                                   const double *charges, int64_t n, double *out, int32_t *status, void *stream);
+int jfgpu_merged_image_coulomb_derivative(double alpha, int32_t fourier_cutoff, int32_t position_cutoff,
+                                          double prefactor, double system_length, const double *velocity,
+                                          const double *separation, const double *charges, int64_t n,
+                                          double *out, int32_t *status, void *stream);
+/* CellBoundingPotential.displacement: potential_change / rate, rate = bounds[cell_separation][direction]
+ * (times the charge correction factor; the lower bound when that factor is not positive). bounds_upper and
+ * bounds_lower are device arrays [cells][3]; cell_separation, direction device arrays [n]; charge_factor [n]. */
+int jfgpu_cell_bounding_displacement(const double *bounds_upper, const double *bounds_lower,
+                                     const int32_t *cell_separation, const int32_t *direction, const double *speed,
+                                     const double *charge_factor, const double *potential_change, int64_t n,
+                                     double *out, int32_t *status, void *stream);
+
+/* ======================================================================================================
+ * Chains: thousands of independent ECMC chains advanced by one kernel with the event loop on the device.
+ * ==================================================================================================== */
+typedef struct {
+    int32_t potential;            /* JFGPU_POT_* */
+    int32_t far;                  /* JFGPU_FAR_* */
+    int32_t n;                    /* particles of the chain */
+    int32_t cells_per_side;
+    int32_t neighbor_layers;
+    int32_t max_occupants;        /* maximum occupants per cell (1 for the far fields) */
+    int32_t initial_active;
+    int32_t initial_direction;
+    int32_t fourier_cutoff;       /* merged-image Coulomb */
+    int32_t position_cutoff;
+    int32_t estimator_points;     /* InnerPointEstimator.points_per_side */
+    int32_t reserved;
+    double system_length;
+    double beta;
+    double chain_time;
+    double speed;
+    double hs_radius;             /* hard sphere radius / hard-core radius of a Coulomb system (0 = none) */
+    double lj_prefactor;
+    double lj_sigma;
+    double coulomb_prefactor;
+    double bound_prefactor;       /* inverse-power Coulomb bounding prefactor */
+    double ewald_alpha;
+    double estimator_prefactor;
+    uint64_t rng_key;             /* key of the chain's keyed random numbers */
+} JfgpuChainDesc;
+
+/* per-chain lifting state (device array of n_chains) */
+typedef struct {
+    double time_q, time_r;        /* time stamp of the active unit (quotient and remainder of t / 1) */
+    double eoc_q, eoc_r;          /* candidate time of the end-of-chain event */
+    int64_t events;               /* committed events */
+    int64_t bound_warnings;       /* thinning events with a real rate above the bounding rate */
+    int64_t refine_fallbacks;     /* mixed mode: events re-solved entirely in FP64 */
+    int64_t candidates;           /* pair candidates solved (nearby occupants and surplus units) */
+    int64_t refined;              /* mixed mode: candidates re-solved in FP64 */
+    int32_t active;
+    int32_t direction;
+    int32_t eoc_new_active;
+    int32_t occ_active;           /* identifier the occupancy treats as active (-1 = none) */
+    int32_t occ_cell;             /* active cell of the occupancy */
+    int32_t n_surplus;
+    int32_t status;               /* JFGPU_STATUS_* of the first failure; the chain stops */
+    int32_t reserved;
+} JfgpuChainState;
+
+/* one committed event (device log array [n_chains][log_capacity]) */
+typedef struct {
+    int32_t kind, moved, target, new_active, new_direction, accepted;
+    double time_q, time_r;
+    double x, y, z;
+} JfgpuEvent;
+
+/* device buffers of a chain batch, all owned by the caller; sizes from jfgpu_engine_layout */
+typedef struct {
+    double *positions;            /* [particles][3], chain c at particle_offset[c] */
+    float *positions32;           /* [particles][4]: FP32 mirror (x, y, z, charge) of the mixed mode */
+    double *charges;              /* [particles] (may be NULL for uncharged systems) */
+    int32_t *occupancy;           /* [occupancy_slots] */
+    int32_t *surplus;             /* [particles] */
+    JfgpuChainState *state;       /* [n_chains] */
+} JfgpuBuffers;
+
+typedef struct {
+    int64_t n_chains;
+    int64_t particles;            /* sum of n over chains */
+    int64_t occupancy_slots;      /* sum of cells * max_occupants over chains */
+    int64_t table_bytes;          /* device bytes of the engine's own tables */
+} JfgpuLayout;
+
+typedef struct JfgpuEngine JfgpuEngine;
+
+/* Build an engine for n_chains chains: geometry tables, far-field bound tables (estimator scan on the GPU)
+ * and Walker tables.  Chains with equal far-field parameters share tables.  Returns JFGPU_OK and *engine. */
+int jfgpu_engine_create(const JfgpuChainDesc *chains, int64_t n_chains, void *stream, JfgpuEngine **engine);
+void jfgpu_engine_destroy(JfgpuEngine *engine);
+int jfgpu_engine_layout(const JfgpuEngine *engine, JfgpuLayout *layout);
+/* host arrays [n_chains]: first particle and first occupancy slot of every chain */
+int jfgpu_engine_offsets(const JfgpuEngine *engine, int64_t *particle_offset, int64_t *occupancy_offset);
+/* host copy of the far-field tables of a chain: upper [cells][3], lower [cells][3] (negated lower bound) */
+int jfgpu_engine_bounds(const JfgpuEngine *engine, int64_t chain, double *upper, double *lower, int64_t capacity);
+
+/* Start the chains from buffers->positions (and charges): FP32 mirror, cell occupancy, surplus lists, lifting
+ * state at time 0 with the first end-of-chain candidate (InitialChainStartOfRunEventHandler). */
+int jfgpu_chains_init(JfgpuEngine *engine, const JfgpuBuffers *buffers, void *stream);
+
+/* Advance chains [first_chain, first_chain + count) by at most max_events committed events each, or until the
+ * next event time reaches the stop time (stop_q = +inf: none), where the active unit is time-sliced to the
+ * stop time.  mode = JFGPU_MODE_*.  log (device, may be NULL) receives [count][log_capacity] events. */
+int jfgpu_chains_run(JfgpuEngine *engine, const JfgpuBuffers *buffers, int64_t first_chain, int64_t count,
+                     int64_t max_events, double stop_q, double stop_r, int32_t mode, JfgpuEvent *log,
+                     int64_t log_capacity, void *stream);
+
+/* Autotuned launch shape of the mixed mode: warps per block used by jfgpu_chains_run (1..16). */
+int jfgpu_chains_set_block_warps(JfgpuEngine *engine, int32_t warps_per_block);
+
+/* Kernel launches issued by the library since the engine was created (all kernels of this library). */
+int64_t jfgpu_engine_launch_count(const JfgpuEngine *engine);
+
+const char *jfgpu_error_string(int code);
+int jfgpu_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

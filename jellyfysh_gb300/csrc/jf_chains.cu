@@ -1,0 +1,843 @@
+// jf_chains.cu -- the event loop of thousands of independent ECMC chains, one warp per chain.
+//
+// One loop iteration is one iteration of SingleProcessMediator.run (jellyfysh/mediator/single_process_mediator.py:
+// 91-156) restricted to the event handlers of the path:
+//   1. occupancy update of the active unit (single_active_cell_occupancy.py:149-203), lane 0;
+//   2. candidate event times: nearby occupants and surplus units (excluded_cells_tagger.py:107-132,
+//      surplus_cells_tagger.py:107-131 with two_leaf_unit_event_handler.py:98-138 or
+//      two_leaf_unit_bounding_potential_event_handler.py:112-143), the far field (cell_bounding_potential_tagger.py:
+//      127-155 with two_leaf_unit_cell_bounding_potential_event_handler.py:137-176, or
+//      cell_veto_event_handler.py:162-238), the cell boundary (cell_boundary_event_handler.py:98-156) and the
+//      persistent end-of-chain candidate;
+//   3. the earliest candidate by a warp-shuffle argmin over (time quotient, time remainder, kind, target) in
+//      place of the heap (heap_scheduler.py:111-212, heap.c:156-304);
+//   4. the out-state: time slice of the active unit with periodic wrap (abstracts.py:82-95), lifting
+//      (abstracts.py:283-321), thinning (event_handler_with_bounding_potential.py:75-101), boundary snap
+//      (cell_boundary_event_handler.py:158-173) or end of chain (end_of_chain_event_handler.py:108-187).
+//
+// JFGPU_MODE_EXACT solves every candidate in FP64 with the reference's arithmetic.  JFGPU_MODE_MIXED screens
+// every candidate in FP32 (jf_screen.cuh), keeps the four smallest FP32 times of every lane, and re-solves in FP64
+// the candidates within (1 + 2^-10) t_min + margin and every flagged one; the winner and its event time are
+// therefore the FP64 ones.  When a lane holds more than four candidates inside the margin the event is re-solved
+// entirely in FP64 (counted in refine_fallbacks).
+#include <cuda_runtime.h>
+
+#include "jf_engine.cuh"
+#include "jf_screen.cuh"
+
+namespace jf {
+
+constexpr unsigned kFull = 0xffffffffu;
+constexpr int kTopK = 4;
+
+struct Cand {
+    double q, r;
+    int kind, target, aux;
+    double rate;
+};
+
+__device__ inline Cand cand_none() {
+    Cand c;
+    c.q = kInf;
+    c.r = kInf;
+    c.kind = 1 << 30;
+    c.target = 1 << 30;
+    c.aux = -1;
+    c.rate = 0.0;
+    return c;
+}
+
+// earliest time first; equal times: lower kind, then lower target
+__device__ inline bool cand_better(const Cand &a, const Cand &b) {
+    if (time_lt(a.q, a.r, b.q, b.r)) return true;
+    if (time_lt(b.q, b.r, a.q, a.r)) return false;
+    if (a.kind != b.kind) return a.kind < b.kind;
+    return a.target < b.target;
+}
+
+__device__ inline void offer(Cand &best, double ts_q, double ts_r, double dt, int kind, int target, int aux, double rate) {
+    if (isinf(dt) && dt > 0) return;  // HeapScheduler.push_event ignores infinite times
+    Cand c;
+    time_add(ts_q, ts_r, dt, c.q, c.r);
+    c.kind = kind;
+    c.target = target;
+    c.aux = aux;
+    c.rate = rate;
+    if (cand_better(c, best)) best = c;
+}
+
+__device__ inline Cand warp_argmin(Cand c) {
+#pragma unroll
+    for (int offset = 16; offset > 0; offset >>= 1) {
+        Cand o;
+        o.q = __shfl_xor_sync(kFull, c.q, offset);
+        o.r = __shfl_xor_sync(kFull, c.r, offset);
+        o.kind = __shfl_xor_sync(kFull, c.kind, offset);
+        o.target = __shfl_xor_sync(kFull, c.target, offset);
+        o.aux = __shfl_xor_sync(kFull, c.aux, offset);
+        o.rate = __shfl_xor_sync(kFull, c.rate, offset);
+        if (cand_better(o, c)) c = o;
+    }
+    return c;
+}
+
+__device__ inline int warp_max_int(int v) {
+#pragma unroll
+    for (int offset = 16; offset > 0; offset >>= 1) v = max(v, __shfl_xor_sync(kFull, v, offset));
+    return v;
+}
+
+__device__ inline int warp_sum_int(int v) {
+#pragma unroll
+    for (int offset = 16; offset > 0; offset >>= 1) v += __shfl_xor_sync(kFull, v, offset);
+    return v;
+}
+
+__device__ inline float warp_min_float(float v) {
+#pragma unroll
+    for (int offset = 16; offset > 0; offset >>= 1) v = fminf(v, __shfl_xor_sync(kFull, v, offset));
+    return v;
+}
+
+// lifting state of one chain while it runs; lane 0 writes, all lanes read after __syncwarp
+struct WarpState {
+    double pa[3];
+    double ts_q, ts_r, eoc_q, eoc_r;
+    long long events, warnings, fallbacks, candidates, refined;
+    int active, direction, eoc_new, occ_active, occ_cell, n_surplus, status, stop;
+};
+
+struct RunArgs {
+    EngineView view;
+    double *positions;
+    float4 *positions32;
+    const double *charges;
+    int32_t *occupancy;
+    int32_t *surplus;
+    JfgpuChainState *state;
+    JfgpuEvent *log;
+    long long log_capacity;
+    long long first_chain, count, max_events;
+    double stop_q, stop_r;
+    int has_stop;
+};
+
+__device__ inline int cell_of(const ChainDev &ch, const double *p, int &cell) {
+    long long ix = (long long)(p[0] / ch.side), iy = (long long)(p[1] / ch.side), iz = (long long)(p[2] / ch.side);
+    long long idx = ix + (long long)ch.m * iy + (long long)ch.m * ch.m * iz;
+    if (idx < 0 || idx >= ch.ncells) return JFGPU_STATUS_CELL_RANGE;
+    cell = (int)idx;
+    return JFGPU_STATUS_OK;
+}
+
+__device__ inline void cell_axes(const ChainDev &ch, int cell, int *a) {
+    a[0] = cell % ch.m;
+    a[1] = (cell / ch.m) % ch.m;
+    a[2] = cell / (ch.m * ch.m);
+}
+
+__device__ inline bool is_nearby(const ChainDev &ch, int cell, int reference) {
+    int a[3], b[3];
+    cell_axes(ch, cell, a);
+    cell_axes(ch, reference, b);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        int diff = a[k] - b[k];
+        if (diff < 0) diff += ch.m;
+        if (!((ch.near_mask >> diff) & 1ull)) return false;
+    }
+    return true;
+}
+
+__device__ inline int relative_cell(const EngineView &v, const ChainDev &ch, int cell, int reference) {
+    int a[3], b[3];
+    cell_axes(ch, cell, a);
+    cell_axes(ch, reference, b);
+    const int16_t *rel = v.rel + ch.table_offset;
+    return rel[a[0] * ch.m + b[0]] + ch.m * rel[a[1] * ch.m + b[1]] + ch.m * ch.m * rel[a[2] * ch.m + b[2]];
+}
+
+__device__ inline int translate_cell(const EngineView &v, const ChainDev &ch, int cell, int relative) {
+    int a[3], b[3];
+    cell_axes(ch, cell, a);
+    cell_axes(ch, relative, b);
+    const int16_t *tra = v.tra + ch.table_offset;
+    return tra[a[0] * ch.m + b[0]] + ch.m * tra[a[1] * ch.m + b[1]] + ch.m * ch.m * tra[a[2] * ch.m + b[2]];
+}
+
+__device__ inline void separation64(const ChainDev &ch, const double *from, const double *to, double *s) {
+#pragma unroll
+    for (int k = 0; k < 3; ++k) s[k] = py_mod((to[k] - from[k]) + ch.half, ch.L) - ch.half;
+}
+
+__device__ inline void load_pos(const RunArgs &A, const ChainDev &ch, int j, double *p) {
+    const double *q = A.positions + 3 * (ch.pos_off + j);
+    p[0] = q[0];
+    p[1] = q[1];
+    p[2] = q[2];
+}
+
+__device__ inline double charge_of(const RunArgs &A, const ChainDev &ch, int j) {
+    return A.charges ? A.charges[ch.pos_off + j] : 1.0;
+}
+
+// FP64 candidates of one (active, target) pair of the nearby / surplus taggers
+__device__ inline int exact_pair(const RunArgs &A, const ChainDev &ch, const SpeciesDev &sp, const WarpState &w,
+                                 int j, long long ev, Cand &best) {
+    double pj[3], s[3];
+    load_pos(A, ch, j, pj);
+    separation64(ch, w.pa, pj, s);
+    const int d = w.direction;
+    double dt;
+    if (ch.potential == JFGPU_POT_HARD_SPHERE) {
+        JF_TRY(hs_displacement_axis(ch.diameter_sq, d, ch.speed, s, dt));
+        offer(best, w.ts_q, w.ts_r, dt, JFGPU_EV_PAIR, j, -1, 0.0);
+    } else if (ch.potential == JFGPU_POT_LENNARD_JONES) {
+        double du = expovariate(draw(ch.key, (uint64_t)ev, kRngPair, (uint32_t)j), ch.beta);
+        double disp;
+        JF_TRY(mh_std_displacement(sp.lj, d, s, du, disp));
+        offer(best, w.ts_q, w.ts_r, disp / ch.speed, JFGPU_EV_PAIR, j, -1, 0.0);
+    } else {
+        if (ch.diameter_sq > 0.0) {
+            double sh[3] = {s[0], s[1], s[2]};
+            JF_TRY(hs_displacement_axis(ch.diameter_sq, d, ch.speed, sh, dt));
+            offer(best, w.ts_q, w.ts_r, dt, JFGPU_EV_HARDCORE, j, -1, 0.0);
+        }
+        double du = expovariate(draw(ch.key, (uint64_t)ev, kRngPair, (uint32_t)j), ch.beta);
+        double p[3];
+        permute3(s, d, p);
+        double pp = ch.bound_prefactor * charge_of(A, ch, w.active) * charge_of(A, ch, j);
+        double disp = ipcb_x_displacement(pp, p[0], p[1], p[2], du, ch.L);
+        offer(best, w.ts_q, w.ts_r, disp / ch.speed, JFGPU_EV_BOUNDED, j, -1, 0.0);
+    }
+    return JFGPU_STATUS_OK;
+}
+
+// FP64 candidate of a far occupant under the cell-bounding potential
+__device__ inline int exact_cell_bounding(const RunArgs &A, const ChainDev &ch, const SpeciesDev &sp,
+                                          const WarpState &w, int j, int active_cell, long long ev, bool from_position,
+                                          int stored_cell, Cand &best) {
+    int target_cell = stored_cell;
+    if (from_position) {
+        double pj[3];
+        load_pos(A, ch, j, pj);
+        JF_TRY(cell_of(ch, pj, target_cell));
+    }
+    int rc = relative_cell(A.view, ch, target_cell, active_cell);
+    double du = expovariate(draw(ch.key, (uint64_t)ev, kRngPair, (uint32_t)j), ch.beta);
+    double rate = sp.bound_upper[rc * 3 + w.direction];
+    double disp = rate > 0 ? du / rate : kInf;
+    offer(best, w.ts_q, w.ts_r, disp / ch.speed, JFGPU_EV_CELL_BOUNDING, j, rc, rate);
+    return JFGPU_STATUS_OK;
+}
+
+// cell veto, cell boundary and end of chain: the single candidates of lane 0
+__device__ inline int single_candidates(const RunArgs &A, const ChainDev &ch, const SpeciesDev &sp, const WarpState &w,
+                                        int active_cell, long long ev, Cand &best) {
+    const int d = w.direction;
+    if (ch.far == JFGPU_FAR_CELL_VETO) {
+        double charge_factor = ch.potential == JFGPU_POT_LENNARD_JONES ? 1.0 : (charge_of(A, ch, w.active) * 1.0) / 1.0;
+        int which = 0;
+        if (!(charge_factor > 0.0)) {
+            charge_factor *= -1.0;
+            which = 1;
+        }
+        const WalkerDev &wk = sp.walker[which][d];
+        double total_rate = wk.total_rate * charge_factor;
+        int k = (int)randbelow(draw(ch.key, (uint64_t)ev, kRngVetoChoice, 0), (uint32_t)wk.size);
+        double u = wk.mean_rate * uniform53(draw(ch.key, (uint64_t)ev, kRngVetoUniform, 0));
+        int rc = (u <= wk.first_rate[k]) ? wk.first_item[k] : wk.second_item[k];
+        double rate = (which == 0 ? sp.bound_upper[rc * 3 + d] : sp.bound_lower[rc * 3 + d]) * charge_factor;
+        if (!(rate > 0.0)) return JFGPU_STATUS_ASSERTION;
+        int target_cell = translate_cell(A.view, ch, active_cell, rc);
+        double dt = expovariate(draw(ch.key, (uint64_t)ev, kRngVetoTime, 0), ch.beta) / (total_rate * ch.speed);
+        offer(best, w.ts_q, w.ts_r, dt, JFGPU_EV_CELL_VETO, -1, target_cell, rate);
+    }
+    int ax[3];
+    cell_axes(ch, active_cell, ax);
+    double boundary = A.view.cell_min[ch.geom_offset + (ax[d] + 1) % ch.m];
+    double sep = boundary - w.pa[d];
+    if (sep < 0.0) sep = sep + ch.L;
+    offer(best, w.ts_q, w.ts_r, sep / ch.speed, JFGPU_EV_BOUNDARY, -1, -1, boundary);
+    Cand e;
+    e.q = w.eoc_q;
+    e.r = w.eoc_r;
+    e.kind = JFGPU_EV_END_OF_CHAIN;
+    e.target = w.eoc_new;
+    e.aux = -1;
+    e.rate = 0.0;
+    if (cand_better(e, best)) best = e;
+    return JFGPU_STATUS_OK;
+}
+
+// ---------------------------------------------------------------------------------------------------------------
+// occupancy (lane 0)
+// ---------------------------------------------------------------------------------------------------------------
+__device__ inline void occ_insert(const RunArgs &A, const ChainDev &ch, WarpState &w, int cell, int id) {
+    int32_t *slots = A.occupancy + ch.occ_off + (long long)cell * ch.max_occ;
+    for (int k = 0; k < ch.max_occ; ++k)
+        if (slots[k] < 0) {
+            slots[k] = id;
+            return;
+        }
+    A.surplus[ch.pos_off + w.n_surplus] = id;
+    w.n_surplus += 1;
+}
+
+__device__ inline int occ_update(const RunArgs &A, const ChainDev &ch, WarpState &w) {
+    if (w.active != w.occ_active) {
+        if (w.occ_active >= 0) occ_insert(A, ch, w, w.occ_cell, w.occ_active);
+        JF_TRY(cell_of(ch, w.pa, w.occ_cell));
+        w.occ_active = w.active;
+        int32_t *slots = A.occupancy + ch.occ_off + (long long)w.occ_cell * ch.max_occ;
+        for (int k = 0; k < ch.max_occ; ++k)
+            if (slots[k] == w.active) {
+                slots[k] = -1;
+                return JFGPU_STATUS_OK;
+            }
+        int32_t *sur = A.surplus + ch.pos_off;
+        for (int k = 0; k < w.n_surplus; ++k)
+            if (sur[k] == w.active) {
+                sur[k] = sur[w.n_surplus - 1];
+                w.n_surplus -= 1;
+                return JFGPU_STATUS_OK;
+            }
+        return JFGPU_STATUS_ASSERTION;
+    }
+    return cell_of(ch, w.pa, w.occ_cell);
+}
+
+// ---------------------------------------------------------------------------------------------------------------
+// out-state (lane 0)
+// ---------------------------------------------------------------------------------------------------------------
+__device__ inline int real_rate(const RunArgs &A, const ChainDev &ch, const SpeciesDev &sp, const WarpState &w, int t,
+                                double &out) {
+    double pt[3], s[3];
+    load_pos(A, ch, t, pt);
+    separation64(ch, w.pa, pt, s);
+    if (ch.potential == JFGPU_POT_LENNARD_JONES) {
+        double value;
+        JF_TRY(mh_std_derivative(sp.lj, w.direction, s, value));
+        out = value * ch.speed;
+        return JFGPU_STATUS_OK;
+    }
+    out = mic_std_derivative(sp.mic, ch.coulomb_prefactor, w.direction, s, charge_of(A, ch, w.active),
+                             charge_of(A, ch, t)) * ch.speed;
+    return JFGPU_STATUS_OK;
+}
+
+__device__ inline int thinning(const RunArgs &A, const ChainDev &ch, const SpeciesDev &sp, WarpState &w, int t,
+                               double bounding_rate, long long ev, int &accepted) {
+    double real;
+    JF_TRY(real_rate(A, ch, sp, w, t, real));
+    accepted = 0;
+    if (real > 0) {
+        if (bounding_rate < real) w.warnings += 1;
+        double u = bounding_rate * uniform53(draw(ch.key, (uint64_t)ev, kRngThin, 0));
+        if (u < real) accepted = 1;
+    }
+    return JFGPU_STATUS_OK;
+}
+
+__device__ inline void store_active(const RunArgs &A, const ChainDev &ch, const WarpState &w, int id) {
+    double *q = A.positions + 3 * (ch.pos_off + id);
+    q[0] = w.pa[0];
+    q[1] = w.pa[1];
+    q[2] = w.pa[2];
+    float4 m = A.positions32[ch.pos_off + id];
+    m.x = (float)w.pa[0];
+    m.y = (float)w.pa[1];
+    m.z = (float)w.pa[2];
+    A.positions32[ch.pos_off + id] = m;
+}
+
+__device__ inline void time_slice(const ChainDev &ch, WarpState &w, double q, double r) {
+    double dt = time_sub(q, r, w.ts_q, w.ts_r);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        double v = k == w.direction ? ch.speed : 0.0;
+        w.pa[k] = py_mod(w.pa[k] + v * dt, ch.L);
+    }
+    w.ts_q = q;
+    w.ts_r = r;
+}
+
+// commit the winner; returns a status
+__device__ inline int commit(const RunArgs &A, const ChainDev &ch, const SpeciesDev &sp, WarpState &w, const Cand &best,
+                             int active_cell, long long chain_index, long long log_index) {
+    const long long ev = w.events;
+    int moved = w.active;
+    JfgpuEvent rec;
+    rec.kind = best.kind;
+    rec.moved = moved;
+    rec.target = -1;
+    rec.accepted = 0;
+    rec.time_q = best.q;
+    rec.time_r = best.r;
+    time_slice(ch, w, best.q, best.r);
+    switch (best.kind) {
+    case JFGPU_EV_PAIR:
+    case JFGPU_EV_HARDCORE:
+        rec.target = best.target;
+        rec.accepted = 1;
+        w.active = best.target;
+        break;
+    case JFGPU_EV_BOUNDED: {
+        double pt[3], s[3], p[3];
+        load_pos(A, ch, best.target, pt);
+        separation64(ch, w.pa, pt, s);
+        permute3(s, w.direction, p);
+        double pp = ch.bound_prefactor * charge_of(A, ch, w.active) * charge_of(A, ch, best.target);
+        double bound = ipcb_x_derivative(pp, p[0], p[1], p[2]) * ch.speed;
+        int accepted;
+        JF_TRY(thinning(A, ch, sp, w, best.target, bound, ev, accepted));
+        rec.target = best.target;
+        rec.accepted = accepted;
+        if (accepted) w.active = best.target;
+        break;
+    }
+    case JFGPU_EV_CELL_BOUNDING: {
+        int now_cell;
+        JF_TRY(cell_of(ch, w.pa, now_cell));
+        if (now_cell != active_cell) return JFGPU_STATUS_ASSERTION;
+        int accepted;
+        JF_TRY(thinning(A, ch, sp, w, best.target, best.rate * ch.speed, ev, accepted));
+        rec.target = best.target;
+        rec.accepted = accepted;
+        if (accepted) w.active = best.target;
+        break;
+    }
+    case JFGPU_EV_CELL_VETO: {
+        int t = A.occupancy[ch.occ_off + (long long)best.aux * ch.max_occ];
+        if (t >= 0) {
+            int accepted;
+            JF_TRY(thinning(A, ch, sp, w, t, best.rate, ev, accepted));
+            rec.target = t;
+            rec.accepted = accepted;
+            if (accepted) w.active = t;
+        }
+        break;
+    }
+    case JFGPU_EV_BOUNDARY:
+        w.pa[w.direction] = best.rate;
+        break;
+    case JFGPU_EV_END_OF_CHAIN: {
+        w.direction = (w.direction + 1) % 3;
+        w.active = best.target;
+        rec.target = best.target;
+        rec.accepted = 1;
+        time_add(w.ts_q, w.ts_r, time_sub(w.ts_q, w.ts_r, w.ts_q, w.ts_r) + ch.chain_time, w.eoc_q, w.eoc_r);
+        w.eoc_new = (int)randbelow(draw(ch.key, (uint64_t)(ev + 1), kRngNewActive, 0), (uint32_t)ch.n);
+        break;
+    }
+    default:
+        return JFGPU_STATUS_ASSERTION;
+    }
+    rec.new_active = w.active;
+    rec.new_direction = w.direction;
+    rec.x = w.pa[0];
+    rec.y = w.pa[1];
+    rec.z = w.pa[2];
+    store_active(A, ch, w, moved);
+    if (w.active != moved) {
+        double pn[3];
+        load_pos(A, ch, w.active, pn);
+        w.pa[0] = pn[0];
+        w.pa[1] = pn[1];
+        w.pa[2] = pn[2];
+    }
+    if (A.log && log_index < A.log_capacity) A.log[(chain_index - A.first_chain) * A.log_capacity + log_index] = rec;
+    w.events = ev + 1;
+    return JFGPU_STATUS_OK;
+}
+
+// ---------------------------------------------------------------------------------------------------------------
+// candidate enumeration
+// ---------------------------------------------------------------------------------------------------------------
+template <typename F>
+__device__ inline void for_each_near(const RunArgs &A, const ChainDev &ch, int occ_cell, int lane, F &&f) {
+    int a[3];
+    cell_axes(ch, occ_cell, a);
+    const int K = ch.n_res;
+    const int total = K * K * K;
+    const int32_t *occ = A.occupancy + ch.occ_off;
+    for (int i = lane; i < total; i += 32) {
+        int ox = i % K, oy = (i / K) % K, oz = i / (K * K);
+        int cx = a[0] + ch.res[ox], cy = a[1] + ch.res[oy], cz = a[2] + ch.res[oz];
+        if (cx >= ch.m) cx -= ch.m;
+        if (cy >= ch.m) cy -= ch.m;
+        if (cz >= ch.m) cz -= ch.m;
+        int cell = cx + ch.m * (cy + ch.m * cz);
+        for (int k = 0; k < ch.max_occ; ++k) {
+            int j = occ[(long long)cell * ch.max_occ + k];
+            if (j >= 0) f(j);
+        }
+    }
+}
+
+// the whole event in FP64 (all lanes); returns the winner in best
+__device__ inline int exact_candidates(const RunArgs &A, const ChainDev &ch, const SpeciesDev &sp, const WarpState &w,
+                                       int active_cell, int lane, Cand &best, int &counted) {
+    const long long ev = w.events;
+    int status = JFGPU_STATUS_OK;
+    int count = 0;
+    best = cand_none();
+    for_each_near(A, ch, w.occ_cell, lane, [&](int j) {
+        int st = exact_pair(A, ch, sp, w, j, ev, best);
+        if (st) status = st;
+        ++count;
+    });
+    for (int i = lane; i < w.n_surplus; i += 32) {
+        int st = exact_pair(A, ch, sp, w, A.surplus[ch.pos_off + i], ev, best);
+        if (st) status = st;
+        ++count;
+    }
+    counted = warp_sum_int(count);
+    if (ch.far == JFGPU_FAR_CELL_BOUNDING) {
+        const int32_t *occ = A.occupancy + ch.occ_off;
+        for (int c = lane; c < ch.ncells; c += 32) {
+            int j = occ[c];
+            if (j < 0 || is_nearby(ch, c, w.occ_cell)) continue;
+            int st = exact_cell_bounding(A, ch, sp, w, j, active_cell, ev, true, c, best);
+            if (st) status = st;
+        }
+    }
+    if (lane == 0) {
+        int st = single_candidates(A, ch, sp, w, active_cell, ev, best);
+        if (st) status = st;
+    }
+    best = warp_argmin(best);
+    return warp_max_int(status);
+}
+
+// top-K insertion of (key, code) pairs kept sorted ascending
+__device__ inline void topk_insert(float (&key)[kTopK], int (&code)[kTopK], float k, int c) {
+    if (!(k < key[kTopK - 1])) return;
+    key[kTopK - 1] = k;
+    code[kTopK - 1] = c;
+#pragma unroll
+    for (int i = kTopK - 1; i > 0; --i) {
+        if (key[i] < key[i - 1]) {
+            float tk = key[i];
+            key[i] = key[i - 1];
+            key[i - 1] = tk;
+            int tc = code[i];
+            code[i] = code[i - 1];
+            code[i - 1] = tc;
+        }
+    }
+}
+
+// mixed precision: FP32 screening, FP64 refinement; returns 1 when the event must be re-solved in FP64
+__device__ inline int mixed_candidates(const RunArgs &A, const ChainDev &ch, const SpeciesDev &sp, const LJ32 &lj32,
+                                       const WarpState &w, int active_cell, int lane, Cand &best, int &status,
+                                       int &counted, int &refined) {
+    const long long ev = w.events;
+    const int d = w.direction;
+    const float speed32 = (float)ch.speed;
+    const float beta32 = (float)ch.beta;
+    const float margin = ch.ulp_margin32;
+    float key[kTopK];
+    int code[kTopK];
+#pragma unroll
+    for (int i = 0; i < kTopK; ++i) {
+        key[i] = kInf32;
+        code[i] = -1;
+    }
+    const float4 pa32 = make_float4((float)w.pa[0], (float)w.pa[1], (float)w.pa[2], 0.0f);
+    // codes: bit 30 marks a far (cell-bounding) candidate, the low bits carry the target
+    int count = 0;
+    auto screen_pair = [&](int j) {
+        ++count;
+        float4 pj = A.positions32[ch.pos_off + j];
+        float s[3];
+        bool flag = false;
+        separation32(pa32, pj, ch.L32, ch.half32, margin, s, flag);
+        float t;
+        if (ch.potential == JFGPU_POT_HARD_SPHERE) {
+            t = hs_screen((float)ch.diameter_sq, d, speed32, s, margin, flag);
+        } else {
+            float du = expovariate32(draw(ch.key, (uint64_t)ev, kRngPair, (uint32_t)j), beta32, flag);
+            t = lj_screen(lj32, d, speed32, s, du, margin, flag);
+        }
+        if (flag) t = -1.0f;
+        if (!isinf(t)) topk_insert(key, code, t, j);
+    };
+    for_each_near(A, ch, w.occ_cell, lane, screen_pair);
+    for (int i = lane; i < w.n_surplus; i += 32) screen_pair(A.surplus[ch.pos_off + i]);
+    if (ch.far == JFGPU_FAR_CELL_BOUNDING) {
+        const int32_t *occ = A.occupancy + ch.occ_off;
+        for (int c = lane; c < ch.ncells; c += 32) {
+            int j = occ[c];
+            if (j < 0 || is_nearby(ch, c, w.occ_cell)) continue;
+            int rc = relative_cell(A.view, ch, c, active_cell);
+            float rate = sp.bound_upper32[rc * 3 + d];
+            bool flag = false;
+            float du = expovariate32(draw(ch.key, (uint64_t)ev, kRngPair, (uint32_t)j), beta32, flag);
+            float t = rate > 0.0f ? (du / rate) / speed32 : kInf32;
+            if (flag) t = -1.0f;
+            if (!isinf(t)) topk_insert(key, code, t, j | (1 << 30));
+        }
+    }
+    // exact single candidates (lane 0) bound the threshold too
+    Cand single = cand_none();
+    int st = JFGPU_STATUS_OK;
+    if (lane == 0) st = single_candidates(A, ch, sp, w, active_cell, ev, single);
+    status = warp_max_int(st);
+    // smallest unflagged FP32 time (flagged entries carry the key -1 and are always refined)
+    float lane_min = kInf32;
+#pragma unroll
+    for (int i = 0; i < kTopK; ++i)
+        if (key[i] >= 0.0f) lane_min = fminf(lane_min, key[i]);
+    float t_min = warp_min_float(lane_min);
+    double single_dt = kInf;
+    if (lane == 0 && !isinf(single.q)) single_dt = time_sub(single.q, single.r, w.ts_q, w.ts_r);
+    single_dt = __shfl_sync(kFull, single_dt, 0);
+    float t_single = (float)single_dt;
+    float base = fminf(t_min, t_single);
+    float threshold = isinf(base) ? kInf32 : base * (1.0f + 1.0f / 1024.0f) + ch.screen_abs32 / speed32;
+    // refinement of the candidates inside the threshold
+    int overflow = (key[kTopK - 1] <= threshold) ? 1 : 0;
+    best = single;
+    int rst = JFGPU_STATUS_OK;
+    int nref = 0;
+#pragma unroll
+    for (int i = 0; i < kTopK; ++i) {
+        if (code[i] >= 0 && key[i] <= threshold) {
+            ++nref;
+            int j = code[i] & ((1 << 30) - 1);
+            int s2;
+            if (code[i] & (1 << 30)) {
+                int c = -1;
+                s2 = exact_cell_bounding(A, ch, sp, w, j, active_cell, ev, true, c, best);
+            } else {
+                s2 = exact_pair(A, ch, sp, w, j, ev, best);
+            }
+            if (s2) rst = s2;
+        }
+    }
+    status = max(status, warp_max_int(rst));
+    best = warp_argmin(best);
+    counted = warp_sum_int(count);
+    refined = warp_sum_int(nref);
+    return warp_max_int(overflow);
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(256) chains_kernel(RunArgs A) {
+    extern __shared__ unsigned char smem_raw[];
+    WarpState *shared = reinterpret_cast<WarpState *>(smem_raw);
+    const int warp = threadIdx.x >> 5;
+    const int lane = threadIdx.x & 31;
+    const long long local = (long long)blockIdx.x * (blockDim.x >> 5) + warp;
+    if (local >= A.count) return;
+    const long long c = A.first_chain + local;
+    const ChainDev &ch = A.view.chains[c];
+    const SpeciesDev &sp = A.view.species[ch.species];
+    WarpState &w = shared[warp];
+    if (lane == 0) {
+        const JfgpuChainState &g = A.state[c];
+        w.ts_q = g.time_q;
+        w.ts_r = g.time_r;
+        w.eoc_q = g.eoc_q;
+        w.eoc_r = g.eoc_r;
+        w.events = g.events;
+        w.warnings = g.bound_warnings;
+        w.fallbacks = g.refine_fallbacks;
+        w.candidates = g.candidates;
+        w.refined = g.refined;
+        w.active = g.active;
+        w.direction = g.direction;
+        w.eoc_new = g.eoc_new_active;
+        w.occ_active = g.occ_active;
+        w.occ_cell = g.occ_cell;
+        w.n_surplus = g.n_surplus;
+        w.status = g.status;
+        w.stop = 0;
+        load_pos(A, ch, w.active, w.pa);
+    }
+    __syncwarp();
+    LJ32 lj32;
+    lj32.a12 = (float)sp.lj.twelve.prefactor;
+    lj32.a6 = (float)sp.lj.six.prefactor;
+    lj32.four_over_k = (float)(4.0 / sp.lj.prefactor);
+    lj32.sigma_sq = (float)(sp.lj.sigma * sp.lj.sigma);
+    lj32.r0_sq = (float)sp.lj.r0_squared;
+    const long long start_events = w.events;
+    for (long long e = 0; e < A.max_events; ++e) {
+        if (w.status != JFGPU_STATUS_OK || w.stop) break;
+        if (lane == 0) {
+            int st = occ_update(A, ch, w);
+            if (st) w.status = st;
+        }
+        __syncwarp();
+        if (w.status != JFGPU_STATUS_OK) break;
+        int active_cell = 0;
+        {
+            int st = cell_of(ch, w.pa, active_cell);
+            if (st) {
+                if (lane == 0) w.status = st;
+                __syncwarp();
+                break;
+            }
+        }
+        Cand best;
+        int status = JFGPU_STATUS_OK;
+        int counted = 0, refined = 0;
+        if (MODE == JFGPU_MODE_MIXED) {
+            int fallback = mixed_candidates(A, ch, sp, lj32, w, active_cell, lane, best, status, counted, refined);
+            if (fallback && status == JFGPU_STATUS_OK) {
+                int recount = 0;
+                status = exact_candidates(A, ch, sp, w, active_cell, lane, best, recount);
+                if (lane == 0) w.fallbacks += 1;
+            }
+        } else {
+            status = exact_candidates(A, ch, sp, w, active_cell, lane, best, counted);
+        }
+        __syncwarp();
+        if (lane == 0) {
+            w.candidates += counted;
+            w.refined += refined;
+        }
+        if (lane == 0) {
+            if (status) {
+                w.status = status;
+            } else if (A.has_stop && !time_lt(best.q, best.r, A.stop_q, A.stop_r)) {
+                time_slice(ch, w, A.stop_q, A.stop_r);
+                store_active(A, ch, w, w.active);
+                w.stop = 1;
+            } else {
+                int st = commit(A, ch, sp, w, best, active_cell, c, w.events - start_events);
+                if (st) w.status = st;
+            }
+        }
+        __syncwarp();
+    }
+    if (lane == 0) {
+        JfgpuChainState &g = A.state[c];
+        g.time_q = w.ts_q;
+        g.time_r = w.ts_r;
+        g.eoc_q = w.eoc_q;
+        g.eoc_r = w.eoc_r;
+        g.events = w.events;
+        g.bound_warnings = w.warnings;
+        g.refine_fallbacks = w.fallbacks;
+        g.candidates = w.candidates;
+        g.refined = w.refined;
+        g.active = w.active;
+        g.direction = w.direction;
+        g.eoc_new_active = w.eoc_new;
+        g.occ_active = w.occ_active;
+        g.occ_cell = w.occ_cell;
+        g.n_surplus = w.n_surplus;
+        g.status = w.status;
+    }
+}
+
+// ---------------------------------------------------------------------------------------------------------------
+// start of the chains: FP32 mirror, occupancy in particle order (single_active_cell_occupancy.py:95-121),
+// lifting state at time 0 (initial_chain_start_of_run_event_handler.py) and the first end-of-chain candidate
+// ---------------------------------------------------------------------------------------------------------------
+__global__ void init_kernel(EngineView view, long long n_chains, double *positions, float4 *positions32,
+                            const double *charges, int32_t *occupancy, int32_t *surplus, JfgpuChainState *state) {
+    const int warp = threadIdx.x >> 5;
+    const int lane = threadIdx.x & 31;
+    const long long c = (long long)blockIdx.x * (blockDim.x >> 5) + warp;
+    if (c >= n_chains) return;
+    const ChainDev &ch = view.chains[c];
+    for (int i = lane; i < ch.n; i += 32) {
+        const double *p = positions + 3 * (ch.pos_off + i);
+        positions32[ch.pos_off + i] =
+            make_float4((float)p[0], (float)p[1], (float)p[2], charges ? (float)charges[ch.pos_off + i] : 1.0f);
+    }
+    for (long long k = lane; k < (long long)ch.ncells * ch.max_occ; k += 32) occupancy[ch.occ_off + k] = -1;
+    __syncwarp();
+    if (lane != 0) return;
+    int status = JFGPU_STATUS_OK;
+    int n_surplus = 0;
+    int32_t *occ = occupancy + ch.occ_off;
+    for (int i = 0; i < ch.n; ++i) {
+        int cell;
+        if (cell_of(ch, positions + 3 * (ch.pos_off + i), cell)) {
+            status = JFGPU_STATUS_CELL_RANGE;
+            break;
+        }
+        int32_t *slots = occ + (long long)cell * ch.max_occ;
+        int k = 0;
+        while (k < ch.max_occ && slots[k] >= 0) ++k;
+        if (k < ch.max_occ) {
+            slots[k] = i;
+        } else {
+            surplus[ch.pos_off + n_surplus++] = i;
+        }
+    }
+    JfgpuChainState g;
+    g.time_q = 0.0;
+    g.time_r = 0.0;
+    time_add(0.0, 0.0, time_sub(0.0, 0.0, 0.0, 0.0) + ch.chain_time, g.eoc_q, g.eoc_r);
+    g.events = 0;
+    g.bound_warnings = 0;
+    g.refine_fallbacks = 0;
+    g.candidates = 0;
+    g.refined = 0;
+    g.active = ch.initial_active;
+    g.direction = ch.initial_direction;
+    g.eoc_new_active = (int)randbelow(draw(ch.key, 0, kRngNewActive, 0), (uint32_t)ch.n);
+    g.occ_active = -1;
+    g.occ_cell = -1;
+    g.n_surplus = n_surplus;
+    g.status = status;
+    g.reserved = 0;
+    state[c] = g;
+}
+
+}  // namespace jf
+
+// ---------------------------------------------------------------------------------------------------------------
+// launchers (called by jf_engine_host.cu)
+// ---------------------------------------------------------------------------------------------------------------
+namespace jf {
+
+cudaError_t launch_init(const EngineView &view, long long n_chains, const JfgpuBuffers &b, cudaStream_t stream) {
+    const int warps = 4;
+    long long blocks = (n_chains + warps - 1) / warps;
+    init_kernel<<<(unsigned)blocks, warps * 32, 0, stream>>>(view, n_chains, b.positions,
+                                                              reinterpret_cast<float4 *>(b.positions32), b.charges,
+                                                              b.occupancy, b.surplus, b.state);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_run(const EngineView &view, const JfgpuBuffers &b, long long first, long long count,
+                       long long max_events, double stop_q, double stop_r, int mode, JfgpuEvent *log,
+                       long long log_capacity, int warps_per_block, cudaStream_t stream) {
+    RunArgs A;
+    A.view = view;
+    A.positions = b.positions;
+    A.positions32 = reinterpret_cast<float4 *>(b.positions32);
+    A.charges = b.charges;
+    A.occupancy = b.occupancy;
+    A.surplus = b.surplus;
+    A.state = b.state;
+    A.log = log;
+    A.log_capacity = log_capacity;
+    A.first_chain = first;
+    A.count = count;
+    A.max_events = max_events;
+    A.stop_q = stop_q;
+    A.stop_r = stop_r;
+    A.has_stop = isinf(stop_q) ? 0 : 1;
+    int warps = warps_per_block;
+    if (warps < 1) warps = 1;
+    if (warps > 8) warps = 8;
+    if (count < warps) warps = (int)count;
+    long long blocks = (count + warps - 1) / warps;
+    size_t smem = sizeof(WarpState) * warps;
+    if (mode == JFGPU_MODE_MIXED) {
+        chains_kernel<JFGPU_MODE_MIXED><<<(unsigned)blocks, warps * 32, smem, stream>>>(A);
+    } else {
+        chains_kernel<JFGPU_MODE_EXACT><<<(unsigned)blocks, warps * 32, smem, stream>>>(A);
+    }
+    return cudaGetLastError();
+}
+
+}  // namespace jf

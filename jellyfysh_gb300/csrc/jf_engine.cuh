@@ -1,0 +1,66 @@
+// jf_engine.cuh -- device-side layout of a chain batch (shared by the engine translation units).
+//
+// HBM layout (all pools are flat arrays, a chain owns a contiguous slice of each):
+//   positions   double[P][3]   FP64 master positions (the reference's Unit.position), chain c at particle_offset
+//   positions32 float4[P]      FP32 mirror (x, y, z, charge) read by the FP32 screening
+//   charges     double[P]
+//   occupancy   int32[O]       cells * max_occupants slots, -1 = empty (SingleActiveCellOccupancy._occupants)
+//   surplus     int32[P]       surplus identifiers of the chain, n_surplus of them (SingleActiveCellOccupancy._surplus)
+//   state       JfgpuChainState[C]
+// Engine tables (owned by the engine): per-chain ChainDev, per-geometry cell bounds and relative/translate
+// tables, per-species far-field bounds (FP64 and FP32), Walker tables and the merged-image Fourier coefficients.
+#pragma once
+#include "jf_device.cuh"
+
+namespace jf {
+
+constexpr int kMaxResidues = 64;  // cells per side limit of the near-cell bit mask
+
+struct WalkerDev {
+    const int32_t *first_item;
+    const int32_t *second_item;
+    const double *first_rate;
+    int32_t size;
+    int32_t pad;
+    double total_rate;
+    double mean_rate;
+};
+
+struct SpeciesDev {
+    MH lj;
+    MIC mic;
+    const double *bound_upper;   // [cells][3]
+    const double *bound_lower;   // [cells][3] negated lower bounds
+    const float *bound_upper32;  // [cells][3] FP32 copy for the screening
+    WalkerDev walker[2][3];      // [upper/lower][direction]
+};
+
+struct ChainDev {
+    int32_t potential, far, n, m;
+    int32_t ncells, max_occ, n_res, species;
+    int32_t initial_active, initial_direction;
+    int32_t geom_offset;         // into cell_min / cell_max pools (m entries)
+    int32_t table_offset;        // into rel / tra pools (m * m entries)
+    int32_t res[16];             // distinct residues of the neighbour-layer offsets modulo m (n_res of them)
+    uint64_t near_mask;          // bit r set when residue r is within the neighbour layers
+    int64_t pos_off, occ_off;
+    double L, half, side, beta, chain_time, speed;
+    double diameter_sq;          // hard sphere / hard core: 4 r r (0 = none)
+    double bound_prefactor;      // inverse-power Coulomb bound
+    double coulomb_prefactor;
+    float L32, half32;
+    float ulp_margin32;          // rounding scale of FP32 separations (16 L 2^-24): closer calls are flagged
+    float screen_abs32;          // absolute screening margin in length units (L 2^-16)
+    uint64_t key;
+};
+
+struct EngineView {
+    const ChainDev *chains;
+    const SpeciesDev *species;
+    const double *cell_min;
+    const double *cell_max;
+    const int16_t *rel;  // relative_cell index along one axis, [a * m + b]
+    const int16_t *tra;  // translate index along one axis, [a * m + b]
+};
+
+}  // namespace jf
