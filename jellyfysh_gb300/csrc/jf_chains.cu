@@ -122,8 +122,26 @@ struct RunArgs {
     int has_stop;
 };
 
-__device__ inline int cell_of(const ChainDev &ch, const double *p, int &cell) {
-    long long ix = (long long)(p[0] / ch.side), iy = (long long)(p[1] / ch.side), iz = (long long)(p[2] / ch.side);
+// int(x / side) along one axis (cuboid_cells.py:190-211), evaluated exactly without a division: the exact float
+// bounds of the cells satisfy cell_min[i] <= x <= cell_max[i] if and only if int(x / side) == i, so a multiply by
+// 1 / side guesses the index and at most a step or two against the bounds corrects it.
+__device__ inline long long axis_index(const EngineView &v, const ChainDev &ch, double x) {
+    if (!(x >= 0.0) || !(x < ch.L)) return (long long)(x / ch.side);
+    const double *lo = v.cell_min + ch.geom_offset;
+    const double *hi = v.cell_max + ch.geom_offset;
+    long long i = (long long)(x * ch.inv_side);
+    if (i > ch.m - 1) i = ch.m - 1;
+    if (i < 0) i = 0;
+    while (i > 0 && x < lo[i]) --i;
+    while (x > hi[i]) {
+        if (i == ch.m - 1) return ch.m;
+        ++i;
+    }
+    return i;
+}
+
+__device__ inline int cell_of(const EngineView &v, const ChainDev &ch, const double *p, int &cell) {
+    long long ix = axis_index(v, ch, p[0]), iy = axis_index(v, ch, p[1]), iz = axis_index(v, ch, p[2]);
     long long idx = ix + (long long)ch.m * iy + (long long)ch.m * ch.m * iz;
     if (idx < 0 || idx >= ch.ncells) return JFGPU_STATUS_CELL_RANGE;
     cell = (int)idx;
@@ -167,7 +185,7 @@ __device__ inline int translate_cell(const EngineView &v, const ChainDev &ch, in
 
 __device__ inline void separation64(const ChainDev &ch, const double *from, const double *to, double *s) {
 #pragma unroll
-    for (int k = 0; k < 3; ++k) s[k] = py_mod((to[k] - from[k]) + ch.half, ch.L) - ch.half;
+    for (int k = 0; k < 3; ++k) s[k] = py_mod_near((to[k] - from[k]) + ch.half, ch.L) - ch.half;
 }
 
 __device__ inline void load_pos(const RunArgs &A, const ChainDev &ch, int j, double *p) {
@@ -182,7 +200,7 @@ __device__ inline double charge_of(const RunArgs &A, const ChainDev &ch, int j) 
 }
 
 // FP64 candidates of one (active, target) pair of the nearby / surplus taggers
-__device__ inline int exact_pair(const RunArgs &A, const ChainDev &ch, const SpeciesDev &sp, const WarpState &w,
+__device__ __noinline__ int exact_pair(const RunArgs &A, const ChainDev &ch, const SpeciesDev &sp, const WarpState &w,
                                  int j, long long ev, Cand &best) {
     double pj[3], s[3];
     load_pos(A, ch, j, pj);
@@ -214,14 +232,14 @@ __device__ inline int exact_pair(const RunArgs &A, const ChainDev &ch, const Spe
 }
 
 // FP64 candidate of a far occupant under the cell-bounding potential
-__device__ inline int exact_cell_bounding(const RunArgs &A, const ChainDev &ch, const SpeciesDev &sp,
+__device__ __noinline__ int exact_cell_bounding(const RunArgs &A, const ChainDev &ch, const SpeciesDev &sp,
                                           const WarpState &w, int j, int active_cell, long long ev, bool from_position,
                                           int stored_cell, Cand &best) {
     int target_cell = stored_cell;
     if (from_position) {
         double pj[3];
         load_pos(A, ch, j, pj);
-        JF_TRY(cell_of(ch, pj, target_cell));
+        JF_TRY(cell_of(A.view, ch, pj, target_cell));
     }
     int rc = relative_cell(A.view, ch, target_cell, active_cell);
     double du = expovariate(draw(ch.key, (uint64_t)ev, kRngPair, (uint32_t)j), ch.beta);
@@ -232,7 +250,7 @@ __device__ inline int exact_cell_bounding(const RunArgs &A, const ChainDev &ch, 
 }
 
 // cell veto, cell boundary and end of chain: the single candidates of lane 0
-__device__ inline int single_candidates(const RunArgs &A, const ChainDev &ch, const SpeciesDev &sp, const WarpState &w,
+__device__ __noinline__ int single_candidates(const RunArgs &A, const ChainDev &ch, const SpeciesDev &sp, const WarpState &w,
                                         int active_cell, long long ev, Cand &best) {
     const int d = w.direction;
     if (ch.far == JFGPU_FAR_CELL_VETO) {
@@ -284,10 +302,10 @@ __device__ inline void occ_insert(const RunArgs &A, const ChainDev &ch, WarpStat
     w.n_surplus += 1;
 }
 
-__device__ inline int occ_update(const RunArgs &A, const ChainDev &ch, WarpState &w) {
+__device__ __noinline__ int occ_update(const RunArgs &A, const ChainDev &ch, WarpState &w) {
     if (w.active != w.occ_active) {
         if (w.occ_active >= 0) occ_insert(A, ch, w, w.occ_cell, w.occ_active);
-        JF_TRY(cell_of(ch, w.pa, w.occ_cell));
+        JF_TRY(cell_of(A.view, ch, w.pa, w.occ_cell));
         w.occ_active = w.active;
         int32_t *slots = A.occupancy + ch.occ_off + (long long)w.occ_cell * ch.max_occ;
         for (int k = 0; k < ch.max_occ; ++k)
@@ -304,7 +322,7 @@ __device__ inline int occ_update(const RunArgs &A, const ChainDev &ch, WarpState
             }
         return JFGPU_STATUS_ASSERTION;
     }
-    return cell_of(ch, w.pa, w.occ_cell);
+    return cell_of(A.view, ch, w.pa, w.occ_cell);
 }
 
 // ---------------------------------------------------------------------------------------------------------------
@@ -326,7 +344,7 @@ __device__ inline int real_rate(const RunArgs &A, const ChainDev &ch, const Spec
     return JFGPU_STATUS_OK;
 }
 
-__device__ inline int thinning(const RunArgs &A, const ChainDev &ch, const SpeciesDev &sp, WarpState &w, int t,
+__device__ __noinline__ int thinning(const RunArgs &A, const ChainDev &ch, const SpeciesDev &sp, WarpState &w, int t,
                                double bounding_rate, long long ev, int &accepted) {
     double real;
     JF_TRY(real_rate(A, ch, sp, w, t, real));
@@ -356,14 +374,14 @@ __device__ inline void time_slice(const ChainDev &ch, WarpState &w, double q, do
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
         double v = k == w.direction ? ch.speed : 0.0;
-        w.pa[k] = py_mod(w.pa[k] + v * dt, ch.L);
+        w.pa[k] = py_mod_near(w.pa[k] + v * dt, ch.L);
     }
     w.ts_q = q;
     w.ts_r = r;
 }
 
 // commit the winner; returns a status
-__device__ inline int commit(const RunArgs &A, const ChainDev &ch, const SpeciesDev &sp, WarpState &w, const Cand &best,
+__device__ __noinline__ int commit(const RunArgs &A, const ChainDev &ch, const SpeciesDev &sp, WarpState &w, const Cand &best,
                              int active_cell, long long chain_index, long long log_index) {
     const long long ev = w.events;
     int moved = w.active;
@@ -398,7 +416,7 @@ __device__ inline int commit(const RunArgs &A, const ChainDev &ch, const Species
     }
     case JFGPU_EV_CELL_BOUNDING: {
         int now_cell;
-        JF_TRY(cell_of(ch, w.pa, now_cell));
+        JF_TRY(cell_of(A.view, ch, w.pa, now_cell));
         if (now_cell != active_cell) return JFGPU_STATUS_ASSERTION;
         int accepted;
         JF_TRY(thinning(A, ch, sp, w, best.target, best.rate * ch.speed, ev, accepted));
@@ -672,19 +690,13 @@ __global__ void __launch_bounds__(256) chains_kernel(RunArgs A) {
         }
         __syncwarp();
         if (w.status != JFGPU_STATUS_OK) break;
-        int active_cell = 0;
-        {
-            int st = cell_of(ch, w.pa, active_cell);
-            if (st) {
-                if (lane == 0) w.status = st;
-                __syncwarp();
-                break;
-            }
-        }
+        // the active cell of the handlers (position_to_cell of the active position) is the occupancy's
+        // active cell just computed from the same position
+        const int active_cell = w.occ_cell;
         Cand best;
         int status = JFGPU_STATUS_OK;
         int counted = 0, refined = 0;
-        if (MODE == JFGPU_MODE_MIXED) {
+        if (MODE == JFGPU_MODE_MIXED && ch.potential != JFGPU_POT_COULOMB) {
             int fallback = mixed_candidates(A, ch, sp, lj32, w, active_cell, lane, best, status, counted, refined);
             if (fallback && status == JFGPU_STATUS_OK) {
                 int recount = 0;
@@ -758,7 +770,7 @@ __global__ void init_kernel(EngineView view, long long n_chains, double *positio
     int32_t *occ = occupancy + ch.occ_off;
     for (int i = 0; i < ch.n; ++i) {
         int cell;
-        if (cell_of(ch, positions + 3 * (ch.pos_off + i), cell)) {
+        if (cell_of(view, ch, positions + 3 * (ch.pos_off + i), cell)) {
             status = JFGPU_STATUS_CELL_RANGE;
             break;
         }

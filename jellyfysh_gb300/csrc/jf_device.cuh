@@ -56,9 +56,22 @@ __host__ __device__ inline double py_mod(double x, double y) {
     return mod;
 }
 
-// divmod(x, 1.0) (CPython float_divmod with the divisor 1.0).
+// float.__mod__ for x in (-y, 2y), y > 0, without fmod: fmod(x, y) is x for |x| < y and the exact x - y for
+// y <= x < 2y; the sign correction of a negative remainder then adds y with one rounding, as CPython does.
+__host__ __device__ inline double py_mod_near(double x, double y) {
+    if (x > 0.0 && x < y) return x;
+    if (x == 0.0) return 0.0;
+    if (x < 0.0 && x > -y) return x + y;
+    if (x >= y && x < 2.0 * y) {
+        double r = x - y;
+        return r == 0.0 ? 0.0 : r;
+    }
+    return py_mod(x, y);
+}
+
+// divmod(x, 1.0) (CPython float_divmod with the divisor 1.0); fmod(x, 1.0) is the exact x - trunc(x)
 __host__ __device__ inline void py_divmod1(double vx, double &quotient, double &remainder) {
-    double mod = fmod(vx, 1.0);
+    double mod = fabs(vx) < 4503599627370496.0 ? vx - trunc(vx) : fmod(vx, 1.0);
     double div = vx - mod;
     if (mod != 0.0) {
         if (mod < 0.0) {
@@ -239,14 +252,18 @@ __device__ inline double pow15_cr(double x) {
 // x ** (1.0 / 6.0) for x > 0 (the exponent is the double nearest 1/6): Newton step on z^6 = x in double-double
 // from the CUDA pow, then the correction x^(e - 1/6) = 1 - c log x with c = 1/6 - double(1/6).
 __device__ inline double sixth_root_cr(double x) {
-    if (!(x > 0.0) || isinf(x)) return pow(x, 1.0 / 6.0);
-    double z0 = pow(x, 1.0 / 6.0);
+    if (!(x > 1e-30 && x < 1e30)) return pow(x, 1.0 / 6.0);
+    // FP32 guess (relative error ~1e-7), one plain Newton step (~1e-14), then the double-double step
+    double g = (double)exp2f(__log2f((float)x) * (1.0f / 6.0f));
+    double g2 = g * g;
+    double g5 = g2 * g2 * g;
+    double z0 = g - (g5 * g - x) / (6.0 * g5);
     DD z6 = dd_ipow(z0, 6);
     double residual = (z6.hi - x) + z6.lo;
     double z5 = ipow_cr(z0, 5);
     double dz = residual / (6.0 * z5);
     const double c = 9.25185853854297e-18;
-    double lo = -dz - z0 * (c * log(x));
+    double lo = -dz - z0 * (c * (double)__logf((float)x));
     return z0 + lo;
 }
 

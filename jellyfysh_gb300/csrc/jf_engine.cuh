@@ -44,7 +44,7 @@ struct ChainDev {
     int32_t res[16];             // distinct residues of the neighbour-layer offsets modulo m (n_res of them)
     uint64_t near_mask;          // bit r set when residue r is within the neighbour layers
     int64_t pos_off, occ_off;
-    double L, half, side, beta, chain_time, speed;
+    double L, half, side, inv_side, beta, chain_time, speed;
     double diameter_sq;          // hard sphere / hard core: 4 r r (0 = none)
     double bound_prefactor;      // inverse-power Coulomb bound
     double coulomb_prefactor;

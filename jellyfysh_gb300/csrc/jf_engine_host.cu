@@ -489,6 +489,7 @@ int jfgpu_engine_create(const JfgpuChainDesc *chains, int64_t n_chains, void *st
         ch.L = d.system_length;
         ch.half = d.system_length / 2.0;
         ch.side = d.system_length / m;
+        ch.inv_side = 1.0 / ch.side;
         ch.beta = d.beta;
         ch.chain_time = d.chain_time;
         ch.speed = d.speed;

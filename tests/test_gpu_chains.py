@@ -124,7 +124,7 @@ def test_random_hard_sphere_systems_against_oracle():
     specs, positions = [], []
     for c in range(12):
         n = int(rng.integers(16, 120))
-        eta = float(rng.uniform(0.1, 0.4))
+        eta = float(rng.uniform(0.1, 0.3))
         length = systems.hard_sphere_box(n, eta, radius=0.5)
         layers = 1 + c % 2
         m = max(3, int(length / (1.0 / layers)))
