@@ -8,7 +8,7 @@ import ctypes
 import os
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIBRARY_PATH = os.path.join(HERE, "_build", "libjfgpu.so")
+LIBRARY_PATH = os.environ.get("JFGPU_LIBRARY") or os.path.join(HERE, "_build", "libjfgpu.so")
 
 OK = 0
 ERROR_NAMES = {0: "ok", 1: "CUDA runtime error", 2: "invalid argument", 3: "device allocation failed",

@@ -42,16 +42,20 @@ def up_to_date() -> bool:
     return all(os.path.getmtime(f) <= built for f in _inputs())
 
 
-def build(force: bool = False, verbose: bool = False) -> str:
-    if not force and up_to_date():
+def build(force: bool = False, verbose: bool = False, defines=(), output: str = None) -> str:
+    """Compile libjfgpu.so; ``defines`` (e.g. JF_CHAIN_MIN_BLOCKS=4) and ``output`` build a tuning variant."""
+    library = output or LIBRARY
+    build_dir = os.path.dirname(library)
+    if not force and not defines and output is None and up_to_date():
         return LIBRARY
-    os.makedirs(BUILD_DIR, exist_ok=True)
+    os.makedirs(build_dir, exist_ok=True)
     compiler = nvcc()
     extra = ["-Xptxas", "-v"] if verbose else []
 
     def compile_one(source):
-        obj = os.path.join(BUILD_DIR, source.replace(".cu", ".o"))
-        command = [compiler, *ARCH, *FLAGS, *extra, "-c", os.path.join(CSRC, source), "-o", obj]
+        obj = os.path.join(build_dir, source.replace(".cu", ".o"))
+        command = [compiler, *ARCH, *FLAGS, *["-D" + d for d in defines], *extra, "-c", os.path.join(CSRC, source),
+                   "-o", obj]
         result = subprocess.run(command, capture_output=True, text=True)
         if result.returncode != 0:
             raise RuntimeError("nvcc failed on %s:\n%s%s" % (source, result.stdout, result.stderr))
@@ -62,12 +66,19 @@ def build(force: bool = False, verbose: bool = False) -> str:
     if verbose:
         for _, log in results:
             sys.stderr.write(log)
-    temporary = LIBRARY + ".%d.tmp" % os.getpid()
+    temporary = library + ".%d.tmp" % os.getpid()
     command = [compiler, *ARCH, "-shared", "-o", temporary] + [obj for obj, _ in results] + ["-lcudart"]
     subprocess.run(command, check=True)
-    os.replace(temporary, LIBRARY)
-    return LIBRARY
+    os.replace(temporary, library)
+    return library
 
 
 if __name__ == "__main__":
-    print(build(force="--force" in sys.argv, verbose="-v" in sys.argv))
+    import argparse
+    parser = argparse.ArgumentParser()
+    parser.add_argument("--force", action="store_true")
+    parser.add_argument("-v", dest="verbose", action="store_true")
+    parser.add_argument("-D", dest="defines", action="append", default=[])
+    parser.add_argument("-o", dest="output", default=None)
+    args = parser.parse_args()
+    print(build(force=args.force, verbose=args.verbose, defines=args.defines, output=args.output))

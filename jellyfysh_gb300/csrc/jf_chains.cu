@@ -199,59 +199,86 @@ __device__ inline double charge_of(const RunArgs &A, const ChainDev &ch, int j) 
     return A.charges ? A.charges[ch.pos_off + j] : 1.0;
 }
 
-// FP64 candidates of one (active, target) pair of the nearby / surplus taggers
-__device__ __noinline__ int exact_pair(const RunArgs &A, const ChainDev &ch, const SpeciesDev &sp, const WarpState &w,
-                                 int j, long long ev, Cand &best) {
-    double pj[3], s[3];
+// x / speed and x * speed: exact no-ops for the unit speed of the reference's configurations
+__device__ inline double div_speed(const ChainDev &ch, double x) { return ch.speed == 1.0 ? x : x / ch.speed; }
+__device__ inline double mul_speed(const ChainDev &ch, double x) { return ch.speed == 1.0 ? x : x * ch.speed; }
+
+// keyed draws of one event and kind: the Weyl state key + (counter + 1) * golden with counter = base | target,
+// split so that the per-target part is one multiply (same bits as draw())
+__device__ inline uint64_t draw_base(uint64_t key, uint64_t event, uint32_t kind) {
+    return key + (((event << 24) | ((uint64_t)(kind & 0xFu) << 20)) + 1) * kGolden;
+}
+__device__ inline uint64_t draw_at(uint64_t base, uint32_t target) {
+    return mix64(base + (uint64_t)(target & 0xFFFFFu) * kGolden);
+}
+
+// FP64 candidates of one (active, target) pair of the nearby / surplus taggers, one function per potential
+__device__ __noinline__ int exact_pair_hs(const RunArgs &A, const ChainDev &ch, const WarpState &w, int j,
+                                         Cand &best) {
+    double pj[3], s[3], dt;
     load_pos(A, ch, j, pj);
     separation64(ch, w.pa, pj, s);
-    const int d = w.direction;
-    double dt;
-    if (ch.potential == JFGPU_POT_HARD_SPHERE) {
-        JF_TRY(hs_displacement_axis(ch.diameter_sq, d, ch.speed, s, dt));
-        offer(best, w.ts_q, w.ts_r, dt, JFGPU_EV_PAIR, j, -1, 0.0);
-    } else if (ch.potential == JFGPU_POT_LENNARD_JONES) {
-        double du = expovariate(draw(ch.key, (uint64_t)ev, kRngPair, (uint32_t)j), ch.beta);
-        double disp;
-        JF_TRY(mh_std_displacement(sp.lj, d, s, du, disp));
-        offer(best, w.ts_q, w.ts_r, disp / ch.speed, JFGPU_EV_PAIR, j, -1, 0.0);
-    } else {
-        if (ch.diameter_sq > 0.0) {
-            double sh[3] = {s[0], s[1], s[2]};
-            JF_TRY(hs_displacement_axis(ch.diameter_sq, d, ch.speed, sh, dt));
-            offer(best, w.ts_q, w.ts_r, dt, JFGPU_EV_HARDCORE, j, -1, 0.0);
-        }
-        double du = expovariate(draw(ch.key, (uint64_t)ev, kRngPair, (uint32_t)j), ch.beta);
-        double p[3];
-        permute3(s, d, p);
-        double pp = ch.bound_prefactor * charge_of(A, ch, w.active) * charge_of(A, ch, j);
-        double disp = ipcb_x_displacement(pp, p[0], p[1], p[2], du, ch.L);
-        offer(best, w.ts_q, w.ts_r, disp / ch.speed, JFGPU_EV_BOUNDED, j, -1, 0.0);
-    }
+    JF_TRY(hs_displacement_axis(ch.diameter_sq, w.direction, ch.speed, s, dt));
+    offer(best, w.ts_q, w.ts_r, dt, JFGPU_EV_PAIR, j, -1, 0.0);
     return JFGPU_STATUS_OK;
 }
 
-// FP64 candidate of a far occupant under the cell-bounding potential
-__device__ __noinline__ int exact_cell_bounding(const RunArgs &A, const ChainDev &ch, const SpeciesDev &sp,
-                                          const WarpState &w, int j, int active_cell, long long ev, bool from_position,
-                                          int stored_cell, Cand &best) {
-    int target_cell = stored_cell;
-    if (from_position) {
-        double pj[3];
-        load_pos(A, ch, j, pj);
-        JF_TRY(cell_of(A.view, ch, pj, target_cell));
+__device__ __noinline__ int exact_pair_lj(const RunArgs &A, const ChainDev &ch, const SpeciesDev &sp,
+                                         const WarpState &w, int j, long long ev, Cand &best) {
+    double pj[3], s[3], disp;
+    load_pos(A, ch, j, pj);
+    separation64(ch, w.pa, pj, s);
+    double du = expovariate(draw(ch.key, (uint64_t)ev, kRngPair, (uint32_t)j), ch.beta);
+    JF_TRY(mh_std_displacement(sp.lj, w.direction, s, du, disp));
+    offer(best, w.ts_q, w.ts_r, div_speed(ch, disp), JFGPU_EV_PAIR, j, -1, 0.0);
+    return JFGPU_STATUS_OK;
+}
+
+__device__ __noinline__ int exact_pair_coulomb(const RunArgs &A, const ChainDev &ch, const WarpState &w, int j,
+                                              long long ev, Cand &best) {
+    double pj[3], s[3], dt;
+    load_pos(A, ch, j, pj);
+    separation64(ch, w.pa, pj, s);
+    const int d = w.direction;
+    if (ch.diameter_sq > 0.0) {
+        double sh[3] = {s[0], s[1], s[2]};
+        JF_TRY(hs_displacement_axis(ch.diameter_sq, d, ch.speed, sh, dt));
+        offer(best, w.ts_q, w.ts_r, dt, JFGPU_EV_HARDCORE, j, -1, 0.0);
     }
+    double du = expovariate(draw(ch.key, (uint64_t)ev, kRngPair, (uint32_t)j), ch.beta);
+    double p[3];
+    permute3(s, d, p);
+    double pp = ch.bound_prefactor * charge_of(A, ch, w.active) * charge_of(A, ch, j);
+    double disp = ipcb_x_displacement(pp, p[0], p[1], p[2], du, ch.L);
+    offer(best, w.ts_q, w.ts_r, div_speed(ch, disp), JFGPU_EV_BOUNDED, j, -1, 0.0);
+    return JFGPU_STATUS_OK;
+}
+
+__device__ inline int exact_pair(const RunArgs &A, const ChainDev &ch, const SpeciesDev &sp, const WarpState &w,
+                                 int j, long long ev, Cand &best) {
+    if (ch.potential == JFGPU_POT_HARD_SPHERE) return exact_pair_hs(A, ch, w, j, best);
+    if (ch.potential == JFGPU_POT_LENNARD_JONES) return exact_pair_lj(A, ch, sp, w, j, ev, best);
+    return exact_pair_coulomb(A, ch, w, j, ev, best);
+}
+
+// FP64 candidate of a far occupant under the cell-bounding potential (cells from the positions, as the handler)
+__device__ __noinline__ int exact_cell_bounding(const RunArgs &A, const ChainDev &ch, const SpeciesDev &sp,
+                                               const WarpState &w, int j, int active_cell, long long ev, Cand &best) {
+    double pj[3];
+    int target_cell;
+    load_pos(A, ch, j, pj);
+    JF_TRY(cell_of(A.view, ch, pj, target_cell));
     int rc = relative_cell(A.view, ch, target_cell, active_cell);
     double du = expovariate(draw(ch.key, (uint64_t)ev, kRngPair, (uint32_t)j), ch.beta);
     double rate = sp.bound_upper[rc * 3 + w.direction];
     double disp = rate > 0 ? du / rate : kInf;
-    offer(best, w.ts_q, w.ts_r, disp / ch.speed, JFGPU_EV_CELL_BOUNDING, j, rc, rate);
+    offer(best, w.ts_q, w.ts_r, div_speed(ch, disp), JFGPU_EV_CELL_BOUNDING, j, rc, rate);
     return JFGPU_STATUS_OK;
 }
 
 // cell veto, cell boundary and end of chain: the single candidates of lane 0
-__device__ __noinline__ int single_candidates(const RunArgs &A, const ChainDev &ch, const SpeciesDev &sp, const WarpState &w,
-                                        int active_cell, long long ev, Cand &best) {
+__device__ __noinline__ int single_candidates(const RunArgs &A, const ChainDev &ch, const SpeciesDev &sp,
+                                             const WarpState &w, int active_cell, long long ev, Cand &best) {
     const int d = w.direction;
     if (ch.far == JFGPU_FAR_CELL_VETO) {
         double charge_factor = ch.potential == JFGPU_POT_LENNARD_JONES ? 1.0 : (charge_of(A, ch, w.active) * 1.0) / 1.0;
@@ -268,15 +295,15 @@ __device__ __noinline__ int single_candidates(const RunArgs &A, const ChainDev &
         double rate = (which == 0 ? sp.bound_upper[rc * 3 + d] : sp.bound_lower[rc * 3 + d]) * charge_factor;
         if (!(rate > 0.0)) return JFGPU_STATUS_ASSERTION;
         int target_cell = translate_cell(A.view, ch, active_cell, rc);
-        double dt = expovariate(draw(ch.key, (uint64_t)ev, kRngVetoTime, 0), ch.beta) / (total_rate * ch.speed);
+        double dt = expovariate(draw(ch.key, (uint64_t)ev, kRngVetoTime, 0), ch.beta) / mul_speed(ch, total_rate);
         offer(best, w.ts_q, w.ts_r, dt, JFGPU_EV_CELL_VETO, -1, target_cell, rate);
     }
     int ax[3];
     cell_axes(ch, active_cell, ax);
-    double boundary = A.view.cell_min[ch.geom_offset + (ax[d] + 1) % ch.m];
+    double boundary = A.view.cell_min[ch.geom_offset + (ax[d] + 1 == ch.m ? 0 : ax[d] + 1)];
     double sep = boundary - w.pa[d];
     if (sep < 0.0) sep = sep + ch.L;
-    offer(best, w.ts_q, w.ts_r, sep / ch.speed, JFGPU_EV_BOUNDARY, -1, -1, boundary);
+    offer(best, w.ts_q, w.ts_r, div_speed(ch, sep), JFGPU_EV_BOUNDARY, -1, -1, boundary);
     Cand e;
     e.q = w.eoc_q;
     e.r = w.eoc_r;
@@ -336,23 +363,56 @@ __device__ inline int real_rate(const RunArgs &A, const ChainDev &ch, const Spec
     if (ch.potential == JFGPU_POT_LENNARD_JONES) {
         double value;
         JF_TRY(mh_std_derivative(sp.lj, w.direction, s, value));
-        out = value * ch.speed;
+        out = mul_speed(ch, value);
         return JFGPU_STATUS_OK;
     }
-    out = mic_std_derivative(sp.mic, ch.coulomb_prefactor, w.direction, s, charge_of(A, ch, w.active),
-                             charge_of(A, ch, t)) * ch.speed;
+    out = mul_speed(ch, mic_std_derivative(sp.mic, ch.coulomb_prefactor, w.direction, s, charge_of(A, ch, w.active),
+                                           charge_of(A, ch, t)));
     return JFGPU_STATUS_OK;
 }
 
+// Thinning: accept iff uniform(0, bound) < real rate (event_handler_with_bounding_potential.py:95-101).  For
+// Lennard-Jones the decision (and the bound-violation count) is first taken in FP32 from the FP32 mirror; only a
+// decision within the FP32 error margin is re-taken in FP64, so the outcome always equals the FP64 one.
 __device__ __noinline__ int thinning(const RunArgs &A, const ChainDev &ch, const SpeciesDev &sp, WarpState &w, int t,
-                               double bounding_rate, long long ev, int &accepted) {
+                                    double bounding_rate, long long ev, int &accepted) {
+    const double u = uniform53(draw(ch.key, (uint64_t)ev, kRngThin, 0));
+    if (ch.potential == JFGPU_POT_LENNARD_JONES) {
+        const float4 pt = A.positions32[ch.pos_off + t];
+        float sv[3] = {pt.x - (float)w.pa[0], pt.y - (float)w.pa[1], pt.z - (float)w.pa[2]};
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            if (sv[k] >= ch.half32) sv[k] -= ch.L32;
+            if (sv[k] < -ch.half32) sv[k] += ch.L32;
+        }
+        const float r2 = sv[0] * sv[0] + sv[1] * sv[1] + sv[2] * sv[2];
+        const float ir2 = 1.0f / r2;
+        const float ir8 = ir2 * ir2 * ir2 * ir2;
+        const float ir14 = ir8 * ir2 * ir2 * ir2;
+        const float c6 = (float)(6.0 * sp.lj.six.prefactor) * ir8;
+        const float c12 = (float)(12.0 * sp.lj.twelve.prefactor) * ir14;
+        const float speed = (float)ch.speed;
+        const float sd = sv[w.direction];
+        const float real32 = (c6 + c12) * sd * speed;
+        const float bound32 = (float)bounding_rate;
+        const float ub32 = bound32 * (float)u;
+        const float scale = (fabsf(c6) + fabsf(c12)) * speed;
+        const float margin = scale * (fabsf(sd) * (1.0f / 1024.0f) + 64.0f * ch.ulp_margin32) + ub32 * (1.0f / 65536.0f) +
+                             bound32 * (1.0f / 65536.0f);
+        const bool ambiguous = !(fabsf(real32 - ub32) > margin) || !(fabsf(bound32 - real32) > margin) ||
+                               !isfinite(real32);
+        if (!ambiguous) {
+            accepted = real32 > ub32 ? 1 : 0;
+            if (real32 > 0.0f && bound32 < real32) w.warnings += 1;
+            return JFGPU_STATUS_OK;
+        }
+    }
     double real;
     JF_TRY(real_rate(A, ch, sp, w, t, real));
     accepted = 0;
     if (real > 0) {
         if (bounding_rate < real) w.warnings += 1;
-        double u = bounding_rate * uniform53(draw(ch.key, (uint64_t)ev, kRngThin, 0));
-        if (u < real) accepted = 1;
+        if (bounding_rate * u < real) accepted = 1;
     }
     return JFGPU_STATUS_OK;
 }
@@ -369,13 +429,12 @@ __device__ inline void store_active(const RunArgs &A, const ChainDev &ch, const 
     A.positions32[ch.pos_off + id] = m;
 }
 
+// BasicEventHandler._time_slice_unit (abstracts.py:82-95): position[d] = (position[d] + v[d] * dt) % L.  For the
+// components of zero velocity this is p + 0.0 * dt then p % L, which returns p exactly for p in [0, L).
 __device__ inline void time_slice(const ChainDev &ch, WarpState &w, double q, double r) {
     double dt = time_sub(q, r, w.ts_q, w.ts_r);
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-        double v = k == w.direction ? ch.speed : 0.0;
-        w.pa[k] = py_mod_near(w.pa[k] + v * dt, ch.L);
-    }
+    const int d = w.direction;
+    w.pa[d] = py_mod_near(w.pa[d] + ch.speed * dt, ch.L);
     w.ts_q = q;
     w.ts_r = r;
 }
@@ -406,7 +465,7 @@ __device__ __noinline__ int commit(const RunArgs &A, const ChainDev &ch, const S
         separation64(ch, w.pa, pt, s);
         permute3(s, w.direction, p);
         double pp = ch.bound_prefactor * charge_of(A, ch, w.active) * charge_of(A, ch, best.target);
-        double bound = ipcb_x_derivative(pp, p[0], p[1], p[2]) * ch.speed;
+        double bound = mul_speed(ch, ipcb_x_derivative(pp, p[0], p[1], p[2]));
         int accepted;
         JF_TRY(thinning(A, ch, sp, w, best.target, bound, ev, accepted));
         rec.target = best.target;
@@ -419,7 +478,7 @@ __device__ __noinline__ int commit(const RunArgs &A, const ChainDev &ch, const S
         JF_TRY(cell_of(A.view, ch, w.pa, now_cell));
         if (now_cell != active_cell) return JFGPU_STATUS_ASSERTION;
         int accepted;
-        JF_TRY(thinning(A, ch, sp, w, best.target, best.rate * ch.speed, ev, accepted));
+        JF_TRY(thinning(A, ch, sp, w, best.target, mul_speed(ch, best.rate), ev, accepted));
         rec.target = best.target;
         rec.accepted = accepted;
         if (accepted) w.active = best.target;
@@ -472,25 +531,102 @@ __device__ __noinline__ int commit(const RunArgs &A, const ChainDev &ch, const S
 // ---------------------------------------------------------------------------------------------------------------
 // candidate enumeration
 // ---------------------------------------------------------------------------------------------------------------
+
+// base-K digits (x, y, z) of lane + 32 k, advanced by 32 without divisions (K >= 1; one carry per digit)
+struct Digits {
+    int x, y, z, sx, sy, sz, K;
+    __device__ inline void start(int lane, int base) {
+        K = base;
+        x = lane % K;
+        y = (lane / K) % K;
+        z = lane / (K * K);
+        sx = 32 % K;
+        sy = (32 / K) % K;
+        sz = 32 / (K * K);
+    }
+    __device__ inline void advance() {
+        x += sx;
+        y += sy;
+        z += sz;
+        if (x >= K) {
+            x -= K;
+            ++y;
+        }
+        if (y >= K) {
+            y -= K;
+            ++z;
+        }
+    }
+};
+
+// occupants of the nearby cells of the occupancy's active cell (ExcludedCellsTagger)
 template <typename F>
 __device__ inline void for_each_near(const RunArgs &A, const ChainDev &ch, int occ_cell, int lane, F &&f) {
     int a[3];
     cell_axes(ch, occ_cell, a);
     const int K = ch.n_res;
-    const int total = K * K * K;
     const int32_t *occ = A.occupancy + ch.occ_off;
-    for (int i = lane; i < total; i += 32) {
-        int ox = i % K, oy = (i / K) % K, oz = i / (K * K);
-        int cx = a[0] + ch.res[ox], cy = a[1] + ch.res[oy], cz = a[2] + ch.res[oz];
+    Digits g;
+    g.start(lane, K);
+    for (; g.z < K; g.advance()) {
+        int cx = a[0] + ch.res[g.x], cy = a[1] + ch.res[g.y], cz = a[2] + ch.res[g.z];
         if (cx >= ch.m) cx -= ch.m;
         if (cy >= ch.m) cy -= ch.m;
         if (cz >= ch.m) cz -= ch.m;
-        int cell = cx + ch.m * (cy + ch.m * cz);
+        const int cell = cx + ch.m * (cy + ch.m * cz);
         for (int k = 0; k < ch.max_occ; ++k) {
             int j = occ[(long long)cell * ch.max_occ + k];
             if (j >= 0) f(j);
         }
     }
+}
+
+// occupants of the cells that are not nearby (CellBoundingPotentialTagger), with their relative cell
+template <typename F>
+__device__ inline void for_each_far(const RunArgs &A, const ChainDev &ch, int occ_cell, int lane, F &&f) {
+    int a[3];
+    cell_axes(ch, occ_cell, a);
+    const int m = ch.m;
+    const int32_t *occ = A.occupancy + ch.occ_off;
+    const int16_t *rel = A.view.rel + ch.table_offset;
+    Digits g;
+    g.start(lane, m);
+    for (; g.z < m; g.advance()) {
+        const int cell = g.x + m * (g.y + m * g.z);
+        const int j = occ[cell];
+        if (j < 0) continue;
+        int dx = g.x - a[0], dy = g.y - a[1], dz = g.z - a[2];
+        if (dx < 0) dx += m;
+        if (dy < 0) dy += m;
+        if (dz < 0) dz += m;
+        if (((ch.near_mask >> dx) & 1ull) && ((ch.near_mask >> dy) & 1ull) && ((ch.near_mask >> dz) & 1ull)) continue;
+        int rc;
+        if (ch.rel_is_mod) {
+            rc = dx + m * (dy + m * dz);
+        } else {
+            rc = rel[g.x * m + a[0]] + m * (rel[g.y * m + a[1]] + m * rel[g.z * m + a[2]]);
+        }
+        f(j, cell, rc);
+    }
+}
+
+// sparse warp argmin: only lanes holding a candidate take part (usually lane 0 and one or two others)
+__device__ inline Cand warp_argmin_sparse(const Cand &c) {
+    unsigned mask = __ballot_sync(kFull, c.kind != (1 << 30));
+    Cand acc = cand_none();
+    while (mask) {
+        int src = __ffs(mask) - 1;
+        mask &= mask - 1;
+        Cand o;
+        o.q = __shfl_sync(kFull, c.q, src);
+        o.r = __shfl_sync(kFull, c.r, src);
+        o.kind = __shfl_sync(kFull, c.kind, src);
+        o.target = __shfl_sync(kFull, c.target, src);
+        o.aux = __shfl_sync(kFull, c.aux, src);
+        o.rate = __shfl_sync(kFull, c.rate, src);
+        if (cand_better(o, acc)) acc = o;
+    }
+    return acc;
 }
 
 // the whole event in FP64 (all lanes); returns the winner in best
@@ -512,13 +648,10 @@ __device__ inline int exact_candidates(const RunArgs &A, const ChainDev &ch, con
     }
     counted = warp_sum_int(count);
     if (ch.far == JFGPU_FAR_CELL_BOUNDING) {
-        const int32_t *occ = A.occupancy + ch.occ_off;
-        for (int c = lane; c < ch.ncells; c += 32) {
-            int j = occ[c];
-            if (j < 0 || is_nearby(ch, c, w.occ_cell)) continue;
-            int st = exact_cell_bounding(A, ch, sp, w, j, active_cell, ev, true, c, best);
+        for_each_far(A, ch, w.occ_cell, lane, [&](int j, int cell, int rc) {
+            int st = exact_cell_bounding(A, ch, sp, w, j, active_cell, ev, best);
             if (st) status = st;
-        }
+        });
     }
     if (lane == 0) {
         int st = single_candidates(A, ch, sp, w, active_cell, ev, best);
@@ -546,7 +679,18 @@ __device__ inline void topk_insert(float (&key)[kTopK], int (&code)[kTopK], floa
     }
 }
 
-// mixed precision: FP32 screening, FP64 refinement; returns 1 when the event must be re-solved in FP64
+__device__ inline float lane_min_unflagged(const float (&key)[kTopK]) {
+    float v = kInf32;
+#pragma unroll
+    for (int i = 0; i < kTopK; ++i)
+        if (key[i] >= 0.0f) v = fminf(v, key[i]);
+    return v;
+}
+
+// Mixed precision: FP32 screening, FP64 refinement; returns 1 when the event must be re-solved in FP64.
+// Order: nearby and surplus candidates, the exact single candidates, a first threshold, then the far field with a
+// rigorous early rejection (-log(1 - u) >= u: a far time is at least u / (beta rate speed)), the final threshold,
+// and the FP64 re-solve of the candidates inside it.
 __device__ inline int mixed_candidates(const RunArgs &A, const ChainDev &ch, const SpeciesDev &sp, const LJ32 &lj32,
                                        const WarpState &w, int active_cell, int lane, Cand &best, int &status,
                                        int &counted, int &refined) {
@@ -555,6 +699,8 @@ __device__ inline int mixed_candidates(const RunArgs &A, const ChainDev &ch, con
     const float speed32 = (float)ch.speed;
     const float beta32 = (float)ch.beta;
     const float margin = ch.ulp_margin32;
+    const float rel = 1.0f + 1.0f / 1024.0f;
+    const float abs_margin = ch.screen_abs32 / speed32;
     float key[kTopK];
     int code[kTopK];
 #pragma unroll
@@ -563,59 +709,57 @@ __device__ inline int mixed_candidates(const RunArgs &A, const ChainDev &ch, con
         code[i] = -1;
     }
     const float4 pa32 = make_float4((float)w.pa[0], (float)w.pa[1], (float)w.pa[2], 0.0f);
+    const uint64_t pair_base = draw_base(ch.key, (uint64_t)ev, kRngPair);
     // codes: bit 30 marks a far (cell-bounding) candidate, the low bits carry the target
     int count = 0;
     auto screen_pair = [&](int j) {
         ++count;
         float4 pj = A.positions32[ch.pos_off + j];
-        float s[3];
+        float sv[3];
         bool flag = false;
-        separation32(pa32, pj, ch.L32, ch.half32, margin, s, flag);
+        separation32(pa32, pj, ch.L32, ch.half32, margin, sv, flag);
         float t;
         if (ch.potential == JFGPU_POT_HARD_SPHERE) {
-            t = hs_screen((float)ch.diameter_sq, d, speed32, s, margin, flag);
+            t = hs_screen((float)ch.diameter_sq, d, speed32, sv, margin, flag);
         } else {
-            float du = expovariate32(draw(ch.key, (uint64_t)ev, kRngPair, (uint32_t)j), beta32, flag);
-            t = lj_screen(lj32, d, speed32, s, du, margin, flag);
+            float du = expovariate32(draw_at(pair_base, (uint32_t)j), beta32, flag);
+            t = lj_screen(lj32, d, speed32, sv, du, margin, flag);
         }
         if (flag) t = -1.0f;
         if (!isinf(t)) topk_insert(key, code, t, j);
     };
     for_each_near(A, ch, w.occ_cell, lane, screen_pair);
     for (int i = lane; i < w.n_surplus; i += 32) screen_pair(A.surplus[ch.pos_off + i]);
-    if (ch.far == JFGPU_FAR_CELL_BOUNDING) {
-        const int32_t *occ = A.occupancy + ch.occ_off;
-        for (int c = lane; c < ch.ncells; c += 32) {
-            int j = occ[c];
-            if (j < 0 || is_nearby(ch, c, w.occ_cell)) continue;
-            int rc = relative_cell(A.view, ch, c, active_cell);
-            float rate = sp.bound_upper32[rc * 3 + d];
-            bool flag = false;
-            float du = expovariate32(draw(ch.key, (uint64_t)ev, kRngPair, (uint32_t)j), beta32, flag);
-            float t = rate > 0.0f ? (du / rate) / speed32 : kInf32;
-            if (flag) t = -1.0f;
-            if (!isinf(t)) topk_insert(key, code, t, j | (1 << 30));
-        }
-    }
     // exact single candidates (lane 0) bound the threshold too
     Cand single = cand_none();
     int st = JFGPU_STATUS_OK;
     if (lane == 0) st = single_candidates(A, ch, sp, w, active_cell, ev, single);
     status = warp_max_int(st);
-    // smallest unflagged FP32 time (flagged entries carry the key -1 and are always refined)
-    float lane_min = kInf32;
-#pragma unroll
-    for (int i = 0; i < kTopK; ++i)
-        if (key[i] >= 0.0f) lane_min = fminf(lane_min, key[i]);
-    float t_min = warp_min_float(lane_min);
     double single_dt = kInf;
     if (lane == 0 && !isinf(single.q)) single_dt = time_sub(single.q, single.r, w.ts_q, w.ts_r);
-    single_dt = __shfl_sync(kFull, single_dt, 0);
-    float t_single = (float)single_dt;
-    float base = fminf(t_min, t_single);
-    float threshold = isinf(base) ? kInf32 : base * (1.0f + 1.0f / 1024.0f) + ch.screen_abs32 / speed32;
+    const float t_single = (float)__shfl_sync(kFull, single_dt, 0);
+    float base = fminf(warp_min_float(lane_min_unflagged(key)), t_single);
+    if (ch.far == JFGPU_FAR_CELL_BOUNDING) {
+        const float threshold0 = isinf(base) ? kInf32 : base * rel + abs_margin;
+        const float reject = threshold0 * beta32 * speed32 * (1.0f + 1.0f / 65536.0f);
+        const float *rates = sp.bound_upper32;
+        for_each_far(A, ch, w.occ_cell, lane, [&](int j, int cell, int rc) {
+            const float rate = rates[rc * 3 + d];
+            if (!(rate > 0.0f)) return;
+            const uint64_t bits = draw_at(pair_base, (uint32_t)j);
+            const float u_low = (float)(uint32_t)(bits >> 40) * (1.0f / 16777216.0f);  // <= the 53-bit uniform
+            if (u_low > reject * rate) return;
+            bool flag = false;
+            const float du = expovariate32(bits, beta32, flag);
+            float t = (du / rate) / speed32;
+            if (flag) t = -1.0f;
+            if (!isinf(t)) topk_insert(key, code, t, j | (1 << 30));
+        });
+        base = fminf(base, warp_min_float(lane_min_unflagged(key)));
+    }
+    const float threshold = isinf(base) ? kInf32 : base * rel + abs_margin;
     // refinement of the candidates inside the threshold
-    int overflow = (key[kTopK - 1] <= threshold) ? 1 : 0;
+    const int overflow = (key[kTopK - 1] <= threshold) ? 1 : 0;
     best = single;
     int rst = JFGPU_STATUS_OK;
     int nref = 0;
@@ -623,26 +767,25 @@ __device__ inline int mixed_candidates(const RunArgs &A, const ChainDev &ch, con
     for (int i = 0; i < kTopK; ++i) {
         if (code[i] >= 0 && key[i] <= threshold) {
             ++nref;
-            int j = code[i] & ((1 << 30) - 1);
-            int s2;
-            if (code[i] & (1 << 30)) {
-                int c = -1;
-                s2 = exact_cell_bounding(A, ch, sp, w, j, active_cell, ev, true, c, best);
-            } else {
-                s2 = exact_pair(A, ch, sp, w, j, ev, best);
-            }
+            const int j = code[i] & ((1 << 30) - 1);
+            const int s2 = (code[i] & (1 << 30)) ? exact_cell_bounding(A, ch, sp, w, j, active_cell, ev, best)
+                                                 : exact_pair(A, ch, sp, w, j, ev, best);
             if (s2) rst = s2;
         }
     }
     status = max(status, warp_max_int(rst));
-    best = warp_argmin(best);
+    best = warp_argmin_sparse(best);
     counted = warp_sum_int(count);
     refined = warp_sum_int(nref);
     return warp_max_int(overflow);
 }
 
+#ifndef JF_CHAIN_MIN_BLOCKS
+#define JF_CHAIN_MIN_BLOCKS 1
+#endif
+
 template <int MODE>
-__global__ void __launch_bounds__(256) chains_kernel(RunArgs A) {
+__global__ void __launch_bounds__(256, JF_CHAIN_MIN_BLOCKS) chains_kernel(RunArgs A) {
     extern __shared__ unsigned char smem_raw[];
     WarpState *shared = reinterpret_cast<WarpState *>(smem_raw);
     const int warp = threadIdx.x >> 5;

@@ -452,14 +452,31 @@ struct MH {
     double power, inverse_power;
 };
 
-__device__ inline int mh_potential(const MH &h, const double *s, double &out) {
-    if (h.kind == 0) {
+// Lennard-Jones potential six.potential(1, s) + twelve.potential(1, s) (lennard_jones_potential.py:83-98,
+// inverse_power_potential.py:127-143): k sigma^6 / |s|^6 terms from norm_sq ** 3.0 and norm_sq ** 6.0, both
+// correctly rounded from one double-double cube
+__device__ inline int lj_potential(const MH &h, const double *s, double &out) {
+    double ns = norm_sq3(s);
+    if (!(ns > 0.0) || isinf(ns)) {
         double a, b;
         JF_TRY(ip_potential(h.six, 1.0, s, a));
         JF_TRY(ip_potential(h.twelve, 1.0, s, b));
         out = a + b;
         return JFGPU_STATUS_OK;
     }
+    DD n3 = dd_ipow(ns, 3);
+    DD n6 = dd_mul(n3, n3);
+    double p3 = n3.hi + n3.lo;
+    double p6 = n6.hi + n6.lo;
+    double a, b;
+    JF_DIV(1.0 * h.six.prefactor, p3, a);
+    JF_DIV(1.0 * h.twelve.prefactor, p6, b);
+    out = a + b;
+    return JFGPU_STATUS_OK;
+}
+
+__device__ inline int mh_potential(const MH &h, const double *s, double &out) {
+    if (h.kind == 0) return lj_potential(h, s, out);
     double powered;
     JF_TRY(py_pow(norm3(s) - h.r0, h.power, powered));
     out = h.prefactor * powered;
@@ -576,14 +593,32 @@ __device__ inline int mh_std_displacement(const MH &h, int d, double *s, double 
     return mh_behind_inside(h, d, u, du, s, out);
 }
 
-__device__ inline int mh_std_derivative(const MH &h, int d, const double *s, double &out) {
-    if (h.kind == 0) {  // lennard_jones_potential.py:63-81
+// Lennard-Jones space derivative (lennard_jones_potential.py:63-81 with inverse_power_potential.py:71-94):
+// norm ** 8 and norm ** 14 correctly rounded from shared double-double powers
+__device__ inline int lj_std_derivative(const MH &h, int d, const double *s, double &out) {
+    double n = norm3(s);
+    if (!(n > 0.0) || isinf(n)) {
         double a, b;
         JF_TRY(ip_std_derivative(h.six, d, s, 1.0, 1.0, a));
         JF_TRY(ip_std_derivative(h.twelve, d, s, 1.0, 1.0, b));
         out = a + b;
         return JFGPU_STATUS_OK;
     }
+    DD n2 = dd_mul(DD{n, 0.0}, DD{n, 0.0});
+    DD n4 = dd_mul(n2, n2);
+    DD n8 = dd_mul(n4, n4);
+    DD n14 = dd_mul(dd_mul(n8, n4), n2);
+    double p8 = n8.hi + n8.lo;
+    double p14 = n14.hi + n14.lo;
+    double a, b;
+    JF_DIV(h.six.power * s[d], p8, a);
+    JF_DIV(h.twelve.power * s[d], p14, b);
+    out = ((a * h.six.prefactor) * 1.0) * 1.0 + ((b * h.twelve.prefactor) * 1.0) * 1.0;
+    return JFGPU_STATUS_OK;
+}
+
+__device__ inline int mh_std_derivative(const MH &h, int d, const double *s, double &out) {
+    if (h.kind == 0) return lj_std_derivative(h, d, s, out);
     double norm = norm3(s);  // displaced_even_power_potential.py:73-93
     double powered;
     JF_TRY(py_pow(norm - h.r0, h.power - 1.0, powered));

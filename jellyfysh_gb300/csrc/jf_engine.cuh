@@ -41,6 +41,8 @@ struct ChainDev {
     int32_t initial_active, initial_direction;
     int32_t geom_offset;         // into cell_min / cell_max pools (m entries)
     int32_t table_offset;        // into rel / tra pools (m * m entries)
+    int32_t rel_is_mod;          // rel[a][b] == (a - b) mod m and tra[a][b] == (a + b) mod m for every a, b
+    int32_t pad0;
     int32_t res[16];             // distinct residues of the neighbour-layer offsets modulo m (n_res of them)
     uint64_t near_mask;          // bit r set when residue r is within the neighbour layers
     int64_t pos_off, occ_off;

@@ -430,6 +430,7 @@ int jfgpu_engine_create(const JfgpuChainDesc *chains, int64_t n_chains, void *st
     std::vector<double> cmin_pool, cmax_pool;
     std::vector<int16_t> rel_pool, tra_pool;
     std::map<std::pair<double, int>, std::pair<int, int>> geometry;  // (L, m) -> (geom offset, table offset)
+    std::map<std::pair<double, int>, int> geometry_mod;                // (L, m) -> tables are modular arithmetic
     std::map<SpeciesKey, int> species_index;
     int error = JFGPU_OK;
     for (int64_t c = 0; c < n_chains && !error; ++c) {
@@ -459,7 +460,14 @@ int jfgpu_engine_create(const JfgpuChainDesc *chains, int64_t n_chains, void *st
                     rel_pool.push_back((int16_t)(long long)(py_mod(center - lo[b], d.system_length) / side));
                     tra_pool.push_back((int16_t)(long long)(py_mod(center + lo[b], d.system_length) / side));
                 }
+            int is_mod = 1;
+            for (int a = 0; a < m; ++a)
+                for (int b = 0; b < m; ++b) {
+                    if (rel_pool[toff + a * m + b] != ((a - b) % m + m) % m) is_mod = 0;
+                    if (tra_pool[toff + a * m + b] != (a + b) % m) is_mod = 0;
+                }
             geometry[gkey] = std::make_pair(goff, toff);
+            geometry_mod[gkey] = is_mod;
         }
         std::vector<unsigned char> near_axis(m, 0);
         for (int o = -d.neighbor_layers; o <= d.neighbor_layers; ++o) near_axis[((o % m) + m) % m] = 1;
@@ -475,6 +483,7 @@ int jfgpu_engine_create(const JfgpuChainDesc *chains, int64_t n_chains, void *st
         ch.initial_direction = d.initial_direction;
         ch.geom_offset = geometry[gkey].first;
         ch.table_offset = geometry[gkey].second;
+        ch.rel_is_mod = geometry_mod[gkey];
         ch.n_res = 0;
         ch.near_mask = 0;
         for (int r = 0; r < m; ++r)

@@ -95,6 +95,8 @@ def lib() -> ctypes.CDLL:
         handle.jfo_chain_positions.argtypes = [ctypes.c_void_p, _PD]
         handle.jfo_chain_state.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int64),
                                            ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int), _PD, _PD]
+        handle.jfo_chain_occupancy.restype = ctypes.c_int
+        handle.jfo_chain_occupancy.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int32)]
         handle.jfo_chain_bounds.restype = ctypes.c_int
         handle.jfo_chain_bounds.argtypes = [ctypes.c_void_p, _PD, ctypes.c_int]
         handle.jfo_chain_walker.restype = ctypes.c_int
@@ -283,6 +285,12 @@ class Chain:
                               ctypes.byref(q), ctypes.byref(r))
         return dict(events=event.value, active=active.value, direction=direction.value, time_q=q.value,
                     time_r=r.value)
+
+    def occupancy(self):
+        """owner[i]: cell of particle i among the occupants, -2 - cell for a surplus unit, -1 for the active unit."""
+        owner = np.zeros(self.system.n, dtype=np.int32)
+        cell = lib().jfo_chain_occupancy(self._handle, owner.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)))
+        return owner, cell
 
     def bounds(self) -> np.ndarray:
         need = -lib().jfo_chain_bounds(self._handle, None, 0)

@@ -1685,3 +1685,15 @@ int jfo_chain_walker(const JfoChain *c, int direction, int which, int32_t *cells
     *total_rate = w->total_rate;
     return w->size;
 }
+
+/* occupancy snapshot for checks: owner[i] = cell of particle i in the occupants (>= 0), -2 - cell when it is a
+ * surplus unit, -1 when it is the occupancy's active unit; returns the occupancy's active cell */
+int jfo_chain_occupancy(const JfoChain *c, int32_t *owner) {
+    for (int i = 0; i < c->sys.n; ++i) owner[i] = -100;
+    for (int cell = 0; cell < c->ncells; ++cell) {
+        for (int k = 0; k < c->occ_count[cell]; ++k) owner[c->occ[cell * c->cap + k]] = cell;
+        for (int k = 0; k < c->sur_count[cell]; ++k) owner[c->sur[(size_t)cell * c->sys.n + k]] = -2 - cell;
+    }
+    if (c->occ_active >= 0) owner[c->occ_active] = -1;
+    return c->occ_cell;
+}

@@ -152,6 +152,7 @@ int64_t jfo_chain_run(JfoChain *chain, int64_t max_events, double stop_q, double
 void jfo_chain_positions(const JfoChain *chain, double *positions);
 void jfo_chain_state(const JfoChain *chain, int64_t *event_count, int *active, int *direction,
                      double *time_q, double *time_r);
+int jfo_chain_occupancy(const JfoChain *chain, int32_t *owner);
 int jfo_chain_bounds(const JfoChain *chain, double *bounds, int capacity);
 int jfo_chain_walker(const JfoChain *chain, int direction, int which, int32_t *cells, double *rates, int capacity,
                      double *total_rate);

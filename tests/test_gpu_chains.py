@@ -123,14 +123,15 @@ def test_random_hard_sphere_systems_against_oracle():
     rng = np.random.default_rng(21)
     specs, positions = [], []
     for c in range(12):
-        n = int(rng.integers(16, 120))
+        # boxes large enough that the nearby cells plus one cell fit in half the box (minimum image holds)
+        layers = 1 + c % 2
+        n = int(rng.integers(200, 600))
         eta = float(rng.uniform(0.1, 0.3))
         length = systems.hard_sphere_box(n, eta, radius=0.5)
-        layers = 1 + c % 2
-        m = max(3, int(length / (1.0 / layers)))
-        m = min(m, 24)
+        m = min(int(length * layers), 24)
         while length / m * layers < 1.0:
             m -= 1
+        assert (layers + 1) * length / m <= length / 2
         specs.append(ChainSpec(n=n, system_length=length, cells_per_side=m, neighbor_layers=layers,
                                max_occupants=1 + c % 3, hs_radius=0.5, chain_time=0.4 * length,
                                initial_active=int(rng.integers(n)), initial_direction=int(rng.integers(3))))
