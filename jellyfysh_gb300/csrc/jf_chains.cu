@@ -254,10 +254,18 @@ __device__ __noinline__ int exact_pair_coulomb(const RunArgs &A, const ChainDev 
     return JFGPU_STATUS_OK;
 }
 
+// potential and far field of a chain: compile-time constants of a specialised kernel, else read from the chain
+template <int POT>
+__device__ inline int potential_of(const ChainDev &ch) { return POT >= 0 ? POT : ch.potential; }
+template <int FAR>
+__device__ inline int far_of(const ChainDev &ch) { return FAR >= 0 ? FAR : ch.far; }
+
+template <int POT>
 __device__ inline int exact_pair(const RunArgs &A, const ChainDev &ch, const SpeciesDev &sp, const WarpState &w,
                                  int j, long long ev, Cand &best) {
-    if (ch.potential == JFGPU_POT_HARD_SPHERE) return exact_pair_hs(A, ch, w, j, best);
-    if (ch.potential == JFGPU_POT_LENNARD_JONES) return exact_pair_lj(A, ch, sp, w, j, ev, best);
+    const int pot = potential_of<POT>(ch);
+    if (pot == JFGPU_POT_HARD_SPHERE) return exact_pair_hs(A, ch, w, j, best);
+    if (pot == JFGPU_POT_LENNARD_JONES) return exact_pair_lj(A, ch, sp, w, j, ev, best);
     return exact_pair_coulomb(A, ch, w, j, ev, best);
 }
 
@@ -630,6 +638,7 @@ __device__ inline Cand warp_argmin_sparse(const Cand &c) {
 }
 
 // the whole event in FP64 (all lanes); returns the winner in best
+template <int POT, int FAR>
 __device__ inline int exact_candidates(const RunArgs &A, const ChainDev &ch, const SpeciesDev &sp, const WarpState &w,
                                        int active_cell, int lane, Cand &best, int &counted) {
     const long long ev = w.events;
@@ -637,17 +646,17 @@ __device__ inline int exact_candidates(const RunArgs &A, const ChainDev &ch, con
     int count = 0;
     best = cand_none();
     for_each_near(A, ch, w.occ_cell, lane, [&](int j) {
-        int st = exact_pair(A, ch, sp, w, j, ev, best);
+        int st = exact_pair<POT>(A, ch, sp, w, j, ev, best);
         if (st) status = st;
         ++count;
     });
     for (int i = lane; i < w.n_surplus; i += 32) {
-        int st = exact_pair(A, ch, sp, w, A.surplus[ch.pos_off + i], ev, best);
+        int st = exact_pair<POT>(A, ch, sp, w, A.surplus[ch.pos_off + i], ev, best);
         if (st) status = st;
         ++count;
     }
     counted = warp_sum_int(count);
-    if (ch.far == JFGPU_FAR_CELL_BOUNDING) {
+    if (far_of<FAR>(ch) == JFGPU_FAR_CELL_BOUNDING) {
         for_each_far(A, ch, w.occ_cell, lane, [&](int j, int cell, int rc) {
             int st = exact_cell_bounding(A, ch, sp, w, j, active_cell, ev, best);
             if (st) status = st;
@@ -691,6 +700,7 @@ __device__ inline float lane_min_unflagged(const float (&key)[kTopK]) {
 // Order: nearby and surplus candidates, the exact single candidates, a first threshold, then the far field with a
 // rigorous early rejection (-log(1 - u) >= u: a far time is at least u / (beta rate speed)), the final threshold,
 // and the FP64 re-solve of the candidates inside it.
+template <int POT, int FAR>
 __device__ inline int mixed_candidates(const RunArgs &A, const ChainDev &ch, const SpeciesDev &sp, const LJ32 &lj32,
                                        const WarpState &w, int active_cell, int lane, Cand &best, int &status,
                                        int &counted, int &refined) {
@@ -719,7 +729,7 @@ __device__ inline int mixed_candidates(const RunArgs &A, const ChainDev &ch, con
         bool flag = false;
         separation32(pa32, pj, ch.L32, ch.half32, margin, sv, flag);
         float t;
-        if (ch.potential == JFGPU_POT_HARD_SPHERE) {
+        if (potential_of<POT>(ch) == JFGPU_POT_HARD_SPHERE) {
             t = hs_screen((float)ch.diameter_sq, d, speed32, sv, margin, flag);
         } else {
             float du = expovariate32(draw_at(pair_base, (uint32_t)j), beta32, flag);
@@ -739,7 +749,7 @@ __device__ inline int mixed_candidates(const RunArgs &A, const ChainDev &ch, con
     if (lane == 0 && !isinf(single.q)) single_dt = time_sub(single.q, single.r, w.ts_q, w.ts_r);
     const float t_single = (float)__shfl_sync(kFull, single_dt, 0);
     float base = fminf(warp_min_float(lane_min_unflagged(key)), t_single);
-    if (ch.far == JFGPU_FAR_CELL_BOUNDING) {
+    if (far_of<FAR>(ch) == JFGPU_FAR_CELL_BOUNDING) {
         const float threshold0 = isinf(base) ? kInf32 : base * rel + abs_margin;
         const float reject = threshold0 * beta32 * speed32 * (1.0f + 1.0f / 65536.0f);
         const float *rates = sp.bound_upper32;
@@ -769,7 +779,7 @@ __device__ inline int mixed_candidates(const RunArgs &A, const ChainDev &ch, con
             ++nref;
             const int j = code[i] & ((1 << 30) - 1);
             const int s2 = (code[i] & (1 << 30)) ? exact_cell_bounding(A, ch, sp, w, j, active_cell, ev, best)
-                                                 : exact_pair(A, ch, sp, w, j, ev, best);
+                                                 : exact_pair<POT>(A, ch, sp, w, j, ev, best);
             if (s2) rst = s2;
         }
     }
@@ -781,10 +791,10 @@ __device__ inline int mixed_candidates(const RunArgs &A, const ChainDev &ch, con
 }
 
 #ifndef JF_CHAIN_MIN_BLOCKS
-#define JF_CHAIN_MIN_BLOCKS 1
+#define JF_CHAIN_MIN_BLOCKS 2
 #endif
 
-template <int MODE>
+template <int MODE, int POT, int FAR>
 __global__ void __launch_bounds__(256, JF_CHAIN_MIN_BLOCKS) chains_kernel(RunArgs A) {
     extern __shared__ unsigned char smem_raw[];
     WarpState *shared = reinterpret_cast<WarpState *>(smem_raw);
@@ -839,15 +849,16 @@ __global__ void __launch_bounds__(256, JF_CHAIN_MIN_BLOCKS) chains_kernel(RunArg
         Cand best;
         int status = JFGPU_STATUS_OK;
         int counted = 0, refined = 0;
-        if (MODE == JFGPU_MODE_MIXED && ch.potential != JFGPU_POT_COULOMB) {
-            int fallback = mixed_candidates(A, ch, sp, lj32, w, active_cell, lane, best, status, counted, refined);
+        if (MODE == JFGPU_MODE_MIXED && potential_of<POT>(ch) != JFGPU_POT_COULOMB) {
+            int fallback =
+                mixed_candidates<POT, FAR>(A, ch, sp, lj32, w, active_cell, lane, best, status, counted, refined);
             if (fallback && status == JFGPU_STATUS_OK) {
                 int recount = 0;
-                status = exact_candidates(A, ch, sp, w, active_cell, lane, best, recount);
+                status = exact_candidates<POT, FAR>(A, ch, sp, w, active_cell, lane, best, recount);
                 if (lane == 0) w.fallbacks += 1;
             }
         } else {
-            status = exact_candidates(A, ch, sp, w, active_cell, lane, best, counted);
+            status = exact_candidates<POT, FAR>(A, ch, sp, w, active_cell, lane, best, counted);
         }
         __syncwarp();
         if (lane == 0) {
@@ -964,7 +975,8 @@ cudaError_t launch_init(const EngineView &view, long long n_chains, const JfgpuB
 
 cudaError_t launch_run(const EngineView &view, const JfgpuBuffers &b, long long first, long long count,
                        long long max_events, double stop_q, double stop_r, int mode, JfgpuEvent *log,
-                       long long log_capacity, int warps_per_block, cudaStream_t stream) {
+                       long long log_capacity, int warps_per_block, int uniform_potential, int uniform_far,
+                       cudaStream_t stream) {
     RunArgs A;
     A.view = view;
     A.positions = b.positions;
@@ -987,10 +999,19 @@ cudaError_t launch_run(const EngineView &view, const JfgpuBuffers &b, long long 
     if (count < warps) warps = (int)count;
     long long blocks = (count + warps - 1) / warps;
     size_t smem = sizeof(WarpState) * warps;
+    const dim3 grid((unsigned)blocks), block(warps * 32);
     if (mode == JFGPU_MODE_MIXED) {
-        chains_kernel<JFGPU_MODE_MIXED><<<(unsigned)blocks, warps * 32, smem, stream>>>(A);
+        // kernels specialised for the common homogeneous batches carry only their potential's code
+        if (uniform_potential == JFGPU_POT_LENNARD_JONES && uniform_far == JFGPU_FAR_CELL_BOUNDING)
+            chains_kernel<JFGPU_MODE_MIXED, JFGPU_POT_LENNARD_JONES, JFGPU_FAR_CELL_BOUNDING><<<grid, block, smem, stream>>>(A);
+        else if (uniform_potential == JFGPU_POT_LENNARD_JONES && uniform_far == JFGPU_FAR_CELL_VETO)
+            chains_kernel<JFGPU_MODE_MIXED, JFGPU_POT_LENNARD_JONES, JFGPU_FAR_CELL_VETO><<<grid, block, smem, stream>>>(A);
+        else if (uniform_potential == JFGPU_POT_HARD_SPHERE && uniform_far == JFGPU_FAR_NONE)
+            chains_kernel<JFGPU_MODE_MIXED, JFGPU_POT_HARD_SPHERE, JFGPU_FAR_NONE><<<grid, block, smem, stream>>>(A);
+        else
+            chains_kernel<JFGPU_MODE_MIXED, -1, -1><<<grid, block, smem, stream>>>(A);
     } else {
-        chains_kernel<JFGPU_MODE_EXACT><<<(unsigned)blocks, warps * 32, smem, stream>>>(A);
+        chains_kernel<JFGPU_MODE_EXACT, -1, -1><<<grid, block, smem, stream>>>(A);
     }
     return cudaGetLastError();
 }

@@ -24,7 +24,8 @@ namespace jf {
 cudaError_t launch_init(const EngineView &view, long long n_chains, const JfgpuBuffers &b, cudaStream_t stream);
 cudaError_t launch_run(const EngineView &view, const JfgpuBuffers &b, long long first, long long count,
                        long long max_events, double stop_q, double stop_r, int mode, JfgpuEvent *log,
-                       long long log_capacity, int warps_per_block, cudaStream_t stream);
+                       long long log_capacity, int warps_per_block, int uniform_potential, int uniform_far,
+                       cudaStream_t stream);
 }  // namespace jf
 
 using namespace jf;
@@ -600,8 +601,11 @@ int jfgpu_chains_run(JfgpuEngine *e, const JfgpuBuffers *b, int64_t first, int64
         (mode != JFGPU_MODE_EXACT && mode != JFGPU_MODE_MIXED) || (log && log_capacity <= 0))
         return JFGPU_ERROR_ARGUMENT;
     if (count == 0 || max_events == 0) return JFGPU_OK;
+    int potential = e->chains[first].potential, far = e->chains[first].far;
+    for (int64_t c = first + 1; c < first + count && potential >= 0; ++c)
+        if (e->chains[c].potential != potential || e->chains[c].far != far) potential = far = -1;
     cudaError_t err = launch_run(e->view, *b, first, count, max_events, stop_q, stop_r, mode, log, log_capacity,
-                                 e->block_warps, static_cast<cudaStream_t>(stream_ptr));
+                                 e->block_warps, potential, far, static_cast<cudaStream_t>(stream_ptr));
     e->launches += 1;
     return err == cudaSuccess ? JFGPU_OK : JFGPU_ERROR_CUDA;
 }
