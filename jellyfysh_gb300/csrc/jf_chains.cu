@@ -791,7 +791,7 @@ __device__ inline int mixed_candidates(const RunArgs &A, const ChainDev &ch, con
 }
 
 #ifndef JF_CHAIN_MIN_BLOCKS
-#define JF_CHAIN_MIN_BLOCKS 2
+#define JF_CHAIN_MIN_BLOCKS 4
 #endif
 
 template <int MODE, int POT, int FAR>
