@@ -113,6 +113,19 @@ int jfgpu_merged_image_coulomb_derivative(double alpha, int32_t fourier_cutoff, 
                                           double prefactor, double system_length, const double *velocity,
                                           const double *separation, const double *charges, int64_t n,
                                           double *out, int32_t *status, void *stream);
+/* The same derivative for callers that cannot allocate device memory (no counterpart in the reference, whose
+ * C extension keeps its table in host memory).  jfgpu_merged_image_coulomb_derivative allocates its
+ * Fourier-coefficient table on every call; callers issuing work while a stream is captured into a CUDA graph,
+ * hosts that must not enter the CUDA allocator while running, and plug-ins inside another framework's memory pool
+ * cannot.  This entry point keeps the table in a fixed file-scope device array (32 KiB, held by every GPU that loads
+ * the library until the process exits) and calls no allocation routine.  Limit: fourier_cutoff <= 15, larger
+ * values return JFGPU_ERROR_ARGUMENT.  Its first call on a device looks up the array's device address with that
+ * device current; make that first call before any stream capture.  Every call shares the array and rewrites it:
+ * calls that overlap on the GPU (different streams without ordering) race. */
+int jfgpu_merged_image_coulomb_derivative_noalloc(double alpha, int32_t fourier_cutoff, int32_t position_cutoff,
+                                                  double prefactor, double system_length, const double *velocity,
+                                                  const double *separation, const double *charges, int64_t n,
+                                                  double *out, int32_t *status, void *stream);
 /* CellBoundingPotential.displacement: potential_change / rate, rate = bounds[cell_separation][direction]
  * (times the charge correction factor; the lower bound when that factor is not positive). bounds_upper and
  * bounds_lower are device arrays [cells][3]; cell_separation, direction device arrays [n]; charge_factor [n]. */

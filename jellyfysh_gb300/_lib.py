@@ -95,6 +95,8 @@ SIGNATURES = {
     "jfgpu_coulomb_bound_derivative": (ctypes.c_int, [_D, _P, _P, _P, _I64, _P, _P, _P]),
     "jfgpu_merged_image_coulomb_derivative": (ctypes.c_int, [_D, _I32, _I32, _D, _D, _P, _P, _P, _I64, _P, _P,
                                                              _P]),
+    "jfgpu_merged_image_coulomb_derivative_noalloc": (ctypes.c_int, [_D, _I32, _I32, _D, _D, _P, _P, _P, _I64,
+                                                                     _P, _P, _P]),
     "jfgpu_cell_bounding_displacement": (ctypes.c_int, [_P, _P, _P, _P, _P, _P, _P, _I64, _P, _P, _P]),
     "jfgpu_engine_create": (ctypes.c_int, [_P, _I64, _P, ctypes.POINTER(ctypes.c_void_p)]),
     "jfgpu_engine_destroy": (None, [_P]),

@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <cmath>
+#include <mutex>
 
 #include "jf_engine.cuh"
 
@@ -324,3 +325,91 @@ int jfgpu_cell_bounding_displacement(const double *bounds_upper, const double *b
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------------------------------------------
+// The merged-image Coulomb derivative for callers that cannot allocate device memory.
+//
+// jfgpu_merged_image_coulomb_derivative allocates its Fourier-coefficient table with cudaMallocAsync on every call.
+// Some callers cannot do that: code that issues work while a stream is being captured into a CUDA graph, hosts that
+// must not enter the CUDA allocator once they are running (real-time loops, embedded controllers with a fixed memory
+// budget), and plug-ins that live inside another framework whose memory pool owns the device.  For them the table
+// lives in the file-scope device array below, of a fixed maximum size, which every GPU that loads this library keeps
+// until the process exits.  The caller still passes every input and output array.
+// ---------------------------------------------------------------------------------------------------------------
+namespace {
+
+constexpr int kNoAllocMaxFourierCutoff = 15;  // (15 + 1)^3 doubles = 32 KiB
+constexpr int kNoAllocSide = kNoAllocMaxFourierCutoff + 1;
+constexpr int kNoAllocEntries = kNoAllocSide * kNoAllocSide * kNoAllocSide;
+
+__device__ __align__(256) double g_merged_image_fourier[kNoAllocEntries];
+
+std::mutex g_fourier_mutex;
+double *g_fourier_address[128] = {};  // device address of the array, per device ordinal
+
+// In host code the array's name only stands for the symbol: the device address is looked up once per device,
+// with that device current, and cached.
+int fourier_scratch(double **address) {
+    int device = -1;
+    if (cudaGetDevice(&device) != cudaSuccess || device < 0 || device >= 128) return JFGPU_ERROR_CUDA;
+    std::lock_guard<std::mutex> lock(g_fourier_mutex);
+    if (!g_fourier_address[device]) {
+        void *ptr = nullptr;
+        if (cudaGetSymbolAddress(&ptr, g_merged_image_fourier) != cudaSuccess || ptr == nullptr)
+            return JFGPU_ERROR_CUDA;
+        g_fourier_address[device] = static_cast<double *>(ptr);
+    }
+    *address = g_fourier_address[device];
+    return JFGPU_OK;
+}
+
+}  // namespace
+
+extern "C" int jfgpu_merged_image_coulomb_derivative_noalloc(double alpha, int32_t fourier_cutoff,
+                                                             int32_t position_cutoff, double prefactor,
+                                                             double system_length, const double *velocity,
+                                                             const double *separation, const double *charges,
+                                                             int64_t n, double *out, int32_t *status, void *stream) {
+    if (!charges || !velocity || !separation || fourier_cutoff < 0 || position_cutoff < 0 || !(alpha > 0.0) ||
+        !(system_length > 0.0))
+        return JFGPU_ERROR_ARGUMENT;
+    if (fourier_cutoff > kNoAllocMaxFourierCutoff) return JFGPU_ERROR_ARGUMENT;  // beyond the fixed table
+    double *table = nullptr;
+    int error = fourier_scratch(&table);
+    if (error) return error;
+    // coefficients on the host with the host libm (merged_image_coulomb_potential.c:77-119); every entry of the
+    // table layout of this cutoff is written, the unused i = 0 plane as zeros, so nothing of an earlier call remains
+    const int nf = fourier_cutoff + 1;
+    const size_t count = (size_t)nf * nf * nf;
+    double host[kNoAllocEntries];
+    for (size_t e = 0; e < count; ++e) host[e] = 0.0;
+    for (int k = 0; k < nf; k++)
+        for (int j = 0; j < nf; j++)
+            for (int i = 1; i < nf; i++) {
+                double coefficient = (j == 0 && k == 0) ? 1.0 : ((k == 0 || j == 0) ? 2.0 : 4.0);
+                double norm_sq = i * i + j * j + k * k;
+                host[(i * nf + j) * nf + k] = 4.0 * i * coefficient / (norm_sq * system_length * system_length) *
+                                              std::exp(-M_PI * M_PI * norm_sq / (alpha * alpha));
+            }
+    // a copy from pageable memory waits for the stream's earlier work (the previous call's kernel) and returns
+    // once the host array has been staged, so the stack array may go out of scope afterwards
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    if (cudaMemcpyAsync(table, host, count * sizeof(double), cudaMemcpyHostToDevice, s) != cudaSuccess)
+        return JFGPU_ERROR_CUDA;
+    PotentialArgs a = base_args(kMergedDerivative, velocity, separation, n, out, status);
+    a.p0 = prefactor;
+    a.charges = charges;
+    MIC m;
+    m.fourier_cutoff = fourier_cutoff;
+    m.fourier_cutoff_sq = fourier_cutoff * fourier_cutoff;
+    m.position_cutoff = position_cutoff;
+    m.position_cutoff_sq = position_cutoff * position_cutoff;
+    m.alpha_over_length = alpha / system_length;
+    m.alpha_over_length_sq = alpha * alpha / (system_length * system_length);
+    m.two_alpha_over_length_root_pi = 2.0 * alpha / (system_length * std::sqrt(M_PI));
+    m.system_length = system_length;
+    m.two_pi_over_length = 2.0 * M_PI / system_length;
+    m.fourier = table;
+    a.mic = m;
+    return launch(a, stream);
+}
