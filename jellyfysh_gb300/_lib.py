@@ -69,7 +69,8 @@ class Event(ctypes.Structure):
 
 class Buffers(ctypes.Structure):
     _fields_ = [("positions", ctypes.c_void_p), ("positions32", ctypes.c_void_p), ("charges", ctypes.c_void_p),
-                ("occupancy", ctypes.c_void_p), ("surplus", ctypes.c_void_p), ("state", ctypes.c_void_p)]
+                ("occupancy", ctypes.c_void_p), ("surplus", ctypes.c_void_p), ("roles", ctypes.c_void_p),
+                ("state", ctypes.c_void_p)]
 
 
 class Layout(ctypes.Structure):

@@ -151,10 +151,12 @@ class ChainBatch:
         self.charges_dev = None if host_charges is None else t.from_numpy(host_charges).to(self.device)
         self.occupancy_dev = t.full((O,), -1, dtype=t.int32, device=self.device)
         self.surplus_dev = t.zeros((P,), dtype=t.int32, device=self.device)
+        self.roles_dev = t.zeros((P,), dtype=t.int32, device=self.device)
         self.state_dev = t.zeros((self.n_chains * STATE_DTYPE.itemsize,), dtype=t.uint8, device=self.device)
         self._buffers = _lib.Buffers(positions=_ptr(self.positions_dev), positions32=_ptr(self.positions32_dev),
                                      charges=_ptr(self.charges_dev), occupancy=_ptr(self.occupancy_dev),
-                                     surplus=_ptr(self.surplus_dev), state=_ptr(self.state_dev))
+                                     surplus=_ptr(self.surplus_dev), roles=_ptr(self.roles_dev),
+                                     state=_ptr(self.state_dev))
         with torch.cuda.device(self.device):
             _lib.check(self.lib.jfgpu_chains_init(self._engine, ctypes.byref(self._buffers), self._stream()),
                        "jfgpu_chains_init")
@@ -244,4 +246,5 @@ class ChainBatch:
 
     # ---- host <-> device state transfer (the end-to-end path of a caller holding host buffers) ----
     def state_tensors(self):
-        return [self.positions_dev, self.positions32_dev, self.occupancy_dev, self.surplus_dev, self.state_dev]
+        return [self.positions_dev, self.positions32_dev, self.occupancy_dev, self.surplus_dev, self.roles_dev,
+                self.state_dev]

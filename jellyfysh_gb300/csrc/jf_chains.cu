@@ -114,6 +114,7 @@ struct RunArgs {
     const double *charges;
     int32_t *occupancy;
     int32_t *surplus;
+    int32_t *roles;
     JfgpuChainState *state;
     JfgpuEvent *log;
     long long log_capacity;
@@ -326,14 +327,26 @@ __device__ __noinline__ int single_candidates(const RunArgs &A, const ChainDev &
 // ---------------------------------------------------------------------------------------------------------------
 // occupancy (lane 0)
 // ---------------------------------------------------------------------------------------------------------------
+// role word of a unit: the axes of its occupancy cell, bit 24 for a surplus unit, bit 25 for the active unit
+constexpr int32_t kRoleSurplus = 1 << 24;
+constexpr int32_t kRoleActive = 1 << 25;
+
+__device__ inline int32_t role_of_cell(const ChainDev &ch, int cell) {
+    int a[3];
+    cell_axes(ch, cell, a);
+    return a[0] | (a[1] << 8) | (a[2] << 16);
+}
+
 __device__ inline void occ_insert(const RunArgs &A, const ChainDev &ch, WarpState &w, int cell, int id) {
     int32_t *slots = A.occupancy + ch.occ_off + (long long)cell * ch.max_occ;
     for (int k = 0; k < ch.max_occ; ++k)
         if (slots[k] < 0) {
             slots[k] = id;
+            A.roles[ch.pos_off + id] = role_of_cell(ch, cell);
             return;
         }
     A.surplus[ch.pos_off + w.n_surplus] = id;
+    A.roles[ch.pos_off + id] = role_of_cell(ch, cell) | kRoleSurplus;
     w.n_surplus += 1;
 }
 
@@ -342,6 +355,7 @@ __device__ __noinline__ int occ_update(const RunArgs &A, const ChainDev &ch, War
         if (w.occ_active >= 0) occ_insert(A, ch, w, w.occ_cell, w.occ_active);
         JF_TRY(cell_of(A.view, ch, w.pa, w.occ_cell));
         w.occ_active = w.active;
+        A.roles[ch.pos_off + w.active] = kRoleActive;
         int32_t *slots = A.occupancy + ch.occ_off + (long long)w.occ_cell * ch.max_occ;
         for (int k = 0; k < ch.max_occ; ++k)
             if (slots[k] == w.active) {
@@ -618,6 +632,39 @@ __device__ inline void for_each_far(const RunArgs &A, const ChainDev &ch, int oc
     }
 }
 
+// Every non-active unit with its role (the cell-bounding far field makes every unit a candidate): surplus units and
+// occupants of nearby cells go to `near(j)`, occupants of the other cells to `far(j, rc)` with their relative cell.
+// The same partition as the taggers (ExcludedCellsTagger, SurplusCellsTagger, CellBoundingPotentialTagger), found by
+// one coalesced pass over the units instead of two passes over the cells.
+template <typename FN, typename FF>
+__device__ inline void for_each_unit(const RunArgs &A, const ChainDev &ch, int occ_cell, int lane, FN &&near, FF &&far) {
+    int a[3];
+    cell_axes(ch, occ_cell, a);
+    const int m = ch.m;
+    const int32_t *roles = A.roles + ch.pos_off;
+    const int16_t *rel = A.view.rel + ch.table_offset;
+    for (int j = lane; j < ch.n; j += 32) {
+        const int32_t role = roles[j];
+        if (role & kRoleActive) continue;
+        if (role & kRoleSurplus) {
+            near(j);
+            continue;
+        }
+        const int cx = role & 0xFF, cy = (role >> 8) & 0xFF, cz = (role >> 16) & 0xFF;
+        int dx = cx - a[0], dy = cy - a[1], dz = cz - a[2];
+        if (dx < 0) dx += m;
+        if (dy < 0) dy += m;
+        if (dz < 0) dz += m;
+        if (((ch.near_mask >> dx) & 1ull) && ((ch.near_mask >> dy) & 1ull) && ((ch.near_mask >> dz) & 1ull)) {
+            near(j);
+            continue;
+        }
+        const int rc = ch.rel_is_mod ? dx + m * (dy + m * dz)
+                                     : rel[cx * m + a[0]] + m * (rel[cy * m + a[1]] + m * rel[cz * m + a[2]]);
+        far(j, rc);
+    }
+}
+
 // sparse warp argmin: only lanes holding a candidate take part (usually lane 0 and one or two others)
 __device__ inline Cand warp_argmin_sparse(const Cand &c) {
     unsigned mask = __ballot_sync(kFull, c.kind != (1 << 30));
@@ -738,9 +785,7 @@ __device__ inline int mixed_candidates(const RunArgs &A, const ChainDev &ch, con
         if (flag) t = -1.0f;
         if (!isinf(t)) topk_insert(key, code, t, j);
     };
-    for_each_near(A, ch, w.occ_cell, lane, screen_pair);
-    for (int i = lane; i < w.n_surplus; i += 32) screen_pair(A.surplus[ch.pos_off + i]);
-    // exact single candidates (lane 0) bound the threshold too
+    // exact single candidates (lane 0) bound the threshold of the far field
     Cand single = cand_none();
     int st = JFGPU_STATUS_OK;
     if (lane == 0) st = single_candidates(A, ch, sp, w, active_cell, ev, single);
@@ -748,24 +793,40 @@ __device__ inline int mixed_candidates(const RunArgs &A, const ChainDev &ch, con
     double single_dt = kInf;
     if (lane == 0 && !isinf(single.q)) single_dt = time_sub(single.q, single.r, w.ts_q, w.ts_r);
     const float t_single = (float)__shfl_sync(kFull, single_dt, 0);
-    float base = fminf(warp_min_float(lane_min_unflagged(key)), t_single);
+    float base;
     if (far_of<FAR>(ch) == JFGPU_FAR_CELL_BOUNDING) {
-        const float threshold0 = isinf(base) ? kInf32 : base * rel + abs_margin;
-        const float reject = threshold0 * beta32 * speed32 * (1.0f + 1.0f / 65536.0f);
+        // one pass over the units: nearby and surplus units are screened, far units are rejected early against the
+        // running threshold of their lane (a lane's threshold only decreases, so a rejected unit is above the final
+        // threshold too)
         const float *rates = sp.bound_upper32;
-        for_each_far(A, ch, w.occ_cell, lane, [&](int j, int cell, int rc) {
-            const float rate = rates[rc * 3 + d];
-            if (!(rate > 0.0f)) return;
-            const uint64_t bits = draw_at(pair_base, (uint32_t)j);
-            const float u_low = (float)(uint32_t)(bits >> 40) * (1.0f / 16777216.0f);  // <= the 53-bit uniform
-            if (u_low > reject * rate) return;
-            bool flag = false;
-            const float du = expovariate32(bits, beta32, flag);
-            float t = (du / rate) / speed32;
-            if (flag) t = -1.0f;
-            if (!isinf(t)) topk_insert(key, code, t, j | (1 << 30));
-        });
-        base = fminf(base, warp_min_float(lane_min_unflagged(key)));
+        const float scale = beta32 * speed32 * (1.0f + 1.0f / 65536.0f);
+        float lane_base = t_single;
+        for_each_unit(A, ch, w.occ_cell, lane,
+                      [&](int j) {
+                          screen_pair(j);
+                          lane_base = fminf(lane_base, lane_min_unflagged(key));
+                      },
+                      [&](int j, int rc) {
+                          const float rate = rates[rc * 3 + d];
+                          if (!(rate > 0.0f)) return;
+                          const uint64_t bits = draw_at(pair_base, (uint32_t)j);
+                          const float u_low = (float)(uint32_t)(bits >> 40) * (1.0f / 16777216.0f);
+                          const float threshold_lane = lane_base * rel + abs_margin;
+                          if (u_low > threshold_lane * scale * rate) return;
+                          bool flag = false;
+                          const float du = expovariate32(bits, beta32, flag);
+                          float t = (du / rate) / speed32;
+                          if (flag) t = -1.0f;
+                          if (!isinf(t)) {
+                              topk_insert(key, code, t, j | (1 << 30));
+                              lane_base = fminf(lane_base, lane_min_unflagged(key));
+                          }
+                      });
+        base = fminf(warp_min_float(lane_min_unflagged(key)), t_single);
+    } else {
+        for_each_near(A, ch, w.occ_cell, lane, screen_pair);
+        for (int i = lane; i < w.n_surplus; i += 32) screen_pair(A.surplus[ch.pos_off + i]);
+        base = fminf(warp_min_float(lane_min_unflagged(key)), t_single);
     }
     const float threshold = isinf(base) ? kInf32 : base * rel + abs_margin;
     // refinement of the candidates inside the threshold
@@ -905,7 +966,8 @@ __global__ void __launch_bounds__(256, JF_CHAIN_MIN_BLOCKS) chains_kernel(RunArg
 // lifting state at time 0 (initial_chain_start_of_run_event_handler.py) and the first end-of-chain candidate
 // ---------------------------------------------------------------------------------------------------------------
 __global__ void init_kernel(EngineView view, long long n_chains, double *positions, float4 *positions32,
-                            const double *charges, int32_t *occupancy, int32_t *surplus, JfgpuChainState *state) {
+                            const double *charges, int32_t *occupancy, int32_t *surplus, int32_t *roles,
+                            JfgpuChainState *state) {
     const int warp = threadIdx.x >> 5;
     const int lane = threadIdx.x & 31;
     const long long c = (long long)blockIdx.x * (blockDim.x >> 5) + warp;
@@ -933,8 +995,10 @@ __global__ void init_kernel(EngineView view, long long n_chains, double *positio
         while (k < ch.max_occ && slots[k] >= 0) ++k;
         if (k < ch.max_occ) {
             slots[k] = i;
+            roles[ch.pos_off + i] = role_of_cell(ch, cell);
         } else {
             surplus[ch.pos_off + n_surplus++] = i;
+            roles[ch.pos_off + i] = role_of_cell(ch, cell) | kRoleSurplus;
         }
     }
     JfgpuChainState g;
@@ -969,7 +1033,7 @@ cudaError_t launch_init(const EngineView &view, long long n_chains, const JfgpuB
     long long blocks = (n_chains + warps - 1) / warps;
     init_kernel<<<(unsigned)blocks, warps * 32, 0, stream>>>(view, n_chains, b.positions,
                                                               reinterpret_cast<float4 *>(b.positions32), b.charges,
-                                                              b.occupancy, b.surplus, b.state);
+                                                              b.occupancy, b.surplus, b.roles, b.state);
     return cudaGetLastError();
 }
 
@@ -984,6 +1048,7 @@ cudaError_t launch_run(const EngineView &view, const JfgpuBuffers &b, long long 
     A.charges = b.charges;
     A.occupancy = b.occupancy;
     A.surplus = b.surplus;
+    A.roles = b.roles;
     A.state = b.state;
     A.log = log;
     A.log_capacity = log_capacity;

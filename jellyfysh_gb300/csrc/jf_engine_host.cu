@@ -584,7 +584,7 @@ int jfgpu_chains_set_block_warps(JfgpuEngine *e, int32_t warps) {
 }
 
 static bool buffers_ok(const JfgpuEngine *e, const JfgpuBuffers *b) {
-    return e && b && b->positions && b->positions32 && b->occupancy && b->surplus && b->state;
+    return e && b && b->positions && b->positions32 && b->occupancy && b->surplus && b->roles && b->state;
 }
 
 int jfgpu_chains_init(JfgpuEngine *e, const JfgpuBuffers *b, void *stream_ptr) {
