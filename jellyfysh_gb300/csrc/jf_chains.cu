@@ -793,40 +793,28 @@ __device__ inline int mixed_candidates(const RunArgs &A, const ChainDev &ch, con
     double single_dt = kInf;
     if (lane == 0 && !isinf(single.q)) single_dt = time_sub(single.q, single.r, w.ts_q, w.ts_r);
     const float t_single = (float)__shfl_sync(kFull, single_dt, 0);
-    float base;
+    for_each_near(A, ch, w.occ_cell, lane, screen_pair);
+    for (int i = lane; i < w.n_surplus; i += 32) screen_pair(A.surplus[ch.pos_off + i]);
+    float base = fminf(warp_min_float(lane_min_unflagged(key)), t_single);
     if (far_of<FAR>(ch) == JFGPU_FAR_CELL_BOUNDING) {
-        // one pass over the units: nearby and surplus units are screened, far units are rejected early against the
-        // running threshold of their lane (a lane's threshold only decreases, so a rejected unit is above the final
-        // threshold too)
+        // far units (one coalesced pass over the role words), rejected against the warp-wide first threshold
+        const float threshold0 = isinf(base) ? kInf32 : base * rel + abs_margin;
+        const float reject = threshold0 * beta32 * speed32 * (1.0f + 1.0f / 65536.0f);
         const float *rates = sp.bound_upper32;
-        const float scale = beta32 * speed32 * (1.0f + 1.0f / 65536.0f);
-        float lane_base = t_single;
-        for_each_unit(A, ch, w.occ_cell, lane,
-                      [&](int j) {
-                          screen_pair(j);
-                          lane_base = fminf(lane_base, lane_min_unflagged(key));
-                      },
+        for_each_unit(A, ch, w.occ_cell, lane, [&](int j) {},
                       [&](int j, int rc) {
                           const float rate = rates[rc * 3 + d];
                           if (!(rate > 0.0f)) return;
                           const uint64_t bits = draw_at(pair_base, (uint32_t)j);
                           const float u_low = (float)(uint32_t)(bits >> 40) * (1.0f / 16777216.0f);
-                          const float threshold_lane = lane_base * rel + abs_margin;
-                          if (u_low > threshold_lane * scale * rate) return;
+                          if (u_low > reject * rate) return;
                           bool flag = false;
                           const float du = expovariate32(bits, beta32, flag);
                           float t = (du / rate) / speed32;
                           if (flag) t = -1.0f;
-                          if (!isinf(t)) {
-                              topk_insert(key, code, t, j | (1 << 30));
-                              lane_base = fminf(lane_base, lane_min_unflagged(key));
-                          }
+                          if (!isinf(t)) topk_insert(key, code, t, j | (1 << 30));
                       });
-        base = fminf(warp_min_float(lane_min_unflagged(key)), t_single);
-    } else {
-        for_each_near(A, ch, w.occ_cell, lane, screen_pair);
-        for (int i = lane; i < w.n_surplus; i += 32) screen_pair(A.surplus[ch.pos_off + i]);
-        base = fminf(warp_min_float(lane_min_unflagged(key)), t_single);
+        base = fminf(base, warp_min_float(lane_min_unflagged(key)));
     }
     const float threshold = isinf(base) ? kInf32 : base * rel + abs_margin;
     // refinement of the candidates inside the threshold
