@@ -743,21 +743,81 @@ __device__ inline float lane_min_unflagged(const float (&key)[kTopK]) {
     return v;
 }
 
-// Mixed precision: FP32 screening, FP64 refinement; returns 1 when the event must be re-solved in FP64.
-// Order: nearby and surplus candidates, the exact single candidates, a first threshold, then the far field with a
-// rigorous early rejection (-log(1 - u) >= u: a far time is at least u / (beta rate speed)), the final threshold,
-// and the FP64 re-solve of the candidates inside it.
+// ---------------------------------------------------------------------------------------------------------------
+// Mixed precision as a two-phase event.
+//   screen_kernel  (one warp per chain, FP32 only): every candidate is screened in FP32; the candidates within
+//                  (1 + 2^-10) t_min + margin, and every flagged one, go to the chain's refine list.
+//   resolve_kernel (one thread per chain, FP64): the single candidates (cell veto, cell boundary, end of chain) and
+//                  the listed candidates are solved with the reference's arithmetic, the earliest is committed and
+//                  the occupancy is updated for the next event.
+// The FP64 work of 32 chains thus shares each warp instruction, instead of occupying lane 0 of 32 warps, and each
+// kernel carries a small instruction footprint.  The winner and its time are the FP64 ones: the mixed path equals
+// the FP64 path event for event.
+// ---------------------------------------------------------------------------------------------------------------
+constexpr int kRefineMax = 28;
+constexpr int32_t kListOverflow = 1;
+constexpr int32_t kListSkip = 2;
+
+struct RefineList {
+    int32_t count, flags, screened, pad;
+    int32_t code[kRefineMax];  // target, bit 30 set for a far (cell-bounding) candidate
+};
+
 template <int POT, int FAR>
-__device__ inline int mixed_candidates(const RunArgs &A, const ChainDev &ch, const SpeciesDev &sp, const LJ32 &lj32,
-                                       const WarpState &w, int active_cell, int lane, Cand &best, int &status,
-                                       int &counted, int &refined) {
-    const long long ev = w.events;
-    const int d = w.direction;
+__global__ void __launch_bounds__(256, 4) screen_kernel(RunArgs A, RefineList *lists, long long round) {
+    const int warp = threadIdx.x >> 5;
+    const int lane = threadIdx.x & 31;
+    const long long local = (long long)blockIdx.x * (blockDim.x >> 5) + warp;
+    if (local >= A.count) return;
+    const long long c = A.first_chain + local;
+    const ChainDev &ch = A.view.chains[c];
+    const SpeciesDev &sp = A.view.species[ch.species];
+    RefineList &list = lists[local];
+    const JfgpuChainState &g = A.state[c];
+    if (g.status != JFGPU_STATUS_OK || (round > 0 && g.reserved)) {
+        if (lane == 0) {
+            list.count = 0;
+            list.flags = kListSkip;
+            list.screened = 0;
+        }
+        return;
+    }
+    if (potential_of<POT>(ch) == JFGPU_POT_COULOMB) {
+        // merged-image Coulomb chains (a few dozen charges) are solved entirely in FP64 by their resolve thread
+        if (lane == 0) {
+            list.count = 0;
+            list.flags = kListOverflow;
+            list.screened = 0;
+        }
+        return;
+    }
+    const int active = g.active, d = g.direction, occ_cell = g.occ_cell, n_surplus = g.n_surplus;
+    const uint64_t ev = (uint64_t)g.events;
     const float speed32 = (float)ch.speed;
     const float beta32 = (float)ch.beta;
     const float margin = ch.ulp_margin32;
     const float rel = 1.0f + 1.0f / 1024.0f;
     const float abs_margin = ch.screen_abs32 / speed32;
+    const float4 pa32 = A.positions32[ch.pos_off + active];
+    // single candidates in FP32 bound the threshold: the cell boundary and the end of chain
+    float t_single;
+    {
+        int ax[3];
+        cell_axes(ch, occ_cell, ax);
+        const int next = ax[d] + 1 == ch.m ? 0 : ax[d] + 1;
+        const float boundary = (float)A.view.cell_min[ch.geom_offset + next];
+        const float x = d == 0 ? pa32.x : (d == 1 ? pa32.y : pa32.z);
+        float sep = boundary - x;
+        if (sep < 0.0f) sep += ch.L32;
+        t_single = sep / speed32;
+        t_single = fminf(t_single, (float)time_sub(g.eoc_q, g.eoc_r, g.time_q, g.time_r));
+    }
+    LJ32 lj32;
+    lj32.a12 = (float)sp.lj.twelve.prefactor;
+    lj32.a6 = (float)sp.lj.six.prefactor;
+    lj32.four_over_k = (float)(4.0 / sp.lj.prefactor);
+    lj32.sigma_sq = (float)(sp.lj.sigma * sp.lj.sigma);
+    lj32.r0_sq = (float)sp.lj.r0_squared;
     float key[kTopK];
     int code[kTopK];
 #pragma unroll
@@ -765,13 +825,11 @@ __device__ inline int mixed_candidates(const RunArgs &A, const ChainDev &ch, con
         key[i] = kInf32;
         code[i] = -1;
     }
-    const float4 pa32 = make_float4((float)w.pa[0], (float)w.pa[1], (float)w.pa[2], 0.0f);
-    const uint64_t pair_base = draw_base(ch.key, (uint64_t)ev, kRngPair);
-    // codes: bit 30 marks a far (cell-bounding) candidate, the low bits carry the target
+    const uint64_t pair_base = draw_base(ch.key, ev, kRngPair);
     int count = 0;
     auto screen_pair = [&](int j) {
         ++count;
-        float4 pj = A.positions32[ch.pos_off + j];
+        const float4 pj = A.positions32[ch.pos_off + j];
         float sv[3];
         bool flag = false;
         separation32(pa32, pj, ch.L32, ch.half32, margin, sv, flag);
@@ -779,29 +837,22 @@ __device__ inline int mixed_candidates(const RunArgs &A, const ChainDev &ch, con
         if (potential_of<POT>(ch) == JFGPU_POT_HARD_SPHERE) {
             t = hs_screen((float)ch.diameter_sq, d, speed32, sv, margin, flag);
         } else {
-            float du = expovariate32(draw_at(pair_base, (uint32_t)j), beta32, flag);
+            const float du = expovariate32(draw_at(pair_base, (uint32_t)j), beta32, flag);
             t = lj_screen(lj32, d, speed32, sv, du, margin, flag);
         }
         if (flag) t = -1.0f;
         if (!isinf(t)) topk_insert(key, code, t, j);
     };
-    // exact single candidates (lane 0) bound the threshold of the far field
-    Cand single = cand_none();
-    int st = JFGPU_STATUS_OK;
-    if (lane == 0) st = single_candidates(A, ch, sp, w, active_cell, ev, single);
-    status = warp_max_int(st);
-    double single_dt = kInf;
-    if (lane == 0 && !isinf(single.q)) single_dt = time_sub(single.q, single.r, w.ts_q, w.ts_r);
-    const float t_single = (float)__shfl_sync(kFull, single_dt, 0);
-    for_each_near(A, ch, w.occ_cell, lane, screen_pair);
-    for (int i = lane; i < w.n_surplus; i += 32) screen_pair(A.surplus[ch.pos_off + i]);
+    for_each_near(A, ch, occ_cell, lane, screen_pair);
+    for (int i = lane; i < n_surplus; i += 32) screen_pair(A.surplus[ch.pos_off + i]);
     float base = fminf(warp_min_float(lane_min_unflagged(key)), t_single);
     if (far_of<FAR>(ch) == JFGPU_FAR_CELL_BOUNDING) {
-        // far units (one coalesced pass over the role words), rejected against the warp-wide first threshold
+        // far units (one coalesced pass over the role words) with the rigorous early rejection
+        // -log(1 - u) >= u: a far time is at least u / (beta rate speed)
         const float threshold0 = isinf(base) ? kInf32 : base * rel + abs_margin;
         const float reject = threshold0 * beta32 * speed32 * (1.0f + 1.0f / 65536.0f);
         const float *rates = sp.bound_upper32;
-        for_each_unit(A, ch, w.occ_cell, lane, [&](int j) {},
+        for_each_unit(A, ch, occ_cell, lane, [&](int j) {},
                       [&](int j, int rc) {
                           const float rate = rates[rc * 3 + d];
                           if (!(rate > 0.0f)) return;
@@ -817,33 +868,136 @@ __device__ inline int mixed_candidates(const RunArgs &A, const ChainDev &ch, con
         base = fminf(base, warp_min_float(lane_min_unflagged(key)));
     }
     const float threshold = isinf(base) ? kInf32 : base * rel + abs_margin;
-    // refinement of the candidates inside the threshold
-    const int overflow = (key[kTopK - 1] <= threshold) ? 1 : 0;
-    best = single;
-    int rst = JFGPU_STATUS_OK;
-    int nref = 0;
+    // compaction of the candidates inside the threshold into the chain's refine list
+    int overflow = (code[kTopK - 1] >= 0 && key[kTopK - 1] <= threshold) ? 1 : 0;
+    int total = 0;
 #pragma unroll
     for (int i = 0; i < kTopK; ++i) {
-        if (code[i] >= 0 && key[i] <= threshold) {
-            ++nref;
-            const int j = code[i] & ((1 << 30) - 1);
-            const int s2 = (code[i] & (1 << 30)) ? exact_cell_bounding(A, ch, sp, w, j, active_cell, ev, best)
-                                                 : exact_pair<POT>(A, ch, sp, w, j, ev, best);
-            if (s2) rst = s2;
+        const bool take = code[i] >= 0 && key[i] <= threshold;
+        const unsigned mask = __ballot_sync(kFull, take);
+        const int offset = total + __popc(mask & ((1u << lane) - 1u));
+        if (take && offset < kRefineMax) list.code[offset] = code[i];
+        total += __popc(mask);
+    }
+    overflow = warp_max_int(overflow);
+    const int screened = warp_sum_int(count);
+    if (lane == 0) {
+        list.count = total < kRefineMax ? total : kRefineMax;
+        list.flags = (overflow || total > kRefineMax) ? kListOverflow : 0;
+        list.screened = screened;
+    }
+}
+
+// every candidate of the event in FP64 by one thread (the rare overflow of a refine list)
+template <int POT, int FAR>
+__device__ __noinline__ int exact_serial(const RunArgs &A, const ChainDev &ch, const SpeciesDev &sp,
+                                         const WarpState &w, Cand &best) {
+    const long long ev = w.events;
+    int a[3];
+    cell_axes(ch, w.occ_cell, a);
+    const int K = ch.n_res;
+    const int32_t *occ = A.occupancy + ch.occ_off;
+    for (int oz = 0; oz < K; ++oz)
+        for (int oy = 0; oy < K; ++oy)
+            for (int ox = 0; ox < K; ++ox) {
+                const int cell = (a[0] + ch.res[ox]) % ch.m + ch.m * ((a[1] + ch.res[oy]) % ch.m) +
+                                 ch.m * ch.m * ((a[2] + ch.res[oz]) % ch.m);
+                for (int k = 0; k < ch.max_occ; ++k) {
+                    const int j = occ[(long long)cell * ch.max_occ + k];
+                    if (j >= 0) JF_TRY(exact_pair<POT>(A, ch, sp, w, j, ev, best));
+                }
+            }
+    for (int i = 0; i < w.n_surplus; ++i) JF_TRY(exact_pair<POT>(A, ch, sp, w, A.surplus[ch.pos_off + i], ev, best));
+    if (far_of<FAR>(ch) == JFGPU_FAR_CELL_BOUNDING) {
+        for (int cell = 0; cell < ch.ncells; ++cell) {
+            const int j = occ[cell];
+            if (j < 0 || is_nearby(ch, cell, w.occ_cell)) continue;
+            JF_TRY(exact_cell_bounding(A, ch, sp, w, j, w.occ_cell, ev, best));
         }
     }
-    status = max(status, warp_max_int(rst));
-    best = warp_argmin_sparse(best);
-    counted = warp_sum_int(count);
-    refined = warp_sum_int(nref);
-    return warp_max_int(overflow);
+    return JFGPU_STATUS_OK;
+}
+
+template <int POT, int FAR>
+__global__ void __launch_bounds__(128) resolve_kernel(RunArgs A, const RefineList *lists, long long round) {
+    const long long local = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (local >= A.count) return;
+    const long long c = A.first_chain + local;
+    const ChainDev &ch = A.view.chains[c];
+    const SpeciesDev &sp = A.view.species[ch.species];
+    JfgpuChainState &g = A.state[c];
+    if (g.status != JFGPU_STATUS_OK || (round > 0 && g.reserved)) return;
+    const RefineList &list = lists[local];
+    if (list.flags & kListSkip) return;
+    WarpState w;
+    w.ts_q = g.time_q;
+    w.ts_r = g.time_r;
+    w.eoc_q = g.eoc_q;
+    w.eoc_r = g.eoc_r;
+    w.events = g.events;
+    w.warnings = g.bound_warnings;
+    w.fallbacks = g.refine_fallbacks;
+    w.candidates = g.candidates + list.screened;
+    w.refined = g.refined + list.count;
+    w.active = g.active;
+    w.direction = g.direction;
+    w.eoc_new = g.eoc_new_active;
+    w.occ_active = g.occ_active;
+    w.occ_cell = g.occ_cell;
+    w.n_surplus = g.n_surplus;
+    w.status = JFGPU_STATUS_OK;
+    w.stop = 0;
+    load_pos(A, ch, w.active, w.pa);
+    Cand best = cand_none();
+    int st = single_candidates(A, ch, sp, w, w.occ_cell, w.events, best);
+    if (!st) {
+        if (list.flags & kListOverflow) {
+            st = exact_serial<POT, FAR>(A, ch, sp, w, best);
+            if (potential_of<POT>(ch) != JFGPU_POT_COULOMB) w.fallbacks += 1;
+        } else {
+            for (int i = 0; i < list.count && !st; ++i) {
+                const int code = list.code[i];
+                const int j = code & ((1 << 30) - 1);
+                st = (code & (1 << 30)) ? exact_cell_bounding(A, ch, sp, w, j, w.occ_cell, w.events, best)
+                                        : exact_pair<POT>(A, ch, sp, w, j, w.events, best);
+            }
+        }
+    }
+    if (st) {
+        w.status = st;
+    } else if (A.has_stop && !time_lt(best.q, best.r, A.stop_q, A.stop_r)) {
+        time_slice(ch, w, A.stop_q, A.stop_r);
+        store_active(A, ch, w, w.active);
+        w.stop = 1;
+    } else {
+        st = commit(A, ch, sp, w, best, w.occ_cell, c, round);
+        if (!st) st = occ_update(A, ch, w);  // the activator's update of the next event
+        if (st) w.status = st;
+    }
+    g.time_q = w.ts_q;
+    g.time_r = w.ts_r;
+    g.eoc_q = w.eoc_q;
+    g.eoc_r = w.eoc_r;
+    g.events = w.events;
+    g.bound_warnings = w.warnings;
+    g.refine_fallbacks = w.fallbacks;
+    g.candidates = w.candidates;
+    g.refined = w.refined;
+    g.active = w.active;
+    g.direction = w.direction;
+    g.eoc_new_active = w.eoc_new;
+    g.occ_active = w.occ_active;
+    g.occ_cell = w.occ_cell;
+    g.n_surplus = w.n_surplus;
+    g.status = w.status;
+    g.reserved = w.stop;
 }
 
 #ifndef JF_CHAIN_MIN_BLOCKS
 #define JF_CHAIN_MIN_BLOCKS 4
 #endif
 
-template <int MODE, int POT, int FAR>
+template <int POT, int FAR>
 __global__ void __launch_bounds__(256, JF_CHAIN_MIN_BLOCKS) chains_kernel(RunArgs A) {
     extern __shared__ unsigned char smem_raw[];
     WarpState *shared = reinterpret_cast<WarpState *>(smem_raw);
@@ -877,12 +1031,6 @@ __global__ void __launch_bounds__(256, JF_CHAIN_MIN_BLOCKS) chains_kernel(RunArg
         load_pos(A, ch, w.active, w.pa);
     }
     __syncwarp();
-    LJ32 lj32;
-    lj32.a12 = (float)sp.lj.twelve.prefactor;
-    lj32.a6 = (float)sp.lj.six.prefactor;
-    lj32.four_over_k = (float)(4.0 / sp.lj.prefactor);
-    lj32.sigma_sq = (float)(sp.lj.sigma * sp.lj.sigma);
-    lj32.r0_sq = (float)sp.lj.r0_squared;
     const long long start_events = w.events;
     for (long long e = 0; e < A.max_events; ++e) {
         if (w.status != JFGPU_STATUS_OK || w.stop) break;
@@ -898,17 +1046,8 @@ __global__ void __launch_bounds__(256, JF_CHAIN_MIN_BLOCKS) chains_kernel(RunArg
         Cand best;
         int status = JFGPU_STATUS_OK;
         int counted = 0, refined = 0;
-        if (MODE == JFGPU_MODE_MIXED && potential_of<POT>(ch) != JFGPU_POT_COULOMB) {
-            int fallback =
-                mixed_candidates<POT, FAR>(A, ch, sp, lj32, w, active_cell, lane, best, status, counted, refined);
-            if (fallback && status == JFGPU_STATUS_OK) {
-                int recount = 0;
-                status = exact_candidates<POT, FAR>(A, ch, sp, w, active_cell, lane, best, recount);
-                if (lane == 0) w.fallbacks += 1;
-            }
-        } else {
-            status = exact_candidates<POT, FAR>(A, ch, sp, w, active_cell, lane, best, counted);
-        }
+        (void)refined;
+        status = exact_candidates<POT, FAR>(A, ch, sp, w, active_cell, lane, best, counted);
         __syncwarp();
         if (lane == 0) {
             w.candidates += counted;
@@ -1006,8 +1145,30 @@ __global__ void init_kernel(EngineView view, long long n_chains, double *positio
     g.n_surplus = n_surplus;
     g.status = status;
     g.reserved = 0;
+    if (status == JFGPU_STATUS_OK) {
+        // the activator's first update after the start of the run: the initial active unit leaves the occupancy
+        RunArgs A;
+        memset(&A, 0, sizeof(A));
+        A.view = view;
+        A.positions = positions;
+        A.occupancy = occupancy;
+        A.surplus = surplus;
+        A.roles = roles;
+        WarpState w;
+        w.active = g.active;
+        w.occ_active = -1;
+        w.occ_cell = -1;
+        w.n_surplus = n_surplus;
+        load_pos(A, ch, w.active, w.pa);
+        g.status = occ_update(A, ch, w);
+        g.occ_active = w.occ_active;
+        g.occ_cell = w.occ_cell;
+        g.n_surplus = w.n_surplus;
+    }
     state[c] = g;
 }
+
+size_t refine_list_bytes() { return sizeof(RefineList); }
 
 }  // namespace jf
 
@@ -1025,10 +1186,21 @@ cudaError_t launch_init(const EngineView &view, long long n_chains, const JfgpuB
     return cudaGetLastError();
 }
 
+template <int POT, int FAR>
+static void launch_mixed_rounds(const RunArgs &A, void *lists, long long rounds, int warps, cudaStream_t stream) {
+    const long long screen_blocks = (A.count + warps - 1) / warps;
+    const long long resolve_blocks = (A.count + 127) / 128;
+    RefineList *l = static_cast<RefineList *>(lists);
+    for (long long r = 0; r < rounds; ++r) {
+        screen_kernel<POT, FAR><<<(unsigned)screen_blocks, warps * 32, 0, stream>>>(A, l, r);
+        resolve_kernel<POT, FAR><<<(unsigned)resolve_blocks, 128, 0, stream>>>(A, l, r);
+    }
+}
+
 cudaError_t launch_run(const EngineView &view, const JfgpuBuffers &b, long long first, long long count,
                        long long max_events, double stop_q, double stop_r, int mode, JfgpuEvent *log,
                        long long log_capacity, int warps_per_block, int uniform_potential, int uniform_far,
-                       cudaStream_t stream) {
+                       void *lists, cudaStream_t stream, long long *launches) {
     RunArgs A;
     A.view = view;
     A.positions = b.positions;
@@ -1050,21 +1222,22 @@ cudaError_t launch_run(const EngineView &view, const JfgpuBuffers &b, long long 
     if (warps < 1) warps = 1;
     if (warps > 8) warps = 8;
     if (count < warps) warps = (int)count;
-    long long blocks = (count + warps - 1) / warps;
-    size_t smem = sizeof(WarpState) * warps;
-    const dim3 grid((unsigned)blocks), block(warps * 32);
     if (mode == JFGPU_MODE_MIXED) {
         // kernels specialised for the common homogeneous batches carry only their potential's code
         if (uniform_potential == JFGPU_POT_LENNARD_JONES && uniform_far == JFGPU_FAR_CELL_BOUNDING)
-            chains_kernel<JFGPU_MODE_MIXED, JFGPU_POT_LENNARD_JONES, JFGPU_FAR_CELL_BOUNDING><<<grid, block, smem, stream>>>(A);
+            launch_mixed_rounds<JFGPU_POT_LENNARD_JONES, JFGPU_FAR_CELL_BOUNDING>(A, lists, max_events, warps, stream);
         else if (uniform_potential == JFGPU_POT_LENNARD_JONES && uniform_far == JFGPU_FAR_CELL_VETO)
-            chains_kernel<JFGPU_MODE_MIXED, JFGPU_POT_LENNARD_JONES, JFGPU_FAR_CELL_VETO><<<grid, block, smem, stream>>>(A);
+            launch_mixed_rounds<JFGPU_POT_LENNARD_JONES, JFGPU_FAR_CELL_VETO>(A, lists, max_events, warps, stream);
         else if (uniform_potential == JFGPU_POT_HARD_SPHERE && uniform_far == JFGPU_FAR_NONE)
-            chains_kernel<JFGPU_MODE_MIXED, JFGPU_POT_HARD_SPHERE, JFGPU_FAR_NONE><<<grid, block, smem, stream>>>(A);
+            launch_mixed_rounds<JFGPU_POT_HARD_SPHERE, JFGPU_FAR_NONE>(A, lists, max_events, warps, stream);
         else
-            chains_kernel<JFGPU_MODE_MIXED, -1, -1><<<grid, block, smem, stream>>>(A);
+            launch_mixed_rounds<-1, -1>(A, lists, max_events, warps, stream);
+        *launches += 2 * max_events;
     } else {
-        chains_kernel<JFGPU_MODE_EXACT, -1, -1><<<grid, block, smem, stream>>>(A);
+        const long long blocks = (count + warps - 1) / warps;
+        const size_t smem = sizeof(WarpState) * warps;
+        chains_kernel<-1, -1><<<(unsigned)blocks, warps * 32, smem, stream>>>(A);
+        *launches += 1;
     }
     return cudaGetLastError();
 }
