@@ -969,6 +969,8 @@ __global__ void __launch_bounds__(128) resolve_kernel(RunArgs A, const RefineLis
         time_slice(ch, w, A.stop_q, A.stop_r);
         store_active(A, ch, w, w.active);
         w.stop = 1;
+        st = occ_update(A, ch, w);
+        if (st) w.status = st;
     } else {
         st = commit(A, ch, sp, w, best, w.occ_cell, c, round);
         if (!st) st = occ_update(A, ch, w);  // the activator's update of the next event
@@ -1034,7 +1036,7 @@ __global__ void __launch_bounds__(256, JF_CHAIN_MIN_BLOCKS) chains_kernel(RunArg
     const long long start_events = w.events;
     for (long long e = 0; e < A.max_events; ++e) {
         if (w.status != JFGPU_STATUS_OK || w.stop) break;
-        if (lane == 0) {
+        if (lane == 0 && w.active != w.occ_active) {
             int st = occ_update(A, ch, w);
             if (st) w.status = st;
         }
@@ -1060,8 +1062,11 @@ __global__ void __launch_bounds__(256, JF_CHAIN_MIN_BLOCKS) chains_kernel(RunArg
                 time_slice(ch, w, A.stop_q, A.stop_r);
                 store_active(A, ch, w, w.active);
                 w.stop = 1;
+                int st = occ_update(A, ch, w);
+                if (st) w.status = st;
             } else {
                 int st = commit(A, ch, sp, w, best, active_cell, c, w.events - start_events);
+                if (!st) st = occ_update(A, ch, w);  // the activator's update of the next event
                 if (st) w.status = st;
             }
         }
