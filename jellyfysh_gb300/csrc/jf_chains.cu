@@ -793,8 +793,8 @@ __global__ void __launch_bounds__(256, 4) screen_kernel(RunArgs A, RefineList *l
     }
     const int active = g.active, d = g.direction, occ_cell = g.occ_cell, n_surplus = g.n_surplus;
     const uint64_t ev = (uint64_t)g.events;
-    const float speed32 = (float)ch.speed;
-    const float beta32 = (float)ch.beta;
+    const float speed32 = ch.speed32;
+    const float inv_beta32 = ch.inv_beta32;
     const float margin = ch.ulp_margin32;
     const float rel = 1.0f + 1.0f / 1024.0f;
     const float abs_margin = ch.screen_abs32 / speed32;
@@ -813,11 +813,11 @@ __global__ void __launch_bounds__(256, 4) screen_kernel(RunArgs A, RefineList *l
         t_single = fminf(t_single, (float)time_sub(g.eoc_q, g.eoc_r, g.time_q, g.time_r));
     }
     LJ32 lj32;
-    lj32.a12 = (float)sp.lj.twelve.prefactor;
-    lj32.a6 = (float)sp.lj.six.prefactor;
-    lj32.four_over_k = (float)(4.0 / sp.lj.prefactor);
-    lj32.sigma_sq = (float)(sp.lj.sigma * sp.lj.sigma);
-    lj32.r0_sq = (float)sp.lj.r0_squared;
+    lj32.a12 = sp.lj32[0];
+    lj32.a6 = sp.lj32[1];
+    lj32.four_over_k = sp.lj32[2];
+    lj32.sigma_sq = sp.lj32[3];
+    lj32.r0_sq = sp.lj32[4];
     float key[kTopK];
     int code[kTopK];
 #pragma unroll
@@ -835,9 +835,9 @@ __global__ void __launch_bounds__(256, 4) screen_kernel(RunArgs A, RefineList *l
         separation32(pa32, pj, ch.L32, ch.half32, margin, sv, flag);
         float t;
         if (potential_of<POT>(ch) == JFGPU_POT_HARD_SPHERE) {
-            t = hs_screen((float)ch.diameter_sq, d, speed32, sv, margin, flag);
+            t = hs_screen(ch.diameter_sq32, d, speed32, sv, margin, flag);
         } else {
-            const float du = expovariate32(draw_at(pair_base, (uint32_t)j), beta32, flag);
+            const float du = expovariate32(draw_at(pair_base, (uint32_t)j), inv_beta32, flag);
             t = lj_screen(lj32, d, speed32, sv, du, margin, flag);
         }
         if (flag) t = -1.0f;
@@ -850,7 +850,7 @@ __global__ void __launch_bounds__(256, 4) screen_kernel(RunArgs A, RefineList *l
         // far units (one coalesced pass over the role words) with the rigorous early rejection
         // -log(1 - u) >= u: a far time is at least u / (beta rate speed)
         const float threshold0 = isinf(base) ? kInf32 : base * rel + abs_margin;
-        const float reject = threshold0 * beta32 * speed32 * (1.0f + 1.0f / 65536.0f);
+        const float reject = threshold0 * speed32 * (1.0f + 1.0f / 65536.0f) / inv_beta32;
         const float *rates = sp.bound_upper32;
         for_each_unit(A, ch, occ_cell, lane, [&](int j) {},
                       [&](int j, int rc) {
@@ -860,7 +860,7 @@ __global__ void __launch_bounds__(256, 4) screen_kernel(RunArgs A, RefineList *l
                           const float u_low = (float)(uint32_t)(bits >> 40) * (1.0f / 16777216.0f);
                           if (u_low > reject * rate) return;
                           bool flag = false;
-                          const float du = expovariate32(bits, beta32, flag);
+                          const float du = expovariate32(bits, inv_beta32, flag);
                           float t = (du / rate) / speed32;
                           if (flag) t = -1.0f;
                           if (!isinf(t)) topk_insert(key, code, t, j | (1 << 30));
@@ -919,7 +919,7 @@ __device__ __noinline__ int exact_serial(const RunArgs &A, const ChainDev &ch, c
 }
 
 template <int POT, int FAR>
-__global__ void __launch_bounds__(128) resolve_kernel(RunArgs A, const RefineList *lists, long long round) {
+__global__ void __launch_bounds__(32) resolve_kernel(RunArgs A, const RefineList *lists, long long round) {
     const long long local = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (local >= A.count) return;
     const long long c = A.first_chain + local;
@@ -1194,11 +1194,11 @@ cudaError_t launch_init(const EngineView &view, long long n_chains, const JfgpuB
 template <int POT, int FAR>
 static void launch_mixed_rounds(const RunArgs &A, void *lists, long long rounds, int warps, cudaStream_t stream) {
     const long long screen_blocks = (A.count + warps - 1) / warps;
-    const long long resolve_blocks = (A.count + 127) / 128;
+    const long long resolve_blocks = (A.count + 31) / 32;  // one warp per block: the resolve work spreads over the SMs
     RefineList *l = static_cast<RefineList *>(lists);
     for (long long r = 0; r < rounds; ++r) {
         screen_kernel<POT, FAR><<<(unsigned)screen_blocks, warps * 32, 0, stream>>>(A, l, r);
-        resolve_kernel<POT, FAR><<<(unsigned)resolve_blocks, 128, 0, stream>>>(A, l, r);
+        resolve_kernel<POT, FAR><<<(unsigned)resolve_blocks, 32, 0, stream>>>(A, l, r);
     }
 }
 

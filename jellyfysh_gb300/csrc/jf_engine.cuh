@@ -27,6 +27,7 @@ struct WalkerDev {
 };
 
 struct SpeciesDev {
+    float lj32[5];               // Lennard-Jones FP32 screening constants: k s^12, -k s^6, 4/k, s^2, r0^2
     MH lj;
     MIC mic;
     const double *bound_upper;   // [cells][3]
@@ -53,6 +54,7 @@ struct ChainDev {
     float L32, half32;
     float ulp_margin32;          // rounding scale of FP32 separations (16 L 2^-24): closer calls are flagged
     float screen_abs32;          // absolute screening margin in length units (L 2^-16)
+    float speed32, inv_beta32, diameter_sq32, pad32;
     uint64_t key;
 };
 

@@ -298,7 +298,14 @@ int build_species(JfgpuEngine *e, const JfgpuChainDesc &d, const std::vector<dou
     int error = JFGPU_OK;
     const int m = d.cells_per_side;
     const int ncells = m * m * m;
-    if (d.potential == JFGPU_POT_LENNARD_JONES) sp.lj = make_lj(d.lj_prefactor, d.lj_sigma);
+    if (d.potential == JFGPU_POT_LENNARD_JONES) {
+        sp.lj = make_lj(d.lj_prefactor, d.lj_sigma);
+        sp.lj32[0] = (float)sp.lj.twelve.prefactor;
+        sp.lj32[1] = (float)sp.lj.six.prefactor;
+        sp.lj32[2] = (float)(4.0 / sp.lj.prefactor);
+        sp.lj32[3] = (float)(sp.lj.sigma * sp.lj.sigma);
+        sp.lj32[4] = (float)sp.lj.r0_squared;
+    }
     if (d.potential == JFGPU_POT_COULOMB) {
         std::vector<double> table = fourier_table(d.fourier_cutoff, d.ewald_alpha, d.system_length);
         const double *dev = device_copy(e, table, stream, error);
@@ -512,6 +519,9 @@ int jfgpu_engine_create(const JfgpuChainDesc *chains, int64_t n_chains, void *st
         ch.half32 = (float)(d.system_length / 2.0);
         ch.ulp_margin32 = (float)(16.0 * d.system_length / 16777216.0);
         ch.screen_abs32 = (float)(d.system_length / 65536.0);
+        ch.speed32 = (float)d.speed;
+        ch.inv_beta32 = (float)(1.0 / d.beta);
+        ch.diameter_sq32 = (float)ch.diameter_sq;
         ch.key = d.rng_key;
         SpeciesKey key{d.potential, d.far, m, d.neighbor_layers, d.fourier_cutoff, d.position_cutoff,
                        d.estimator_points, d.system_length, d.lj_prefactor, d.lj_sigma, d.coulomb_prefactor,

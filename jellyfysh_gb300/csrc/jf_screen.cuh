@@ -13,18 +13,22 @@ namespace jf {
 constexpr float kScreenRel = 1.0f / 4096.0f;  // conditioning thresholds
 constexpr float kInf32 = __builtin_inff();
 
-// potential change of a keyed draw in FP32, relative error about 2^-22: log1p near u = 0, log(1 - u) otherwise
-__device__ inline float expovariate32(uint64_t bits, float beta, bool &flag) {
-    double u = uniform53(bits);
+// potential change of a keyed draw in FP32 without FP64 instructions: the uniform is (bits >> 11) 2^-53; its top 32
+// bits k give u within 2^-32, so -log1p(-u) (u < 1/2) and -log(1 - u) with 1 - u from 2^32 - k (u >= 1/2) carry a
+// relative error of about 2^-22 except for u < 2^-16 or 1 - u < 2^-16, which are flagged
+__device__ inline float expovariate32(uint64_t bits, float inv_beta, bool &flag) {
+    const uint32_t k = (uint32_t)(bits >> 32);
     float du;
-    if (u < 0.5) {
-        du = -log1pf(-(float)u);
+    if (k < 0x80000000u) {
+        if (k < 0x10000u) flag = true;
+        du = -log1pf(-(float)k * (1.0f / 4294967296.0f));
     } else {
-        double w = 1.0 - u;  // exact
-        du = -logf((float)w);
+        const uint32_t complement = 0u - k;  // 2^32 - k
+        if (complement < 0x10000u) flag = true;
+        du = -logf((float)complement * (1.0f / 4294967296.0f));
     }
     if (!(du >= 0.0f) || isinf(du)) flag = true;
-    return du / beta;
+    return du * inv_beta;
 }
 
 // minimum-image separation in FP32 from the FP32 mirror; flags components within rounding of +-L/2
