@@ -888,6 +888,66 @@ __global__ void __launch_bounds__(256, 4) screen_kernel(RunArgs A, RefineList *l
     }
 }
 
+// FP64 re-solves of the first kRefineSlots entries of every refine list, one thread per entry; the resolve kernel
+// takes the earliest of them (and solves any further entry itself)
+constexpr int kRefineSlots = 2;
+
+struct Refined {
+    double q, r, rate;
+    int32_t kind, target, aux, status;
+};
+
+__device__ inline void load_lifting(const JfgpuChainState &g, const RunArgs &A, const ChainDev &ch, WarpState &w) {
+    w.ts_q = g.time_q;
+    w.ts_r = g.time_r;
+    w.eoc_q = g.eoc_q;
+    w.eoc_r = g.eoc_r;
+    w.events = g.events;
+    w.warnings = g.bound_warnings;
+    w.fallbacks = g.refine_fallbacks;
+    w.candidates = g.candidates;
+    w.refined = g.refined;
+    w.active = g.active;
+    w.direction = g.direction;
+    w.eoc_new = g.eoc_new_active;
+    w.occ_active = g.occ_active;
+    w.occ_cell = g.occ_cell;
+    w.n_surplus = g.n_surplus;
+    w.status = JFGPU_STATUS_OK;
+    w.stop = 0;
+    load_pos(A, ch, w.active, w.pa);
+}
+
+template <int POT, int FAR>
+__global__ void __launch_bounds__(64) refine_kernel(RunArgs A, const RefineList *lists, Refined *refined,
+                                                     long long round) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long local = t / kRefineSlots;
+    const int slot = (int)(t % kRefineSlots);
+    if (local >= A.count) return;
+    Refined &out = refined[local * kRefineSlots + slot];
+    out.kind = 1 << 30;
+    const RefineList &list = lists[local];
+    if ((list.flags & (kListSkip | kListOverflow)) || slot >= list.count) return;
+    const long long c = A.first_chain + local;
+    const ChainDev &ch = A.view.chains[c];
+    const SpeciesDev &sp = A.view.species[ch.species];
+    WarpState w;
+    load_lifting(A.state[c], A, ch, w);
+    Cand best = cand_none();
+    const int code = list.code[slot];
+    const int j = code & ((1 << 30) - 1);
+    const int st = (code & (1 << 30)) ? exact_cell_bounding(A, ch, sp, w, j, w.occ_cell, w.events, best)
+                                      : exact_pair<POT>(A, ch, sp, w, j, w.events, best);
+    out.q = best.q;
+    out.r = best.r;
+    out.rate = best.rate;
+    out.kind = best.kind;
+    out.target = best.target;
+    out.aux = best.aux;
+    out.status = st;
+}
+
 // every candidate of the event in FP64 by one thread (the rare overflow of a refine list)
 template <int POT, int FAR>
 __device__ __noinline__ int exact_serial(const RunArgs &A, const ChainDev &ch, const SpeciesDev &sp,
@@ -919,7 +979,8 @@ __device__ __noinline__ int exact_serial(const RunArgs &A, const ChainDev &ch, c
 }
 
 template <int POT, int FAR>
-__global__ void __launch_bounds__(32) resolve_kernel(RunArgs A, const RefineList *lists, long long round) {
+__global__ void __launch_bounds__(32) resolve_kernel(RunArgs A, const RefineList *lists, const Refined *refined,
+                                                     long long round) {
     const long long local = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (local >= A.count) return;
     const long long c = A.first_chain + local;
@@ -930,24 +991,9 @@ __global__ void __launch_bounds__(32) resolve_kernel(RunArgs A, const RefineList
     const RefineList &list = lists[local];
     if (list.flags & kListSkip) return;
     WarpState w;
-    w.ts_q = g.time_q;
-    w.ts_r = g.time_r;
-    w.eoc_q = g.eoc_q;
-    w.eoc_r = g.eoc_r;
-    w.events = g.events;
-    w.warnings = g.bound_warnings;
-    w.fallbacks = g.refine_fallbacks;
-    w.candidates = g.candidates + list.screened;
-    w.refined = g.refined + list.count;
-    w.active = g.active;
-    w.direction = g.direction;
-    w.eoc_new = g.eoc_new_active;
-    w.occ_active = g.occ_active;
-    w.occ_cell = g.occ_cell;
-    w.n_surplus = g.n_surplus;
-    w.status = JFGPU_STATUS_OK;
-    w.stop = 0;
-    load_pos(A, ch, w.active, w.pa);
+    load_lifting(g, A, ch, w);
+    w.candidates += list.screened;
+    w.refined += list.count;
     Cand best = cand_none();
     int st = single_candidates(A, ch, sp, w, w.occ_cell, w.events, best);
     if (!st) {
@@ -955,7 +1001,22 @@ __global__ void __launch_bounds__(32) resolve_kernel(RunArgs A, const RefineList
             st = exact_serial<POT, FAR>(A, ch, sp, w, best);
             if (potential_of<POT>(ch) != JFGPU_POT_COULOMB) w.fallbacks += 1;
         } else {
-            for (int i = 0; i < list.count && !st; ++i) {
+            for (int i = 0; i < list.count && i < kRefineSlots && !st; ++i) {
+                const Refined &rf = refined[local * kRefineSlots + i];
+                if (rf.status) {
+                    st = rf.status;
+                } else if (rf.kind != (1 << 30)) {
+                    Cand cnd;
+                    cnd.q = rf.q;
+                    cnd.r = rf.r;
+                    cnd.kind = rf.kind;
+                    cnd.target = rf.target;
+                    cnd.aux = rf.aux;
+                    cnd.rate = rf.rate;
+                    if (cand_better(cnd, best)) best = cnd;
+                }
+            }
+            for (int i = kRefineSlots; i < list.count && !st; ++i) {
                 const int code = list.code[i];
                 const int j = code & ((1 << 30) - 1);
                 st = (code & (1 << 30)) ? exact_cell_bounding(A, ch, sp, w, j, w.occ_cell, w.events, best)
@@ -1174,6 +1235,7 @@ __global__ void init_kernel(EngineView view, long long n_chains, double *positio
 }
 
 size_t refine_list_bytes() { return sizeof(RefineList); }
+size_t refined_bytes() { return sizeof(Refined) * kRefineSlots; }
 
 }  // namespace jf
 
@@ -1192,20 +1254,24 @@ cudaError_t launch_init(const EngineView &view, long long n_chains, const JfgpuB
 }
 
 template <int POT, int FAR>
-static void launch_mixed_rounds(const RunArgs &A, void *lists, long long rounds, int warps, cudaStream_t stream) {
+static void launch_mixed_rounds(const RunArgs &A, void *lists, void *refined, long long rounds, int warps,
+                                cudaStream_t stream) {
     const long long screen_blocks = (A.count + warps - 1) / warps;
+    const long long refine_blocks = (A.count * kRefineSlots + 63) / 64;
     const long long resolve_blocks = (A.count + 31) / 32;  // one warp per block: the resolve work spreads over the SMs
     RefineList *l = static_cast<RefineList *>(lists);
+    Refined *f = static_cast<Refined *>(refined);
     for (long long r = 0; r < rounds; ++r) {
         screen_kernel<POT, FAR><<<(unsigned)screen_blocks, warps * 32, 0, stream>>>(A, l, r);
-        resolve_kernel<POT, FAR><<<(unsigned)resolve_blocks, 32, 0, stream>>>(A, l, r);
+        refine_kernel<POT, FAR><<<(unsigned)refine_blocks, 64, 0, stream>>>(A, l, f, r);
+        resolve_kernel<POT, FAR><<<(unsigned)resolve_blocks, 32, 0, stream>>>(A, l, f, r);
     }
 }
 
 cudaError_t launch_run(const EngineView &view, const JfgpuBuffers &b, long long first, long long count,
                        long long max_events, double stop_q, double stop_r, int mode, JfgpuEvent *log,
                        long long log_capacity, int warps_per_block, int uniform_potential, int uniform_far,
-                       void *lists, cudaStream_t stream, long long *launches) {
+                       void *lists, void *refined, cudaStream_t stream, long long *launches) {
     RunArgs A;
     A.view = view;
     A.positions = b.positions;
@@ -1230,14 +1296,14 @@ cudaError_t launch_run(const EngineView &view, const JfgpuBuffers &b, long long 
     if (mode == JFGPU_MODE_MIXED) {
         // kernels specialised for the common homogeneous batches carry only their potential's code
         if (uniform_potential == JFGPU_POT_LENNARD_JONES && uniform_far == JFGPU_FAR_CELL_BOUNDING)
-            launch_mixed_rounds<JFGPU_POT_LENNARD_JONES, JFGPU_FAR_CELL_BOUNDING>(A, lists, max_events, warps, stream);
+            launch_mixed_rounds<JFGPU_POT_LENNARD_JONES, JFGPU_FAR_CELL_BOUNDING>(A, lists, refined, max_events, warps, stream);
         else if (uniform_potential == JFGPU_POT_LENNARD_JONES && uniform_far == JFGPU_FAR_CELL_VETO)
-            launch_mixed_rounds<JFGPU_POT_LENNARD_JONES, JFGPU_FAR_CELL_VETO>(A, lists, max_events, warps, stream);
+            launch_mixed_rounds<JFGPU_POT_LENNARD_JONES, JFGPU_FAR_CELL_VETO>(A, lists, refined, max_events, warps, stream);
         else if (uniform_potential == JFGPU_POT_HARD_SPHERE && uniform_far == JFGPU_FAR_NONE)
-            launch_mixed_rounds<JFGPU_POT_HARD_SPHERE, JFGPU_FAR_NONE>(A, lists, max_events, warps, stream);
+            launch_mixed_rounds<JFGPU_POT_HARD_SPHERE, JFGPU_FAR_NONE>(A, lists, refined, max_events, warps, stream);
         else
-            launch_mixed_rounds<-1, -1>(A, lists, max_events, warps, stream);
-        *launches += 2 * max_events;
+            launch_mixed_rounds<-1, -1>(A, lists, refined, max_events, warps, stream);
+        *launches += 3 * max_events;
     } else {
         const long long blocks = (count + warps - 1) / warps;
         const size_t smem = sizeof(WarpState) * warps;

@@ -25,8 +25,9 @@ cudaError_t launch_init(const EngineView &view, long long n_chains, const JfgpuB
 cudaError_t launch_run(const EngineView &view, const JfgpuBuffers &b, long long first, long long count,
                        long long max_events, double stop_q, double stop_r, int mode, JfgpuEvent *log,
                        long long log_capacity, int warps_per_block, int uniform_potential, int uniform_far,
-                       void *lists, cudaStream_t stream, long long *launches);
+                       void *lists, void *refined, cudaStream_t stream, long long *launches);
 size_t refine_list_bytes();
+size_t refined_bytes();
 }  // namespace jf
 
 using namespace jf;
@@ -49,6 +50,7 @@ struct JfgpuEngine {
     int64_t launches = 0;
     int block_warps = 4;
     void *refine_lists = nullptr;  // per-chain refine lists of the mixed-precision rounds
+    void *refined = nullptr;       // per-chain FP64 re-solves of the first list entries
 };
 
 namespace {
@@ -551,6 +553,8 @@ int jfgpu_engine_create(const JfgpuChainDesc *chains, int64_t n_chains, void *st
         e->view.tra = device_copy(e, tra_pool, stream, error);
         std::vector<unsigned char> lists(refine_list_bytes() * (size_t)n_chains, 0);
         e->refine_lists = device_copy(e, lists, stream, error);
+        std::vector<unsigned char> slots(refined_bytes() * (size_t)n_chains, 0);
+        e->refined = device_copy(e, slots, stream, error);
         if (!error && cudaStreamSynchronize(stream) != cudaSuccess) error = JFGPU_ERROR_CUDA;
     }
     if (error) {
@@ -620,7 +624,8 @@ int jfgpu_chains_run(JfgpuEngine *e, const JfgpuBuffers *b, int64_t first, int64
         if (e->chains[c].potential != potential || e->chains[c].far != far) potential = far = -1;
     long long launches = 0;
     cudaError_t err = launch_run(e->view, *b, first, count, max_events, stop_q, stop_r, mode, log, log_capacity,
-                                 e->block_warps, potential, far, e->refine_lists, static_cast<cudaStream_t>(stream_ptr),
+                                 e->block_warps, potential, far, e->refine_lists, e->refined,
+                                 static_cast<cudaStream_t>(stream_ptr),
                                  &launches);
     e->launches += launches;
     return err == cudaSuccess ? JFGPU_OK : JFGPU_ERROR_CUDA;
