@@ -33,21 +33,24 @@ METRIC = "events/s on 1 GB300, batched mixed-precision vs plain FP64 at <=1e-9 r
 WORKLOAD = dict(workload="lennard_jones_chains_4096x1024_cell_bounding", chains=4096, n=1024, density=0.8,
                 beta=1.0 / 1.2, cells_per_side=12, neighbor_layers=3, chain_time=2.0, far="cell_bounding",
                 jitter=0.05, estimator_points=10, estimator_prefactor=1.5)
-CELLS = WORKLOAD["cells_per_side"] ** 3
-# measured DRAM traffic of the chain kernel per committed event (ncu dram__bytes_read.sum + write.sum of one launch
-# of this workload divided by its events; see profiles/chains_kernel_lennard_jones_4096x1024.md); None if unknown
+NEAR_CELLS = (2 * WORKLOAD["neighbor_layers"] + 1) ** 3  # cells scanned for pair candidates per event
+CPU_SECONDS = 10.0  # wall time of the CPU baseline sample
+# DRAM traffic of the screening kernel per event: ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch of
+# this workload divided by the events of that launch (profiles/screen_kernel_lennard_jones_4096x1024.md); None if
+# not captured
 NCU_TRAFFIC_PER_EVENT = None
 
 
 def parse():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--steps", type=int, default=100)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     p.add_argument("--events", type=int, default=128, help="events per chain and step")
     p.add_argument("--chains", type=int, default=WORKLOAD["chains"])
     p.add_argument("--block-warps", type=int, default=0, help="warps per block (0 = autotune)")
+    p.add_argument("--groups", type=int, default=0, help="chain groups on streams of their own (0 = autotune)")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-fp64", action="store_true")
     return p.parse_args()
@@ -85,7 +88,7 @@ class ClockSampler:
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.QUERY,
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.thread = threading.Thread(target=self._read, daemon=True)
             self.thread.start()
@@ -135,11 +138,10 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-def cpu_reference_sample(threads, events_per_chain, chains_per_thread=1):
-    """The oracle (C restatement of the reference's event loop) on host threads; returns events/s."""
-    import concurrent.futures
+def cpu_chains(threads, pool, seed_offset=99):
+    """One oracle chain (C restatement of the reference's event loop) of the workload per host thread."""
     import oracle
-    specs, positions, length = make_workload(threads * chains_per_thread, seed_offset=99)
+    specs, positions, length = make_workload(threads, seed_offset=seed_offset)
     systems = []
     for c, spec in enumerate(specs):
         systems.append(oracle.make_system(
@@ -149,32 +151,49 @@ def cpu_reference_sample(threads, events_per_chain, chains_per_thread=1):
             potential=oracle.POT_LENNARD_JONES, far=oracle.FAR_CELL_BOUNDING,
             estimator_points=spec.estimator_points, estimator_prefactor=spec.estimator_prefactor,
             rng_key=oracle.chain_key(99, c)))
-    with concurrent.futures.ThreadPoolExecutor(max_workers=threads) as pool:
-        chains = list(pool.map(lambda i: oracle.Chain(systems[i], positions[i]), range(len(systems))))
-        start = time.perf_counter()
-        done = list(pool.map(lambda ch: ch.run(events_per_chain, record=False), chains))
-        elapsed = time.perf_counter() - start
-    return sum(done) / elapsed, sum(done), elapsed
+    return list(pool.map(lambda i: oracle.Chain(systems[i], positions[i]), range(len(systems))))
+
+
+def cpu_run(pool, chains, seconds, chunk=500):
+    """Every thread advances its chain in chunks of events until `seconds` have passed; returns (events, wall s)."""
+    def work(chain):
+        done, start = 0, time.perf_counter()
+        while time.perf_counter() - start < seconds:
+            done += chain.run(chunk, record=False)
+        return done
+    start = time.perf_counter()
+    done = sum(pool.map(work, chains))
+    return done, time.perf_counter() - start
+
+
+def host_threads():
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
 
 
 def reference_arm(args):
+    """The reference's CPU path on all host threads: the oracle's restatement of its event loop, one chain per
+    thread (the reference is single-threaded), each step a bounded time sample of the same workload."""
+    import concurrent.futures
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    threads = os.cpu_count() or 1
-    events = 60
-    values = []
-    for _ in range(args.warmup):
-        cpu_reference_sample(threads, 10)
-    total_events, total_time = 0, 0.0
-    for _ in range(args.steps):
-        rate, done, elapsed = cpu_reference_sample(threads, events)
-        values.append(rate)
-        total_events += done
-        total_time += elapsed
+    threads = host_threads()
+    seconds = 3.0
+    with concurrent.futures.ThreadPoolExecutor(max_workers=threads) as pool:
+        chains = cpu_chains(threads, pool)
+        for _ in range(args.warmup):
+            cpu_run(pool, chains, 0.5)
+        total_events, total_time = 0, 0.0
+        for _ in range(args.steps):
+            done, elapsed = cpu_run(pool, chains, seconds)
+            total_events += done
+            total_time += elapsed
     value = total_events / total_time
     config = dict(WORKLOAD)
-    config["sample"] = "%d chains x %d events per step" % (threads, events)
+    config["sample"] = "%d chains (one per host thread) x %.0f s of events per step" % (threads, seconds)
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "events/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * total_time / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
@@ -185,19 +204,23 @@ def reference_arm(args):
     print(json.dumps(line))
 
 
-def autotune(batch, events):
-    """Pick warps per block of the mixed kernel by a short timed sweep."""
+def autotune(batch, events, warps_choices=(2, 4, 8), group_choices=(1, 2, 4)):
+    """Pick warps per block and chain groups of the mixed mode by a short timed sweep (the sweep's events also
+    warm the chains up)."""
     import torch
-    best, best_time = 4, math.inf
-    for warps in (1, 2, 4, 8):
-        batch.set_block_warps(warps)
-        torch.cuda.synchronize()
-        start = time.perf_counter()
-        batch.run(events, mode="mixed")
-        elapsed = time.perf_counter() - start
-        if elapsed < best_time:
-            best, best_time = warps, elapsed
-    batch.set_block_warps(best)
+    best, best_time = (4, 1), math.inf
+    for warps in warps_choices:
+        for groups in group_choices:
+            batch.set_block_warps(warps)
+            batch.set_groups(groups)
+            torch.cuda.synchronize()
+            start = time.perf_counter()
+            batch.run(events, mode="mixed")
+            elapsed = time.perf_counter() - start
+            if elapsed < best_time:
+                best, best_time = (warps, groups), elapsed
+    batch.set_block_warps(best[0])
+    batch.set_groups(best[1])
     return best
 
 
@@ -216,31 +239,36 @@ def gpu_arm(args):
     specs, positions, length = make_workload(args.chains, seed_offset=rank)
     batch = ChainBatch(specs, positions, seed=1000 + rank, device="cuda:%d" % local)
     stream = torch.cuda.current_stream(device)
-    warps = args.block_warps or autotune(batch, 8)
+    if args.block_warps and args.groups:
+        warps, groups = args.block_warps, args.groups
+    else:
+        warps, groups = autotune(batch, 8, (args.block_warps,) if args.block_warps else (2, 4, 8),
+                                 (args.groups,) if args.groups else (1, 2, 4))
     batch.set_block_warps(warps)
+    batch.set_groups(groups)
+    # per-kernel CUDA events on the launching streams stay on through the warm-up and the timed region
+    batch.set_timing(True)
     for _ in range(args.warmup):
         batch.run(args.events, mode="mixed")
     batch.check_status()
+    batch.kernel_times(reset=True)
     state0 = batch.state()
     launches0 = batch.launch_count()
     if world > 1:
         dist.barrier()
     torch.cuda.synchronize(device)
-    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     with ClockSampler(local) as clocks:
         begin = torch.cuda.Event(enable_timing=True)
         finish = torch.cuda.Event(enable_timing=True)
         begin.record(stream)
         for s in range(args.steps):
-            starts[s].record(stream)
             batch.run(args.events, mode="mixed", sync=False)
-            ends[s].record(stream)
         finish.record(stream)
         torch.cuda.synchronize(device)
     elapsed_ms = begin.elapsed_time(finish)
     launches = batch.launch_count() - launches0
-    kernel_ms = [a.elapsed_time(b) for a, b in zip(starts, ends)]
+    kernel_times = batch.kernel_times(reset=True)
+    batch.set_timing(False)
     batch.check_status()
     state1 = batch.state()
     events_done = int(state1["events"].sum() - state0["events"].sum())
@@ -306,28 +334,41 @@ def gpu_arm(args):
             dist.destroy_process_group()
         return
 
-    # roofline of the chain kernel: algorithmic bytes per event (cell scan of every cell, FP32 neighbour
-    # positions and identifiers of the pair candidates, active position write, cell index and time)
-    events_per_launch = args.chains * args.events
+    # roofline of the screening kernel, which reads the neighbourhood: algorithmic bytes per event (occupancy of the
+    # nearby cells, FP32 position and identifier of every pair candidate, active position write, cell index and time)
+    # times the events of one launch, over its mean CUDA-event duration on its stream in the timed region
+    screen = kernel_times["screen"]
+    screen_launches = max(screen["launches"], 1)
+    events_per_launch = events_done / screen_launches
     nb = candidates / max(events_done, 1)
-    bytes_per_event = 4 * CELLS + 12 * nb + 4 * nb + 32
-    kernel_s = float(np.mean(kernel_ms)) / 1000.0
-    achieved = bytes_per_event * events_per_launch / kernel_s / 1e9
+    bytes_per_event = 4 * NEAR_CELLS + 12 * nb + 4 * nb + 32
+    screen_s = screen["ms"] / screen_launches / 1000.0
+    achieved = bytes_per_event * events_per_launch / screen_s / 1e9
     peak, peak_kind = measured_peaks()
     traffic = None if NCU_TRAFFIC_PER_EVENT is None else NCU_TRAFFIC_PER_EVENT * events_per_launch
+    total_kernel_ms = sum(v["ms"] for v in kernel_times.values()) or 1.0
+    kernels = {name: {"launches": v["launches"], "ms_per_launch": v["ms"] / max(v["launches"], 1),
+                      "share": v["ms"] / total_kernel_ms}
+               for name, v in kernel_times.items() if v["launches"]}
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                "traffic": traffic, "peak_source": peak_kind, "bytes_per_event": bytes_per_event,
-                "neighbours_per_event": nb, "refined_per_event": refined / max(events_done, 1),
-                "fallback_events": fallbacks, "kernel": "jf::chains_kernel<1>"}
+                "traffic": traffic, "peak_source": peak_kind, "kernel": "jf::screen_kernel<1, 2>",
+                "bytes_per_event": bytes_per_event, "events_per_launch": events_per_launch,
+                "ms_per_launch": screen_s * 1000.0, "neighbours_per_event": nb,
+                "refined_per_event": refined / max(events_done, 1), "fallback_events": fallbacks,
+                "kernels": kernels}
     cpu = None
     if not args.no_cpu_baseline and world == 1:
-        threads = os.cpu_count() or 1
-        rate, done, elapsed = cpu_reference_sample(threads, 40)
-        cpu = {"value": rate, "unit": "events/s", "cores": threads, "kind": "port",
-               "sample": "%d chains x 40 events of the same workload, one chain per thread (%.1f s)"
-                         % (threads, elapsed)}
+        import concurrent.futures
+        threads = host_threads()
+        with concurrent.futures.ThreadPoolExecutor(max_workers=threads) as pool:
+            chains = cpu_chains(threads, pool)
+            cpu_run(pool, chains, 0.5)
+            done, elapsed = cpu_run(pool, chains, CPU_SECONDS)
+        cpu = {"value": done / elapsed, "unit": "events/s", "cores": threads, "kind": "port",
+               "sample": "%d chains of the workload (one per host thread), %d events in %.1f s"
+                         % (threads, done, elapsed)}
     config = dict(WORKLOAD)
-    config.update(chains=args.chains, events_per_chain_per_step=args.events, block_warps=warps,
+    config.update(chains=args.chains, events_per_chain_per_step=args.events, block_warps=warps, chain_groups=groups,
                   l2="inputs larger than L2 (working set %.0f MB)" % (sum(
                       t.numel() * t.element_size() for t in batch.state_tensors()) / 1e6),
                   parallelism="replicas" if world > 1 else "single GPU")

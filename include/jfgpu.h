@@ -232,11 +232,31 @@ int jfgpu_chains_run(JfgpuEngine *engine, const JfgpuBuffers *buffers, int64_t f
                      int64_t max_events, double stop_q, double stop_r, int32_t mode, JfgpuEvent *log,
                      int64_t log_capacity, void *stream);
 
-/* Autotuned launch shape of the mixed mode: warps per block used by jfgpu_chains_run (1..16). */
+/* Autotuned launch shape of the mixed mode: warps per block used by jfgpu_chains_run (1..8). */
 int jfgpu_chains_set_block_warps(JfgpuEngine *engine, int32_t warps_per_block);
+
+/* Chain groups of the mixed mode: the chains of one jfgpu_chains_run call are split into `groups` contiguous
+ * groups (1..8) whose event rounds run on streams of their own, forked from and joined back into the caller's
+ * stream, so that one group's FP64 re-solves overlap another group's FP32 screening.  Default 1. */
+int jfgpu_chains_set_groups(JfgpuEngine *engine, int32_t groups);
 
 /* Kernel launches issued by the library since the engine was created (all kernels of this library). */
 int64_t jfgpu_engine_launch_count(const JfgpuEngine *engine);
+
+/* kernel kinds of jfgpu_engine_kernel_times */
+#define JFGPU_KERNEL_SCREEN 0          /* FP32 screening of every candidate (one warp per chain) */
+#define JFGPU_KERNEL_REFINE 1          /* FP64 re-solve of the listed near-winners */
+#define JFGPU_KERNEL_RESOLVE 2         /* single candidates, argmin, commit and occupancy update */
+#define JFGPU_KERNEL_CHAINS 3          /* the FP64 event loop of JFGPU_MODE_EXACT */
+#define JFGPU_KERNEL_INIT 4            /* chain start */
+#define JFGPU_KERNEL_KINDS 5
+
+/* Per-kernel device time.  While timing is on, the chain launches of jfgpu_chains_init / jfgpu_chains_run are
+ * bracketed by CUDA events on the stream they are launched on.  jfgpu_engine_kernel_times waits for those events
+ * and returns, per kernel kind, the milliseconds and launches accumulated since the last reset (arrays of
+ * JFGPU_KERNEL_KINDS entries; reset != 0 clears the totals after reading). */
+int jfgpu_engine_set_timing(JfgpuEngine *engine, int32_t enable);
+int jfgpu_engine_kernel_times(JfgpuEngine *engine, double *milliseconds, int64_t *launches, int32_t reset);
 
 const char *jfgpu_error_string(int code);
 int jfgpu_version(void);

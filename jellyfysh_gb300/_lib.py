@@ -108,6 +108,9 @@ SIGNATURES = {
     "jfgpu_chains_run": (ctypes.c_int, [_P, ctypes.POINTER(Buffers), _I64, _I64, _I64, _D, _D, _I32, _P, _I64,
                                         _P]),
     "jfgpu_chains_set_block_warps": (ctypes.c_int, [_P, _I32]),
+    "jfgpu_chains_set_groups": (ctypes.c_int, [_P, _I32]),
+    "jfgpu_engine_set_timing": (ctypes.c_int, [_P, _I32]),
+    "jfgpu_engine_kernel_times": (ctypes.c_int, [_P, _P, _P, _I32]),
     "jfgpu_engine_launch_count": (ctypes.c_int64, [_P]),
     "jfgpu_error_string": (ctypes.c_char_p, [ctypes.c_int]),
     "jfgpu_version": (ctypes.c_int, []),

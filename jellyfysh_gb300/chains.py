@@ -36,6 +36,8 @@ POTENTIALS = {"hard_sphere": _lib.POT_HARD_SPHERE, "lennard_jones": _lib.POT_LEN
               "coulomb": _lib.POT_COULOMB}
 FAR_FIELDS = {"none": _lib.FAR_NONE, "cell_veto": _lib.FAR_CELL_VETO, "cell_bounding": _lib.FAR_CELL_BOUNDING}
 MODES = {"exact": _lib.MODE_EXACT, "mixed": _lib.MODE_MIXED}
+# kernel kinds of jfgpu_engine_kernel_times, in JFGPU_KERNEL_* order
+KERNEL_KINDS = ("screen", "refine", "resolve", "chains", "init")
 
 EVENT_DTYPE = np.dtype([("kind", np.int32), ("moved", np.int32), ("target", np.int32), ("new_active", np.int32),
                         ("new_direction", np.int32), ("accepted", np.int32), ("time_q", np.float64),
@@ -180,8 +182,25 @@ class ChainBatch:
     def set_block_warps(self, warps: int) -> None:
         _lib.check(self.lib.jfgpu_chains_set_block_warps(self._engine, int(warps)), "jfgpu_chains_set_block_warps")
 
+    def set_groups(self, groups: int) -> None:
+        """Split the chains of every mixed-mode run into ``groups`` groups on streams of their own."""
+        with self._torch.cuda.device(self.device):
+            _lib.check(self.lib.jfgpu_chains_set_groups(self._engine, int(groups)), "jfgpu_chains_set_groups")
+
     def launch_count(self) -> int:
         return int(self.lib.jfgpu_engine_launch_count(self._engine))
+
+    def set_timing(self, enable: bool) -> None:
+        """Bracket every chain launch by CUDA events on its stream (read back by kernel_times)."""
+        _lib.check(self.lib.jfgpu_engine_set_timing(self._engine, 1 if enable else 0), "jfgpu_engine_set_timing")
+
+    def kernel_times(self, reset: bool = True) -> dict:
+        """Device milliseconds and launches per kernel kind since the last reset (waits for the events)."""
+        ms = (ctypes.c_double * len(KERNEL_KINDS))()
+        n = (ctypes.c_int64 * len(KERNEL_KINDS))()
+        _lib.check(self.lib.jfgpu_engine_kernel_times(self._engine, ms, n, 1 if reset else 0),
+                   "jfgpu_engine_kernel_times")
+        return {name: {"ms": ms[k], "launches": int(n[k])} for k, name in enumerate(KERNEL_KINDS)}
 
     def run(self, max_events: int, stop_time: Optional[float] = None, mode: str = "mixed", first: int = 0,
             count: Optional[int] = None, log_capacity: int = 0, sync: bool = True):

@@ -758,13 +758,36 @@ constexpr int kRefineMax = 28;
 constexpr int32_t kListOverflow = 1;
 constexpr int32_t kListSkip = 2;
 
+// list entry: target in bits 0-19, screening path in bits 20-23, bit 30 for a far (cell-bounding) candidate
+constexpr int32_t kCodeFar = 1 << 30;
+__device__ inline int32_t make_code(int target, int path, bool far) {
+    return target | (path << 20) | (far ? kCodeFar : 0);
+}
+__device__ inline int code_target(int32_t code) { return code & 0xFFFFF; }
+__device__ inline int code_path(int32_t code) { return (code >> 20) & 0xF; }
+__device__ inline bool code_far(int32_t code) { return (code & kCodeFar) != 0; }
+
 struct RefineList {
     int32_t count, flags, screened, pad;
-    int32_t code[kRefineMax];  // target, bit 30 set for a far (cell-bounding) candidate
+    int32_t code[kRefineMax];
+};
+
+// FP64 re-solves of the first kRefineSlots entries of every refine list, one thread per entry; the resolve kernel
+// takes the earliest of them (and solves any further entry itself)
+constexpr int kRefineSlots = 2;
+
+// Refine queue of a chain group: per screening path, the entries (local chain * kRefineSlots + slot) to re-solve.
+// counts[kPaths] sit in the group's header; entries[path][...] use the slice [lo, hi) * kRefineSlots of the group's
+// chains, so that groups on different streams never share a word.
+struct RefineQueue {
+    int32_t *counts;   // [kPaths], zeroed by the resolve kernel of the round
+    int32_t *entries;  // [kPaths][stride], offset to the group's slice
+    long long stride;  // n_chains * kRefineSlots
 };
 
 template <int POT, int FAR>
-__global__ void __launch_bounds__(256, 4) screen_kernel(RunArgs A, RefineList *lists, long long round) {
+__global__ void __launch_bounds__(256, 4) screen_kernel(RunArgs A, RefineList *lists, RefineQueue queue,
+                                                        long long round) {
     const int warp = threadIdx.x >> 5;
     const int lane = threadIdx.x & 31;
     const long long local = (long long)blockIdx.x * (blockDim.x >> 5) + warp;
@@ -834,14 +857,18 @@ __global__ void __launch_bounds__(256, 4) screen_kernel(RunArgs A, RefineList *l
         bool flag = false;
         separation32(pa32, pj, ch.L32, ch.half32, margin, sv, flag);
         float t;
+        int path = kPathHardSphere;
         if (potential_of<POT>(ch) == JFGPU_POT_HARD_SPHERE) {
             t = hs_screen(ch.diameter_sq32, d, speed32, sv, margin, flag);
         } else {
             const float du = expovariate32(draw_at(pair_base, (uint32_t)j), inv_beta32, flag);
-            t = lj_screen(lj32, d, speed32, sv, du, margin, flag);
+            t = lj_screen(lj32, d, speed32, sv, du, margin, flag, path);
         }
-        if (flag) t = -1.0f;
-        if (!isinf(t)) topk_insert(key, code, t, j);
+        if (flag) {
+            t = -1.0f;
+            path = kPathFlagged;
+        }
+        if (!isinf(t)) topk_insert(key, code, t, make_code(j, path, false));
     };
     for_each_near(A, ch, occ_cell, lane, screen_pair);
     for (int i = lane; i < n_surplus; i += 32) screen_pair(A.surplus[ch.pos_off + i]);
@@ -863,7 +890,7 @@ __global__ void __launch_bounds__(256, 4) screen_kernel(RunArgs A, RefineList *l
                           const float du = expovariate32(bits, inv_beta32, flag);
                           float t = (du / rate) / speed32;
                           if (flag) t = -1.0f;
-                          if (!isinf(t)) topk_insert(key, code, t, j | (1 << 30));
+                          if (!isinf(t)) topk_insert(key, code, t, make_code(j, kPathFar, true));
                       });
         base = fminf(base, warp_min_float(lane_min_unflagged(key)));
     }
@@ -871,26 +898,39 @@ __global__ void __launch_bounds__(256, 4) screen_kernel(RunArgs A, RefineList *l
     // compaction of the candidates inside the threshold into the chain's refine list
     int overflow = (code[kTopK - 1] >= 0 && key[kTopK - 1] <= threshold) ? 1 : 0;
     int total = 0;
+    static_assert(kRefineSlots == 2, "the queued entries of a lane are held in two registers");
+    int queued0 = -1, queued1 = -1;  // the lane's entries at list offsets 0 and 1, if any (one lane may hold both)
 #pragma unroll
     for (int i = 0; i < kTopK; ++i) {
         const bool take = code[i] >= 0 && key[i] <= threshold;
         const unsigned mask = __ballot_sync(kFull, take);
         const int offset = total + __popc(mask & ((1u << lane) - 1u));
         if (take && offset < kRefineMax) list.code[offset] = code[i];
+        if (take && offset == 0) queued0 = code[i];
+        if (take && offset == 1) queued1 = code[i];
         total += __popc(mask);
     }
-    overflow = warp_max_int(overflow);
+    overflow = warp_max_int(overflow) || total > kRefineMax;
     const int screened = warp_sum_int(count);
     if (lane == 0) {
         list.count = total < kRefineMax ? total : kRefineMax;
-        list.flags = (overflow || total > kRefineMax) ? kListOverflow : 0;
+        list.flags = overflow ? kListOverflow : 0;
         list.screened = screened;
     }
+    // the entries at the first kRefineSlots offsets go to the queues of their paths
+    if (!overflow) {
+        if (queued0 >= 0) {
+            const int path = code_path(queued0);
+            const int at = atomicAdd(queue.counts + path, 1);
+            queue.entries[path * queue.stride + at] = (int32_t)(local * kRefineSlots);
+        }
+        if (queued1 >= 0) {
+            const int path = code_path(queued1);
+            const int at = atomicAdd(queue.counts + path, 1);
+            queue.entries[path * queue.stride + at] = (int32_t)(local * kRefineSlots + 1);
+        }
+    }
 }
-
-// FP64 re-solves of the first kRefineSlots entries of every refine list, one thread per entry; the resolve kernel
-// takes the earliest of them (and solves any further entry itself)
-constexpr int kRefineSlots = 2;
 
 struct Refined {
     double q, r, rate;
@@ -918,17 +958,32 @@ __device__ inline void load_lifting(const JfgpuChainState &g, const RunArgs &A, 
     load_pos(A, ch, w.active, w.pa);
 }
 
+// The queued entries by path: each path's range is padded to whole warps, so that the 32 threads of a warp re-solve
+// candidates that take the same branch of the case analysis (up to the rare FP32/FP64 disagreement).
 template <int POT, int FAR>
 __global__ void __launch_bounds__(64) refine_kernel(RunArgs A, const RefineList *lists, Refined *refined,
-                                                     long long round) {
+                                                     RefineQueue queue, long long round) {
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    const long long local = t / kRefineSlots;
-    const int slot = (int)(t % kRefineSlots);
-    if (local >= A.count) return;
+    long long start = 0;
+    int path = -1;
+    long long index = 0;
+#pragma unroll
+    for (int k = 0; k < kPaths; ++k) {
+        const long long n = queue.counts[k];
+        const long long padded = (n + 31) & ~31LL;
+        if (path < 0 && t < start + padded) {
+            path = k;
+            index = t - start;
+            if (index >= n) return;
+        }
+        start += padded;
+    }
+    if (path < 0) return;
+    const int entry = queue.entries[path * queue.stride + index];
+    const long long local = entry / kRefineSlots;
+    const int slot = entry % kRefineSlots;
     Refined &out = refined[local * kRefineSlots + slot];
-    out.kind = 1 << 30;
     const RefineList &list = lists[local];
-    if ((list.flags & (kListSkip | kListOverflow)) || slot >= list.count) return;
     const long long c = A.first_chain + local;
     const ChainDev &ch = A.view.chains[c];
     const SpeciesDev &sp = A.view.species[ch.species];
@@ -936,9 +991,9 @@ __global__ void __launch_bounds__(64) refine_kernel(RunArgs A, const RefineList 
     load_lifting(A.state[c], A, ch, w);
     Cand best = cand_none();
     const int code = list.code[slot];
-    const int j = code & ((1 << 30) - 1);
-    const int st = (code & (1 << 30)) ? exact_cell_bounding(A, ch, sp, w, j, w.occ_cell, w.events, best)
-                                      : exact_pair<POT>(A, ch, sp, w, j, w.events, best);
+    const int j = code_target(code);
+    const int st = code_far(code) ? exact_cell_bounding(A, ch, sp, w, j, w.occ_cell, w.events, best)
+                                  : exact_pair<POT>(A, ch, sp, w, j, w.events, best);
     out.q = best.q;
     out.r = best.r;
     out.rate = best.rate;
@@ -980,8 +1035,9 @@ __device__ __noinline__ int exact_serial(const RunArgs &A, const ChainDev &ch, c
 
 template <int POT, int FAR>
 __global__ void __launch_bounds__(32) resolve_kernel(RunArgs A, const RefineList *lists, const Refined *refined,
-                                                     long long round) {
+                                                     RefineQueue queue, long long round) {
     const long long local = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (local < kPaths) queue.counts[local] = 0;  // the refine kernel of this round has consumed the queue
     if (local >= A.count) return;
     const long long c = A.first_chain + local;
     const ChainDev &ch = A.view.chains[c];
@@ -1018,9 +1074,9 @@ __global__ void __launch_bounds__(32) resolve_kernel(RunArgs A, const RefineList
             }
             for (int i = kRefineSlots; i < list.count && !st; ++i) {
                 const int code = list.code[i];
-                const int j = code & ((1 << 30) - 1);
-                st = (code & (1 << 30)) ? exact_cell_bounding(A, ch, sp, w, j, w.occ_cell, w.events, best)
-                                        : exact_pair<POT>(A, ch, sp, w, j, w.events, best);
+                const int j = code_target(code);
+                st = code_far(code) ? exact_cell_bounding(A, ch, sp, w, j, w.occ_cell, w.events, best)
+                                    : exact_pair<POT>(A, ch, sp, w, j, w.events, best);
             }
         }
     }
@@ -1236,6 +1292,10 @@ __global__ void init_kernel(EngineView view, long long n_chains, double *positio
 
 size_t refine_list_bytes() { return sizeof(RefineList); }
 size_t refined_bytes() { return sizeof(Refined) * kRefineSlots; }
+// refine queues of up to 8 chain groups: 32 counters per group, then kPaths slices of n_chains * kRefineSlots entries
+size_t refine_queue_bytes(long long n_chains) {
+    return sizeof(int32_t) * (8 * 32 + (size_t)kPaths * (size_t)n_chains * kRefineSlots);
+}
 
 }  // namespace jf
 
@@ -1244,34 +1304,62 @@ size_t refined_bytes() { return sizeof(Refined) * kRefineSlots; }
 // ---------------------------------------------------------------------------------------------------------------
 namespace jf {
 
-cudaError_t launch_init(const EngineView &view, long long n_chains, const JfgpuBuffers &b, cudaStream_t stream) {
+cudaError_t launch_init(const EngineView &view, long long n_chains, const JfgpuBuffers &b, const LaunchPlan &plan) {
     const int warps = 4;
     long long blocks = (n_chains + warps - 1) / warps;
-    init_kernel<<<(unsigned)blocks, warps * 32, 0, stream>>>(view, n_chains, b.positions,
-                                                              reinterpret_cast<float4 *>(b.positions32), b.charges,
-                                                              b.occupancy, b.surplus, b.roles, b.state);
+    if (plan.clock) plan.clock->begin(plan.stream);
+    init_kernel<<<(unsigned)blocks, warps * 32, 0, plan.stream>>>(view, n_chains, b.positions,
+                                                                   reinterpret_cast<float4 *>(b.positions32),
+                                                                   b.charges, b.occupancy, b.surplus, b.roles,
+                                                                   b.state);
+    if (plan.clock) plan.clock->end(plan.stream, JFGPU_KERNEL_INIT);
     return cudaGetLastError();
 }
 
+// one group of chains [A.first_chain, A.first_chain + A.count) with its slices of the refine lists
+struct GroupLaunch {
+    RunArgs args;
+    RefineList *lists;
+    Refined *refined;
+    RefineQueue queue;
+    cudaStream_t stream;
+};
+
+// The event rounds of the mixed mode: per round the screening, the FP64 re-solves and the resolve kernel of every
+// group, issued round by round so that the groups' streams advance together.
 template <int POT, int FAR>
-static void launch_mixed_rounds(const RunArgs &A, void *lists, void *refined, long long rounds, int warps,
-                                cudaStream_t stream) {
-    const long long screen_blocks = (A.count + warps - 1) / warps;
-    const long long refine_blocks = (A.count * kRefineSlots + 63) / 64;
-    const long long resolve_blocks = (A.count + 31) / 32;  // one warp per block: the resolve work spreads over the SMs
-    RefineList *l = static_cast<RefineList *>(lists);
-    Refined *f = static_cast<Refined *>(refined);
+static long long launch_mixed_rounds(const GroupLaunch *groups, int n_groups, long long rounds, int warps,
+                                     KernelClock *clock) {
+    long long launches = 0;
+    if (clock)
+        for (int g = 0; g < n_groups; ++g) clock->begin(groups[g].stream);
     for (long long r = 0; r < rounds; ++r) {
-        screen_kernel<POT, FAR><<<(unsigned)screen_blocks, warps * 32, 0, stream>>>(A, l, r);
-        refine_kernel<POT, FAR><<<(unsigned)refine_blocks, 64, 0, stream>>>(A, l, f, r);
-        resolve_kernel<POT, FAR><<<(unsigned)resolve_blocks, 32, 0, stream>>>(A, l, f, r);
+        for (int g = 0; g < n_groups; ++g) {
+            const GroupLaunch &G = groups[g];
+            const long long count = G.args.count;
+            const long long screen_blocks = (count + warps - 1) / warps;
+            // every queued entry plus the padding of each path to whole warps
+            const long long refine_blocks = (count * kRefineSlots + kPaths * 31 + 63) / 64;
+            const long long resolve_blocks = (count + 31) / 32;  // one warp per block: resolve spreads over the SMs
+            screen_kernel<POT, FAR><<<(unsigned)screen_blocks, warps * 32, 0, G.stream>>>(G.args, G.lists, G.queue,
+                                                                                         r);
+            if (clock) clock->end(G.stream, JFGPU_KERNEL_SCREEN);
+            refine_kernel<POT, FAR><<<(unsigned)refine_blocks, 64, 0, G.stream>>>(G.args, G.lists, G.refined, G.queue,
+                                                                                 r);
+            if (clock) clock->end(G.stream, JFGPU_KERNEL_REFINE);
+            resolve_kernel<POT, FAR><<<(unsigned)resolve_blocks, 32, 0, G.stream>>>(G.args, G.lists, G.refined,
+                                                                                   G.queue, r);
+            if (clock) clock->end(G.stream, JFGPU_KERNEL_RESOLVE);
+            launches += 3;
+        }
     }
+    return launches;
 }
 
 cudaError_t launch_run(const EngineView &view, const JfgpuBuffers &b, long long first, long long count,
                        long long max_events, double stop_q, double stop_r, int mode, JfgpuEvent *log,
-                       long long log_capacity, int warps_per_block, int uniform_potential, int uniform_far,
-                       void *lists, void *refined, cudaStream_t stream, long long *launches) {
+                       long long log_capacity, int uniform_potential, int uniform_far, void *lists, void *refined,
+                       void *queue, long long n_chains, const LaunchPlan &plan, long long *launches) {
     RunArgs A;
     A.view = view;
     A.positions = b.positions;
@@ -1289,25 +1377,67 @@ cudaError_t launch_run(const EngineView &view, const JfgpuBuffers &b, long long 
     A.stop_q = stop_q;
     A.stop_r = stop_r;
     A.has_stop = isinf(stop_q) ? 0 : 1;
-    int warps = warps_per_block;
+    int warps = plan.warps;
     if (warps < 1) warps = 1;
     if (warps > 8) warps = 8;
     if (count < warps) warps = (int)count;
     if (mode == JFGPU_MODE_MIXED) {
+        // groups of at least one block of warps each; the event log stays on the caller's stream
+        int n_groups = plan.groups;
+        if (log || !plan.group_streams) n_groups = 1;
+        if (n_groups > 8) n_groups = 8;
+        while (n_groups > 1 && count < (long long)n_groups * 32) --n_groups;
+        GroupLaunch groups[8];
+        const long long chunk = (count + n_groups - 1) / n_groups;
+        int used = 0;
+        for (int g = 0; g < n_groups; ++g) {
+            const long long lo = g * chunk, hi = count < lo + chunk ? count : lo + chunk;
+            if (hi <= lo) break;
+            GroupLaunch &G = groups[used++];
+            G.args = A;
+            G.args.first_chain = first + lo;
+            G.args.count = hi - lo;
+            G.args.log = nullptr;
+            G.lists = static_cast<RefineList *>(lists) + lo;
+            G.refined = static_cast<Refined *>(refined) + lo * kRefineSlots;
+            G.queue.counts = static_cast<int32_t *>(queue) + 32 * g;
+            G.queue.entries = static_cast<int32_t *>(queue) + 8 * 32 + (first + lo) * kRefineSlots;
+            G.queue.stride = n_chains * kRefineSlots;
+            G.stream = n_groups > 1 ? plan.group_streams[g] : plan.stream;
+        }
+        // counters start at zero in every run (a run that stopped on an error may have left some behind)
+        cudaMemsetAsync(queue, 0, sizeof(int32_t) * 8 * 32, plan.stream);
+        if (n_groups == 1) groups[0].args.log = log;
+        if (used > 1) {
+            cudaEventRecord(plan.fork, plan.stream);
+            for (int g = 0; g < used; ++g) cudaStreamWaitEvent(groups[g].stream, plan.fork, 0);
+        }
         // kernels specialised for the common homogeneous batches carry only their potential's code
+        long long issued;
         if (uniform_potential == JFGPU_POT_LENNARD_JONES && uniform_far == JFGPU_FAR_CELL_BOUNDING)
-            launch_mixed_rounds<JFGPU_POT_LENNARD_JONES, JFGPU_FAR_CELL_BOUNDING>(A, lists, refined, max_events, warps, stream);
+            issued = launch_mixed_rounds<JFGPU_POT_LENNARD_JONES, JFGPU_FAR_CELL_BOUNDING>(groups, used, max_events,
+                                                                                          warps, plan.clock);
         else if (uniform_potential == JFGPU_POT_LENNARD_JONES && uniform_far == JFGPU_FAR_CELL_VETO)
-            launch_mixed_rounds<JFGPU_POT_LENNARD_JONES, JFGPU_FAR_CELL_VETO>(A, lists, refined, max_events, warps, stream);
+            issued = launch_mixed_rounds<JFGPU_POT_LENNARD_JONES, JFGPU_FAR_CELL_VETO>(groups, used, max_events, warps,
+                                                                                      plan.clock);
         else if (uniform_potential == JFGPU_POT_HARD_SPHERE && uniform_far == JFGPU_FAR_NONE)
-            launch_mixed_rounds<JFGPU_POT_HARD_SPHERE, JFGPU_FAR_NONE>(A, lists, refined, max_events, warps, stream);
+            issued = launch_mixed_rounds<JFGPU_POT_HARD_SPHERE, JFGPU_FAR_NONE>(groups, used, max_events, warps,
+                                                                               plan.clock);
         else
-            launch_mixed_rounds<-1, -1>(A, lists, refined, max_events, warps, stream);
-        *launches += 3 * max_events;
+            issued = launch_mixed_rounds<-1, -1>(groups, used, max_events, warps, plan.clock);
+        if (used > 1) {
+            for (int g = 0; g < used; ++g) {
+                cudaEventRecord(plan.join[g], groups[g].stream);
+                cudaStreamWaitEvent(plan.stream, plan.join[g], 0);
+            }
+        }
+        *launches += issued;
     } else {
         const long long blocks = (count + warps - 1) / warps;
         const size_t smem = sizeof(WarpState) * warps;
-        chains_kernel<-1, -1><<<(unsigned)blocks, warps * 32, smem, stream>>>(A);
+        if (plan.clock) plan.clock->begin(plan.stream);
+        chains_kernel<-1, -1><<<(unsigned)blocks, warps * 32, smem, plan.stream>>>(A);
+        if (plan.clock) plan.clock->end(plan.stream, JFGPU_KERNEL_CHAINS);
         *launches += 1;
     }
     return cudaGetLastError();

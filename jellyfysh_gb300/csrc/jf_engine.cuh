@@ -67,4 +67,22 @@ struct EngineView {
     const int16_t *tra;  // translate index along one axis, [a * m + b]
 };
 
+// host side of a run: CUDA events around the launches when per-kernel timing is on
+struct KernelClock {
+    virtual ~KernelClock() {}
+    virtual void begin(cudaStream_t stream) = 0;            // an event before the next launch on the stream
+    virtual void end(cudaStream_t stream, int kind) = 0;    // an event after a launch of this JFGPU_KERNEL_* kind
+};
+
+// streams of a run: the caller's stream, or chain groups on streams of their own forked from it
+struct LaunchPlan {
+    cudaStream_t stream = nullptr;
+    int warps = 4;                          // warps per block of the screening and FP64 kernels
+    int groups = 1;                         // chain groups of the mixed mode
+    cudaStream_t *group_streams = nullptr;  // [groups] when groups > 1
+    cudaEvent_t fork = nullptr;             // recorded on the caller's stream, waited for by every group
+    cudaEvent_t *join = nullptr;            // [groups] recorded by every group, waited for by the caller's stream
+    KernelClock *clock = nullptr;           // null when timing is off
+};
+
 }  // namespace jf

@@ -21,13 +21,14 @@
 #include "jf_engine.cuh"
 
 namespace jf {
-cudaError_t launch_init(const EngineView &view, long long n_chains, const JfgpuBuffers &b, cudaStream_t stream);
+cudaError_t launch_init(const EngineView &view, long long n_chains, const JfgpuBuffers &b, const LaunchPlan &plan);
 cudaError_t launch_run(const EngineView &view, const JfgpuBuffers &b, long long first, long long count,
                        long long max_events, double stop_q, double stop_r, int mode, JfgpuEvent *log,
-                       long long log_capacity, int warps_per_block, int uniform_potential, int uniform_far,
-                       void *lists, void *refined, cudaStream_t stream, long long *launches);
+                       long long log_capacity, int uniform_potential, int uniform_far, void *lists, void *refined,
+                       void *queue, long long n_chains, const LaunchPlan &plan, long long *launches);
 size_t refine_list_bytes();
 size_t refined_bytes();
+size_t refine_queue_bytes(long long n_chains);
 }  // namespace jf
 
 using namespace jf;
@@ -36,6 +37,70 @@ struct HostWalker {
     std::vector<int32_t> first_item, second_item;
     std::vector<double> first_rate;
     double total_rate = 0.0, mean_rate = 0.0;
+};
+
+// CUDA events around the launches: one event before the first launch on a stream, one after every launch, so
+// that a launch's time is the interval between its stream's previous event and its own
+class EventClock : public KernelClock {
+  public:
+    ~EventClock() override {
+        for (cudaEvent_t ev : pool_) cudaEventDestroy(ev);
+    }
+    void begin(cudaStream_t stream) override {
+        int i = next();
+        if (i < 0) return;
+        cudaEventRecord(pool_[i], stream);
+        last_[stream] = i;
+    }
+    void end(cudaStream_t stream, int kind) override {
+        auto it = last_.find(stream);
+        int i = next();
+        if (i < 0 || it == last_.end()) return;
+        cudaEventRecord(pool_[i], stream);
+        marks_.push_back({kind, it->second, i});
+        it->second = i;
+    }
+    // waits for the recorded events and adds their intervals to the totals
+    int collect() {
+        int error = JFGPU_OK;
+        for (const Mark &m : marks_) {
+            float ms = 0.0f;
+            if (cudaEventSynchronize(pool_[m.after]) != cudaSuccess ||
+                cudaEventElapsedTime(&ms, pool_[m.before], pool_[m.after]) != cudaSuccess) {
+                error = JFGPU_ERROR_CUDA;
+                continue;
+            }
+            milliseconds[m.kind] += ms;
+            launches[m.kind] += 1;
+        }
+        marks_.clear();
+        last_.clear();
+        used_ = 0;
+        return failed_ ? JFGPU_ERROR_CUDA : error;
+    }
+    double milliseconds[JFGPU_KERNEL_KINDS] = {};
+    int64_t launches[JFGPU_KERNEL_KINDS] = {};
+
+  private:
+    struct Mark {
+        int kind, before, after;
+    };
+    int next() {
+        if (used_ == pool_.size()) {
+            cudaEvent_t ev;
+            if (cudaEventCreate(&ev) != cudaSuccess) {
+                failed_ = true;
+                return -1;
+            }
+            pool_.push_back(ev);
+        }
+        return (int)used_++;
+    }
+    std::vector<cudaEvent_t> pool_;
+    size_t used_ = 0;
+    bool failed_ = false;
+    std::map<cudaStream_t, int> last_;
+    std::vector<Mark> marks_;
 };
 
 struct JfgpuEngine {
@@ -51,6 +116,11 @@ struct JfgpuEngine {
     int block_warps = 4;
     void *refine_lists = nullptr;  // per-chain refine lists of the mixed-precision rounds
     void *refined = nullptr;       // per-chain FP64 re-solves of the first list entries
+    void *refine_queue = nullptr;  // the re-solves queued by screening path
+    int groups = 1;                // chain groups of the mixed mode, each on a stream of its own
+    cudaStream_t group_streams[8] = {};
+    cudaEvent_t fork = nullptr, join[8] = {};
+    EventClock *clock = nullptr;   // per-kernel timing, null while off
 };
 
 namespace {
@@ -430,6 +500,12 @@ const char *jfgpu_error_string(int code) {
 
 void jfgpu_engine_destroy(JfgpuEngine *engine) {
     if (!engine) return;
+    for (int g = 0; g < 8; ++g) {
+        if (engine->group_streams[g]) cudaStreamDestroy(engine->group_streams[g]);
+        if (engine->join[g]) cudaEventDestroy(engine->join[g]);
+    }
+    if (engine->fork) cudaEventDestroy(engine->fork);
+    delete engine->clock;
     for (void *p : engine->allocations) cudaFree(p);
     delete engine;
 }
@@ -555,6 +631,8 @@ int jfgpu_engine_create(const JfgpuChainDesc *chains, int64_t n_chains, void *st
         e->refine_lists = device_copy(e, lists, stream, error);
         std::vector<unsigned char> slots(refined_bytes() * (size_t)n_chains, 0);
         e->refined = device_copy(e, slots, stream, error);
+        std::vector<unsigned char> queue(refine_queue_bytes(n_chains), 0);
+        e->refine_queue = device_copy(e, queue, stream, error);
         if (!error && cudaStreamSynchronize(stream) != cudaSuccess) error = JFGPU_ERROR_CUDA;
     }
     if (error) {
@@ -605,9 +683,67 @@ static bool buffers_ok(const JfgpuEngine *e, const JfgpuBuffers *b) {
     return e && b && b->positions && b->positions32 && b->occupancy && b->surplus && b->roles && b->state;
 }
 
+int jfgpu_chains_set_groups(JfgpuEngine *e, int32_t groups) {
+    if (!e || groups < 1 || groups > 8) return JFGPU_ERROR_ARGUMENT;
+    // the streams and events are made once, on the engine's device, the first time more than one group is asked for
+    for (int g = 0; g < groups && groups > 1; ++g) {
+        if (!e->group_streams[g] && cudaStreamCreateWithFlags(&e->group_streams[g], cudaStreamNonBlocking) != cudaSuccess)
+            return JFGPU_ERROR_CUDA;
+        if (!e->join[g] && cudaEventCreateWithFlags(&e->join[g], cudaEventDisableTiming) != cudaSuccess)
+            return JFGPU_ERROR_CUDA;
+    }
+    if (groups > 1 && !e->fork && cudaEventCreateWithFlags(&e->fork, cudaEventDisableTiming) != cudaSuccess)
+        return JFGPU_ERROR_CUDA;
+    e->groups = groups;
+    return JFGPU_OK;
+}
+
+int jfgpu_engine_set_timing(JfgpuEngine *e, int32_t enable) {
+    if (!e) return JFGPU_ERROR_ARGUMENT;
+    if (enable && !e->clock) e->clock = new EventClock();
+    if (!enable && e->clock) {
+        e->clock->collect();
+        delete e->clock;
+        e->clock = nullptr;
+    }
+    return JFGPU_OK;
+}
+
+int jfgpu_engine_kernel_times(JfgpuEngine *e, double *milliseconds, int64_t *launches, int32_t reset) {
+    if (!e) return JFGPU_ERROR_ARGUMENT;
+    int error = JFGPU_OK;
+    for (int k = 0; k < JFGPU_KERNEL_KINDS; ++k) {
+        if (milliseconds) milliseconds[k] = 0.0;
+        if (launches) launches[k] = 0;
+    }
+    if (!e->clock) return JFGPU_OK;
+    error = e->clock->collect();
+    for (int k = 0; k < JFGPU_KERNEL_KINDS; ++k) {
+        if (milliseconds) milliseconds[k] = e->clock->milliseconds[k];
+        if (launches) launches[k] = e->clock->launches[k];
+        if (reset) {
+            e->clock->milliseconds[k] = 0.0;
+            e->clock->launches[k] = 0;
+        }
+    }
+    return error;
+}
+
+static LaunchPlan make_plan(const JfgpuEngine *e, void *stream_ptr) {
+    LaunchPlan plan;
+    plan.stream = static_cast<cudaStream_t>(stream_ptr);
+    plan.warps = e->block_warps;
+    plan.groups = e->groups;
+    plan.group_streams = e->groups > 1 ? const_cast<cudaStream_t *>(e->group_streams) : nullptr;
+    plan.fork = e->fork;
+    plan.join = const_cast<cudaEvent_t *>(e->join);
+    plan.clock = e->clock;
+    return plan;
+}
+
 int jfgpu_chains_init(JfgpuEngine *e, const JfgpuBuffers *b, void *stream_ptr) {
     if (!buffers_ok(e, b)) return JFGPU_ERROR_ARGUMENT;
-    cudaError_t err = launch_init(e->view, (long long)e->chains.size(), *b, static_cast<cudaStream_t>(stream_ptr));
+    cudaError_t err = launch_init(e->view, (long long)e->chains.size(), *b, make_plan(e, stream_ptr));
     e->launches += 1;
     return err == cudaSuccess ? JFGPU_OK : JFGPU_ERROR_CUDA;
 }
@@ -624,9 +760,8 @@ int jfgpu_chains_run(JfgpuEngine *e, const JfgpuBuffers *b, int64_t first, int64
         if (e->chains[c].potential != potential || e->chains[c].far != far) potential = far = -1;
     long long launches = 0;
     cudaError_t err = launch_run(e->view, *b, first, count, max_events, stop_q, stop_r, mode, log, log_capacity,
-                                 e->block_warps, potential, far, e->refine_lists, e->refined,
-                                 static_cast<cudaStream_t>(stream_ptr),
-                                 &launches);
+                                 potential, far, e->refine_lists, e->refined, e->refine_queue,
+                                 (long long)e->chains.size(), make_plan(e, stream_ptr), &launches);
     e->launches += launches;
     return err == cudaSuccess ? JFGPU_OK : JFGPU_ERROR_CUDA;
 }

@@ -13,6 +13,18 @@ namespace jf {
 constexpr float kScreenRel = 1.0f / 4096.0f;  // conditioning thresholds
 constexpr float kInf32 = __builtin_inff();
 
+// solve paths of a candidate as the FP32 screening takes them; the FP64 re-solves are queued by path so that the
+// threads of a warp follow one branch of the reference's case analysis
+constexpr int kPathFrontOutside = 0;   // Lennard-Jones: in front, outside the minimum shell
+constexpr int kPathBehindShell = 1;    // behind, outside, the line of motion crosses the shell
+constexpr int kPathBehindNoShell = 2;  // behind, outside, the line misses the shell
+constexpr int kPathFrontInside = 3;    // in front, inside the shell
+constexpr int kPathBehindInside = 4;   // behind, inside the shell
+constexpr int kPathHardSphere = 5;
+constexpr int kPathFar = 6;            // far-field (cell-bounding) candidate
+constexpr int kPathFlagged = 7;        // flagged by the screening: path unknown
+constexpr int kPaths = 8;
+
 // potential change of a keyed draw in FP32 without FP64 instructions: the uniform is (bits >> 11) 2^-53; its top 32
 // bits k give u within 2^-32, so -log1p(-u) (u < 1/2) and -log(1 - u) with 1 - u from 2^32 - k (u >= 1/2) carry a
 // relative error of about 2^-22 except for u < 2^-16 or 1 - u < 2^-16, which are flagged
@@ -142,7 +154,7 @@ __device__ inline float lj_behind_inside32(const LJ32 &c, float u, float du, flo
 }
 
 __device__ inline float lj_screen(const LJ32 &c, int d, float speed, const float *s, float du, float margin,
-                                  bool &flag) {
+                                  bool &flag, int &path) {
     float sd = s[d];
     int a = d == 0 ? 1 : 0;
     int b = d == 2 ? 1 : 2;
@@ -153,24 +165,29 @@ __device__ inline float lj_screen(const LJ32 &c, int d, float speed, const float
     float disp;
     if (norm_sq >= c.r0_sq) {
         if (sd <= 0.0f) {
+            path = kPathFrontOutside;
             disp = lj_front_outside32(c, lj_u32(c, norm_sq), du, sd, perp, flag);
         } else {
             // behind and outside: reach the shell if the line crosses it, else slide to s_d = 0
             float radicand = c.r0_sq - perp;
             if (fabsf(radicand) < kScreenRel * 16.0f * c.r0_sq) flag = true;
             if (radicand >= 0.0f) {
+                path = kPathBehindShell;
                 float to_shell = sd - sqrtf(radicand);
                 float sd_new = sd - to_shell;
                 float u = lj_u32(c, sd_new * sd_new + perp);
                 disp = to_shell + lj_behind_inside32(c, u, du, sd_new, perp, flag);
             } else {
+                path = kPathBehindNoShell;
                 disp = sd + lj_front_outside32(c, lj_u32(c, perp), du, 0.0f, perp, flag);
             }
         }
     } else {
         if (sd <= 0.0f) {
+            path = kPathFrontInside;
             disp = lj_front_inside32(c, du, sd, perp, flag);
         } else {
+            path = kPathBehindInside;
             disp = lj_behind_inside32(c, lj_u32(c, norm_sq), du, sd, perp, flag);
         }
     }

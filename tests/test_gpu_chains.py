@@ -107,6 +107,40 @@ def test_batched_mixed_equals_fp64_lennard_jones():
     assert (exact_state["events"] == 1500).all()
 
 
+def test_chain_groups_and_kernel_timing_leave_results_unchanged():
+    """Chain groups on streams of their own, and CUDA events around every launch, change no bit of the run."""
+    from jellyfysh_gb300 import ChainBatch, ChainSpec, systems
+    n, chains, events = 64, 256, 300
+    length = systems.lennard_jones_box(n, 0.8)
+    rng = np.random.default_rng(3)
+    specs = [ChainSpec(n=n, system_length=length, cells_per_side=4, potential="lennard_jones", far="cell_bounding",
+                       beta=1.0 / 1.2, chain_time=2.0, initial_active=int(rng.integers(n)),
+                       initial_direction=int(rng.integers(3))) for _ in range(chains)]
+    positions = [systems.simple_cubic_jitter(n, length, 0.05, rng) for _ in range(chains)]
+    results = {}
+    for label, mode, groups, timing in (("exact", "exact", 1, False), ("mixed", "mixed", 1, False),
+                                        ("grouped", "mixed", 4, True)):
+        batch = ChainBatch(specs, positions, seed=11)
+        batch.set_groups(groups)
+        batch.set_timing(timing)
+        batch.run(events, mode=mode)
+        batch.check_status()
+        results[label] = (batch.positions(), batch.state())
+        if timing:
+            times = batch.kernel_times()
+            for kind in ("screen", "refine", "resolve"):
+                assert times[kind]["launches"] == 4 * events, (kind, times[kind])
+                assert times[kind]["ms"] > 0.0
+            assert times["chains"]["launches"] == 0
+        batch.close()
+    for label in ("mixed", "grouped"):
+        for a, b in zip(results["exact"][0], results[label][0]):
+            assert np.array_equal(a, b), label
+        for field in ("time_q", "time_r", "events", "active", "direction", "n_surplus", "occ_cell"):
+            assert np.array_equal(results["exact"][1][field], results[label][1][field]), (label, field)
+    assert (results["grouped"][1]["events"] == events).all()
+
+
 def _occupancy_consistent(batch, chain):
     spec = batch.specs[chain]
     occ = batch.occupancy(chain).ravel()
