@@ -180,7 +180,11 @@ typedef struct {
     int32_t occ_cell;             /* active cell of the occupancy */
     int32_t n_surplus;
     int32_t status;               /* JFGPU_STATUS_* of the first failure; the chain stops */
-    int32_t reserved;
+    int32_t stopped;              /* the chain reached the stop time of the current call */
+    double lift_sum;              /* sum over the accepted liftings of the separation target - active along the
+                                     direction of motion (the excess displacement of the chains, whose ratio to the
+                                     total displacement gives the pressure: beta P / rho = 1 + lift_sum / (v t)) */
+    int64_t liftings;             /* accepted liftings (pair, bounded, cell-bounding and cell-veto events) */
 } JfgpuChainState;
 
 /* one committed event (device log array [n_chains][log_capacity]) */
@@ -235,6 +239,17 @@ int jfgpu_chains_run(JfgpuEngine *engine, const JfgpuBuffers *buffers, int64_t f
 /* Autotuned launch shape of the mixed mode: warps per block used by jfgpu_chains_run (1..8). */
 int jfgpu_chains_set_block_warps(JfgpuEngine *engine, int32_t warps_per_block);
 
+/* Observables of chains [first_chain, first_chain + count) at their current positions, for the estimators of
+ * long runs (all pairs of a chain, minimum-image separations from the FP32 mirror):
+ *   energy    [count] (device, may be NULL): potential energy of the chain's pair potential, the sum over pairs
+ *             of the Lennard-Jones potential (lennard_jones_potential.py:83-98), 0 for hard spheres, NaN for
+ *             merged-image Coulomb chains (the reference defines no Coulomb energy);
+ *   histogram [count][bins] (device, may be NULL): pair distances in [0, r_max) with bins equal bins, ADDED to
+ *             the array (samples accumulate over calls); 1 <= bins <= 4096.
+ * The pair-separation samples of separation_output_handler.py:75-97, reduced on the device. */
+int jfgpu_chains_observe(JfgpuEngine *engine, const JfgpuBuffers *buffers, int64_t first_chain, int64_t count,
+                         int32_t bins, double r_max, double *energy, uint64_t *histogram, void *stream);
+
 /* Chain groups of the mixed mode: the chains of one jfgpu_chains_run call are split into `groups` contiguous
  * groups (1..8) whose event rounds run on streams of their own, forked from and joined back into the caller's
  * stream, so that one group's FP64 re-solves overlap another group's FP32 screening.  Default 1. */
@@ -249,7 +264,8 @@ int64_t jfgpu_engine_launch_count(const JfgpuEngine *engine);
 #define JFGPU_KERNEL_RESOLVE 2         /* single candidates, argmin, commit and occupancy update */
 #define JFGPU_KERNEL_CHAINS 3          /* the FP64 event loop of JFGPU_MODE_EXACT */
 #define JFGPU_KERNEL_INIT 4            /* chain start */
-#define JFGPU_KERNEL_KINDS 5
+#define JFGPU_KERNEL_OBSERVE 5         /* observables of jfgpu_chains_observe */
+#define JFGPU_KERNEL_KINDS 6
 
 /* Per-kernel device time.  While timing is on, the chain launches of jfgpu_chains_init / jfgpu_chains_run are
  * bracketed by CUDA events on the stream they are launched on.  jfgpu_engine_kernel_times waits for those events

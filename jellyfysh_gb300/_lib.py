@@ -57,7 +57,8 @@ class ChainState(ctypes.Structure):
                 ("refine_fallbacks", ctypes.c_int64), ("candidates", ctypes.c_int64), ("refined", ctypes.c_int64),
                 ("active", ctypes.c_int32), ("direction", ctypes.c_int32),
                 ("eoc_new_active", ctypes.c_int32), ("occ_active", ctypes.c_int32), ("occ_cell", ctypes.c_int32),
-                ("n_surplus", ctypes.c_int32), ("status", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+                ("n_surplus", ctypes.c_int32), ("status", ctypes.c_int32), ("stopped", ctypes.c_int32),
+                ("lift_sum", ctypes.c_double), ("liftings", ctypes.c_int64)]
 
 
 class Event(ctypes.Structure):
@@ -109,6 +110,7 @@ SIGNATURES = {
                                         _P]),
     "jfgpu_chains_set_block_warps": (ctypes.c_int, [_P, _I32]),
     "jfgpu_chains_set_groups": (ctypes.c_int, [_P, _I32]),
+    "jfgpu_chains_observe": (ctypes.c_int, [_P, ctypes.POINTER(Buffers), _I64, _I64, _I32, _D, _P, _P, _P]),
     "jfgpu_engine_set_timing": (ctypes.c_int, [_P, _I32]),
     "jfgpu_engine_kernel_times": (ctypes.c_int, [_P, _P, _P, _I32]),
     "jfgpu_engine_launch_count": (ctypes.c_int64, [_P]),

@@ -37,7 +37,7 @@ POTENTIALS = {"hard_sphere": _lib.POT_HARD_SPHERE, "lennard_jones": _lib.POT_LEN
 FAR_FIELDS = {"none": _lib.FAR_NONE, "cell_veto": _lib.FAR_CELL_VETO, "cell_bounding": _lib.FAR_CELL_BOUNDING}
 MODES = {"exact": _lib.MODE_EXACT, "mixed": _lib.MODE_MIXED}
 # kernel kinds of jfgpu_engine_kernel_times, in JFGPU_KERNEL_* order
-KERNEL_KINDS = ("screen", "refine", "resolve", "chains", "init")
+KERNEL_KINDS = ("screen", "refine", "resolve", "chains", "init", "observe")
 
 EVENT_DTYPE = np.dtype([("kind", np.int32), ("moved", np.int32), ("target", np.int32), ("new_active", np.int32),
                         ("new_direction", np.int32), ("accepted", np.int32), ("time_q", np.float64),
@@ -47,7 +47,8 @@ STATE_DTYPE = np.dtype([("time_q", np.float64), ("time_r", np.float64), ("eoc_q"
                         ("refine_fallbacks", np.int64), ("candidates", np.int64), ("refined", np.int64),
                         ("active", np.int32), ("direction", np.int32),
                         ("eoc_new_active", np.int32), ("occ_active", np.int32), ("occ_cell", np.int32),
-                        ("n_surplus", np.int32), ("status", np.int32), ("reserved", np.int32)])
+                        ("n_surplus", np.int32), ("status", np.int32), ("stopped", np.int32),
+                        ("lift_sum", np.float64), ("liftings", np.int64)])
 assert EVENT_DTYPE.itemsize == ctypes.sizeof(_lib.Event)
 assert STATE_DTYPE.itemsize == ctypes.sizeof(_lib.ChainState)
 
@@ -189,6 +190,23 @@ class ChainBatch:
 
     def launch_count(self) -> int:
         return int(self.lib.jfgpu_engine_launch_count(self._engine))
+
+    def observe(self, bins: int = 0, r_max: float = 0.0, first: int = 0, count: Optional[int] = None,
+                histogram=None):
+        """Potential energy of every chain's configuration (device tensor [count], NaN for Coulomb chains) and,
+        with bins > 0, its pair-distance histogram over [0, r_max) ADDED to ``histogram`` (a device int64 tensor
+        [count, bins], created when None).  Returns (energy, histogram)."""
+        torch = self._torch
+        count = self.n_chains - first if count is None else count
+        energy = torch.empty(count, dtype=torch.float64, device=self.device)
+        if bins and histogram is None:
+            histogram = torch.zeros((count, bins), dtype=torch.int64, device=self.device)
+        with torch.cuda.device(self.device):
+            _lib.check(self.lib.jfgpu_chains_observe(self._engine, ctypes.byref(self._buffers), int(first), int(count),
+                                                     int(bins), float(r_max), _ptr(energy),
+                                                     _ptr(histogram) if bins else None, self._stream()),
+                       "jfgpu_chains_observe")
+        return energy, histogram
 
     def set_timing(self, enable: bool) -> None:
         """Bracket every chain launch by CUDA events on its stream (read back by kernel_times)."""

@@ -103,7 +103,8 @@ __device__ inline float warp_min_float(float v) {
 struct WarpState {
     double pa[3];
     double ts_q, ts_r, eoc_q, eoc_r;
-    long long events, warnings, fallbacks, candidates, refined;
+    double lift_sum;
+    long long events, warnings, fallbacks, candidates, refined, liftings;
     int active, direction, eoc_new, occ_active, occ_cell, n_surplus, status, stop;
 };
 
@@ -541,6 +542,12 @@ __device__ __noinline__ int commit(const RunArgs &A, const ChainDev &ch, const S
     if (w.active != moved) {
         double pn[3];
         load_pos(A, ch, w.active, pn);
+        if (best.kind != JFGPU_EV_END_OF_CHAIN) {
+            // excess displacement of the lifting: separation target - active along the (unchanged) direction
+            const int d = w.direction;
+            w.lift_sum += py_mod_near((pn[d] - w.pa[d]) + ch.half, ch.L) - ch.half;
+            w.liftings += 1;
+        }
         w.pa[0] = pn[0];
         w.pa[1] = pn[1];
         w.pa[2] = pn[2];
@@ -797,7 +804,7 @@ __global__ void __launch_bounds__(256, 4) screen_kernel(RunArgs A, RefineList *l
     const SpeciesDev &sp = A.view.species[ch.species];
     RefineList &list = lists[local];
     const JfgpuChainState &g = A.state[c];
-    if (g.status != JFGPU_STATUS_OK || (round > 0 && g.reserved)) {
+    if (g.status != JFGPU_STATUS_OK || (round > 0 && g.stopped)) {
         if (lane == 0) {
             list.count = 0;
             list.flags = kListSkip;
@@ -947,6 +954,8 @@ __device__ inline void load_lifting(const JfgpuChainState &g, const RunArgs &A, 
     w.fallbacks = g.refine_fallbacks;
     w.candidates = g.candidates;
     w.refined = g.refined;
+    w.lift_sum = g.lift_sum;
+    w.liftings = g.liftings;
     w.active = g.active;
     w.direction = g.direction;
     w.eoc_new = g.eoc_new_active;
@@ -1043,7 +1052,7 @@ __global__ void __launch_bounds__(32) resolve_kernel(RunArgs A, const RefineList
     const ChainDev &ch = A.view.chains[c];
     const SpeciesDev &sp = A.view.species[ch.species];
     JfgpuChainState &g = A.state[c];
-    if (g.status != JFGPU_STATUS_OK || (round > 0 && g.reserved)) return;
+    if (g.status != JFGPU_STATUS_OK || (round > 0 && g.stopped)) return;
     const RefineList &list = lists[local];
     if (list.flags & kListSkip) return;
     WarpState w;
@@ -1102,6 +1111,8 @@ __global__ void __launch_bounds__(32) resolve_kernel(RunArgs A, const RefineList
     g.refine_fallbacks = w.fallbacks;
     g.candidates = w.candidates;
     g.refined = w.refined;
+    g.lift_sum = w.lift_sum;
+    g.liftings = w.liftings;
     g.active = w.active;
     g.direction = w.direction;
     g.eoc_new_active = w.eoc_new;
@@ -1109,7 +1120,7 @@ __global__ void __launch_bounds__(32) resolve_kernel(RunArgs A, const RefineList
     g.occ_cell = w.occ_cell;
     g.n_surplus = w.n_surplus;
     g.status = w.status;
-    g.reserved = w.stop;
+    g.stopped = w.stop;
 }
 
 #ifndef JF_CHAIN_MIN_BLOCKS
@@ -1139,6 +1150,8 @@ __global__ void __launch_bounds__(256, JF_CHAIN_MIN_BLOCKS) chains_kernel(RunArg
         w.fallbacks = g.refine_fallbacks;
         w.candidates = g.candidates;
         w.refined = g.refined;
+        w.lift_sum = g.lift_sum;
+        w.liftings = g.liftings;
         w.active = g.active;
         w.direction = g.direction;
         w.eoc_new = g.eoc_new_active;
@@ -1200,6 +1213,8 @@ __global__ void __launch_bounds__(256, JF_CHAIN_MIN_BLOCKS) chains_kernel(RunArg
         g.refine_fallbacks = w.fallbacks;
         g.candidates = w.candidates;
         g.refined = w.refined;
+        g.lift_sum = w.lift_sum;
+        g.liftings = w.liftings;
         g.active = w.active;
         g.direction = w.direction;
         g.eoc_new_active = w.eoc_new;
@@ -1207,6 +1222,7 @@ __global__ void __launch_bounds__(256, JF_CHAIN_MIN_BLOCKS) chains_kernel(RunArg
         g.occ_cell = w.occ_cell;
         g.n_surplus = w.n_surplus;
         g.status = w.status;
+        g.stopped = w.stop;
     }
 }
 
@@ -1266,7 +1282,9 @@ __global__ void init_kernel(EngineView view, long long n_chains, double *positio
     g.occ_cell = -1;
     g.n_surplus = n_surplus;
     g.status = status;
-    g.reserved = 0;
+    g.stopped = 0;
+    g.lift_sum = 0.0;
+    g.liftings = 0;
     if (status == JFGPU_STATUS_OK) {
         // the activator's first update after the start of the run: the initial active unit leaves the occupancy
         RunArgs A;

@@ -29,6 +29,9 @@ cudaError_t launch_run(const EngineView &view, const JfgpuBuffers &b, long long 
 size_t refine_list_bytes();
 size_t refined_bytes();
 size_t refine_queue_bytes(long long n_chains);
+cudaError_t launch_observe(const EngineView &view, long long first, long long count, int max_n,
+                           const float4 *positions32, int bins, double r_max, double *energy,
+                           unsigned long long *histogram, const LaunchPlan &plan);
 }  // namespace jf
 
 using namespace jf;
@@ -727,6 +730,24 @@ int jfgpu_engine_kernel_times(JfgpuEngine *e, double *milliseconds, int64_t *lau
         }
     }
     return error;
+}
+
+static LaunchPlan make_plan(const JfgpuEngine *e, void *stream_ptr);
+
+int jfgpu_chains_observe(JfgpuEngine *e, const JfgpuBuffers *b, int64_t first, int64_t count, int32_t bins,
+                         double r_max, double *energy, uint64_t *histogram, void *stream_ptr) {
+    if (!e || !b || !b->positions32 || first < 0 || count < 0 || first + count > (int64_t)e->chains.size() ||
+        (histogram && (bins < 1 || bins > 4096 || !(r_max > 0.0))))
+        return JFGPU_ERROR_ARGUMENT;
+    if (count == 0 || (!energy && !histogram)) return JFGPU_OK;
+    int max_n = 0;
+    for (int64_t c = first; c < first + count; ++c) max_n = e->chains[c].n > max_n ? e->chains[c].n : max_n;
+    if (!histogram) bins = 1;
+    cudaError_t err = launch_observe(e->view, first, count, max_n, reinterpret_cast<const float4 *>(b->positions32),
+                                     bins, histogram ? r_max : 1.0, energy,
+                                     reinterpret_cast<unsigned long long *>(histogram), make_plan(e, stream_ptr));
+    e->launches += 1;
+    return err == cudaSuccess ? JFGPU_OK : JFGPU_ERROR_CUDA;
 }
 
 static LaunchPlan make_plan(const JfgpuEngine *e, void *stream_ptr) {

@@ -97,6 +97,7 @@ def lib() -> ctypes.CDLL:
                                            ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int), _PD, _PD]
         handle.jfo_chain_occupancy.restype = ctypes.c_int
         handle.jfo_chain_occupancy.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int32)]
+        handle.jfo_chain_liftings.argtypes = [ctypes.c_void_p, _PD, ctypes.POINTER(ctypes.c_int64)]
         handle.jfo_chain_bounds.restype = ctypes.c_int
         handle.jfo_chain_bounds.argtypes = [ctypes.c_void_p, _PD, ctypes.c_int]
         handle.jfo_chain_walker.restype = ctypes.c_int
@@ -285,6 +286,13 @@ class Chain:
                               ctypes.byref(q), ctypes.byref(r))
         return dict(events=event.value, active=active.value, direction=direction.value, time_q=q.value,
                     time_r=r.value)
+
+    def liftings(self):
+        """(sum of the lifting separations along the direction of motion, number of liftings)."""
+        total = ctypes.c_double()
+        count = ctypes.c_int64()
+        lib().jfo_chain_liftings(self._handle, ctypes.byref(total), ctypes.byref(count))
+        return total.value, count.value
 
     def occupancy(self):
         """owner[i]: cell of particle i among the occupants, -2 - cell for a surplus unit, -1 for the active unit."""

@@ -1015,6 +1015,9 @@ struct JfoChain {
     double eoc_q, eoc_r;
     int eoc_new_active;
     int64_t event;
+    /* excess displacement of the liftings (pressure estimator of the harness, not part of the reference) */
+    double lift_sum;
+    int64_t liftings;
     /* potentials */
     MH lj;
     MIC mic;
@@ -1637,6 +1640,13 @@ int64_t jfo_chain_run(JfoChain *c, int64_t max_events, double stop_q, double sto
             *status = JFO_ASSERT;
             return done;
         }
+        if (c->active != moved && best.kind != JFO_EV_END_OF_CHAIN) {
+            /* separation target - active along the direction of motion, as separation_vector computes it */
+            int d = c->direction;
+            c->lift_sum += jfo_py_mod((c->pos[3 * c->active + d] - c->pos[3 * moved + d]) + c->half,
+                                      s->system_length) - c->half;
+            c->liftings++;
+        }
         ev.new_active = c->active;
         ev.new_direction = c->direction;
         ev.x = c->pos[3 * moved];
@@ -1660,6 +1670,11 @@ void jfo_chain_state(const JfoChain *c, int64_t *event_count, int *active, int *
     *direction = c->direction;
     *time_q = c->ts_q;
     *time_r = c->ts_r;
+}
+
+void jfo_chain_liftings(const JfoChain *c, double *lift_sum, int64_t *liftings) {
+    *lift_sum = c->lift_sum;
+    *liftings = c->liftings;
 }
 
 /* far-field bound table: [ncells][3] upper bounds followed by [ncells][3] negated lower bounds */

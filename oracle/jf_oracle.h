@@ -153,6 +153,9 @@ void jfo_chain_positions(const JfoChain *chain, double *positions);
 void jfo_chain_state(const JfoChain *chain, int64_t *event_count, int *active, int *direction,
                      double *time_q, double *time_r);
 int jfo_chain_occupancy(const JfoChain *chain, int32_t *owner);
+/* sum over the accepted liftings of the separation target - active along the direction of motion, and their
+ * number (the harness's pressure estimator: beta P / rho = 1 + lift_sum / (speed * elapsed time)) */
+void jfo_chain_liftings(const JfoChain *chain, double *lift_sum, int64_t *liftings);
 int jfo_chain_bounds(const JfoChain *chain, double *bounds, int capacity);
 int jfo_chain_walker(const JfoChain *chain, int direction, int which, int32_t *cells, double *rates, int capacity,
                      double *total_rate);
