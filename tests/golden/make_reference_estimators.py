@@ -13,8 +13,10 @@ injected (``AtomRandomNodeCreator.fill_root_node``), and every commit of the sta
 * at every accepted lifting the separation target - active along the direction of motion is added to the
   excess displacement of the current chain.
 
-The fixture holds per-chain samples (energy, lifting sum, displacement) and per-block histograms, from which
-the tests compute the estimators and their errors exactly as they do for the GPU engine and the oracle.
+Sixteen independent runs (own Python seed, own initial jitter, burn-in of `burn_in` chains) give independent
+blocks for the errors.  The fixture holds per-run, per-chain samples (energy, lifting sum) and per-run
+histograms, from which the tests compute the estimators and their errors exactly as they do for the GPU engine and
+the oracle.
 """
 import json
 import os
@@ -33,16 +35,17 @@ sys.path.insert(0, ROOT)
 import make_reference_trajectories as trajectories  # noqa: E402
 
 BINS = 40
+RUNS = 16  # independent runs of the reference (own Python seed and initial jitter): the blocks of the errors
 SYSTEMS = {
-    "lennard_jones_n64_cell_veto": dict(trajectories.SYSTEMS["lennard_jones_n64_cell_veto"], chains=4000,
-                                        burn_in=200, r_max_fraction=0.5, blocks=40, python_seed=2024),
-    "hard_spheres_n64": dict(trajectories.SYSTEMS["hard_spheres_n64"], chains=16000, burn_in=400,
-                             r_max_fraction=0.5, blocks=40, python_seed=2025),
+    "lennard_jones_n64_cell_veto": dict(trajectories.SYSTEMS["lennard_jones_n64_cell_veto"], burn_in=200,
+                                        samples=240, r_max_fraction=0.5, python_seed=2024),
+    "hard_spheres_n64": dict(trajectories.SYSTEMS["hard_spheres_n64"], burn_in=400, samples=1000,
+                             r_max_fraction=0.5, python_seed=2025),
 }
 
 
-def run_one(tree: str, name: str) -> None:
-    spec = SYSTEMS[name]
+def run_one(tree: str, name: str, run: int, out: str) -> None:
+    spec = dict(SYSTEMS[name], seed=SYSTEMS[name]["seed"] + 1000 * run)
     sys.path.insert(0, tree)
     import configparser
     import logging
@@ -57,7 +60,7 @@ def run_one(tree: str, name: str) -> None:
     from jellyfysh.state_handler.tree_state_handler import TreeStateHandler
     from jellyfysh.scheduler.heap_scheduler.heap_scheduler import HeapScheduler
 
-    random.seed(spec["python_seed"])
+    random.seed(spec["python_seed"] + run)
     n = spec["n"]
     r_max = spec["r_max_fraction"] * length
     queue = list(range(n))
@@ -76,9 +79,8 @@ def run_one(tree: str, name: str) -> None:
         return handler
     HeapScheduler.get_succeeding_event = get_succeeding_event
 
-    samples = {"energy": [], "lift": [], "liftings": [], "histograms": []}
-    block_hist = np.zeros(BINS, dtype=np.int64)
-    per_block = (spec["chains"] - spec["burn_in"]) // spec["blocks"]
+    samples = {"energy": [], "lift": [], "liftings": []}
+    histogram = np.zeros(BINS, dtype=np.int64)
 
     class Stop(Exception):
         pass
@@ -86,7 +88,6 @@ def run_one(tree: str, name: str) -> None:
     original_insert = TreeStateHandler.insert_into_global_state
 
     def insert_into_global_state(self, out_state):
-        nonlocal block_hist
         ctx["depth"] += 1
         try:
             result = original_insert(self, out_state)
@@ -108,12 +109,8 @@ def run_one(tree: str, name: str) -> None:
                                          if spec["potential"] == "lennard_jones" else 0.0)
                 samples["lift"].append(ctx["lift"])
                 samples["liftings"].append(ctx["liftings"])
-                block_hist += estimators.pair_histogram(config, length, BINS, r_max)
-                done = ctx["chains"] - spec["burn_in"]
-                if done % per_block == 0:
-                    samples["histograms"].append(block_hist.copy())
-                    block_hist[:] = 0
-                if done >= per_block * spec["blocks"]:
+                histogram[:] += estimators.pair_histogram(config, length, BINS, r_max)
+                if ctx["chains"] - spec["burn_in"] >= spec["samples"]:
                     raise Stop()
             ctx["lift"] = 0.0
             ctx["liftings"] = 0
@@ -136,24 +133,39 @@ def run_one(tree: str, name: str) -> None:
         mediator.run()
     except (Stop, EndOfRun):
         pass
-    out = os.path.join(HERE, "estimators_%s.npz" % name)
-    fixture = dict(spec, system_length=length, r_max=r_max, bins=BINS, speed=1.0)
-    np.savez_compressed(out, energy=np.array(samples["energy"]), lift=np.array(samples["lift"]),
-                        liftings=np.array(samples["liftings"]), histograms=np.array(samples["histograms"]),
-                        spec=json.dumps(fixture))
-    print("%s: %d chain samples in %.0f s -> %s" % (name, len(samples["energy"]), time.time() - start, out))
+    np.savez(out, energy=np.array(samples["energy"]), lift=np.array(samples["lift"]),
+             liftings=np.array(samples["liftings"]), histogram=histogram, length=length, r_max=r_max)
+    print("%s run %d: %d chain samples in %.0f s" % (name, run, len(samples["energy"]), time.time() - start))
 
 
 def main(tree: str, names) -> None:
-    procs = [subprocess.Popen([sys.executable, os.path.abspath(__file__), "--one", tree, name]) for name in names]
-    for p in procs:
-        if p.wait() != 0:
-            raise SystemExit(p.returncode)
+    import concurrent.futures
+    import tempfile
+    with tempfile.TemporaryDirectory() as scratch:
+        def one(job):
+            name, run = job
+            out = os.path.join(scratch, "%s_%d.npz" % (name, run))
+            subprocess.run([sys.executable, os.path.abspath(__file__), "--one", tree, name, str(run), out],
+                           check=True)
+            return out
+        jobs = [(name, run) for name in names for run in range(RUNS)]
+        with concurrent.futures.ThreadPoolExecutor(max_workers=os.cpu_count() or 4) as pool:
+            outs = dict(zip(jobs, pool.map(one, jobs)))
+        for name in names:
+            runs = [np.load(outs[(name, run)]) for run in range(RUNS)]
+            spec = dict(SYSTEMS[name], system_length=float(runs[0]["length"]), r_max=float(runs[0]["r_max"]),
+                        bins=BINS, runs=RUNS, speed=1.0)
+            path = os.path.join(HERE, "estimators_%s.npz" % name)
+            np.savez_compressed(path, energy=np.array([r["energy"] for r in runs]),
+                                lift=np.array([r["lift"] for r in runs]),
+                                liftings=np.array([r["liftings"] for r in runs]),
+                                histograms=np.array([r["histogram"] for r in runs]), spec=json.dumps(spec))
+            print("%s: %d runs -> %s" % (name, RUNS, path))
 
 
 if __name__ == "__main__":
     if len(sys.argv) > 1 and sys.argv[1] == "--one":
-        run_one(sys.argv[2], sys.argv[3])
+        run_one(sys.argv[2], sys.argv[3], int(sys.argv[4]), sys.argv[5])
     else:
         tree_path = sys.argv[1] if len(sys.argv) > 1 else "/tmp/jf_ref"
         main(tree_path, sys.argv[2:] or list(SYSTEMS))

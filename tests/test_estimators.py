@@ -92,6 +92,6 @@ def oracle_samples(spec, chains, samples, seed):
 @pytest.mark.parametrize("name", estimator_names())
 def test_oracle_long_runs_reproduce_the_reference_estimators(name):
     spec, reference = reference_estimates(name)
-    energies, lifts, histograms = oracle_samples(spec, chains=16, samples=spec["chains"] // 16, seed=77)
+    energies, lifts, histograms = oracle_samples(spec, chains=16, samples=spec["samples"], seed=77)
     other = sampled_estimates(spec, energies, lifts, histograms)
     assert compare(reference, other) == []

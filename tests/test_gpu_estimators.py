@@ -1,7 +1,8 @@
 """Estimators of long runs on the GPU engine.
 
-* The lifting sums of the engine (exact and mixed precision) equal the oracle's bit for bit on the reference
-  trajectories, and so the sums replayed from the reference's own events.
+* The lifting sums of the engine (exact and mixed precision) equal the oracle's on the reference trajectories
+  (bit for bit for hard spheres, to 1e-12 of the box per lifting otherwise), and so the sums replayed from the
+  reference's own events.
 * The device observables (potential energy, pair-distance histogram) agree with the host estimator functions on
   the same configurations (FP32 pair terms: energy to 1e-5 relative, histograms up to pairs on bin edges).
 * Long runs of many chains in mixed precision reproduce the reference's estimators (``golden/estimators_*.npz``,
@@ -40,7 +41,13 @@ def test_lifting_sums_equal_the_oracle(name, mode):
     state = batch.state()[0]
     chain = oracle.Chain(oracle_system(spec), initial, charges)
     chain.run(len(events), record=False)
-    assert (float(state["lift_sum"]), int(state["liftings"])) == chain.liftings()
+    lift_sum, liftings = chain.liftings()
+    assert int(state["liftings"]) == liftings
+    if spec["potential"] == "hard_sphere":
+        assert float(state["lift_sum"]) == lift_sum  # positions bit for bit (square roots only)
+    else:
+        # positions agree to 1e-12 of the box (correctly rounded powers, CUDA's transcendentals)
+        assert float(state["lift_sum"]) == pytest.approx(lift_sum, abs=1e-12 * spec["system_length"] * liftings)
     batch.close()
 
 
@@ -97,7 +104,7 @@ def gpu_samples(spec, chains, samples, seed, max_events):
 def test_long_gpu_runs_reproduce_the_reference_estimators(name):
     spec, reference = reference_estimates(name)
     max_events = 600 if spec["potential"] == "lennard_jones" else 200
-    energies, lifts, histograms = gpu_samples(spec, chains=256, samples=max(spec["chains"] // 64, 50), seed=31,
+    energies, lifts, histograms = gpu_samples(spec, chains=256, samples=spec["samples"] // 4, seed=31,
                                               max_events=max_events)
     other = sampled_estimates(spec, energies, lifts, histograms)
     assert compare(reference, other) == []
