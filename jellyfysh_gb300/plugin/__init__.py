@@ -1,0 +1,32 @@
+"""Drop-in classes for the reference's INI factory.
+
+The reference builds every object of a run from its configuration file with ``base/factory.py:22-135``: a class
+``CamelName`` is found as ``jellyfysh.<package>.camel_name`` (``factory.py:111-122``) and constructed from the keys
+of its section, typed by the constructor's annotations (``factory.py:180-235``).  ``install()`` appends this
+package's directories to the search paths of ``jellyfysh.potential`` and ``jellyfysh.mediator``, so that a
+configuration names the GPU classes exactly like the reference's own:
+
+    [TwoLeafUnitEventHandler]
+    potential = gpu_lennard_jones_potential          ; instead of lennard_jones_potential
+
+    [Run]
+    mediator = gpu_chain_batch_mediator              ; instead of single_process_mediator
+
+The potentials evaluate the reference's displacement / derivative on the GPU one call at a time (a drop-in for
+the reference's own event handlers); the mediator runs the whole configured system as a batch of chains on the GPU.
+Nothing here needs the reference to be importable except ``install()`` and the mediator's translation of a
+configured run.
+"""
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+PACKAGES = {"potential": os.path.join(HERE, "potential"), "mediator": os.path.join(HERE, "mediator")}
+
+
+def install() -> None:
+    """Make the GPU classes resolvable by the reference's factory (requires the ``jellyfysh`` package)."""
+    import importlib
+    for package, directory in PACKAGES.items():
+        module = importlib.import_module("jellyfysh." + package)
+        if directory not in module.__path__:
+            module.__path__.append(directory)

@@ -1,0 +1,134 @@
+"""The drop-in classes against the reference's own factory (CPU only; needs the reference's source tree).
+
+Set JELLYFYSH_TREE to a JeLLyFysh source tree (with its cffi extensions built for the Coulomb systems) to run
+these tests; without it they are skipped.  They check that a configuration file in the reference's vocabulary
+selects the GPU classes by name:
+
+* ``potential = gpu_lennard_jones_potential`` (and the other GPU potentials) builds the GPU class inside the
+  reference's own event handler;
+* ``mediator = gpu_chain_batch_mediator`` builds the drop-in mediator from the same object graph, and its batch
+  plan is the system of the configuration (the chain parameters that the GPU trajectory tests run, the injected
+  initial positions and charges).
+"""
+import configparser
+import dataclasses
+import importlib
+import json
+import os
+import subprocess
+import sys
+
+import numpy as np
+import pytest
+
+from tests.trajectory_cases import load_trajectory, trajectory_names
+
+TREE = os.environ.get("JELLYFYSH_TREE")
+pytestmark = pytest.mark.skipif(not TREE or not os.path.isdir(os.path.join(TREE or "", "jellyfysh")),
+                                reason="JELLYFYSH_TREE does not name a JeLLyFysh source tree")
+
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _reference():
+    if TREE not in sys.path:
+        sys.path.insert(0, TREE)
+    from jellyfysh.base import factory
+    from jellyfysh.base.strings import to_camel_case
+    from jellyfysh_gb300 import plugin
+    plugin.install()
+    return factory, to_camel_case
+
+
+def _in_child(function, *args):
+    """The reference keeps its setting in module globals (one per process): every build runs in its own
+    interpreter, as the reference's own runs do.  Returns the child's JSON result."""
+    code = "import json, sys; import tests.test_plugin as t; print(json.dumps(t.%s(*sys.argv[1:])))" % function
+    done = subprocess.run([sys.executable, "-c", code, *args], cwd=ROOT, capture_output=True, text=True,
+                          timeout=300)
+    assert done.returncode == 0, done.stderr[-3000:]
+    return json.loads(done.stdout.strip().splitlines()[-1])
+
+
+def build_handler_with_gpu_potential():
+    factory, camel = _reference()
+    config = configparser.ConfigParser()
+    config.read_string("""
+[Run]
+setting = hypercubic_setting
+[HypercubicSetting]
+system_length = 4.0
+beta = 1.0
+dimension = 3
+[TwoLeafUnitEventHandler]
+potential = gpu_lennard_jones_potential
+[GpuLennardJonesPotential]
+prefactor = 2.0
+characteristic_length = 1.1
+""")
+    factory.build_from_config(config, "HypercubicSetting", "jellyfysh.setting")
+    handler = factory.build_from_config(config, "TwoLeafUnitEventHandler", "jellyfysh.event_handler")
+    potential = handler._potential
+    modules = []
+    for module in ("gpu_hard_sphere_potential", "gpu_inverse_power_potential", "gpu_displaced_even_power_potential",
+                   "gpu_inverse_power_coulomb_bounding_potential", "gpu_merged_image_coulomb_potential"):
+        modules.append(importlib.import_module("jellyfysh.potential." + module).__name__)
+    return [type(potential).__name__, potential._prefactor, potential._characteristic_length, modules]
+
+
+def translate_configuration(name):
+    factory, camel = _reference()
+    sys.path.insert(0, os.path.join(ROOT, "tests", "golden"))
+    import make_reference_trajectories as trajectories
+    spec, initial, charges, events, final = load_trajectory(name)
+    text = trajectories.config_text(spec, spec["system_length"])
+    text = text.replace("mediator = single_process_mediator", "mediator = gpu_chain_batch_mediator")
+    text = text.replace("[SingleProcessMediator]", "[GpuChainBatchMediator]\nchains = 3\nmode = exact\nseed = 5")
+    config = configparser.ConfigParser()
+    config.read_string(text)
+    # the reference's input handler places random units; inject the fixture's, as the trajectory recorder does
+    from jellyfysh.base.particle import Particle
+    from jellyfysh.input_output_handler.input_handler.random_node_creator import atom_random_node_creator
+    queue = list(range(spec["n"]))
+
+    def fill_root_node(self, node):
+        i = queue.pop(0)
+        charge = {} if charges is None else {"electric_charge": float(charges[i])}
+        node.value = Particle([float(v) for v in initial[i]], charge)
+    atom_random_node_creator.AtomRandomNodeCreator.fill_root_node = fill_root_node
+    factory.build_from_config(config, camel(config.get("Run", "setting")), "jellyfysh.setting")
+    mediator = factory.build_from_config(config, camel(config.get("Run", "mediator")), "jellyfysh.mediator")
+    plan = mediator.plan
+    return {"spec": dataclasses.asdict(plan.spec), "positions": plan.positions.tolist(),
+            "charges": None if plan.charges is None else plan.charges.tolist(),
+            "end_of_run_time": plan.end_of_run_time, "chains": plan.chains, "mode": plan.mode, "seed": plan.seed}
+
+
+def test_gpu_potentials_are_built_inside_the_reference_event_handler():
+    name, prefactor, sigma, modules = _in_child("build_handler_with_gpu_potential")
+    assert (name, prefactor, sigma) == ("GpuLennardJonesPotential", 2.0, 1.1)
+    assert len(modules) == 5
+
+
+@pytest.mark.parametrize("name", trajectory_names())
+def test_mediator_translates_the_reference_configuration(name):
+    spec, initial, charges, events, final = load_trajectory(name)
+    plan = _in_child("translate_configuration", name)
+    assert (plan["chains"], plan["mode"], plan["seed"]) == (3, "exact", 5)
+    s = plan["spec"]
+    expected = dict(n=spec["n"], system_length=spec["system_length"], cells_per_side=spec["cells_per_side"],
+                    neighbor_layers=spec["neighbor_layers"], beta=spec["beta"], chain_time=spec["chain_time"],
+                    far=spec["far"], initial_active=0, initial_direction=0, speed=1.0, potential=spec["potential"],
+                    max_occupants=1)
+    for key, value in expected.items():
+        assert s[key] == value, key
+    if spec["potential"] in ("hard_sphere", "coulomb"):
+        assert s["hs_radius"] == spec["radius"]
+    if spec["far"] != "none":
+        assert (s["estimator_points"], s["estimator_prefactor"]) == (spec["estimator_points"],
+                                                                    spec["estimator_prefactor"])
+    assert np.array_equal(np.array(plan["positions"]), initial)
+    if charges is not None:
+        assert np.array_equal(np.array(plan["charges"]), charges)
+    assert plan["end_of_run_time"] == 1e9
