@@ -35,10 +35,11 @@ WORKLOAD = dict(workload="lennard_jones_chains_4096x1024_cell_bounding", chains=
                 jitter=0.05, estimator_points=10, estimator_prefactor=1.5)
 NEAR_CELLS = (2 * WORKLOAD["neighbor_layers"] + 1) ** 3  # cells scanned for pair candidates per event
 CPU_SECONDS = 10.0  # wall time of the CPU baseline sample
+TIMING_STRIDE = 16  # event rounds between two rounds bracketed by per-kernel CUDA events
 # DRAM traffic of the screening kernel per event: ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch of
-# this workload divided by the events of that launch (profiles/screen_kernel_lennard_jones_4096x1024.md); None if
-# not captured
-NCU_TRAFFIC_PER_EVENT = None
+# this workload (56.50 MB + 0.40 MB) divided by the 4096 events of that launch
+# (profiles/round_kernels_lennard_jones_4096x1024.md)
+NCU_TRAFFIC_PER_EVENT = (56.499712e6 + 0.400128e6) / 4096
 
 
 def parse():
@@ -181,7 +182,8 @@ def reference_arm(args):
     if rank != 0:
         return
     threads = host_threads()
-    seconds = 3.0
+    # each step a bounded sample: the timed steps take about 90 s of wall time in total
+    seconds = max(0.2, min(3.0, 90.0 / max(args.steps, 1)))
     with concurrent.futures.ThreadPoolExecutor(max_workers=threads) as pool:
         chains = cpu_chains(threads, pool)
         for _ in range(args.warmup):
@@ -246,8 +248,9 @@ def gpu_arm(args):
                                  (args.groups,) if args.groups else (1, 2, 4))
     batch.set_block_warps(warps)
     batch.set_groups(groups)
-    # per-kernel CUDA events on the launching streams stay on through the warm-up and the timed region
-    batch.set_timing(True)
+    # per-kernel CUDA events on the launching streams stay on through the warm-up and the timed region, around
+    # every TIMING_STRIDE-th event round
+    batch.set_timing(True, stride=TIMING_STRIDE)
     for _ in range(args.warmup):
         batch.run(args.events, mode="mixed")
     batch.check_status()
@@ -338,8 +341,8 @@ def gpu_arm(args):
     # nearby cells, FP32 position and identifier of every pair candidate, active position write, cell index and time)
     # times the events of one launch, over its mean CUDA-event duration on its stream in the timed region
     screen = kernel_times["screen"]
-    screen_launches = max(screen["launches"], 1)
-    events_per_launch = events_done / screen_launches
+    screen_launches = max(screen["launches"], 1)  # the timed launches
+    events_per_launch = events_done / max(launches / 3, 1)  # three kernels per event round and chain group
     nb = candidates / max(events_done, 1)
     bytes_per_event = 4 * NEAR_CELLS + 12 * nb + 4 * nb + 32
     screen_s = screen["ms"] / screen_launches / 1000.0

@@ -267,9 +267,11 @@ int64_t jfgpu_engine_launch_count(const JfgpuEngine *engine);
 #define JFGPU_KERNEL_OBSERVE 5         /* observables of jfgpu_chains_observe */
 #define JFGPU_KERNEL_KINDS 6
 
-/* Per-kernel device time.  While timing is on, the chain launches of jfgpu_chains_init / jfgpu_chains_run are
- * bracketed by CUDA events on the stream they are launched on.  jfgpu_engine_kernel_times waits for those events
- * and returns, per kernel kind, the milliseconds and launches accumulated since the last reset (arrays of
+/* Per-kernel device time.  While timing is on (enable = k >= 1), the chain launches of jfgpu_chains_init,
+ * jfgpu_chains_run and jfgpu_chains_observe are bracketed by CUDA events on the stream they are launched on; in
+ * the mixed mode only every k-th event round is bracketed (k = 1: all), so that the events barely perturb the
+ * run they measure.  enable = 0 switches timing off.  jfgpu_engine_kernel_times waits for those events and
+ * returns, per kernel kind, the milliseconds and the timed launches accumulated since the last reset (arrays of
  * JFGPU_KERNEL_KINDS entries; reset != 0 clears the totals after reading). */
 int jfgpu_engine_set_timing(JfgpuEngine *engine, int32_t enable);
 int jfgpu_engine_kernel_times(JfgpuEngine *engine, double *milliseconds, int64_t *launches, int32_t reset);

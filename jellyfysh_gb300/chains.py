@@ -208,9 +208,11 @@ class ChainBatch:
                        "jfgpu_chains_observe")
         return energy, histogram
 
-    def set_timing(self, enable: bool) -> None:
-        """Bracket every chain launch by CUDA events on its stream (read back by kernel_times)."""
-        _lib.check(self.lib.jfgpu_engine_set_timing(self._engine, 1 if enable else 0), "jfgpu_engine_set_timing")
+    def set_timing(self, enable: bool, stride: int = 1) -> None:
+        """Bracket the chain launches by CUDA events on their streams (read back by kernel_times); in the mixed
+        mode every `stride`-th event round only."""
+        _lib.check(self.lib.jfgpu_engine_set_timing(self._engine, int(stride) if enable else 0),
+                   "jfgpu_engine_set_timing")
 
     def kernel_times(self, reset: bool = True) -> dict:
         """Device milliseconds and launches per kernel kind since the last reset (waits for the events)."""

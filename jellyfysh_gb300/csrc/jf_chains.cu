@@ -1349,11 +1349,11 @@ template <int POT, int FAR>
 static long long launch_mixed_rounds(const GroupLaunch *groups, int n_groups, long long rounds, int warps,
                                      KernelClock *clock) {
     long long launches = 0;
-    if (clock)
-        for (int g = 0; g < n_groups; ++g) clock->begin(groups[g].stream);
     for (long long r = 0; r < rounds; ++r) {
+        KernelClock *timed = (clock && r % clock->stride == 0) ? clock : nullptr;
         for (int g = 0; g < n_groups; ++g) {
             const GroupLaunch &G = groups[g];
+            if (timed) timed->begin(G.stream);
             const long long count = G.args.count;
             const long long screen_blocks = (count + warps - 1) / warps;
             // every queued entry plus the padding of each path to whole warps
@@ -1361,13 +1361,13 @@ static long long launch_mixed_rounds(const GroupLaunch *groups, int n_groups, lo
             const long long resolve_blocks = (count + 31) / 32;  // one warp per block: resolve spreads over the SMs
             screen_kernel<POT, FAR><<<(unsigned)screen_blocks, warps * 32, 0, G.stream>>>(G.args, G.lists, G.queue,
                                                                                          r);
-            if (clock) clock->end(G.stream, JFGPU_KERNEL_SCREEN);
+            if (timed) timed->end(G.stream, JFGPU_KERNEL_SCREEN);
             refine_kernel<POT, FAR><<<(unsigned)refine_blocks, 64, 0, G.stream>>>(G.args, G.lists, G.refined, G.queue,
                                                                                  r);
-            if (clock) clock->end(G.stream, JFGPU_KERNEL_REFINE);
+            if (timed) timed->end(G.stream, JFGPU_KERNEL_REFINE);
             resolve_kernel<POT, FAR><<<(unsigned)resolve_blocks, 32, 0, G.stream>>>(G.args, G.lists, G.refined,
                                                                                    G.queue, r);
-            if (clock) clock->end(G.stream, JFGPU_KERNEL_RESOLVE);
+            if (timed) timed->end(G.stream, JFGPU_KERNEL_RESOLVE);
             launches += 3;
         }
     }

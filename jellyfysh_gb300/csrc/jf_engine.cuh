@@ -72,6 +72,7 @@ struct KernelClock {
     virtual ~KernelClock() {}
     virtual void begin(cudaStream_t stream) = 0;            // an event before the next launch on the stream
     virtual void end(cudaStream_t stream, int kind) = 0;    // an event after a launch of this JFGPU_KERNEL_* kind
+    int stride = 1;  // the event rounds of the mixed mode that are timed: every stride-th round
 };
 
 // streams of a run: the caller's stream, or chain groups on streams of their own forked from it

@@ -702,8 +702,9 @@ int jfgpu_chains_set_groups(JfgpuEngine *e, int32_t groups) {
 }
 
 int jfgpu_engine_set_timing(JfgpuEngine *e, int32_t enable) {
-    if (!e) return JFGPU_ERROR_ARGUMENT;
+    if (!e || enable < 0) return JFGPU_ERROR_ARGUMENT;
     if (enable && !e->clock) e->clock = new EventClock();
+    if (enable) e->clock->stride = enable;
     if (!enable && e->clock) {
         e->clock->collect();
         delete e->clock;
