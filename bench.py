@@ -50,8 +50,8 @@ def parse():
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     p.add_argument("--events", type=int, default=128, help="events per chain and step")
     p.add_argument("--chains", type=int, default=WORKLOAD["chains"])
-    p.add_argument("--block-warps", type=int, default=0, help="warps per block (0 = autotune)")
-    p.add_argument("--groups", type=int, default=0, help="chain groups on streams of their own (0 = autotune)")
+    p.add_argument("--block-warps", type=int, default=4, help="warps per screening block (0 = autotune)")
+    p.add_argument("--groups", type=int, default=1, help="chain groups on streams of their own (0 = autotune)")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-fp64", action="store_true")
     return p.parse_args()

@@ -201,8 +201,9 @@ typedef struct {
     double *charges;              /* [particles] (may be NULL for uncharged systems) */
     int32_t *occupancy;           /* [occupancy_slots] */
     int32_t *surplus;             /* [particles] */
-    int32_t *roles;               /* [particles]: cell axes (x | y << 8 | z << 16) of every unit's occupancy entry,
-                                     bit 24 set for surplus units, bit 25 for the occupancy's active unit */
+    int32_t *roles;               /* [particles]: cell axes (x | y << 8 | z << 16) of every unit's occupancy entry;
+                                     for surplus units bit 24 and the unit's index in the surplus list instead;
+                                     bit 25 for the occupancy's active unit */
     JfgpuChainState *state;       /* [n_chains] */
 } JfgpuBuffers;
 

@@ -266,6 +266,12 @@ class ChainBatch:
         o = self.particle_offset[chain]
         return self.surplus_dev[o:o + n_surplus].cpu().numpy().copy()
 
+    def roles(self, chain: int) -> np.ndarray:
+        """Role word of every unit (cell axes x | y << 8 | z << 16; surplus units: bit 24 and their index in the
+        surplus list; the occupancy's active unit: bit 25)."""
+        o = self.particle_offset[chain]
+        return self.roles_dev[o:o + self.specs[chain].n].cpu().numpy().copy()
+
     def bounds(self, chain: int):
         spec = self.specs[chain]
         cells = spec.cells_per_side ** 3

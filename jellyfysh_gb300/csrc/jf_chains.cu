@@ -328,7 +328,8 @@ __device__ __noinline__ int single_candidates(const RunArgs &A, const ChainDev &
 // ---------------------------------------------------------------------------------------------------------------
 // occupancy (lane 0)
 // ---------------------------------------------------------------------------------------------------------------
-// role word of a unit: the axes of its occupancy cell, bit 24 for a surplus unit, bit 25 for the active unit
+// role word of a unit: the axes of its occupancy cell (x | y << 8 | z << 16); for a surplus unit bit 24 and its
+// index in the chain's surplus list instead of the axes; bit 25 for the occupancy's active unit
 constexpr int32_t kRoleSurplus = 1 << 24;
 constexpr int32_t kRoleActive = 1 << 25;
 
@@ -347,7 +348,7 @@ __device__ inline void occ_insert(const RunArgs &A, const ChainDev &ch, WarpStat
             return;
         }
     A.surplus[ch.pos_off + w.n_surplus] = id;
-    A.roles[ch.pos_off + id] = role_of_cell(ch, cell) | kRoleSurplus;
+    A.roles[ch.pos_off + id] = kRoleSurplus | w.n_surplus;
     w.n_surplus += 1;
 }
 
@@ -356,6 +357,7 @@ __device__ __noinline__ int occ_update(const RunArgs &A, const ChainDev &ch, War
         if (w.occ_active >= 0) occ_insert(A, ch, w, w.occ_cell, w.occ_active);
         JF_TRY(cell_of(A.view, ch, w.pa, w.occ_cell));
         w.occ_active = w.active;
+        const int32_t role = A.roles[ch.pos_off + w.active];
         A.roles[ch.pos_off + w.active] = kRoleActive;
         int32_t *slots = A.occupancy + ch.occ_off + (long long)w.occ_cell * ch.max_occ;
         for (int k = 0; k < ch.max_occ; ++k)
@@ -363,14 +365,17 @@ __device__ __noinline__ int occ_update(const RunArgs &A, const ChainDev &ch, War
                 slots[k] = -1;
                 return JFGPU_STATUS_OK;
             }
+        // a surplus unit: its role word (read before it was overwritten above) holds its index in the list;
+        // the last entry moves into its place (SingleActiveCellOccupancy._surplus keeps no order)
         int32_t *sur = A.surplus + ch.pos_off;
-        for (int k = 0; k < w.n_surplus; ++k)
-            if (sur[k] == w.active) {
-                sur[k] = sur[w.n_surplus - 1];
-                w.n_surplus -= 1;
-                return JFGPU_STATUS_OK;
-            }
-        return JFGPU_STATUS_ASSERTION;
+        if (!(role & kRoleSurplus)) return JFGPU_STATUS_ASSERTION;
+        const int k = role & 0xFFFFFF;
+        if (k >= w.n_surplus || sur[k] != w.active) return JFGPU_STATUS_ASSERTION;
+        const int last = sur[w.n_surplus - 1];
+        sur[k] = last;
+        if (last != w.active) A.roles[ch.pos_off + last] = kRoleSurplus | k;
+        w.n_surplus -= 1;
+        return JFGPU_STATUS_OK;
     }
     return cell_of(A.view, ch, w.pa, w.occ_cell);
 }
@@ -781,7 +786,16 @@ struct RefineList {
 
 // FP64 re-solves of the first kRefineSlots entries of every refine list, one thread per entry; the resolve kernel
 // takes the earliest of them (and solves any further entry itself)
-constexpr int kRefineSlots = 2;
+#ifndef JF_REFINE_SLOTS
+#define JF_REFINE_SLOTS 4
+#endif
+#ifndef JF_SOLO_FLAGGED
+#define JF_SOLO_FLAGGED 256
+#endif
+constexpr int kRefineSlots = JF_REFINE_SLOTS;
+// flagged entries (their branch of the case analysis unknown) are re-solved one per warp, up to this many a round:
+// a warp of mixed branches would run the union of the branches and hold up the round
+constexpr int kSoloFlagged = JF_SOLO_FLAGGED;
 
 // Refine queue of a chain group: per screening path, the entries (local chain * kRefineSlots + slot) to re-solve.
 // counts[kPaths] sit in the group's header; entries[path][...] use the slice [lo, hi) * kRefineSlots of the group's
@@ -792,9 +806,17 @@ struct RefineQueue {
     long long stride;  // n_chains * kRefineSlots
 };
 
+#ifndef JF_NEAR_COMPACT
+#define JF_NEAR_COMPACT 0
+#endif
+#ifndef JF_FAR_UNROLL
+#define JF_FAR_UNROLL 0
+#endif
+
 template <int POT, int FAR>
 __global__ void __launch_bounds__(256, 4) screen_kernel(RunArgs A, RefineList *lists, RefineQueue queue,
                                                         long long round) {
+    __shared__ int32_t near_buffer[8][64];  // per warp: compacted nearby candidates (fewer than 32 + 32 pending)
     const int warp = threadIdx.x >> 5;
     const int lane = threadIdx.x & 31;
     const long long local = (long long)blockIdx.x * (blockDim.x >> 5) + warp;
@@ -871,16 +893,124 @@ __global__ void __launch_bounds__(256, 4) screen_kernel(RunArgs A, RefineList *l
             const float du = expovariate32(draw_at(pair_base, (uint32_t)j), inv_beta32, flag);
             t = lj_screen(lj32, d, speed32, sv, du, margin, flag, path);
         }
-        if (flag) {
-            t = -1.0f;
-            path = kPathFlagged;
-        }
+        // a flagged candidate keeps the branch its FP32 solve took (the flag concerns the time, rarely the branch):
+        // its FP64 re-solve joins the warps of that branch
+        if (flag) t = -1.0f;
         if (!isinf(t)) topk_insert(key, code, t, make_code(j, path, false));
     };
+#if JF_NEAR_COMPACT
+    // Nearby occupants and surplus units, compacted into a per-warp buffer in shared memory so that every lane
+    // screens a candidate in each pass; the occupancy words of four cell batches are loaded before they are used.
+    {
+        int32_t *buf = near_buffer[warp];
+        int buffered = 0;  // warp-uniform
+        auto push = [&](int j) {
+            const bool has = j >= 0;
+            const unsigned mask = __ballot_sync(kFull, has);
+            if (has) buf[buffered + __popc(mask & ((1u << lane) - 1u))] = j;
+            buffered += __popc(mask);
+            __syncwarp();
+            if (buffered >= 32) {
+                const int mine = buf[lane];
+                const int rest = buffered - 32;
+                const int moved = lane < rest ? buf[32 + lane] : 0;
+                __syncwarp();
+                if (lane < rest) buf[lane] = moved;
+                __syncwarp();
+                buffered = rest;
+                screen_pair(mine);
+            }
+        };
+        int a[3];
+        cell_axes(ch, occ_cell, a);
+        const int K = ch.n_res, m = ch.m;
+        const int32_t *occ = A.occupancy + ch.occ_off;
+        Digits dg;
+        dg.start(lane, K);
+        const int near_cells = K * K * K;
+        for (int first = 0; first < near_cells; first += 4 * 32) {
+            int cell[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                cell[u] = -1;
+                if (dg.z < K) {
+                    int cx = a[0] + ch.res[dg.x], cy = a[1] + ch.res[dg.y], cz = a[2] + ch.res[dg.z];
+                    if (cx >= m) cx -= m;
+                    if (cy >= m) cy -= m;
+                    if (cz >= m) cz -= m;
+                    cell[u] = cx + m * (cy + m * cz);
+                    dg.advance();
+                }
+            }
+            for (int k = 0; k < ch.max_occ; ++k) {
+                int j[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) j[u] = cell[u] >= 0 ? occ[(long long)cell[u] * ch.max_occ + k] : -1;
+#pragma unroll
+                for (int u = 0; u < 4; ++u) push(j[u]);
+            }
+        }
+        for (int i0 = 0; i0 < n_surplus; i0 += 32) push(i0 + lane < n_surplus ? A.surplus[ch.pos_off + i0 + lane] : -1);
+        if (buffered > 0) {
+            const int mine = lane < buffered ? buf[lane] : -1;
+            __syncwarp();
+            if (mine >= 0) screen_pair(mine);
+        }
+    }
+#else
     for_each_near(A, ch, occ_cell, lane, screen_pair);
     for (int i = lane; i < n_surplus; i += 32) screen_pair(A.surplus[ch.pos_off + i]);
+#endif
     float base = fminf(warp_min_float(lane_min_unflagged(key)), t_single);
     if (far_of<FAR>(ch) == JFGPU_FAR_CELL_BOUNDING) {
+#if JF_FAR_UNROLL
+        // far units (one coalesced pass over the role words, four units per lane in flight) with the rigorous early
+        // rejection -log(1 - u) >= u: a far time is at least u / (beta rate speed)
+        const float threshold0 = isinf(base) ? kInf32 : base * rel + abs_margin;
+        const float reject = threshold0 * speed32 * (1.0f + 1.0f / 65536.0f) / inv_beta32;
+        const float *rates = sp.bound_upper32;
+        int a[3];
+        cell_axes(ch, occ_cell, a);
+        const int m = ch.m;
+        const int32_t *roles = A.roles + ch.pos_off;
+        const int16_t *rel_table = A.view.rel + ch.table_offset;
+        for (int j0 = lane; j0 < ch.n; j0 += 4 * 32) {
+            int32_t role[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) role[u] = j0 + 32 * u < ch.n ? roles[j0 + 32 * u] : kRoleActive;
+            float rate[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                rate[u] = 0.0f;
+                const int32_t r = role[u];
+                if (r & (kRoleActive | kRoleSurplus)) continue;
+                const int cx = r & 0xFF, cy = (r >> 8) & 0xFF, cz = (r >> 16) & 0xFF;
+                int dx = cx - a[0], dy = cy - a[1], dz = cz - a[2];
+                if (dx < 0) dx += m;
+                if (dy < 0) dy += m;
+                if (dz < 0) dz += m;
+                if (((ch.near_mask >> dx) & 1ull) && ((ch.near_mask >> dy) & 1ull) && ((ch.near_mask >> dz) & 1ull))
+                    continue;
+                const int rc = ch.rel_is_mod ? dx + m * (dy + m * dz)
+                                             : rel_table[cx * m + a[0]] +
+                                                   m * (rel_table[cy * m + a[1]] + m * rel_table[cz * m + a[2]]);
+                rate[u] = rates[rc * 3 + d];
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                if (!(rate[u] > 0.0f)) continue;
+                const int j = j0 + 32 * u;
+                const uint64_t bits = draw_at(pair_base, (uint32_t)j);
+                const float u_low = (float)(uint32_t)(bits >> 40) * (1.0f / 16777216.0f);
+                if (u_low > reject * rate[u]) continue;
+                bool flag = false;
+                const float du = expovariate32(bits, inv_beta32, flag);
+                float t = (du / rate[u]) / speed32;
+                if (flag) t = -1.0f;
+                if (!isinf(t)) topk_insert(key, code, t, make_code(j, kPathFar, true));
+            }
+        }
+#else
         // far units (one coalesced pass over the role words) with the rigorous early rejection
         // -log(1 - u) >= u: a far time is at least u / (beta rate speed)
         const float threshold0 = isinf(base) ? kInf32 : base * rel + abs_margin;
@@ -899,22 +1029,25 @@ __global__ void __launch_bounds__(256, 4) screen_kernel(RunArgs A, RefineList *l
                           if (flag) t = -1.0f;
                           if (!isinf(t)) topk_insert(key, code, t, make_code(j, kPathFar, true));
                       });
+#endif
         base = fminf(base, warp_min_float(lane_min_unflagged(key)));
     }
     const float threshold = isinf(base) ? kInf32 : base * rel + abs_margin;
     // compaction of the candidates inside the threshold into the chain's refine list
     int overflow = (code[kTopK - 1] >= 0 && key[kTopK - 1] <= threshold) ? 1 : 0;
     int total = 0;
-    static_assert(kRefineSlots == 2, "the queued entries of a lane are held in two registers");
-    int queued0 = -1, queued1 = -1;  // the lane's entries at list offsets 0 and 1, if any (one lane may hold both)
+    int queued[kRefineSlots];  // the lane's entries at list offsets 0 .. kRefineSlots - 1, if any
+#pragma unroll
+    for (int q = 0; q < kRefineSlots; ++q) queued[q] = -1;
 #pragma unroll
     for (int i = 0; i < kTopK; ++i) {
         const bool take = code[i] >= 0 && key[i] <= threshold;
         const unsigned mask = __ballot_sync(kFull, take);
         const int offset = total + __popc(mask & ((1u << lane) - 1u));
         if (take && offset < kRefineMax) list.code[offset] = code[i];
-        if (take && offset == 0) queued0 = code[i];
-        if (take && offset == 1) queued1 = code[i];
+#pragma unroll
+        for (int q = 0; q < kRefineSlots; ++q)
+            if (take && offset == q) queued[q] = code[i];
         total += __popc(mask);
     }
     overflow = warp_max_int(overflow) || total > kRefineMax;
@@ -926,15 +1059,12 @@ __global__ void __launch_bounds__(256, 4) screen_kernel(RunArgs A, RefineList *l
     }
     // the entries at the first kRefineSlots offsets go to the queues of their paths
     if (!overflow) {
-        if (queued0 >= 0) {
-            const int path = code_path(queued0);
+#pragma unroll
+        for (int q = 0; q < kRefineSlots; ++q) {
+            if (queued[q] < 0) continue;
+            const int path = code_path(queued[q]);
             const int at = atomicAdd(queue.counts + path, 1);
-            queue.entries[path * queue.stride + at] = (int32_t)(local * kRefineSlots);
-        }
-        if (queued1 >= 0) {
-            const int path = code_path(queued1);
-            const int at = atomicAdd(queue.counts + path, 1);
-            queue.entries[path * queue.stride + at] = (int32_t)(local * kRefineSlots + 1);
+            queue.entries[path * queue.stride + at] = (int32_t)(local * kRefineSlots + q);
         }
     }
 }
@@ -979,10 +1109,18 @@ __global__ void __launch_bounds__(64) refine_kernel(RunArgs A, const RefineList 
 #pragma unroll
     for (int k = 0; k < kPaths; ++k) {
         const long long n = queue.counts[k];
-        const long long padded = (n + 31) & ~31LL;
+        // flagged entries: the first kSoloFlagged one per warp (lane 0), the rest packed
+        const long long solo = k == kPathFlagged ? (n < kSoloFlagged ? n : kSoloFlagged) : 0;
+        const long long padded = solo * 32 + ((n - solo + 31) & ~31LL);
         if (path < 0 && t < start + padded) {
             path = k;
-            index = t - start;
+            const long long offset = t - start;
+            if (offset < solo * 32) {
+                if (offset % 32) return;
+                index = offset / 32;
+            } else {
+                index = solo + (offset - solo * 32);
+            }
             if (index >= n) return;
         }
         start += padded;
@@ -1059,6 +1197,7 @@ __global__ void __launch_bounds__(32) resolve_kernel(RunArgs A, const RefineList
     load_lifting(g, A, ch, w);
     w.candidates += list.screened;
     w.refined += list.count;
+
     Cand best = cand_none();
     int st = single_candidates(A, ch, sp, w, w.occ_cell, w.events, best);
     if (!st) {
@@ -1262,8 +1401,8 @@ __global__ void init_kernel(EngineView view, long long n_chains, double *positio
             slots[k] = i;
             roles[ch.pos_off + i] = role_of_cell(ch, cell);
         } else {
+            roles[ch.pos_off + i] = kRoleSurplus | n_surplus;
             surplus[ch.pos_off + n_surplus++] = i;
-            roles[ch.pos_off + i] = role_of_cell(ch, cell) | kRoleSurplus;
         }
     }
     JfgpuChainState g;
@@ -1357,7 +1496,7 @@ static long long launch_mixed_rounds(const GroupLaunch *groups, int n_groups, lo
             const long long count = G.args.count;
             const long long screen_blocks = (count + warps - 1) / warps;
             // every queued entry plus the padding of each path to whole warps
-            const long long refine_blocks = (count * kRefineSlots + kPaths * 31 + 63) / 64;
+            const long long refine_blocks = (count * kRefineSlots + kPaths * 31 + kSoloFlagged * 31 + 63) / 64;
             const long long resolve_blocks = (count + 31) / 32;  // one warp per block: resolve spreads over the SMs
             screen_kernel<POT, FAR><<<(unsigned)screen_blocks, warps * 32, 0, G.stream>>>(G.args, G.lists, G.queue,
                                                                                          r);

@@ -22,7 +22,7 @@ constexpr int kPathFrontInside = 3;    // in front, inside the shell
 constexpr int kPathBehindInside = 4;   // behind, inside the shell
 constexpr int kPathHardSphere = 5;
 constexpr int kPathFar = 6;            // far-field (cell-bounding) candidate
-constexpr int kPathFlagged = 7;        // flagged by the screening: path unknown
+constexpr int kPathFlagged = 7;        // path unknown (kept for candidates of no classified branch)
 constexpr int kPaths = 8;
 
 // potential change of a keyed draw in FP32 without FP64 instructions: the uniform is (bits >> 11) 2^-53; its top 32

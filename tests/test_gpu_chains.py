@@ -142,13 +142,27 @@ def test_chain_groups_and_kernel_timing_leave_results_unchanged():
 
 
 def _occupancy_consistent(batch, chain):
+    """Every unit is in exactly one place (a cell slot, the surplus list or active), and the role words agree."""
     spec = batch.specs[chain]
-    occ = batch.occupancy(chain).ravel()
-    ids = list(occ[occ >= 0]) + list(batch.surplus(chain))
+    occupancy = batch.occupancy(chain)
+    occ = occupancy.ravel()
+    surplus = batch.surplus(chain)
+    ids = list(occ[occ >= 0]) + list(surplus)
     state = batch.state()[chain]
     if state["occ_active"] >= 0:
         ids.append(int(state["occ_active"]))
-    return sorted(ids) == list(range(spec.n))
+    if sorted(ids) != list(range(spec.n)):
+        return False
+    roles = batch.roles(chain)
+    m = spec.cells_per_side
+    for k, j in enumerate(surplus):
+        if roles[j] != (1 << 24) | k:
+            return False
+    for cell, slots in enumerate(occupancy):
+        axes = (cell % m) | (((cell // m) % m) << 8) | ((cell // (m * m)) << 16)
+        if any(roles[j] != axes for j in slots if j >= 0):
+            return False
+    return state["occ_active"] < 0 or roles[state["occ_active"]] == 1 << 25
 
 
 def test_random_hard_sphere_systems_against_oracle():
@@ -192,6 +206,7 @@ def test_random_hard_sphere_systems_against_oracle():
     for c in range(len(specs)):
         for field in logs.dtype.names:
             assert np.array_equal(mixed_logs[c][field], logs[c][field]), (c, field)
+        assert _occupancy_consistent(mixed, c)
     batch.close()
     mixed.close()
 
