@@ -806,17 +806,9 @@ struct RefineQueue {
     long long stride;  // n_chains * kRefineSlots
 };
 
-#ifndef JF_NEAR_COMPACT
-#define JF_NEAR_COMPACT 0
-#endif
-#ifndef JF_FAR_UNROLL
-#define JF_FAR_UNROLL 0
-#endif
-
 template <int POT, int FAR>
 __global__ void __launch_bounds__(256, 4) screen_kernel(RunArgs A, RefineList *lists, RefineQueue queue,
                                                         long long round) {
-    __shared__ int32_t near_buffer[8][64];  // per warp: compacted nearby candidates (fewer than 32 + 32 pending)
     const int warp = threadIdx.x >> 5;
     const int lane = threadIdx.x & 31;
     const long long local = (long long)blockIdx.x * (blockDim.x >> 5) + warp;
@@ -898,119 +890,10 @@ __global__ void __launch_bounds__(256, 4) screen_kernel(RunArgs A, RefineList *l
         if (flag) t = -1.0f;
         if (!isinf(t)) topk_insert(key, code, t, make_code(j, path, false));
     };
-#if JF_NEAR_COMPACT
-    // Nearby occupants and surplus units, compacted into a per-warp buffer in shared memory so that every lane
-    // screens a candidate in each pass; the occupancy words of four cell batches are loaded before they are used.
-    {
-        int32_t *buf = near_buffer[warp];
-        int buffered = 0;  // warp-uniform
-        auto push = [&](int j) {
-            const bool has = j >= 0;
-            const unsigned mask = __ballot_sync(kFull, has);
-            if (has) buf[buffered + __popc(mask & ((1u << lane) - 1u))] = j;
-            buffered += __popc(mask);
-            __syncwarp();
-            if (buffered >= 32) {
-                const int mine = buf[lane];
-                const int rest = buffered - 32;
-                const int moved = lane < rest ? buf[32 + lane] : 0;
-                __syncwarp();
-                if (lane < rest) buf[lane] = moved;
-                __syncwarp();
-                buffered = rest;
-                screen_pair(mine);
-            }
-        };
-        int a[3];
-        cell_axes(ch, occ_cell, a);
-        const int K = ch.n_res, m = ch.m;
-        const int32_t *occ = A.occupancy + ch.occ_off;
-        Digits dg;
-        dg.start(lane, K);
-        const int near_cells = K * K * K;
-        for (int first = 0; first < near_cells; first += 4 * 32) {
-            int cell[4];
-#pragma unroll
-            for (int u = 0; u < 4; ++u) {
-                cell[u] = -1;
-                if (dg.z < K) {
-                    int cx = a[0] + ch.res[dg.x], cy = a[1] + ch.res[dg.y], cz = a[2] + ch.res[dg.z];
-                    if (cx >= m) cx -= m;
-                    if (cy >= m) cy -= m;
-                    if (cz >= m) cz -= m;
-                    cell[u] = cx + m * (cy + m * cz);
-                    dg.advance();
-                }
-            }
-            for (int k = 0; k < ch.max_occ; ++k) {
-                int j[4];
-#pragma unroll
-                for (int u = 0; u < 4; ++u) j[u] = cell[u] >= 0 ? occ[(long long)cell[u] * ch.max_occ + k] : -1;
-#pragma unroll
-                for (int u = 0; u < 4; ++u) push(j[u]);
-            }
-        }
-        for (int i0 = 0; i0 < n_surplus; i0 += 32) push(i0 + lane < n_surplus ? A.surplus[ch.pos_off + i0 + lane] : -1);
-        if (buffered > 0) {
-            const int mine = lane < buffered ? buf[lane] : -1;
-            __syncwarp();
-            if (mine >= 0) screen_pair(mine);
-        }
-    }
-#else
     for_each_near(A, ch, occ_cell, lane, screen_pair);
     for (int i = lane; i < n_surplus; i += 32) screen_pair(A.surplus[ch.pos_off + i]);
-#endif
     float base = fminf(warp_min_float(lane_min_unflagged(key)), t_single);
     if (far_of<FAR>(ch) == JFGPU_FAR_CELL_BOUNDING) {
-#if JF_FAR_UNROLL
-        // far units (one coalesced pass over the role words, four units per lane in flight) with the rigorous early
-        // rejection -log(1 - u) >= u: a far time is at least u / (beta rate speed)
-        const float threshold0 = isinf(base) ? kInf32 : base * rel + abs_margin;
-        const float reject = threshold0 * speed32 * (1.0f + 1.0f / 65536.0f) / inv_beta32;
-        const float *rates = sp.bound_upper32;
-        int a[3];
-        cell_axes(ch, occ_cell, a);
-        const int m = ch.m;
-        const int32_t *roles = A.roles + ch.pos_off;
-        const int16_t *rel_table = A.view.rel + ch.table_offset;
-        for (int j0 = lane; j0 < ch.n; j0 += 4 * 32) {
-            int32_t role[4];
-#pragma unroll
-            for (int u = 0; u < 4; ++u) role[u] = j0 + 32 * u < ch.n ? roles[j0 + 32 * u] : kRoleActive;
-            float rate[4];
-#pragma unroll
-            for (int u = 0; u < 4; ++u) {
-                rate[u] = 0.0f;
-                const int32_t r = role[u];
-                if (r & (kRoleActive | kRoleSurplus)) continue;
-                const int cx = r & 0xFF, cy = (r >> 8) & 0xFF, cz = (r >> 16) & 0xFF;
-                int dx = cx - a[0], dy = cy - a[1], dz = cz - a[2];
-                if (dx < 0) dx += m;
-                if (dy < 0) dy += m;
-                if (dz < 0) dz += m;
-                if (((ch.near_mask >> dx) & 1ull) && ((ch.near_mask >> dy) & 1ull) && ((ch.near_mask >> dz) & 1ull))
-                    continue;
-                const int rc = ch.rel_is_mod ? dx + m * (dy + m * dz)
-                                             : rel_table[cx * m + a[0]] +
-                                                   m * (rel_table[cy * m + a[1]] + m * rel_table[cz * m + a[2]]);
-                rate[u] = rates[rc * 3 + d];
-            }
-#pragma unroll
-            for (int u = 0; u < 4; ++u) {
-                if (!(rate[u] > 0.0f)) continue;
-                const int j = j0 + 32 * u;
-                const uint64_t bits = draw_at(pair_base, (uint32_t)j);
-                const float u_low = (float)(uint32_t)(bits >> 40) * (1.0f / 16777216.0f);
-                if (u_low > reject * rate[u]) continue;
-                bool flag = false;
-                const float du = expovariate32(bits, inv_beta32, flag);
-                float t = (du / rate[u]) / speed32;
-                if (flag) t = -1.0f;
-                if (!isinf(t)) topk_insert(key, code, t, make_code(j, kPathFar, true));
-            }
-        }
-#else
         // far units (one coalesced pass over the role words) with the rigorous early rejection
         // -log(1 - u) >= u: a far time is at least u / (beta rate speed)
         const float threshold0 = isinf(base) ? kInf32 : base * rel + abs_margin;
@@ -1029,7 +912,6 @@ __global__ void __launch_bounds__(256, 4) screen_kernel(RunArgs A, RefineList *l
                           if (flag) t = -1.0f;
                           if (!isinf(t)) topk_insert(key, code, t, make_code(j, kPathFar, true));
                       });
-#endif
         base = fminf(base, warp_min_float(lane_min_unflagged(key)));
     }
     const float threshold = isinf(base) ? kInf32 : base * rel + abs_margin;
