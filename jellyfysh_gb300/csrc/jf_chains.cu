@@ -872,7 +872,6 @@ __global__ void __launch_bounds__(256, 4) screen_kernel(RunArgs A, RefineList *l
     const uint64_t pair_base = draw_base(ch.key, ev, kRngPair);
     int count = 0;
     auto screen_pair = [&](int j) {
-        ++count;
         const float4 pj = A.positions32[ch.pos_off + j];
         float sv[3];
         bool flag = false;
@@ -890,8 +889,91 @@ __global__ void __launch_bounds__(256, 4) screen_kernel(RunArgs A, RefineList *l
         if (flag) t = -1.0f;
         if (!isinf(t)) topk_insert(key, code, t, make_code(j, path, false));
     };
-    for_each_near(A, ch, occ_cell, lane, screen_pair);
-    for (int i = lane; i < n_surplus; i += 32) screen_pair(A.surplus[ch.pos_off + i]);
+    // Pre-test of every nearby occupant and surplus unit: a candidate whose event cannot come before the single
+    // candidates (cell boundary, end of chain) is dropped before its logarithm and inversion.  Along the active's
+    // move x in [0, D] (D the single candidates' time, padded) the distance to the target is smallest at
+    // x* = clamp(s_d, 0, D).  Hard spheres: no contact if that distance exceeds the diameter.  Lennard-Jones: if the
+    // whole path stays outside the minimum shell, U rises by at most |U(r_min)| (it falls towards r_min and rises
+    // after), and an event needs du = -log(1 - u) / beta <= |U(r_min)|, impossible for u > beta |U(r_min)|.  Both
+    // tests carry relative margins far above FP32 rounding.  The kept candidates are compacted per warp so that
+    // every lane solves one in each pass.
+    const float horizon = (t_single * rel + abs_margin) * speed32;
+    const float shell32 = potential_of<POT>(ch) == JFGPU_POT_HARD_SPHERE ? ch.diameter_sq32 : lj32.r0_sq;
+    const float beta32 = 1.0f / inv_beta32;
+    auto keep = [&](int j) -> bool {
+        const float4 pj = A.positions32[ch.pos_off + j];
+        float sv[3];
+        bool flag = false;
+        separation32(pa32, pj, ch.L32, ch.half32, margin, sv, flag);
+        if (flag) return true;
+        const float sd = sv[d];
+        const float pa = d == 0 ? sv[1] : sv[0];
+        const float pb = d == 2 ? sv[1] : sv[2];
+        const float x = fminf(fmaxf(sd, 0.0f), horizon);
+        const float gap = sd - x;
+        const float r_min_sq = (gap * gap + (pa * pa + pb * pb)) * (1.0f - 1.0f / 4096.0f);
+        if (!(r_min_sq > shell32 * (1.0f + 1.0f / 4096.0f))) return true;
+        if (potential_of<POT>(ch) == JFGPU_POT_HARD_SPHERE) return false;
+        const float ir2 = 1.0f / r_min_sq;
+        const float ir6 = ir2 * ir2 * ir2;
+        const float rise = -((lj32.a12 * ir6 + lj32.a6) * ir6);  // |U(r_min)|, U < 0 outside the shell
+        const uint64_t bits = draw_at(pair_base, (uint32_t)j);
+        const float u_low = (float)(uint32_t)(bits >> 40) * (1.0f / 16777216.0f);
+        return !(u_low > beta32 * rise * (1.0f + 1.0f / 1024.0f));
+    };
+    {
+        __shared__ int32_t pending[8][64];  // per warp: kept candidates not yet solved (fewer than 32 + 32)
+        int32_t *buf = pending[warp];
+        int buffered = 0;  // warp-uniform
+        int axes[3];
+        cell_axes(ch, occ_cell, axes);
+        const int K = ch.n_res, m = ch.m;
+        const int32_t *occ = A.occupancy + ch.occ_off;
+        const int cell_iters = (K * K * K + 31) / 32;
+        const int near_iters = cell_iters * ch.max_occ;
+        const int iters = near_iters + (n_surplus + 31) / 32;
+        Digits dg;
+        int batch = 0, slot = 0;
+        for (int it = 0; it < iters; ++it) {
+            int j = -1;
+            if (it < near_iters) {
+                if (batch == 0) dg.start(lane, K);
+                if (dg.z < K) {
+                    int cx = axes[0] + ch.res[dg.x], cy = axes[1] + ch.res[dg.y], cz = axes[2] + ch.res[dg.z];
+                    if (cx >= m) cx -= m;
+                    if (cy >= m) cy -= m;
+                    if (cz >= m) cz -= m;
+                    j = occ[(long long)(cx + m * (cy + m * cz)) * ch.max_occ + slot];
+                }
+                dg.advance();
+                if (++batch == cell_iters) {
+                    batch = 0;
+                    ++slot;
+                }
+            } else {
+                const int i = (it - near_iters) * 32 + lane;
+                if (i < n_surplus) j = A.surplus[ch.pos_off + i];
+            }
+            bool kept = false;
+            if (j >= 0) {
+                ++count;
+                kept = keep(j);
+            }
+            const unsigned mask = __ballot_sync(kFull, kept);
+            if (kept) buf[buffered + __popc(mask & ((1u << lane) - 1u))] = j;
+            buffered += __popc(mask);
+            __syncwarp();
+            if (buffered >= 32) {
+                buffered -= 32;
+                const int mine = buf[buffered + lane];
+                __syncwarp();
+                screen_pair(mine);
+            }
+        }
+        const int mine = lane < buffered ? buf[lane] : -1;
+        __syncwarp();
+        if (mine >= 0) screen_pair(mine);
+    }
     float base = fminf(warp_min_float(lane_min_unflagged(key)), t_single);
     if (far_of<FAR>(ch) == JFGPU_FAR_CELL_BOUNDING) {
         // far units (one coalesced pass over the role words) with the rigorous early rejection
