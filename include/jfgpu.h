@@ -256,6 +256,11 @@ int jfgpu_chains_observe(JfgpuEngine *engine, const JfgpuBuffers *buffers, int64
  * stream, so that one group's FP64 re-solves overlap another group's FP32 screening.  Default 1. */
 int jfgpu_chains_set_groups(JfgpuEngine *engine, int32_t groups);
 
+/* CUDA graphs for the event rounds of the mixed mode (default on): the launches of a run call are captured once per
+ * shape (chains, rounds, stop time, buffers, launch shape) and replayed as one graph launch afterwards; calls with
+ * an event log, or on a stream the caller is capturing, launch plainly.  Results are identical either way. */
+int jfgpu_chains_set_graphs(JfgpuEngine *engine, int32_t enable);
+
 /* Kernel launches issued by the library since the engine was created (all kernels of this library). */
 int64_t jfgpu_engine_launch_count(const JfgpuEngine *engine);
 

@@ -183,6 +183,10 @@ class ChainBatch:
     def set_block_warps(self, warps: int) -> None:
         _lib.check(self.lib.jfgpu_chains_set_block_warps(self._engine, int(warps)), "jfgpu_chains_set_block_warps")
 
+    def set_graphs(self, enable: bool) -> None:
+        """Replay the event rounds of the mixed mode from captured CUDA graphs (default) or launch them plainly."""
+        _lib.check(self.lib.jfgpu_chains_set_graphs(self._engine, 1 if enable else 0), "jfgpu_chains_set_graphs")
+
     def set_groups(self, groups: int) -> None:
         """Split the chains of every mixed-mode run into ``groups`` groups on streams of their own."""
         with self._torch.cuda.device(self.device):

@@ -20,6 +20,9 @@
 // the candidates within (1 + 2^-10) t_min + margin and every flagged one; the winner and its event time are
 // therefore the FP64 ones.  When a lane holds more than four candidates inside the margin the event is re-solved
 // entirely in FP64 (counted in refine_fallbacks).
+#include <cstring>
+#include <map>
+
 #include <cuda_runtime.h>
 
 #include "jf_engine.cuh"
@@ -644,16 +647,17 @@ __device__ inline void for_each_far(const RunArgs &A, const ChainDev &ch, int oc
     }
 }
 
-// Every non-active unit with its role (the cell-bounding far field makes every unit a candidate): surplus units and
+// Every non-active unit with its role word (from `roles`, the chain's role array in global or shared memory; the
+// cell-bounding far field makes every unit a candidate): surplus units and
 // occupants of nearby cells go to `near(j)`, occupants of the other cells to `far(j, rc)` with their relative cell.
 // The same partition as the taggers (ExcludedCellsTagger, SurplusCellsTagger, CellBoundingPotentialTagger), found by
 // one coalesced pass over the units instead of two passes over the cells.
 template <typename FN, typename FF>
-__device__ inline void for_each_unit(const RunArgs &A, const ChainDev &ch, int occ_cell, int lane, FN &&near, FF &&far) {
+__device__ inline void for_each_unit(const int32_t *roles, const RunArgs &A, const ChainDev &ch, int occ_cell, int lane,
+                                     FN &&near, FF &&far) {
     int a[3];
     cell_axes(ch, occ_cell, a);
     const int m = ch.m;
-    const int32_t *roles = A.roles + ch.pos_off;
     const int16_t *rel = A.view.rel + ch.table_offset;
     for (int j = lane; j < ch.n; j += 32) {
         const int32_t role = roles[j];
@@ -767,6 +771,10 @@ __device__ inline float lane_min_unflagged(const float (&key)[kTopK]) {
 // the FP64 path event for event.
 // ---------------------------------------------------------------------------------------------------------------
 constexpr int kRefineMax = 28;
+constexpr int kStagedRoles = 1024;  // units whose role words the screening kernel stages in shared memory
+// the screening kernels that may run the cell-bounding far field stage role words (dynamic shared memory)
+template <int FAR>
+__host__ __device__ constexpr bool stages_roles() { return FAR < 0 || FAR == JFGPU_FAR_CELL_BOUNDING; }
 constexpr int32_t kListOverflow = 1;
 constexpr int32_t kListSkip = 2;
 
@@ -808,7 +816,7 @@ struct RefineQueue {
 
 template <int POT, int FAR>
 __global__ void __launch_bounds__(256, 4) screen_kernel(RunArgs A, RefineList *lists, RefineQueue queue,
-                                                        long long round) {
+                                                        long long round, int first_round) {
     const int warp = threadIdx.x >> 5;
     const int lane = threadIdx.x & 31;
     const long long local = (long long)blockIdx.x * (blockDim.x >> 5) + warp;
@@ -818,7 +826,7 @@ __global__ void __launch_bounds__(256, 4) screen_kernel(RunArgs A, RefineList *l
     const SpeciesDev &sp = A.view.species[ch.species];
     RefineList &list = lists[local];
     const JfgpuChainState &g = A.state[c];
-    if (g.status != JFGPU_STATUS_OK || (round > 0 && g.stopped)) {
+    if (g.status != JFGPU_STATUS_OK || (!first_round && g.stopped)) {
         if (lane == 0) {
             list.count = 0;
             list.flags = kListSkip;
@@ -836,6 +844,22 @@ __global__ void __launch_bounds__(256, 4) screen_kernel(RunArgs A, RefineList *l
         return;
     }
     const int active = g.active, d = g.direction, occ_cell = g.occ_cell, n_surplus = g.n_surplus;
+    // the role words of the chain's units, copied asynchronously into shared memory while the nearby candidates are
+    // screened (16-byte chunks; the far pass reads them from there)
+    extern __shared__ __align__(16) int32_t role_stage[];  // [warps][kStagedRoles] when the far field stages
+    int32_t *my_roles = role_stage + warp * kStagedRoles;
+    const bool staged = stages_roles<FAR>() && far_of<FAR>(ch) == JFGPU_FAR_CELL_BOUNDING && ch.n <= kStagedRoles &&
+                        ((uintptr_t)(A.roles + ch.pos_off) & 15) == 0;
+    if (staged) {
+        const int32_t *src = A.roles + ch.pos_off;
+        const int chunks = ch.n >> 2;
+        for (int k = lane; k < chunks; k += 32) {
+            const unsigned dst = (unsigned)__cvta_generic_to_shared(my_roles + 4 * k);
+            asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(dst), "l"(src + 4 * k) : "memory");
+        }
+        asm volatile("cp.async.commit_group;\n" ::: "memory");
+        for (int k = 4 * chunks + lane; k < ch.n; k += 32) my_roles[k] = src[k];
+    }
     const uint64_t ev = (uint64_t)g.events;
     const float speed32 = ch.speed32;
     const float inv_beta32 = ch.inv_beta32;
@@ -981,7 +1005,11 @@ __global__ void __launch_bounds__(256, 4) screen_kernel(RunArgs A, RefineList *l
         const float threshold0 = isinf(base) ? kInf32 : base * rel + abs_margin;
         const float reject = threshold0 * speed32 * (1.0f + 1.0f / 65536.0f) / inv_beta32;
         const float *rates = sp.bound_upper32;
-        for_each_unit(A, ch, occ_cell, lane, [&](int j) {},
+        if (staged) {
+            asm volatile("cp.async.wait_all;\n" ::: "memory");
+            __syncwarp();
+        }
+        for_each_unit(staged ? my_roles : A.roles + ch.pos_off, A, ch, occ_cell, lane, [&](int j) {},
                       [&](int j, int rc) {
                           const float rate = rates[rc * 3 + d];
                           if (!(rate > 0.0f)) return;
@@ -1065,7 +1093,7 @@ __device__ inline void load_lifting(const JfgpuChainState &g, const RunArgs &A, 
 // candidates that take the same branch of the case analysis (up to the rare FP32/FP64 disagreement).
 template <int POT, int FAR>
 __global__ void __launch_bounds__(64) refine_kernel(RunArgs A, const RefineList *lists, Refined *refined,
-                                                     RefineQueue queue, long long round) {
+                                                     RefineQueue queue, long long round, int first_round) {
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     long long start = 0;
     int path = -1;
@@ -1146,7 +1174,7 @@ __device__ __noinline__ int exact_serial(const RunArgs &A, const ChainDev &ch, c
 
 template <int POT, int FAR>
 __global__ void __launch_bounds__(32) resolve_kernel(RunArgs A, const RefineList *lists, const Refined *refined,
-                                                     RefineQueue queue, long long round) {
+                                                     RefineQueue queue, long long round, int first_round) {
     const long long local = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (local < kPaths) queue.counts[local] = 0;  // the refine kernel of this round has consumed the queue
     if (local >= A.count) return;
@@ -1154,7 +1182,7 @@ __global__ void __launch_bounds__(32) resolve_kernel(RunArgs A, const RefineList
     const ChainDev &ch = A.view.chains[c];
     const SpeciesDev &sp = A.view.species[ch.species];
     JfgpuChainState &g = A.state[c];
-    if (g.status != JFGPU_STATUS_OK || (round > 0 && g.stopped)) return;
+    if (g.status != JFGPU_STATUS_OK || (!first_round && g.stopped)) return;
     const RefineList &list = lists[local];
     if (list.flags & kListSkip) return;
     WarpState w;
@@ -1446,14 +1474,17 @@ struct GroupLaunch {
     cudaStream_t stream;
 };
 
-// The event rounds of the mixed mode: per round the screening, the FP64 re-solves and the resolve kernel of every
-// group, issued round by round so that the groups' streams advance together.
+// Rounds [r0, r0 + n) of the mixed mode: per round the screening, the FP64 re-solves and the resolve kernel of every
+// group, issued round by round so that the groups' streams advance together; `clock` (may be null) brackets the
+// rounds it samples.  The round index reaches the kernels for the event log only; `first_round` marks round 0 of a
+// run call, where chains stopped by an earlier call start again.
 template <int POT, int FAR>
-static long long launch_mixed_rounds(const GroupLaunch *groups, int n_groups, long long rounds, int warps,
-                                     KernelClock *clock) {
+static long long issue_rounds(const GroupLaunch *groups, int n_groups, long long r0, long long n, int warps,
+                              KernelClock *clock) {
     long long launches = 0;
-    for (long long r = 0; r < rounds; ++r) {
+    for (long long r = r0; r < r0 + n; ++r) {
         KernelClock *timed = (clock && r % clock->stride == 0) ? clock : nullptr;
+        const int first_round = r == 0 ? 1 : 0;
         for (int g = 0; g < n_groups; ++g) {
             const GroupLaunch &G = groups[g];
             if (timed) timed->begin(G.stream);
@@ -1462,17 +1493,133 @@ static long long launch_mixed_rounds(const GroupLaunch *groups, int n_groups, lo
             // every queued entry plus the padding of each path to whole warps
             const long long refine_blocks = (count * kRefineSlots + kPaths * 31 + kSoloFlagged * 31 + 63) / 64;
             const long long resolve_blocks = (count + 31) / 32;  // one warp per block: resolve spreads over the SMs
-            screen_kernel<POT, FAR><<<(unsigned)screen_blocks, warps * 32, 0, G.stream>>>(G.args, G.lists, G.queue,
-                                                                                         r);
+            const size_t stage = stages_roles<FAR>() ? (size_t)warps * kStagedRoles * sizeof(int32_t) : 0;
+            screen_kernel<POT, FAR><<<(unsigned)screen_blocks, warps * 32, stage, G.stream>>>(G.args, G.lists,
+                                                                                             G.queue, r, first_round);
             if (timed) timed->end(G.stream, JFGPU_KERNEL_SCREEN);
             refine_kernel<POT, FAR><<<(unsigned)refine_blocks, 64, 0, G.stream>>>(G.args, G.lists, G.refined, G.queue,
-                                                                                 r);
+                                                                                 r, first_round);
             if (timed) timed->end(G.stream, JFGPU_KERNEL_REFINE);
             resolve_kernel<POT, FAR><<<(unsigned)resolve_blocks, 32, 0, G.stream>>>(G.args, G.lists, G.refined,
-                                                                                   G.queue, r);
+                                                                                   G.queue, r, first_round);
             if (timed) timed->end(G.stream, JFGPU_KERNEL_RESOLVE);
             launches += 3;
         }
+    }
+    return launches;
+}
+
+// Captured round segments, replayed with one graph launch: the per-launch costs of the three kernels per round and
+// group shrink to those of a graph node.  A segment is keyed by everything its launches bake in.
+struct SegmentKey {
+    RunArgs args;
+    void *lists, *refined, *queue;
+    long long rounds;
+    int first, warps, groups, pot, far;
+    bool operator<(const SegmentKey &o) const { return memcmp(this, &o, sizeof(SegmentKey)) < 0; }
+};
+
+class GraphCache {
+  public:
+    ~GraphCache() {
+        for (auto &entry : graphs_) cudaGraphExecDestroy(entry.second);
+        if (stream) cudaStreamDestroy(stream);
+        if (fork) cudaEventDestroy(fork);
+        if (join) cudaEventDestroy(join);
+    }
+    // the stream the segments are captured on and replayed on, and the events that order it after and before the
+    // caller's stream (created on first use, on the current device)
+    bool ready() {
+        if (stream) return true;
+        if (cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking) != cudaSuccess ||
+            cudaEventCreateWithFlags(&fork, cudaEventDisableTiming) != cudaSuccess ||
+            cudaEventCreateWithFlags(&join, cudaEventDisableTiming) != cudaSuccess) {
+            cudaGetLastError();
+            return false;
+        }
+        return true;
+    }
+    cudaGraphExec_t find(const SegmentKey &key) {
+        auto it = graphs_.find(key);
+        return it == graphs_.end() ? nullptr : it->second;
+    }
+    void insert(const SegmentKey &key, cudaGraphExec_t exec) {
+        if (graphs_.size() >= kMaxGraphs) {  // a batch reuses few shapes; a full cache starts afresh
+            for (auto &entry : graphs_) cudaGraphExecDestroy(entry.second);
+            graphs_.clear();
+        }
+        graphs_[key] = exec;
+    }
+    cudaStream_t stream = nullptr;
+    cudaEvent_t fork = nullptr, join = nullptr;
+
+  private:
+    static constexpr size_t kMaxGraphs = 32;
+    std::map<SegmentKey, cudaGraphExec_t> graphs_;
+};
+
+void *graph_cache_create() { return new GraphCache(); }
+void graph_cache_destroy(void *cache) { delete static_cast<GraphCache *>(cache); }
+
+// rounds [r0, r0 + n) of one chain group as one graph on the cache's stream, ordered after the caller's stream and
+// before its next work: captured the first time this segment is met, replayed afterwards
+template <int POT, int FAR>
+static long long replay_rounds(const GroupLaunch &group, long long r0, long long n, int warps, const LaunchPlan &plan,
+                               GraphCache *cache, SegmentKey key) {
+    key.rounds = n;
+    key.first = r0 == 0 ? 1 : 0;
+    GroupLaunch G = group;
+    G.stream = cache->stream;
+    cudaGraphExec_t exec = cache->find(key);
+    if (!exec) {
+        if (cudaStreamBeginCapture(cache->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+            cudaGetLastError();
+            return issue_rounds<POT, FAR>(&group, 1, r0, n, warps, nullptr);
+        }
+        issue_rounds<POT, FAR>(&G, 1, r0, n, warps, nullptr);
+        cudaGraph_t graph = nullptr;
+        if (cudaStreamEndCapture(cache->stream, &graph) != cudaSuccess || !graph) {
+            cudaGetLastError();
+            return issue_rounds<POT, FAR>(&group, 1, r0, n, warps, nullptr);
+        }
+        const cudaError_t made = cudaGraphInstantiate(&exec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (made != cudaSuccess) {
+            cudaGetLastError();
+            return issue_rounds<POT, FAR>(&group, 1, r0, n, warps, nullptr);
+        }
+        cache->insert(key, exec);
+    }
+    cudaEventRecord(cache->fork, group.stream);
+    cudaStreamWaitEvent(cache->stream, cache->fork, 0);
+    cudaGraphLaunch(exec, cache->stream);
+    cudaEventRecord(cache->join, cache->stream);
+    cudaStreamWaitEvent(group.stream, cache->join, 0);
+    return 3 * n;
+}
+
+// All rounds of a run call.  One chain group without an event log: graph segments (with timing on, every sampled
+// round is launched plainly between graphs of the rounds in between); otherwise, or when the caller's stream is
+// itself being captured, plain launches.
+template <int POT, int FAR>
+static long long launch_mixed_rounds(const GroupLaunch *groups, int n_groups, long long rounds, int warps,
+                                     const LaunchPlan &plan, bool graphs, const SegmentKey &key) {
+    GraphCache *cache = static_cast<GraphCache *>(plan.graphs);
+    cudaStreamCaptureStatus capturing = cudaStreamCaptureStatusNone;
+    if (graphs && (cudaStreamIsCapturing(groups[0].stream, &capturing) != cudaSuccess ||
+                   capturing != cudaStreamCaptureStatusNone)) {
+        cudaGetLastError();
+        graphs = false;
+    }
+    if (!graphs || !cache || n_groups != 1 || !cache->ready())
+        return issue_rounds<POT, FAR>(groups, n_groups, 0, rounds, warps, plan.clock);
+    if (!plan.clock) return replay_rounds<POT, FAR>(groups[0], 0, rounds, warps, plan, cache, key);
+    long long launches = 0;
+    const long long stride = plan.clock->stride;
+    for (long long r = 0; r < rounds; r += stride) {
+        launches += issue_rounds<POT, FAR>(groups, 1, r, 1, warps, plan.clock);  // the sampled round
+        const long long n = (r + stride < rounds ? r + stride : rounds) - (r + 1);
+        if (n > 0) launches += replay_rounds<POT, FAR>(groups[0], r + 1, n, warps, plan, cache, key);
     }
     return launches;
 }
@@ -1482,6 +1629,7 @@ cudaError_t launch_run(const EngineView &view, const JfgpuBuffers &b, long long 
                        long long log_capacity, int uniform_potential, int uniform_far, void *lists, void *refined,
                        void *queue, long long n_chains, const LaunchPlan &plan, long long *launches) {
     RunArgs A;
+    memset(&A, 0, sizeof(A));  // padding included: the arguments key the graph cache bytewise
     A.view = view;
     A.positions = b.positions;
     A.positions32 = reinterpret_cast<float4 *>(b.positions32);
@@ -1533,19 +1681,30 @@ cudaError_t launch_run(const EngineView &view, const JfgpuBuffers &b, long long 
             cudaEventRecord(plan.fork, plan.stream);
             for (int g = 0; g < used; ++g) cudaStreamWaitEvent(groups[g].stream, plan.fork, 0);
         }
+        SegmentKey key;
+        memset(&key, 0, sizeof(key));
+        key.args = A;
+        key.lists = lists;
+        key.refined = refined;
+        key.queue = queue;
+        key.warps = warps;
+        key.groups = used;
+        key.pot = uniform_potential;
+        key.far = uniform_far;
+        const bool graphs = plan.graphs != nullptr && log == nullptr;
         // kernels specialised for the common homogeneous batches carry only their potential's code
         long long issued;
         if (uniform_potential == JFGPU_POT_LENNARD_JONES && uniform_far == JFGPU_FAR_CELL_BOUNDING)
             issued = launch_mixed_rounds<JFGPU_POT_LENNARD_JONES, JFGPU_FAR_CELL_BOUNDING>(groups, used, max_events,
-                                                                                          warps, plan.clock);
+                                                                                          warps, plan, graphs, key);
         else if (uniform_potential == JFGPU_POT_LENNARD_JONES && uniform_far == JFGPU_FAR_CELL_VETO)
             issued = launch_mixed_rounds<JFGPU_POT_LENNARD_JONES, JFGPU_FAR_CELL_VETO>(groups, used, max_events, warps,
-                                                                                      plan.clock);
+                                                                                      plan, graphs, key);
         else if (uniform_potential == JFGPU_POT_HARD_SPHERE && uniform_far == JFGPU_FAR_NONE)
             issued = launch_mixed_rounds<JFGPU_POT_HARD_SPHERE, JFGPU_FAR_NONE>(groups, used, max_events, warps,
-                                                                               plan.clock);
+                                                                               plan, graphs, key);
         else
-            issued = launch_mixed_rounds<-1, -1>(groups, used, max_events, warps, plan.clock);
+            issued = launch_mixed_rounds<-1, -1>(groups, used, max_events, warps, plan, graphs, key);
         if (used > 1) {
             for (int g = 0; g < used; ++g) {
                 cudaEventRecord(plan.join[g], groups[g].stream);

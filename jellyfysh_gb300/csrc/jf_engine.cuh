@@ -84,6 +84,7 @@ struct LaunchPlan {
     cudaEvent_t fork = nullptr;             // recorded on the caller's stream, waited for by every group
     cudaEvent_t *join = nullptr;            // [groups] recorded by every group, waited for by the caller's stream
     KernelClock *clock = nullptr;           // null when timing is off
+    void *graphs = nullptr;                 // cache of captured round segments (null: plain launches)
 };
 
 }  // namespace jf

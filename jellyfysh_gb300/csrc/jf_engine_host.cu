@@ -29,6 +29,8 @@ cudaError_t launch_run(const EngineView &view, const JfgpuBuffers &b, long long 
 size_t refine_list_bytes();
 size_t refined_bytes();
 size_t refine_queue_bytes(long long n_chains);
+void *graph_cache_create();
+void graph_cache_destroy(void *cache);
 cudaError_t launch_observe(const EngineView &view, long long first, long long count, int max_n,
                            const float4 *positions32, int bins, double r_max, double *energy,
                            unsigned long long *histogram, const LaunchPlan &plan);
@@ -124,6 +126,7 @@ struct JfgpuEngine {
     cudaStream_t group_streams[8] = {};
     cudaEvent_t fork = nullptr, join[8] = {};
     EventClock *clock = nullptr;   // per-kernel timing, null while off
+    void *graphs = nullptr;        // captured round segments of the mixed mode (null: plain launches)
 };
 
 namespace {
@@ -509,6 +512,7 @@ void jfgpu_engine_destroy(JfgpuEngine *engine) {
     }
     if (engine->fork) cudaEventDestroy(engine->fork);
     delete engine->clock;
+    graph_cache_destroy(engine->graphs);
     for (void *p : engine->allocations) cudaFree(p);
     delete engine;
 }
@@ -642,6 +646,7 @@ int jfgpu_engine_create(const JfgpuChainDesc *chains, int64_t n_chains, void *st
         jfgpu_engine_destroy(e);
         return error;
     }
+    e->graphs = graph_cache_create();
     *out = e;
     return JFGPU_OK;
 }
@@ -698,6 +703,16 @@ int jfgpu_chains_set_groups(JfgpuEngine *e, int32_t groups) {
     if (groups > 1 && !e->fork && cudaEventCreateWithFlags(&e->fork, cudaEventDisableTiming) != cudaSuccess)
         return JFGPU_ERROR_CUDA;
     e->groups = groups;
+    return JFGPU_OK;
+}
+
+int jfgpu_chains_set_graphs(JfgpuEngine *e, int32_t enable) {
+    if (!e) return JFGPU_ERROR_ARGUMENT;
+    if (enable && !e->graphs) e->graphs = graph_cache_create();
+    if (!enable && e->graphs) {
+        graph_cache_destroy(e->graphs);
+        e->graphs = nullptr;
+    }
     return JFGPU_OK;
 }
 
@@ -760,6 +775,7 @@ static LaunchPlan make_plan(const JfgpuEngine *e, void *stream_ptr) {
     plan.fork = e->fork;
     plan.join = const_cast<cudaEvent_t *>(e->join);
     plan.clock = e->clock;
+    plan.graphs = e->graphs;
     return plan;
 }
 

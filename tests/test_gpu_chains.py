@@ -108,7 +108,8 @@ def test_batched_mixed_equals_fp64_lennard_jones():
 
 
 def test_chain_groups_and_kernel_timing_leave_results_unchanged():
-    """Chain groups on streams of their own, and CUDA events around every launch, change no bit of the run."""
+    """Chain groups on streams of their own, CUDA events around every launch, and plain launches instead of CUDA
+    graphs change no bit of the run."""
     from jellyfysh_gb300 import ChainBatch, ChainSpec, systems
     n, chains, events = 64, 256, 300
     length = systems.lennard_jones_box(n, 0.8)
@@ -118,22 +119,30 @@ def test_chain_groups_and_kernel_timing_leave_results_unchanged():
                        initial_direction=int(rng.integers(3))) for _ in range(chains)]
     positions = [systems.simple_cubic_jitter(n, length, 0.05, rng) for _ in range(chains)]
     results = {}
-    for label, mode, groups, timing in (("exact", "exact", 1, False), ("mixed", "mixed", 1, False),
-                                        ("grouped", "mixed", 4, True)):
+    for label, mode, groups, timing, graphs in (("exact", "exact", 1, False, True), ("mixed", "mixed", 1, False, True),
+                                                ("grouped", "mixed", 4, True, True),
+                                                ("plain", "mixed", 1, False, False),
+                                                ("sampled", "mixed", 1, 7, True)):
         batch = ChainBatch(specs, positions, seed=11)
         batch.set_groups(groups)
-        batch.set_timing(timing)
-        batch.run(events, mode=mode)
+        batch.set_graphs(graphs)
+        batch.set_timing(bool(timing), stride=int(timing) or 1)
+        for part in (events // 3, events // 3, events - 2 * (events // 3)):  # replays of captured segments
+            batch.run(part, mode=mode)
         batch.check_status()
         results[label] = (batch.positions(), batch.state())
-        if timing:
+        if label == "grouped":
             times = batch.kernel_times()
             for kind in ("screen", "refine", "resolve"):
                 assert times[kind]["launches"] == 4 * events, (kind, times[kind])
                 assert times[kind]["ms"] > 0.0
             assert times["chains"]["launches"] == 0
+        if label == "sampled":  # rounds 0, 7, 14, ... of each call are timed, the others replayed from graphs
+            times = batch.kernel_times()
+            sampled = sum((part + 6) // 7 for part in (events // 3, events // 3, events - 2 * (events // 3)))
+            assert times["screen"]["launches"] == sampled
         batch.close()
-    for label in ("mixed", "grouped"):
+    for label in ("mixed", "grouped", "plain", "sampled"):
         for a, b in zip(results["exact"][0], results[label][0]):
             assert np.array_equal(a, b), label
         for field in ("time_q", "time_r", "events", "active", "direction", "n_surplus", "occ_cell"):
