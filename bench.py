@@ -37,9 +37,9 @@ NEAR_CELLS = (2 * WORKLOAD["neighbor_layers"] + 1) ** 3  # cells scanned for pai
 CPU_SECONDS = 10.0  # wall time of the CPU baseline sample
 TIMING_STRIDE = 16  # event rounds between two rounds bracketed by per-kernel CUDA events
 # DRAM traffic of the screening kernel per event: ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch of
-# this workload (56.50 MB + 0.40 MB) divided by the 4096 events of that launch
+# this workload (56.53 MB + 0.74 MB) divided by the 4096 events of that launch
 # (profiles/round_kernels_lennard_jones_4096x1024.md)
-NCU_TRAFFIC_PER_EVENT = (56.499712e6 + 0.400128e6) / 4096
+NCU_TRAFFIC_PER_EVENT = (56.533504e6 + 0.742656e6) / 4096
 
 
 def parse():
