@@ -97,3 +97,21 @@ def min_image_min_distance(positions: np.ndarray, system_length: float, limit: O
         s -= system_length * np.round(s / system_length)
         best = min(best, float(np.sqrt(np.min(np.einsum("ij,ij->i", s, s)))))
     return best
+
+
+def batched_hard_sphere_state(n: int, packing_fraction: float, radius: float, rng: np.random.Generator,
+                              rsa_limit: float = 0.35, fcc_jitter_fraction: float = 0.02):
+    """A start of the batched hard-sphere workload: random sequential addition below ``rsa_limit``, a face-centred
+    cubic lattice with a uniform jitter of ``fcc_jitter_fraction`` of the nearest-neighbour spacing above it.
+    Returns (positions, system length)."""
+    length = hard_sphere_box(n, packing_fraction, radius)
+    if packing_fraction < rsa_limit:
+        return random_sequential_addition(n, radius, length, rng), length
+    # a partly filled lattice of k^3 cells is compressed into the box: it must still keep the spheres apart
+    k = max(1, int(math.ceil(round((n / 4.0) ** (1.0 / 3.0), 9))))
+    spacing = length / k / math.sqrt(2.0)
+    if spacing * (1.0 - 2.0 * fcc_jitter_fraction) < 2.0 * radius:
+        raise ValueError("n = %d spheres at packing fraction %.3f overlap on a partly filled fcc lattice of %d^3 "
+                         "cells; take n = 4 k^3" % (n, packing_fraction, k))
+    return fcc_jitter(n, length, fcc_jitter_fraction, rng), length
+

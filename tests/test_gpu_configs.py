@@ -1,0 +1,97 @@
+"""The batched configurations of the path on the GPU against the oracle, event by event.
+
+* Batched hard spheres: per chain the packing fraction drawn from [0.10, 0.45] and N from {32 .. 640}, started by
+  random sequential addition below 0.35 and from a jittered face-centred cubic lattice (±2 % of the spacing)
+  above (N = 4 k^3 there, whole lattice cells), chain length 0.3 L, cells of at least one diameter: every event of the FP64 path equals the oracle's bit
+  for bit, and the mixed path equals the FP64 path.
+* Batched Coulomb replicas: 32 point charges (16 of each sign) with a hard core of radius 0.05 in the unit cube,
+  beta = 1, merged-image Coulomb (alpha = 3.45, real-space images to |n| <= 2, k-vectors to |k| <= 6) bounded by
+  the inverse-power bound, cell veto on 8^3 cells: discrete outcomes equal the oracle's, event times to 1e-12
+  relative, positions to 1e-12 of the box.
+"""
+import numpy as np
+import pytest
+
+import oracle
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+DISCRETE = ("kind", "moved", "target", "new_active", "new_direction", "accepted")
+
+
+def test_batched_hard_spheres_against_the_oracle():
+    from jellyfysh_gb300 import ChainBatch, ChainSpec, chain_key, systems
+    rng = np.random.default_rng(33)
+    specs, positions = [], []
+    for c in range(24):
+        eta = float(rng.uniform(0.10, 0.45))
+        # lattice starts fill whole fcc cells (n = 4 k^3): a partly filled lattice compressed into the box overlaps
+        n = int(rng.integers(32, 641)) if eta < 0.35 else 4 * int(rng.integers(2, 6)) ** 3
+        state, length = systems.batched_hard_sphere_state(n, eta, 0.5, rng)
+        m = max(3, min(int(length / 1.0), 24))
+        specs.append(ChainSpec(n=n, system_length=length, cells_per_side=m, neighbor_layers=1, max_occupants=1,
+                               hs_radius=0.5, chain_time=0.3 * length, initial_active=int(rng.integers(n)),
+                               initial_direction=int(rng.integers(3))))
+        positions.append(state)
+    events = 300
+    batch = ChainBatch(specs, positions, seed=8)
+    logs = batch.run(events, mode="exact", log_capacity=events)
+    batch.check_status()
+    mixed = ChainBatch(specs, positions, seed=8)
+    mixed_logs = mixed.run(events, mode="mixed", log_capacity=events)
+    mixed.check_status()
+    for c, spec in enumerate(specs):
+        system = oracle.make_system(n=spec.n, system_length=spec.system_length, cells_per_side=spec.cells_per_side,
+                                    neighbor_layers=1, max_occupants=1, chain_time=spec.chain_time,
+                                    initial_active=spec.initial_active, initial_direction=spec.initial_direction,
+                                    potential=oracle.POT_HARD_SPHERE, hs_radius=0.5, rng_key=chain_key(8, c))
+        chain = oracle.Chain(system, positions[c])
+        expected = chain.run(events)
+        for field in expected.dtype.names:
+            assert np.array_equal(logs[c][field], expected[field]), (c, field)
+            assert np.array_equal(mixed_logs[c][field], expected[field]), (c, field)
+        assert np.array_equal(batch.positions(c), chain.positions())
+        assert np.array_equal(mixed.positions(c), chain.positions())
+    batch.close()
+    mixed.close()
+
+
+def test_batched_coulomb_replicas_against_the_oracle():
+    from jellyfysh_gb300 import ChainBatch, ChainSpec, chain_key, systems
+    rng = np.random.default_rng(44)
+    n, replicas, events = 32, 6, 400
+    charges = systems.alternating_charges(n)
+    specs, positions = [], []
+    for c in range(replicas):
+        specs.append(ChainSpec(n=n, system_length=1.0, cells_per_side=8, neighbor_layers=1, potential="coulomb",
+                               far="cell_veto", hs_radius=0.05, beta=1.0, chain_time=0.7, coulomb_prefactor=1.0,
+                               bound_prefactor=1.5837, ewald_alpha=3.45, fourier_cutoff=6, position_cutoff=2,
+                               estimator_points=4, estimator_prefactor=1.0, initial_active=int(rng.integers(n)),
+                               initial_direction=int(rng.integers(3))))
+        positions.append(systems.random_sequential_addition(n, 0.05, 1.0, rng))
+    batch = ChainBatch(specs, positions, [charges] * replicas, seed=9)
+    logs = batch.run(events, mode="exact", log_capacity=events)
+    batch.check_status()
+    mixed = ChainBatch(specs, positions, [charges] * replicas, seed=9)
+    mixed_logs = mixed.run(events, mode="mixed", log_capacity=events)
+    mixed.check_status()
+    for c, spec in enumerate(specs):
+        system = oracle.make_system(n=n, system_length=1.0, cells_per_side=8, neighbor_layers=1, max_occupants=1,
+                                    beta=1.0, chain_time=0.7, initial_active=spec.initial_active,
+                                    initial_direction=spec.initial_direction, potential=oracle.POT_COULOMB,
+                                    hs_radius=0.05, coulomb_prefactor=1.0, bound_prefactor=1.5837, ewald_alpha=3.45,
+                                    fourier_cutoff=6, position_cutoff=2, far=oracle.FAR_CELL_VETO,
+                                    estimator_points=4, estimator_prefactor=1.0, rng_key=chain_key(9, c))
+        chain = oracle.Chain(system, positions[c], charges)
+        expected = chain.run(events)
+        for field in DISCRETE:
+            assert np.array_equal(logs[c][field], expected[field]), (c, field)
+        t_gpu = logs[c]["time_q"] + logs[c]["time_r"]
+        t_cpu = expected["time_q"] + expected["time_r"]
+        assert np.allclose(t_gpu, t_cpu, rtol=1e-12, atol=0.0), c
+        assert np.allclose(batch.positions(c), chain.positions(), rtol=0.0, atol=1e-12)
+        for field in logs.dtype.names:
+            assert np.array_equal(mixed_logs[c][field], logs[c][field]), (c, field)
+    batch.close()
+    mixed.close()
