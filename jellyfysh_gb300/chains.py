@@ -10,6 +10,7 @@ event loop runs on the device.  It replaces, for the event-time path, the refere
 """
 import ctypes
 import dataclasses
+import json
 import math
 from typing import List, Optional, Sequence
 
@@ -182,6 +183,43 @@ class ChainBatch:
     # ------------------------------------------------------------------------------------------------
     def set_block_warps(self, warps: int) -> None:
         _lib.check(self.lib.jfgpu_chains_set_block_warps(self._engine, int(warps)), "jfgpu_chains_set_block_warps")
+
+    # ------------------------------------------------------------------------------------------------
+    # checkpoint / resume (the reference dumps its whole mediator with dill, dumping_output_handler.py:70-90, and
+    # resumes from it, resume.py:63-105; the device state of a batch is its buffers)
+    def checkpoint(self, path: str) -> None:
+        """Write the batch (chain parameters with their random-number keys, and every device buffer) to `path`
+        (numpy .npz).  ``ChainBatch.restore(path)`` continues it exactly where it stopped."""
+        self._torch.cuda.synchronize(self.device)
+        specs = [dict(dataclasses.asdict(spec), rng_key=int(key)) for spec, key in zip(self.specs, self.keys)]
+        arrays = {name: getattr(self, name + "_dev").cpu().numpy()
+                  for name in ("positions", "positions32", "occupancy", "surplus", "roles", "state")}
+        if self.charges_dev is not None:
+            arrays["charges"] = self.charges_dev.cpu().numpy()
+        np.savez(path, specs=json.dumps(specs), **arrays)
+
+    @classmethod
+    def restore(cls, path: str, device: str = "cuda") -> "ChainBatch":
+        """The batch written by `checkpoint`: the engine's tables are rebuilt from the chain parameters (they are
+        deterministic) and every buffer is loaded back."""
+        data = np.load(path)
+        specs = [ChainSpec(**entry) for entry in json.loads(str(data["specs"]))]
+        batch = cls.__new__(cls)
+        positions = np.asarray(data["positions"])
+        charges = np.asarray(data["charges"]) if "charges" in data.files else None
+        # construct from the saved positions (any valid start), then replace every buffer by the saved one
+        offsets = np.concatenate([[0], np.cumsum([spec.n for spec in specs])])
+        per_chain = [positions[offsets[c]:offsets[c + 1]] for c in range(len(specs))]
+        per_charges = None if charges is None else [charges[offsets[c]:offsets[c + 1]] for c in range(len(specs))]
+        batch.__init__(specs, per_chain, per_charges, device=device)
+        for name in ("positions", "positions32", "occupancy", "surplus", "roles", "state"):
+            target = getattr(batch, name + "_dev")
+            source = batch._torch.from_numpy(np.ascontiguousarray(data[name])).to(batch.device)
+            if source.shape != target.shape or source.dtype != target.dtype:
+                raise ValueError("checkpoint buffer %s does not match the batch layout" % name)
+            target.copy_(source)
+        batch._torch.cuda.synchronize(batch.device)
+        return batch
 
     def set_graphs(self, enable: bool) -> None:
         """Replay the event rounds of the mixed mode from captured CUDA graphs (default) or launch them plainly."""

@@ -132,3 +132,44 @@ def test_mediator_translates_the_reference_configuration(name):
     if charges is not None:
         assert np.array_equal(np.array(plan["charges"]), charges)
     assert plan["end_of_run_time"] == 1e9
+
+
+def reference_separation_file(path):
+    """The reference's SeparationOutputHandler writing one sample of a fixed configuration (run in a child)."""
+    if TREE not in sys.path:
+        sys.path.insert(0, TREE)
+    import configparser as cp
+    from jellyfysh.base import factory
+    from jellyfysh.base.node import Node
+    from jellyfysh.base.particle import Particle
+    from jellyfysh.base.unit import Unit
+    config = cp.ConfigParser()
+    config.read_string("[Run]\nsetting = hypercubic_setting\n[HypercubicSetting]\nsystem_length = 4.308869380063767\n"
+                       "beta = 1.0\ndimension = 3\n[SeparationOutputHandler]\nfilename = %s\n" % path)
+    factory.build_from_config(config, "HypercubicSetting", "jellyfysh.setting")
+    from jellyfysh import setting
+    positions = np.random.default_rng(9).uniform(0.0, 4.308869380063767, size=(20, 3))
+    setting.set_number_of_root_nodes(20)
+    setting.set_number_of_nodes_per_root_node(1)
+    setting.set_number_of_node_levels(1)
+    handler = factory.build_from_config(config, "SeparationOutputHandler",
+                                        "jellyfysh.input_output_handler.output_handler")
+    nodes = [Node(Unit(identifier=(i,), position=[float(v) for v in positions[i]], charge=None))
+             for i in range(20)]
+    handler.write(nodes)
+    handler.post_run()
+    return positions.tolist()
+
+
+def test_separation_samples_equal_the_reference_output_handler(tmp_path):
+    from jellyfysh_gb300 import outputs
+    reference_path = str(tmp_path / "reference.dat")
+    positions = np.array(_in_child("reference_separation_file", reference_path))
+    ours_path = str(tmp_path / "ours.dat")
+    with outputs.SeparationWriter(ours_path) as writer:
+        writer.write(positions, 4.308869380063767)
+    reference = open(reference_path).read().splitlines()
+    ours = open(ours_path).read().splitlines()
+    assert reference[0].startswith("# Run identification hash") and ours[0].startswith("# Run identification hash")
+    assert reference[1:] == ours[1:]
+
