@@ -229,8 +229,7 @@ def autotune(batch, events, warps_choices=(2, 4, 8), group_choices=(1, 2, 4)):
 def gpu_arm(args):
     import torch
     import torch.distributed as dist
-    from jellyfysh_gb300 import ChainBatch
-    from jellyfysh_gb300.chains import STATE_DTYPE
+    from jellyfysh_gb300 import ChainBatch, replicas
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
@@ -278,13 +277,8 @@ def gpu_arm(args):
     candidates = int(state1["candidates"].sum() - state0["candidates"].sum())
     refined = int(state1["refined"].sum() - state0["refined"].sum())
     fallbacks = int(state1["refine_fallbacks"].sum() - state0["refine_fallbacks"].sum())
-    elapsed_t = torch.tensor([elapsed_ms], dtype=torch.float64, device=device)
-    events_t = torch.tensor([events_done], dtype=torch.float64, device=device)
-    if world > 1:
-        dist.all_reduce(elapsed_t, op=dist.ReduceOp.MAX)
-        dist.all_reduce(events_t, op=dist.ReduceOp.SUM)
-    total_ms = float(elapsed_t.item())
-    value = float(events_t.item()) / (total_ms / 1000.0)
+    # whole job: events of all ranks over the longest rank's timed region
+    _, total_ms, value = replicas.timed_throughput(events_done, elapsed_ms, device)
 
     # end to end through ChainBatch with host buffers: H2D of the chain state, the run, D2H of the results
     host = [t.cpu().pin_memory() for t in batch.state_tensors()]
