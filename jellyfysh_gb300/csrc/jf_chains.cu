@@ -681,25 +681,6 @@ __device__ inline void for_each_unit(const int32_t *roles, const RunArgs &A, con
     }
 }
 
-// sparse warp argmin: only lanes holding a candidate take part (usually lane 0 and one or two others)
-__device__ inline Cand warp_argmin_sparse(const Cand &c) {
-    unsigned mask = __ballot_sync(kFull, c.kind != (1 << 30));
-    Cand acc = cand_none();
-    while (mask) {
-        int src = __ffs(mask) - 1;
-        mask &= mask - 1;
-        Cand o;
-        o.q = __shfl_sync(kFull, c.q, src);
-        o.r = __shfl_sync(kFull, c.r, src);
-        o.kind = __shfl_sync(kFull, c.kind, src);
-        o.target = __shfl_sync(kFull, c.target, src);
-        o.aux = __shfl_sync(kFull, c.aux, src);
-        o.rate = __shfl_sync(kFull, c.rate, src);
-        if (cand_better(o, acc)) acc = o;
-    }
-    return acc;
-}
-
 // the whole event in FP64 (all lanes); returns the winner in best
 template <int POT, int FAR>
 __device__ inline int exact_candidates(const RunArgs &A, const ChainDev &ch, const SpeciesDev &sp, const WarpState &w,
@@ -794,16 +775,7 @@ struct RefineList {
 
 // FP64 re-solves of the first kRefineSlots entries of every refine list, one thread per entry; the resolve kernel
 // takes the earliest of them (and solves any further entry itself)
-#ifndef JF_REFINE_SLOTS
-#define JF_REFINE_SLOTS 4
-#endif
-#ifndef JF_SOLO_FLAGGED
-#define JF_SOLO_FLAGGED 256
-#endif
-constexpr int kRefineSlots = JF_REFINE_SLOTS;
-// flagged entries (their branch of the case analysis unknown) are re-solved one per warp, up to this many a round:
-// a warp of mixed branches would run the union of the branches and hold up the round
-constexpr int kSoloFlagged = JF_SOLO_FLAGGED;
+constexpr int kRefineSlots = 4;
 
 // Refine queue of a chain group: per screening path, the entries (local chain * kRefineSlots + slot) to re-solve.
 // counts[kPaths] sit in the group's header; entries[path][...] use the slice [lo, hi) * kRefineSlots of the group's
@@ -1101,18 +1073,10 @@ __global__ void __launch_bounds__(64) refine_kernel(RunArgs A, const RefineList 
 #pragma unroll
     for (int k = 0; k < kPaths; ++k) {
         const long long n = queue.counts[k];
-        // flagged entries: the first kSoloFlagged one per warp (lane 0), the rest packed
-        const long long solo = k == kPathFlagged ? (n < kSoloFlagged ? n : kSoloFlagged) : 0;
-        const long long padded = solo * 32 + ((n - solo + 31) & ~31LL);
+        const long long padded = (n + 31) & ~31LL;
         if (path < 0 && t < start + padded) {
             path = k;
-            const long long offset = t - start;
-            if (offset < solo * 32) {
-                if (offset % 32) return;
-                index = offset / 32;
-            } else {
-                index = solo + (offset - solo * 32);
-            }
+            index = t - start;
             if (index >= n) return;
         }
         start += padded;
@@ -1491,7 +1455,7 @@ static long long issue_rounds(const GroupLaunch *groups, int n_groups, long long
             const long long count = G.args.count;
             const long long screen_blocks = (count + warps - 1) / warps;
             // every queued entry plus the padding of each path to whole warps
-            const long long refine_blocks = (count * kRefineSlots + kPaths * 31 + kSoloFlagged * 31 + 63) / 64;
+            const long long refine_blocks = (count * kRefineSlots + kPaths * 31 + 63) / 64;
             const long long resolve_blocks = (count + 31) / 32;  // one warp per block: resolve spreads over the SMs
             const size_t stage = stages_roles<FAR>() ? (size_t)warps * kStagedRoles * sizeof(int32_t) : 0;
             screen_kernel<POT, FAR><<<(unsigned)screen_blocks, warps * 32, stage, G.stream>>>(G.args, G.lists,

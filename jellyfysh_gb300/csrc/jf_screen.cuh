@@ -22,8 +22,7 @@ constexpr int kPathFrontInside = 3;    // in front, inside the shell
 constexpr int kPathBehindInside = 4;   // behind, inside the shell
 constexpr int kPathHardSphere = 5;
 constexpr int kPathFar = 6;            // far-field (cell-bounding) candidate
-constexpr int kPathFlagged = 7;        // path unknown (kept for candidates of no classified branch)
-constexpr int kPaths = 8;
+constexpr int kPaths = 7;
 
 // potential change of a keyed draw in FP32 without FP64 instructions: the uniform is (bits >> 11) 2^-53; its top 32
 // bits k give u within 2^-32, so -log1p(-u) (u < 1/2) and -log(1 - u) with 1 - u from 2^32 - k (u >= 1/2) carry a
