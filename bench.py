@@ -280,8 +280,9 @@ def gpu_arm(args):
     # whole job: events of all ranks over the longest rank's timed region
     _, total_ms, value = replicas.timed_throughput(events_done, elapsed_ms, device)
 
-    # end to end through ChainBatch with host buffers: H2D of the chain state, the run, D2H of the results
-    host = [t.cpu().pin_memory() for t in batch.state_tensors()]
+    # end to end through ChainBatch with host buffers: H2D of the chain state (the FP32 mirror is rebuilt on the
+    # device from the uploaded positions), the run, D2H of the results
+    host = [t.cpu().pin_memory() for t in batch.input_tensors()]
     results = [batch.positions_dev, batch.state_dev]
     host_results = [t.cpu().pin_memory() for t in results]
     h2d = sum(t.numel() * t.element_size() for t in host)
@@ -293,8 +294,9 @@ def gpu_arm(args):
     e_end = torch.cuda.Event(enable_timing=True)
     e_begin.record(stream)
     for _ in range(e2e_steps):
-        for dst, src in zip(batch.state_tensors(), host):
+        for dst, src in zip(batch.input_tensors(), host):
             dst.copy_(src, non_blocking=True)
+        batch.refresh_mirror()
         batch.run(args.events, mode="mixed", sync=False)
         for dst, src in zip(host_results, results):
             dst.copy_(src, non_blocking=True)

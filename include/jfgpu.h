@@ -240,6 +240,12 @@ int jfgpu_chains_run(JfgpuEngine *engine, const JfgpuBuffers *buffers, int64_t f
 /* Autotuned launch shape of the mixed mode: warps per block used by jfgpu_chains_run (1..8). */
 int jfgpu_chains_set_block_warps(JfgpuEngine *engine, int32_t warps_per_block);
 
+/* Rewrite the FP32 mirror (buffers->positions32: x, y, z, charge) of chains [first_chain, first_chain + count) from
+ * their FP64 positions (and charges): for hosts that upload positions between runs, instead of uploading the
+ * mirror as well.  The mirror is otherwise kept by the engine (jfgpu_chains_init and every committed event). */
+int jfgpu_chains_refresh_mirror(JfgpuEngine *engine, const JfgpuBuffers *buffers, int64_t first_chain, int64_t count,
+                                void *stream);
+
 /* Observables of chains [first_chain, first_chain + count) at their current positions, for the estimators of
  * long runs (all pairs of a chain, minimum-image separations from the FP32 mirror):
  *   energy    [count] (device, may be NULL): potential energy of the chain's pair potential, the sum over pairs

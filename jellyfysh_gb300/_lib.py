@@ -111,6 +111,7 @@ SIGNATURES = {
     "jfgpu_chains_set_block_warps": (ctypes.c_int, [_P, _I32]),
     "jfgpu_chains_set_groups": (ctypes.c_int, [_P, _I32]),
     "jfgpu_chains_set_graphs": (ctypes.c_int, [_P, _I32]),
+    "jfgpu_chains_refresh_mirror": (ctypes.c_int, [_P, ctypes.POINTER(Buffers), _I64, _I64, _P]),
     "jfgpu_chains_observe": (ctypes.c_int, [_P, ctypes.POINTER(Buffers), _I64, _I64, _I32, _D, _P, _P, _P]),
     "jfgpu_engine_set_timing": (ctypes.c_int, [_P, _I32]),
     "jfgpu_engine_kernel_times": (ctypes.c_int, [_P, _P, _P, _I32]),

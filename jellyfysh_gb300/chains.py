@@ -221,6 +221,20 @@ class ChainBatch:
         batch._torch.cuda.synchronize(batch.device)
         return batch
 
+    def refresh_mirror(self, first: int = 0, count: Optional[int] = None) -> None:
+        """Rewrite the FP32 mirror of chains [first, first + count) from their FP64 positions (after the host
+        has written positions_dev)."""
+        count = self.n_chains - first if count is None else count
+        with self._torch.cuda.device(self.device):
+            _lib.check(self.lib.jfgpu_chains_refresh_mirror(self._engine, ctypes.byref(self._buffers), int(first),
+                                                            int(count), self._stream()),
+                       "jfgpu_chains_refresh_mirror")
+
+    def input_tensors(self):
+        """The device buffers a host uploads to set the batch's state: FP64 positions, occupancy, surplus lists,
+        role words and chain states (the FP32 mirror follows from the positions: ``refresh_mirror``)."""
+        return [self.positions_dev, self.occupancy_dev, self.surplus_dev, self.roles_dev, self.state_dev]
+
     def set_graphs(self, enable: bool) -> None:
         """Replay the event rounds of the mixed mode from captured CUDA graphs (default) or launch them plainly."""
         _lib.check(self.lib.jfgpu_chains_set_graphs(self._engine, 1 if enable else 0), "jfgpu_chains_set_graphs")

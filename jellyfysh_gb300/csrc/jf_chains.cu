@@ -1417,6 +1417,22 @@ size_t refine_queue_bytes(long long n_chains) {
 // ---------------------------------------------------------------------------------------------------------------
 namespace jf {
 
+// the FP32 mirror (x, y, z, charge) of the FP64 positions of units [first, first + count)
+__global__ void mirror_kernel(const double *positions, const double *charges, float4 *positions32, long long first,
+                              long long count) {
+    const long long i = first + (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= first + count) return;
+    const double *p = positions + 3 * i;
+    positions32[i] = make_float4((float)p[0], (float)p[1], (float)p[2], charges ? (float)charges[i] : 1.0f);
+}
+
+cudaError_t launch_mirror(const JfgpuBuffers &b, long long first_unit, long long units, cudaStream_t stream) {
+    if (units <= 0) return cudaSuccess;
+    mirror_kernel<<<(unsigned)((units + 255) / 256), 256, 0, stream>>>(
+        b.positions, b.charges, reinterpret_cast<float4 *>(b.positions32), first_unit, units);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_init(const EngineView &view, long long n_chains, const JfgpuBuffers &b, const LaunchPlan &plan) {
     const int warps = 4;
     long long blocks = (n_chains + warps - 1) / warps;

@@ -22,6 +22,7 @@
 
 namespace jf {
 cudaError_t launch_init(const EngineView &view, long long n_chains, const JfgpuBuffers &b, const LaunchPlan &plan);
+cudaError_t launch_mirror(const JfgpuBuffers &b, long long first_unit, long long units, cudaStream_t stream);
 cudaError_t launch_run(const EngineView &view, const JfgpuBuffers &b, long long first, long long count,
                        long long max_events, double stop_q, double stop_r, int mode, JfgpuEvent *log,
                        long long log_capacity, int uniform_potential, int uniform_far, void *lists, void *refined,
@@ -704,6 +705,19 @@ int jfgpu_chains_set_groups(JfgpuEngine *e, int32_t groups) {
         return JFGPU_ERROR_CUDA;
     e->groups = groups;
     return JFGPU_OK;
+}
+
+int jfgpu_chains_refresh_mirror(JfgpuEngine *e, const JfgpuBuffers *b, int64_t first, int64_t count,
+                                void *stream_ptr) {
+    if (!e || !b || !b->positions || !b->positions32 || first < 0 || count < 0 ||
+        first + count > (int64_t)e->chains.size())
+        return JFGPU_ERROR_ARGUMENT;
+    if (count == 0) return JFGPU_OK;
+    const long long first_unit = e->chains[first].pos_off;
+    const long long last_unit = e->chains[first + count - 1].pos_off + e->chains[first + count - 1].n;
+    cudaError_t err = launch_mirror(*b, first_unit, last_unit - first_unit, static_cast<cudaStream_t>(stream_ptr));
+    e->launches += 1;
+    return err == cudaSuccess ? JFGPU_OK : JFGPU_ERROR_CUDA;
 }
 
 int jfgpu_chains_set_graphs(JfgpuEngine *e, int32_t enable) {

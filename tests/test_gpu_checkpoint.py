@@ -39,3 +39,24 @@ def test_restored_batch_continues_bit_for_bit(tmp_path, mode):
         assert np.array_equal(original[field], again[field]), field
     batch.close()
     restored.close()
+
+
+def test_mirror_refresh_rebuilds_the_fp32_mirror_from_uploaded_positions():
+    from jellyfysh_gb300 import ChainBatch, ChainSpec, systems
+    rng = np.random.default_rng(2)
+    n = 64
+    length = systems.lennard_jones_box(n, 0.8)
+    specs = [ChainSpec(n=n, system_length=length, cells_per_side=4, potential="lennard_jones", far="cell_veto",
+                       beta=1.0 / 1.2, chain_time=2.0) for _ in range(3)]
+    batch = ChainBatch(specs, [systems.simple_cubic_jitter(n, length, 0.05, rng) for _ in range(3)], seed=4)
+    batch.run(100, mode="mixed")
+    mirror = batch.positions32_dev.clone()
+    batch.positions32_dev.zero_()
+    batch.refresh_mirror()
+    assert torch.equal(batch.positions32_dev, mirror)  # the engine's mirror is exactly float(positions)
+    expected = batch.positions_dev[n:2 * n].to(torch.float32)
+    batch.positions32_dev.zero_()
+    batch.refresh_mirror(first=1, count=1)
+    assert torch.equal(batch.positions32_dev[n:2 * n, :3], expected)
+    assert not batch.positions32_dev[:n].any() and not batch.positions32_dev[2 * n:].any()
+    batch.close()
