@@ -201,7 +201,7 @@ def reference_arm(args):
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic: seeded simple-cubic lattice + uniform jitter", "config": config,
             "cpu_baseline": {"value": value, "unit": "events/s", "cores": threads, "kind": "port",
-                             "sample": config["sample"]},
+                             "per_core": value / threads, "sample": config["sample"]},
             "e2e": {"value": value, "unit": "events/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
 
@@ -364,6 +364,7 @@ def gpu_arm(args):
             cpu_run(pool, chains, 0.5)
             done, elapsed = cpu_run(pool, chains, CPU_SECONDS)
         cpu = {"value": done / elapsed, "unit": "events/s", "cores": threads, "kind": "port",
+               "per_core": done / elapsed / threads,
                "sample": "%d chains of the workload (one per host thread), %d events in %.1f s"
                          % (threads, done, elapsed)}
     config = dict(WORKLOAD)
