@@ -52,6 +52,8 @@ extern "C" {
 #define JFGPU_STATUS_COMPLEX 4         /* negative ** fractional */
 #define JFGPU_STATUS_CELL_RANGE 7      /* position outside the cell list */
 #define JFGPU_STATUS_EVENT_CAP 8       /* the refinement set of a mixed-precision event overflowed twice */
+#define JFGPU_STATUS_LIFTING 9         /* LiftingSchemeError: the lifting table holds no active unit */
+#define JFGPU_STATUS_INDEX 10          /* IndexError: the lifting table holds no negative derivative */
 
 /* ---- potentials ---- */
 #define JFGPU_POT_HARD_SPHERE 0
@@ -133,6 +135,72 @@ int jfgpu_cell_bounding_displacement(const double *bounds_upper, const double *b
                                      const int32_t *cell_separation, const int32_t *direction, const double *speed,
                                      const double *charge_factor, const double *potential_change, int64_t n,
                                      double *out, int32_t *status, void *stream);
+
+/* ======================================================================================================
+ * Lifting schemes of composite objects: the new active unit after an event between more than two units.
+ * Replaces Lifting.reset / insert / get_active_identifier (jellyfysh/lifting/lifting.py:47-108) of
+ * InsideFirstLifting (lifting/inside_first_lifting.py:37-54), OutsideFirstLifting
+ * (lifting/outside_first_lifting.py:38-55) and RatioLifting (lifting/ratio_lifting.py:38-56), as the event
+ * handlers of composite objects fill and query them (event_handler/abstracts/
+ * event_handler_with_bounding_potential.py:170-220).
+ * ==================================================================================================== */
+#define JFGPU_LIFTING_INSIDE_FIRST 0
+#define JFGPU_LIFTING_OUTSIDE_FIRST 1
+#define JFGPU_LIFTING_RATIO 2
+#define JFGPU_DRAW_VALUE 0             /* draws[i] is the value random.uniform(0.0, b) returned */
+#define JFGPU_DRAW_UNIT 1              /* draws[i] is random(), the value is 0.0 + (b - 0.0) * draws[i] */
+/* n tables in one launch.  Table i is entries offsets[i] .. offsets[i+1]-1 of rates (the factor derivatives in
+ * insertion order) and active (1 for the active unit); offsets is a device array [n+1], non-decreasing.
+ * draws[i] decides table i: the draw of the active unit's insert for inside-first and outside-first, the draw of
+ * get_active_identifier for ratio.  selected[i] receives the index within table i of the new active unit (-1
+ * on an error), bound[i] the upper end b of that random.uniform(0.0, b) call (NaN when the reference raises
+ * before it), status[i] JFGPU_STATUS_OK, _ASSERTION (an active unit with a derivative <= 0, or a second
+ * active unit), _LIFTING (no active unit) or _INDEX (no negative derivative).  bound may be null; with n = 0
+ * every pointer may be null. */
+int jfgpu_lifting(int32_t scheme, int32_t draw_mode, const double *rates, const int32_t *active,
+                  const int64_t *offsets, int64_t n, const double *draws, int64_t *selected, double *bound,
+                  int32_t *status, void *stream);
+
+/* ======================================================================================================
+ * Composite objects: events between two composite objects (dipoles, water molecules) of `units` point charges
+ * each, merged-image Coulomb between the charges, bounded pair by pair by the inverse-power Coulomb bound and
+ * summed over the target object.  Replaces TwoCompositeObjectSummedBoundingPotentialEventHandler
+ * (event_handler/two_composite_object_summed_bounding_potential_event_handler.py:119-202) with its
+ * _fill_lifting (event_handler/abstracts/event_handler_with_bounding_potential.py:170-220) and lifting scheme.
+ * Position arrays are device arrays of 3 doubles per unit; unit arrays of an event are contiguous.
+ * ==================================================================================================== */
+typedef struct {
+    int32_t units;                /* leaf units per composite object, 1..8 */
+    int32_t lifting;              /* JFGPU_LIFTING_* */
+    int32_t fourier_cutoff;       /* MergedImageCoulombPotential */
+    int32_t position_cutoff;
+    double alpha;
+    double coulomb_prefactor;
+    double bound_prefactor;       /* InversePowerCoulombBoundingPotential */
+    double system_length;
+} JfgpuCompositeDesc;
+/* send_event_time (:119-150) of n events: displacement[i] = min over the target units j of the bounding
+ * displacement of the active unit (velocity [n][3], active_position [n][3], active_charge [n]) against target unit
+ * j (target_positions [n][units][3], target_charges [n][units]) with potential change potential_changes[i][j] (the
+ * reference's random.expovariate(beta) per target unit, in target order). */
+int jfgpu_composite_event_time(const JfgpuCompositeDesc *desc, const double *velocity, const double *active_position,
+                               const double *active_charge, const double *target_positions,
+                               const double *target_charges, const double *potential_changes, int64_t n,
+                               double *displacement, int32_t *status, void *stream);
+/* send_out_state (:152-202) of n events at the event time.  local_positions / target_positions [n][units][3] and
+ * charges [n][units], each object's units sorted by identifier; active_index [n] the active unit among the local
+ * ones; local_first [n] 1 when the local object's identifier is the smaller (the derivative table lists it
+ * first).  draws [n][3]: the thinning draw random.uniform(0.0, bounding rate), the draw of the active unit's
+ * insert into the lifting table, the ratio scheme's draw of get_active_identifier (unused by the other schemes);
+ * draw_mode JFGPU_DRAW_VALUE or JFGPU_DRAW_UNIT as for jfgpu_lifting.  new_active [n]: -1 when the event is
+ * thinned out, i for local unit i, units + j for target unit j.  rates [n][2] (may be null): the summed bounding
+ * event rate and the event rate max(0, factor derivative).  status [n]: JFGPU_STATUS_* (lifting statuses as for
+ * jfgpu_lifting; _ASSERTION for a velocity that is not along one positive axis). */
+int jfgpu_composite_out_state(const JfgpuCompositeDesc *desc, int32_t draw_mode, const double *velocity,
+                              const double *local_positions, const double *local_charges,
+                              const int32_t *active_index, const double *target_positions,
+                              const double *target_charges, const int32_t *local_first, const double *draws,
+                              int64_t n, int32_t *new_active, double *rates, int32_t *status, void *stream);
 
 /* ======================================================================================================
  * Chains: thousands of independent ECMC chains advanced by one kernel with the event loop on the device.

@@ -15,9 +15,11 @@ ERROR_NAMES = {0: "ok", 1: "CUDA runtime error", 2: "invalid argument", 3: "devi
                4: "table construction failed"}
 
 STATUS_OK, STATUS_VALUE_ERROR, STATUS_ASSERTION, STATUS_ZERO_DIVISION, STATUS_COMPLEX = 0, 1, 2, 3, 4
-STATUS_CELL_RANGE, STATUS_EVENT_CAP = 7, 8
+STATUS_CELL_RANGE, STATUS_EVENT_CAP, STATUS_LIFTING, STATUS_INDEX = 7, 8, 9, 10
 STATUS_NAMES = {0: "ok", 1: "ValueError", 2: "AssertionError", 3: "ZeroDivisionError", 4: "complex result",
-                7: "cell index out of range", 8: "refinement overflow"}
+                7: "cell index out of range", 8: "refinement overflow", 9: "LiftingSchemeError", 10: "IndexError"}
+LIFTING_INSIDE_FIRST, LIFTING_OUTSIDE_FIRST, LIFTING_RATIO = 0, 1, 2
+DRAW_VALUE, DRAW_UNIT = 0, 1
 
 POT_HARD_SPHERE, POT_LENNARD_JONES, POT_COULOMB = 0, 1, 2
 FAR_NONE, FAR_CELL_VETO, FAR_CELL_BOUNDING = 0, 1, 2
@@ -35,6 +37,13 @@ class NoGpu(RuntimeError):
 
 class JfgpuError(RuntimeError):
     pass
+
+
+class CompositeDesc(ctypes.Structure):
+    """JfgpuCompositeDesc."""
+    _fields_ = [("units", ctypes.c_int32), ("lifting", ctypes.c_int32), ("fourier_cutoff", ctypes.c_int32),
+                ("position_cutoff", ctypes.c_int32), ("alpha", ctypes.c_double), ("coulomb_prefactor", ctypes.c_double),
+                ("bound_prefactor", ctypes.c_double), ("system_length", ctypes.c_double)]
 
 
 class ChainDesc(ctypes.Structure):
@@ -100,6 +109,11 @@ SIGNATURES = {
     "jfgpu_merged_image_coulomb_derivative_noalloc": (ctypes.c_int, [_D, _I32, _I32, _D, _D, _P, _P, _P, _I64,
                                                                      _P, _P, _P]),
     "jfgpu_cell_bounding_displacement": (ctypes.c_int, [_P, _P, _P, _P, _P, _P, _P, _I64, _P, _P, _P]),
+    "jfgpu_lifting": (ctypes.c_int, [_I32, _I32, _P, _P, _P, _I64, _P, _P, _P, _P, _P]),
+    "jfgpu_composite_event_time": (ctypes.c_int, [ctypes.POINTER(CompositeDesc), _P, _P, _P, _P, _P, _P, _I64, _P,
+                                                  _P, _P]),
+    "jfgpu_composite_out_state": (ctypes.c_int, [ctypes.POINTER(CompositeDesc), _I32, _P, _P, _P, _P, _P, _P, _P,
+                                                 _P, _I64, _P, _P, _P, _P]),
     "jfgpu_engine_create": (ctypes.c_int, [_P, _I64, _P, ctypes.POINTER(ctypes.c_void_p)]),
     "jfgpu_engine_destroy": (None, [_P]),
     "jfgpu_engine_layout": (ctypes.c_int, [_P, ctypes.POINTER(Layout)]),

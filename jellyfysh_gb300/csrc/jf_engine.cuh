@@ -10,6 +10,8 @@
 // Engine tables (owned by the engine): per-chain ChainDev, per-geometry cell bounds and relative/translate
 // tables, per-species far-field bounds (FP64 and FP32), Walker tables and the merged-image Fourier coefficients.
 #pragma once
+#include <vector>
+
 #include "jf_device.cuh"
 
 namespace jf {
@@ -86,5 +88,10 @@ struct LaunchPlan {
     KernelClock *clock = nullptr;           // null when timing is off
     void *graphs = nullptr;                 // cache of captured round segments (null: plain launches)
 };
+
+// merged-image Coulomb: the Fourier coefficients on the host with the host libm
+// (merged_image_coulomb_potential.c:77-119) and the device description pointing at their device copy
+std::vector<double> fourier_table(int fc, double alpha, double length);
+MIC make_mic(int fc, int pc, double alpha, double length, const double *fourier);
 
 }  // namespace jf

@@ -250,6 +250,10 @@ MH make_lj(double prefactor, double sigma) {
     return h;
 }
 
+}  // namespace
+
+namespace jf {
+
 // merged_image_coulomb_potential.c:77-119
 std::vector<double> fourier_table(int fc, double alpha, double length) {
     int n = fc + 1;
@@ -280,7 +284,7 @@ MIC make_mic(int fc, int pc, double alpha, double length, const double *fourier)
     return m;
 }
 
-}  // namespace
+}  // namespace jf
 
 // ---------------------------------------------------------------------------------------------------------------
 // estimator scan: one block per (far cell, direction); the grid points of InnerPointEstimator.derivative_bound

@@ -21,7 +21,9 @@ FAR_NONE, FAR_CELL_VETO, FAR_CELL_BOUNDING = range(3)
 RNG_PAIR, RNG_THIN, RNG_VETO_TIME, RNG_VETO_CHOICE, RNG_VETO_UNIFORM, RNG_NEW_ACTIVE = range(6)
 
 STATUS_NAMES = {0: "ok", 1: "ValueError", 2: "AssertionError", 3: "ZeroDivisionError", 4: "complex result",
-                5: "bad configuration", 6: "allocation failure", 7: "cell index out of range"}
+                5: "bad configuration", 6: "allocation failure", 7: "cell index out of range",
+                9: "LiftingSchemeError", 10: "IndexError"}
+LIFTING_SCHEMES = {"inside_first": 0, "outside_first": 1, "ratio": 2}
 
 
 class OracleError(RuntimeError):
@@ -74,6 +76,12 @@ def lib() -> ctypes.CDLL:
         handle.jfo_randbelow.restype = ctypes.c_uint32
         handle.jfo_randbelow.argtypes = [ctypes.c_uint64, ctypes.c_uint32]
         handle.jfo_hs_displacement.argtypes = [_D, _PD, _PD, _PD]
+        _I = ctypes.c_int
+        handle.jfo_composite_event_time.argtypes = [_I, _D, _I, _I, _D, _D, _D, _PD, _PD, _D, _PD, _PD, _PD, _PD]
+        handle.jfo_composite_out_state.argtypes = [_I, _I, _I, _D, _I, _I, _D, _D, _D, _PD, _PD, _PD, _I, _PD, _PD,
+                                                   _I, _PD, ctypes.POINTER(ctypes.c_int), _PD, _PD]
+        handle.jfo_lifting.argtypes = [ctypes.c_int, ctypes.c_int, _PD, ctypes.POINTER(ctypes.c_int32), ctypes.c_int,
+                                       _D, ctypes.POINTER(ctypes.c_int64), _PD]
         handle.jfo_ip_displacement.argtypes = [_D, _D, _PD, _PD, _D, _D, _D, _PD]
         handle.jfo_ip_derivative.argtypes = [_D, _D, _PD, _PD, _D, _D, _PD]
         handle.jfo_lj_displacement.argtypes = [_D, _D, _PD, _PD, _D, _PD]
@@ -163,6 +171,53 @@ def expovariate(bits: int, beta: float) -> float:
 
 def randbelow(bits: int, n: int) -> int:
     return lib().jfo_randbelow(bits, n)
+
+
+# ---- lifting schemes ----
+def lifting(scheme: str, rates: Sequence[float], active: Sequence[bool], draw: float, unit_draw: bool = False):
+    """(status, table index of the new active unit, b of the deciding random.uniform(0.0, b)) of one table."""
+    count = len(rates)
+    r = (ctypes.c_double * max(count, 1))(*[float(x) for x in rates])
+    a = (ctypes.c_int32 * max(count, 1))(*[1 if x else 0 for x in active])
+    selected = ctypes.c_int64(-1)
+    bound = ctypes.c_double(0.0)
+    status = lib().jfo_lifting(LIFTING_SCHEMES[scheme], 1 if unit_draw else 0, r, a, count, float(draw),
+                               ctypes.byref(selected), ctypes.byref(bound))
+    return status, selected.value, bound.value
+
+
+# ---- composite objects ----
+def _doubles(values):
+    flat = [float(x) for x in np.asarray(values, dtype=np.float64).reshape(-1)]
+    return (ctypes.c_double * max(len(flat), 1))(*flat)
+
+
+def composite_event_time(model: dict, velocity, active_position, active_charge, target_positions, target_charges,
+                         potential_changes):
+    """(status, displacement) of send_event_time of two composite objects; model holds units, alpha,
+    fourier_cutoff, position_cutoff, coulomb_prefactor, bound_prefactor, system_length."""
+    out = ctypes.c_double(0.0)
+    status = lib().jfo_composite_event_time(
+        model["units"], model["alpha"], model["fourier_cutoff"], model["position_cutoff"],
+        model["coulomb_prefactor"], model["bound_prefactor"], model["system_length"], _doubles(velocity),
+        _doubles(active_position), float(active_charge), _doubles(target_positions), _doubles(target_charges),
+        _doubles(potential_changes), ctypes.byref(out))
+    return status, out.value
+
+
+def composite_out_state(model: dict, scheme: str, velocity, local_positions, local_charges, active_index,
+                        target_positions, target_charges, local_first, draws, unit_draw: bool = False):
+    """(status, new active, bounding rate, event rate) of send_out_state of two composite objects."""
+    new_active = ctypes.c_int(-1)
+    bounding = ctypes.c_double(0.0)
+    rate = ctypes.c_double(0.0)
+    status = lib().jfo_composite_out_state(
+        model["units"], LIFTING_SCHEMES[scheme], 1 if unit_draw else 0, model["alpha"], model["fourier_cutoff"],
+        model["position_cutoff"], model["coulomb_prefactor"], model["bound_prefactor"], model["system_length"],
+        _doubles(velocity), _doubles(local_positions), _doubles(local_charges), int(active_index),
+        _doubles(target_positions), _doubles(target_charges), 1 if local_first else 0, _doubles(draws),
+        ctypes.byref(new_active), ctypes.byref(bounding), ctypes.byref(rate))
+    return status, new_active.value, bounding.value, rate.value
 
 
 # ---- potentials (reference argument order: velocity, separation, [charges], [potential_change]) ----

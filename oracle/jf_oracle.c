@@ -876,6 +876,113 @@ int jfo_mic_derivative(double alpha, int fourier_cutoff, int position_cutoff, do
 }
 
 /* ======================================================================================
+ * Composite objects (event_handler/two_composite_object_summed_bounding_potential_event_handler.py)
+ * ==================================================================================== */
+
+/* setting.periodic_boundaries.separation_vector (hypercubic_setting.py:120-140, :156-172) */
+static void composite_separation(double length, const double *from, const double *to, double *s) {
+    double half = length / 2.0;
+    for (int d = 0; d < 3; ++d) s[d] = jfo_py_mod((to[d] - from[d]) + half, length) - half;
+}
+
+/* send_event_time (:119-150): min() over the target units of the bounding displacement */
+int jfo_composite_event_time(int units, double alpha, int fourier_cutoff, int position_cutoff,
+                             double coulomb_prefactor, double bound_prefactor, double system_length,
+                             const double *velocity, const double *active_position, double active_charge,
+                             const double *target_positions, const double *target_charges,
+                             const double *potential_changes, double *displacement) {
+    (void)alpha;
+    (void)fourier_cutoff;
+    (void)position_cutoff;
+    (void)coulomb_prefactor;
+    for (int j = 0; j < units; ++j) {
+        double s[3], value;
+        composite_separation(system_length, active_position, target_positions + 3 * j, s);
+        int st = jfo_ipcb_displacement(bound_prefactor, system_length, velocity, s, active_charge,
+                                       target_charges[j], potential_changes[j], &value);
+        if (st) return st;
+        if (j == 0 || value < *displacement) *displacement = value;
+    }
+    return JFO_OK;
+}
+
+/* send_out_state (:152-202) with _fill_lifting (event_handler_with_bounding_potential.py:170-220) */
+int jfo_composite_out_state(int units, int scheme, int unit_draw, double alpha, int fourier_cutoff,
+                            int position_cutoff, double coulomb_prefactor, double bound_prefactor,
+                            double system_length, const double *velocity, const double *local_positions,
+                            const double *local_charges, int active_index, const double *target_positions,
+                            const double *target_charges, int local_first, const double *draws, int *new_active,
+                            double *bounding_rate, double *event_rate) {
+    const double *active = local_positions + 3 * active_index;
+    double active_charge = local_charges[active_index];
+    double *target_factor = (double *)calloc((size_t)units, sizeof(double));
+    double *local_factor = (double *)calloc((size_t)units, sizeof(double));
+    double *table = (double *)malloc(sizeof(double) * (size_t)(2 * units));
+    int32_t *flags = (int32_t *)malloc(sizeof(int32_t) * (size_t)(2 * units));
+    int st = JFO_OK;
+    double bounding = 0.0, factor = 0.0;
+    *new_active = -1;
+    for (int j = 0; j < units && !st; ++j) {
+        double s[3], b, pair;
+        composite_separation(system_length, active, target_positions + 3 * j, s);
+        st = jfo_ipcb_derivative(bound_prefactor, velocity, s, active_charge, target_charges[j], &b);
+        if (!st) st = jfo_mic_derivative(alpha, fourier_cutoff, position_cutoff, coulomb_prefactor, system_length,
+                                         velocity, s, active_charge, target_charges[j], &pair);
+        if (st) break;
+        bounding += b > 0.0 ? b : 0.0;  /* max(0.0, b) keeps 0.0 unless b is larger */
+        factor += pair;
+        target_factor[j] -= pair;
+    }
+    double rate = factor > 0.0 ? factor : 0.0;
+    *bounding_rate = bounding;
+    *event_rate = rate;
+    double thinning = unit_draw ? 0.0 + (bounding - 0.0) * draws[0] : draws[0];
+    if (!st && !(rate <= thinning)) {
+        for (int i = 0; i < units && !st; ++i) {
+            if (i == active_index) {
+                local_factor[i] = rate;
+                continue;
+            }
+            for (int j = 0; j < units; ++j) {
+                double s[3], pair;
+                composite_separation(system_length, local_positions + 3 * i, target_positions + 3 * j, s);
+                st = jfo_mic_derivative(alpha, fourier_cutoff, position_cutoff, coulomb_prefactor, system_length,
+                                        velocity, s, local_charges[i], target_charges[j], &pair);
+                if (st) break;
+                local_factor[i] += pair;
+                target_factor[j] -= pair;
+            }
+        }
+        if (!st) {
+            /* insertion order of the derivative table: the object with the smaller identifier first */
+            int n = 0;
+            for (int pass = 0; pass < 2; ++pass) {
+                int locals = (pass == 0) == (local_first != 0);
+                for (int i = 0; i < units; ++i, ++n) {
+                    table[n] = locals ? local_factor[i] : target_factor[i];
+                    flags[n] = locals && i == active_index;
+                }
+            }
+            int64_t selected;
+            double bound;
+            st = jfo_lifting(scheme, unit_draw, table, flags, 2 * units, scheme == 2 ? draws[2] : draws[1],
+                             &selected, &bound);
+            if (!st) {
+                int local_start = local_first ? 0 : units;
+                int index = (int)selected;
+                *new_active = (index >= local_start && index < local_start + units) ? index - local_start
+                                                                                    : units + (index - (units - local_start));
+            }
+        }
+    }
+    free(target_factor);
+    free(local_factor);
+    free(table);
+    free(flags);
+    return st;
+}
+
+/* ======================================================================================
  * Cells (activator/internal_state/cell_occupancy/cells/cuboid_cells.py,
  *        cuboid_periodic_cells.py)
  * ==================================================================================== */
@@ -888,6 +995,75 @@ static double next_up(double x) {
 static double next_down(double x) { return -next_up(-x); }
 
 /* exact float bounds of the cells along one axis (cuboid_cells.py:115-131) */
+/* ---- lifting schemes ---------------------------------------------------------------------------------- */
+
+/* random.uniform(a, b) = a + (b - a) * random() (Python 3.12 random.py) */
+static double py_uniform(double a, double b, double unit) { return a + (b - a) * unit; }
+
+int jfo_lifting(int scheme, int unit_draw, const double *rates, const int32_t *active, int count, double draw,
+                int64_t *selected, double *bound) {
+    /* Lifting.reset / insert (lifting.py:38-80): the negated negative derivatives and their table indices,
+     * the random position from the positive derivatives up to and including the active unit */
+    double *negative = (double *)malloc(sizeof(double) * (size_t)(count > 0 ? count : 1));
+    int *where = (int *)malloc(sizeof(int) * (size_t)(count > 0 ? count : 1));
+    int negatives = 0, active_recorded = 0, status = JFO_OK;
+    double random_position = 0.0, uniform_bound = NAN;
+    *selected = -1;
+    for (int i = 0; i < count && status == JFO_OK; ++i) {
+        if (rates[i] > 0.0) {
+            if (active[i]) {
+                if (active_recorded) {
+                    status = JFO_ASSERT;  /* one active unit per table (lifting.py:33-34) */
+                    break;
+                }
+                active_recorded = 1;
+                uniform_bound = rates[i];
+                random_position += unit_draw ? py_uniform(0.0, rates[i], draw) : draw;
+            } else if (!active_recorded) {
+                random_position += rates[i];
+            }
+        } else {
+            if (active[i]) {
+                status = JFO_ASSERT;  /* lifting.py:76 */
+                break;
+            }
+            negative[negatives] = -rates[i];
+            where[negatives] = i;
+            ++negatives;
+        }
+    }
+    if (status == JFO_OK && !active_recorded) status = JFO_LIFTING;  /* lifting.py:107-108 */
+    if (status != JFO_OK) {
+        *bound = NAN;
+    } else {
+        double total = jfo_py_sum(negative, negatives);
+        double position = random_position;
+        if (scheme == 1) {
+            position = total - random_position;  /* outside_first_lifting.py:49 */
+        } else if (scheme == 2) {
+            uniform_bound = total;               /* ratio_lifting.py:50 */
+            position = unit_draw ? py_uniform(0.0, total, draw) : draw;
+        }
+        *bound = uniform_bound;
+        if (negatives == 0) {
+            status = JFO_INDEX;                  /* identifiers[-1] of an empty list */
+        } else {
+            double summed = 0.0;
+            *selected = where[negatives - 1];
+            for (int k = 0; k < negatives; ++k) {
+                summed += negative[k];
+                if (position <= summed) {
+                    *selected = where[k];
+                    break;
+                }
+            }
+        }
+    }
+    free(negative);
+    free(where);
+    return status;
+}
+
 void jfo_cell_bounds(double system_length, int m, double *cell_min, double *cell_max) {
     double side = system_length / m;
     for (int i = 0; i < m; ++i) {

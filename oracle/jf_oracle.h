@@ -27,6 +27,8 @@ extern "C" {
 #define JFO_BAD_CONFIG 5
 #define JFO_ALLOC 6
 #define JFO_CELL_RANGE 7       /* position_to_cell index outside the cell list (IndexError) */
+#define JFO_LIFTING 9          /* LiftingSchemeError: no active unit in the lifting table */
+#define JFO_INDEX 10           /* IndexError: no negative derivative in the lifting table */
 
 /* ---- event kinds recorded in the event log ---- */
 #define JFO_EV_PAIR 0          /* inverted pair potential (hard sphere / Lennard-Jones): lifting */
@@ -98,6 +100,30 @@ double jfo_mic_x_derivative(double alpha, int fourier_cutoff, int position_cutof
 int jfo_mic_derivative(double alpha, int fourier_cutoff, int position_cutoff, double prefactor,
                        double system_length, const double *velocity, const double *separation,
                        double charge_one, double charge_two, double *out);
+
+/* lifting schemes of composite objects (lifting/lifting.py:47-108 with inside_first_lifting.py:37-54,
+ * outside_first_lifting.py:38-55, ratio_lifting.py:38-56).  scheme 0 inside-first, 1 outside-first, 2 ratio;
+ * unit_draw 0: draw is the value random.uniform returned, 1: draw is random() and the value is formed as
+ * random.uniform does.  *selected = table index of the new active unit, *bound = b of the deciding
+ * random.uniform(0.0, b) call (NaN if the reference raises first). */
+int jfo_lifting(int scheme, int unit_draw, const double *rates, const int32_t *active, int count, double draw,
+                int64_t *selected, double *bound);
+
+/* events between two composite objects of `units` point charges each
+ * (two_composite_object_summed_bounding_potential_event_handler.py:119-202): merged-image Coulomb
+ * (alpha, fourier_cutoff, position_cutoff, coulomb_prefactor) bounded by the inverse-power Coulomb bound
+ * (bound_prefactor).  Positions are [units][3]; scheme and unit_draw as for jfo_lifting. */
+int jfo_composite_event_time(int units, double alpha, int fourier_cutoff, int position_cutoff,
+                             double coulomb_prefactor, double bound_prefactor, double system_length,
+                             const double *velocity, const double *active_position, double active_charge,
+                             const double *target_positions, const double *target_charges,
+                             const double *potential_changes, double *displacement);
+int jfo_composite_out_state(int units, int scheme, int unit_draw, double alpha, int fourier_cutoff,
+                            int position_cutoff, double coulomb_prefactor, double bound_prefactor,
+                            double system_length, const double *velocity, const double *local_positions,
+                            const double *local_charges, int active_index, const double *target_positions,
+                            const double *target_charges, int local_first, const double *draws, int *new_active,
+                            double *bounding_rate, double *event_rate);
 
 /* cells */
 void jfo_cell_bounds(double system_length, int cells_per_side, double *cell_min, double *cell_max);

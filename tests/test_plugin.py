@@ -6,6 +6,8 @@ selects the GPU classes by name:
 
 * ``potential = gpu_lennard_jones_potential`` (and the other GPU potentials) builds the GPU class inside the
   reference's own event handler;
+* ``lifting = gpu_inside_first_lifting`` (and the other schemes) builds the GPU lifting inside the reference's
+  composite-object event handler;
 * ``mediator = gpu_chain_batch_mediator`` builds the drop-in mediator from the same object graph, and its batch
   plan is the system of the configuration (the chain parameters that the GPU trajectory tests run, the injected
   initial positions and charges).
@@ -103,6 +105,45 @@ def translate_configuration(name):
     return {"spec": dataclasses.asdict(plan.spec), "positions": plan.positions.tolist(),
             "charges": None if plan.charges is None else plan.charges.tolist(),
             "end_of_run_time": plan.end_of_run_time, "chains": plan.chains, "mode": plan.mode, "seed": plan.seed}
+
+
+def build_composite_handler_with_gpu_lifting(scheme):
+    factory, camel = _reference()
+    config = configparser.ConfigParser()
+    config.read_string("""
+[Run]
+setting = hypercubic_setting
+[HypercubicSetting]
+system_length = 10.0
+beta = 1.679
+dimension = 3
+[TwoCompositeObjectSummedBoundingPotentialEventHandler]
+potential = merged_image_coulomb_potential
+bounding_potential = inverse_power_coulomb_bounding_potential
+lifting = gpu_%s_lifting
+charge = electric_charge
+[MergedImageCoulombPotential]
+prefactor = 332
+[InversePowerCoulombBoundingPotential]
+prefactor = 531.2
+""" % scheme)
+    factory.build_from_config(config, camel(config.get("Run", "setting")), "jellyfysh.setting")
+    from jellyfysh import setting
+    # two water molecules, as the reference's water node creator sets them: the handler wants composite objects
+    setting.set_number_of_root_nodes(2)
+    setting.set_number_of_nodes_per_root_node(3)
+    setting.set_number_of_node_levels(2)
+    handler = factory.build_from_config(config, "TwoCompositeObjectSummedBoundingPotentialEventHandler",
+                                        "jellyfysh.event_handler")
+    return [type(handler._lifting).__name__, type(handler._lifting).__module__]
+
+
+@pytest.mark.parametrize("scheme", ["inside_first", "outside_first", "ratio"])
+def test_gpu_lifting_is_built_inside_the_reference_composite_handler(scheme):
+    name, module = _in_child("build_composite_handler_with_gpu_lifting", scheme)
+    camel = "".join(part.capitalize() for part in scheme.split("_"))
+    assert name == "Gpu%sLifting" % camel
+    assert module == "jellyfysh.lifting.gpu_%s_lifting" % scheme
 
 
 def test_gpu_potentials_are_built_inside_the_reference_event_handler():
