@@ -115,3 +115,38 @@ def batched_hard_sphere_state(n: int, packing_fraction: float, radius: float, rn
                          "cells; take n = 4 k^3" % (n, packing_fraction, k))
     return fcc_jitter(n, length, fcc_jitter_fraction, rng), length
 
+
+
+def random_rotation(rng: np.random.Generator) -> np.ndarray:
+    """A uniformly random rotation matrix (unit quaternion from four normal deviates)."""
+    q = rng.normal(size=4)
+    q /= np.linalg.norm(q)
+    w, x, y, z = q
+    return np.array([[1 - 2 * (y * y + z * z), 2 * (x * y - z * w), 2 * (x * z + y * w)],
+                     [2 * (x * y + z * w), 1 - 2 * (x * x + z * z), 2 * (y * z - x * w)],
+                     [2 * (x * z - y * w), 2 * (y * z + x * w), 1 - 2 * (x * x + y * y)]])
+
+
+def water_lattice(molecules_per_side: int, system_length: float, oh_length: float, hh_length: float,
+                  rng: np.random.Generator, charge_oxygen: float = -0.82, charge_hydrogen: float = 0.41):
+    """Water molecules on a simple-cubic lattice of ``molecules_per_side``^3 sites (site centres ``(i + 1/2) L / m``)
+    in seeded uniformly random orientations; the bonds have the equilibrium lengths (O–H and H–H, hence the angle).
+    As the reference's water node creator does (``water_random_node_creator.py``), the site is the molecule's
+    barycentre of equal weights, so that the oxygens are off the lattice lines.  Leaf units in the reference's order
+    per molecule, hydrogen, oxygen, hydrogen.  Returns (positions [3 m^3][3] in [0, L), charges [3 m^3])."""
+    half_angle = math.asin(hh_length / (2.0 * oh_length))
+    bond_one = np.array([math.sin(half_angle), math.cos(half_angle), 0.0]) * oh_length
+    bond_two = np.array([-math.sin(half_angle), math.cos(half_angle), 0.0]) * oh_length
+    spacing = system_length / molecules_per_side
+    positions = []
+    for iz in range(molecules_per_side):
+        for iy in range(molecules_per_side):
+            for ix in range(molecules_per_side):
+                centre = (np.array([ix, iy, iz], dtype=np.float64) + 0.5) * spacing
+                rotation = random_rotation(rng)
+                one, two = rotation @ bond_one, rotation @ bond_two
+                oxygen = centre - (one + two) / 3.0
+                positions.extend([oxygen + one, oxygen, oxygen + two])
+    molecules = molecules_per_side ** 3
+    charges = np.tile(np.array([charge_hydrogen, charge_oxygen, charge_hydrogen]), molecules)
+    return _wrap(np.array(positions, dtype=np.float64), system_length), charges

@@ -16,9 +16,10 @@ import numpy as np
 from .build_oracle import build as _build
 
 EV_PAIR, EV_BOUNDED, EV_HARDCORE, EV_CELL_BOUNDING, EV_CELL_VETO, EV_BOUNDARY, EV_END_OF_CHAIN, EV_STOP = range(8)
+EV_BOND, EV_COMPOSITE = 8, 9
 POT_HARD_SPHERE, POT_LENNARD_JONES, POT_COULOMB = range(3)
 FAR_NONE, FAR_CELL_VETO, FAR_CELL_BOUNDING = range(3)
-RNG_PAIR, RNG_THIN, RNG_VETO_TIME, RNG_VETO_CHOICE, RNG_VETO_UNIFORM, RNG_NEW_ACTIVE = range(6)
+RNG_PAIR, RNG_THIN, RNG_VETO_TIME, RNG_VETO_CHOICE, RNG_VETO_UNIFORM, RNG_NEW_ACTIVE, RNG_COMPOSITE, RNG_LIFT = range(8)
 
 STATUS_NAMES = {0: "ok", 1: "ValueError", 2: "AssertionError", 3: "ZeroDivisionError", 4: "complex result",
                 5: "bad configuration", 6: "allocation failure", 7: "cell index out of range",
@@ -40,6 +41,17 @@ class JfoSystem(ctypes.Structure):
                 ("ewald_alpha", ctypes.c_double), ("fourier_cutoff", ctypes.c_int),
                 ("position_cutoff", ctypes.c_int), ("far", ctypes.c_int), ("estimator_points", ctypes.c_int),
                 ("estimator_prefactor", ctypes.c_double), ("rng_key", ctypes.c_uint64)]
+
+
+class JfoWaterSystem(ctypes.Structure):
+    _fields_ = [("molecules", ctypes.c_int), ("system_length", ctypes.c_double), ("beta", ctypes.c_double),
+                ("chain_time", ctypes.c_double), ("speed", ctypes.c_double), ("initial_direction", ctypes.c_int),
+                ("initial_active", ctypes.c_int), ("oh_r0", ctypes.c_double), ("oh_prefactor", ctypes.c_double),
+                ("hh_r0", ctypes.c_double), ("hh_prefactor", ctypes.c_double), ("lj_prefactor", ctypes.c_double),
+                ("lj_sigma", ctypes.c_double), ("coulomb_prefactor", ctypes.c_double),
+                ("bound_prefactor", ctypes.c_double), ("ewald_alpha", ctypes.c_double),
+                ("fourier_cutoff", ctypes.c_int), ("position_cutoff", ctypes.c_int), ("lifting", ctypes.c_int),
+                ("rng_key", ctypes.c_uint64)]
 
 
 EVENT_DTYPE = np.dtype([("kind", np.int32), ("moved", np.int32), ("target", np.int32), ("new_active", np.int32),
@@ -94,6 +106,12 @@ def lib() -> ctypes.CDLL:
         handle.jfo_mic_x_derivative.argtypes = [_D, ctypes.c_int, ctypes.c_int, _D, _D, _D, _D]
         handle.jfo_mic_derivative.argtypes = [_D, ctypes.c_int, ctypes.c_int, _D, _D, _PD, _PD, _D, _D, _PD]
         handle.jfo_cell_bounds.argtypes = [_D, ctypes.c_int, _PD, _PD]
+        handle.jfo_water_create.restype = ctypes.c_void_p
+        handle.jfo_water_create.argtypes = [ctypes.POINTER(JfoWaterSystem), _PD, _PD, ctypes.POINTER(ctypes.c_int)]
+        handle.jfo_water_destroy.argtypes = [ctypes.c_void_p]
+        handle.jfo_water_run.restype = ctypes.c_int64
+        handle.jfo_water_run.argtypes = [ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p, ctypes.POINTER(ctypes.c_int)]
+        handle.jfo_water_positions.argtypes = [ctypes.c_void_p, _PD]
         handle.jfo_chain_create.restype = ctypes.c_void_p
         handle.jfo_chain_create.argtypes = [ctypes.POINTER(JfoSystem), _PD, _PD, ctypes.POINTER(ctypes.c_int)]
         handle.jfo_chain_destroy.argtypes = [ctypes.c_void_p]
@@ -372,3 +390,61 @@ class Chain:
         lib().jfo_chain_walker(self._handle, direction, which, cells.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)),
                                rates.ctypes.data_as(_PD), size, ctypes.byref(total))
         return cells, rates, total.value
+
+
+# ---- flexible water -----------------------------------------------------------------------------
+WATER_FIELDS = [name for name, _ in JfoWaterSystem._fields_]
+
+
+def make_water_system(spec: dict, rng_key: int) -> JfoWaterSystem:
+    """The oracle's water system from a specification with the keys of the water trajectories (molecules_per_side or
+    molecules, system_length, beta, chain_time, speed, initial_direction, initial_active, oh_r0, oh_prefactor,
+    hh_r0, hh_prefactor, lj_prefactor, lj_sigma, coulomb_prefactor, bound_prefactor, alpha, fourier_cutoff,
+    position_cutoff, lifting)."""
+    molecules = spec.get("molecules", spec.get("molecules_per_side", 0) ** 3)
+    lifting = {"inside_first": 0, "outside_first": 1, "ratio": 2}[spec.get("lifting", "inside_first")]
+    return JfoWaterSystem(molecules=molecules, system_length=float(spec["system_length"]), beta=float(spec["beta"]),
+                          chain_time=float(spec["chain_time"]), speed=float(spec["speed"]),
+                          initial_direction=int(spec["initial_direction"]), initial_active=int(spec["initial_active"]),
+                          oh_r0=float(spec["oh_r0"]), oh_prefactor=float(spec["oh_prefactor"]),
+                          hh_r0=float(spec["hh_r0"]), hh_prefactor=float(spec["hh_prefactor"]),
+                          lj_prefactor=float(spec["lj_prefactor"]), lj_sigma=float(spec["lj_sigma"]),
+                          coulomb_prefactor=float(spec["coulomb_prefactor"]),
+                          bound_prefactor=float(spec["bound_prefactor"]), ewald_alpha=float(spec["alpha"]),
+                          fourier_cutoff=int(spec["fourier_cutoff"]), position_cutoff=int(spec["position_cutoff"]),
+                          lifting=lifting, rng_key=int(rng_key))
+
+
+class Water:
+    """One chain of flexible water molecules run by the oracle."""
+
+    def __init__(self, system: JfoWaterSystem, positions: np.ndarray, charges: np.ndarray):
+        self.system = system
+        self._positions_in = np.ascontiguousarray(positions, dtype=np.float64).reshape(-1, 3)
+        self._charges_in = np.ascontiguousarray(charges, dtype=np.float64)
+        assert self._positions_in.shape[0] == 3 * system.molecules == len(self._charges_in)
+        status = ctypes.c_int()
+        self._handle = lib().jfo_water_create(ctypes.byref(system), self._positions_in.ctypes.data_as(_PD),
+                                              self._charges_in.ctypes.data_as(_PD), ctypes.byref(status))
+        if not self._handle:
+            raise OracleError("water creation failed: " + STATUS_NAMES.get(status.value, str(status.value)))
+
+    def __del__(self):
+        handle = getattr(self, "_handle", None)
+        if handle:
+            lib().jfo_water_destroy(handle)
+            self._handle = None
+
+    def run(self, max_events: int):
+        log_array = np.zeros(max_events, dtype=EVENT_DTYPE)
+        status = ctypes.c_int()
+        done = lib().jfo_water_run(self._handle, max_events, log_array.ctypes.data, ctypes.byref(status))
+        if status.value != 0:
+            raise OracleError("water run stopped after %d events: %s"
+                              % (done, STATUS_NAMES.get(status.value, str(status.value))))
+        return log_array[:done]
+
+    def positions(self) -> np.ndarray:
+        out = np.zeros((3 * self.system.molecules, 3), dtype=np.float64)
+        lib().jfo_water_positions(self._handle, out.ctypes.data_as(_PD))
+        return out

@@ -1888,3 +1888,217 @@ int jfo_chain_occupancy(const JfoChain *c, int32_t *owner) {
     if (c->occ_active >= 0) owner[c->occ_active] = -1;
     return c->occ_cell;
 }
+
+/* ======================================================================================
+ * Flexible water (composite objects): the reference's event loop over the factors of a factor-set file
+ * (two_leaf_unit_event_handler.py:98-154 for the bonds and Lennard-Jones, the composite-object Coulomb factor of
+ * two_composite_object_summed_bounding_potential_event_handler.py:119-202, the end of chain of
+ * single_independent_active_periodic_direction_end_of_chain_event_handler.py:151-237)
+ * ==================================================================================== */
+struct JfoWater {
+    JfoWaterSystem sys;
+    int units;
+    double *pos;
+    double *charge;
+    MH oh, hh, lj;
+    int active, direction;
+    double ts_q, ts_r;      /* time stamp of the active unit */
+    double eoc_q, eoc_r;    /* end-of-chain candidate */
+    int eoc_new_active;
+    int64_t event;
+};
+
+static int water_new_active(const JfoWater *w, uint64_t event) {
+    int molecule = (int)jfo_randbelow(jfo_draw(w->sys.rng_key, event, JFO_RNG_NEW_ACTIVE, 0),
+                                      (uint32_t)w->sys.molecules);
+    int unit = (int)jfo_randbelow(jfo_draw(w->sys.rng_key, event, JFO_RNG_NEW_ACTIVE, 1), 3u);
+    return 3 * molecule + unit;
+}
+
+JfoWater *jfo_water_create(const JfoWaterSystem *system, const double *positions, const double *charges,
+                           int *status) {
+    *status = JFO_BAD_CONFIG;
+    if (system->molecules < 2 || !(system->system_length > 0.0) || system->initial_active < 0 ||
+        system->initial_active >= 3 * system->molecules || system->lifting < 0 || system->lifting > 2)
+        return NULL;
+    JfoWater *w = (JfoWater *)calloc(1, sizeof(JfoWater));
+    if (!w) {
+        *status = JFO_ALLOC;
+        return NULL;
+    }
+    w->sys = *system;
+    w->units = 3 * system->molecules;
+    w->pos = (double *)malloc(sizeof(double) * 3 * (size_t)w->units);
+    w->charge = (double *)malloc(sizeof(double) * (size_t)w->units);
+    if (!w->pos || !w->charge) {
+        jfo_water_destroy(w);
+        *status = JFO_ALLOC;
+        return NULL;
+    }
+    memcpy(w->pos, positions, sizeof(double) * 3 * (size_t)w->units);
+    memcpy(w->charge, charges, sizeof(double) * (size_t)w->units);
+    w->oh = mh_dep(system->oh_r0, 2, system->oh_prefactor);
+    w->hh = mh_dep(system->hh_r0, 2, system->hh_prefactor);
+    w->lj = mh_lj(system->lj_prefactor, system->lj_sigma);
+    w->active = system->initial_active;
+    w->direction = system->initial_direction;
+    w->ts_q = 0.0;
+    w->ts_r = 0.0;
+    jfo_time_add(0.0, 0.0, jfo_time_sub(0.0, 0.0, 0.0, 0.0) + system->chain_time, &w->eoc_q, &w->eoc_r);
+    w->eoc_new_active = water_new_active(w, 0);
+    *status = JFO_OK;
+    return w;
+}
+
+void jfo_water_destroy(JfoWater *w) {
+    if (!w) return;
+    free(w->pos);
+    free(w->charge);
+    free(w);
+}
+
+static void water_separation(const JfoWater *w, int from, int to, double *s) {
+    composite_separation(w->sys.system_length, &w->pos[3 * from], &w->pos[3 * to], s);
+}
+
+int64_t jfo_water_run(JfoWater *w, int64_t max_events, JfoEvent *log, int *status) {
+    const JfoWaterSystem *s = &w->sys;
+    const int M = s->molecules;
+    int64_t done = 0;
+    *status = JFO_OK;
+    while (done < max_events) {
+        const int a = w->active, m = a / 3, t = a % 3;
+        double velocity[3] = {0.0, 0.0, 0.0};
+        velocity[w->direction] = s->speed;
+        Cand best;
+        best.q = INFINITY;
+        best.r = INFINITY;
+        best.kind = 1 << 30;
+        best.target = 1 << 30;
+        best.aux = -1;
+        best.rate = 0.0;
+        int st = JFO_OK;
+        /* bonds of the active unit's molecule: O-H for pairs with the oxygen, H-H between the hydrogens */
+        for (int u = 0; u < 3 && !st; ++u) {
+            if (u == t) continue;
+            const MH *bond = (t == 1 || u == 1) ? &w->oh : &w->hh;
+            int b = 3 * m + u;
+            double sep[3], dt;
+            water_separation(w, a, b, sep);
+            double du = jfo_expovariate(jfo_draw(s->rng_key, w->event, JFO_RNG_PAIR, b), s->beta);
+            st = mh_displacement(bond, velocity, sep, du, &dt);
+            if (!st) offer(&best, w->ts_q, w->ts_r, dt, JFO_EV_BOND, b, -1, 0.0);
+        }
+        /* Lennard-Jones between the active oxygen and every other oxygen */
+        for (int other = 0; other < M && !st && t == 1; ++other) {
+            if (other == m) continue;
+            int b = 3 * other + 1;
+            double sep[3], dt;
+            water_separation(w, a, b, sep);
+            double du = jfo_expovariate(jfo_draw(s->rng_key, w->event, JFO_RNG_PAIR, b), s->beta);
+            st = mh_displacement(&w->lj, velocity, sep, du, &dt);
+            if (!st) offer(&best, w->ts_q, w->ts_r, dt, JFO_EV_PAIR, b, -1, 0.0);
+        }
+        /* Coulomb factor of the active molecule with every other molecule */
+        for (int other = 0; other < M && !st; ++other) {
+            if (other == m) continue;
+            double du[3], dt;
+            for (int j = 0; j < 3; ++j)
+                du[j] = jfo_expovariate(jfo_draw(s->rng_key, w->event, JFO_RNG_COMPOSITE, (uint32_t)(3 * other + j)),
+                                        s->beta);
+            st = jfo_composite_event_time(3, s->ewald_alpha, s->fourier_cutoff, s->position_cutoff,
+                                          s->coulomb_prefactor, s->bound_prefactor, s->system_length, velocity,
+                                          &w->pos[3 * a], w->charge[a], &w->pos[9 * other], &w->charge[3 * other], du,
+                                          &dt);
+            if (!st) offer(&best, w->ts_q, w->ts_r, dt, JFO_EV_COMPOSITE, other, -1, 0.0);
+        }
+        if (st) {
+            *status = st;
+            return done;
+        }
+        {
+            Cand e;
+            e.q = w->eoc_q;
+            e.r = w->eoc_r;
+            e.kind = JFO_EV_END_OF_CHAIN;
+            e.target = w->eoc_new_active;
+            e.aux = -1;
+            e.rate = 0.0;
+            if (cand_better(&e, &best)) best = e;
+        }
+        /* commit: time slice of the active unit, then the out-state */
+        JfoEvent ev;
+        ev.kind = best.kind;
+        ev.moved = a;
+        ev.target = best.target;
+        ev.accepted = 1;
+        ev.time_q = best.q;
+        ev.time_r = best.r;
+        {
+            double dt = jfo_time_sub(best.q, best.r, w->ts_q, w->ts_r);
+            double *p = &w->pos[3 * a];
+            for (int d = 0; d < 3; ++d) {
+                double v = d == w->direction ? s->speed : 0.0;
+                p[d] = jfo_py_mod(p[d] + v * dt, s->system_length);
+            }
+            w->ts_q = best.q;
+            w->ts_r = best.r;
+        }
+        switch (best.kind) {
+        case JFO_EV_BOND:
+        case JFO_EV_PAIR:
+            w->active = best.target;
+            break;
+        case JFO_EV_COMPOSITE: {
+            int other = best.target, new_active;
+            double draws[3], bounding, rate;
+            draws[0] = jfo_uniform(jfo_draw(s->rng_key, w->event, JFO_RNG_THIN, 0));
+            draws[1] = jfo_uniform(jfo_draw(s->rng_key, w->event, JFO_RNG_LIFT, 0));
+            draws[2] = draws[1];
+            st = jfo_composite_out_state(3, s->lifting, 1, s->ewald_alpha, s->fourier_cutoff, s->position_cutoff,
+                                         s->coulomb_prefactor, s->bound_prefactor, s->system_length, velocity,
+                                         &w->pos[9 * m], &w->charge[3 * m], t, &w->pos[9 * other],
+                                         &w->charge[3 * other], m < other, draws, &new_active, &bounding, &rate);
+            if (st) {
+                *status = st;
+                return done;
+            }
+            ev.accepted = new_active >= 0;
+            if (new_active >= 0) w->active = new_active < 3 ? 3 * m + new_active : 3 * other + (new_active - 3);
+            break;
+        }
+        case JFO_EV_END_OF_CHAIN:
+            w->direction = (w->direction + 1) % 3;
+            w->active = best.target;
+            jfo_time_add(w->ts_q, w->ts_r, jfo_time_sub(w->ts_q, w->ts_r, w->ts_q, w->ts_r) + s->chain_time,
+                         &w->eoc_q, &w->eoc_r);
+            w->eoc_new_active = water_new_active(w, (uint64_t)(w->event + 1));
+            break;
+        default:
+            *status = JFO_ASSERT;
+            return done;
+        }
+        ev.new_active = w->active;
+        ev.new_direction = w->direction;
+        ev.x = w->pos[3 * a];
+        ev.y = w->pos[3 * a + 1];
+        ev.z = w->pos[3 * a + 2];
+        if (log) log[done] = ev;
+        w->event++;
+        done++;
+    }
+    return done;
+}
+
+void jfo_water_positions(const JfoWater *w, double *positions) {
+    memcpy(positions, w->pos, sizeof(double) * 3 * (size_t)w->units);
+}
+
+void jfo_water_state(const JfoWater *w, int64_t *event_count, int *active, int *direction, double *time_q,
+                     double *time_r) {
+    *event_count = w->event;
+    *active = w->active;
+    *direction = w->direction;
+    *time_q = w->ts_q;
+    *time_r = w->ts_r;
+}

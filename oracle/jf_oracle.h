@@ -39,6 +39,8 @@ extern "C" {
 #define JFO_EV_BOUNDARY 5      /* cell-boundary event */
 #define JFO_EV_END_OF_CHAIN 6  /* end-of-chain event */
 #define JFO_EV_STOP 7          /* run stopped at a stop time (sampling / end-of-run time slice) */
+#define JFO_EV_BOND 8          /* intramolecular bond (displaced even power) of a water molecule: lifting */
+#define JFO_EV_COMPOSITE 9     /* Coulomb factor of two molecules: thinning and lifting within both */
 
 /* ---- pair potential kinds of a chain system ---- */
 #define JFO_POT_HARD_SPHERE 0
@@ -56,7 +58,9 @@ extern "C" {
 #define JFO_RNG_VETO_TIME 2    /* potential change of the cell-veto handler */
 #define JFO_RNG_VETO_CHOICE 3  /* Walker table entry */
 #define JFO_RNG_VETO_UNIFORM 4 /* Walker uniform */
-#define JFO_RNG_NEW_ACTIVE 5   /* end-of-chain randint */
+#define JFO_RNG_NEW_ACTIVE 5   /* end-of-chain randint (target 0: molecule or atom, 1: unit of the molecule) */
+#define JFO_RNG_COMPOSITE 6    /* potential change of a Coulomb factor of two molecules, per target unit */
+#define JFO_RNG_LIFT 7         /* uniform of the lifting scheme */
 
 /* primitives */
 double jfo_py_mod(double x, double y);
@@ -166,6 +170,36 @@ typedef struct {
     double time_q, time_r;  /* event time */
     double x, y, z;         /* committed position of the moved particle */
 } JfoEvent;
+
+/* flexible water: molecules of three units (hydrogen, oxygen, hydrogen; unit 3 m + t), harmonic O-H and H-H bonds
+ * (displaced even power, power 2), Lennard-Jones between oxygens and a Coulomb factor of every pair of molecules
+ * (merged-image Coulomb bounded by the summed inverse-power Coulomb bound, lifting scheme `lifting`), all pairs of
+ * molecules, periodic-direction end of chain */
+typedef struct {
+    int molecules;
+    double system_length;
+    double beta;
+    double chain_time;
+    double speed;
+    int initial_direction;
+    int initial_active;     /* unit index */
+    double oh_r0, oh_prefactor;
+    double hh_r0, hh_prefactor;
+    double lj_prefactor, lj_sigma;
+    double coulomb_prefactor, bound_prefactor, ewald_alpha;
+    int fourier_cutoff, position_cutoff;
+    int lifting;            /* 0 inside-first, 1 outside-first, 2 ratio */
+    uint64_t rng_key;
+} JfoWaterSystem;
+
+typedef struct JfoWater JfoWater;
+JfoWater *jfo_water_create(const JfoWaterSystem *system, const double *positions, const double *charges, int *status);
+void jfo_water_destroy(JfoWater *water);
+/* runs up to max_events events; returns the number run; *status is JFO_OK or the first failure */
+int64_t jfo_water_run(JfoWater *water, int64_t max_events, JfoEvent *log, int *status);
+void jfo_water_positions(const JfoWater *water, double *positions);
+void jfo_water_state(const JfoWater *water, int64_t *event_count, int *active, int *direction, double *time_q,
+                     double *time_r);
 
 typedef struct JfoChain JfoChain;
 

@@ -1,0 +1,39 @@
+"""The oracle's water event loop against trajectories of the reference's own event loop (bit-exact)."""
+import numpy as np
+import pytest
+
+import oracle
+from tests.water_cases import FIELDS, load_water, water_names
+
+
+@pytest.mark.parametrize("name", water_names())
+def test_oracle_reproduces_the_reference_water_trajectory(name):
+    spec, initial, charges, events, final = load_water(name)
+    water = oracle.Water(oracle.make_water_system(spec, spec["rng_key"]), initial, charges)
+    log = water.run(len(events))
+    assert len(log) == len(events)
+    for field in FIELDS + ("time_q", "time_r", "x", "y", "z"):
+        assert (log[field] == events[field]).all(), field
+    assert (water.positions() == final).all()
+
+
+def test_water_trajectories_cover_every_event_kind():
+    kinds = set()
+    for name in water_names():
+        events = load_water(name)[3]
+        kinds |= set(zip(events["kind"].tolist(), events["accepted"].tolist()))
+    assert {(oracle.EV_COMPOSITE, 0), (oracle.EV_COMPOSITE, 1), (oracle.EV_BOND, 1), (oracle.EV_PAIR, 1),
+            (oracle.EV_END_OF_CHAIN, 1)} <= kinds
+    assert "water_n64" in water_names()  # the 64-molecule box of the batched water workload
+
+
+def test_water_lattice_geometry():
+    from jellyfysh_gb300 import systems
+    positions, charges = systems.water_lattice(4, 12.42, 1.0, 1.633, np.random.default_rng(5))
+    assert positions.shape == (192, 3) and (positions >= 0).all() and (positions < 12.42).all()
+    assert charges.sum() == pytest.approx(0.0, abs=1e-12)
+    s = positions.reshape(64, 3, 3)
+    wrap = lambda v: (v + 6.21) % 12.42 - 6.21
+    assert np.allclose(np.linalg.norm(wrap(s[:, 0] - s[:, 1]), axis=1), 1.0)
+    assert np.allclose(np.linalg.norm(wrap(s[:, 2] - s[:, 1]), axis=1), 1.0)
+    assert np.allclose(np.linalg.norm(wrap(s[:, 2] - s[:, 0]), axis=1), 1.633)
