@@ -77,6 +77,8 @@ extern "C" {
 #define JFGPU_EV_CELL_VETO 4
 #define JFGPU_EV_BOUNDARY 5
 #define JFGPU_EV_END_OF_CHAIN 6
+#define JFGPU_EV_BOND 8                /* intramolecular bond of a water molecule (lifting) */
+#define JFGPU_EV_COMPOSITE 9           /* Coulomb factor of two molecules (thinning, lifting within both) */
 
 /* ======================================================================================================
  * Potentials: batched displacement / derivative.  velocity and separation are device arrays [n][3];
@@ -261,6 +263,54 @@ typedef struct {
     double time_q, time_r;
     double x, y, z;
 } JfgpuEvent;
+
+/* ======================================================================================================
+ * Flexible water: batched chains of `molecules` water molecules (hydrogen, oxygen, hydrogen; unit 3 m + t of
+ * molecule m) with harmonic O-H and H-H bonds (DisplacedEvenPowerPotential, power 2), Lennard-Jones between the
+ * oxygens and one Coulomb factor per pair of molecules (the composite-object event above, inside-first,
+ * outside-first or ratio lifting), for every pair of molecules, and the periodic-direction end of chain.  One
+ * warp advances one chain, in FP64 with the reference's arithmetic.  Replaces the reference's event loop
+ * (mediator/single_process_mediator.py:91-156) over the handlers of these factors:
+ * two_leaf_unit_event_handler.py:98-154, two_composite_object_summed_bounding_potential_event_handler.py:119-202,
+ * single_independent_active_periodic_direction_end_of_chain_event_handler.py:151-237.
+ * ==================================================================================================== */
+typedef struct {
+    int32_t molecules;            /* per chain, 2..4096 */
+    int32_t lifting;              /* JFGPU_LIFTING_* */
+    int32_t fourier_cutoff;       /* merged-image Coulomb */
+    int32_t position_cutoff;
+    int32_t initial_active;       /* unit index */
+    int32_t initial_direction;
+    double system_length;
+    double beta;
+    double chain_time;
+    double speed;
+    double oh_r0, oh_prefactor;   /* O-H bond: prefactor (r - r0)^2 */
+    double hh_r0, hh_prefactor;   /* H-H bond */
+    double lj_prefactor, lj_sigma;
+    double coulomb_prefactor, bound_prefactor, alpha;
+    uint64_t seed;                /* chain c draws its random numbers with the key of (seed, c) */
+} JfgpuWaterDesc;
+
+/* per-chain state of a water batch (device array [chains]) */
+typedef struct {
+    double time_q, time_r;        /* time stamp of the active unit */
+    double eoc_q, eoc_r;          /* end-of-chain candidate */
+    int32_t active, direction, eoc_new_active, status;
+    int64_t events;               /* committed events: the event index of the keyed draws */
+    int64_t composite_events, composite_accepted, bond_events, lj_events, eoc_events;
+} JfgpuWaterState;
+
+/* the model on the current device (the Fourier table of the Coulomb factor) */
+int jfgpu_water_create(const JfgpuWaterDesc *desc, void **water);
+void jfgpu_water_destroy(void *water);
+/* chains first_chain .. first_chain + chains - 1 at time 0: the initial active unit and direction, the first end
+ * of chain (time chain_time, new active unit drawn for event 0) */
+int jfgpu_water_init(void *water, JfgpuWaterState *state, int64_t chains, int64_t first_chain, void *stream);
+/* `events` events of every chain.  positions [chains][3 molecules][3] and charges [3 molecules] are device arrays;
+ * log [chains][events] (may be null) receives every committed event; warps_per_block 1..8 (0: 1). */
+int jfgpu_water_run(void *water, double *positions, const double *charges, JfgpuWaterState *state, int64_t chains,
+                    int64_t first_chain, int64_t events, JfgpuEvent *log, int32_t warps_per_block, void *stream);
 
 /* device buffers of a chain batch, all owned by the caller; sizes from jfgpu_engine_layout */
 typedef struct {

@@ -25,6 +25,7 @@ POT_HARD_SPHERE, POT_LENNARD_JONES, POT_COULOMB = 0, 1, 2
 FAR_NONE, FAR_CELL_VETO, FAR_CELL_BOUNDING = 0, 1, 2
 MODE_EXACT, MODE_MIXED = 0, 1
 EV_PAIR, EV_BOUNDED, EV_HARDCORE, EV_CELL_BOUNDING, EV_CELL_VETO, EV_BOUNDARY, EV_END_OF_CHAIN = range(7)
+EV_BOND, EV_COMPOSITE = 8, 9
 
 
 class LibraryMissing(RuntimeError):
@@ -44,6 +45,18 @@ class CompositeDesc(ctypes.Structure):
     _fields_ = [("units", ctypes.c_int32), ("lifting", ctypes.c_int32), ("fourier_cutoff", ctypes.c_int32),
                 ("position_cutoff", ctypes.c_int32), ("alpha", ctypes.c_double), ("coulomb_prefactor", ctypes.c_double),
                 ("bound_prefactor", ctypes.c_double), ("system_length", ctypes.c_double)]
+
+
+class WaterDesc(ctypes.Structure):
+    """JfgpuWaterDesc."""
+    _fields_ = [("molecules", ctypes.c_int32), ("lifting", ctypes.c_int32), ("fourier_cutoff", ctypes.c_int32),
+                ("position_cutoff", ctypes.c_int32), ("initial_active", ctypes.c_int32),
+                ("initial_direction", ctypes.c_int32), ("system_length", ctypes.c_double), ("beta", ctypes.c_double),
+                ("chain_time", ctypes.c_double), ("speed", ctypes.c_double), ("oh_r0", ctypes.c_double),
+                ("oh_prefactor", ctypes.c_double), ("hh_r0", ctypes.c_double), ("hh_prefactor", ctypes.c_double),
+                ("lj_prefactor", ctypes.c_double), ("lj_sigma", ctypes.c_double),
+                ("coulomb_prefactor", ctypes.c_double), ("bound_prefactor", ctypes.c_double),
+                ("alpha", ctypes.c_double), ("seed", ctypes.c_uint64)]
 
 
 class ChainDesc(ctypes.Structure):
@@ -114,6 +127,10 @@ SIGNATURES = {
                                                   _P, _P]),
     "jfgpu_composite_out_state": (ctypes.c_int, [ctypes.POINTER(CompositeDesc), _I32, _P, _P, _P, _P, _P, _P, _P,
                                                  _P, _I64, _P, _P, _P, _P]),
+    "jfgpu_water_create": (ctypes.c_int, [ctypes.POINTER(WaterDesc), ctypes.POINTER(ctypes.c_void_p)]),
+    "jfgpu_water_destroy": (None, [_P]),
+    "jfgpu_water_init": (ctypes.c_int, [_P, _P, _I64, _I64, _P]),
+    "jfgpu_water_run": (ctypes.c_int, [_P, _P, _P, _P, _I64, _I64, _I64, _P, _I32, _P]),
     "jfgpu_engine_create": (ctypes.c_int, [_P, _I64, _P, ctypes.POINTER(ctypes.c_void_p)]),
     "jfgpu_engine_destroy": (None, [_P]),
     "jfgpu_engine_layout": (ctypes.c_int, [_P, ctypes.POINTER(Layout)]),

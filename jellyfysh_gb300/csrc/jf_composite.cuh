@@ -64,40 +64,32 @@ __device__ inline int composite_event_time(const CompositeModel &m, const double
     return JFGPU_STATUS_OK;
 }
 
-// send_out_state (:152-202).  locals / targets [units][3] and their charges, sorted by identifier; active is the
-// index of the active unit among the locals; local_first tells whether the local object's identifier is the
-// smaller one (the order of the derivative table).  draws: [0] thinning random.uniform(0.0, bounding rate),
-// [1] the active unit's insert into the lifting table, [2] the ratio scheme's draw; values or unit draws as in
-// lifting_select.  new_active: -1 when thinned, else 0..units-1 (a local unit) or units..2 units-1 (a target).
-__device__ inline int composite_out_state(const CompositeModel &m, int draw_mode, const double *velocity,
-                                          const double *locals, const double *local_charges, int active,
-                                          const double *targets, const double *target_charges, int local_first,
-                                          const double *draws, int &new_active, double &bounding_rate,
-                                          double &event_rate) {
-    new_active = -1;
+// The thinning of send_out_state (:171-192) from the pair derivatives of the active unit against the target units
+// (bound[j]: bounding potential, pair[j]: potential), in the reference's order of additions.  Fills target_factor
+// (0.0 - pair[j], the start of _fill_lifting's target derivatives) and returns whether the event is confirmed.
+__device__ inline bool composite_thinning(const CompositeModel &m, int draw_mode, const double *bound,
+                                          const double *pair, const double *draws, double *target_factor,
+                                          double &bounding_rate, double &event_rate) {
     bounding_rate = 0.0;
-    event_rate = 0.0;
-    int d;
-    double speed;
-    JF_TRY(analyse_velocity(velocity, d, speed));
-    const int k = m.units;
-    const double *a = locals + 3 * active;
-    const double ca = local_charges[active];
-    double target_factor[kMaxCompositeUnits], local_factor[kMaxCompositeUnits];
     double factor = 0.0;
-    for (int j = 0; j < k; ++j) {
-        double s[3];
-        periodic_separation(a, targets + 3 * j, m.system_length, s);
-        const double b = bound_derivative(m, d, speed, s, ca, target_charges[j]);
-        bounding_rate += b > 0.0 ? b : 0.0;  // max(0.0, b)
-        const double pair = coulomb_derivative(m, d, speed, s, ca, target_charges[j]);
-        factor += pair;
-        target_factor[j] = 0.0 - pair;
+    for (int j = 0; j < m.units; ++j) {
+        bounding_rate += bound[j] > 0.0 ? bound[j] : 0.0;  // max(0.0, b)
+        factor += pair[j];
+        target_factor[j] = 0.0 - pair[j];
     }
     event_rate = factor > 0.0 ? factor : 0.0;
     const double thinning = draw_mode == JFGPU_DRAW_UNIT ? 0.0 + (bounding_rate - 0.0) * draws[0] : draws[0];
-    if (event_rate <= thinning) return JFGPU_STATUS_OK;
-    // _fill_lifting: factor derivatives of the local units against every target unit, with the active's velocity
+    return !(event_rate <= thinning);
+}
+
+// _fill_lifting (event_handler_with_bounding_potential.py:170-220) and the lifting scheme, from the potential
+// derivatives cross[i * units + j] of the non-active local units i against the target units j (the active
+// unit's velocity).  new_active as in composite_out_state.
+__device__ inline int composite_lifting(const CompositeModel &m, int draw_mode, int active, int local_first,
+                                        double event_rate, double *target_factor, const double *cross,
+                                        const double *draws, int &new_active) {
+    const int k = m.units;
+    double local_factor[kMaxCompositeUnits];
     for (int i = 0; i < k; ++i) {
         local_factor[i] = 0.0;
         if (i == active) {
@@ -105,11 +97,8 @@ __device__ inline int composite_out_state(const CompositeModel &m, int draw_mode
             continue;
         }
         for (int j = 0; j < k; ++j) {
-            double s[3];
-            periodic_separation(locals + 3 * i, targets + 3 * j, m.system_length, s);
-            const double pair = coulomb_derivative(m, d, speed, s, local_charges[i], target_charges[j]);
-            local_factor[i] += pair;
-            target_factor[j] -= pair;
+            local_factor[i] += cross[i * k + j];
+            target_factor[j] -= cross[i * k + j];
         }
     }
     double rates[2 * kMaxCompositeUnits];
@@ -129,6 +118,47 @@ __device__ inline int composite_out_state(const CompositeModel &m, int draw_mode
     const int index = (int)selected;
     new_active = index >= local_offset && index < local_offset + k ? index - local_offset : k + (index - target_offset);
     return JFGPU_STATUS_OK;
+}
+
+// send_out_state (:152-202).  locals / targets [units][3] and their charges, sorted by identifier; active is the
+// index of the active unit among the locals; local_first tells whether the local object's identifier is the
+// smaller one (the order of the derivative table).  draws: [0] thinning random.uniform(0.0, bounding rate),
+// [1] the active unit's insert into the lifting table, [2] the ratio scheme's draw; values or unit draws as in
+// lifting_select.  new_active: -1 when thinned, else 0..units-1 (a local unit) or units..2 units-1 (a target).
+__device__ inline int composite_out_state(const CompositeModel &m, int draw_mode, const double *velocity,
+                                          const double *locals, const double *local_charges, int active,
+                                          const double *targets, const double *target_charges, int local_first,
+                                          const double *draws, int &new_active, double &bounding_rate,
+                                          double &event_rate) {
+    new_active = -1;
+    bounding_rate = 0.0;
+    event_rate = 0.0;
+    int d;
+    double speed;
+    JF_TRY(analyse_velocity(velocity, d, speed));
+    const int k = m.units;
+    const double *a = locals + 3 * active;
+    const double ca = local_charges[active];
+    double bound[kMaxCompositeUnits], pair[kMaxCompositeUnits], target_factor[kMaxCompositeUnits];
+    for (int j = 0; j < k; ++j) {
+        double s[3];
+        periodic_separation(a, targets + 3 * j, m.system_length, s);
+        bound[j] = bound_derivative(m, d, speed, s, ca, target_charges[j]);
+        pair[j] = coulomb_derivative(m, d, speed, s, ca, target_charges[j]);
+    }
+    if (!composite_thinning(m, draw_mode, bound, pair, draws, target_factor, bounding_rate, event_rate))
+        return JFGPU_STATUS_OK;
+    double cross[kMaxCompositeUnits * kMaxCompositeUnits];
+    for (int i = 0; i < k; ++i) {
+        if (i == active) continue;
+        for (int j = 0; j < k; ++j) {
+            double s[3];
+            periodic_separation(locals + 3 * i, targets + 3 * j, m.system_length, s);
+            cross[i * k + j] = coulomb_derivative(m, d, speed, s, local_charges[i], target_charges[j]);
+        }
+    }
+    return composite_lifting(m, draw_mode, active, local_first, event_rate, target_factor, cross, draws,
+                             new_active);
 }
 
 }  // namespace jf

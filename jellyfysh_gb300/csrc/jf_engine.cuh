@@ -93,5 +93,8 @@ struct LaunchPlan {
 // (merged_image_coulomb_potential.c:77-119) and the device description pointing at their device copy
 std::vector<double> fourier_table(int fc, double alpha, double length);
 MIC make_mic(int fc, int pc, double alpha, double length, const double *fourier);
+// Lennard-Jones and displaced-even-power parameters as the reference's constructors derive them
+MH make_lj(double prefactor, double sigma);
+MH make_displaced(double r0, int power, double prefactor);
 
 }  // namespace jf

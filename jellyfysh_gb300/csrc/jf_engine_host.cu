@@ -237,6 +237,12 @@ T *device_copy(JfgpuEngine *e, const std::vector<T> &host, cudaStream_t stream, 
     return static_cast<T *>(ptr);
 }
 
+
+}  // namespace
+
+namespace jf {
+
+// LennardJonesPotential.__init__ (lennard_jones_potential.py:43-61)
 MH make_lj(double prefactor, double sigma) {
     MH h;
     memset(&h, 0, sizeof(h));
@@ -250,9 +256,18 @@ MH make_lj(double prefactor, double sigma) {
     return h;
 }
 
-}  // namespace
-
-namespace jf {
+// DisplacedEvenPowerPotential.__init__ (displaced_even_power_potential.py:44-71)
+MH make_displaced(double r0, int power, double prefactor) {
+    MH h;
+    memset(&h, 0, sizeof(h));
+    h.kind = 1;
+    h.prefactor = prefactor;
+    h.r0 = r0;
+    h.r0_squared = r0 * r0;  // displaced_even_power_potential.py:68
+    h.power = (double)power;
+    h.inverse_power = 1.0 / (double)power;
+    return h;
+}
 
 // merged_image_coulomb_potential.c:77-119
 std::vector<double> fourier_table(int fc, double alpha, double length) {

@@ -139,30 +139,6 @@ static PotentialArgs base_args(int op, const double *velocity, const double *sep
     return a;
 }
 
-static MH lennard_jones(double prefactor, double sigma) {
-    MH h;
-    memset(&h, 0, sizeof(h));
-    h.kind = 0;
-    h.prefactor = prefactor;
-    h.sigma = sigma;
-    h.r0 = sigma * std::pow(2.0, 1.0 / 6.0);
-    h.r0_squared = std::pow(h.r0, 2.0);
-    h.six = ip_make(6.0, -prefactor * std::pow(sigma, 6.0));
-    h.twelve = ip_make(12.0, prefactor * std::pow(sigma, 12.0));
-    return h;
-}
-
-static MH displaced(double r0, int power, double prefactor) {
-    MH h;
-    memset(&h, 0, sizeof(h));
-    h.kind = 1;
-    h.prefactor = prefactor;
-    h.r0 = r0;
-    h.r0_squared = r0 * r0;  // displaced_even_power_potential.py:68
-    h.power = (double)power;
-    h.inverse_power = 1.0 / (double)power;
-    return h;
-}
 
 }  // namespace jf
 
@@ -203,7 +179,7 @@ int jfgpu_lennard_jones_displacement(double prefactor, double characteristic_len
                                      double *out, int32_t *status, void *stream) {
     if (!potential_change) return JFGPU_ERROR_ARGUMENT;
     PotentialArgs a = base_args(kLennardJonesDisplacement, velocity, separation, n, out, status);
-    a.mh = lennard_jones(prefactor, characteristic_length);
+    a.mh = make_lj(prefactor, characteristic_length);
     a.potential_change = potential_change;
     return launch(a, stream);
 }
@@ -212,7 +188,7 @@ int jfgpu_lennard_jones_derivative(double prefactor, double characteristic_lengt
                                    const double *separation, int64_t n, double *out, int32_t *status,
                                    void *stream) {
     PotentialArgs a = base_args(kLennardJonesDerivative, velocity, separation, n, out, status);
-    a.mh = lennard_jones(prefactor, characteristic_length);
+    a.mh = make_lj(prefactor, characteristic_length);
     return launch(a, stream);
 }
 
@@ -222,7 +198,7 @@ int jfgpu_displaced_even_power_displacement(double equilibrium_separation, int32
                                             int32_t *status, void *stream) {
     if (!potential_change || power <= 0 || power % 2) return JFGPU_ERROR_ARGUMENT;
     PotentialArgs a = base_args(kDisplacedDisplacement, velocity, separation, n, out, status);
-    a.mh = displaced(equilibrium_separation, power, prefactor);
+    a.mh = make_displaced(equilibrium_separation, power, prefactor);
     a.potential_change = potential_change;
     return launch(a, stream);
 }
@@ -232,7 +208,7 @@ int jfgpu_displaced_even_power_derivative(double equilibrium_separation, int32_t
                                           double *out, int32_t *status, void *stream) {
     if (power <= 0 || power % 2) return JFGPU_ERROR_ARGUMENT;
     PotentialArgs a = base_args(kDisplacedDerivative, velocity, separation, n, out, status);
-    a.mh = displaced(equilibrium_separation, power, prefactor);
+    a.mh = make_displaced(equilibrium_separation, power, prefactor);
     return launch(a, stream);
 }
 

@@ -1,0 +1,99 @@
+"""Batched water chains on the GPU through the C ABI against the reference's water trajectories and the oracle.
+
+Bars, as for the atomic trajectories: kind, moved unit, target, new active unit, direction and thinning outcome of
+every event exactly; event times to 1e-12 relative and committed positions to 1e-12 of the box (the device's
+merged-image Coulomb derivative, exponentials and powers agree with the reference's to about an ulp, not bit for
+bit).
+"""
+import numpy as np
+import pytest
+
+import oracle
+from tests.water_cases import FIELDS, load_water, water_names
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+REL = 1e-12
+
+
+@pytest.fixture(scope="module")
+def water():
+    from jellyfysh_gb300 import _lib, water as module
+    _lib.load()
+    return module
+
+
+def compare_logs(log, events, length):
+    assert len(log) == len(events)
+    for field in FIELDS:
+        bad = np.nonzero(log[field] != events[field])[0]
+        assert bad.size == 0, (field, int(bad[0]), log[bad[0]], events[bad[0]])
+    t_gpu = log["time_q"] + log["time_r"]
+    t_ref = events["time_q"] + events["time_r"]
+    assert np.all(np.abs(t_gpu - t_ref) <= REL * np.maximum(np.abs(t_ref), 1.0))
+    for axis in ("x", "y", "z"):
+        diff = np.abs(log[axis] - events[axis])
+        diff = np.minimum(diff, length - diff)
+        assert np.all(diff <= REL * length), (axis, float(diff.max()))
+
+
+@pytest.mark.parametrize("name", water_names())
+def test_gpu_water_reproduces_the_reference_trajectory(water, name):
+    spec, initial, charges, events, final = load_water(name)
+    model = water.WaterModel.from_spec(spec)
+    batch = water.WaterBatch(model, initial[None], seed=spec["seed"], charges=charges)
+    log = batch.run(len(events), record=True)[0]
+    batch.check_status()
+    compare_logs(log, events, model.system_length)
+    diff = np.abs(batch.positions()[0] - final)
+    assert np.all(np.minimum(diff, model.system_length - diff) <= REL * model.system_length)
+    state = batch.states()[0]
+    assert state["events"] == len(events)
+    assert state["composite_events"] == np.sum(events["kind"] == oracle.EV_COMPOSITE)
+    assert state["composite_accepted"] == np.sum((events["kind"] == oracle.EV_COMPOSITE) & (events["accepted"] == 1))
+    assert state["bond_events"] == np.sum(events["kind"] == oracle.EV_BOND)
+    assert state["lj_events"] == np.sum(events["kind"] == oracle.EV_PAIR)
+    assert state["eoc_events"] == np.sum(events["kind"] == oracle.EV_END_OF_CHAIN)
+
+
+def test_gpu_water_in_pieces_equals_one_run(water):
+    spec, initial, charges, events, final = load_water("water_n8")
+    model = water.WaterModel.from_spec(spec)
+    whole = water.WaterBatch(model, initial[None], seed=spec["seed"], charges=charges)
+    one = whole.run(600, record=True)[0]
+    parts = water.WaterBatch(model, initial[None], seed=spec["seed"], charges=charges, warps_per_block=2)
+    pieces = np.concatenate([parts.run(n, record=True)[0] for n in (1, 99, 250, 250)])
+    for field in one.dtype.names:
+        assert np.array_equal(one[field], pieces[field]), field
+    assert np.array_equal(whole.positions(), parts.positions())
+
+
+def test_batched_water_chains_match_the_oracle(water):
+    """64 chains of the 64-molecule box (lattice starts of their own, keys of their own) against the oracle."""
+    model = water.WaterModel()
+    chains, events, seed = 64, 300, 1234
+    positions = water.lattice_positions(model, chains, seed)
+    batch = water.WaterBatch(model, positions, seed=seed)
+    log = batch.run(events, record=True)
+    batch.check_status()
+    spec = dict(vars(model))
+    for c in (0, 1, 31, 63):
+        reference = oracle.Water(oracle.make_water_system(spec, oracle.chain_key(seed, c)), positions[c],
+                                 model.charges())
+        compare_logs(log[c], reference.run(events), model.system_length)
+    kinds = np.bincount(log["kind"].reshape(-1), minlength=10)
+    assert kinds[oracle.EV_COMPOSITE] > 0 and kinds[oracle.EV_BOND] > 0
+
+
+def test_water_replicas_of_the_batched_workload_run_clean(water):
+    """512 replicas of 64 molecules: every chain advances without a status, positions stay in the box."""
+    model = water.WaterModel()
+    positions = water.lattice_positions(model, 512, 99)
+    batch = water.WaterBatch(model, positions, seed=99)
+    batch.run(100)
+    batch.check_status()
+    states = batch.states()
+    assert (states["events"] == 100).all()
+    final = batch.positions()
+    assert np.isfinite(final).all() and (final >= 0).all() and (final < model.system_length).all()

@@ -37,3 +37,27 @@ def test_water_lattice_geometry():
     assert np.allclose(np.linalg.norm(wrap(s[:, 0] - s[:, 1]), axis=1), 1.0)
     assert np.allclose(np.linalg.norm(wrap(s[:, 2] - s[:, 1]), axis=1), 1.0)
     assert np.allclose(np.linalg.norm(wrap(s[:, 2] - s[:, 0]), axis=1), 1.633)
+
+
+def test_water_model_matches_the_header_layouts():
+    import ctypes
+    from jellyfysh_gb300 import _lib, water
+    assert ctypes.sizeof(_lib.WaterDesc) == 136
+    assert water.STATE_DTYPE.itemsize == 96  # JfgpuWaterState: 4 doubles, 4 int32, 6 int64
+    model = water.WaterModel.from_spec({"molecules_per_side": 2, "system_length": 6.21, "lifting": "ratio",
+                                        "unused": 1})
+    assert model.molecules == 8 and model.system_length == 6.21
+    desc = model.desc(seed=7)
+    assert (desc.molecules, desc.lifting, desc.seed, desc.initial_active) == (8, _lib.LIFTING_RATIO, 7, 1)
+    assert desc.oh_prefactor == 529.5 and desc.hh_prefactor == 342.0
+    assert model.charges().tolist()[:3] == [0.41, -0.82, 0.41]
+
+
+def test_lattice_positions_are_seeded_per_chain():
+    from jellyfysh_gb300 import water
+    model = water.WaterModel(molecules=8, system_length=6.21)
+    a = water.lattice_positions(model, 3, seed=5)
+    b = water.lattice_positions(model, 2, seed=5, rng_offset=1)
+    assert a.shape == (3, 24, 3) and np.array_equal(a[1:], b)
+    with pytest.raises(ValueError):
+        water.lattice_positions(water.WaterModel(molecules=10), 1, seed=0)
