@@ -12,6 +12,12 @@ Arms:
     default            the GPU engine (value = device-timed events/s; e2e = through ChainBatch with host buffers)
     --impl reference   the CPU oracle (a C restatement of the reference's event loop) on all host threads
 
+Second workload (``--workload water``, a parity configuration measured beside the headline, not the headline):
+    512 independent chains of 64 flexible water molecules (12.42 A box, 300 K, O-H and H-H harmonic bonds,
+    Lennard-Jones on oxygen, merged-image Coulomb between molecules with the summed inverse-power Coulomb bound and
+    inside-first lifting), FP64 (thinning screened in FP32 with an error bound), one block per chain; seeded lattices
+    of molecules in random orientations.
+
 Multi-GPU: one process per GPU under torchrun; every rank runs its own 4096 chains (independent replicas, no
 collective on the data path), value = all ranks' events / max-over-ranks time.
 """
@@ -33,6 +39,8 @@ METRIC = "events/s on 1 GB300, batched mixed-precision vs plain FP64 at <=1e-9 r
 WORKLOAD = dict(workload="lennard_jones_chains_4096x1024_cell_bounding", chains=4096, n=1024, density=0.8,
                 beta=1.0 / 1.2, cells_per_side=12, neighbor_layers=3, chain_time=2.0, far="cell_bounding",
                 jitter=0.05, estimator_points=10, estimator_prefactor=1.5)
+WATER_WORKLOAD = dict(workload="water_chains_512x64_molecular_coulomb", chains=512, molecules=64,
+                      system_length=12.42, temperature_kelvin=300.0, chain_time=2.0, lifting="inside_first")
 NEAR_CELLS = (2 * WORKLOAD["neighbor_layers"] + 1) ** 3  # cells scanned for pair candidates per event
 CPU_SECONDS = 10.0  # wall time of the CPU baseline sample
 TIMING_STRIDE = 16  # event rounds between two rounds bracketed by per-kernel CUDA events
@@ -54,7 +62,13 @@ def parse():
     p.add_argument("--groups", type=int, default=1, help="chain groups on streams of their own (0 = autotune)")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-fp64", action="store_true")
-    return p.parse_args()
+    p.add_argument("--workload", default="lennard_jones", choices=["lennard_jones", "water"])
+    args = p.parse_args()
+    if args.workload == "water" and "--chains" not in sys.argv:
+        args.chains = WATER_WORKLOAD["chains"]
+    if args.workload == "water" and "--events" not in sys.argv:
+        args.events = 32
+    return args
 
 
 def make_workload(chains, seed_offset=0):
@@ -386,9 +400,161 @@ def gpu_arm(args):
     batch.close()
 
 
+def water_model_and_positions(chains, seed):
+    from jellyfysh_gb300 import water
+    model = water.WaterModel(molecules=WATER_WORKLOAD["molecules"], system_length=WATER_WORKLOAD["system_length"],
+                             chain_time=WATER_WORKLOAD["chain_time"], lifting=WATER_WORKLOAD["lifting"])
+    return model, water.lattice_positions(model, chains, seed)
+
+
+def water_cpu_chains(threads, pool, seed=99):
+    """One oracle water chain of the water workload per host thread."""
+    import oracle
+    model, positions = water_model_and_positions(threads, seed)
+    spec = dict(vars(model))
+    return list(pool.map(lambda c: oracle.Water(oracle.make_water_system(spec, oracle.chain_key(seed, c)),
+                                                positions[c], model.charges()), range(threads)))
+
+
+def water_gpu_arm(args):
+    """events/s of the water workload: device-timed, and end to end with host buffers."""
+    import torch
+    from jellyfysh_gb300 import replicas, water
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    device = torch.device("cuda", local)
+    model, positions = water_model_and_positions(args.chains, 1000 + rank)
+    batch = water.WaterBatch(model, positions, seed=1000 + rank, first_chain=0)
+    stream = torch.cuda.current_stream(device)
+    for _ in range(args.warmup):
+        batch.run(args.events)
+    batch.check_status()
+    before = batch.states()
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize(device)
+    with ClockSampler(local) as clocks:
+        begin = torch.cuda.Event(enable_timing=True)
+        finish = torch.cuda.Event(enable_timing=True)
+        begin.record(stream)
+        for _ in range(args.steps):
+            batch.run(args.events)
+        finish.record(stream)
+        torch.cuda.synchronize(device)
+    elapsed_ms = begin.elapsed_time(finish)
+    batch.check_status()
+    after = batch.states()
+    events_done = int(after["events"].sum() - before["events"].sum())
+    _, total_ms, value = replicas.timed_throughput(events_done, elapsed_ms, device)
+    # end to end: H2D of positions and chain states from pinned host memory, the run, D2H of both
+    host_in = [batch.positions_dev.cpu().pin_memory(), batch.state_dev.cpu().pin_memory()]
+    host_out = [t.clone().pin_memory() for t in host_in]
+    h2d = sum(t.numel() * t.element_size() for t in host_in)
+    e2e_steps = max(2, args.steps // 2)
+    torch.cuda.synchronize(device)
+    e_begin = torch.cuda.Event(enable_timing=True)
+    e_end = torch.cuda.Event(enable_timing=True)
+    e_begin.record(stream)
+    for _ in range(e2e_steps):
+        batch.positions_dev.copy_(host_in[0], non_blocking=True)
+        batch.state_dev.copy_(host_in[1], non_blocking=True)
+        batch.run(args.events)
+        host_out[0].copy_(batch.positions_dev, non_blocking=True)
+        host_out[1].copy_(batch.state_dev, non_blocking=True)
+    e_end.record(stream)
+    torch.cuda.synchronize(device)
+    e2e_value = e2e_steps * args.chains * args.events / (e_begin.elapsed_time(e_end) / 1000.0)
+    if rank != 0:
+        if world > 1:
+            dist.barrier()
+            dist.destroy_process_group()
+        return
+    counts = {key: int(after[key].sum() - before[key].sum())
+              for key in ("composite_events", "composite_accepted", "bond_events", "lj_events", "eoc_events",
+                          "thinning_exact", "refined_items")}
+    # algorithmic bytes per event: every unit's position and charge read once (the candidates of all molecule
+    # pairs), the active unit's position written, the chain state read and written
+    units = 3 * model.molecules
+    bytes_per_event = units * (24 + 8) + 24 + 2 * 96
+    step_s = elapsed_ms / args.steps / 1000.0
+    achieved = bytes_per_event * args.chains * args.events / step_s / 1e9
+    peak, peak_kind = measured_peaks()
+    cpu = None
+    if not args.no_cpu_baseline and world == 1:
+        import concurrent.futures
+        threads = host_threads()
+        with concurrent.futures.ThreadPoolExecutor(max_workers=threads) as pool:
+            chains = water_cpu_chains(threads, pool)
+            cpu_run(pool, chains, 0.5)
+            done, seconds = cpu_run(pool, chains, CPU_SECONDS)
+        cpu = {"value": done / seconds, "unit": "events/s", "cores": threads, "kind": "port",
+               "per_core": done / seconds / threads,
+               "sample": "%d water chains (one per host thread), %d events in %.1f s" % (threads, done, seconds)}
+    config = dict(WATER_WORKLOAD)
+    config.update(chains=args.chains, events_per_chain_per_step=args.events,
+                  l2="working set %.1f MB (in L2): the step is FP64-latency-bound, not HBM-bound" % (
+                      (batch.positions_dev.numel() * 8 + batch.state_dev.numel()) / 1e6),
+                  event_counts=counts, parallelism="replicas" if world > 1 else "single GPU")
+    line = {"metric": "events/s on 1 GB300, batched FP64 water chains", "value": value, "unit": "events/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic: seeded lattices of water molecules in random orientations", "config": config,
+            "e2e": {"value": e2e_value, "unit": "events/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": h2d},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": None, "peak_source": peak_kind,
+                         "kernel": "jf::water_kernel", "bytes_per_event": bytes_per_event},
+            "cpu_baseline": cpu, "gpu_launches": args.steps, "clocks": clocks.summary()}
+    print(json.dumps(line))
+    if world > 1:
+        dist.barrier()
+        dist.destroy_process_group()
+    batch.close()
+
+
+def water_reference_arm(args):
+    """The oracle's water loop on all host threads, one chain per thread, bounded time samples."""
+    import concurrent.futures
+    if int(os.environ.get("RANK", "0")) != 0:
+        return
+    threads = host_threads()
+    seconds = max(0.2, min(3.0, 90.0 / max(args.steps, 1)))
+    with concurrent.futures.ThreadPoolExecutor(max_workers=threads) as pool:
+        chains = water_cpu_chains(threads, pool)
+        for _ in range(args.warmup):
+            cpu_run(pool, chains, 0.5)
+        total_events, total_time = 0, 0.0
+        for _ in range(args.steps):
+            done, elapsed = cpu_run(pool, chains, seconds)
+            total_events += done
+            total_time += elapsed
+    value = total_events / total_time
+    config = dict(WATER_WORKLOAD)
+    config["sample"] = "%d water chains (one per host thread) x %.0f s of events per step" % (threads, seconds)
+    print(json.dumps({"impl": "reference", "metric": "events/s on 1 GB300, batched FP64 water chains",
+                      "value": value, "unit": "events/s", "n_gpus": args.gpus, "steps": args.steps,
+                      "warmup": args.warmup, "ms_per_step": 1000.0 * total_time / args.steps,
+                      "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                      "data": "synthetic: seeded lattices of water molecules in random orientations",
+                      "config": config,
+                      "cpu_baseline": {"value": value, "unit": "events/s", "cores": threads, "kind": "port",
+                                       "per_core": value / threads, "sample": config["sample"]},
+                      "e2e": {"value": value, "unit": "events/s", "h2d_bytes_per_step": 0,
+                              "d2h_bytes_per_step": 0}}))
+
+
 def main():
     args = parse()
-    if args.impl == "reference":
+    if args.workload == "water":
+        if args.impl == "reference":
+            water_reference_arm(args)
+        else:
+            water_gpu_arm(args)
+    elif args.impl == "reference":
         reference_arm(args)
     else:
         gpu_arm(args)

@@ -269,7 +269,7 @@ typedef struct {
  * molecule m) with harmonic O-H and H-H bonds (DisplacedEvenPowerPotential, power 2), Lennard-Jones between the
  * oxygens and one Coulomb factor per pair of molecules (the composite-object event above, inside-first,
  * outside-first or ratio lifting), for every pair of molecules, and the periodic-direction end of chain.  One
- * warp advances one chain, in FP64 with the reference's arithmetic.  Replaces the reference's event loop
+ * block advances one chain, in FP64 with the reference's arithmetic.  Replaces the reference's event loop
  * (mediator/single_process_mediator.py:91-156) over the handlers of these factors:
  * two_leaf_unit_event_handler.py:98-154, two_composite_object_summed_bounding_potential_event_handler.py:119-202,
  * single_independent_active_periodic_direction_end_of_chain_event_handler.py:151-237.
@@ -281,6 +281,12 @@ typedef struct {
     int32_t position_cutoff;
     int32_t initial_active;       /* unit index */
     int32_t initial_direction;
+    int32_t mode;                 /* JFGPU_MODE_EXACT: every candidate and merged-image sum in FP64;
+                                     JFGPU_MODE_MIXED: the Coulomb candidates are screened in FP32 with error bounds
+                                     and only those that may come first are solved in FP64, and the thinning of a
+                                     Coulomb event rejects on FP32 sums with an error bound when the bound decides,
+                                     else takes the FP64 sums (the same outcomes as the exact mode) */
+    int32_t reserved;
     double system_length;
     double beta;
     double chain_time;
@@ -299,6 +305,8 @@ typedef struct {
     int32_t active, direction, eoc_new_active, status;
     int64_t events;               /* committed events: the event index of the keyed draws */
     int64_t composite_events, composite_accepted, bond_events, lj_events, eoc_events;
+    int64_t thinning_exact;       /* Coulomb events whose thinning took the FP64 sums (all of them in exact mode) */
+    int64_t refined_items;        /* candidate items solved in FP64 (every item in exact mode) */
 } JfgpuWaterState;
 
 /* the model on the current device (the Fourier table of the Coulomb factor) */
@@ -308,7 +316,8 @@ void jfgpu_water_destroy(void *water);
  * of chain (time chain_time, new active unit drawn for event 0) */
 int jfgpu_water_init(void *water, JfgpuWaterState *state, int64_t chains, int64_t first_chain, void *stream);
 /* `events` events of every chain.  positions [chains][3 molecules][3] and charges [3 molecules] are device arrays;
- * log [chains][events] (may be null) receives every committed event; warps_per_block 1..8 (0: 1). */
+ * log [chains][events] (may be null) receives every committed event.  One block of warps_per_block warps runs one
+ * chain, 1..8 (0: 4). */
 int jfgpu_water_run(void *water, double *positions, const double *charges, JfgpuWaterState *state, int64_t chains,
                     int64_t first_chain, int64_t events, JfgpuEvent *log, int32_t warps_per_block, void *stream);
 

@@ -51,7 +51,8 @@ class WaterDesc(ctypes.Structure):
     """JfgpuWaterDesc."""
     _fields_ = [("molecules", ctypes.c_int32), ("lifting", ctypes.c_int32), ("fourier_cutoff", ctypes.c_int32),
                 ("position_cutoff", ctypes.c_int32), ("initial_active", ctypes.c_int32),
-                ("initial_direction", ctypes.c_int32), ("system_length", ctypes.c_double), ("beta", ctypes.c_double),
+                ("initial_direction", ctypes.c_int32), ("mode", ctypes.c_int32), ("reserved", ctypes.c_int32),
+                ("system_length", ctypes.c_double), ("beta", ctypes.c_double),
                 ("chain_time", ctypes.c_double), ("speed", ctypes.c_double), ("oh_r0", ctypes.c_double),
                 ("oh_prefactor", ctypes.c_double), ("hh_r0", ctypes.c_double), ("hh_prefactor", ctypes.c_double),
                 ("lj_prefactor", ctypes.c_double), ("lj_sigma", ctypes.c_double),

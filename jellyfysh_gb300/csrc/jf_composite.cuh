@@ -23,7 +23,135 @@ struct CompositeModel {
     double system_length;
     int units;                // leaf units per composite object
     int lifting;              // JFGPU_LIFTING_*
+    // the terms of the merged-image sum in lists, for a warp that shares one evaluation (mic_x_warp): the
+    // real-space images (i, j, k) and the Fourier rows (i, j, last k) of the reference's loops
+    const int4 *images = nullptr;
+    const int4 *rows = nullptr;
+    int n_images = 0, n_rows = 0;
+    // FP32 copies of the merged-image constants and Fourier table, for the screened thinning (mic_x_warp32)
+    const float *fourier32 = nullptr;
+    float alpha_over_length32 = 0.f, alpha_over_length_sq32 = 0.f, two_alpha_over_length_root_pi32 = 0.f;
+    float system_length32 = 0.f, two_pi_over_length32 = 0.f;
 };
+
+// mic_x_warp in FP32 with an absolute error bound, for decisions that need the sum only to within that bound.
+// The bound covers the rounding of the separation to FP32 and the FP32 evaluation: an image term x (c exp(-a^2 r^2)
+// + erfc(a r) / r) / r^2 within 4096 ulp of its magnitude (the argument errors of exp and erfc grow with a^2 r^2,
+// at most about 75 here, times the documented 2-4 ulp of expf and erfcf), a Fourier term within 512 ulp of its
+// coefficient (the recurrences of sin and cos over at most 18 steps from angles known to 2 ulp), and the additions.
+static __device__ __noinline__ void mic_x_warp32(const CompositeModel &c, float sx, float sy, float sz, int lane,
+                                                 float &value, float &error) {
+    const int n = c.mic.fourier_cutoff + 1;
+    const float length = c.system_length32;
+    float derivative = 0.f, image_magnitude = 0.f, fourier_magnitude = 0.f;
+    for (int e = lane; e < c.n_images; e += 32) {
+        const int4 image = c.images[e];
+        const float vz = sz + (float)image.z * length, vy = sy + (float)image.y * length;
+        const float vector_x = sx + (float)image.x * length;
+        const float vector_sq = vector_x * vector_x + vy * vy + vz * vz;
+        const float vector_norm = sqrtf(vector_sq);
+        const float term = vector_x *
+                           (c.two_alpha_over_length_root_pi32 * expf(-c.alpha_over_length_sq32 * vector_sq) +
+                            erfcf(c.alpha_over_length32 * vector_norm) / vector_norm) /
+                           vector_sq;
+        derivative += term;
+        image_magnitude += fabsf(term);
+    }
+    if (c.n_rows > 0 && 31 - lane < c.n_rows) {
+        float delta_sin_x, delta_cos_x, delta_sin_y, delta_cos_y, delta_sin_z, delta_cos_z;
+        sincosf(c.two_pi_over_length32 * sx, &delta_sin_x, &delta_cos_x);
+        sincosf(c.two_pi_over_length32 * sy, &delta_sin_y, &delta_cos_y);
+        sincosf(c.two_pi_over_length32 * sz, &delta_sin_z, &delta_cos_z);
+        for (int e = 31 - lane; e < c.n_rows; e += 32) {
+            const int4 row = c.rows[e];
+            float cos_x = delta_cos_x, sin_x = delta_sin_x, store;
+            for (int i = 1; i < row.x; ++i) {
+                store = cos_x;
+                cos_x = store * delta_cos_x - sin_x * delta_sin_x;
+                sin_x = sin_x * delta_cos_x + store * delta_sin_x;
+            }
+            float cos_y = 1.f, sin_y = 0.f;
+            for (int j = 0; j < row.y; ++j) {
+                store = cos_y;
+                cos_y = store * delta_cos_y - sin_y * delta_sin_y;
+                sin_y = sin_y * delta_cos_y + store * delta_sin_y;
+            }
+            float cos_z = 1.f, sin_z = 0.f;
+            for (int k = 0; k < row.z + 1; ++k) {
+                const float coefficient = c.fourier32[(row.x * n + row.y) * n + k];
+                derivative += coefficient * sin_x * cos_y * cos_z;
+                fourier_magnitude += fabsf(coefficient);
+                store = cos_z;
+                cos_z = store * delta_cos_z - sin_z * delta_sin_z;
+                sin_z = sin_z * delta_cos_z + store * delta_sin_z;
+            }
+        }
+    }
+    for (int offset = 16; offset > 0; offset >>= 1) {
+        derivative += __shfl_xor_sync(0xffffffffu, derivative, offset);
+        image_magnitude += __shfl_xor_sync(0xffffffffu, image_magnitude, offset);
+        fourier_magnitude += __shfl_xor_sync(0xffffffffu, fourier_magnitude, offset);
+    }
+    value = derivative;
+    const float ulp = 5.9604645e-8f;  // 2^-24
+    error = ulp * (4096.f * image_magnitude + 512.f * fourier_magnitude) + fabsf(derivative) * (16.f * ulp);
+}
+
+// The x-derivative of the merged-image sum (mic_x) shared by the 32 lanes of a warp: lane l takes the real-space
+// images l, l + 32, ... and the Fourier rows (i, j) 31 - l, 63 - l, ...; each term is computed with the reference's
+// arithmetic (the cos/sin recurrences rebuilt up to the lane's row), so every term equals mic_x's, and the lanes'
+// sums are added by a butterfly that leaves the same total in every lane.  Only the order of the additions differs
+// from mic_x's (a rounding of the sum, about 1e-16 relative).  Every lane of the warp must call it with the same
+// separation.
+static __device__ __noinline__ double mic_x_warp(const CompositeModel &c, double sx, double sy, double sz, int lane) {
+    const MIC &m = c.mic;
+    const int n = m.fourier_cutoff + 1;
+    double derivative = 0.0;
+    for (int e = lane; e < c.n_images; e += 32) {
+        const int4 image = c.images[e];
+        const double vector_z_sq = (sz + image.z * m.system_length) * (sz + image.z * m.system_length);
+        const double vector_y_sq = (sy + image.y * m.system_length) * (sy + image.y * m.system_length);
+        const double vector_x = sx + image.x * m.system_length;
+        const double vector_sq = vector_x * vector_x + vector_y_sq + vector_z_sq;
+        const double vector_norm = sqrt(vector_sq);
+        derivative += vector_x *
+                      (m.two_alpha_over_length_root_pi * exp(-m.alpha_over_length_sq * vector_sq) +
+                       erfc(m.alpha_over_length * vector_norm) / vector_norm) /
+                      vector_sq;
+    }
+    if (c.n_rows > 0 && 31 - lane < c.n_rows) {
+        const double delta_cos_x = cos(m.two_pi_over_length * sx);
+        const double delta_sin_x = sin(m.two_pi_over_length * sx);
+        const double delta_cos_y = cos(m.two_pi_over_length * sy);
+        const double delta_sin_y = sin(m.two_pi_over_length * sy);
+        const double delta_cos_z = cos(m.two_pi_over_length * sz);
+        const double delta_sin_z = sin(m.two_pi_over_length * sz);
+        for (int e = 31 - lane; e < c.n_rows; e += 32) {
+            const int4 row = c.rows[e];  // (i, j, last k, unused)
+            double cos_x = delta_cos_x, sin_x = delta_sin_x, store;
+            for (int i = 1; i < row.x; ++i) {
+                store = cos_x;
+                cos_x = store * delta_cos_x - sin_x * delta_sin_x;
+                sin_x = sin_x * delta_cos_x + store * delta_sin_x;
+            }
+            double cos_y = 1.0, sin_y = 0.0;
+            for (int j = 0; j < row.y; ++j) {
+                store = cos_y;
+                cos_y = store * delta_cos_y - sin_y * delta_sin_y;
+                sin_y = sin_y * delta_cos_y + store * delta_sin_y;
+            }
+            double cos_z = 1.0, sin_z = 0.0;
+            for (int k = 0; k < row.z + 1; ++k) {
+                derivative += m.fourier[(row.x * n + row.y) * n + k] * sin_x * cos_y * cos_z;
+                store = cos_z;
+                cos_z = store * delta_cos_z - sin_z * delta_sin_z;
+                sin_z = sin_z * delta_cos_z + store * delta_sin_z;
+            }
+        }
+    }
+    for (int offset = 16; offset > 0; offset >>= 1) derivative += __shfl_xor_sync(0xffffffffu, derivative, offset);
+    return derivative;
+}
 
 // HypercubicPeriodicBoundaries.separation_vector (setting/hypercubic_setting.py:120-140, :156-172)
 __device__ inline void periodic_separation(const double *from, const double *to, double length, double *s) {
@@ -43,6 +171,99 @@ __device__ inline double bound_derivative(const CompositeModel &m, int d, double
 __device__ inline double coulomb_derivative(const CompositeModel &m, int d, double speed, const double *s, double c1,
                                             double c2) {
     return mic_std_derivative(m.mic, m.coulomb_prefactor, d, s, c1, c2) * speed;
+}
+
+// coulomb_derivative with the merged-image sum shared by the warp (mic_x_warp); every lane gets the value
+__device__ inline double coulomb_derivative_warp(const CompositeModel &m, int d, double speed, const double *s,
+                                                 double c1, double c2, int lane) {
+    double p[3];
+    permute3(s, d, p);
+    return m.coulomb_prefactor * c1 * c2 * mic_x_warp(m, p[0], p[1], p[2], lane) * speed;
+}
+
+// ipcb_x_displacement in FP32, to screen candidates: the same steps (inverse_power_coulomb_bounding_potential.c:
+// 85-139) on FP32 inputs, with a first-order bound `error` on the absolute difference from the exact value.  Each
+// step's relative error is counted in units of 2^-24 (inputs rounded from FP64, correctly rounded +, -, *, / and
+// sqrtf) and carried through the differences and the square root; du_error is the bound on du.  `unsafe` is set
+// where the first-order bound does not hold or the case is rare enough to leave to FP64: a whole box or more of
+// potential change, a branch decided within the bounds, a radicand within four bounds of zero, a non-finite value.
+__device__ inline float ipcb_x_displacement32(float pp, float sx, float sy, float sz, float du, float du_error,
+                                              float length, float &error, bool &unsafe) {
+    const float u = 0x1p-24f;
+    const float half = 0.5f * length;
+    const float perp = sy * sy + sz * sz;                           // 4u
+    float current = pp / sqrtf(sx * sx + perp);                     // 8u
+    const float u_zero = pp / sqrtf(perp);                          // 7u
+    const float u_half = pp / sqrtf(half * half + perp);            // 8u
+    const float per_length = fabsf(u_zero - u_half);
+    if (!(du < 0.9f * per_length)) unsafe = true;                   // whole boxes of potential change
+    float current_error = 8.f * u * fabsf(current);
+    float shift = 0.f, shift_error = 0.f;  // displacement before the final solve
+    float x = sx, x_error = u * fabsf(sx);
+    float sign = pp > 0.f ? -1.f : 1.f;     // displacement += x -/+ sqrt(...)
+    if (pp > 0.f) {
+        if (sx <= 0.f) {
+            shift = half + sx;
+            shift_error = u * (half + fabsf(sx)) + u * fabsf(shift);
+            x = half;
+            x_error = 0.f;
+            current = u_half;
+            current_error = 8.f * u * fabsf(u_half);
+        } else {
+            const float rise = u_zero - current;
+            const float rise_error = 7.f * u * fabsf(u_zero) + current_error + u * fabsf(rise);
+            if (fabsf(du - rise) <= 2.f * (rise_error + du_error)) unsafe = true;
+            if (du >= rise) {
+                du = du - rise;
+                du_error += rise_error + u * fabsf(du);
+                shift = sx + half;
+                shift_error = u * fabsf(sx) + u * fabsf(shift);
+                x = half;
+                x_error = 0.f;
+                current = u_half;
+                current_error = 8.f * u * fabsf(u_half);
+            }
+        }
+    } else {
+        if (sx > 0.f) {
+            shift = sx;
+            shift_error = u * fabsf(sx);
+            x = 0.f;
+            x_error = 0.f;
+            current = u_zero;
+            current_error = 7.f * u * fabsf(u_zero);
+        } else {
+            const float rise = u_half - current;
+            const float rise_error = 8.f * u * fabsf(u_half) + current_error + u * fabsf(rise);
+            if (fabsf(du - rise) <= 2.f * (rise_error + du_error)) unsafe = true;
+            if (du >= rise) {
+                du = du - rise;
+                du_error += rise_error + u * fabsf(du);
+                shift = sx + length;
+                shift_error = u * fabsf(sx) + u * fabsf(shift);
+                x = 0.f;
+                x_error = 0.f;
+                current = u_zero;
+                current_error = 7.f * u * fabsf(u_zero);
+            }
+        }
+    }
+    const float denominator = current + du;
+    const float denominator_error = current_error + du_error + u * fabsf(denominator);
+    if (!(fabsf(denominator) > 4.f * denominator_error)) unsafe = true;
+    const float new_norm = pp / denominator;
+    const float new_norm_relative = denominator_error / fabsf(denominator) + 2.f * u;
+    const float radicand = new_norm * new_norm - perp;
+    const float radicand_error = (2.f * new_norm_relative + u) * new_norm * new_norm + 4.f * u * perp +
+                                 u * fabsf(radicand);
+    if (!(radicand > 4.f * radicand_error)) unsafe = true;
+    const float root = sqrtf(fmaxf(radicand, 0.f));
+    const float root_error = radicand_error / (2.f * fmaxf(root, 1e-30f)) + u * root;
+    const float tail = x + sign * root;
+    const float value = shift + tail;
+    error = 2.f * (shift_error + x_error + root_error + u * fabsf(tail) + u * fabsf(value)) + u * length;
+    if (!isfinite(value) || !isfinite(error)) unsafe = true;
+    return value;
 }
 
 // send_event_time (:119-150): min over the target units of the bounding displacement (Python's min keeps the first

@@ -1,12 +1,14 @@
-// jf_water.cu -- batched chains of flexible water: one warp per chain, the event loop on the device.
+// jf_water.cu -- batched chains of flexible water: one block per chain, the event loop on the device.
 //
-// Per event the lanes share the candidates of the active unit: every lane takes the other molecules lane,
-// lane + 32, ... (the Coulomb factor of the two molecules: three bounded displacements; Lennard-Jones when the active
-// unit is an oxygen), lanes 0-2 the bonds within the active molecule; a warp argmin over (time, kind, target) picks
-// the event.  The out-state of a Coulomb event needs up to nine merged-image Coulomb derivatives: lanes 0-2 take the
-// active unit against the three target units, lanes 3-8 the other two local units against them, all at once; every
-// lane then runs the same thinning and lifting arithmetic (jf_composite.cuh) on the gathered values.  FP64 with the
-// reference's arithmetic throughout; the random numbers are the keyed draws of (chain, event, kind, target).
+// Per event the threads share the candidate items of the active unit: the bounded displacement against every unit
+// of every other molecule (the Coulomb factors), Lennard-Jones against every other oxygen when the active unit is an
+// oxygen, the two bonds within the molecule; a block argmin over (time, kind, target) picks the event.  The
+// out-state of a Coulomb event needs three merged-image Coulomb derivatives for the thinning and six more for the
+// lifting; each is shared by one warp (mic_x_warp: the images and Fourier rows of the sum spread over the lanes), the
+// warps take different ones, and thread 0 runs the thinning and lifting arithmetic (jf_composite.cuh).  FP64 with
+// the reference's arithmetic throughout (the merged-image sums in another order of additions); in the mixed mode the
+// thinning first tries FP32 sums with an error bound.  The random numbers are the keyed draws of (chain, event,
+// kind, target).
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -15,6 +17,7 @@
 
 #include "jf_composite.cuh"
 #include "jf_engine.cuh"
+#include "jf_screen.cuh"
 
 namespace jf {
 
@@ -22,7 +25,10 @@ struct WaterModel {
     CompositeModel coulomb;  // units 3
     MH oh, hh, lj;
     double beta, chain_time, speed, length;
-    int molecules, initial_active, initial_direction;
+    float beta32, speed32, length32;
+    LJ32 lj32;            // the Lennard-Jones constants of the FP32 screen
+    float margin32;       // rounding scale of FP32 separations, 16 L 2^-24
+    int molecules, initial_active, initial_direction, mode;
     uint64_t seed;
 };
 
@@ -65,8 +71,6 @@ __device__ inline int water_new_active(const WaterModel &w, uint64_t key, uint64
 
 constexpr unsigned kFull = 0xffffffffu;
 
-__device__ inline double shfl_double(double v, int lane) { return __shfl_sync(kFull, v, lane); }
-
 __global__ void water_init_kernel(WaterModel w, JfgpuWaterState *state, int64_t chains, int64_t first_chain) {
     const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= chains) return;
@@ -80,21 +84,179 @@ __global__ void water_init_kernel(WaterModel w, JfgpuWaterState *state, int64_t 
     state[c] = s;
 }
 
+constexpr int kMaxWarps = 8;
+
+// candidate items of an event at most: Coulomb items in three warp-padded groups, Lennard-Jones, two bonds
+__host__ __device__ inline int water_items_max(int molecules) {
+    return 3 * (((molecules - 1) + 31) & ~31) + (molecules - 1) + 2;
+}
+
+__host__ inline size_t water_shared_bytes(int molecules) {
+    const int items = water_items_max(molecules);
+    return (size_t)items * sizeof(double) + (size_t)items * sizeof(int);
+}
+
+// one candidate item of the event: the bounded displacement of the active unit against one unit of another molecule
+// (the Coulomb factor of the two molecules takes the smallest over the three), Lennard-Jones against another oxygen,
+// or a bond within the molecule.  Returns a status; the candidate is offered to best.
+__device__ inline int water_item(const WaterModel &w, const double *pos, const double *charge, uint64_t key,
+                                 uint64_t ev, int item, int m, int t, int d, const double *pa, double ca, double ts_q,
+                                 double ts_r, WaterCand &best) {
+    const int M = w.molecules;
+    // Coulomb items grouped by target unit type (hydrogen, oxygen, hydrogen), each group padded to whole warps, so
+    // that a warp solves displacements of one charge sign (one branch of the inversion)
+    const int group = ((M - 1) + 31) & ~31;
+    const int n_coulomb = 3 * group, n_lj = t == 1 ? M - 1 : 0;
+    double sep[3];
+    if (item < n_coulomb) {
+        const int j = item / group;
+        int other = item % group;
+        if (other >= M - 1) return JFGPU_STATUS_OK;  // padding
+        other += other >= m;
+        const int b = 3 * other + j;
+        const double du = expovariate(draw(key, ev, kRngComposite, (uint32_t)b), w.beta);
+        periodic_separation(pa, pos + 3 * b, w.length, sep);
+        double p[3];
+        permute3(sep, d, p);
+        const double value = ipcb_x_displacement(w.coulomb.bound_prefactor * ca * charge[b], p[0], p[1], p[2], du,
+                                                 w.length) / w.speed;
+        // the factor's candidate is the smallest of its three displacements; as time_add does not decrease with the
+        // displacement, the smallest of the three times is the same time
+        water_offer(best, ts_q, ts_r, value, JFGPU_EV_COMPOSITE, other);
+        return JFGPU_STATUS_OK;
+    }
+    item -= n_coulomb;
+    int b, kind;
+    const MH *h;
+    if (item < n_lj) {
+        const int other = item + (item >= m);
+        b = 3 * other + 1;
+        h = &w.lj;
+        kind = JFGPU_EV_PAIR;
+    } else {
+        const int u = (item - n_lj) + ((item - n_lj) >= t);  // the two other units of the molecule
+        b = 3 * m + u;
+        h = (t == 1 || u == 1) ? &w.oh : &w.hh;
+        kind = JFGPU_EV_BOND;
+    }
+    periodic_separation(pa, pos + 3 * b, w.length, sep);
+    const double du = expovariate(draw(key, ev, kRngPair, (uint32_t)b), w.beta);
+    double value;
+    JF_TRY(mh_std_displacement(*h, d, sep, du, value));
+    water_offer(best, ts_q, ts_r, value / w.speed, kind, b);
+    return JFGPU_STATUS_OK;
+}
+
+// FP32 screen of a candidate item: the Coulomb items solve the bound's inversion in FP32 with an error bound
+// (ipcb_x_displacement32); the Lennard-Jones and bond items are always left to FP64 (unsafe).  time and error are
+// displacements over the speed.
+__device__ inline void water_screen(const WaterModel &w, const double *pos, const double *charge, uint64_t key,
+                                   uint64_t ev, int item, int m, int t, int d, const double *pa, double ca,
+                                   float &time, float &error, bool &unsafe) {
+    const int M = w.molecules;
+    const int group = ((M - 1) + 31) & ~31;
+    unsafe = false;
+    time = 0.f;
+    error = 0.f;
+    if (item >= 3 * group + (t == 1 ? M - 1 : 0)) {  // bonds: FP64
+        unsafe = true;
+        return;
+    }
+    if (item >= 3 * group) {
+        // Lennard-Jones against another oxygen (only listed when the active unit is an oxygen): the FP32 screen
+        // of the atomic engine, within 2^-13 relative plus its absolute margin unless flagged
+        int other = item - 3 * group;
+        other += other >= m;
+        const int b = 3 * other + 1;
+        bool flag = false;
+        const float du = expovariate32(draw(key, ev, kRngPair, (uint32_t)b), 1.0f / w.beta32, flag);
+        double sep64[3];
+        periodic_separation(pa, pos + 3 * b, w.length, sep64);
+        float sep[3] = {(float)sep64[0], (float)sep64[1], (float)sep64[2]};
+        int path;
+        time = lj_screen(w.lj32, d, w.speed32, sep, du, w.margin32, flag, path);
+        error = 0x1p-11f * fabsf(time) + w.length32 * 0x1p-17f / w.speed32;
+        unsafe = flag || isinf(time);
+        if (isinf(time) && !flag) {  // no event from this pair (U + du stays below zero): not a candidate
+            unsafe = false;
+            time = INFINITY;
+            error = 0.f;
+        }
+        return;
+    }
+    const int j = item / group;
+    int other = item % group;
+    if (other >= M - 1) {
+        time = INFINITY;  // padding
+        return;
+    }
+    other += other >= m;
+    const int b = 3 * other + j;
+    const uint64_t bits = draw(key, ev, kRngComposite, (uint32_t)b);
+    // the uniform to within 2^-24 relative, -log(1 - u) with log1pf (conditioning grows near u = 1: left to FP64)
+    const float uniform = (float)(uint32_t)(bits >> 40) * 0x1p-24f;
+    if (uniform > 1.f - 0x1p-6f) {
+        unsafe = true;
+        return;
+    }
+    const float du = -log1pf(-uniform) / w.beta32;
+    // relative error of log1pf, the division and the conditioning below u = 1 - 2^-6, plus the truncation of the
+    // uniform to 24 bits (an absolute 2^-24 in u, 2^-24 / (1 - u) / beta in du)
+    const float du_error = 24.f * 0x1p-24f * du + 2.f * 0x1p-24f / ((1.f - uniform) * w.beta32);
+    double sep[3], p[3];
+    periodic_separation(pa, pos + 3 * b, w.length, sep);
+    permute3(sep, d, p);
+    float value_error;
+    const float value = ipcb_x_displacement32((float)(w.coulomb.bound_prefactor * ca * charge[b]), (float)p[0],
+                                              (float)p[1], (float)p[2], du, du_error, w.length32, value_error,
+                                              unsafe);
+    time = value / w.speed32;
+    error = value_error / w.speed32 + 0x1p-23f * fabsf(time);
+}
+
+__device__ inline void shuffle_better(WaterCand &best, int offset) {
+    WaterCand o;
+    o.q = __shfl_xor_sync(kFull, best.q, offset);
+    o.r = __shfl_xor_sync(kFull, best.r, offset);
+    o.kind = __shfl_xor_sync(kFull, best.kind, offset);
+    o.target = __shfl_xor_sync(kFull, best.target, offset);
+    if (water_better(o, best)) best = o;
+}
+
+// One block of `warps` warps advances one chain.  Candidate items are spread over all threads; the argmin goes
+// through warp shuffles and shared memory; the merged-image sums of a Coulomb out-state go to different warps.
 __global__ void water_kernel(WaterArgs a) {
-    const int lane = threadIdx.x & 31;
-    const int64_t chain = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    if (chain >= a.chains) return;  // whole warps
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, warps = blockDim.x >> 5;
+    const int64_t chain = blockIdx.x;
+    if (chain >= a.chains) return;  // whole blocks
     const WaterModel &w = a.w;
     const int M = w.molecules;
     const uint64_t key = chain_key(w.seed, (uint64_t)(a.first_chain + chain));
     double *pos = a.positions + (size_t)chain * 9 * M;
     const double *charge = a.charges;
-    JfgpuWaterState s = a.state[chain];
+    __shared__ JfgpuWaterState s;
+    __shared__ WaterCand warp_best[kMaxWarps];
+    __shared__ double warp_upper[kMaxWarps];
+    __shared__ int warp_count[kMaxWarps], warp_count_coulomb[kMaxWarps], warp_count_lj[kMaxWarps];
+    __shared__ double upper;
+    __shared__ int refined;
+    // per-item lower bounds of the screen and the list of items for the FP64 pass (dynamic shared memory)
+    extern __shared__ double dynamic[];
+    double *lower = dynamic;
+    int *list = reinterpret_cast<int *>(dynamic + water_items_max(M));
+    __shared__ WaterCand winner;
+    __shared__ int status;
+    __shared__ double bound[3], pair[3], cross[9];
+    __shared__ float pair32[3], error32[3];
+    __shared__ int decision;  // 0 rejected, 1 thinning in FP64, 2 accepted
+    if (threadIdx.x == 0) {
+        s = a.state[chain];
+        status = JFGPU_STATUS_OK;
+    }
+    __syncthreads();
     for (int64_t step = 0; step < a.events && s.status == JFGPU_STATUS_OK; ++step) {
         const int act = s.active, m = act / 3, t = act % 3, d = s.direction;
         const uint64_t ev = (uint64_t)s.events;
-        double velocity[3] = {0.0, 0.0, 0.0};
-        velocity[d] = w.speed;
         double pa[3];
         for (int c = 0; c < 3; ++c) pa[c] = pos[3 * act + c];
         const double ca = charge[act];
@@ -103,153 +265,261 @@ __global__ void water_kernel(WaterArgs a) {
         best.r = INFINITY;
         best.kind = 1 << 30;
         best.target = 1 << 30;
+        const int items = 3 * (((M - 1) + 31) & ~31) + (t == 1 ? M - 1 : 0) + 2;
         int st = JFGPU_STATUS_OK;
-        for (int other = lane; other < M && !st; other += 32) {
-            if (other == m) continue;
-            double du[3], dt = 0.0;
-            for (int j = 0; j < 3; ++j)
-                du[j] = expovariate(draw(key, ev, kRngComposite, (uint32_t)(3 * other + j)), w.beta);
-            st = composite_event_time(w.coulomb, velocity, pa, ca, pos + 9 * other, charge + 3 * other, du, dt);
-            if (st) break;
-            water_offer(best, s.time_q, s.time_r, dt, JFGPU_EV_COMPOSITE, other);
-            if (t == 1) {
-                const int b = 3 * other + 1;
-                double sep[3], value;
-                periodic_separation(pa, pos + 3 * b, w.length, sep);
-                const double u = expovariate(draw(key, ev, kRngPair, (uint32_t)b), w.beta);
-                st = mh_std_displacement(w.lj, d, sep, u, value);
-                if (st) break;
-                water_offer(best, s.time_q, s.time_r, value / w.speed, JFGPU_EV_PAIR, b);
+        if (w.mode == JFGPU_MODE_MIXED) {
+            // phase A: FP32 screen of every item; lower[item] = the earliest time the item may reach (-inf where
+            // the screen cannot judge), upper = the smallest time that some candidate surely reaches (a screened
+            // time plus its error bound, or the end of chain)
+            double mine = INFINITY;
+            for (int item = threadIdx.x; item < items; item += blockDim.x) {
+                float t32, e32;
+                bool unsafe;
+                water_screen(w, pos, charge, key, ev, item, m, t, d, pa, ca, t32, e32, unsafe);
+                lower[item] = unsafe ? -INFINITY : (double)t32 - (double)e32;
+                if (!unsafe) mine = fmin(mine, (double)t32 + (double)e32);
             }
+            for (int offset = 16; offset > 0; offset >>= 1) mine = fmin(mine, __shfl_xor_sync(kFull, mine, offset));
+            if (lane == 0) warp_upper[warp] = mine;
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                double u = time_sub(s.eoc_q, s.eoc_r, s.time_q, s.time_r);
+                for (int k = 0; k < warps; ++k) u = fmin(u, warp_upper[k]);
+                upper = u;
+            }
+            __syncthreads();
+            // the items that may come first, listed in item order (Coulomb items by unit type, then Lennard-Jones,
+            // then bonds) so that each warp of the FP64 pass follows one kind of solve
+            const double bound_time = upper;
+            const int coulomb_items = 3 * (((M - 1) + 31) & ~31), lj_items = t == 1 ? M - 1 : 0;
+            int base = 0, coulomb_taken = 0, lj_taken = 0;
+            for (int round = 0; round * (int)blockDim.x < items; ++round) {
+                const int item = round * blockDim.x + threadIdx.x;
+                const bool take = item < items && lower[item] <= bound_time;
+                const unsigned votes = __ballot_sync(kFull, take);
+                const unsigned coulomb_votes = __ballot_sync(kFull, take && item < coulomb_items);
+                const unsigned lj_votes = __ballot_sync(kFull, take && item >= coulomb_items &&
+                                                                   item < coulomb_items + lj_items);
+                if (lane == 0) {
+                    warp_count[warp] = __popc(votes);
+                    warp_count_coulomb[warp] = __popc(coulomb_votes);
+                    warp_count_lj[warp] = __popc(lj_votes);
+                }
+                __syncthreads();
+                int offset = base;
+                for (int k = 0; k < warp; ++k) offset += warp_count[k];
+                if (take) list[offset + __popc(votes & ((1u << lane) - 1u))] = item;
+                for (int k = 0; k < warps; ++k) {
+                    base += warp_count[k];
+                    coulomb_taken += warp_count_coulomb[k];
+                    lj_taken += warp_count_lj[k];
+                }
+                __syncthreads();
+            }
+            // phase B: the FP64 solve of the listed items; each kind of solve starts on a warp boundary, so that a
+            // warp follows one kind (Coulomb, Lennard-Jones, bonds)
+            const int lj_start = (coulomb_taken + 31) & ~31;
+            const int bond_start = lj_start + ((lj_taken + 31) & ~31);
+            const int bonds_taken = base - coulomb_taken - lj_taken;
+            for (int v = threadIdx.x; v < bond_start + bonds_taken && !st; v += blockDim.x) {
+                int k = -1;
+                if (v < coulomb_taken)
+                    k = v;
+                else if (v >= lj_start && v < lj_start + lj_taken)
+                    k = coulomb_taken + (v - lj_start);
+                else if (v >= bond_start)
+                    k = coulomb_taken + lj_taken + (v - bond_start);
+                if (k >= 0)
+                    st = water_item(w, pos, charge, key, ev, list[k], m, t, d, pa, ca, s.time_q, s.time_r, best);
+            }
+            if (threadIdx.x == 0) refined = base;
+        } else {
+            for (int item = threadIdx.x; item < items && !st; item += blockDim.x)
+                st = water_item(w, pos, charge, key, ev, item, m, t, d, pa, ca, s.time_q, s.time_r, best);
         }
-        if (!st && lane < 3 && lane != t) {
-            const int b = 3 * m + lane;
-            const MH &bond = (t == 1 || lane == 1) ? w.oh : w.hh;
-            double sep[3], value;
-            periodic_separation(pa, pos + 3 * b, w.length, sep);
-            const double u = expovariate(draw(key, ev, kRngPair, (uint32_t)b), w.beta);
-            st = mh_std_displacement(bond, d, sep, u, value);
-            if (!st) water_offer(best, s.time_q, s.time_r, value / w.speed, JFGPU_EV_BOND, b);
-        }
-        const unsigned failed = __ballot_sync(kFull, st != JFGPU_STATUS_OK);
-        if (failed) {
-            s.status = __shfl_sync(kFull, st, __ffs(failed) - 1);
+        if (st) status = st;  // any failing thread; all stop after the barrier
+        for (int offset = 16; offset > 0; offset >>= 1) shuffle_better(best, offset);
+        if (lane == 0) warp_best[warp] = best;
+        __syncthreads();
+        if (status != JFGPU_STATUS_OK) {
+            if (threadIdx.x == 0) s.status = status;
             break;
         }
-        for (int offset = 16; offset > 0; offset >>= 1) {
-            WaterCand o;
-            o.q = __shfl_xor_sync(kFull, best.q, offset);
-            o.r = __shfl_xor_sync(kFull, best.r, offset);
-            o.kind = __shfl_xor_sync(kFull, best.kind, offset);
-            o.target = __shfl_xor_sync(kFull, best.target, offset);
-            if (water_better(o, best)) best = o;
-        }
-        {
+        if (threadIdx.x == 0) {
+            WaterCand b = warp_best[0];
+            for (int k = 1; k < warps; ++k)
+                if (water_better(warp_best[k], b)) b = warp_best[k];
             WaterCand e;
             e.q = s.eoc_q;
             e.r = s.eoc_r;
             e.kind = JFGPU_EV_END_OF_CHAIN;
             e.target = s.eoc_new_active;
-            if (water_better(e, best)) best = e;
+            if (water_better(e, b)) b = e;
+            winner = b;
         }
-        // commit: time slice of the active unit (every lane computes the same position; lane 0 stores it)
+        __syncthreads();
+        best = winner;
+        // commit: time slice of the active unit (every thread computes the same position; thread 0 stores it)
         {
             const double dt = time_sub(best.q, best.r, s.time_q, s.time_r);
-            for (int c = 0; c < 3; ++c) pa[c] = py_mod(pa[c] + velocity[c] * dt, w.length);
-            if (lane == 0)
-                for (int c = 0; c < 3; ++c) pos[3 * act + c] = pa[c];
-            s.time_q = best.q;
-            s.time_r = best.r;
+            for (int c = 0; c < 3; ++c) pa[c] = py_mod(pa[c] + (c == d ? w.speed : 0.0) * dt, w.length);
         }
-        __syncwarp();
         int accepted = 1;
-        if (best.kind == JFGPU_EV_BOND || best.kind == JFGPU_EV_PAIR) {
-            s.active = best.target;
-            if (best.kind == JFGPU_EV_BOND) ++s.bond_events; else ++s.lj_events;
-        } else if (best.kind == JFGPU_EV_COMPOSITE) {
+        if (best.kind == JFGPU_EV_COMPOSITE) {
             const int other = best.target;
             const double *locals = pos + 9 * m, *targets = pos + 9 * other;
-            // lanes 0-2: the active unit against target unit `lane` (bound and potential); lanes 3-8: local unit
-            // i (the (lane - 3) / 3-th unit other than the active one) against target unit (lane - 3) % 3
-            double mine_bound = 0.0, mine_pair = 0.0;
-            if (lane < 3) {
-                double sep[3];
-                periodic_separation(pa, targets + 3 * lane, w.length, sep);
-                mine_bound = bound_derivative(w.coulomb, d, w.speed, sep, ca, charge[3 * other + lane]);
-                mine_pair = coulomb_derivative(w.coulomb, d, w.speed, sep, ca, charge[3 * other + lane]);
-            } else if (lane < 9) {
-                const int k = (lane - 3) / 3, j = (lane - 3) % 3;
-                const int i = k < t ? k : k + 1;
-                double sep[3];
-                periodic_separation(locals + 3 * i, targets + 3 * j, w.length, sep);
-                mine_pair = coulomb_derivative(w.coulomb, d, w.speed, sep, charge[3 * m + i], charge[3 * other + j]);
-            }
-            double bound[3], pair[3], cross[9], target_factor[3];
-            for (int j = 0; j < 3; ++j) {
-                bound[j] = shfl_double(mine_bound, j);
-                pair[j] = shfl_double(mine_pair, j);
-            }
-            for (int k = 0; k < 2; ++k) {
-                const int i = k < t ? k : k + 1;
-                for (int j = 0; j < 3; ++j) cross[i * 3 + j] = shfl_double(mine_pair, 3 + 3 * k + j);
-            }
-            for (int j = 0; j < 3; ++j) cross[t * 3 + j] = 0.0;  // the active row is not read
             double draws[3];
             draws[0] = uniform53(draw(key, ev, kRngThin, 0));
             draws[1] = uniform53(draw(key, ev, kRngLift, 0));
             draws[2] = draws[1];
-            double bounding_rate, event_rate;
-            ++s.composite_events;
-            accepted = 0;
-            if (composite_thinning(w.coulomb, JFGPU_DRAW_UNIT, bound, pair, draws, target_factor, bounding_rate,
-                                   event_rate)) {
-                int new_active = -1;
-                st = composite_lifting(w.coulomb, JFGPU_DRAW_UNIT, t, m < other, event_rate, target_factor, cross,
-                                       draws, new_active);
-                if (st) {
-                    s.status = st;
-                    break;
-                }
-                accepted = 1;
-                ++s.composite_accepted;
-                s.active = new_active < 3 ? 3 * m + new_active : 3 * other + (new_active - 3);
+            // bounding derivatives (threads 0-2) and, in the mixed mode, the FP32 merged-image sums (warp j for
+            // target unit j), at the time-sliced position of the active unit
+            if (threadIdx.x < 3) {
+                double sep[3];
+                periodic_separation(pa, targets + 3 * threadIdx.x, w.length, sep);
+                bound[threadIdx.x] = bound_derivative(w.coulomb, d, w.speed, sep, ca, charge[3 * other + threadIdx.x]);
             }
-        } else if (best.kind == JFGPU_EV_END_OF_CHAIN) {
-            s.direction = (s.direction + 1) % 3;
-            s.active = best.target;
-            time_add(s.time_q, s.time_r, time_sub(s.time_q, s.time_r, s.time_q, s.time_r) + w.chain_time, s.eoc_q,
-                     s.eoc_r);
-            s.eoc_new_active = water_new_active(w, key, ev + 1);
-            ++s.eoc_events;
-        } else {
-            s.status = JFGPU_STATUS_ASSERTION;
-            break;
+            if (w.mode == JFGPU_MODE_MIXED) {
+                for (int j = warp; j < 3; j += warps) {
+                    double sep[3], p[3];
+                    periodic_separation(pa, targets + 3 * j, w.length, sep);
+                    permute3(sep, d, p);
+                    float value, value_error;
+                    mic_x_warp32(w.coulomb, (float)p[0], (float)p[1], (float)p[2], lane, value, value_error);
+                    if (lane == 0) {
+                        const double scale = w.coulomb.coulomb_prefactor * ca * charge[3 * other + j] * w.speed;
+                        pair32[j] = (float)scale * value;
+                        error32[j] = fabsf((float)scale) * value_error + fabsf((float)scale * value) * 2.4e-7f;
+                    }
+                }
+            }
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                decision = 1;
+                if (w.mode == JFGPU_MODE_MIXED) {
+                    double bounding = 0.0;
+                    for (int j = 0; j < 3; ++j) bounding += bound[j] > 0.0 ? bound[j] : 0.0;
+                    const double thinning = 0.0 + (bounding - 0.0) * draws[0];
+                    const float factor = pair32[0] + pair32[1] + pair32[2];
+                    const float error = error32[0] + error32[1] + error32[2] + fabsf(factor) * 2.4e-7f;
+                    if ((double)factor + (double)error < thinning) decision = 0;  // rejection certain
+                }
+                ++s.composite_events;
+                if (decision) ++s.thinning_exact;
+            }
+            __syncthreads();
+            if (decision) {
+                for (int j = warp; j < 3; j += warps) {
+                    double sep[3];
+                    periodic_separation(pa, targets + 3 * j, w.length, sep);
+                    const double value =
+                        coulomb_derivative_warp(w.coulomb, d, w.speed, sep, ca, charge[3 * other + j], lane);
+                    if (lane == 0) pair[j] = value;
+                }
+                __syncthreads();
+                if (threadIdx.x == 0) {
+                    double target_factor[3], bounding_rate, event_rate;
+                    decision = composite_thinning(w.coulomb, JFGPU_DRAW_UNIT, bound, pair, draws, target_factor,
+                                                  bounding_rate, event_rate) ? 2 : 0;
+                }
+                __syncthreads();
+            }
+            if (decision == 2) {
+                // the derivatives of the two other local units against the three target units
+                for (int k = warp; k < 6; k += warps) {
+                    const int i = k / 3 < t ? k / 3 : k / 3 + 1, j = k % 3;
+                    double sep[3];
+                    periodic_separation(locals + 3 * i, targets + 3 * j, w.length, sep);
+                    const double value = coulomb_derivative_warp(w.coulomb, d, w.speed, sep, charge[3 * m + i],
+                                                                 charge[3 * other + j], lane);
+                    if (lane == 0) cross[i * 3 + j] = value;
+                }
+                __syncthreads();
+                if (threadIdx.x == 0) {
+                    double target_factor[3], bounding_rate, event_rate, local_cross[9];
+                    composite_thinning(w.coulomb, JFGPU_DRAW_UNIT, bound, pair, draws, target_factor, bounding_rate,
+                                       event_rate);
+                    for (int k = 0; k < 9; ++k) local_cross[k] = cross[k];
+                    int new_active = -1;
+                    const int lst = composite_lifting(w.coulomb, JFGPU_DRAW_UNIT, t, m < other, event_rate,
+                                                      target_factor, local_cross, draws, new_active);
+                    if (lst) {
+                        s.status = lst;
+                    } else {
+                        ++s.composite_accepted;
+                        s.active = new_active < 3 ? 3 * m + new_active : 3 * other + (new_active - 3);
+                    }
+                }
+            }
+            accepted = decision == 2;
+        } else if (threadIdx.x == 0) {
+            if (best.kind == JFGPU_EV_BOND || best.kind == JFGPU_EV_PAIR) {
+                s.active = best.target;
+                if (best.kind == JFGPU_EV_BOND) ++s.bond_events; else ++s.lj_events;
+            } else if (best.kind == JFGPU_EV_END_OF_CHAIN) {
+                s.direction = (s.direction + 1) % 3;
+                s.active = best.target;
+                // the next end of chain from the time stamp of this event
+                time_add(best.q, best.r, time_sub(best.q, best.r, best.q, best.r) + w.chain_time, s.eoc_q, s.eoc_r);
+                s.eoc_new_active = water_new_active(w, key, ev + 1);
+                ++s.eoc_events;
+            } else {
+                s.status = JFGPU_STATUS_ASSERTION;
+            }
         }
-        if (lane == 0 && a.log) {
-            JfgpuEvent e;
-            e.kind = best.kind;
-            e.moved = act;
-            e.target = best.target;
-            e.new_active = s.active;
-            e.new_direction = s.direction;
-            e.accepted = accepted;
-            e.time_q = best.q;
-            e.time_r = best.r;
-            e.x = pa[0];
-            e.y = pa[1];
-            e.z = pa[2];
-            a.log[chain * a.events + step] = e;
+        if (threadIdx.x == 0) {
+            for (int c = 0; c < 3; ++c) pos[3 * act + c] = pa[c];
+            s.time_q = best.q;
+            s.time_r = best.r;
+            if (a.log) {
+                JfgpuEvent e;
+                e.kind = best.kind;
+                e.moved = act;
+                e.target = best.target;
+                e.new_active = s.active;
+                e.new_direction = s.direction;
+                e.accepted = accepted;
+                e.time_q = best.q;
+                e.time_r = best.r;
+                e.x = pa[0];
+                e.y = pa[1];
+                e.z = pa[2];
+                a.log[chain * a.events + step] = e;
+            }
+            ++s.events;
+            s.refined_items += w.mode == JFGPU_MODE_MIXED ? refined : 3 * (M - 1) + (t == 1 ? M - 1 : 0) + 2;
         }
-        ++s.events;
+        __syncthreads();
     }
-    if (lane == 0) a.state[chain] = s;
+    if (threadIdx.x == 0) a.state[chain] = s;
 }
 
 struct WaterHandle {
     WaterModel model;
     double *fourier = nullptr;
+    float *fourier32 = nullptr;
+    int4 *terms = nullptr;  // real-space images, then Fourier rows
     int device = -1;
 };
+
+// the terms of the merged-image sum in the order of merged_image_coulomb_potential.c:205-274: real-space images
+// (i, j, k) with i^2 + j^2 + k^2 <= position_cutoff^2, Fourier rows (i, j, last k) with i >= 1
+static void merged_image_terms(int fc, int pc, std::vector<int4> &images, std::vector<int4> &rows) {
+    for (int k = -pc; k < pc + 1; k++) {
+        int cutoff_y = (int)std::sqrt((double)(pc * pc - k * k));
+        for (int j = -cutoff_y; j < cutoff_y + 1; j++) {
+            int cutoff_x = (int)std::sqrt((double)(pc * pc - j * j - k * k));
+            for (int i = -cutoff_x; i < cutoff_x + 1; i++) images.push_back(make_int4(i, j, k, 0));
+        }
+    }
+    for (int i = 1; i < fc + 1; i++) {
+        int cutoff_y = (int)std::sqrt((double)(fc * fc - i * i));
+        for (int j = 0; j < cutoff_y + 1; j++) {
+            int cutoff_x = (int)std::sqrt((double)(fc * fc - i * i - j * j));
+            rows.push_back(make_int4(i, j, cutoff_x, 0));
+        }
+    }
+}
 
 }  // namespace jf
 
@@ -262,7 +532,8 @@ extern "C" int jfgpu_water_create(const JfgpuWaterDesc *desc, void **water) {
         !(desc->speed > 0.0) || !(desc->chain_time > 0.0) || desc->initial_active < 0 ||
         desc->initial_active >= 3 * desc->molecules || desc->initial_direction < 0 || desc->initial_direction > 2 ||
         desc->lifting < JFGPU_LIFTING_INSIDE_FIRST || desc->lifting > JFGPU_LIFTING_RATIO ||
-        desc->fourier_cutoff < 0 || desc->position_cutoff < 0 || !(desc->alpha > 0.0))
+        desc->fourier_cutoff < 0 || desc->position_cutoff < 0 || !(desc->alpha > 0.0) ||
+        (desc->mode != JFGPU_MODE_EXACT && desc->mode != JFGPU_MODE_MIXED))
         return JFGPU_ERROR_ARGUMENT;
     WaterHandle *h = new WaterHandle();
     if (cudaGetDevice(&h->device) != cudaSuccess) {
@@ -279,9 +550,47 @@ extern "C" int jfgpu_water_create(const JfgpuWaterDesc *desc, void **water) {
         delete h;
         return JFGPU_ERROR_CUDA;
     }
+    std::vector<float> table32(table.begin(), table.end());
+    if (cudaMalloc((void **)&h->fourier32, table32.size() * sizeof(float)) != cudaSuccess ||
+        cudaMemcpy(h->fourier32, table32.data(), table32.size() * sizeof(float), cudaMemcpyHostToDevice) !=
+            cudaSuccess) {
+        if (h->fourier32) cudaFree(h->fourier32);
+        cudaFree(h->fourier);
+        delete h;
+        return JFGPU_ERROR_ALLOCATION;
+    }
+    std::vector<int4> images, rows;
+    merged_image_terms(desc->fourier_cutoff, desc->position_cutoff, images, rows);
+    std::vector<int4> terms(images);
+    terms.insert(terms.end(), rows.begin(), rows.end());
+    if (cudaMalloc((void **)&h->terms, terms.size() * sizeof(int4)) != cudaSuccess) {
+        cudaFree(h->fourier32);
+        cudaFree(h->fourier);
+        delete h;
+        return JFGPU_ERROR_ALLOCATION;
+    }
+    if (cudaMemcpy(h->terms, terms.data(), terms.size() * sizeof(int4), cudaMemcpyHostToDevice) != cudaSuccess) {
+        cudaFree(h->terms);
+        cudaFree(h->fourier32);
+        cudaFree(h->fourier);
+        delete h;
+        return JFGPU_ERROR_CUDA;
+    }
     WaterModel &w = h->model;
     w.coulomb.mic = make_mic(desc->fourier_cutoff, desc->position_cutoff, desc->alpha, desc->system_length,
                              h->fourier);
+    w.coulomb.images = h->terms;
+    w.coulomb.n_images = (int)images.size();
+    w.coulomb.rows = h->terms + images.size();
+    w.coulomb.n_rows = (int)rows.size();
+    const MIC &mic = w.coulomb.mic;
+    w.coulomb.fourier32 = h->fourier32;
+    w.coulomb.alpha_over_length32 = (float)mic.alpha_over_length;
+    w.coulomb.alpha_over_length_sq32 = (float)mic.alpha_over_length_sq;
+    w.coulomb.two_alpha_over_length_root_pi32 = (float)mic.two_alpha_over_length_root_pi;
+    w.coulomb.system_length32 = (float)mic.system_length;
+    w.coulomb.two_pi_over_length32 = (float)mic.two_pi_over_length;
+    w.mode = desc->mode;
     w.coulomb.coulomb_prefactor = desc->coulomb_prefactor;
     w.coulomb.bound_prefactor = desc->bound_prefactor;
     w.coulomb.system_length = desc->system_length;
@@ -294,6 +603,15 @@ extern "C" int jfgpu_water_create(const JfgpuWaterDesc *desc, void **water) {
     w.chain_time = desc->chain_time;
     w.speed = desc->speed;
     w.length = desc->system_length;
+    w.beta32 = (float)desc->beta;
+    w.speed32 = (float)desc->speed;
+    w.length32 = (float)desc->system_length;
+    w.lj32.a12 = (float)w.lj.twelve.prefactor;
+    w.lj32.a6 = (float)w.lj.six.prefactor;
+    w.lj32.four_over_k = (float)(4.0 / w.lj.prefactor);
+    w.lj32.sigma_sq = (float)(w.lj.sigma * w.lj.sigma);
+    w.lj32.r0_sq = (float)w.lj.r0_squared;
+    w.margin32 = (float)(16.0 * desc->system_length / 16777216.0);
     w.molecules = desc->molecules;
     w.initial_active = desc->initial_active;
     w.initial_direction = desc->initial_direction;
@@ -306,6 +624,8 @@ extern "C" void jfgpu_water_destroy(void *water) {
     WaterHandle *h = static_cast<WaterHandle *>(water);
     if (!h) return;
     if (h->fourier) cudaFree(h->fourier);
+    if (h->fourier32) cudaFree(h->fourier32);
+    if (h->terms) cudaFree(h->terms);
     delete h;
 }
 
@@ -329,7 +649,7 @@ extern "C" int jfgpu_water_run(void *water, double *positions, const double *cha
         return JFGPU_ERROR_ARGUMENT;
     if (chains == 0 || events == 0) return JFGPU_OK;
     if (!positions || !charges || !state) return JFGPU_ERROR_ARGUMENT;
-    const int warps = warps_per_block ? warps_per_block : 1;
+    const int warps = warps_per_block ? warps_per_block : 4;
     WaterArgs a;
     a.w = h->model;
     a.positions = positions;
@@ -339,7 +659,10 @@ extern "C" int jfgpu_water_run(void *water, double *positions, const double *cha
     a.chains = chains;
     a.first_chain = first_chain;
     a.events = events;
-    const int64_t blocks = (chains + warps - 1) / warps;
-    water_kernel<<<(unsigned)blocks, 32 * warps, 0, static_cast<cudaStream_t>(stream)>>>(a);
+    const size_t shared = water_shared_bytes(h->model.molecules);
+    if (shared > 48 * 1024 &&
+        cudaFuncSetAttribute(water_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shared) != cudaSuccess)
+        return JFGPU_ERROR_CUDA;
+    water_kernel<<<(unsigned)chains, 32 * warps, shared, static_cast<cudaStream_t>(stream)>>>(a);
     return cudaGetLastError() == cudaSuccess ? JFGPU_OK : JFGPU_ERROR_CUDA;
 }

@@ -6,7 +6,10 @@ hydrogen; unit ``3 m + t``).  Its factors are those of the reference's water bui
 Lennard-Jones between oxygens (``TwoLeafUnitEventHandler``) and one Coulomb factor per pair of molecules
 (``TwoCompositeObjectSummedBoundingPotentialEventHandler`` with merged-image Coulomb, the summed inverse-power
 Coulomb bound and a lifting scheme), for every pair of molecules; chains end by the periodic-direction end of
-chain.  One warp advances one chain with the event loop on the device, in FP64 with the reference's arithmetic.
+chain.  One block advances one chain with the event loop on the device, in FP64 with the reference's arithmetic.  In
+the mixed mode (the default) the Coulomb candidates are screened in FP32 with error bounds and only those that may
+come first are solved in FP64, and the thinning of a Coulomb event first tries FP32 merged-image sums with an
+error bound; every outcome is the exact mode's.
 """
 import ctypes
 from dataclasses import asdict, dataclass
@@ -24,7 +27,8 @@ STATE_DTYPE = np.dtype([("time_q", np.float64), ("time_r", np.float64), ("eoc_q"
                         ("active", np.int32), ("direction", np.int32), ("eoc_new_active", np.int32),
                         ("status", np.int32), ("events", np.int64), ("composite_events", np.int64),
                         ("composite_accepted", np.int64), ("bond_events", np.int64), ("lj_events", np.int64),
-                        ("eoc_events", np.int64)])
+                        ("eoc_events", np.int64), ("thinning_exact", np.int64), ("refined_items", np.int64)])
+MODES = {"exact": _lib.MODE_EXACT, "mixed": _lib.MODE_MIXED}
 
 
 @dataclass
@@ -55,6 +59,7 @@ class WaterModel:
     lifting: str = "inside_first"
     charge_oxygen: float = -0.82
     charge_hydrogen: float = 0.41
+    mode: str = "mixed"
 
     @classmethod
     def from_spec(cls, spec: dict) -> "WaterModel":
@@ -73,6 +78,7 @@ class WaterModel:
         values.pop("charge_oxygen")
         values.pop("charge_hydrogen")
         values["lifting"] = LIFTING[self.lifting]
+        values["mode"] = MODES[self.mode]
         return _lib.WaterDesc(seed=int(seed), **values)
 
 
@@ -81,7 +87,7 @@ class WaterBatch:
     its random numbers with the key of (seed, first_chain + c)."""
 
     def __init__(self, model: WaterModel, positions, seed: int = 0, first_chain: int = 0, charges=None,
-                 warps_per_block: int = 1):
+                 warps_per_block: int = 4):
         import torch
         self._torch = torch
         self.lib = _lib.load()

@@ -435,14 +435,16 @@ class Water:
             lib().jfo_water_destroy(handle)
             self._handle = None
 
-    def run(self, max_events: int):
-        log_array = np.zeros(max_events, dtype=EVENT_DTYPE)
+    def run(self, max_events: int, record: bool = True):
+        """Advance by ``max_events`` events; returns the event log (or the count without ``record``)."""
+        log_array = np.zeros(max_events if record else 0, dtype=EVENT_DTYPE)
         status = ctypes.c_int()
-        done = lib().jfo_water_run(self._handle, max_events, log_array.ctypes.data, ctypes.byref(status))
+        done = lib().jfo_water_run(self._handle, max_events, log_array.ctypes.data if record else None,
+                                   ctypes.byref(status))
         if status.value != 0:
             raise OracleError("water run stopped after %d events: %s"
                               % (done, STATUS_NAMES.get(status.value, str(status.value))))
-        return log_array[:done]
+        return log_array[:done] if record else done
 
     def positions(self) -> np.ndarray:
         out = np.zeros((3 * self.system.molecules, 3), dtype=np.float64)

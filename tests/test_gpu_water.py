@@ -86,6 +86,25 @@ def test_batched_water_chains_match_the_oracle(water):
     assert kinds[oracle.EV_COMPOSITE] > 0 and kinds[oracle.EV_BOND] > 0
 
 
+def test_mixed_mode_equals_exact_mode(water):
+    """The FP32-screened rejections of the mixed mode leave every event, time and position as in the exact mode."""
+    chains, events, seed = 96, 200, 77
+    runs = {}
+    for mode in ("exact", "mixed"):
+        model = water.WaterModel(mode=mode)
+        batch = water.WaterBatch(model, water.lattice_positions(model, chains, seed), seed=seed)
+        runs[mode] = (batch.run(events, record=True), batch.positions(), batch.states())
+        batch.check_status()
+    for field in runs["exact"][0].dtype.names:
+        assert np.array_equal(runs["exact"][0][field], runs["mixed"][0][field]), field
+    assert np.array_equal(runs["exact"][1], runs["mixed"][1])
+    exact, mixed = runs["exact"][2], runs["mixed"][2]
+    assert (exact["thinning_exact"] == exact["composite_events"]).all()
+    # most rejections are decided by the FP32 sums, most candidates by the FP32 screen
+    assert mixed["thinning_exact"].sum() < 0.5 * mixed["composite_events"].sum()
+    assert mixed["refined_items"].sum() < 0.2 * exact["refined_items"].sum()
+
+
 def test_water_replicas_of_the_batched_workload_run_clean(water):
     """512 replicas of 64 molecules: every chain advances without a status, positions stay in the box."""
     model = water.WaterModel()

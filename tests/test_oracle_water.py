@@ -42,13 +42,14 @@ def test_water_lattice_geometry():
 def test_water_model_matches_the_header_layouts():
     import ctypes
     from jellyfysh_gb300 import _lib, water
-    assert ctypes.sizeof(_lib.WaterDesc) == 136
-    assert water.STATE_DTYPE.itemsize == 96  # JfgpuWaterState: 4 doubles, 4 int32, 6 int64
+    assert ctypes.sizeof(_lib.WaterDesc) == 144
+    assert water.STATE_DTYPE.itemsize == 112  # JfgpuWaterState: 4 doubles, 4 int32, 8 int64
     model = water.WaterModel.from_spec({"molecules_per_side": 2, "system_length": 6.21, "lifting": "ratio",
                                         "unused": 1})
     assert model.molecules == 8 and model.system_length == 6.21
     desc = model.desc(seed=7)
     assert (desc.molecules, desc.lifting, desc.seed, desc.initial_active) == (8, _lib.LIFTING_RATIO, 7, 1)
+    assert desc.mode == _lib.MODE_MIXED and water.WaterModel(mode="exact").desc(0).mode == _lib.MODE_EXACT
     assert desc.oh_prefactor == 529.5 and desc.hh_prefactor == 342.0
     assert model.charges().tolist()[:3] == [0.41, -0.82, 0.41]
 
