@@ -247,7 +247,7 @@ __global__ void water_kernel(WaterArgs a) {
     __shared__ WaterCand winner;
     __shared__ int status;
     __shared__ double bound[3], pair[3], cross[9];
-    __shared__ float pair32[3], error32[3];
+    __shared__ float pair32[3], error32[3], bound32[3];
     __shared__ int decision;  // 0 rejected, 1 thinning in FP64, 2 accepted
     if (threadIdx.x == 0) {
         s = a.state[chain];
@@ -372,13 +372,8 @@ __global__ void water_kernel(WaterArgs a) {
             draws[0] = uniform53(draw(key, ev, kRngThin, 0));
             draws[1] = uniform53(draw(key, ev, kRngLift, 0));
             draws[2] = draws[1];
-            // bounding derivatives (threads 0-2) and, in the mixed mode, the FP32 merged-image sums (warp j for
-            // target unit j), at the time-sliced position of the active unit
-            if (threadIdx.x < 3) {
-                double sep[3];
-                periodic_separation(pa, targets + 3 * threadIdx.x, w.length, sep);
-                bound[threadIdx.x] = bound_derivative(w.coulomb, d, w.speed, sep, ca, charge[3 * other + threadIdx.x]);
-            }
+            // in the mixed mode, FP32 first: the merged-image sums (warp j for target unit j) and the bounding
+            // derivatives, each with an error bound, at the time-sliced position of the active unit
             if (w.mode == JFGPU_MODE_MIXED) {
                 for (int j = warp; j < 3; j += warps) {
                     double sep[3], p[3];
@@ -390,6 +385,12 @@ __global__ void water_kernel(WaterArgs a) {
                         const double scale = w.coulomb.coulomb_prefactor * ca * charge[3 * other + j] * w.speed;
                         pair32[j] = (float)scale * value;
                         error32[j] = fabsf((float)scale) * value_error + fabsf((float)scale * value) * 2.4e-7f;
+                        // bounding derivative pp s_x / |s|^3 times the speed: within about 14 ulp, taken as 32
+                        const float x = (float)p[0], y = (float)p[1], z = (float)p[2];
+                        const float r2 = x * x + y * y + z * z;
+                        const float b = (float)(w.coulomb.bound_prefactor * ca * charge[3 * other + j]) * x /
+                                        (r2 * sqrtf(r2)) * w.speed32;
+                        bound32[j] = b - fabsf(b) * 32.f * 0x1p-24f;  // a lower bound
                     }
                 }
             }
@@ -397,18 +398,27 @@ __global__ void water_kernel(WaterArgs a) {
             if (threadIdx.x == 0) {
                 decision = 1;
                 if (w.mode == JFGPU_MODE_MIXED) {
-                    double bounding = 0.0;
-                    for (int j = 0; j < 3; ++j) bounding += bound[j] > 0.0 ? bound[j] : 0.0;
-                    const double thinning = 0.0 + (bounding - 0.0) * draws[0];
+                    // max(0, factor) <= uniform(0, bounding rate) is certain when the factor's upper bound stays
+                    // below the draw times a lower bound of the bounding rate
+                    float bounding = 0.f;
+                    for (int j = 0; j < 3; ++j) bounding += fmaxf(bound32[j], 0.f);
+                    const double thinning_lower = (double)bounding * draws[0] * (1.0 - 0x1p-20);
                     const float factor = pair32[0] + pair32[1] + pair32[2];
                     const float error = error32[0] + error32[1] + error32[2] + fabsf(factor) * 2.4e-7f;
-                    if ((double)factor + (double)error < thinning) decision = 0;  // rejection certain
+                    if ((double)factor + (double)error < thinning_lower) decision = 0;  // rejection certain
                 }
                 ++s.composite_events;
                 if (decision) ++s.thinning_exact;
             }
             __syncthreads();
             if (decision) {
+                // the FP64 bounding derivatives (threads 0-2) and merged-image sums (warp j for target unit j)
+                if (threadIdx.x < 3) {
+                    double sep[3];
+                    periodic_separation(pa, targets + 3 * threadIdx.x, w.length, sep);
+                    bound[threadIdx.x] =
+                        bound_derivative(w.coulomb, d, w.speed, sep, ca, charge[3 * other + threadIdx.x]);
+                }
                 for (int j = warp; j < 3; j += warps) {
                     double sep[3];
                     periodic_separation(pa, targets + 3 * j, w.length, sep);
