@@ -147,19 +147,37 @@ __device__ inline int water_item(const WaterModel &w, const double *pos, const d
     return JFGPU_STATUS_OK;
 }
 
-// FP32 screen of a candidate item: the Coulomb items solve the bound's inversion in FP32 with an error bound
-// (ipcb_x_displacement32); the Lennard-Jones and bond items are always left to FP64 (unsafe).  time and error are
-// displacements over the speed.
+// FP32 screen of a candidate item, in displacements over the speed: the Coulomb items solve the bound's inversion
+// in FP32 with an error bound (ipcb_x_displacement32), the Lennard-Jones items take the FP32 screen of the atomic
+// engine; a bond gets only a lower bound of its time (lower_only: it does not bound the earliest time).  unsafe:
+// the screen cannot judge, the item goes to FP64.
 __device__ inline void water_screen(const WaterModel &w, const double *pos, const double *charge, uint64_t key,
                                    uint64_t ev, int item, int m, int t, int d, const double *pa, double ca,
-                                   float &time, float &error, bool &unsafe) {
+                                   float &time, float &error, bool &unsafe, bool &lower_only) {
     const int M = w.molecules;
     const int group = ((M - 1) + 31) & ~31;
     unsafe = false;
+    lower_only = false;
     time = 0.f;
     error = 0.f;
-    if (item >= 3 * group + (t == 1 ? M - 1 : 0)) {  // bonds: FP64
-        unsafe = true;
+    if (item >= 3 * group + (t == 1 ? M - 1 : 0)) {
+        // a bond k (|s| - r0)^2: along the motion |d|s|/dx| <= 1, so the potential rises at most at
+        // 2 k (a + x) with a = ||s| - r0| after a displacement x, and a rise du takes at least
+        // (du / k) / (a + sqrt(a^2 + du / k)); computed with every rounding towards a smaller value
+        const int k = item - 3 * group - (t == 1 ? M - 1 : 0);
+        const int u = k + (k >= t);
+        const int b = 3 * m + u;
+        const MH &bond = (t == 1 || u == 1) ? w.oh : w.hh;
+        bool flag = false;
+        const float du = expovariate32(draw(key, ev, kRngPair, (uint32_t)b), 1.0f / w.beta32, flag);
+        double sep[3];
+        periodic_separation(pa, pos + 3 * b, w.length, sep);
+        const float r = sqrtf((float)(sep[0] * sep[0] + sep[1] * sep[1] + sep[2] * sep[2]));
+        const float a = fabsf(r - (float)bond.r0) * (1.f + 0x1p-16f) + 0x1p-20f * (float)bond.r0;
+        const float ratio = du * (1.f - 0x1p-16f) / (float)(bond.prefactor * (1.0 + 0x1p-20));
+        time = ratio / (a + sqrtf(a * a + ratio)) * (1.f - 0x1p-16f) / w.speed32;
+        lower_only = true;
+        unsafe = flag || !(time >= 0.f);
         return;
     }
     if (item >= 3 * group) {
@@ -274,10 +292,10 @@ __global__ void water_kernel(WaterArgs a) {
             double mine = INFINITY;
             for (int item = threadIdx.x; item < items; item += blockDim.x) {
                 float t32, e32;
-                bool unsafe;
-                water_screen(w, pos, charge, key, ev, item, m, t, d, pa, ca, t32, e32, unsafe);
+                bool unsafe, lower_only;
+                water_screen(w, pos, charge, key, ev, item, m, t, d, pa, ca, t32, e32, unsafe, lower_only);
                 lower[item] = unsafe ? -INFINITY : (double)t32 - (double)e32;
-                if (!unsafe) mine = fmin(mine, (double)t32 + (double)e32);
+                if (!unsafe && !lower_only) mine = fmin(mine, (double)t32 + (double)e32);
             }
             for (int offset = 16; offset > 0; offset >>= 1) mine = fmin(mine, __shfl_xor_sync(kFull, mine, offset));
             if (lane == 0) warp_upper[warp] = mine;
