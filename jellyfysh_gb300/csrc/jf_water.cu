@@ -243,7 +243,9 @@ __device__ inline void shuffle_better(WaterCand &best, int offset) {
 
 // One block of `warps` warps advances one chain.  Candidate items are spread over all threads; the argmin goes
 // through warp shuffles and shared memory; the merged-image sums of a Coulomb out-state go to different warps.
-__global__ void water_kernel(WaterArgs a) {
+// At most 128 registers a thread, so that four blocks of 128 threads share an SM and 512 chains run in one wave on
+// the 152 SMs.
+__global__ void __launch_bounds__(256, 2) water_kernel(WaterArgs a) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, warps = blockDim.x >> 5;
     const int64_t chain = blockIdx.x;
     if (chain >= a.chains) return;  // whole blocks
