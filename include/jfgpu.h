@@ -303,6 +303,8 @@ typedef struct {
     double time_q, time_r;        /* time stamp of the active unit */
     double eoc_q, eoc_r;          /* end-of-chain candidate */
     int32_t active, direction, eoc_new_active, status;
+    int32_t stopped;              /* the chain reached the stop time of the current call */
+    int32_t reserved;
     int64_t events;               /* committed events: the event index of the keyed draws */
     int64_t composite_events, composite_accepted, bond_events, lj_events, eoc_events;
     int64_t thinning_exact;       /* Coulomb events whose thinning took the FP64 sums (all of them in exact mode) */
@@ -315,11 +317,14 @@ void jfgpu_water_destroy(void *water);
 /* chains first_chain .. first_chain + chains - 1 at time 0: the initial active unit and direction, the first end
  * of chain (time chain_time, new active unit drawn for event 0) */
 int jfgpu_water_init(void *water, JfgpuWaterState *state, int64_t chains, int64_t first_chain, void *stream);
-/* `events` events of every chain.  positions [chains][3 molecules][3] and charges [3 molecules] are device arrays;
- * log [chains][events] (may be null) receives every committed event.  One block of warps_per_block warps runs one
- * chain, 1..8 (0: 4). */
+/* up to `events` events of every chain, stopping at the stop time (stop_q, stop_r as Time quotient and remainder;
+ * inf, inf for none): a chain whose next event would come at or after it (the stop wins ties) has its active unit
+ * time-sliced to the stop time, `stopped` set and no further event in this call, like the reference's end of run.
+ * positions [chains][3 molecules][3] and charges [3 molecules] are device arrays; log [chains][events] (may be
+ * null) receives every committed event.  One block of warps_per_block warps runs one chain, 1..8 (0: 4). */
 int jfgpu_water_run(void *water, double *positions, const double *charges, JfgpuWaterState *state, int64_t chains,
-                    int64_t first_chain, int64_t events, JfgpuEvent *log, int32_t warps_per_block, void *stream);
+                    int64_t first_chain, int64_t events, double stop_q, double stop_r, JfgpuEvent *log,
+                    int32_t warps_per_block, void *stream);
 
 /* device buffers of a chain batch, all owned by the caller; sizes from jfgpu_engine_layout */
 typedef struct {

@@ -131,7 +131,7 @@ SIGNATURES = {
     "jfgpu_water_create": (ctypes.c_int, [ctypes.POINTER(WaterDesc), ctypes.POINTER(ctypes.c_void_p)]),
     "jfgpu_water_destroy": (None, [_P]),
     "jfgpu_water_init": (ctypes.c_int, [_P, _P, _I64, _I64, _P]),
-    "jfgpu_water_run": (ctypes.c_int, [_P, _P, _P, _P, _I64, _I64, _I64, _P, _I32, _P]),
+    "jfgpu_water_run": (ctypes.c_int, [_P, _P, _P, _P, _I64, _I64, _I64, _D, _D, _P, _I32, _P]),
     "jfgpu_engine_create": (ctypes.c_int, [_P, _I64, _P, ctypes.POINTER(ctypes.c_void_p)]),
     "jfgpu_engine_destroy": (None, [_P]),
     "jfgpu_engine_layout": (ctypes.c_int, [_P, ctypes.POINTER(Layout)]),

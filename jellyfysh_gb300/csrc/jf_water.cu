@@ -39,7 +39,10 @@ struct WaterArgs {
     JfgpuWaterState *state;
     JfgpuEvent *log;
     int64_t chains, first_chain, events;
+    double stop_q, stop_r;  // stop time (inf: none)
 };
+
+constexpr int kStopKind = 1 << 29;  // the winner is the stop time
 
 struct WaterCand {
     double q, r;
@@ -271,6 +274,7 @@ __global__ void __launch_bounds__(256, 2) water_kernel(WaterArgs a) {
     __shared__ int decision;  // 0 rejected, 1 thinning in FP64, 2 accepted
     if (threadIdx.x == 0) {
         s = a.state[chain];
+        s.stopped = 0;
         status = JFGPU_STATUS_OK;
     }
     __syncthreads();
@@ -375,10 +379,28 @@ __global__ void __launch_bounds__(256, 2) water_kernel(WaterArgs a) {
             e.kind = JFGPU_EV_END_OF_CHAIN;
             e.target = s.eoc_new_active;
             if (water_better(e, b)) b = e;
+            if (!isinf(a.stop_q) && !time_lt(b.q, b.r, a.stop_q, a.stop_r)) {  // the stop time wins ties
+                b.q = a.stop_q;
+                b.r = a.stop_r;
+                b.kind = kStopKind;
+                b.target = -1;
+            }
             winner = b;
         }
         __syncthreads();
         best = winner;
+        if (best.kind == kStopKind) {
+            // the end of the run: the active unit time-sliced to the stop time, no event
+            if (threadIdx.x == 0) {
+                const double dt = time_sub(best.q, best.r, s.time_q, s.time_r);
+                for (int c = 0; c < 3; ++c) pos[3 * act + c] = py_mod(pa[c] + (c == d ? w.speed : 0.0) * dt, w.length);
+                s.time_q = best.q;
+                s.time_r = best.r;
+                s.stopped = 1;
+            }
+            __syncthreads();
+            break;
+        }
         // commit: time slice of the active unit (every thread computes the same position; thread 0 stores it)
         {
             const double dt = time_sub(best.q, best.r, s.time_q, s.time_r);
@@ -672,8 +694,8 @@ extern "C" int jfgpu_water_init(void *water, JfgpuWaterState *state, int64_t cha
 }
 
 extern "C" int jfgpu_water_run(void *water, double *positions, const double *charges, JfgpuWaterState *state,
-                               int64_t chains, int64_t first_chain, int64_t events, JfgpuEvent *log,
-                               int32_t warps_per_block, void *stream) {
+                               int64_t chains, int64_t first_chain, int64_t events, double stop_q, double stop_r,
+                               JfgpuEvent *log, int32_t warps_per_block, void *stream) {
     WaterHandle *h = static_cast<WaterHandle *>(water);
     if (!h || chains < 0 || first_chain < 0 || events < 0 || warps_per_block < 0 || warps_per_block > 8)
         return JFGPU_ERROR_ARGUMENT;
@@ -689,6 +711,8 @@ extern "C" int jfgpu_water_run(void *water, double *positions, const double *cha
     a.chains = chains;
     a.first_chain = first_chain;
     a.events = events;
+    a.stop_q = stop_q;
+    a.stop_r = stop_r;
     const size_t shared = water_shared_bytes(h->model.molecules);
     if (shared > 48 * 1024 &&
         cudaFuncSetAttribute(water_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shared) != cudaSuccess)

@@ -18,7 +18,8 @@ A configuration switches to it by naming it in ``[Run]`` and giving its section 
 
 The factory builds the reference's objects exactly as for its own mediator (the constructor's annotations are the
 reference's classes, from which the factory finds their packages); ``jellyfysh_gb300.plugin.plan`` turns them into
-a batch of chains and runs it.  This module is imported by the factory, with the reference present.
+a batch of chains (atoms, or water molecules as composite objects) and runs it.  This module is imported by the
+factory, with the reference present.
 """
 from jellyfysh.activator import Activator
 from jellyfysh.base.exceptions import EndOfRun

@@ -1,11 +1,12 @@
 """Translation of a run configured for the reference into a batch of GPU chains, and its execution.
 
 ``translate`` reads the system from the objects the reference's factory built (setting, initial units, taggers
-with their event handlers and potentials, cell occupancy, far field, chain and run control) into a ``BatchPlan``,
-without running any of the reference's initialisation (whose far-field tables take minutes in Python);
-``run_plan`` executes a plan on the GPU until the end-of-run time.  Configurations outside the engine's scope
-(composite objects, other potentials or taggers) raise ``ConfigurationError``.  Nothing here imports the
-reference: ``translate`` only reads the objects it is given.
+with their event handlers and potentials, cell occupancy, far field, chain and run control) into a ``BatchPlan``
+(atoms) or a ``WaterPlan`` (water molecules as composite objects with factor-type-map taggers), without running any
+of the reference's initialisation (whose far-field tables take minutes in Python); ``run_plan`` executes a plan on
+the GPU until the end-of-run time.  Configurations outside the engines' scope (other potentials, taggers or
+composite objects) raise ``ConfigurationError``.  Nothing here imports the reference: ``translate`` only reads the
+objects it is given.
 """
 import dataclasses
 import math
@@ -62,8 +63,115 @@ def _lennard_jones(potential):
     return float(potential._prefactor), float(potential._characteristic_length)
 
 
+@dataclasses.dataclass
+class WaterPlan:
+    """One configured water system run as `chains` independent chains on the GPU (``jellyfysh_gb300.water``)."""
+    model: Any
+    positions: np.ndarray
+    charges: np.ndarray
+    end_of_run_time: float
+    chains: int = 1
+    mode: str = "mixed"
+    seed: int = 0
+    events_per_launch: int = 256
+
+
+_LIFTINGS = {"InsideFirstLifting": "inside_first", "OutsideFirstLifting": "outside_first",
+             "RatioLifting": "ratio"}
+
+
+def _factor_groups(tagger) -> set:
+    """The factors of a factor-type-map tagger as sorted tuples of leaf numbers
+    (``activator/tagger/factor_type_maps.py:286-352``)."""
+    mapping = tagger._factor_type_map._map
+    return {tuple(sorted(group)) for groups in mapping.values() for group in groups}
+
+
+def _translate_water(state_handler, activator, setting, roots, chains, mode, seed, events_per_launch) -> WaterPlan:
+    """Water molecules of three units (hydrogen, oxygen, hydrogen: unit 1 the oxygen) with harmonic O-H and H-H bonds,
+    Lennard-Jones between the oxygens and one Coulomb factor per pair of molecules, all through
+    ``FactorTypeMapInStateTagger`` (``activator/tagger/factor_type_map_in_state_tagger.py``)."""
+    from jellyfysh_gb300.water import WaterModel
+    if setting.number_of_nodes_per_root_node != 3 or any(len(node.children) != 3 for node in roots):
+        raise ConfigurationError("the water engine runs composite objects of three units")
+    roots = sorted(roots, key=lambda node: node.value.identifier)
+    leaves = [leaf.value for node in roots for leaf in sorted(node.children, key=lambda c: c.value.identifier)]
+    positions = np.array([unit.position for unit in leaves], dtype=np.float64)
+    labels = set().union(*[set(unit.charge or {}) for unit in leaves])
+    if len(labels) != 1:
+        raise ConfigurationError("the water units need exactly one charge: %s" % sorted(labels))
+    label = labels.pop()
+    charges = np.array([float(unit.charge[label]) for unit in leaves])
+    fields = dict(molecules=len(roots), system_length=float(setting.system_length), beta=float(setting.beta),
+                  mode=mode)
+    bonds = {}
+    end_of_run_time = math.inf
+    for tagger in activator._taggers:
+        tagger_name = _name(tagger)
+        handler = tagger._event_handler_to_copy
+        handler_name = _name(handler)
+        if tagger_name == "FactorTypeMapInStateTagger":
+            groups = _factor_groups(tagger)
+            if handler_name == "TwoLeafUnitEventHandler":
+                potential = handler._potential
+                if _name(potential) == "DisplacedEvenPowerPotential":
+                    if int(potential._power) != 2:
+                        raise ConfigurationError("the water engine's bonds are harmonic (power 2)")
+                    for group in groups:
+                        if group not in ((0, 1), (1, 2), (0, 2)):
+                            raise ConfigurationError("bond factor %s is not within one water molecule" % (group,))
+                        bonds[group] = (float(potential._equilibrium_separation), float(potential._prefactor))
+                elif _potential_kind(potential) == "LennardJones":
+                    if groups != {(1, 4)}:
+                        raise ConfigurationError("the water engine's Lennard-Jones acts between the oxygens (1, 4)")
+                    fields["lj_prefactor"], fields["lj_sigma"] = _lennard_jones(potential)
+                else:
+                    raise ConfigurationError("potential %s is not on the water engine's path" % _name(potential))
+            elif handler_name == "TwoCompositeObjectSummedBoundingPotentialEventHandler":
+                if groups != {(0, 1, 2, 3, 4, 5)}:
+                    raise ConfigurationError("the water engine's Coulomb factor takes both molecules whole")
+                mic, bound = handler._potential, handler._bounding_potential
+                if _potential_kind(mic) != "MergedImageCoulomb" or \
+                        _potential_kind(bound) != "InversePowerCoulombBounding":
+                    raise ConfigurationError("the Coulomb factor runs merged-image Coulomb with its inverse-power bound")
+                lifting = _name(handler._lifting).replace("Gpu", "", 1) if _name(handler._lifting).startswith(
+                    "Gpu") else _name(handler._lifting)
+                if lifting not in _LIFTINGS:
+                    raise ConfigurationError("lifting scheme %s is not on the water engine's path" % lifting)
+                fields.update(coulomb_prefactor=float(mic._prefactor), alpha=float(mic._alpha),
+                              fourier_cutoff=int(mic._fourier_cutoff), position_cutoff=int(mic._position_cutoff),
+                              bound_prefactor=float(bound._prefactor), lifting=_LIFTINGS[lifting])
+            else:
+                raise ConfigurationError("factor event handler %s is not on the water engine's path" % handler_name)
+        elif handler_name == "SingleIndependentActivePeriodicDirectionEndOfChainEventHandler":
+            fields["chain_time"] = float(handler._chain_time)
+        elif handler_name == "InitialChainStartOfRunEventHandler":
+            velocity = list(handler._initial_velocity)
+            direction = [i for i, v in enumerate(velocity) if v != 0.0]
+            identifier = tuple(handler._initial_active_identifier)
+            if len(direction) != 1 or velocity[direction[0]] <= 0.0 or len(identifier) != 2:
+                raise ConfigurationError("the water engine starts one active unit moving along +x, +y or +z")
+            fields.update(initial_direction=direction[0], speed=float(velocity[direction[0]]),
+                          initial_active=3 * int(identifier[0]) + int(identifier[1]))
+        elif handler_name == "FinalTimeEndOfRunEventHandler":
+            end_of_run_time = float(handler._event_time.quotient + handler._event_time.remainder)
+        else:
+            raise ConfigurationError("tagger %s with %s is not on the water engine's path" % (tagger_name,
+                                                                                           handler_name))
+    if set(bonds) != {(0, 1), (1, 2), (0, 2)} or bonds[(0, 1)] != bonds[(1, 2)]:
+        raise ConfigurationError("the water engine needs the two O-H bonds (alike) and the H-H bond")
+    fields["oh_r0"], fields["oh_prefactor"] = bonds[(0, 1)]
+    fields["hh_r0"], fields["hh_prefactor"] = bonds[(0, 2)]
+    for key in ("chain_time", "initial_direction", "lj_prefactor", "coulomb_prefactor"):
+        if key not in fields:
+            raise ConfigurationError("the water system lacks %s" % key)
+    return WaterPlan(model=WaterModel(**fields), positions=positions, charges=charges,
+                     end_of_run_time=end_of_run_time, chains=int(chains), mode=mode, seed=int(seed),
+                     events_per_launch=int(events_per_launch))
+
+
 def translate(state_handler, activator, setting, chains: int = 1, mode: str = "mixed", seed: int = 0,
-              events_per_launch: int = 256) -> BatchPlan:
+              events_per_launch: int = 256):
     """Read a configured run from the reference's constructed objects (the hypercubic setting module
     ``setting/hypercubic_setting.py``, taggers ``activator/tagger/*.py``, event
     handlers ``event_handler/*.py``, potentials ``potential/*.py``, occupancy
@@ -74,9 +182,8 @@ def translate(state_handler, activator, setting, chains: int = 1, mode: str = "m
     length = float(setting.system_length)
     beta = float(setting.beta)
     roots = state_handler.extract_global_state()
-    for node in roots:
-        if node.children:
-            raise ConfigurationError("composite objects are not on the GPU engine's path")
+    if any(node.children for node in roots):
+        return _translate_water(state_handler, activator, setting, roots, chains, mode, seed, events_per_launch)
     roots = sorted(roots, key=lambda node: node.value.identifier)
     positions = np.array([node.value.position for node in roots], dtype=np.float64)
     n = len(roots)
@@ -175,12 +282,24 @@ def translate(state_handler, activator, setting, chains: int = 1, mode: str = "m
                      chains=int(chains), mode=mode, seed=int(seed), events_per_launch=int(events_per_launch))
 
 
-def run_plan(plan: BatchPlan, stop_time: Optional[float] = None, device: str = "cuda:0"):
-    """Advance every chain of the plan to `stop_time` (default: the end-of-run time); returns the ChainBatch."""
+def run_plan(plan, stop_time: Optional[float] = None, device: str = "cuda:0"):
+    """Advance every chain of the plan to `stop_time` (default: the end-of-run time); returns the ChainBatch or
+    WaterBatch."""
     from jellyfysh_gb300 import ChainBatch
     t_stop = plan.end_of_run_time if stop_time is None else float(stop_time)
     if math.isinf(t_stop):
         raise ConfigurationError("the run needs a finite end-of-run time")
+    if isinstance(plan, WaterPlan):
+        import torch
+        from jellyfysh_gb300.water import WaterBatch
+        with torch.cuda.device(torch.device(device)):
+            batch = WaterBatch(plan.model, np.repeat(plan.positions[None], plan.chains, axis=0), seed=plan.seed,
+                               charges=plan.charges)
+            while True:
+                batch.run(plan.events_per_launch, stop_time=t_stop)
+                batch.check_status()
+                if (batch.states()["stopped"] == 1).all():
+                    return batch
     charges = None if plan.charges is None else [plan.charges] * plan.chains
     batch = ChainBatch([plan.spec] * plan.chains, [plan.positions] * plan.chains, charges, seed=plan.seed,
                        device=device)

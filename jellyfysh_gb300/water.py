@@ -12,6 +12,7 @@ come first are solved in FP64, and the thinning of a Coulomb event first tries F
 error bound; every outcome is the exact mode's.
 """
 import ctypes
+import math
 from dataclasses import asdict, dataclass
 from typing import Optional
 
@@ -25,7 +26,8 @@ LIFTING = {"inside_first": _lib.LIFTING_INSIDE_FIRST, "outside_first": _lib.LIFT
            "ratio": _lib.LIFTING_RATIO}
 STATE_DTYPE = np.dtype([("time_q", np.float64), ("time_r", np.float64), ("eoc_q", np.float64), ("eoc_r", np.float64),
                         ("active", np.int32), ("direction", np.int32), ("eoc_new_active", np.int32),
-                        ("status", np.int32), ("events", np.int64), ("composite_events", np.int64),
+                        ("status", np.int32), ("stopped", np.int32), ("reserved", np.int32), ("events", np.int64),
+                        ("composite_events", np.int64),
                         ("composite_accepted", np.int64), ("bond_events", np.int64), ("lj_events", np.int64),
                         ("eoc_events", np.int64), ("thinning_exact", np.int64), ("refined_items", np.int64)])
 MODES = {"exact": _lib.MODE_EXACT, "mixed": _lib.MODE_MIXED}
@@ -116,17 +118,19 @@ class WaterBatch:
     def _stream(self):
         return self._torch.cuda.current_stream(self.device).cuda_stream
 
-    def run(self, events: int, record: bool = False):
-        """Advance every chain by ``events`` events; with ``record`` returns the event log [chains][events]."""
+    def run(self, events: int, record: bool = False, stop_time: Optional[float] = None):
+        """Advance every chain by up to ``events`` events, stopping at ``stop_time`` (the active unit time-sliced to
+        it, ``stopped`` set); with ``record`` returns the event log [chains][events] (zero rows after a stop)."""
         torch = self._torch
         log = None
         if record:
             log = torch.zeros(max(self.chains * events, 1) * EVENT_DTYPE.itemsize, dtype=torch.uint8,
                               device=self.device)
+        stop_q, stop_r = (math.inf, math.inf) if stop_time is None else divmod(float(stop_time), 1.0)
         _lib.check(self.lib.jfgpu_water_run(self._handle, self.positions_dev.data_ptr(), self.charges_dev.data_ptr(),
                                             self.state_dev.data_ptr(), self.chains, self.first_chain, int(events),
-                                            log.data_ptr() if record else None, self.warps_per_block,
-                                            self._stream()), "jfgpu_water_run")
+                                            stop_q, stop_r, log.data_ptr() if record else None,
+                                            self.warps_per_block, self._stream()), "jfgpu_water_run")
         if not record:
             return None
         host = log.cpu().numpy()[:self.chains * events * EVENT_DTYPE.itemsize]

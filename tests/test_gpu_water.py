@@ -116,3 +116,38 @@ def test_water_replicas_of_the_batched_workload_run_clean(water):
     assert (states["events"] == 100).all()
     final = batch.positions()
     assert np.isfinite(final).all() and (final >= 0).all() and (final < model.system_length).all()
+
+
+def test_stop_time_time_slices_the_active_unit(water):
+    """A run with a stop time ends like the reference's end of run: the events before it, then the active unit
+    time-sliced to the stop time; the drop-in plan runs every chain to its end-of-run time."""
+    spec, initial, charges, events, final = load_water("water_n8")
+    model = water.WaterModel.from_spec(spec)
+    k = 150
+    t_k = events["time_q"][k] + events["time_r"][k]
+    t_next = events["time_q"][k + 1] + events["time_r"][k + 1]
+    stop = 0.5 * (t_k + t_next)
+    before = water.WaterBatch(model, initial[None], seed=spec["seed"], charges=charges)
+    before.run(k + 1)
+    stopped = water.WaterBatch(model, initial[None], seed=spec["seed"], charges=charges)
+    stopped.run(1000, stop_time=stop)
+    stopped.check_status()
+    state = stopped.states()[0]
+    assert state["stopped"] == 1 and state["events"] == k + 1
+    assert (state["time_q"], state["time_r"]) == divmod(stop, 1.0)
+    expected = before.positions()[0].copy()
+    active, direction = int(state["active"]), int(state["direction"])
+    dt = (divmod(stop, 1.0)[0] - events["time_q"][k]) + divmod(stop, 1.0)[1] - events["time_r"][k]
+    expected[active, direction] = (expected[active, direction] + dt) % model.system_length
+    assert np.allclose(stopped.positions()[0], expected, rtol=0, atol=REL * model.system_length)
+    # a second call at the same stop time does nothing
+    stopped.run(10, stop_time=stop)
+    assert stopped.states()[0]["events"] == k + 1
+
+    from jellyfysh_gb300.plugin.plan import WaterPlan, run_plan
+    plan = WaterPlan(model=model, positions=initial, charges=charges, end_of_run_time=stop, chains=3, seed=spec["seed"],
+                     events_per_launch=64)
+    batch = run_plan(plan)
+    states = batch.states()
+    assert (states["stopped"] == 1).all() and (states["time_q"] + states["time_r"] == stop).all()
+    assert states["events"][0] == k + 1  # chain 0 draws the keys of the recorded trajectory

@@ -43,7 +43,7 @@ def test_water_model_matches_the_header_layouts():
     import ctypes
     from jellyfysh_gb300 import _lib, water
     assert ctypes.sizeof(_lib.WaterDesc) == 144
-    assert water.STATE_DTYPE.itemsize == 112  # JfgpuWaterState: 4 doubles, 4 int32, 8 int64
+    assert water.STATE_DTYPE.itemsize == 120  # JfgpuWaterState: 4 doubles, 6 int32, 8 int64
     model = water.WaterModel.from_spec({"molecules_per_side": 2, "system_length": 6.21, "lifting": "ratio",
                                         "unused": 1})
     assert model.molecules == 8 and model.system_length == 6.21

@@ -9,7 +9,7 @@ selects the GPU classes by name:
 * ``lifting = gpu_inside_first_lifting`` (and the other schemes) builds the GPU lifting inside the reference's
   composite-object event handler;
 * ``mediator = gpu_chain_batch_mediator`` builds the drop-in mediator from the same object graph, and its batch
-  plan is the system of the configuration (the chain parameters that the GPU trajectory tests run, the injected
+  plan (atoms) or water plan (water molecules through factor-type-map taggers) is the system of the configuration (the chain parameters that the GPU trajectory tests run, the injected
   initial positions and charges).
 """
 import configparser
@@ -172,6 +172,61 @@ def test_mediator_translates_the_reference_configuration(name):
     assert np.array_equal(np.array(plan["positions"]), initial)
     if charges is not None:
         assert np.array_equal(np.array(plan["charges"]), charges)
+    assert plan["end_of_run_time"] == 1e9
+
+
+def translate_water_configuration(name):
+    """The reference's factory builds the drop-in mediator from the water configuration of the water trajectories
+    (run in a child); returns the water plan."""
+    factory, camel = _reference()
+    sys.path.insert(0, os.path.join(ROOT, "tests", "golden"))
+    import tempfile
+    import make_water_trajectories as waters
+    from tests.water_cases import load_water
+    spec, initial, charges, events, final = load_water(name)
+    scratch = tempfile.mkdtemp()
+    factor_file = os.path.join(scratch, "factors.txt")
+    with open(factor_file, "w") as handle:
+        handle.write(waters.FACTORS)
+    text = waters.config_text(spec, factor_file)
+    text = text.replace("mediator = single_process_mediator", "mediator = gpu_chain_batch_mediator")
+    text = text.replace("[SingleProcessMediator]", "[GpuChainBatchMediator]\nchains = 4\nmode = exact\nseed = 7")
+    config = configparser.ConfigParser()
+    config.read_string(text)
+    from jellyfysh.base.node import Node
+    from jellyfysh.base.particle import Particle
+    from jellyfysh.input_output_handler.input_handler.random_node_creator import water_random_node_creator
+    queue = list(range(len(initial) // 3))
+
+    def fill_root_node(self, node):
+        m = queue.pop(0)
+        for t in range(3):
+            node.add_child(Node(Particle([float(v) for v in initial[3 * m + t]],
+                                         {"electric_charge": float(charges[3 * m + t])})))
+        node.value = Particle(position=[float(v) for v in initial[3 * m + 1]])
+    water_random_node_creator.WaterRandomNodeCreator.fill_root_node = fill_root_node
+    factory.build_from_config(config, camel(config.get("Run", "setting")), "jellyfysh.setting")
+    mediator = factory.build_from_config(config, camel(config.get("Run", "mediator")), "jellyfysh.mediator")
+    plan = mediator.plan
+    return {"type": type(plan).__name__, "model": dataclasses.asdict(plan.model), "positions": plan.positions.tolist(),
+            "charges": plan.charges.tolist(), "end_of_run_time": plan.end_of_run_time, "chains": plan.chains,
+            "mode": plan.mode, "seed": plan.seed}
+
+
+@pytest.mark.parametrize("name", ["water_n8"])
+def test_mediator_translates_the_reference_water_configuration(name):
+    from tests.water_cases import load_water
+    spec, initial, charges, events, final = load_water(name)
+    plan = _in_child("translate_water_configuration", name)
+    assert plan["type"] == "WaterPlan" and (plan["chains"], plan["mode"], plan["seed"]) == (4, "exact", 7)
+    model = plan["model"]
+    for key in ("system_length", "beta", "chain_time", "speed", "oh_r0", "oh_prefactor", "hh_r0", "hh_prefactor",
+                "lj_prefactor", "lj_sigma", "coulomb_prefactor", "bound_prefactor", "alpha", "fourier_cutoff",
+                "position_cutoff", "initial_direction", "initial_active", "lifting"):
+        assert model[key] == spec[key], key
+    assert model["molecules"] == spec["molecules_per_side"] ** 3 and model["mode"] == "exact"
+    assert np.array_equal(np.array(plan["positions"]), initial)
+    assert np.array_equal(np.array(plan["charges"]), charges)
     assert plan["end_of_run_time"] == 1e9
 
 
