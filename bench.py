@@ -12,7 +12,10 @@ Arms:
     default            the GPU engine (value = device-timed events/s; e2e = through ChainBatch with host buffers)
     --impl reference   the CPU oracle (a C restatement of the reference's event loop) on all host threads
 
-Second workload (``--workload water``, a parity configuration measured beside the headline, not the headline):
+Other workloads (parity configurations measured beside the headline, not the headline):
+    ``--workload coulomb``: 1024 replicas of 32 point charges (16 of each sign) with a hard core of radius 0.05 in the
+    unit cube, beta = 1, merged-image Coulomb bounded by the inverse-power bound, cell veto on 8^3 cells.
+    ``--workload water``:
     512 independent chains of 64 flexible water molecules (12.42 A box, 300 K, O-H and H-H harmonic bonds,
     Lennard-Jones on oxygen, merged-image Coulomb between molecules with the summed inverse-power Coulomb bound and
     inside-first lifting), FP64 (thinning screened in FP32 with an error bound), one block per chain; seeded lattices
@@ -39,6 +42,10 @@ METRIC = "events/s on 1 GB300, batched mixed-precision vs plain FP64 at <=1e-9 r
 WORKLOAD = dict(workload="lennard_jones_chains_4096x1024_cell_bounding", chains=4096, n=1024, density=0.8,
                 beta=1.0 / 1.2, cells_per_side=12, neighbor_layers=3, chain_time=2.0, far="cell_bounding",
                 jitter=0.05, estimator_points=10, estimator_prefactor=1.5)
+COULOMB_WORKLOAD = dict(workload="coulomb_replicas_1024x32_cell_veto", chains=1024, n=32, hard_core_radius=0.05,
+                        system_length=1.0, beta=1.0, cells_per_side=8, neighbor_layers=1, chain_time=0.7,
+                        coulomb_prefactor=1.0, bound_prefactor=1.5837, ewald_alpha=3.45, fourier_cutoff=6,
+                        position_cutoff=2, far="cell_veto", estimator_points=10, estimator_prefactor=1.0)
 WATER_WORKLOAD = dict(workload="water_chains_512x64_molecular_coulomb", chains=512, molecules=64,
                       system_length=12.42, temperature_kelvin=300.0, chain_time=2.0, lifting="inside_first")
 NEAR_CELLS = (2 * WORKLOAD["neighbor_layers"] + 1) ** 3  # cells scanned for pair candidates per event
@@ -62,13 +69,57 @@ def parse():
     p.add_argument("--groups", type=int, default=1, help="chain groups on streams of their own (0 = autotune)")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-fp64", action="store_true")
-    p.add_argument("--workload", default="lennard_jones", choices=["lennard_jones", "water"])
+    p.add_argument("--workload", default="lennard_jones", choices=["lennard_jones", "coulomb", "water"])
     args = p.parse_args()
     if args.workload == "water" and "--chains" not in sys.argv:
         args.chains = WATER_WORKLOAD["chains"]
     if args.workload == "water" and "--events" not in sys.argv:
         args.events = 32
+    if args.workload == "coulomb" and "--chains" not in sys.argv:
+        args.chains = COULOMB_WORKLOAD["chains"]
     return args
+
+
+def workload_of(args):
+    return COULOMB_WORKLOAD if args.workload == "coulomb" else WORKLOAD
+
+
+def metric_of(args):
+    return "events/s on 1 GB300, batched Coulomb replicas" if args.workload == "coulomb" else METRIC
+
+
+def data_of(args):
+    if args.workload == "coulomb":
+        return "synthetic: seeded random sequential addition of +-1 charges with a hard core"
+    return "synthetic: seeded simple-cubic lattice + uniform jitter"
+
+
+def make_coulomb_workload(chains, seed_offset=0):
+    """Replicas of 32 point charges (16 of each sign) with a hard core in the unit cube, cell veto on 8^3 cells."""
+    from jellyfysh_gb300 import ChainSpec, systems
+    w = COULOMB_WORKLOAD
+    rng = np.random.default_rng(4321 + seed_offset)
+    specs, positions = [], []
+    for c in range(chains):
+        specs.append(ChainSpec(n=w["n"], system_length=w["system_length"], cells_per_side=w["cells_per_side"],
+                               neighbor_layers=w["neighbor_layers"], potential="coulomb", far=w["far"],
+                               hs_radius=w["hard_core_radius"], beta=w["beta"], chain_time=w["chain_time"],
+                               coulomb_prefactor=w["coulomb_prefactor"], bound_prefactor=w["bound_prefactor"],
+                               ewald_alpha=w["ewald_alpha"], fourier_cutoff=w["fourier_cutoff"],
+                               position_cutoff=w["position_cutoff"], estimator_points=w["estimator_points"],
+                               estimator_prefactor=w["estimator_prefactor"], initial_active=int(rng.integers(w["n"])),
+                               initial_direction=int(rng.integers(3))))
+        positions.append(systems.random_sequential_addition(w["n"], w["hard_core_radius"], w["system_length"], rng))
+    charges = [systems.alternating_charges(w["n"])] * chains
+    return specs, positions, charges, w["system_length"]
+
+
+def build_workload(args, chains, seed_offset=0):
+    """(specs, positions, charges or None, box length) of the selected atomic workload."""
+    if args.workload == "coulomb":
+        return make_coulomb_workload(chains, seed_offset)
+    specs, positions, length = make_workload(chains, seed_offset)
+    return specs, positions, None, length
 
 
 def make_workload(chains, seed_offset=0):
@@ -153,20 +204,30 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-def cpu_chains(threads, pool, seed_offset=99):
+def cpu_chains(threads, pool, seed_offset=99, args=None):
     """One oracle chain (C restatement of the reference's event loop) of the workload per host thread."""
     import oracle
-    specs, positions, length = make_workload(threads, seed_offset=seed_offset)
+    if args is not None and args.workload == "coulomb":
+        specs, positions, charges, _ = make_coulomb_workload(threads, seed_offset=seed_offset)
+    else:
+        specs, positions, _ = make_workload(threads, seed_offset=seed_offset)
+        charges = None
+    potentials = {"hard_sphere": oracle.POT_HARD_SPHERE, "lennard_jones": oracle.POT_LENNARD_JONES,
+                  "coulomb": oracle.POT_COULOMB}
+    fars = {"none": oracle.FAR_NONE, "cell_veto": oracle.FAR_CELL_VETO, "cell_bounding": oracle.FAR_CELL_BOUNDING}
     systems = []
     for c, spec in enumerate(specs):
         systems.append(oracle.make_system(
             n=spec.n, system_length=spec.system_length, cells_per_side=spec.cells_per_side,
             neighbor_layers=spec.neighbor_layers, max_occupants=1, beta=spec.beta, chain_time=spec.chain_time,
             initial_active=spec.initial_active, initial_direction=spec.initial_direction,
-            potential=oracle.POT_LENNARD_JONES, far=oracle.FAR_CELL_BOUNDING,
-            estimator_points=spec.estimator_points, estimator_prefactor=spec.estimator_prefactor,
-            rng_key=oracle.chain_key(99, c)))
-    return list(pool.map(lambda i: oracle.Chain(systems[i], positions[i]), range(len(systems))))
+            potential=potentials[spec.potential], far=fars[spec.far], hs_radius=spec.hs_radius,
+            lj_prefactor=spec.lj_prefactor, lj_sigma=spec.lj_sigma, coulomb_prefactor=spec.coulomb_prefactor,
+            bound_prefactor=spec.bound_prefactor, ewald_alpha=spec.ewald_alpha, fourier_cutoff=spec.fourier_cutoff,
+            position_cutoff=spec.position_cutoff, estimator_points=spec.estimator_points,
+            estimator_prefactor=spec.estimator_prefactor, rng_key=oracle.chain_key(99, c)))
+    return list(pool.map(lambda i: oracle.Chain(systems[i], positions[i], None if charges is None else charges[i]),
+                         range(len(systems))))
 
 
 def cpu_run(pool, chains, seconds, chunk=500):
@@ -199,7 +260,7 @@ def reference_arm(args):
     # each step a bounded sample: the timed steps take about 90 s of wall time in total
     seconds = max(0.2, min(3.0, 90.0 / max(args.steps, 1)))
     with concurrent.futures.ThreadPoolExecutor(max_workers=threads) as pool:
-        chains = cpu_chains(threads, pool)
+        chains = cpu_chains(threads, pool, args=args)
         for _ in range(args.warmup):
             cpu_run(pool, chains, 0.5)
         total_events, total_time = 0, 0.0
@@ -208,12 +269,12 @@ def reference_arm(args):
             total_events += done
             total_time += elapsed
     value = total_events / total_time
-    config = dict(WORKLOAD)
+    config = dict(workload_of(args))
     config["sample"] = "%d chains (one per host thread) x %.0f s of events per step" % (threads, seconds)
-    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "events/s", "n_gpus": args.gpus,
+    line = {"impl": "reference", "metric": metric_of(args), "value": value, "unit": "events/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * total_time / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic: seeded simple-cubic lattice + uniform jitter", "config": config,
+            "data": data_of(args), "config": config,
             "cpu_baseline": {"value": value, "unit": "events/s", "cores": threads, "kind": "port",
                              "per_core": value / threads, "sample": config["sample"]},
             "e2e": {"value": value, "unit": "events/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -251,8 +312,8 @@ def gpu_arm(args):
     if world > 1:
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     device = torch.device("cuda", local)
-    specs, positions, length = make_workload(args.chains, seed_offset=rank)
-    batch = ChainBatch(specs, positions, seed=1000 + rank, device="cuda:%d" % local)
+    specs, positions, charges, length = build_workload(args, args.chains, seed_offset=rank)
+    batch = ChainBatch(specs, positions, charges, seed=1000 + rank, device="cuda:%d" % local)
     stream = torch.cuda.current_stream(device)
     if args.block_warps and args.groups:
         warps, groups = args.block_warps, args.groups
@@ -350,23 +411,28 @@ def gpu_arm(args):
     # roofline of the screening kernel, which reads the neighbourhood: algorithmic bytes per event (occupancy of the
     # nearby cells, FP32 position and identifier of every pair candidate, active position write, cell index and time)
     # times the events of one launch, over its mean CUDA-event duration on its stream in the timed region
-    screen = kernel_times["screen"]
-    screen_launches = max(screen["launches"], 1)  # the timed launches
-    events_per_launch = events_done / max(launches / 3, 1)  # three kernels per event round and chain group
+    # (Coulomb replicas run the warp-per-chain FP64 kernel, one launch per step reading FP64 positions and charges)
+    coulomb = args.workload == "coulomb"
+    dominant = kernel_times["chains" if coulomb else "screen"]
+    dominant_launches = max(dominant["launches"], 1)  # the timed launches
+    # three kernels per event round and chain group (mixed rounds); one launch per step (FP64 kernel)
+    events_per_launch = events_done / max(launches if coulomb else launches / 3, 1)
     nb = candidates / max(events_done, 1)
-    bytes_per_event = 4 * NEAR_CELLS + 12 * nb + 4 * nb + 32
-    screen_s = screen["ms"] / screen_launches / 1000.0
-    achieved = bytes_per_event * events_per_launch / screen_s / 1e9
+    near_cells = (2 * specs[0].neighbor_layers + 1) ** 3
+    bytes_per_event = 4 * near_cells + (24 + 8 + 4) * nb + 32 if coulomb else 4 * near_cells + 12 * nb + 4 * nb + 32
+    dominant_s = dominant["ms"] / dominant_launches / 1000.0
+    achieved = bytes_per_event * events_per_launch / dominant_s / 1e9
     peak, peak_kind = measured_peaks()
-    traffic = None if NCU_TRAFFIC_PER_EVENT is None else NCU_TRAFFIC_PER_EVENT * events_per_launch
+    traffic = None if NCU_TRAFFIC_PER_EVENT is None or coulomb else NCU_TRAFFIC_PER_EVENT * events_per_launch
     total_kernel_ms = sum(v["ms"] for v in kernel_times.values()) or 1.0
     kernels = {name: {"launches": v["launches"], "ms_per_launch": v["ms"] / max(v["launches"], 1),
                       "share": v["ms"] / total_kernel_ms}
                for name, v in kernel_times.items() if v["launches"]}
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                "traffic": traffic, "peak_source": peak_kind, "kernel": "jf::screen_kernel<1, 2>",
+                "traffic": traffic, "peak_source": peak_kind,
+                "kernel": "jf::chains_kernel<-1, -1>" if coulomb else "jf::screen_kernel<1, 2>",
                 "bytes_per_event": bytes_per_event, "events_per_launch": events_per_launch,
-                "ms_per_launch": screen_s * 1000.0, "neighbours_per_event": nb,
+                "ms_per_launch": dominant_s * 1000.0, "neighbours_per_event": nb,
                 "refined_per_event": refined / max(events_done, 1), "fallback_events": fallbacks,
                 "kernels": kernels}
     cpu = None
@@ -374,22 +440,22 @@ def gpu_arm(args):
         import concurrent.futures
         threads = host_threads()
         with concurrent.futures.ThreadPoolExecutor(max_workers=threads) as pool:
-            chains = cpu_chains(threads, pool)
+            chains = cpu_chains(threads, pool, args=args)
             cpu_run(pool, chains, 0.5)
             done, elapsed = cpu_run(pool, chains, CPU_SECONDS)
         cpu = {"value": done / elapsed, "unit": "events/s", "cores": threads, "kind": "port",
                "per_core": done / elapsed / threads,
                "sample": "%d chains of the workload (one per host thread), %d events in %.1f s"
                          % (threads, done, elapsed)}
-    config = dict(WORKLOAD)
+    config = dict(workload_of(args))
     config.update(chains=args.chains, events_per_chain_per_step=args.events, block_warps=warps, chain_groups=groups,
                   l2="inputs larger than L2 (working set %.0f MB)" % (sum(
                       t.numel() * t.element_size() for t in batch.state_tensors()) / 1e6),
                   parallelism="replicas" if world > 1 else "single GPU")
-    line = {"metric": METRIC, "value": value, "unit": "events/s", "n_gpus": world, "steps": args.steps,
+    line = {"metric": metric_of(args), "value": value, "unit": "events/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
-            "data": "synthetic: seeded simple-cubic lattice + uniform jitter", "config": config,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64" if coulomb else "f32+f64",
+            "data": data_of(args), "config": config,
             "e2e": {"value": e2e_value, "unit": "events/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "roofline": roofline, "cpu_baseline": cpu, "gpu_launches": launches, "clocks": clocks.summary(),
             "fp64_one_chain_per_launch": fp64}

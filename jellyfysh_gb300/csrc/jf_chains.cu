@@ -1630,6 +1630,10 @@ cudaError_t launch_run(const EngineView &view, const JfgpuBuffers &b, long long 
     if (warps < 1) warps = 1;
     if (warps > 8) warps = 8;
     if (count < warps) warps = (int)count;
+    // merged-image Coulomb chains have no FP32 screen in the round kernels (their resolve thread would solve the
+    // whole event serially, 32 chains diverging in a warp): a batch of them runs the warp-per-chain FP64 kernel in
+    // either mode, with the same events
+    if (mode == JFGPU_MODE_MIXED && uniform_potential == JFGPU_POT_COULOMB) mode = JFGPU_MODE_EXACT;
     if (mode == JFGPU_MODE_MIXED) {
         // groups of at least one block of warps each; the event log stays on the caller's stream
         int n_groups = plan.groups;
