@@ -26,6 +26,7 @@
 #include <cuda_runtime.h>
 
 #include "jf_engine.cuh"
+#include "jf_composite.cuh"
 #include "jf_screen.cuh"
 
 namespace jf {
@@ -109,6 +110,9 @@ struct WarpState {
     double lift_sum;
     long long events, warnings, fallbacks, candidates, refined, liftings;
     int active, direction, eoc_new, occ_active, occ_cell, n_surplus, status, stop;
+    // the merged-image thinning derivative of the event against unit real_target, when the warp computed it
+    double real_value = 0.0;
+    int real_target = -1;
 };
 
 struct RunArgs {
@@ -397,9 +401,53 @@ __device__ inline int real_rate(const RunArgs &A, const ChainDev &ch, const Spec
         out = mul_speed(ch, value);
         return JFGPU_STATUS_OK;
     }
+    if (w.real_target == t) {  // shared by the warp before the commit (warp_real_rate)
+        out = w.real_value;
+        return JFGPU_STATUS_OK;
+    }
     out = mul_speed(ch, mic_std_derivative(sp.mic, ch.coulomb_prefactor, w.direction, s, charge_of(A, ch, w.active),
                                            charge_of(A, ch, t)));
     return JFGPU_STATUS_OK;
+}
+
+// The thinning derivative of a merged-image Coulomb event (bounded pair or cell veto with an occupant) computed by
+// the whole warp before lane 0 commits it: the target and the time-sliced active position as the commit will have
+// them, the sum shared by the lanes (mic_x_warp: the serial sum's terms in another order of additions, within
+// 1e-12).  Every lane calls it; lane 0 stores the value for real_rate.
+__device__ inline void warp_real_rate(const RunArgs &A, const ChainDev &ch, const SpeciesDev &sp, WarpState &w,
+                                      const Cand &best, int lane) {
+    int t = -1;
+    double pa[3] = {0.0, 0.0, 0.0};
+    if (lane == 0) {
+        w.real_target = -1;
+        if (best.kind == JFGPU_EV_BOUNDED)
+            t = best.target;
+        else if (best.kind == JFGPU_EV_CELL_VETO)
+            t = A.occupancy[ch.occ_off + (long long)best.aux * ch.max_occ];
+        if (t >= 0) {
+            const double dt = time_sub(best.q, best.r, w.ts_q, w.ts_r);  // as time_slice
+            for (int k = 0; k < 3; ++k) pa[k] = w.pa[k];
+            pa[w.direction] = py_mod_near(w.pa[w.direction] + ch.speed * dt, ch.L);
+        }
+    }
+    t = __shfl_sync(0xffffffffu, t, 0);
+    if (t < 0) return;
+    for (int k = 0; k < 3; ++k) pa[k] = __shfl_sync(0xffffffffu, pa[k], 0);
+    double pt[3], s[3], p[3];
+    load_pos(A, ch, t, pt);
+    separation64(ch, pa, pt, s);
+    permute3(s, w.direction, p);
+    CompositeModel model;
+    model.mic = sp.mic;
+    model.images = sp.mic_terms;
+    model.n_images = sp.mic_images;
+    model.rows = sp.mic_terms + sp.mic_images;
+    model.n_rows = sp.mic_rows;
+    const double value = mic_x_warp(model, p[0], p[1], p[2], lane);
+    if (lane == 0) {
+        w.real_value = mul_speed(ch, ch.coulomb_prefactor * charge_of(A, ch, w.active) * charge_of(A, ch, t) * value);
+        w.real_target = t;
+    }
 }
 
 // Thinning: accept iff uniform(0, bound) < real rate (event_handler_with_bounding_potential.py:95-101).  For
@@ -1255,6 +1303,7 @@ __global__ void __launch_bounds__(256, JF_CHAIN_MIN_BLOCKS) chains_kernel(RunArg
         w.n_surplus = g.n_surplus;
         w.status = g.status;
         w.stop = 0;
+        w.real_target = -1;
         load_pos(A, ch, w.active, w.pa);
     }
     __syncwarp();
@@ -1280,6 +1329,11 @@ __global__ void __launch_bounds__(256, JF_CHAIN_MIN_BLOCKS) chains_kernel(RunArg
             w.candidates += counted;
             w.refined += refined;
         }
+        if (potential_of<POT>(ch) == JFGPU_POT_COULOMB && sp.mic_terms != nullptr && warp_max_int(status) == 0 &&
+            !(A.has_stop && !time_lt(best.q, best.r, A.stop_q, A.stop_r))) {
+            warp_real_rate(A, ch, sp, w, best, lane);
+            __syncwarp();
+        }
         if (lane == 0) {
             if (status) {
                 w.status = status;
@@ -1294,6 +1348,7 @@ __global__ void __launch_bounds__(256, JF_CHAIN_MIN_BLOCKS) chains_kernel(RunArg
                 if (!st) st = occ_update(A, ch, w);  // the activator's update of the next event
                 if (st) w.status = st;
             }
+            w.real_target = -1;
         }
         __syncwarp();
     }

@@ -36,6 +36,8 @@ struct SpeciesDev {
     const double *bound_lower;   // [cells][3] negated lower bounds
     const float *bound_upper32;  // [cells][3] FP32 copy for the screening
     WalkerDev walker[2][3];      // [upper/lower][direction]
+    const int4 *mic_terms;       // merged-image sum: real-space images, then Fourier rows (mic_x_warp)
+    int mic_images, mic_rows;
 };
 
 struct ChainDev {
@@ -93,6 +95,8 @@ struct LaunchPlan {
 // (merged_image_coulomb_potential.c:77-119) and the device description pointing at their device copy
 std::vector<double> fourier_table(int fc, double alpha, double length);
 MIC make_mic(int fc, int pc, double alpha, double length, const double *fourier);
+// the real-space images and Fourier rows of the merged-image sum, in the reference's order
+void merged_image_terms(int fc, int pc, std::vector<int4> &images, std::vector<int4> &rows);
 // Lennard-Jones and displaced-even-power parameters as the reference's constructors derive them
 MH make_lj(double prefactor, double sigma);
 MH make_displaced(double r0, int power, double prefactor);

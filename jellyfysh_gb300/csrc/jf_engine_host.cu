@@ -284,6 +284,25 @@ std::vector<double> fourier_table(int fc, double alpha, double length) {
     return t;
 }
 
+// the terms of the merged-image sum in the order of merged_image_coulomb_potential.c:205-274: real-space images
+// (i, j, k) with i^2 + j^2 + k^2 <= position_cutoff^2, Fourier rows (i, j, last k) with i >= 1
+void merged_image_terms(int fc, int pc, std::vector<int4> &images, std::vector<int4> &rows) {
+    for (int k = -pc; k < pc + 1; k++) {
+        int cutoff_y = (int)std::sqrt((double)(pc * pc - k * k));
+        for (int j = -cutoff_y; j < cutoff_y + 1; j++) {
+            int cutoff_x = (int)std::sqrt((double)(pc * pc - j * j - k * k));
+            for (int i = -cutoff_x; i < cutoff_x + 1; i++) images.push_back(make_int4(i, j, k, 0));
+        }
+    }
+    for (int i = 1; i < fc + 1; i++) {
+        int cutoff_y = (int)std::sqrt((double)(fc * fc - i * i));
+        for (int j = 0; j < cutoff_y + 1; j++) {
+            int cutoff_x = (int)std::sqrt((double)(fc * fc - i * i - j * j));
+            rows.push_back(make_int4(i, j, cutoff_x, 0));
+        }
+    }
+}
+
 MIC make_mic(int fc, int pc, double alpha, double length, const double *fourier) {
     MIC m;
     m.fourier_cutoff = fc;
@@ -409,6 +428,16 @@ int build_species(JfgpuEngine *e, const JfgpuChainDesc &d, const std::vector<dou
         const double *dev = device_copy(e, table, stream, error);
         if (error) return error;
         sp.mic = make_mic(d.fourier_cutoff, d.position_cutoff, d.ewald_alpha, d.system_length, dev);
+        // the terms of the sum as lists, for the warp-shared evaluation of the thinning derivative
+        std::vector<int4> images, rows;
+        merged_image_terms(d.fourier_cutoff, d.position_cutoff, images, rows);
+        std::vector<int4> terms(images);
+        terms.insert(terms.end(), rows.begin(), rows.end());
+        const int4 *dev_terms = device_copy(e, terms, stream, error);
+        if (error) return error;
+        sp.mic_terms = dev_terms;
+        sp.mic_images = (int)images.size();
+        sp.mic_rows = (int)rows.size();
     }
     if (d.far == JFGPU_FAR_NONE) return JFGPU_OK;
     if (d.max_occupants != 1) return JFGPU_ERROR_ARGUMENT;

@@ -554,25 +554,6 @@ struct WaterHandle {
     int device = -1;
 };
 
-// the terms of the merged-image sum in the order of merged_image_coulomb_potential.c:205-274: real-space images
-// (i, j, k) with i^2 + j^2 + k^2 <= position_cutoff^2, Fourier rows (i, j, last k) with i >= 1
-static void merged_image_terms(int fc, int pc, std::vector<int4> &images, std::vector<int4> &rows) {
-    for (int k = -pc; k < pc + 1; k++) {
-        int cutoff_y = (int)std::sqrt((double)(pc * pc - k * k));
-        for (int j = -cutoff_y; j < cutoff_y + 1; j++) {
-            int cutoff_x = (int)std::sqrt((double)(pc * pc - j * j - k * k));
-            for (int i = -cutoff_x; i < cutoff_x + 1; i++) images.push_back(make_int4(i, j, k, 0));
-        }
-    }
-    for (int i = 1; i < fc + 1; i++) {
-        int cutoff_y = (int)std::sqrt((double)(fc * fc - i * i));
-        for (int j = 0; j < cutoff_y + 1; j++) {
-            int cutoff_x = (int)std::sqrt((double)(fc * fc - i * i - j * j));
-            rows.push_back(make_int4(i, j, cutoff_x, 0));
-        }
-    }
-}
-
 }  // namespace jf
 
 using namespace jf;
