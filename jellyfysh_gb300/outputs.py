@@ -7,8 +7,10 @@ before second, in identifier order), one per line, as Python prints a float.  Th
 reference's operations on the same doubles: the separation ``target - reference`` corrected as
 ``(s + L/2) % L - L/2`` (``setting/hypercubic_setting.py:120-172``) and the norm ``sum(c * c) ** 0.5``
 (``base/vectors.py:29-43``, ``sum`` with CPython 3.12's compensation, ``**`` with the C library's ``pow``), so that
-the reference's analysis scripts read the files unchanged.  Like the reference's writer
-(``output_handler.py:90-125``), the file is written under a temporary name and renamed when closed.
+the reference's analysis scripts read the files unchanged.  ``OxygenSeparationWriter`` writes the water samples of
+``OxygenOxygenSeparationOutputHandler`` (``oxygen_oxygen_separation_output_handler.py:67-88``): the same norms for the
+oxygens, the second unit of every molecule.  Like the reference's writer (``output_handler.py:90-125``), a file is
+written under a temporary name and renamed when closed.
 """
 import os
 import uuid
@@ -63,3 +65,14 @@ class SeparationWriter:
 
     def __exit__(self, *exc):
         self.close()
+
+
+class OxygenSeparationWriter(SeparationWriter):
+    """The reference's oxygen-oxygen separation samples file for water, one sample per ``write`` of the positions of
+    all units (hydrogen, oxygen, hydrogen per molecule)."""
+
+    def write(self, positions: np.ndarray, system_length: float) -> None:
+        units = np.ascontiguousarray(positions, dtype=np.float64).reshape(-1, 3)
+        if len(units) % 3:
+            raise ValueError("water positions come in molecules of three units")
+        super().write(units[1::3], system_length)

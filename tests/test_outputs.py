@@ -6,6 +6,7 @@ with Python floats: separation target - reference corrected by ``(s + L/2) % L -
 printed as Python prints a float (``separation_output_handler.py:75-97``).
 """
 import numpy as np
+import pytest
 
 from jellyfysh_gb300 import outputs
 
@@ -44,3 +45,17 @@ def test_separation_writer_file_layout(tmp_path):
     assert lines[0].startswith("# Run identification hash: ")
     expected = sum((reference_lines(p, length) for p in samples), [])
     assert lines[1:] == expected
+
+
+def test_oxygen_separation_writer_takes_the_second_unit_of_every_molecule(tmp_path):
+    from jellyfysh_gb300 import outputs, systems
+    positions, _ = systems.water_lattice(2, 6.21, 1.0, 1.633, np.random.default_rng(3))
+    path = str(tmp_path / "oo.dat")
+    with outputs.OxygenSeparationWriter(path) as writer:
+        writer.write(positions, 6.21)
+    lines = open(path).read().splitlines()
+    expected = outputs.pair_separation_norms(positions[1::3], 6.21)
+    assert [float(x) for x in lines[1:]] == expected.tolist()
+    with pytest.raises(ValueError):
+        with outputs.OxygenSeparationWriter(str(tmp_path / "bad.dat")) as writer:
+            writer.write(positions[:4], 6.21)

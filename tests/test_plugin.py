@@ -257,6 +257,51 @@ def reference_separation_file(path):
     return positions.tolist()
 
 
+def reference_oxygen_separation_file(path):
+    """The reference's OxygenOxygenSeparationOutputHandler writing one sample of a water configuration (child)."""
+    if TREE not in sys.path:
+        sys.path.insert(0, TREE)
+    import configparser as cp
+    from jellyfysh.base import factory
+    from jellyfysh.base.node import Node
+    from jellyfysh.base.unit import Unit
+    from jellyfysh_gb300 import systems
+    config = cp.ConfigParser()
+    config.read_string("[Run]\nsetting = hypercubic_setting\n[HypercubicSetting]\nsystem_length = 12.42\n"
+                       "beta = 1.0\ndimension = 3\n[OxygenOxygenSeparationOutputHandler]\nfilename = %s\n" % path)
+    factory.build_from_config(config, "HypercubicSetting", "jellyfysh.setting")
+    from jellyfysh import setting
+    positions, _ = systems.water_lattice(4, 12.42, 1.0, 1.633, np.random.default_rng(10))
+    setting.set_number_of_root_nodes(64)
+    setting.set_number_of_nodes_per_root_node(3)
+    setting.set_number_of_node_levels(2)
+    handler = factory.build_from_config(config, "OxygenOxygenSeparationOutputHandler",
+                                        "jellyfysh.input_output_handler.output_handler")
+    roots = []
+    for m in range(64):
+        root = Node(Unit(identifier=(m,), position=[float(v) for v in positions[3 * m + 1]], charge=None))
+        for t in range(3):
+            root.add_child(Node(Unit(identifier=(m, t), position=[float(v) for v in positions[3 * m + t]],
+                                     charge=None)))
+        roots.append(root)
+    handler.write(roots)
+    handler.post_run()
+    return positions.tolist()
+
+
+def test_oxygen_separation_samples_equal_the_reference_output_handler(tmp_path):
+    from jellyfysh_gb300 import outputs
+    reference_path = str(tmp_path / "reference.dat")
+    positions = np.array(_in_child("reference_oxygen_separation_file", reference_path))
+    ours_path = str(tmp_path / "ours.dat")
+    with outputs.OxygenSeparationWriter(ours_path) as writer:
+        writer.write(positions, 12.42)
+    reference = open(reference_path).read().splitlines()
+    ours = open(ours_path).read().splitlines()
+    assert reference[0].startswith("# Run identification hash") and ours[0].startswith("# Run identification hash")
+    assert len(ours) == 1 + 64 * 63 // 2 and reference[1:] == ours[1:]
+
+
 def test_separation_samples_equal_the_reference_output_handler(tmp_path):
     from jellyfysh_gb300 import outputs
     reference_path = str(tmp_path / "reference.dat")
