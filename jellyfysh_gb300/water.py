@@ -12,6 +12,7 @@ come first are solved in FP64, and the thinning of a Coulomb event first tries F
 error bound; every outcome is the exact mode's.
 """
 import ctypes
+import json
 import math
 from dataclasses import asdict, dataclass
 from typing import Optional
@@ -135,6 +136,28 @@ class WaterBatch:
             return None
         host = log.cpu().numpy()[:self.chains * events * EVENT_DTYPE.itemsize]
         return host.view(EVENT_DTYPE).reshape(self.chains, events)
+
+    def checkpoint(self, path: str) -> None:
+        """Write the batch (model, seed, first chain, charges, positions and chain states) to `path` (numpy .npz);
+        ``WaterBatch.restore(path)`` continues it exactly where it stopped (the random numbers are keyed by chain and
+        event)."""
+        self._torch.cuda.synchronize(self.device)
+        np.savez(path, model=json.dumps(asdict(self.model)), seed=self.seed, first_chain=self.first_chain,
+                 warps_per_block=self.warps_per_block, charges=self.charges_dev.cpu().numpy(),
+                 positions=self.positions_dev.cpu().numpy(), state=self.state_dev.cpu().numpy())
+
+    @classmethod
+    def restore(cls, path: str) -> "WaterBatch":
+        data = np.load(path)
+        batch = cls(WaterModel(**json.loads(str(data["model"]))), np.asarray(data["positions"]), seed=int(data["seed"]),
+                    first_chain=int(data["first_chain"]), charges=np.asarray(data["charges"]),
+                    warps_per_block=int(data["warps_per_block"]))
+        state = batch._torch.from_numpy(np.ascontiguousarray(data["state"])).to(batch.device)
+        if state.shape != batch.state_dev.shape:
+            raise ValueError("checkpoint state does not match the batch layout")
+        batch.state_dev.copy_(state)
+        batch._torch.cuda.synchronize(batch.device)
+        return batch
 
     def positions(self) -> np.ndarray:
         return self.positions_dev.cpu().numpy()

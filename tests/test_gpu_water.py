@@ -151,3 +151,22 @@ def test_stop_time_time_slices_the_active_unit(water):
     states = batch.states()
     assert (states["stopped"] == 1).all() and (states["time_q"] + states["time_r"] == stop).all()
     assert states["events"][0] == k + 1  # chain 0 draws the keys of the recorded trajectory
+
+
+def test_checkpoint_and_restore_continue_bit_for_bit(water, tmp_path):
+    model = water.WaterModel()
+    positions = water.lattice_positions(model, 16, 5)
+    straight = water.WaterBatch(model, positions, seed=5)
+    straight.run(300)
+    reference = straight.run(200, record=True)
+    interrupted = water.WaterBatch(model, positions, seed=5)
+    interrupted.run(300)
+    path = str(tmp_path / "water.npz")
+    interrupted.checkpoint(path)
+    interrupted.close()
+    resumed = water.WaterBatch.restore(path)
+    continued = resumed.run(200, record=True)
+    for field in reference.dtype.names:
+        assert np.array_equal(reference[field], continued[field]), field
+    assert np.array_equal(straight.positions(), resumed.positions())
+    assert np.array_equal(straight.states(), resumed.states())
