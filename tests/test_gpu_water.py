@@ -170,3 +170,22 @@ def test_checkpoint_and_restore_continue_bit_for_bit(water, tmp_path):
         assert np.array_equal(reference[field], continued[field]), field
     assert np.array_equal(straight.positions(), resumed.positions())
     assert np.array_equal(straight.states(), resumed.states())
+
+
+@pytest.mark.parametrize("lifting", ["outside_first", "ratio"])
+def test_other_lifting_schemes_match_the_oracle(water, lifting):
+    """The water engine with the outside-first and ratio schemes against the oracle, mixed and exact modes."""
+    chains, events, seed = 24, 300, 61
+    for mode in ("mixed", "exact"):
+        model = water.WaterModel(lifting=lifting, mode=mode)
+        positions = water.lattice_positions(model, chains, seed)
+        batch = water.WaterBatch(model, positions, seed=seed)
+        log = batch.run(events, record=True)
+        batch.check_status()
+        spec = dict(vars(model))
+        for c in (0, 7, 23):
+            reference = oracle.Water(oracle.make_water_system(spec, oracle.chain_key(seed, c)), positions[c],
+                                     model.charges())
+            compare_logs(log[c], reference.run(events), model.system_length)
+        assert (log["kind"] == oracle.EV_COMPOSITE).any() and ((log["kind"] == oracle.EV_COMPOSITE) &
+                                                              (log["accepted"] == 1)).any()
