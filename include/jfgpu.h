@@ -321,7 +321,7 @@ int jfgpu_water_init(void *water, JfgpuWaterState *state, int64_t chains, int64_
  * inf, inf for none): a chain whose next event would come at or after it (the stop wins ties) has its active unit
  * time-sliced to the stop time, `stopped` set and no further event in this call, like the reference's end of run.
  * positions [chains][3 molecules][3] and charges [3 molecules] are device arrays; log [chains][events] (may be
- * null) receives every committed event.  One block of warps_per_block warps runs one chain, 1..8 (0: 4). */
+ * null) receives every committed event.  One block of warps_per_block warps runs one chain, 1..8 (0: 3). */
 int jfgpu_water_run(void *water, double *positions, const double *charges, JfgpuWaterState *state, int64_t chains,
                     int64_t first_chain, int64_t events, double stop_q, double stop_r, JfgpuEvent *log,
                     int32_t warps_per_block, void *stream);

@@ -42,8 +42,6 @@ struct WaterArgs {
     double stop_q, stop_r;  // stop time (inf: none)
 };
 
-constexpr int kStopKind = 1 << 29;  // the winner is the stop time
-
 struct WaterCand {
     double q, r;
     int kind, target;
@@ -94,9 +92,14 @@ __host__ __device__ inline int water_items_max(int molecules) {
     return 3 * (((molecules - 1) + 31) & ~31) + (molecules - 1) + 2;
 }
 
+// chunks of 32 items (one warp's share of a round)
+__host__ __device__ inline int water_chunks_max(int molecules) { return (water_items_max(molecules) + 31) >> 5; }
+
+// per-item lower bounds (float), the item list (int), the taken count of every chunk (int)
 __host__ inline size_t water_shared_bytes(int molecules) {
     const int items = water_items_max(molecules);
-    return (size_t)items * sizeof(double) + (size_t)items * sizeof(int);
+    return (size_t)items * sizeof(float) + (size_t)items * sizeof(int) +
+           (size_t)water_chunks_max(molecules) * sizeof(int);
 }
 
 // one candidate item of the event: the bounded displacement of the active unit against one unit of another molecule
@@ -213,17 +216,14 @@ __device__ inline void water_screen(const WaterModel &w, const double *pos, cons
     }
     other += other >= m;
     const int b = 3 * other + j;
-    const uint64_t bits = draw(key, ev, kRngComposite, (uint32_t)b);
-    // the uniform to within 2^-24 relative, -log(1 - u) with log1pf (conditioning grows near u = 1: left to FP64)
-    const float uniform = (float)(uint32_t)(bits >> 40) * 0x1p-24f;
-    if (uniform > 1.f - 0x1p-6f) {
-        unsafe = true;
-        return;
-    }
-    const float du = -log1pf(-uniform) / w.beta32;
-    // relative error of log1pf, the division and the conditioning below u = 1 - 2^-6, plus the truncation of the
-    // uniform to 24 bits (an absolute 2^-24 in u, 2^-24 / (1 - u) / beta in du)
-    const float du_error = 24.f * 0x1p-24f * du + 2.f * 0x1p-24f / ((1.f - uniform) * w.beta32);
+    // du = -log(1 - u) / beta of the FP64 draw u = n 2^-53 (uniform53): log1pf(-u) below u = 1/2 (u rounded to
+    // FP32 moves -log(1 - u) by at most 2 units of 2^-24 relative there), logf of the exact 1 - u = (2^53 - n) 2^-53
+    // from u = 1/2 (the rounding of the argument moves the logarithm by 2^-24, at least ln 2 in size); with the
+    // errors of log1pf or logf, beta in FP32 and the division, within 8 units, taken as 24
+    const uint64_t n = draw(key, ev, kRngComposite, (uint32_t)b) >> 11;
+    const float du = n < (1ull << 52) ? -log1pf(-(float)n * 0x1p-53f) / w.beta32
+                                      : -logf((float)((1ull << 53) - n) * 0x1p-53f) / w.beta32;
+    const float du_error = 24.f * 0x1p-24f * du;
     double sep[3], p[3];
     periodic_separation(pa, pos + 3 * b, w.length, sep);
     permute3(sep, d, p);
@@ -246,8 +246,12 @@ __device__ inline void shuffle_better(WaterCand &best, int offset) {
 
 // One block of `warps` warps advances one chain.  Candidate items are spread over all threads; the argmin goes
 // through warp shuffles and shared memory; the merged-image sums of a Coulomb out-state go to different warps.
-// At most 128 registers a thread, so that four blocks of 128 threads share an SM and 512 chains run in one wave on
-// the 152 SMs.
+// Decisions that every thread can take from shared values (the bound of the screen, the list offsets, the winner,
+// the thinning) are taken by every thread, so that an event crosses few block barriers: after the screen, after the
+// chunk counts, after the list, after the argmin, after the out-state sums, and at the end of the event.  Thread 0
+// alone updates the chain state, after the last read of it by the other threads (the state of the event is read
+// into registers at its start).  At most 128 registers a thread, so that five blocks of 96 threads (the default
+// three warps) share an SM and 512 chains run in one wave on the 152 SMs.
 __global__ void __launch_bounds__(256, 2) water_kernel(WaterArgs a) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, warps = blockDim.x >> 5;
     const int64_t chain = blockIdx.x;
@@ -259,19 +263,16 @@ __global__ void __launch_bounds__(256, 2) water_kernel(WaterArgs a) {
     const double *charge = a.charges;
     __shared__ JfgpuWaterState s;
     __shared__ WaterCand warp_best[kMaxWarps];
-    __shared__ double warp_upper[kMaxWarps];
-    __shared__ int warp_count[kMaxWarps], warp_count_coulomb[kMaxWarps], warp_count_lj[kMaxWarps];
-    __shared__ double upper;
-    __shared__ int refined;
-    // per-item lower bounds of the screen and the list of items for the FP64 pass (dynamic shared memory)
-    extern __shared__ double dynamic[];
-    double *lower = dynamic;
+    __shared__ float warp_upper[kMaxWarps];
+    // per-item lower bounds of the screen, the list of items for the FP64 pass and the taken count of every chunk of
+    // 32 items (dynamic shared memory)
+    extern __shared__ float dynamic[];
+    float *lower = dynamic;
     int *list = reinterpret_cast<int *>(dynamic + water_items_max(M));
-    __shared__ WaterCand winner;
+    int *chunk_count = list + water_items_max(M);
     __shared__ int status;
     __shared__ double bound[3], pair[3], cross[9];
     __shared__ float pair32[3], error32[3], bound32[3];
-    __shared__ int decision;  // 0 rejected, 1 thinning in FP64, 2 accepted
     if (threadIdx.x == 0) {
         s = a.state[chain];
         s.stopped = 0;
@@ -281,6 +282,12 @@ __global__ void __launch_bounds__(256, 2) water_kernel(WaterArgs a) {
     for (int64_t step = 0; step < a.events && s.status == JFGPU_STATUS_OK; ++step) {
         const int act = s.active, m = act / 3, t = act % 3, d = s.direction;
         const uint64_t ev = (uint64_t)s.events;
+        const double ts_q = s.time_q, ts_r = s.time_r;
+        WaterCand eoc;
+        eoc.q = s.eoc_q;
+        eoc.r = s.eoc_r;
+        eoc.kind = JFGPU_EV_END_OF_CHAIN;
+        eoc.target = s.eoc_new_active;
         double pa[3];
         for (int c = 0; c < 3; ++c) pa[c] = pos[3 * act + c];
         const double ca = charge[act];
@@ -290,61 +297,63 @@ __global__ void __launch_bounds__(256, 2) water_kernel(WaterArgs a) {
         best.kind = 1 << 30;
         best.target = 1 << 30;
         const int items = 3 * (((M - 1) + 31) & ~31) + (t == 1 ? M - 1 : 0) + 2;
-        int st = JFGPU_STATUS_OK;
+        int st = JFGPU_STATUS_OK, refined = 3 * (M - 1) + (t == 1 ? M - 1 : 0) + 2;
         if (w.mode == JFGPU_MODE_MIXED) {
             // phase A: FP32 screen of every item; lower[item] = the earliest time the item may reach (-inf where
-            // the screen cannot judge), upper = the smallest time that some candidate surely reaches (a screened
-            // time plus its error bound, or the end of chain)
-            double mine = INFINITY;
+            // the screen cannot judge), the bound = the smallest time that some candidate surely reaches (a screened
+            // time plus its error bound, or the end of chain); the differences round outwards, towards a smaller
+            // lower bound and a larger bound, so that an item is listed whenever its exact time may come first
+            float mine = INFINITY;
             for (int item = threadIdx.x; item < items; item += blockDim.x) {
                 float t32, e32;
                 bool unsafe, lower_only;
                 water_screen(w, pos, charge, key, ev, item, m, t, d, pa, ca, t32, e32, unsafe, lower_only);
-                lower[item] = unsafe ? -INFINITY : (double)t32 - (double)e32;
-                if (!unsafe && !lower_only) mine = fmin(mine, (double)t32 + (double)e32);
+                lower[item] = unsafe ? -INFINITY : __fsub_rd(t32, e32);
+                if (!unsafe && !lower_only) mine = fminf(mine, __fadd_ru(t32, e32));
             }
-            for (int offset = 16; offset > 0; offset >>= 1) mine = fmin(mine, __shfl_xor_sync(kFull, mine, offset));
+            for (int offset = 16; offset > 0; offset >>= 1) mine = fminf(mine, __shfl_xor_sync(kFull, mine, offset));
             if (lane == 0) warp_upper[warp] = mine;
             __syncthreads();
-            if (threadIdx.x == 0) {
-                double u = time_sub(s.eoc_q, s.eoc_r, s.time_q, s.time_r);
-                for (int k = 0; k < warps; ++k) u = fmin(u, warp_upper[k]);
-                upper = u;
+            float bound_time = __double2float_ru(time_sub(eoc.q, eoc.r, ts_q, ts_r));
+            for (int k = 0; k < warps; ++k) bound_time = fminf(bound_time, warp_upper[k]);
+            // the items that may come first, listed in item order (Coulomb items by unit type, then Lennard-Jones,
+            // then bonds) so that each warp of the FP64 pass follows one kind of solve: the taken count of every
+            // chunk of 32 items, then (every warp scanning the counts) the items of the warp's chunks at their offsets
+            const int chunks = (items + 31) >> 5, coulomb_chunks = (3 * (((M - 1) + 31) & ~31)) >> 5;
+            for (int c = warp; c < chunks; c += warps) {
+                const int item = 32 * c + lane;
+                const unsigned votes = __ballot_sync(kFull, item < items && lower[item] <= bound_time);
+                if (lane == 0) chunk_count[c] = __popc(votes);
             }
             __syncthreads();
-            // the items that may come first, listed in item order (Coulomb items by unit type, then Lennard-Jones,
-            // then bonds) so that each warp of the FP64 pass follows one kind of solve
-            const double bound_time = upper;
-            const int coulomb_items = 3 * (((M - 1) + 31) & ~31), lj_items = t == 1 ? M - 1 : 0;
-            int base = 0, coulomb_taken = 0, lj_taken = 0;
-            for (int round = 0; round * (int)blockDim.x < items; ++round) {
-                const int item = round * blockDim.x + threadIdx.x;
-                const bool take = item < items && lower[item] <= bound_time;
-                const unsigned votes = __ballot_sync(kFull, take);
-                const unsigned coulomb_votes = __ballot_sync(kFull, take && item < coulomb_items);
-                const unsigned lj_votes = __ballot_sync(kFull, take && item >= coulomb_items &&
-                                                                   item < coulomb_items + lj_items);
-                if (lane == 0) {
-                    warp_count[warp] = __popc(votes);
-                    warp_count_coulomb[warp] = __popc(coulomb_votes);
-                    warp_count_lj[warp] = __popc(lj_votes);
+            int taken = 0, coulomb_taken = 0;
+            for (int g = 0; g < chunks; g += 32) {
+                const int v = g + lane < chunks ? chunk_count[g + lane] : 0;
+                int inclusive = v;
+                for (int o = 1; o < 32; o <<= 1) {
+                    const int y = __shfl_up_sync(kFull, inclusive, o);
+                    if (lane >= o) inclusive += y;
                 }
-                __syncthreads();
-                int offset = base;
-                for (int k = 0; k < warp; ++k) offset += warp_count[k];
-                if (take) list[offset + __popc(votes & ((1u << lane) - 1u))] = item;
-                for (int k = 0; k < warps; ++k) {
-                    base += warp_count[k];
-                    coulomb_taken += warp_count_coulomb[k];
-                    lj_taken += warp_count_lj[k];
+                const int before = taken + inclusive - v;  // items taken before chunk g + lane
+                if (coulomb_chunks >= g && coulomb_chunks < g + 32)
+                    coulomb_taken = __shfl_sync(kFull, before, coulomb_chunks - g);
+                const int first = warp >= g ? warp : warp + ((g - warp + warps - 1) / warps) * warps;
+                for (int c = first; c < g + 32 && c < chunks; c += warps) {
+                    const int offset = __shfl_sync(kFull, before, c - g);
+                    const int item = 32 * c + lane;
+                    const bool take = item < items && lower[item] <= bound_time;
+                    const unsigned votes = __ballot_sync(kFull, take);
+                    if (take) list[offset + __popc(votes & ((1u << lane) - 1u))] = item;
                 }
-                __syncthreads();
+                taken += __shfl_sync(kFull, inclusive, 31);
             }
+            const int bonds_taken = (lower[items - 2] <= bound_time) + (lower[items - 1] <= bound_time);
+            const int lj_taken = taken - coulomb_taken - bonds_taken;
+            __syncthreads();
             // phase B: the FP64 solve of the listed items; each kind of solve starts on a warp boundary, so that a
             // warp follows one kind (Coulomb, Lennard-Jones, bonds)
             const int lj_start = (coulomb_taken + 31) & ~31;
             const int bond_start = lj_start + ((lj_taken + 31) & ~31);
-            const int bonds_taken = base - coulomb_taken - lj_taken;
             for (int v = threadIdx.x; v < bond_start + bonds_taken && !st; v += blockDim.x) {
                 int k = -1;
                 if (v < coulomb_taken)
@@ -353,13 +362,12 @@ __global__ void __launch_bounds__(256, 2) water_kernel(WaterArgs a) {
                     k = coulomb_taken + (v - lj_start);
                 else if (v >= bond_start)
                     k = coulomb_taken + lj_taken + (v - bond_start);
-                if (k >= 0)
-                    st = water_item(w, pos, charge, key, ev, list[k], m, t, d, pa, ca, s.time_q, s.time_r, best);
+                if (k >= 0) st = water_item(w, pos, charge, key, ev, list[k], m, t, d, pa, ca, ts_q, ts_r, best);
             }
-            if (threadIdx.x == 0) refined = base;
+            refined = taken;
         } else {
             for (int item = threadIdx.x; item < items && !st; item += blockDim.x)
-                st = water_item(w, pos, charge, key, ev, item, m, t, d, pa, ca, s.time_q, s.time_r, best);
+                st = water_item(w, pos, charge, key, ev, item, m, t, d, pa, ca, ts_q, ts_r, best);
         }
         if (st) status = st;  // any failing thread; all stop after the barrier
         for (int offset = 16; offset > 0; offset >>= 1) shuffle_better(best, offset);
@@ -369,41 +377,25 @@ __global__ void __launch_bounds__(256, 2) water_kernel(WaterArgs a) {
             if (threadIdx.x == 0) s.status = status;
             break;
         }
-        if (threadIdx.x == 0) {
-            WaterCand b = warp_best[0];
-            for (int k = 1; k < warps; ++k)
-                if (water_better(warp_best[k], b)) b = warp_best[k];
-            WaterCand e;
-            e.q = s.eoc_q;
-            e.r = s.eoc_r;
-            e.kind = JFGPU_EV_END_OF_CHAIN;
-            e.target = s.eoc_new_active;
-            if (water_better(e, b)) b = e;
-            if (!isinf(a.stop_q) && !time_lt(b.q, b.r, a.stop_q, a.stop_r)) {  // the stop time wins ties
-                b.q = a.stop_q;
-                b.r = a.stop_r;
-                b.kind = kStopKind;
-                b.target = -1;
-            }
-            winner = b;
-        }
-        __syncthreads();
-        best = winner;
-        if (best.kind == kStopKind) {
+        // every thread takes the winner: the warps' best, the end of chain, the stop time (which wins ties)
+        best = warp_best[0];
+        for (int k = 1; k < warps; ++k)
+            if (water_better(warp_best[k], best)) best = warp_best[k];
+        if (water_better(eoc, best)) best = eoc;
+        if (!isinf(a.stop_q) && !time_lt(best.q, best.r, a.stop_q, a.stop_r)) {
             // the end of the run: the active unit time-sliced to the stop time, no event
             if (threadIdx.x == 0) {
-                const double dt = time_sub(best.q, best.r, s.time_q, s.time_r);
+                const double dt = time_sub(a.stop_q, a.stop_r, ts_q, ts_r);
                 for (int c = 0; c < 3; ++c) pos[3 * act + c] = py_mod(pa[c] + (c == d ? w.speed : 0.0) * dt, w.length);
-                s.time_q = best.q;
-                s.time_r = best.r;
+                s.time_q = a.stop_q;
+                s.time_r = a.stop_r;
                 s.stopped = 1;
             }
-            __syncthreads();
             break;
         }
         // commit: time slice of the active unit (every thread computes the same position; thread 0 stores it)
         {
-            const double dt = time_sub(best.q, best.r, s.time_q, s.time_r);
+            const double dt = time_sub(best.q, best.r, ts_q, ts_r);
             for (int c = 0; c < 3; ++c) pa[c] = py_mod(pa[c] + (c == d ? w.speed : 0.0) * dt, w.length);
         }
         int accepted = 1;
@@ -435,24 +427,24 @@ __global__ void __launch_bounds__(256, 2) water_kernel(WaterArgs a) {
                         bound32[j] = b - fabsf(b) * 32.f * 0x1p-24f;  // a lower bound
                     }
                 }
+                __syncthreads();
             }
-            __syncthreads();
+            // 0 rejected, 1 thinning in FP64, 2 accepted; every thread takes the same decision
+            int decision = 1;
+            if (w.mode == JFGPU_MODE_MIXED) {
+                // max(0, factor) <= uniform(0, bounding rate) is certain when the factor's upper bound stays below
+                // the draw times a lower bound of the bounding rate
+                float bounding = 0.f;
+                for (int j = 0; j < 3; ++j) bounding += fmaxf(bound32[j], 0.f);
+                const double thinning_lower = (double)bounding * draws[0] * (1.0 - 0x1p-20);
+                const float factor = pair32[0] + pair32[1] + pair32[2];
+                const float error = error32[0] + error32[1] + error32[2] + fabsf(factor) * 2.4e-7f;
+                if ((double)factor + (double)error < thinning_lower) decision = 0;  // rejection certain
+            }
             if (threadIdx.x == 0) {
-                decision = 1;
-                if (w.mode == JFGPU_MODE_MIXED) {
-                    // max(0, factor) <= uniform(0, bounding rate) is certain when the factor's upper bound stays
-                    // below the draw times a lower bound of the bounding rate
-                    float bounding = 0.f;
-                    for (int j = 0; j < 3; ++j) bounding += fmaxf(bound32[j], 0.f);
-                    const double thinning_lower = (double)bounding * draws[0] * (1.0 - 0x1p-20);
-                    const float factor = pair32[0] + pair32[1] + pair32[2];
-                    const float error = error32[0] + error32[1] + error32[2] + fabsf(factor) * 2.4e-7f;
-                    if ((double)factor + (double)error < thinning_lower) decision = 0;  // rejection certain
-                }
                 ++s.composite_events;
                 if (decision) ++s.thinning_exact;
             }
-            __syncthreads();
             if (decision) {
                 // the FP64 bounding derivatives (threads 0-2) and merged-image sums (warp j for target unit j)
                 if (threadIdx.x < 3) {
@@ -469,12 +461,9 @@ __global__ void __launch_bounds__(256, 2) water_kernel(WaterArgs a) {
                     if (lane == 0) pair[j] = value;
                 }
                 __syncthreads();
-                if (threadIdx.x == 0) {
-                    double target_factor[3], bounding_rate, event_rate;
-                    decision = composite_thinning(w.coulomb, JFGPU_DRAW_UNIT, bound, pair, draws, target_factor,
-                                                  bounding_rate, event_rate) ? 2 : 0;
-                }
-                __syncthreads();
+                double target_factor[3], bounding_rate, event_rate;
+                decision = composite_thinning(w.coulomb, JFGPU_DRAW_UNIT, bound, pair, draws, target_factor,
+                                              bounding_rate, event_rate) ? 2 : 0;
             }
             if (decision == 2) {
                 // the derivatives of the two other local units against the three target units
@@ -539,7 +528,7 @@ __global__ void __launch_bounds__(256, 2) water_kernel(WaterArgs a) {
                 a.log[chain * a.events + step] = e;
             }
             ++s.events;
-            s.refined_items += w.mode == JFGPU_MODE_MIXED ? refined : 3 * (M - 1) + (t == 1 ? M - 1 : 0) + 2;
+            s.refined_items += refined;
         }
         __syncthreads();
     }
@@ -682,7 +671,7 @@ extern "C" int jfgpu_water_run(void *water, double *positions, const double *cha
         return JFGPU_ERROR_ARGUMENT;
     if (chains == 0 || events == 0) return JFGPU_OK;
     if (!positions || !charges || !state) return JFGPU_ERROR_ARGUMENT;
-    const int warps = warps_per_block ? warps_per_block : 4;
+    const int warps = warps_per_block ? warps_per_block : 3;
     WaterArgs a;
     a.w = h->model;
     a.positions = positions;

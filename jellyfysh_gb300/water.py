@@ -90,7 +90,7 @@ class WaterBatch:
     its random numbers with the key of (seed, first_chain + c)."""
 
     def __init__(self, model: WaterModel, positions, seed: int = 0, first_chain: int = 0, charges=None,
-                 warps_per_block: int = 4):
+                 warps_per_block: int = 3):
         import torch
         self._torch = torch
         self.lib = _lib.load()
