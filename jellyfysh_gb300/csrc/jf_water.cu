@@ -156,7 +156,7 @@ __device__ inline int water_item(const WaterModel &w, const double *pos, const d
 // FP32 screen of a candidate item, in displacements over the speed: the Coulomb items solve the bound's inversion
 // in FP32 with an error bound (ipcb_x_displacement32), the Lennard-Jones items take the FP32 screen of the atomic
 // engine; a bond gets only a lower bound of its time (lower_only: it does not bound the earliest time).  unsafe:
-// the screen cannot judge, the item goes to FP64.
+// the screen cannot decide, the item goes to FP64.
 __device__ inline void water_screen(const WaterModel &w, const double *pos, const double *charge, uint64_t key,
                                    uint64_t ev, int item, int m, int t, int d, const double *pa, double ca,
                                    float &time, float &error, bool &unsafe, bool &lower_only) {
@@ -300,7 +300,7 @@ __global__ void __launch_bounds__(256, 2) water_kernel(WaterArgs a) {
         int st = JFGPU_STATUS_OK, refined = 3 * (M - 1) + (t == 1 ? M - 1 : 0) + 2;
         if (w.mode == JFGPU_MODE_MIXED) {
             // phase A: FP32 screen of every item; lower[item] = the earliest time the item may reach (-inf where
-            // the screen cannot judge), the bound = the smallest time that some candidate surely reaches (a screened
+            // the screen cannot decide), the bound = the smallest time that some candidate surely reaches (a screened
             // time plus its error bound, or the end of chain); the differences round outwards, towards a smaller
             // lower bound and a larger bound, so that an item is listed whenever its exact time may come first
             float mine = INFINITY;

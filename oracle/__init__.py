@@ -1,6 +1,6 @@
 """CPU oracle of the ECMC event-time path: ctypes front end of ``oracle/jf_oracle.c``.
 
-TEST INFRASTRUCTURE ONLY.  This package is the checker of the GPU product.  Only ``tests/``,
+TEST INFRASTRUCTURE ONLY.  This package is the CPU oracle the GPU product is tested against.  Only ``tests/``,
 ``__graft_entry__.smoke()`` and the CPU-baseline leg of ``bench.py`` import it; the product package
 ``jellyfysh_gb300`` never does.
 

@@ -1,4 +1,4 @@
-"""Build recipe of the CPU oracle (test infrastructure, the checker of the GPU product).
+"""Build recipe of the CPU oracle (test infrastructure: the CPU oracle the GPU product is tested against).
 
 Compiles ``oracle/jf_oracle.c`` into ``oracle/_build/libjforacle.so`` with ``-ffp-contract=off`` so that
 every floating-point operation is rounded on its own, as CPython rounds Python-level float arithmetic.

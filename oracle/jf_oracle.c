@@ -1,7 +1,7 @@
 /*
  * jf_oracle.c -- CPU restatement of JeLLyFysh's event-time path.
  *
- * TEST INFRASTRUCTURE ONLY: the checker of the GPU product.  Loaded by tests/,
+ * TEST INFRASTRUCTURE ONLY: the oracle the GPU product is tested against.  Loaded by tests/,
  * __graft_entry__.smoke() and the CPU-baseline leg of bench.py; never by the product.
  *
  * Build: gcc -O2 -fPIC -shared -ffp-contract=off (see oracle/build_oracle.py).  The flag

@@ -1,7 +1,7 @@
 /*
  * jf_oracle.h -- CPU restatement of JeLLyFysh's event-time path.
  *
- * TEST INFRASTRUCTURE ONLY.  This library is the checker for the GPU product: it is
+ * TEST INFRASTRUCTURE ONLY.  This library is the oracle the GPU product is tested against: it is
  * loaded by tests/, by __graft_entry__.smoke() and by bench.py's CPU-baseline leg.
  * The product (jellyfysh_gb300) never links, loads or calls it.
  *
