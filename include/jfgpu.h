@@ -204,6 +204,42 @@ int jfgpu_composite_out_state(const JfgpuCompositeDesc *desc, int32_t draw_mode,
                               const double *target_charges, const int32_t *local_first, const double *draws,
                               int64_t n, int32_t *new_active, double *rates, int32_t *status, void *stream);
 
+/* Molecular cell-bounding and cell-veto handlers (the far field between composite objects):
+ * TwoCompositeObjectCellBoundingPotentialEventHandler (two_composite_object_cell_bounding_potential_event_handler.py:
+ * 153-265) and CompositeObjectCellVetoEventHandler (composite_object_cell_veto_event_handler.py:110-162 with
+ * abstracts/cell_veto_event_handler.py:162-238).  Their out-state is send_out_state of the summed handler with the
+ * thinning drawn against a given bounding event rate: jfgpu_composite_bounded_out_state takes bounding_rates [n]
+ * (the cell-bounding rate times the speed, or the cell veto's rate) and otherwise the arguments and outputs of
+ * jfgpu_composite_out_state (rates [n][2] returns the given rate and the event rate; desc->bound_prefactor is
+ * unused). */
+int jfgpu_composite_bounded_out_state(const JfgpuCompositeDesc *desc, int32_t draw_mode, const double *velocity,
+                                      const double *local_positions, const double *local_charges,
+                                      const int32_t *active_index, const double *target_positions,
+                                      const double *target_charges, const int32_t *local_first,
+                                      const double *bounding_rates, const double *draws, int64_t n,
+                                      int32_t *new_active, double *rates, int32_t *status, void *stream);
+/* The cell-bounding event time of n events: CellBoundingPotential.standard_velocity_displacement
+ * (cell_bounding_potential.py:155-198) through Potential.displacement, with DipoleMonteCarloEstimator's charge factor
+ * (estimator/dipole_monte_carlo_estimator.py:157-190).  upper / lower [cells][3]: the estimator's derivative bounds by
+ * relative cell (x fastest) and direction, NaN for nearby cells; relative_cell [n]; velocity [n][3]; active_charge
+ * [n]; target_charges [n][units]; potential_change [n] (random.expovariate(beta)).  rate [n]: the stored bounding
+ * event rate; time [n]: the time displacement (inf for a rate <= 0).  status [n]: _ASSERTION for a nearby cell,
+ * target charges that do not sum to 0.0 or a velocity off one positive axis, _INDEX for a cell outside the table. */
+int jfgpu_composite_cell_bound_time(const double *upper, const double *lower, int64_t cells,
+                                    const int32_t *relative_cell, const double *velocity, const double *active_charge,
+                                    const double *target_charges, int32_t units, double dipole_charge,
+                                    const double *potential_change, int64_t n, double *rate, double *time,
+                                    int32_t *status, void *stream);
+/* The cell-veto event time of n events for the sampled relative cells: rate [n] = bound * |active charge| (upper
+ * bounds for a positive charge, else lower), time [n] = potential_change / (Walker total * |active charge| * speed).
+ * walker_upper / walker_lower [3]: the Walker tables' total rates by direction; the other arguments as for
+ * jfgpu_composite_cell_bound_time. */
+int jfgpu_composite_cell_veto_time(const double *upper, const double *lower, int64_t cells,
+                                   const double *walker_upper, const double *walker_lower,
+                                   const int32_t *relative_cell, const double *velocity, const double *active_charge,
+                                   const double *potential_change, int64_t n, double *rate, double *time,
+                                   int32_t *status, void *stream);
+
 /* ======================================================================================================
  * Chains: thousands of independent ECMC chains advanced by one kernel with the event loop on the device.
  * ==================================================================================================== */

@@ -6,6 +6,13 @@ object (``TwoCompositeObjectSummedBoundingPotentialEventHandler``,
 ``event_time`` is the handler's ``send_event_time`` and ``out_state`` its ``send_out_state`` (thinning, the
 derivative table of ``_fill_lifting`` and the lifting scheme) for n events in one launch each, through
 ``jfgpu_composite_event_time`` / ``jfgpu_composite_out_state`` (``include/jfgpu.h``).
+
+The far field between composite objects: ``cell_bound_time`` is the event time of the molecular cell-bounding
+handler (``TwoCompositeObjectCellBoundingPotentialEventHandler``,
+``event_handler/two_composite_object_cell_bounding_potential_event_handler.py:153-265``), ``cell_veto_time`` that of
+the molecular cell veto for sampled relative cells (``CompositeObjectCellVetoEventHandler``,
+``event_handler/composite_object_cell_veto_event_handler.py:110-162``), and ``bounded_out_state`` the out-state of
+both: the summed merged-image derivative thinned against the given bounding event rate, then the lifting.
 """
 import ctypes
 from dataclasses import dataclass
@@ -107,3 +114,100 @@ def out_state(model: CompositeModel, velocity, local_positions, local_charges, a
                                              rates.data_ptr(), status.data_ptr(), stream),
                "jfgpu_composite_out_state")
     return new_active[:n].cpu().numpy(), rates[:n].cpu().numpy(), status[:n].cpu().numpy()
+
+
+def bounded_out_state(model: CompositeModel, velocity, local_positions, local_charges, active_index,
+                      target_positions, target_charges, local_first, bounding_rates, draws, unit_draws: bool = False):
+    """Out-state of n events of the molecular cell-bounding or cell-veto handler: as ``out_state``, with the thinning
+    drawn against bounding_rates [n] (the cell-bounding rate times the speed, or the cell veto's rate)."""
+    torch, device = _device()
+    lib = _lib.load()
+    k = model.units
+    v = _on_device(torch, device, velocity, torch.float64, (-1, 3))
+    n = v.shape[0]
+    arrays = [v, _on_device(torch, device, local_positions, torch.float64, (n, k, 3)),
+              _on_device(torch, device, local_charges, torch.float64, (n, k)),
+              _on_device(torch, device, active_index, torch.int32, (n,)),
+              _on_device(torch, device, target_positions, torch.float64, (n, k, 3)),
+              _on_device(torch, device, target_charges, torch.float64, (n, k)),
+              _on_device(torch, device, local_first, torch.int32, (n,)),
+              _on_device(torch, device, bounding_rates, torch.float64, (n,)),
+              _on_device(torch, device, draws, torch.float64, (n, 3))]
+    new_active = torch.empty(max(n, 1), dtype=torch.int32, device=device)
+    rates = torch.empty((max(n, 1), 2), dtype=torch.float64, device=device)
+    status = torch.empty(max(n, 1), dtype=torch.int32, device=device)
+    desc = model.desc()
+    stream = torch.cuda.current_stream(device).cuda_stream
+    _lib.check(lib.jfgpu_composite_bounded_out_state(
+        ctypes.byref(desc), _lib.DRAW_UNIT if unit_draws else _lib.DRAW_VALUE, *[a.data_ptr() for a in arrays], n,
+        new_active.data_ptr(), rates.data_ptr(), status.data_ptr(), stream), "jfgpu_composite_bounded_out_state")
+    return new_active[:n].cpu().numpy(), rates[:n].cpu().numpy(), status[:n].cpu().numpy()
+
+
+class CellBounds:
+    """The estimator's derivative bounds of the far cells, on the device: upper and lower [cells][3] by relative cell
+    (the cuboid cell index, x fastest) and direction, NaN for the nearby cells; for the cell veto also the Walker
+    tables' total rates by direction."""
+
+    def __init__(self, upper, lower, walker_upper=None, walker_lower=None):
+        torch, device = _device()
+        upper = np.asarray(upper, dtype=np.float64).reshape(-1, 3)
+        lower = np.asarray(lower, dtype=np.float64).reshape(-1, 3)
+        if upper.shape != lower.shape:
+            raise ValueError("upper and lower bounds differ in shape")
+        self.cells = upper.shape[0]
+        self.upper = torch.from_numpy(np.ascontiguousarray(upper)).to(device)
+        self.lower = torch.from_numpy(np.ascontiguousarray(lower)).to(device)
+        self.walker_upper = self.walker_lower = None
+        if walker_upper is not None:
+            self.walker_upper = torch.as_tensor(np.asarray(walker_upper, dtype=np.float64).reshape(3)).to(device)
+            self.walker_lower = torch.as_tensor(np.asarray(walker_lower, dtype=np.float64).reshape(3)).to(device)
+
+
+def cell_bound_time(bounds: CellBounds, relative_cell, velocity, active_charge, target_charges, dipole_charge,
+                    potential_change):
+    """Event time of n molecular cell-bounding events: (rate [n], time displacement [n], status [n]) as host
+    arrays.  relative_cell [n], velocity [n][3], active_charge [n], target_charges [n][units], potential_change
+    [n]."""
+    torch, device = _device()
+    lib = _lib.load()
+    v = _on_device(torch, device, velocity, torch.float64, (-1, 3))
+    n = v.shape[0]
+    charges = _on_device(torch, device, target_charges, torch.float64, (n, -1)) if n else \
+        torch.zeros((0, 1), dtype=torch.float64, device=device)
+    units = charges.shape[1]
+    arrays = [_on_device(torch, device, relative_cell, torch.int32, (n,)), v,
+              _on_device(torch, device, active_charge, torch.float64, (n,)), charges]
+    du = _on_device(torch, device, potential_change, torch.float64, (n,))
+    rate = torch.empty(max(n, 1), dtype=torch.float64, device=device)
+    time = torch.empty(max(n, 1), dtype=torch.float64, device=device)
+    status = torch.empty(max(n, 1), dtype=torch.int32, device=device)
+    stream = torch.cuda.current_stream(device).cuda_stream
+    _lib.check(lib.jfgpu_composite_cell_bound_time(
+        bounds.upper.data_ptr(), bounds.lower.data_ptr(), bounds.cells, *[a.data_ptr() for a in arrays], units,
+        float(dipole_charge), du.data_ptr(), n, rate.data_ptr(), time.data_ptr(), status.data_ptr(), stream),
+        "jfgpu_composite_cell_bound_time")
+    return rate[:n].cpu().numpy(), time[:n].cpu().numpy(), status[:n].cpu().numpy()
+
+
+def cell_veto_time(bounds: CellBounds, relative_cell, velocity, active_charge, potential_change):
+    """Event time of n molecular cell-veto events for sampled relative cells: (rate [n], time displacement [n],
+    status [n]) as host arrays."""
+    if bounds.walker_upper is None:
+        raise ValueError("the cell veto needs the Walker tables' total rates")
+    torch, device = _device()
+    lib = _lib.load()
+    v = _on_device(torch, device, velocity, torch.float64, (-1, 3))
+    n = v.shape[0]
+    arrays = [_on_device(torch, device, relative_cell, torch.int32, (n,)), v,
+              _on_device(torch, device, active_charge, torch.float64, (n,)),
+              _on_device(torch, device, potential_change, torch.float64, (n,))]
+    rate = torch.empty(max(n, 1), dtype=torch.float64, device=device)
+    time = torch.empty(max(n, 1), dtype=torch.float64, device=device)
+    status = torch.empty(max(n, 1), dtype=torch.int32, device=device)
+    stream = torch.cuda.current_stream(device).cuda_stream
+    _lib.check(lib.jfgpu_composite_cell_veto_time(
+        bounds.upper.data_ptr(), bounds.lower.data_ptr(), bounds.cells, bounds.walker_upper.data_ptr(),
+        bounds.walker_lower.data_ptr(), *[a.data_ptr() for a in arrays], n, rate.data_ptr(), time.data_ptr(),
+        status.data_ptr(), stream), "jfgpu_composite_cell_veto_time")
+    return rate[:n].cpu().numpy(), time[:n].cpu().numpy(), status[:n].cpu().numpy()

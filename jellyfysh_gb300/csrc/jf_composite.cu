@@ -16,6 +16,7 @@ struct CompositeArgs {
     int64_t n;
     const double *velocity, *active_position, *active_charge, *target_positions, *target_charges;
     const double *potential_changes, *local_positions, *local_charges, *draws;
+    const double *bounding_rates;  // given bounding event rates (molecular cell-bounding / cell-veto handlers), or null
     const int32_t *active_index, *local_first;
     double *displacement, *rates;
     int32_t *new_active, *status;
@@ -50,12 +51,45 @@ __global__ void composite_out_kernel(CompositeArgs a) {
     if (active >= 0 && active < k)
         st = composite_out_state(a.model, a.draw_mode, v, a.local_positions + 3 * k * i, a.local_charges + k * i,
                                  active, a.target_positions + 3 * k * i, a.target_charges + k * i,
-                                 a.local_first[i], a.draws + 3 * i, new_active, bounding_rate, event_rate);
+                                 a.local_first[i], a.draws + 3 * i, new_active, bounding_rate, event_rate,
+                                 a.bounding_rates ? a.bounding_rates + i : nullptr);
     a.new_active[i] = st ? -1 : new_active;
     if (a.rates) {
         a.rates[2 * i] = bounding_rate;
         a.rates[2 * i + 1] = event_rate;
     }
+    a.status[i] = st;
+}
+
+struct CellTimeArgs {
+    const double *upper, *lower;                // [cells][3]
+    const double *walker_upper, *walker_lower;  // [3] (cell veto)
+    int64_t cells, n;
+    const int32_t *relative_cell;
+    const double *velocity, *active_charge, *target_charges, *potential_change;
+    int units;
+    double dipole_charge;
+    double *rate, *time;
+    int32_t *status;
+};
+
+// one thread per event: the molecular cell-bounding (veto = false) or cell-veto event time
+__global__ void cell_time_kernel(CellTimeArgs a, bool veto) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.n) return;
+    const int32_t cell = a.relative_cell[i];
+    double rate = NAN, time = NAN;
+    int st = JFGPU_STATUS_INDEX;  // a relative cell outside the table
+    if (cell >= 0 && cell < a.cells) {
+        const double *v = a.velocity + 3 * i;
+        st = veto ? composite_cell_veto_time(a.upper + 3 * cell, a.lower + 3 * cell, a.walker_upper, a.walker_lower,
+                                             v, a.active_charge[i], a.potential_change[i], rate, time)
+                  : composite_cell_bound_time(a.upper + 3 * cell, a.lower + 3 * cell, v, a.active_charge[i],
+                                              a.target_charges + (int64_t)a.units * i, a.units, a.dipole_charge,
+                                              a.potential_change[i], rate, time);
+    }
+    a.rate[i] = st ? NAN : rate;
+    a.time[i] = st ? NAN : time;
     a.status[i] = st;
 }
 
@@ -153,4 +187,98 @@ extern "C" int jfgpu_composite_out_state(const JfgpuCompositeDesc *desc, int32_t
     a.rates = rates;
     a.status = status;
     return jf::run(a, desc, stream, true);
+}
+
+extern "C" int jfgpu_composite_bounded_out_state(const JfgpuCompositeDesc *desc, int32_t draw_mode,
+                                                 const double *velocity, const double *local_positions,
+                                                 const double *local_charges, const int32_t *active_index,
+                                                 const double *target_positions, const double *target_charges,
+                                                 const int32_t *local_first, const double *bounding_rates,
+                                                 const double *draws, int64_t n, int32_t *new_active, double *rates,
+                                                 int32_t *status, void *stream) {
+    if (!desc || n < 0) return JFGPU_ERROR_ARGUMENT;
+    if (draw_mode != JFGPU_DRAW_VALUE && draw_mode != JFGPU_DRAW_UNIT) return JFGPU_ERROR_ARGUMENT;
+    if (n == 0) return JFGPU_OK;
+    if (!velocity || !local_positions || !local_charges || !active_index || !target_positions || !target_charges ||
+        !local_first || !bounding_rates || !draws || !new_active || !status)
+        return JFGPU_ERROR_ARGUMENT;
+    jf::CompositeArgs a{};
+    a.draw_mode = draw_mode;
+    a.n = n;
+    a.velocity = velocity;
+    a.local_positions = local_positions;
+    a.local_charges = local_charges;
+    a.active_index = active_index;
+    a.target_positions = target_positions;
+    a.target_charges = target_charges;
+    a.local_first = local_first;
+    a.bounding_rates = bounding_rates;
+    a.draws = draws;
+    a.new_active = new_active;
+    a.rates = rates;
+    a.status = status;
+    return jf::run(a, desc, stream, true);
+}
+
+static int launch_cell_time(jf::CellTimeArgs &a, bool veto, void *stream) {
+    const int threads = 128;
+    const int64_t blocks = (a.n + threads - 1) / threads;
+    jf::cell_time_kernel<<<(unsigned)blocks, threads, 0, static_cast<cudaStream_t>(stream)>>>(a, veto);
+    return cudaGetLastError() == cudaSuccess ? JFGPU_OK : JFGPU_ERROR_CUDA;
+}
+
+extern "C" int jfgpu_composite_cell_bound_time(const double *upper, const double *lower, int64_t cells,
+                                               const int32_t *relative_cell, const double *velocity,
+                                               const double *active_charge, const double *target_charges,
+                                               int32_t units, double dipole_charge, const double *potential_change,
+                                               int64_t n, double *rate, double *time, int32_t *status,
+                                               void *stream) {
+    if (n < 0 || cells < 0 || units < 1 || units > jf::kMaxCompositeUnits) return JFGPU_ERROR_ARGUMENT;
+    if (n == 0) return JFGPU_OK;
+    if (!upper || !lower || !relative_cell || !velocity || !active_charge || !target_charges || !potential_change ||
+        !rate || !time || !status)
+        return JFGPU_ERROR_ARGUMENT;
+    jf::CellTimeArgs a{};
+    a.upper = upper;
+    a.lower = lower;
+    a.cells = cells;
+    a.n = n;
+    a.relative_cell = relative_cell;
+    a.velocity = velocity;
+    a.active_charge = active_charge;
+    a.target_charges = target_charges;
+    a.units = units;
+    a.dipole_charge = dipole_charge;
+    a.potential_change = potential_change;
+    a.rate = rate;
+    a.time = time;
+    a.status = status;
+    return launch_cell_time(a, false, stream);
+}
+
+extern "C" int jfgpu_composite_cell_veto_time(const double *upper, const double *lower, int64_t cells,
+                                              const double *walker_upper, const double *walker_lower,
+                                              const int32_t *relative_cell, const double *velocity,
+                                              const double *active_charge, const double *potential_change, int64_t n,
+                                              double *rate, double *time, int32_t *status, void *stream) {
+    if (n < 0 || cells < 0) return JFGPU_ERROR_ARGUMENT;
+    if (n == 0) return JFGPU_OK;
+    if (!upper || !lower || !walker_upper || !walker_lower || !relative_cell || !velocity || !active_charge ||
+        !potential_change || !rate || !time || !status)
+        return JFGPU_ERROR_ARGUMENT;
+    jf::CellTimeArgs a{};
+    a.upper = upper;
+    a.lower = lower;
+    a.walker_upper = walker_upper;
+    a.walker_lower = walker_lower;
+    a.cells = cells;
+    a.n = n;
+    a.relative_cell = relative_cell;
+    a.velocity = velocity;
+    a.active_charge = active_charge;
+    a.potential_change = potential_change;
+    a.rate = rate;
+    a.time = time;
+    a.status = status;
+    return launch_cell_time(a, true, stream);
 }

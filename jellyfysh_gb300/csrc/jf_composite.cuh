@@ -346,11 +346,15 @@ __device__ inline int composite_lifting(const CompositeModel &m, int draw_mode, 
 // smaller one (the order of the derivative table).  draws: [0] thinning random.uniform(0.0, bounding rate),
 // [1] the active unit's insert into the lifting table, [2] the ratio scheme's draw; values or unit draws as in
 // lifting_select.  new_active: -1 when thinned, else 0..units-1 (a local unit) or units..2 units-1 (a target).
+// given: nullptr for this handler's summed inverse-power bound; else the bounding event rate that the molecular
+// cell-bounding handler (two_composite_object_cell_bounding_potential_event_handler.py:231-265) or the molecular cell
+// veto with a target (composite_object_cell_veto_event_handler.py:131-162) draws the thinning against, with the same
+// summed merged-image derivative, _fill_lifting and lifting after it.
 __device__ inline int composite_out_state(const CompositeModel &m, int draw_mode, const double *velocity,
                                           const double *locals, const double *local_charges, int active,
                                           const double *targets, const double *target_charges, int local_first,
                                           const double *draws, int &new_active, double &bounding_rate,
-                                          double &event_rate) {
+                                          double &event_rate, const double *given = nullptr) {
     new_active = -1;
     bounding_rate = 0.0;
     event_rate = 0.0;
@@ -364,11 +368,26 @@ __device__ inline int composite_out_state(const CompositeModel &m, int draw_mode
     for (int j = 0; j < k; ++j) {
         double s[3];
         periodic_separation(a, targets + 3 * j, m.system_length, s);
-        bound[j] = bound_derivative(m, d, speed, s, ca, target_charges[j]);
+        bound[j] = given ? 0.0 : bound_derivative(m, d, speed, s, ca, target_charges[j]);
         pair[j] = coulomb_derivative(m, d, speed, s, ca, target_charges[j]);
     }
-    if (!composite_thinning(m, draw_mode, bound, pair, draws, target_factor, bounding_rate, event_rate))
-        return JFGPU_STATUS_OK;
+    bool confirmed;
+    if (given) {
+        // assert bounding_event_rate >= 0.0 (:243, composite_object_cell_veto_event_handler.py:150)
+        if (!(*given >= 0.0)) return JFGPU_STATUS_ASSERTION;
+        double factor = 0.0;
+        for (int j = 0; j < k; ++j) {
+            factor += pair[j];
+            target_factor[j] = 0.0 - pair[j];
+        }
+        bounding_rate = *given;
+        event_rate = factor > 0.0 ? factor : 0.0;
+        const double thinning = draw_mode == JFGPU_DRAW_UNIT ? 0.0 + (bounding_rate - 0.0) * draws[0] : draws[0];
+        confirmed = !(event_rate <= thinning);
+    } else {
+        confirmed = composite_thinning(m, draw_mode, bound, pair, draws, target_factor, bounding_rate, event_rate);
+    }
+    if (!confirmed) return JFGPU_STATUS_OK;
     double cross[kMaxCompositeUnits * kMaxCompositeUnits];
     for (int i = 0; i < k; ++i) {
         if (i == active) continue;
@@ -380,6 +399,83 @@ __device__ inline int composite_out_state(const CompositeModel &m, int draw_mode
     }
     return composite_lifting(m, draw_mode, active, local_first, event_rate, target_factor, cross, draws,
                              new_active);
+}
+
+// CellBoundingPotential.standard_velocity_displacement (cell_bounding_potential.py:155-198) through
+// Potential.displacement (potential/abstracts.py:212-245), with the charge factor of
+// DipoleMonteCarloEstimator.charge_correction_factor (estimator/dipole_monte_carlo_estimator.py:157-190): the active
+// charge times the largest absolute target charge over the estimator's dipole charge, the target charges summing to
+// 0.0 by the builtin sum (asserted).  upper / lower: the relative cell's bounds in the three directions (NaN for a
+// nearby cell, which the handler asserts against).  rate: the stored bounding event rate (per unit length; the
+// out-state draws against rate times the speed); time: the time displacement.
+__host__ __device__ inline int composite_cell_bound_time(const double *upper, const double *lower,
+                                                         const double *velocity, double active_charge,
+                                                         const double *target_charges, int units,
+                                                         double dipole_charge, double potential_change,
+                                                         double &rate, double &time) {
+    int d = -1, count = 0;
+    for (int c = 0; c < 3; ++c)
+        if (velocity[c] != 0.0) {
+            ++count;
+            d = c;
+        }
+    if (count != 1 || !(velocity[d] > 0.0)) return JFGPU_STATUS_ASSERTION;
+    const double speed = velocity[d];
+    if (units < 1 || units > kMaxCompositeUnits) return JFGPU_STATUS_ASSERTION;
+    // sum(target_charges) == 0.0 with CPython 3.12's compensated sum: 0 + q0 exactly, then Neumaier
+    double sum = 0.0 + target_charges[0], compensation = 0.0;
+    for (int j = 1; j < units; ++j) {
+        const double x = target_charges[j], t = sum + x;
+        compensation += fabs(sum) >= fabs(x) ? (sum - t) + x : (x - t) + sum;
+        sum = t;
+    }
+    if (compensation != 0.0 && isfinite(compensation)) sum += compensation;
+    if (sum != 0.0) return JFGPU_STATUS_ASSERTION;
+    if (isnan(upper[d]) || isnan(lower[d])) return JFGPU_STATUS_ASSERTION;
+    double largest = fabs(target_charges[0]);
+    for (int j = 1; j < units; ++j)
+        if (fabs(target_charges[j]) > largest) largest = fabs(target_charges[j]);
+    if (dipole_charge == 0.0) return JFGPU_STATUS_ZERO_DIVISION;
+    const double product = active_charge * largest / dipole_charge;
+    rate = product > 0.0 ? upper[d] * product : lower[d] * product;
+    const double displacement = rate > 0 ? potential_change / rate : INFINITY;
+    time = displacement / speed;
+    return JFGPU_STATUS_OK;
+}
+
+// CellVetoEventHandler.send_event_time (abstracts/cell_veto_event_handler.py:200-238) for a composite object, whose
+// charge factor is the active charge (charge_correction_factor without target charges): positive, the upper bounds
+// and their Walker table's total rate; else its negative and the lower ones.  upper / lower: the sampled relative
+// cell's bounds, walker_upper / walker_lower: the Walker totals, each in the three directions.  rate: the bounding
+// event rate of the out-state; time: potential_change / (total rate * speed).
+__host__ __device__ inline int composite_cell_veto_time(const double *upper, const double *lower,
+                                                        const double *walker_upper, const double *walker_lower,
+                                                        const double *velocity, double active_charge,
+                                                        double potential_change, double &rate, double &time) {
+    int d = -1, count = 0;
+    for (int c = 0; c < 3; ++c)
+        if (velocity[c] != 0.0) {
+            ++count;
+            d = c;
+        }
+    if (count != 1 || !(velocity[d] > 0.0)) return JFGPU_STATUS_ASSERTION;
+    const double speed = velocity[d];
+    double factor = active_charge, total, bound;
+    if (factor > 0.0) {
+        total = walker_upper[d];
+        bound = upper[d];
+    } else {
+        factor *= -1.0;
+        total = walker_lower[d];
+        bound = lower[d];
+    }
+    const double total_rate = total * factor;
+    rate = bound * factor;
+    if (!(rate > 0.0)) return JFGPU_STATUS_ASSERTION;
+    const double denominator = total_rate * speed;
+    if (denominator == 0.0) return JFGPU_STATUS_ZERO_DIVISION;
+    time = potential_change / denominator;
+    return JFGPU_STATUS_OK;
 }
 
 }  // namespace jf

@@ -92,6 +92,10 @@ def lib() -> ctypes.CDLL:
         handle.jfo_composite_event_time.argtypes = [_I, _D, _I, _I, _D, _D, _D, _PD, _PD, _D, _PD, _PD, _PD, _PD]
         handle.jfo_composite_out_state.argtypes = [_I, _I, _I, _D, _I, _I, _D, _D, _D, _PD, _PD, _PD, _I, _PD, _PD,
                                                    _I, _PD, ctypes.POINTER(ctypes.c_int), _PD, _PD]
+        handle.jfo_composite_bounded_out_state.argtypes = [_I, _I, _I, _D, _I, _I, _D, _D, _PD, _PD, _PD, _I, _PD,
+                                                           _PD, _I, _D, _PD, ctypes.POINTER(ctypes.c_int), _PD]
+        handle.jfo_composite_cell_bound_time.argtypes = [_PD, _PD, _PD, _D, _PD, _I, _D, _D, _PD, _PD]
+        handle.jfo_composite_cell_veto_time.argtypes = [_PD, _PD, _PD, _PD, _PD, _D, _D, _PD, _PD]
         handle.jfo_lifting.argtypes = [ctypes.c_int, ctypes.c_int, _PD, ctypes.POINTER(ctypes.c_int32), ctypes.c_int,
                                        _D, ctypes.POINTER(ctypes.c_int64), _PD]
         handle.jfo_ip_displacement.argtypes = [_D, _D, _PD, _PD, _D, _D, _D, _PD]
@@ -236,6 +240,46 @@ def composite_out_state(model: dict, scheme: str, velocity, local_positions, loc
         _doubles(target_positions), _doubles(target_charges), 1 if local_first else 0, _doubles(draws),
         ctypes.byref(new_active), ctypes.byref(bounding), ctypes.byref(rate))
     return status, new_active.value, bounding.value, rate.value
+
+
+def composite_bounded_out_state(model: dict, scheme: str, velocity, local_positions, local_charges, active_index,
+                                target_positions, target_charges, local_first, bounding_rate, draws,
+                                unit_draw: bool = False):
+    """(status, new active, event rate) of send_out_state of the molecular cell-bounding or cell-veto handler: the
+    thinning draws against the given bounding event rate."""
+    new_active = ctypes.c_int(-1)
+    rate = ctypes.c_double(0.0)
+    status = lib().jfo_composite_bounded_out_state(
+        model["units"], LIFTING_SCHEMES[scheme], 1 if unit_draw else 0, model["alpha"], model["fourier_cutoff"],
+        model["position_cutoff"], model["coulomb_prefactor"], model["system_length"], _doubles(velocity),
+        _doubles(local_positions), _doubles(local_charges), int(active_index), _doubles(target_positions),
+        _doubles(target_charges), 1 if local_first else 0, float(bounding_rate), _doubles(draws),
+        ctypes.byref(new_active), ctypes.byref(rate))
+    return status, new_active.value, rate.value
+
+
+def composite_cell_bound_time(upper, lower, velocity, active_charge, target_charges, dipole_charge,
+                              potential_change):
+    """(status, bounding event rate, time displacement) of the molecular cell-bounding handler's event time; upper
+    and lower are the relative cell's bounds in the three directions."""
+    rate = ctypes.c_double(0.0)
+    time = ctypes.c_double(0.0)
+    charges = [float(q) for q in target_charges]
+    status = lib().jfo_composite_cell_bound_time(
+        _doubles(upper), _doubles(lower), _doubles(velocity), float(active_charge), _doubles(charges), len(charges),
+        float(dipole_charge), float(potential_change), ctypes.byref(rate), ctypes.byref(time))
+    return status, rate.value, time.value
+
+
+def composite_cell_veto_time(upper, lower, walker_upper, walker_lower, velocity, active_charge, potential_change):
+    """(status, bounding event rate, time displacement) of the molecular cell veto's event time for a sampled
+    relative cell (bounds upper / lower in the three directions; Walker totals per direction)."""
+    rate = ctypes.c_double(0.0)
+    time = ctypes.c_double(0.0)
+    status = lib().jfo_composite_cell_veto_time(
+        _doubles(upper), _doubles(lower), _doubles(walker_upper), _doubles(walker_lower), _doubles(velocity),
+        float(active_charge), float(potential_change), ctypes.byref(rate), ctypes.byref(time))
+    return status, rate.value, time.value
 
 
 # ---- potentials (reference argument order: velocity, separation, [charges], [potential_change]) ----

@@ -906,13 +906,15 @@ int jfo_composite_event_time(int units, double alpha, int fourier_cutoff, int po
     return JFO_OK;
 }
 
-/* send_out_state (:152-202) with _fill_lifting (event_handler_with_bounding_potential.py:170-220) */
-int jfo_composite_out_state(int units, int scheme, int unit_draw, double alpha, int fourier_cutoff,
-                            int position_cutoff, double coulomb_prefactor, double bound_prefactor,
-                            double system_length, const double *velocity, const double *local_positions,
-                            const double *local_charges, int active_index, const double *target_positions,
-                            const double *target_charges, int local_first, const double *draws, int *new_active,
-                            double *bounding_rate, double *event_rate) {
+/* send_out_state (:152-202) with _fill_lifting (event_handler_with_bounding_potential.py:170-220).  given: NULL for
+ * the summed inverse-power bound of this handler, else the bounding event rate the thinning draws against (the
+ * molecular cell-bounding and cell-veto handlers). */
+static int composite_out_state(int units, int scheme, int unit_draw, double alpha, int fourier_cutoff,
+                               int position_cutoff, double coulomb_prefactor, double bound_prefactor,
+                               double system_length, const double *velocity, const double *local_positions,
+                               const double *local_charges, int active_index, const double *target_positions,
+                               const double *target_charges, int local_first, const double *given,
+                               const double *draws, int *new_active, double *bounding_rate, double *event_rate) {
     const double *active = local_positions + 3 * active_index;
     double active_charge = local_charges[active_index];
     double *target_factor = (double *)calloc((size_t)units, sizeof(double));
@@ -925,7 +927,8 @@ int jfo_composite_out_state(int units, int scheme, int unit_draw, double alpha, 
     for (int j = 0; j < units && !st; ++j) {
         double s[3], b, pair;
         composite_separation(system_length, active, target_positions + 3 * j, s);
-        st = jfo_ipcb_derivative(bound_prefactor, velocity, s, active_charge, target_charges[j], &b);
+        b = 0.0;
+        if (!given) st = jfo_ipcb_derivative(bound_prefactor, velocity, s, active_charge, target_charges[j], &b);
         if (!st) st = jfo_mic_derivative(alpha, fourier_cutoff, position_cutoff, coulomb_prefactor, system_length,
                                          velocity, s, active_charge, target_charges[j], &pair);
         if (st) break;
@@ -934,6 +937,12 @@ int jfo_composite_out_state(int units, int scheme, int unit_draw, double alpha, 
         target_factor[j] -= pair;
     }
     double rate = factor > 0.0 ? factor : 0.0;
+    if (given) {
+        bounding = *given;
+        /* assert bounding_event_rate >= 0.0 (two_composite_object_cell_bounding_potential_event_handler.py:243,
+         * composite_object_cell_veto_event_handler.py:150) */
+        if (!st && !(bounding >= 0.0)) st = JFO_ASSERT;
+    }
     *bounding_rate = bounding;
     *event_rate = rate;
     double thinning = unit_draw ? 0.0 + (bounding - 0.0) * draws[0] : draws[0];
@@ -980,6 +989,94 @@ int jfo_composite_out_state(int units, int scheme, int unit_draw, double alpha, 
     free(table);
     free(flags);
     return st;
+}
+
+int jfo_composite_out_state(int units, int scheme, int unit_draw, double alpha, int fourier_cutoff,
+                            int position_cutoff, double coulomb_prefactor, double bound_prefactor,
+                            double system_length, const double *velocity, const double *local_positions,
+                            const double *local_charges, int active_index, const double *target_positions,
+                            const double *target_charges, int local_first, const double *draws, int *new_active,
+                            double *bounding_rate, double *event_rate) {
+    return composite_out_state(units, scheme, unit_draw, alpha, fourier_cutoff, position_cutoff, coulomb_prefactor,
+                               bound_prefactor, system_length, velocity, local_positions, local_charges,
+                               active_index, target_positions, target_charges, local_first, NULL, draws, new_active,
+                               bounding_rate, event_rate);
+}
+
+/* send_out_state of the molecular cell-bounding handler
+ * (two_composite_object_cell_bounding_potential_event_handler.py:231-265) and of the molecular cell veto with a
+ * target (composite_object_cell_veto_event_handler.py:131-162): the summed merged-image derivative of the active
+ * unit against the target object, thinned against the given bounding event rate, then _fill_lifting and the
+ * lifting scheme. */
+int jfo_composite_bounded_out_state(int units, int scheme, int unit_draw, double alpha, int fourier_cutoff,
+                                    int position_cutoff, double coulomb_prefactor, double system_length,
+                                    const double *velocity, const double *local_positions,
+                                    const double *local_charges, int active_index, const double *target_positions,
+                                    const double *target_charges, int local_first, double bounding_rate,
+                                    const double *draws, int *new_active, double *event_rate) {
+    double bounding;
+    return composite_out_state(units, scheme, unit_draw, alpha, fourier_cutoff, position_cutoff, coulomb_prefactor,
+                               0.0, system_length, velocity, local_positions, local_charges, active_index,
+                               target_positions, target_charges, local_first, &bounding_rate, draws, new_active,
+                               &bounding, event_rate);
+}
+
+/* CellBoundingPotential.standard_velocity_displacement (cell_bounding_potential.py:155-198) through
+ * Potential.displacement (potential/abstracts.py:212-245), with the charge factor of
+ * DipoleMonteCarloEstimator.charge_correction_factor (estimator/dipole_monte_carlo_estimator.py:157-190): the active
+ * charge times the largest absolute target charge over the estimator's dipole charge (the target charges summing to
+ * 0.0 by the builtin sum).  upper / lower are the bounds of the relative cell in the three directions; rate is the
+ * stored bounding event rate (per unit length: the out-state draws against rate times the speed), time the time
+ * displacement. */
+int jfo_composite_cell_bound_time(const double *upper, const double *lower, const double *velocity,
+                                  double active_charge,
+                                  const double *target_charges, int units, double dipole_charge,
+                                  double potential_change, double *rate, double *time) {
+    int d;
+    double speed;
+    int st = analyse_velocity(velocity, &d, &speed);
+    if (st) return st;
+    if (units < 1 || jfo_py_sum(target_charges, units) != 0.0) return JFO_ASSERT;
+    if (isnan(upper[d]) || isnan(lower[d])) return JFO_ASSERT;  /* a nearby relative cell: no bound */
+    double largest = fabs(target_charges[0]);
+    for (int j = 1; j < units; ++j)
+        if (fabs(target_charges[j]) > largest) largest = fabs(target_charges[j]);
+    if (dipole_charge == 0.0) return JFO_ZERO_DIVISION;
+    double product = active_charge * largest / dipole_charge;
+    *rate = product > 0.0 ? upper[d] * product : lower[d] * product;
+    double displacement = *rate > 0 ? potential_change / *rate : INFINITY;
+    *time = displacement / speed;
+    return JFO_OK;
+}
+
+/* CellVetoEventHandler.send_event_time (abstracts/cell_veto_event_handler.py:200-238) for a composite object, whose
+ * charge factor is the active charge (DipoleMonteCarloEstimator.charge_correction_factor without target charges):
+ * positive, the upper bounds and their Walker table's total rate (walker_upper, one per direction); else its
+ * negative, the lower ones.  upper / lower are the bounds of the sampled relative cell in the three directions; rate
+ * is the bounding event rate of the out-state, time the time displacement potential_change / (total rate * speed). */
+int jfo_composite_cell_veto_time(const double *upper, const double *lower, const double *walker_upper,
+                                 const double *walker_lower, const double *velocity, double active_charge,
+                                 double potential_change, double *rate, double *time) {
+    int d;
+    double speed;
+    int st = analyse_velocity(velocity, &d, &speed);
+    if (st) return st;
+    double factor = active_charge, total, bound;
+    if (factor > 0.0) {
+        total = walker_upper[d];
+        bound = upper[d];
+    } else {
+        factor *= -1.0;
+        total = walker_lower[d];
+        bound = lower[d];
+    }
+    double total_rate = total * factor;
+    *rate = bound * factor;
+    if (!(*rate > 0.0)) return JFO_ASSERT;
+    double denominator = total_rate * speed;
+    if (denominator == 0.0) return JFO_ZERO_DIVISION;
+    *time = potential_change / denominator;
+    return JFO_OK;
 }
 
 /* ======================================================================================

@@ -128,6 +128,21 @@ int jfo_composite_out_state(int units, int scheme, int unit_draw, double alpha, 
                             const double *local_charges, int active_index, const double *target_positions,
                             const double *target_charges, int local_first, const double *draws, int *new_active,
                             double *bounding_rate, double *event_rate);
+/* the molecular cell-bounding and cell-veto handlers: the out-state against a given bounding event rate, the event
+ * times from the bound of the relative cell */
+int jfo_composite_bounded_out_state(int units, int scheme, int unit_draw, double alpha, int fourier_cutoff,
+                                    int position_cutoff, double coulomb_prefactor, double system_length,
+                                    const double *velocity, const double *local_positions,
+                                    const double *local_charges, int active_index, const double *target_positions,
+                                    const double *target_charges, int local_first, double bounding_rate,
+                                    const double *draws, int *new_active, double *event_rate);
+int jfo_composite_cell_bound_time(const double *upper, const double *lower, const double *velocity,
+                                  double active_charge,
+                                  const double *target_charges, int units, double dipole_charge,
+                                  double potential_change, double *rate, double *time);
+int jfo_composite_cell_veto_time(const double *upper, const double *lower, const double *walker_upper,
+                                 const double *walker_lower, const double *velocity, double active_charge,
+                                 double potential_change, double *rate, double *time);
 
 /* cells */
 void jfo_cell_bounds(double system_length, int cells_per_side, double *cell_min, double *cell_max);
