@@ -544,24 +544,48 @@ def water_gpu_arm(args):
     after = batch.states()
     events_done = int(after["events"].sum() - before["events"].sum())
     _, total_ms, value = replicas.timed_throughput(events_done, elapsed_ms, device)
-    # end to end: H2D of positions and chain states from pinned host memory, the run, D2H of both
+    # end to end: every step uploads positions and chain states from pinned host memory, runs, and reads both back;
+    # double-buffered as for the atomic chains (two batches take the steps in turn, each batch's copies on a stream of
+    # its own, the runs one after the other on one stream)
+    pair = [batch, water.WaterBatch(model, positions, seed=1000 + rank, first_chain=0)]
     host_in = [batch.positions_dev.cpu().pin_memory(), batch.state_dev.cpu().pin_memory()]
-    host_out = [t.clone().pin_memory() for t in host_in]
+    host_out = [[t.clone().pin_memory() for t in host_in] for _ in pair]
     h2d = sum(t.numel() * t.element_size() for t in host_in)
     e2e_steps = max(2, args.steps // 2)
+    copy_streams = [torch.cuda.Stream(device), torch.cuda.Stream(device)]
     torch.cuda.synchronize(device)
     e_begin = torch.cuda.Event(enable_timing=True)
     e_end = torch.cuda.Event(enable_timing=True)
     e_begin.record(stream)
-    for _ in range(e2e_steps):
-        batch.positions_dev.copy_(host_in[0], non_blocking=True)
-        batch.state_dev.copy_(host_in[1], non_blocking=True)
-        batch.run(args.events)
-        host_out[0].copy_(batch.positions_dev, non_blocking=True)
-        host_out[1].copy_(batch.state_dev, non_blocking=True)
+    for copy in copy_streams:
+        copy.wait_event(e_begin)
+    for step in range(e2e_steps):
+        x = step % 2
+        b, copy = pair[x], copy_streams[x]
+        with torch.cuda.stream(copy):  # after this batch's previous read-back, in stream order
+            b.positions_dev.copy_(host_in[0], non_blocking=True)
+            b.state_dev.copy_(host_in[1], non_blocking=True)
+        uploaded = torch.cuda.Event()
+        uploaded.record(copy)
+        stream.wait_event(uploaded)
+        b.run(args.events)
+        ran = torch.cuda.Event()
+        ran.record(stream)
+        copy.wait_event(ran)
+        with torch.cuda.stream(copy):
+            host_out[x][0].copy_(b.positions_dev, non_blocking=True)
+            host_out[x][1].copy_(b.state_dev, non_blocking=True)
+    for copy in copy_streams:
+        done = torch.cuda.Event()
+        done.record(copy)
+        stream.wait_event(done)
     e_end.record(stream)
     torch.cuda.synchronize(device)
+    for b in pair:
+        b.check_status()
     e2e_value = e2e_steps * args.chains * args.events / (e_begin.elapsed_time(e_end) / 1000.0)
+    pair[1].close()
+    del pair
     if rank != 0:
         if world > 1:
             dist.barrier()
@@ -597,7 +621,8 @@ def water_gpu_arm(args):
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic: seeded lattices of water molecules in random orientations", "config": config,
-            "e2e": {"value": e2e_value, "unit": "events/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": h2d},
+            "e2e": {"value": e2e_value, "unit": "events/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": h2d,
+                    "pipelining": "two batches take the steps in turn; each batch's copies overlap the other's run"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": None, "peak_source": peak_kind,
                          "kernel": "jf::water_kernel", "bytes_per_event": bytes_per_event},
