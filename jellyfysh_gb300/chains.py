@@ -104,6 +104,22 @@ def _ptr(tensor) -> Optional[int]:
     return None if tensor is None else tensor.data_ptr()
 
 
+def check_positions(positions, length: float, what: str) -> None:
+    """Refuse positions the device cannot take, before they reach it: not finite, or outside [0, L).  The
+    reference's cells map a position by int(x / side) (cuboid_cells.py:190-211), which raises IndexError past the
+    box and indexes from the other end below it; on the device such a position would land in a wrong cell."""
+    p = np.asarray(positions, dtype=np.float64)
+    if not np.isfinite(p).all():
+        raise ValueError("%s: positions must be finite" % what)
+    if (p < 0.0).any() or (p >= length).any():
+        raise ValueError("%s: positions must lie in [0, %r)" % (what, float(length)))
+
+
+def check_charges(charges, what: str) -> None:
+    if not np.isfinite(np.asarray(charges, dtype=np.float64)).all():
+        raise ValueError("%s: charges must be finite" % what)
+
+
 class ChainBatch:
     """Independent ECMC chains advanced together on one GPU."""
 
@@ -111,11 +127,15 @@ class ChainBatch:
                  charges: Optional[Sequence[Optional[np.ndarray]]] = None, seed: int = 0, device: str = "cuda"):
         import torch
         self._torch = torch
-        self.lib = _lib.load()
-        self.device = torch.device(device)
         self.specs = list(specs)
         if len(positions) != len(self.specs):
             raise ValueError("one position array per chain is required")
+        for c, spec in enumerate(self.specs):
+            check_positions(positions[c], spec.system_length, "chain %d" % c)
+            if charges is not None and charges[c] is not None:
+                check_charges(charges[c], "chain %d" % c)
+        self.lib = _lib.load()
+        self.device = torch.device(device)
         self.n_chains = len(self.specs)
         descs = (_lib.ChainDesc * self.n_chains)()
         self.keys = []

@@ -92,7 +92,17 @@ class WaterBatch:
     def __init__(self, model: WaterModel, positions, seed: int = 0, first_chain: int = 0, charges=None,
                  warps_per_block: int = 3):
         import torch
+        from .chains import check_charges, check_positions
         self._torch = torch
+        if isinstance(positions, torch.Tensor):
+            inside = torch.isfinite(positions).all() and bool(((positions >= 0) & (positions < model.system_length))
+                                                              .all())
+            if not inside:
+                raise ValueError("water positions must be finite and lie in [0, %r)" % float(model.system_length))
+        else:
+            check_positions(positions, model.system_length, "water positions")
+        if charges is not None:
+            check_charges(charges, "water charges")
         self.lib = _lib.load()
         self.device = torch.device("cuda", torch.cuda.current_device())
         self.model = model

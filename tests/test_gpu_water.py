@@ -192,13 +192,14 @@ def test_other_lifting_schemes_match_the_oracle(water, lifting):
 
 
 def test_invalid_descriptions_and_launch_shapes_are_errors(water):
-    """The C ABI refuses a model it cannot run (fewer than two molecules, a box that is not positive, an initial
-    active unit outside the system) and more than eight warps a chain, with an argument error."""
+    """The C ABI refuses a model it cannot run (fewer than two molecules, an initial active unit outside the system)
+    and more than eight warps a chain, with an argument error; a box that is not positive stops on the host."""
     from jellyfysh_gb300 import _lib
-    for bad in (water.WaterModel(molecules=1), water.WaterModel(system_length=-1.0),
-                water.WaterModel(initial_active=3 * 64)):
+    for bad in (water.WaterModel(molecules=1), water.WaterModel(initial_active=3 * 64)):
         with pytest.raises(_lib.JfgpuError):
             water.WaterBatch(bad, np.zeros((1, 3 * bad.molecules, 3)), seed=0)
+    with pytest.raises(ValueError, match="must lie in"):  # no position lies in a box that is not positive
+        water.WaterBatch(water.WaterModel(system_length=-1.0), np.zeros((1, 192, 3)), seed=0)
     model = water.WaterModel(molecules=8, system_length=6.21)
     batch = water.WaterBatch(model, water.lattice_positions(model, 1, 0), seed=0, warps_per_block=9)
     with pytest.raises(_lib.JfgpuError):
