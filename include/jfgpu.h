@@ -240,6 +240,20 @@ int jfgpu_composite_cell_veto_time(const double *upper, const double *lower, int
                                    const double *potential_change, int64_t n, double *rate, double *time,
                                    int32_t *status, void *stream);
 
+/* Walker's alias table (event_handler/walker.py:53-122), which samples the cell veto's relative cell.
+ * jfgpu_walker_table builds it on the HOST from n items in the handler's order (items and rates host arrays; the
+ * cell veto gives every non-nearby relative cell with max(bound, 0.0), cell_veto_event_handler.py:148-160):
+ * first_item / first_rate / second_item [n] (second_item -1 for an entry of one item), the total and mean rate;
+ * JFGPU_ERROR_TABLE where the reference's assertions fail.  jfgpu_walker_sample picks n items on the device from
+ * such a table (device arrays): choice [n] the table index of random.choice, draws [n] random.uniform(0.0, mean
+ * rate) as values (JFGPU_DRAW_VALUE) or unit draws (JFGPU_DRAW_UNIT); items [n], status [n] (_INDEX for an index
+ * outside the table). */
+int jfgpu_walker_table(const int32_t *items, const double *rates, int64_t n, int32_t *first_item, double *first_rate,
+                       int32_t *second_item, double *total_rate, double *mean_rate);
+int jfgpu_walker_sample(const int32_t *first_item, const double *first_rate, const int32_t *second_item, int64_t size,
+                        double mean_rate, const int64_t *choice, const double *draws, int32_t draw_mode, int64_t n,
+                        int32_t *items, int32_t *status, void *stream);
+
 /* ======================================================================================================
  * Chains: thousands of independent ECMC chains advanced by one kernel with the event loop on the device.
  * ==================================================================================================== */

@@ -133,6 +133,8 @@ SIGNATURES = {
     "jfgpu_composite_cell_bound_time": (ctypes.c_int, [_P, _P, _I64, _P, _P, _P, _P, _I32, _D, _P, _I64, _P, _P, _P,
                                                        _P]),
     "jfgpu_composite_cell_veto_time": (ctypes.c_int, [_P, _P, _I64, _P, _P, _P, _P, _P, _P, _I64, _P, _P, _P, _P]),
+    "jfgpu_walker_table": (ctypes.c_int, [_P, _P, _I64, _P, _P, _P, _P, _P]),
+    "jfgpu_walker_sample": (ctypes.c_int, [_P, _P, _P, _I64, _D, _P, _P, _I32, _I64, _P, _P, _P]),
     "jfgpu_water_create": (ctypes.c_int, [ctypes.POINTER(WaterDesc), ctypes.POINTER(ctypes.c_void_p)]),
     "jfgpu_water_destroy": (None, [_P]),
     "jfgpu_water_init": (ctypes.c_int, [_P, _P, _I64, _I64, _P]),

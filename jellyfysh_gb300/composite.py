@@ -13,6 +13,7 @@ handler (``TwoCompositeObjectCellBoundingPotentialEventHandler``,
 the molecular cell veto for sampled relative cells (``CompositeObjectCellVetoEventHandler``,
 ``event_handler/composite_object_cell_veto_event_handler.py:110-162``), and ``bounded_out_state`` the out-state of
 both: the summed merged-image derivative thinned against the given bounding event rate, then the lifting.
+``WalkerTable`` / ``walker_sample`` build the cell veto's alias table and sample its relative cells.
 """
 import ctypes
 from dataclasses import dataclass
@@ -211,3 +212,49 @@ def cell_veto_time(bounds: CellBounds, relative_cell, velocity, active_charge, p
         bounds.walker_lower.data_ptr(), *[a.data_ptr() for a in arrays], n, rate.data_ptr(), time.data_ptr(),
         status.data_ptr(), stream), "jfgpu_composite_cell_veto_time")
     return rate[:n].cpu().numpy(), time[:n].cpu().numpy(), status[:n].cpu().numpy()
+
+
+class WalkerTable:
+    """Walker's alias table (``event_handler/walker.py:53-103``) built on the host in the reference's order and held
+    on the device: ``items`` the relative cells and ``rates`` their rates, in the order the handler lists them."""
+
+    def __init__(self, items, rates):
+        torch, device = _device()
+        lib = _lib.load()
+        items = np.ascontiguousarray(np.asarray(items, dtype=np.int32))
+        rates = np.ascontiguousarray(np.asarray(rates, dtype=np.float64))
+        n = len(items)
+        if len(rates) != n:
+            raise ValueError("one rate per item is required")
+        first_item = np.zeros(max(n, 1), dtype=np.int32)
+        second_item = np.zeros(max(n, 1), dtype=np.int32)
+        first_rate = np.zeros(max(n, 1), dtype=np.float64)
+        total, mean = ctypes.c_double(0.0), ctypes.c_double(0.0)
+        _lib.check(lib.jfgpu_walker_table(items.ctypes.data, rates.ctypes.data, n, first_item.ctypes.data,
+                                          first_rate.ctypes.data, second_item.ctypes.data, ctypes.byref(total),
+                                          ctypes.byref(mean)), "jfgpu_walker_table")
+        self.size = n
+        self.total_rate, self.mean_rate = total.value, mean.value
+        self.first_item_host, self.first_rate_host, self.second_item_host = first_item, first_rate, second_item
+        self.first_item = torch.from_numpy(first_item).to(device)
+        self.first_rate = torch.from_numpy(first_rate).to(device)
+        self.second_item = torch.from_numpy(second_item).to(device)
+
+
+def walker_sample(table: WalkerTable, choices, draws, unit_draws: bool = False):
+    """Walker.sample_cell (``walker.py:105-122``) for n draws: (items [n], status [n]) as host arrays.  choices [n]
+    are table indices (what random.choice picked), draws [n] the random.uniform(0.0, mean rate) values, or unit draws
+    with ``unit_draws``."""
+    torch, device = _device()
+    lib = _lib.load()
+    k = _on_device(torch, device, choices, torch.int64, (-1,))
+    n = k.shape[0]
+    u = _on_device(torch, device, draws, torch.float64, (n,))
+    items = torch.empty(max(n, 1), dtype=torch.int32, device=device)
+    status = torch.empty(max(n, 1), dtype=torch.int32, device=device)
+    stream = torch.cuda.current_stream(device).cuda_stream
+    _lib.check(lib.jfgpu_walker_sample(table.first_item.data_ptr(), table.first_rate.data_ptr(),
+                                       table.second_item.data_ptr(), table.size, table.mean_rate, k.data_ptr(),
+                                       u.data_ptr(), _lib.DRAW_UNIT if unit_draws else _lib.DRAW_VALUE, n,
+                                       items.data_ptr(), status.data_ptr(), stream), "jfgpu_walker_sample")
+    return items[:n].cpu().numpy(), status[:n].cpu().numpy()

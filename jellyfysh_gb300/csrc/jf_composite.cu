@@ -220,6 +220,43 @@ extern "C" int jfgpu_composite_bounded_out_state(const JfgpuCompositeDesc *desc,
     return jf::run(a, desc, stream, true);
 }
 
+namespace jf {
+
+// Walker.sample_cell (walker.py:105-122): the table entry random.choice picked, then random.uniform(0.0, mean) against
+// the entry's first rate (a value, or 0.0 + (mean - 0.0) * u for a unit draw u)
+__global__ void walker_sample_kernel(const int32_t *first_item, const double *first_rate, const int32_t *second_item,
+                                     int64_t size, double mean_rate, const int64_t *choice, const double *draws,
+                                     int draw_mode, int64_t n, int32_t *items, int32_t *status) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int64_t k = choice[i];
+    if (k < 0 || k >= size) {
+        items[i] = -1;
+        status[i] = JFGPU_STATUS_INDEX;
+        return;
+    }
+    const double value = draw_mode == JFGPU_DRAW_UNIT ? 0.0 + (mean_rate - 0.0) * draws[i] : draws[i];
+    items[i] = value <= first_rate[k] ? first_item[k] : second_item[k];
+    status[i] = JFGPU_STATUS_OK;
+}
+
+}  // namespace jf
+
+extern "C" int jfgpu_walker_sample(const int32_t *first_item, const double *first_rate, const int32_t *second_item,
+                                   int64_t size, double mean_rate, const int64_t *choice, const double *draws,
+                                   int32_t draw_mode, int64_t n, int32_t *items, int32_t *status, void *stream) {
+    if (n < 0 || size < 0) return JFGPU_ERROR_ARGUMENT;
+    if (draw_mode != JFGPU_DRAW_VALUE && draw_mode != JFGPU_DRAW_UNIT) return JFGPU_ERROR_ARGUMENT;
+    if (n == 0) return JFGPU_OK;
+    if (!first_item || !first_rate || !second_item || !choice || !draws || !items || !status)
+        return JFGPU_ERROR_ARGUMENT;
+    const int threads = 128;
+    const int64_t blocks = (n + threads - 1) / threads;
+    jf::walker_sample_kernel<<<(unsigned)blocks, threads, 0, static_cast<cudaStream_t>(stream)>>>(
+        first_item, first_rate, second_item, size, mean_rate, choice, draws, draw_mode, n, items, status);
+    return cudaGetLastError() == cudaSuccess ? JFGPU_OK : JFGPU_ERROR_CUDA;
+}
+
 static int launch_cell_time(jf::CellTimeArgs &a, bool veto, void *stream) {
     const int threads = 128;
     const int64_t blocks = (a.n + threads - 1) / threads;

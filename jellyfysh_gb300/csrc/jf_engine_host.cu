@@ -532,6 +532,30 @@ int build_species(JfgpuEngine *e, const JfgpuChainDesc &d, const std::vector<dou
 
 }  // namespace
 
+// Walker's alias table over n items in the order given (walker.py:53-103), built on the host as the engine builds
+// its cell-veto tables: first_item / first_rate / second_item [n] (second_item -1 for an entry of one item), the
+// total rate (builtin sum) and the mean rate.  JFGPU_ERROR_TABLE for a negative rate or a leftover entry whose rate
+// strays from the mean by 1e-6 or more (the reference's assertions).
+extern "C" int jfgpu_walker_table(const int32_t *items, const double *rates, int64_t n, int32_t *first_item,
+                                  double *first_rate, int32_t *second_item, double *total_rate, double *mean_rate) {
+    if (n < 1 || n > INT32_MAX || !items || !rates || !first_item || !first_rate || !second_item || !total_rate ||
+        !mean_rate)
+        return JFGPU_ERROR_ARGUMENT;
+    std::vector<int> item_list(items, items + n);
+    std::vector<double> rate_list(rates, rates + n);
+    HostWalker w;
+    const int error = walker_build(item_list, rate_list, w);
+    if (error) return error;
+    for (int64_t k = 0; k < n; ++k) {
+        first_item[k] = w.first_item[k];
+        first_rate[k] = w.first_rate[k];
+        second_item[k] = w.second_item[k];
+    }
+    *total_rate = w.total_rate;
+    *mean_rate = w.mean_rate;
+    return JFGPU_OK;
+}
+
 extern "C" {
 
 int jfgpu_version(void) { return 1; }

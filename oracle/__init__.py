@@ -96,6 +96,9 @@ def lib() -> ctypes.CDLL:
                                                            _PD, _I, _D, _PD, ctypes.POINTER(ctypes.c_int), _PD]
         handle.jfo_composite_cell_bound_time.argtypes = [_PD, _PD, _PD, _D, _PD, _I, _D, _D, _PD, _PD]
         handle.jfo_composite_cell_veto_time.argtypes = [_PD, _PD, _PD, _PD, _PD, _D, _D, _PD, _PD]
+        _PI = ctypes.POINTER(ctypes.c_int)
+        handle.jfo_walker_table.argtypes = [_PI, _PD, _I, _PI, _PD, _PI, _PD, _PD]
+        handle.jfo_walker_pick.argtypes = [_PI, _PD, _PI, _I, _I, _D]
         handle.jfo_lifting.argtypes = [ctypes.c_int, ctypes.c_int, _PD, ctypes.POINTER(ctypes.c_int32), ctypes.c_int,
                                        _D, ctypes.POINTER(ctypes.c_int64), _PD]
         handle.jfo_ip_displacement.argtypes = [_D, _D, _PD, _PD, _D, _D, _D, _PD]
@@ -280,6 +283,26 @@ def composite_cell_veto_time(upper, lower, walker_upper, walker_lower, velocity,
         _doubles(upper), _doubles(lower), _doubles(walker_upper), _doubles(walker_lower), _doubles(velocity),
         float(active_charge), float(potential_change), ctypes.byref(rate), ctypes.byref(time))
     return status, rate.value, time.value
+
+
+def walker_table(items, rates):
+    """(status, first_item, first_rate, second_item, total rate, mean rate) of Walker's alias table."""
+    n = len(items)
+    size = max(n, 1)
+    first_item = (ctypes.c_int * size)()
+    second_item = (ctypes.c_int * size)()
+    first_rate = (ctypes.c_double * size)()
+    total, mean = ctypes.c_double(0.0), ctypes.c_double(0.0)
+    status = lib().jfo_walker_table((ctypes.c_int * size)(*[int(i) for i in items]), _doubles(rates), n,
+                                    first_item, first_rate, second_item, ctypes.byref(total), ctypes.byref(mean))
+    return status, list(first_item)[:n], list(first_rate)[:n], list(second_item)[:n], total.value, mean.value
+
+
+def walker_pick(first_item, first_rate, second_item, choice, uniform):
+    """The item Walker.sample_cell returns for the table index of random.choice and the random.uniform value."""
+    n = len(first_item)
+    return lib().jfo_walker_pick((ctypes.c_int * n)(*first_item), _doubles(first_rate),
+                                 (ctypes.c_int * n)(*second_item), n, int(choice), float(uniform))
 
 
 # ---- potentials (reference argument order: velocity, separation, [charges], [potential_change]) ----

@@ -1253,6 +1253,34 @@ static void walker_free(Walker *w) {
     free(w->first_rate);
 }
 
+/* Walker's alias table (walker.py:53-103) over n items, exported: first_item / first_rate / second_item [n]
+ * (second_item -1 for an entry of one item), the total and the mean rate. */
+int jfo_walker_table(const int *items, const double *rates, int n, int *first_item, double *first_rate,
+                     int *second_item, double *total_rate, double *mean_rate) {
+    if (n < 1) return JFO_BAD_CONFIG;
+    Walker w;
+    int st = walker_build(&w, items, rates, n);
+    if (st == JFO_OK) {
+        for (int k = 0; k < w.size; ++k) {
+            first_item[k] = w.first_item[k];
+            first_rate[k] = w.first_rate[k];
+            second_item[k] = w.second_item[k];
+        }
+        *total_rate = w.total_rate;
+        *mean_rate = w.mean_rate;
+    }
+    walker_free(&w);
+    return st;
+}
+
+/* Walker.sample_cell (walker.py:105-122) with the table index random.choice returned and the value of
+ * random.uniform(0.0, mean rate): the entry's first item when the value does not exceed its first rate. */
+int jfo_walker_pick(const int *first_item, const double *first_rate, const int *second_item, int size, int choice,
+                    double uniform) {
+    if (choice < 0 || choice >= size) return -1;
+    return uniform <= first_rate[choice] ? first_item[choice] : second_item[choice];
+}
+
 /* Walker.sample_cell: random.choice(table), then uniform(0, mean) <= first rate */
 static int walker_sample(const Walker *w, uint64_t choice_bits, uint64_t uniform_bits) {
     int k = (int)jfo_randbelow(choice_bits, (uint32_t)w->size);

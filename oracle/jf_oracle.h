@@ -144,6 +144,12 @@ int jfo_composite_cell_veto_time(const double *upper, const double *lower, const
                                  const double *walker_lower, const double *velocity, double active_charge,
                                  double potential_change, double *rate, double *time);
 
+/* Walker's alias table (event_handler/walker.py:53-122) */
+int jfo_walker_table(const int *items, const double *rates, int n, int *first_item, double *first_rate,
+                     int *second_item, double *total_rate, double *mean_rate);
+int jfo_walker_pick(const int *first_item, const double *first_rate, const int *second_item, int size, int choice,
+                    double uniform);
+
 /* cells */
 void jfo_cell_bounds(double system_length, int cells_per_side, double *cell_min, double *cell_max);
 

@@ -59,3 +59,17 @@ def out_arrays(record):
     out = out_state_arrays(record)
     out["given_rate"] = np.array([e["bounding_event_rate"] for e in record["out_states"]], dtype=np.float64)
     return out
+
+
+def walkers(record):
+    """The cell veto's Walker tables: {(which, direction): {"items", "rates", "table", "mean_rate", "total_rate"}}
+    with which 0 for the upper bounds and 1 for the lower ones."""
+    tables = record["tables"]["walkers"]
+    return {(which, d): w for which, name in enumerate(("upper", "lower")) for d, w in enumerate(tables[name])}
+
+
+def walker_draws(record):
+    """Per recorded cell-veto event time: (which, direction, table index of random.choice, random.uniform value,
+    sampled relative cell)."""
+    return [(0 if t["charge_factor"] > 0.0 else 1, t["direction"], t["walker_choice"], t["walker_uniform"],
+             t["relative_cell"]) for t in record["times"]]

@@ -85,7 +85,15 @@ def run_one(tree, name, out):
         if ctx["calls"] is not None:
             ctx["calls"].append(("uniform", [a, b], value))
         return value
-    random.expovariate, random.uniform = expovariate, uniform
+
+    original_choice = random.choice
+
+    def choice(seq):
+        value = original_choice(seq)
+        if ctx["calls"] is not None:
+            ctx["calls"].append(("choice", [len(seq)], [i for i, entry in enumerate(seq) if entry is value][0]))
+        return value
+    random.expovariate, random.uniform, random.choice = expovariate, uniform, choice
 
     def cell_index(cell):
         """The flat index of a cuboid cell: its identifier (x, y, z) with x running fastest."""
@@ -96,7 +104,8 @@ def run_one(tree, name, out):
         return index
 
     def tables(self):
-        """upper[cell][direction], lower[cell][direction] over every cell index (None for nearby cells)."""
+        """upper[cell][direction], lower[cell][direction] over every cell index (None for nearby cells); for the
+        cell veto also the Walker tables by bound and direction."""
         if kind == "cell_bounding":
             bounds = self._bounding_potential._derivative_bounds
             estimator = self._bounding_potential._estimator
@@ -118,7 +127,26 @@ def run_one(tree, name, out):
         if kind == "cell_veto":
             result["walker_upper"] = [walker.total_rate for walker in self._upper_bound_walker]
             result["walker_lower"] = [walker.total_rate for walker in self._lower_bound_walker]
+            result["walkers"] = {
+                "upper": [walker_record(self, w, d, 0) for d, w in enumerate(self._upper_bound_walker)],
+                "lower": [walker_record(self, w, d, 1) for d, w in enumerate(self._lower_bound_walker)]}
         return result
+
+    def walker_record(self, walker, direction, which):
+        """The items the handler gave the Walker table (relative cell and rate, in its order: the non-nearby cells
+        in cell order with max(bound, 0.0), cell_veto_event_handler.py:148-160) and the table it built (first
+        item, first rate, second item or -1)."""
+        items, rates = [], []
+        for cell in self._cells.yield_cells():
+            if cell in self._cells.nearby_cells(self._cells.zero_cell):
+                continue
+            separation = self._cells.relative_cell(cell, self._cells.zero_cell)
+            items.append(cell_index(separation))
+            rates.append(max(self._derivative_bounds[separation][direction][which], 0.0))
+        table = [[cell_index(entry[0].item), entry[0].rate, cell_index(entry[1].item) if len(entry) > 1 else -1]
+                 for entry in walker._table]
+        return {"items": items, "rates": rates, "table": table, "mean_rate": walker._mean_rate,
+                "total_rate": walker.total_rate}
 
     def first_call(self):
         if "coulomb" in record:
@@ -241,6 +269,8 @@ def run_one(tree, name, out):
                     "potential_change": [v for k, _, v in calls if k == "expovariate"][0],
                     "time_stamp": ctx["stamp"], "event_time": [event_time.quotient, event_time.remainder],
                     "relative_cell": cell_index(ctx["relative_cell"]),
+                    "walker_choice": [v for k, _, v in calls if k == "choice"][0],
+                    "walker_uniform": [v for k, _, v in calls if k == "uniform"][0],
                     "bounding_event_rate": self._bounding_event_rate})
             return result
 

@@ -99,3 +99,22 @@ def test_handler_assertions():
         o["active_index"][0], o["target_positions"][0], o["target_charges"][0], o["local_first"][0], -1.0,
         o["draws"][0])[0]
     assert status == ASSERT
+
+
+@pytest.mark.parametrize("name", ["dipoles_cell_veto", "water_cell_veto"])
+def test_walker_tables_and_samples_match_the_reference(name):
+    """The cell veto's alias tables (walker.py:53-103) rebuilt from the handler's items equal the reference's entry
+    for entry, with its total and mean rate; every recorded sample_cell call picks the recorded relative cell."""
+    from tests.composite_cell_cases import walker_draws, walkers
+    record = SYSTEMS[name]
+    tables = walkers(record)
+    for key, w in tables.items():
+        status, first_item, first_rate, second_item, total, mean = oracle.walker_table(w["items"], w["rates"])
+        assert status == 0
+        assert [list(entry) for entry in zip(first_item, first_rate, second_item)] == [list(e) for e in w["table"]]
+        assert (total, mean) == (w["total_rate"], w["mean_rate"])
+    for which, d, choice, uniform, cell in walker_draws(record):
+        table = tables[(which, d)]["table"]
+        picked = oracle.walker_pick([e[0] for e in table], [e[1] for e in table], [e[2] for e in table], choice,
+                                    uniform)
+        assert picked == cell

@@ -137,3 +137,47 @@ def test_statuses_and_empty_batches(composite):
         o["active_index"][:1], o["target_positions"][:1], o["target_charges"][:1], o["local_first"][:1], [-1.0],
         o["draws"][:1])
     assert status.tolist() == [_lib.STATUS_ASSERTION]
+
+
+@pytest.mark.parametrize("name", ["dipoles_cell_veto", "water_cell_veto"])
+def test_walker_tables_and_samples_match_the_reference(composite, name):
+    from tests.composite_cell_cases import walker_draws, walkers
+    record = SYSTEMS[name]
+    tables = {}
+    for key, w in walkers(record).items():
+        table = composite.WalkerTable(w["items"], w["rates"])
+        assert [list(e) for e in zip(table.first_item_host.tolist(), table.first_rate_host.tolist(),
+                                     table.second_item_host.tolist())] == [list(e) for e in w["table"]]
+        assert (table.total_rate, table.mean_rate) == (w["total_rate"], w["mean_rate"])
+        tables[key] = table
+    draws = walker_draws(record)
+    for key, table in tables.items():
+        mine = [row for row in draws if (row[0], row[1]) == key]
+        if not mine:
+            continue
+        items, status = composite.walker_sample(table, [row[2] for row in mine], [row[3] for row in mine])
+        assert (status == 0).all()
+        assert items.tolist() == [row[4] for row in mine]
+
+
+def test_walker_sampling_of_unit_draws_matches_the_oracle(composite):
+    """Seeded tables of uneven rates: every entry of a 4000-sample batch of unit draws picks the oracle's item, and
+    an index outside the table is an _INDEX status."""
+    from jellyfysh_gb300 import _lib
+    rng = np.random.default_rng(17)
+    items = list(range(100, 191))
+    rates = rng.exponential(1.0, len(items)) * (rng.random(len(items)) < 0.8)
+    table = composite.WalkerTable(items, rates)
+    status, first_item, first_rate, second_item, total, mean = oracle.walker_table(items, rates)
+    assert status == 0 and (table.total_rate, table.mean_rate) == (total, mean)
+    choices = rng.integers(0, len(items), 4000)
+    units = rng.random(4000)
+    got, st = composite.walker_sample(table, choices, units, unit_draws=True)
+    assert (st == 0).all()
+    want = [oracle.walker_pick(first_item, first_rate, second_item, k, 0.0 + (mean - 0.0) * u)
+            for k, u in zip(choices, units)]
+    assert got.tolist() == want
+    _, st = composite.walker_sample(table, [len(items), -1], [0.5, 0.5], unit_draws=True)
+    assert st.tolist() == [_lib.STATUS_INDEX, _lib.STATUS_INDEX]
+    with pytest.raises(_lib.JfgpuError):
+        composite.WalkerTable([1, 2], [1.0, -1.0])  # a negative rate fails the reference's assertion
