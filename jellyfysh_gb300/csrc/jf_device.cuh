@@ -651,8 +651,15 @@ static __device__ __noinline__ double ipcb_x_displacement(double pp, double sx, 
     double u_zero = ipcb_potential(pp, 0.0, sy, sz);
     double u_half = ipcb_potential(pp, half, sy, sz);
     double per_length = fabs(u_zero - u_half);
-    double displacement = floor(du / per_length) * length;
-    du = fmod(du, per_length);
+    double displacement;
+    if (du >= 0.0 && du < per_length * (1.0 - 0x1p-50)) {
+        // floor(du / per_length) is 0 (the product's rounding keeps du below per_length (1 - 2^-51), so the rounded
+        // quotient stays below 1) and fmod returns du itself: the same values without the division and fmod
+        displacement = 0.0 * length;
+    } else {
+        displacement = floor(du / per_length) * length;
+        du = fmod(du, per_length);
+    }
     double new_norm;
     if (pp > 0.0) {
         if (sx <= 0.0) {

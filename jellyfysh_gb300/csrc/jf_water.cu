@@ -386,7 +386,8 @@ __global__ void __launch_bounds__(256, 2) water_kernel(WaterArgs a) {
             // the end of the run: the active unit time-sliced to the stop time, no event
             if (threadIdx.x == 0) {
                 const double dt = time_sub(a.stop_q, a.stop_r, ts_q, ts_r);
-                for (int c = 0; c < 3; ++c) pos[3 * act + c] = py_mod(pa[c] + (c == d ? w.speed : 0.0) * dt, w.length);
+                for (int c = 0; c < 3; ++c)
+                    pos[3 * act + c] = py_mod_near(pa[c] + (c == d ? w.speed : 0.0) * dt, w.length);
                 s.time_q = a.stop_q;
                 s.time_r = a.stop_r;
                 s.stopped = 1;
@@ -396,7 +397,7 @@ __global__ void __launch_bounds__(256, 2) water_kernel(WaterArgs a) {
         // commit: time slice of the active unit (every thread computes the same position; thread 0 stores it)
         {
             const double dt = time_sub(best.q, best.r, ts_q, ts_r);
-            for (int c = 0; c < 3; ++c) pa[c] = py_mod(pa[c] + (c == d ? w.speed : 0.0) * dt, w.length);
+            for (int c = 0; c < 3; ++c) pa[c] = py_mod_near(pa[c] + (c == d ? w.speed : 0.0) * dt, w.length);
         }
         int accepted = 1;
         if (best.kind == JFGPU_EV_COMPOSITE) {
