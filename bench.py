@@ -52,9 +52,14 @@ NEAR_CELLS = (2 * WORKLOAD["neighbor_layers"] + 1) ** 3  # cells scanned for pai
 CPU_SECONDS = 10.0  # wall time of the CPU baseline sample
 TIMING_STRIDE = 16  # event rounds between two rounds bracketed by per-kernel CUDA events
 # DRAM traffic of the screening kernel per event: ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch of
-# this workload (56.53 MB + 0.74 MB) divided by the 4096 events of that launch
-# (profiles/round_kernels_lennard_jones_4096x1024.md)
+# this workload (56.53 MB + 0.74 MB) divided by the 4096 events of that launch (the committed ncu summary of the
+# round kernels)
 NCU_TRAFFIC_PER_EVENT = (56.533504e6 + 0.742656e6) / 4096
+# the same for the water kernel (2.83 MB + 0.22 MB over 512 chains x 32 events) and the Coulomb chains kernel
+# (4.01 MB + 0.71 MB over 1024 chains x 128 events), with the FP64 pipe's busy fraction of active cycles
+# (sm__pipe_fp64_cycles_active) from the same captures: both kernels are bound by FP64 latency, not by HBM
+WATER_NCU = {"traffic_per_event": (2.830080e6 + 0.221952e6) / (512 * 32), "fp64_pipe_active": 0.501}
+COULOMB_NCU = {"traffic_per_event": (4.010496e6 + 0.713728e6) / (1024 * 128), "fp64_pipe_active": 0.598}
 
 
 def parse():
@@ -449,7 +454,7 @@ def gpu_arm(args):
     dominant_s = dominant["ms"] / dominant_launches / 1000.0
     achieved = bytes_per_event * events_per_launch / dominant_s / 1e9
     peak, peak_kind = measured_peaks()
-    traffic = None if NCU_TRAFFIC_PER_EVENT is None or coulomb else NCU_TRAFFIC_PER_EVENT * events_per_launch
+    traffic = (COULOMB_NCU["traffic_per_event"] if coulomb else NCU_TRAFFIC_PER_EVENT) * events_per_launch
     total_kernel_ms = sum(v["ms"] for v in kernel_times.values()) or 1.0
     kernels = {name: {"launches": v["launches"], "ms_per_launch": v["ms"] / max(v["launches"], 1),
                       "share": v["ms"] / total_kernel_ms}
@@ -461,6 +466,8 @@ def gpu_arm(args):
                 "ms_per_launch": dominant_s * 1000.0, "neighbours_per_event": nb,
                 "refined_per_event": refined / max(events_done, 1), "fallback_events": fallbacks,
                 "kernels": kernels}
+    if coulomb:
+        roofline["fp64_pipe_active"] = COULOMB_NCU["fp64_pipe_active"]
     cpu = None
     if not args.no_cpu_baseline and world == 1:
         import concurrent.futures
@@ -624,8 +631,10 @@ def water_gpu_arm(args):
             "e2e": {"value": e2e_value, "unit": "events/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": h2d,
                     "pipelining": "two batches take the steps in turn; each batch's copies overlap the other's run"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": None, "peak_source": peak_kind,
-                         "kernel": "jf::water_kernel", "bytes_per_event": bytes_per_event},
+                         "frac": achieved / peak,
+                         "traffic": WATER_NCU["traffic_per_event"] * args.chains * args.events,
+                         "peak_source": peak_kind, "kernel": "jf::water_kernel", "bytes_per_event": bytes_per_event,
+                         "fp64_pipe_active": WATER_NCU["fp64_pipe_active"]},
             "cpu_baseline": cpu, "gpu_launches": args.steps, "clocks": clocks.summary()}
     print(json.dumps(line))
     if world > 1:
