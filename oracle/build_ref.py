@@ -6,7 +6,8 @@ cffi builders compile (``jellyfysh/potential/merged_image_coulomb_potential/merg
 ``jellyfysh/potential/inverse_power_coulomb_bounding_potential/inverse_power_coulomb_bounding_potential.c``).  This
 recipe compiles each, where it lies in the reference tree, into its own shared library under ``oracle/_ref/`` (both
 define ``derivative``), with floating-point contraction off as on the x86-64 baseline the reference is built for.
-The reference tree is found through ``JELLYFYSH_REFERENCE`` or at /root/reference; without it nothing is built.
+The reference tree is the ``tree`` argument of ``build`` or the ``JELLYFYSH_REFERENCE`` environment variable (there
+is no default); without one nothing is built.
 """
 import os
 import subprocess
@@ -22,14 +23,15 @@ SOURCES = {
 }
 
 
-def reference_tree():
-    tree = os.environ.get("JELLYFYSH_REFERENCE", "/root/reference")
-    return tree if os.path.isdir(os.path.join(tree, "jellyfysh", "potential")) else None
+def reference_tree(tree=None):
+    tree = tree or os.environ.get("JELLYFYSH_REFERENCE")
+    return tree if tree and os.path.isdir(os.path.join(tree, "jellyfysh", "potential")) else None
 
 
-def build(force: bool = False):
-    """Compile the reference's C files into oracle/_ref/; returns the built paths (empty without the reference)."""
-    tree = reference_tree()
+def build(tree=None, force: bool = False):
+    """Compile the reference's C files of the tree ``tree`` (or JELLYFYSH_REFERENCE) into oracle/_ref/; returns the
+    built paths (empty without a reference tree)."""
+    tree = reference_tree(tree)
     if tree is None:
         return []
     os.makedirs(REF_DIR, exist_ok=True)
@@ -48,4 +50,5 @@ def build(force: bool = False):
 
 
 if __name__ == "__main__":
-    print("\n".join(build(force="--force" in sys.argv)) or "no reference tree: nothing built")
+    trees = [a for a in sys.argv[1:] if not a.startswith("--")]
+    print("\n".join(build(trees[0] if trees else None, force="--force" in sys.argv)) or "no reference tree: nothing built")

@@ -193,7 +193,8 @@ def main(tree):
 
 
 if __name__ == "__main__":
+    from _tree import tree_argument
     if len(sys.argv) > 1 and sys.argv[1] == "--one":
         run_one(sys.argv[2], sys.argv[3], sys.argv[4])
     else:
-        main(sys.argv[1] if len(sys.argv) > 1 else "/tmp/jf_ref")
+        main(tree_argument(sys.argv))

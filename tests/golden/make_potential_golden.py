@@ -120,5 +120,6 @@ def main(tree: str, output: str) -> None:
 
 
 if __name__ == "__main__":
-    tree_path = sys.argv[1] if len(sys.argv) > 1 else "/tmp/jf_ref"
+    from _tree import tree_argument
+    tree_path = tree_argument(sys.argv)
     main(tree_path, os.path.join(os.path.dirname(os.path.abspath(__file__)), "potential_known_answers.json"))

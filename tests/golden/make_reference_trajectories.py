@@ -422,8 +422,9 @@ def main(tree: str, names) -> None:
 
 
 if __name__ == "__main__":
+    from _tree import tree_argument
     if len(sys.argv) > 1 and sys.argv[1] == "--one":
         run_one(sys.argv[2], sys.argv[3])
     else:
-        tree_path = sys.argv[1] if len(sys.argv) > 1 else "/tmp/jf_ref"
+        tree_path = tree_argument(sys.argv)
         main(tree_path, sys.argv[2:] or list(SYSTEMS))

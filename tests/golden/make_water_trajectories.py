@@ -406,7 +406,8 @@ def main(tree, names):
 
 
 if __name__ == "__main__":
+    from _tree import tree_argument
     if len(sys.argv) > 1 and sys.argv[1] == "--one":
         run_one(sys.argv[2], sys.argv[3])
     else:
-        main(sys.argv[1] if len(sys.argv) > 1 else "/tmp/jf_ref", sys.argv[2:] or list(SYSTEMS))
+        main(tree_argument(sys.argv), sys.argv[2:] or list(SYSTEMS))
