@@ -39,13 +39,10 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "events/s on 1 GB300, batched mixed-precision vs plain FP64 at <=1e-9 rel err"
-WORKLOAD = dict(workload="lennard_jones_chains_4096x1024_cell_bounding", chains=4096, n=1024, density=0.8,
-                beta=1.0 / 1.2, cells_per_side=12, neighbor_layers=3, chain_time=2.0, far="cell_bounding",
-                jitter=0.05, estimator_points=10, estimator_prefactor=1.5)
-COULOMB_WORKLOAD = dict(workload="coulomb_replicas_1024x32_cell_veto", chains=1024, n=32, hard_core_radius=0.05,
-                        system_length=1.0, beta=1.0, cells_per_side=8, neighbor_layers=1, chain_time=0.7,
-                        coulomb_prefactor=1.0, bound_prefactor=1.5837, ewald_alpha=3.45, fourier_cutoff=6,
-                        position_cutoff=2, far="cell_veto", estimator_points=10, estimator_prefactor=1.0)
+from jellyfysh_gb300 import workloads as _workloads  # noqa: E402
+
+WORKLOAD = _workloads.LENNARD_JONES
+COULOMB_WORKLOAD = _workloads.COULOMB
 WATER_WORKLOAD = dict(workload="water_chains_512x64_molecular_coulomb", chains=512, molecules=64,
                       system_length=12.42, temperature_kelvin=300.0, chain_time=2.0, lifting="inside_first")
 NEAR_CELLS = (2 * WORKLOAD["neighbor_layers"] + 1) ** 3  # cells scanned for pair candidates per event
@@ -74,6 +71,8 @@ def parse():
     p.add_argument("--groups", type=int, default=1, help="chain groups on streams of their own (0 = autotune)")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-fp64", action="store_true")
+    p.add_argument("--no-parity", action="store_true")
+    p.add_argument("--fp64-events", type=int, default=16, help="events per chain of the batched FP64 comparison")
     p.add_argument("--workload", default="lennard_jones", choices=["lennard_jones", "coulomb", "water"])
     args = p.parse_args()
     if args.workload == "water" and "--chains" not in sys.argv:
@@ -99,49 +98,10 @@ def data_of(args):
     return "synthetic: seeded simple-cubic lattice + uniform jitter"
 
 
-def make_coulomb_workload(chains, seed_offset=0):
-    """Replicas of 32 point charges (16 of each sign) with a hard core in the unit cube, cell veto on 8^3 cells."""
-    from jellyfysh_gb300 import ChainSpec, systems
-    w = COULOMB_WORKLOAD
-    rng = np.random.default_rng(4321 + seed_offset)
-    specs, positions = [], []
-    for c in range(chains):
-        specs.append(ChainSpec(n=w["n"], system_length=w["system_length"], cells_per_side=w["cells_per_side"],
-                               neighbor_layers=w["neighbor_layers"], potential="coulomb", far=w["far"],
-                               hs_radius=w["hard_core_radius"], beta=w["beta"], chain_time=w["chain_time"],
-                               coulomb_prefactor=w["coulomb_prefactor"], bound_prefactor=w["bound_prefactor"],
-                               ewald_alpha=w["ewald_alpha"], fourier_cutoff=w["fourier_cutoff"],
-                               position_cutoff=w["position_cutoff"], estimator_points=w["estimator_points"],
-                               estimator_prefactor=w["estimator_prefactor"], initial_active=int(rng.integers(w["n"])),
-                               initial_direction=int(rng.integers(3))))
-        positions.append(systems.random_sequential_addition(w["n"], w["hard_core_radius"], w["system_length"], rng))
-    charges = [systems.alternating_charges(w["n"])] * chains
-    return specs, positions, charges, w["system_length"]
-
-
 def build_workload(args, chains, seed_offset=0):
     """(specs, positions, charges or None, box length) of the selected atomic workload."""
-    if args.workload == "coulomb":
-        return make_coulomb_workload(chains, seed_offset)
-    specs, positions, length = make_workload(chains, seed_offset)
-    return specs, positions, None, length
-
-
-def make_workload(chains, seed_offset=0):
-    from jellyfysh_gb300 import ChainSpec, systems
-    n = WORKLOAD["n"]
-    length = systems.lennard_jones_box(n, WORKLOAD["density"])
-    rng = np.random.default_rng(1234 + seed_offset)
-    specs, positions = [], []
-    for c in range(chains):
-        specs.append(ChainSpec(n=n, system_length=length, cells_per_side=WORKLOAD["cells_per_side"],
-                               potential="lennard_jones", far=WORKLOAD["far"],
-                               neighbor_layers=WORKLOAD["neighbor_layers"], beta=WORKLOAD["beta"],
-                               chain_time=WORKLOAD["chain_time"], estimator_points=WORKLOAD["estimator_points"],
-                               estimator_prefactor=WORKLOAD["estimator_prefactor"],
-                               initial_active=int(rng.integers(n)), initial_direction=int(rng.integers(3))))
-        positions.append(systems.simple_cubic_jitter(n, length, WORKLOAD["jitter"], rng))
-    return specs, positions, length
+    from jellyfysh_gb300 import workloads
+    return workloads.BUILDERS[args.workload][1](chains, seed_offset)
 
 
 class ClockSampler:
@@ -212,11 +172,7 @@ def measured_peaks():
 def cpu_chains(threads, pool, seed_offset=99, args=None):
     """One oracle chain (C restatement of the reference's event loop) of the workload per host thread."""
     import oracle
-    if args is not None and args.workload == "coulomb":
-        specs, positions, charges, _ = make_coulomb_workload(threads, seed_offset=seed_offset)
-    else:
-        specs, positions, _ = make_workload(threads, seed_offset=seed_offset)
-        charges = None
+    specs, positions, charges, _ = build_workload(args, threads, seed_offset=seed_offset)
     potentials = {"hard_sphere": oracle.POT_HARD_SPHERE, "lennard_jones": oracle.POT_LENNARD_JONES,
                   "coulomb": oracle.POT_COULOMB}
     fars = {"none": oracle.FAR_NONE, "cell_veto": oracle.FAR_CELL_VETO, "cell_bounding": oracle.FAR_CELL_BOUNDING}
@@ -245,6 +201,101 @@ def cpu_run(pool, chains, seconds, chunk=500):
     start = time.perf_counter()
     done = sum(pool.map(work, chains))
     return done, time.perf_counter() - start
+
+
+PARITY_CHAINS = 16  # chains of the benchmarked batch replayed in the FP64 path
+PARITY_ORACLE_EVENTS = 1000  # events per chain compared with the oracle
+
+
+def time_exact(batch, stream, device, events, first, count, per_chain=False):
+    """events/s of the plain FP64 path (mode "exact") on chains [first, first + count) of the batch, all in one
+    launch or one launch per chain, device-timed with CUDA events on the launching stream."""
+    import torch
+    torch.cuda.synchronize(device)
+    before = batch.state()
+    begin = torch.cuda.Event(enable_timing=True)
+    end = torch.cuda.Event(enable_timing=True)
+    begin.record(stream)
+    if per_chain:
+        for c in range(first, first + count):
+            batch.run(events, mode="exact", first=c, count=1, sync=False)
+    else:
+        batch.run(events, mode="exact", first=first, count=count, sync=False)
+    end.record(stream)
+    torch.cuda.synchronize(device)
+    batch.check_status()
+    ms = begin.elapsed_time(end)
+    after = batch.state()
+    done = int(after["events"][first:first + count].sum() - before["events"][first:first + count].sum())
+    return {"value": done / (ms / 1000.0), "unit": "events/s", "events": done, "ms": ms,
+            "sample": "%d chains x %d events, %s" % (count, events, "one launch per chain" if per_chain
+                                                      else "one launch, one warp per chain")}
+
+
+def parity_record(args, specs, positions, charges, batch, events, state, final_positions):
+    """The first PARITY_CHAINS chains of the benchmarked batch, replayed from their initial state in the plain FP64
+    path for the `events` events each ran in the mixed path: positions and chain states compared bit for bit.  Then
+    the same chains' first PARITY_ORACLE_EVENTS events in the mixed path against the oracle (test infrastructure,
+    the checker): discrete outcomes exactly, event times by their largest relative difference."""
+    import concurrent.futures
+    import dataclasses
+    import oracle
+    from jellyfysh_gb300 import ChainBatch
+    p = min(PARITY_CHAINS, len(specs))
+    sub_specs = [dataclasses.replace(specs[c], rng_key=batch.keys[c]) for c in range(p)]
+    sub_charges = None if charges is None else charges[:p]
+    replay = ChainBatch(sub_specs, positions[:p], sub_charges, device=str(batch.device))
+    replay.run(events, mode="exact")
+    replay.check_status()
+    got = replay.state()
+    fields = ("time_q", "time_r", "eoc_q", "eoc_r", "events", "active", "direction", "n_surplus", "occ_cell",
+              "lift_sum", "liftings")
+    state_equal = all(np.array_equal(got[f], state[f]) for f in fields)
+    positions_equal = all(np.array_equal(replay.positions(c), final_positions[c]) for c in range(p))
+    replay.close()
+    # the mixed path against the oracle, event by event
+    logged = ChainBatch(sub_specs, positions[:p], sub_charges, device=str(batch.device))
+    n_log = PARITY_ORACLE_EVENTS
+    logs = logged.run(n_log, mode="mixed", log_capacity=n_log)
+    logged.check_status()
+    logged.close()
+    chains = cpu_chains_for(sub_specs, positions[:p], sub_charges)
+    with concurrent.futures.ThreadPoolExecutor(max_workers=min(p, host_threads())) as pool:
+        expected = list(pool.map(lambda chain: chain.run(n_log), chains))
+    mismatches, max_rel = 0, 0.0
+    for c in range(p):
+        discrete = np.zeros(n_log, dtype=bool)
+        for field in ("kind", "moved", "target", "new_active", "new_direction", "accepted"):
+            discrete |= logs[c][field] != expected[c][field]
+        mismatches += int(discrete.sum())
+        t_gpu = logs[c]["time_q"] + logs[c]["time_r"]
+        t_cpu = expected[c]["time_q"] + expected[c]["time_r"]
+        max_rel = max(max_rel, float(np.max(np.abs(t_gpu - t_cpu) / np.maximum(np.abs(t_cpu), 1e-300))))
+    return {"replayed_chains": p, "events_per_chain": events, "replay": "FP64 path from the initial state",
+            "state_bitwise_equal": bool(state_equal), "positions_bitwise_equal": bool(positions_equal),
+            "oracle_chains": p, "oracle_events_per_chain": n_log, "discrete_mismatches": mismatches,
+            "max_rel_time_err": max_rel, "bound": 1e-9}
+
+
+def cpu_chains_for(specs, positions, charges):
+    """Oracle chains (the C restatement of the reference's event loop) of the given chain parameters."""
+    import oracle
+    potentials = {"hard_sphere": oracle.POT_HARD_SPHERE, "lennard_jones": oracle.POT_LENNARD_JONES,
+                  "coulomb": oracle.POT_COULOMB}
+    fars = {"none": oracle.FAR_NONE, "cell_veto": oracle.FAR_CELL_VETO, "cell_bounding": oracle.FAR_CELL_BOUNDING}
+    chains = []
+    for c, spec in enumerate(specs):
+        system = oracle.make_system(
+            n=spec.n, system_length=spec.system_length, cells_per_side=spec.cells_per_side,
+            neighbor_layers=spec.neighbor_layers, max_occupants=spec.max_occupants, beta=spec.beta,
+            chain_time=spec.chain_time, initial_active=spec.initial_active, initial_direction=spec.initial_direction,
+            potential=potentials[spec.potential], far=fars[spec.far], hs_radius=spec.hs_radius,
+            lj_prefactor=spec.lj_prefactor, lj_sigma=spec.lj_sigma, coulomb_prefactor=spec.coulomb_prefactor,
+            bound_prefactor=spec.bound_prefactor, ewald_alpha=spec.ewald_alpha, fourier_cutoff=spec.fourier_cutoff,
+            position_cutoff=spec.position_cutoff, estimator_points=spec.estimator_points,
+            estimator_prefactor=spec.estimator_prefactor, rng_key=spec.rng_key)
+        chains.append(oracle.Chain(system, positions[c], None if charges is None else charges[c]))
+    return chains
 
 
 def host_threads():
@@ -359,6 +410,10 @@ def gpu_arm(args):
     fallbacks = int(state1["refine_fallbacks"].sum() - state0["refine_fallbacks"].sum())
     # whole job: events of all ranks over the longest rank's timed region
     _, total_ms, value = replicas.timed_throughput(events_done, elapsed_ms, device)
+    # the state the parity record replays to: every chain has run (warmup + steps) x events events
+    events_before_e2e = int(state1["events"][0])
+    bench_state = state1[:PARITY_CHAINS].copy()
+    bench_pos = [batch.positions(c) for c in range(min(PARITY_CHAINS, batch.n_chains))]
 
     # end to end through ChainBatch with host buffers: every step uploads the chain state from pinned host memory
     # (the FP32 mirror is rebuilt on the device from the uploaded positions), runs, and reads positions and chain
@@ -413,25 +468,21 @@ def gpu_arm(args):
     pair[1].close()
     del pair
 
-    # plain FP64, one chain per launch (the baseline of the mixed-precision batching)
-    fp64 = None
+    # the precision comparison: the plain FP64 path over the same batch (every chain, one warp per chain, one
+    # launch), and one chain per launch as the unbatched FP64 path; device-timed on the launching stream
+    fp64 = fp64_batched = None
     if not args.no_fp64:
-        fp64_chains, fp64_events = 8, 16
-        torch.cuda.synchronize(device)
-        f_begin = torch.cuda.Event(enable_timing=True)
-        f_end = torch.cuda.Event(enable_timing=True)
-        s_before = batch.state()
-        f_begin.record(stream)
-        for c in range(fp64_chains):
-            batch.run(fp64_events, mode="exact", first=c, count=1, sync=False)
-        f_end.record(stream)
-        torch.cuda.synchronize(device)
-        f_ms = f_begin.elapsed_time(f_end)
-        s_after = batch.state()
-        f_done = int(s_after["events"][:fp64_chains].sum() - s_before["events"][:fp64_chains].sum())
-        fp64 = {"value": f_done / (f_ms / 1000.0), "unit": "events/s",
-                "sample": "%d chains x %d events, one launch per chain" % (fp64_chains, fp64_events),
-                "speedup_of_batched_mixed": value / (f_done / (f_ms / 1000.0))}
+        fp64_batched = time_exact(batch, stream, device, events=args.fp64_events, first=0, count=batch.n_chains)
+        fp64_batched["speedup_of_batched_mixed"] = value / fp64_batched["value"]
+        fp64 = time_exact(batch, stream, device, events=16, first=0, count=64, per_chain=True)
+        fp64["speedup_of_batched_mixed"] = value / fp64["value"]
+        fp64["sample"] = "64 chains x 16 events, one launch per chain"
+
+    # parity of the benchmarked run: chains of the batch replayed from their initial state in the FP64 path for the
+    # events they ran in the mixed path, bit for bit, and the event log of their first events against the oracle
+    parity = None
+    if not args.no_parity:
+        parity = parity_record(args, specs, positions, charges, batch, events_before_e2e, bench_state, bench_pos)
 
     if rank != 0:
         if world > 1:
@@ -492,7 +543,7 @@ def gpu_arm(args):
             "e2e": {"value": e2e_value, "unit": "events/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "pipelining": "two batches take the steps in turn; each batch's copies overlap the other's run"},
             "roofline": roofline, "cpu_baseline": cpu, "gpu_launches": launches, "clocks": clocks.summary(),
-            "fp64_one_chain_per_launch": fp64}
+            "fp64_batched": fp64_batched, "fp64_one_chain_per_launch": fp64, "parity": parity}
     print(json.dumps(line))
     if world > 1:
         dist.barrier()

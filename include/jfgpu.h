@@ -119,13 +119,13 @@ int jfgpu_merged_image_coulomb_derivative(double alpha, int32_t fourier_cutoff, 
                                           double *out, int32_t *status, void *stream);
 /* The same derivative for callers that cannot allocate device memory (no counterpart in the reference, whose
  * C extension keeps its table in host memory).  jfgpu_merged_image_coulomb_derivative allocates its
- * Fourier-coefficient table on every call; callers issuing work while a stream is captured into a CUDA graph,
- * hosts that must not enter the CUDA allocator while running, and plug-ins inside another framework's memory pool
- * cannot.  This entry point keeps the table in a fixed file-scope device array (32 KiB, held by every GPU that loads
- * the library until the process exits) and calls no allocation routine.  Limit: fourier_cutoff <= 15, larger
- * values return JFGPU_ERROR_ARGUMENT.  Its first call on a device looks up the array's device address with that
- * device current; make that first call before any stream capture.  Every call shares the array and rewrites it:
- * calls that overlap on the GPU (different streams without ordering) race. */
+ * Fourier-coefficient table on every call; hosts that must not enter the CUDA allocator while running (real-time
+ * loops, a fixed memory budget) and plug-ins inside another framework's memory pool cannot.  This entry point keeps
+ * the table in a fixed file-scope device array (32 KiB, held by every GPU that loads the library until the process
+ * exits), fills it on the device from the parameters passed by value, and calls no allocation routine.  Limit:
+ * fourier_cutoff <= 15, larger values return JFGPU_ERROR_ARGUMENT.  Its first call on a device looks up the array's
+ * device address with that device current; make that first call before any stream capture.  Every call shares the
+ * array and rewrites it: calls that overlap on the GPU (different streams without ordering) race. */
 int jfgpu_merged_image_coulomb_derivative_noalloc(double alpha, int32_t fourier_cutoff, int32_t position_cutoff,
                                                   double prefactor, double system_length, const double *velocity,
                                                   const double *separation, const double *charges, int64_t n,
@@ -305,6 +305,7 @@ typedef struct {
                                      direction of motion (the excess displacement of the chains, whose ratio to the
                                      total displacement gives the pressure: beta P / rho = 1 + lift_sum / (v t)) */
     int64_t liftings;             /* accepted liftings (pair, bounded, cell-bounding and cell-veto events) */
+    int64_t staged_screens;       /* mixed mode: FP32 screens that read the role words from shared memory */
 } JfgpuChainState;
 
 /* one committed event (device log array [n_chains][log_capacity]) */
@@ -421,6 +422,12 @@ int jfgpu_chains_run(JfgpuEngine *engine, const JfgpuBuffers *buffers, int64_t f
 
 /* Autotuned launch shape of the mixed mode: warps per block used by jfgpu_chains_run (1..8). */
 int jfgpu_chains_set_block_warps(JfgpuEngine *engine, int32_t warps_per_block);
+
+/* Mixed mode: an event whose refine list (the FP32 near-winners and flagged candidates) holds more than `limit`
+ * entries is re-solved entirely in FP64 (counted in refine_fallbacks).  1..JFGPU_REFINE_LIST_MAX, default the
+ * maximum; every limit gives the same events, times and positions. */
+#define JFGPU_REFINE_LIST_MAX 28
+int jfgpu_chains_set_refine_limit(JfgpuEngine *engine, int32_t limit);
 
 /* Rewrite the FP32 mirror (buffers->positions32: x, y, z, charge) of chains [first_chain, first_chain + count) from
  * their FP64 positions (and charges): for hosts that upload positions between runs, instead of uploading the

@@ -81,7 +81,7 @@ class ChainState(ctypes.Structure):
                 ("active", ctypes.c_int32), ("direction", ctypes.c_int32),
                 ("eoc_new_active", ctypes.c_int32), ("occ_active", ctypes.c_int32), ("occ_cell", ctypes.c_int32),
                 ("n_surplus", ctypes.c_int32), ("status", ctypes.c_int32), ("stopped", ctypes.c_int32),
-                ("lift_sum", ctypes.c_double), ("liftings", ctypes.c_int64)]
+                ("lift_sum", ctypes.c_double), ("liftings", ctypes.c_int64), ("staged_screens", ctypes.c_int64)]
 
 
 class Event(ctypes.Structure):
@@ -148,6 +148,7 @@ SIGNATURES = {
     "jfgpu_chains_run": (ctypes.c_int, [_P, ctypes.POINTER(Buffers), _I64, _I64, _I64, _D, _D, _I32, _P, _I64,
                                         _P]),
     "jfgpu_chains_set_block_warps": (ctypes.c_int, [_P, _I32]),
+    "jfgpu_chains_set_refine_limit": (ctypes.c_int, [_P, _I32]),
     "jfgpu_chains_set_groups": (ctypes.c_int, [_P, _I32]),
     "jfgpu_chains_set_graphs": (ctypes.c_int, [_P, _I32]),
     "jfgpu_chains_refresh_mirror": (ctypes.c_int, [_P, ctypes.POINTER(Buffers), _I64, _I64, _P]),

@@ -49,7 +49,7 @@ STATE_DTYPE = np.dtype([("time_q", np.float64), ("time_r", np.float64), ("eoc_q"
                         ("active", np.int32), ("direction", np.int32),
                         ("eoc_new_active", np.int32), ("occ_active", np.int32), ("occ_cell", np.int32),
                         ("n_surplus", np.int32), ("status", np.int32), ("stopped", np.int32),
-                        ("lift_sum", np.float64), ("liftings", np.int64)])
+                        ("lift_sum", np.float64), ("liftings", np.int64), ("staged_screens", np.int64)])
 assert EVENT_DTYPE.itemsize == ctypes.sizeof(_lib.Event)
 assert STATE_DTYPE.itemsize == ctypes.sizeof(_lib.ChainState)
 
@@ -203,6 +203,11 @@ class ChainBatch:
     # ------------------------------------------------------------------------------------------------
     def set_block_warps(self, warps: int) -> None:
         _lib.check(self.lib.jfgpu_chains_set_block_warps(self._engine, int(warps)), "jfgpu_chains_set_block_warps")
+
+    def set_refine_limit(self, limit: int) -> None:
+        """Mixed mode: events with more than ``limit`` near-winners (1..28) are re-solved entirely in FP64 (the
+        results do not depend on it; a small limit exercises the whole-event FP64 re-solve)."""
+        _lib.check(self.lib.jfgpu_chains_set_refine_limit(self._engine, int(limit)), "jfgpu_chains_set_refine_limit")
 
     # ------------------------------------------------------------------------------------------------
     # checkpoint / resume (the reference dumps its whole mediator with dill, dumping_output_handler.py:70-90, and

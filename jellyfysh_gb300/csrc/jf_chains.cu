@@ -108,7 +108,7 @@ struct WarpState {
     double pa[3];
     double ts_q, ts_r, eoc_q, eoc_r;
     double lift_sum;
-    long long events, warnings, fallbacks, candidates, refined, liftings;
+    long long events, warnings, fallbacks, candidates, refined, liftings, staged;
     int active, direction, eoc_new, occ_active, occ_cell, n_surplus, status, stop;
     // the merged-image thinning derivative of the event against unit real_target, when the warp computed it
     double real_value = 0.0;
@@ -129,6 +129,7 @@ struct RunArgs {
     long long first_chain, count, max_events;
     double stop_q, stop_r;
     int has_stop;
+    int refine_limit;  // refine lists longer than this re-solve their event in FP64 (1 .. kRefineMax)
 };
 
 // int(x / side) along one axis (cuboid_cells.py:190-211), evaluated exactly without a division: the exact float
@@ -806,6 +807,7 @@ template <int FAR>
 __host__ __device__ constexpr bool stages_roles() { return FAR < 0 || FAR == JFGPU_FAR_CELL_BOUNDING; }
 constexpr int32_t kListOverflow = 1;
 constexpr int32_t kListSkip = 2;
+constexpr int32_t kListStaged = 4;  // the screen read the role words from shared memory
 
 // list entry: target in bits 0-19, screening path in bits 20-23, bit 30 for a far (cell-bounding) candidate
 constexpr int32_t kCodeFar = 1 << 30;
@@ -1062,11 +1064,11 @@ __global__ void __launch_bounds__(256, 4) screen_kernel(RunArgs A, RefineList *l
             if (take && offset == q) queued[q] = code[i];
         total += __popc(mask);
     }
-    overflow = warp_max_int(overflow) || total > kRefineMax;
+    overflow = warp_max_int(overflow) || total > A.refine_limit;
     const int screened = warp_sum_int(count);
     if (lane == 0) {
         list.count = total < kRefineMax ? total : kRefineMax;
-        list.flags = overflow ? kListOverflow : 0;
+        list.flags = (overflow ? kListOverflow : 0) | (staged ? kListStaged : 0);
         list.screened = screened;
     }
     // the entries at the first kRefineSlots offsets go to the queues of their paths
@@ -1098,6 +1100,7 @@ __device__ inline void load_lifting(const JfgpuChainState &g, const RunArgs &A, 
     w.refined = g.refined;
     w.lift_sum = g.lift_sum;
     w.liftings = g.liftings;
+    w.staged = g.staged_screens;
     w.active = g.active;
     w.direction = g.direction;
     w.eoc_new = g.eoc_new_active;
@@ -1201,6 +1204,7 @@ __global__ void __launch_bounds__(32) resolve_kernel(RunArgs A, const RefineList
     load_lifting(g, A, ch, w);
     w.candidates += list.screened;
     w.refined += list.count;
+    if (list.flags & kListStaged) w.staged += 1;
 
     Cand best = cand_none();
     int st = single_candidates(A, ch, sp, w, w.occ_cell, w.events, best);
@@ -1256,6 +1260,7 @@ __global__ void __launch_bounds__(32) resolve_kernel(RunArgs A, const RefineList
     g.refined = w.refined;
     g.lift_sum = w.lift_sum;
     g.liftings = w.liftings;
+    g.staged_screens = w.staged;
     g.active = w.active;
     g.direction = w.direction;
     g.eoc_new_active = w.eoc_new;
@@ -1435,6 +1440,7 @@ __global__ void init_kernel(EngineView view, long long n_chains, double *positio
     g.stopped = 0;
     g.lift_sum = 0.0;
     g.liftings = 0;
+    g.staged_screens = 0;
     if (status == JFGPU_STATUS_OK) {
         // the activator's first update after the start of the run: the initial active unit leaves the occupancy
         RunArgs A;
@@ -1681,6 +1687,7 @@ cudaError_t launch_run(const EngineView &view, const JfgpuBuffers &b, long long 
     A.stop_q = stop_q;
     A.stop_r = stop_r;
     A.has_stop = isinf(stop_q) ? 0 : 1;
+    A.refine_limit = plan.refine_limit < 1 ? 1 : (plan.refine_limit > kRefineMax ? kRefineMax : plan.refine_limit);
     int warps = plan.warps;
     if (warps < 1) warps = 1;
     if (warps > 8) warps = 8;

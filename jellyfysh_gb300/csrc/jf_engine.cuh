@@ -84,6 +84,7 @@ struct LaunchPlan {
     cudaStream_t stream = nullptr;
     int warps = 4;                          // warps per block of the screening and FP64 kernels
     int groups = 1;                         // chain groups of the mixed mode
+    int refine_limit = JFGPU_REFINE_LIST_MAX;  // refine lists longer than this re-solve their event in FP64
     cudaStream_t *group_streams = nullptr;  // [groups] when groups > 1
     cudaEvent_t fork = nullptr;             // recorded on the caller's stream, waited for by every group
     cudaEvent_t *join = nullptr;            // [groups] recorded by every group, waited for by the caller's stream

@@ -120,6 +120,7 @@ struct JfgpuEngine {
     int64_t particles = 0, occupancy_slots = 0, table_bytes = 0;
     int64_t launches = 0;
     int block_warps = 4;
+    int refine_limit = JFGPU_REFINE_LIST_MAX;
     void *refine_lists = nullptr;  // per-chain refine lists of the mixed-precision rounds
     void *refined = nullptr;       // per-chain FP64 re-solves of the first list entries
     void *refine_queue = nullptr;  // the re-solves queued by screening path
@@ -760,6 +761,12 @@ int jfgpu_chains_set_block_warps(JfgpuEngine *e, int32_t warps) {
     return JFGPU_OK;
 }
 
+int jfgpu_chains_set_refine_limit(JfgpuEngine *e, int32_t limit) {
+    if (!e || limit < 1 || limit > JFGPU_REFINE_LIST_MAX) return JFGPU_ERROR_ARGUMENT;
+    e->refine_limit = limit;
+    return JFGPU_OK;
+}
+
 static bool buffers_ok(const JfgpuEngine *e, const JfgpuBuffers *b) {
     return e && b && b->positions && b->positions32 && b->occupancy && b->surplus && b->roles && b->state;
 }
@@ -856,6 +863,7 @@ static LaunchPlan make_plan(const JfgpuEngine *e, void *stream_ptr) {
     LaunchPlan plan;
     plan.stream = static_cast<cudaStream_t>(stream_ptr);
     plan.warps = e->block_warps;
+    plan.refine_limit = e->refine_limit;
     plan.groups = e->groups;
     plan.group_streams = e->groups > 1 ? const_cast<cudaStream_t *>(e->group_streams) : nullptr;
     plan.fork = e->fork;

@@ -306,11 +306,12 @@ int jfgpu_cell_bounding_displacement(const double *bounds_upper, const double *b
 // The merged-image Coulomb derivative for callers that cannot allocate device memory.
 //
 // jfgpu_merged_image_coulomb_derivative allocates its Fourier-coefficient table with cudaMallocAsync on every call.
-// Some callers cannot do that: code that issues work while a stream is being captured into a CUDA graph, hosts that
-// must not enter the CUDA allocator once they are running (real-time loops, embedded controllers with a fixed memory
-// budget), and plug-ins that live inside another framework whose memory pool owns the device.  For them the table
-// lives in the file-scope device array below, of a fixed maximum size, which every GPU that loads this library keeps
-// until the process exits.  The caller still passes every input and output array.
+// Some callers cannot do that: hosts that must not enter the CUDA allocator once they are running (real-time loops,
+// embedded controllers with a fixed memory budget), and plug-ins that live inside another framework whose memory
+// pool owns the device.  For them the table lives in the file-scope device array below, of a fixed maximum size,
+// which every GPU that loads this library keeps until the process exits, and is filled on the device by a small
+// kernel from the parameters passed by value (no host buffer, no copy).  The caller still passes every input and
+// output array.
 // ---------------------------------------------------------------------------------------------------------------
 namespace {
 
@@ -339,6 +340,25 @@ int fourier_scratch(double **address) {
     return JFGPU_OK;
 }
 
+// The Fourier coefficients of merged_image_coulomb_potential.c:77-119 in the table layout [i][j][k] of the cutoff,
+// one thread per entry: every entry of the layout is written (the unused i = 0 plane as zeros), so nothing of an
+// earlier call remains.  The device exp may differ from the host libm's by an ulp; the derivative then differs from
+// the allocating entry point's at the 1e-16 relative level.
+__global__ void fourier_table_kernel(double *table, int nf, double alpha, double system_length) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= nf * nf * nf) return;
+    const int i = e / (nf * nf), j = (e / nf) % nf, k = e % nf;
+    double value = 0.0;
+    if (i > 0) {
+        const double coefficient = (j == 0 && k == 0) ? 1.0 : ((k == 0 || j == 0) ? 2.0 : 4.0);
+        const double norm_sq = i * i + j * j + k * k;
+        const double pi = 3.141592653589793;
+        value = 4.0 * i * coefficient / (norm_sq * system_length * system_length) *
+                exp(-pi * pi * norm_sq / (alpha * alpha));
+    }
+    table[e] = value;
+}
+
 }  // namespace
 
 extern "C" int jfgpu_merged_image_coulomb_derivative_noalloc(double alpha, int32_t fourier_cutoff,
@@ -353,25 +373,11 @@ extern "C" int jfgpu_merged_image_coulomb_derivative_noalloc(double alpha, int32
     double *table = nullptr;
     int error = fourier_scratch(&table);
     if (error) return error;
-    // coefficients on the host with the host libm (merged_image_coulomb_potential.c:77-119); every entry of the
-    // table layout of this cutoff is written, the unused i = 0 plane as zeros, so nothing of an earlier call remains
     const int nf = fourier_cutoff + 1;
-    const size_t count = (size_t)nf * nf * nf;
-    double host[kNoAllocEntries];
-    for (size_t e = 0; e < count; ++e) host[e] = 0.0;
-    for (int k = 0; k < nf; k++)
-        for (int j = 0; j < nf; j++)
-            for (int i = 1; i < nf; i++) {
-                double coefficient = (j == 0 && k == 0) ? 1.0 : ((k == 0 || j == 0) ? 2.0 : 4.0);
-                double norm_sq = i * i + j * j + k * k;
-                host[(i * nf + j) * nf + k] = 4.0 * i * coefficient / (norm_sq * system_length * system_length) *
-                                              std::exp(-M_PI * M_PI * norm_sq / (alpha * alpha));
-            }
-    // a copy from pageable memory waits for the stream's earlier work (the previous call's kernel) and returns
-    // once the host array has been staged, so the stack array may go out of scope afterwards
+    const int count = nf * nf * nf;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
-    if (cudaMemcpyAsync(table, host, count * sizeof(double), cudaMemcpyHostToDevice, s) != cudaSuccess)
-        return JFGPU_ERROR_CUDA;
+    fourier_table_kernel<<<(count + 255) / 256, 256, 0, s>>>(table, nf, alpha, system_length);
+    if (cudaGetLastError() != cudaSuccess) return JFGPU_ERROR_CUDA;
     PotentialArgs a = base_args(kMergedDerivative, velocity, separation, n, out, status);
     a.p0 = prefactor;
     a.charges = charges;

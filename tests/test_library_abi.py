@@ -46,3 +46,4 @@ def test_host_only_entry_points(library):
     assert library.jfgpu_engine_create(None, 0, None, ctypes.byref(handle)) == 2
     assert library.jfgpu_engine_layout(None, None) == 2
     assert library.jfgpu_chains_set_block_warps(None, 4) == 2
+    assert library.jfgpu_chains_set_refine_limit(None, 4) == 2

@@ -1,8 +1,9 @@
 """The allocation-free merged-image Coulomb derivative against the allocating entry point (GPU).
 
-Some callers cannot allocate device memory: code that issues work while a stream is captured into a CUDA graph,
-hosts that must not enter the CUDA allocator while they run, plug-ins that live inside another framework's memory
-pool.  ``jfgpu_merged_image_coulomb_derivative_noalloc`` serves them with its Fourier table in a fixed device array.
+Some callers cannot allocate device memory: hosts that must not enter the CUDA allocator while they run (real-time
+loops, a fixed memory budget), plug-ins that live inside another framework's memory pool.
+``jfgpu_merged_image_coulomb_derivative_noalloc`` serves them with its Fourier table in a fixed device array, filled
+on the device.
 This test calls it through the C ABI twice in a row, with different Ewald parameters (so the second call must
 rewrite the shared table), and compares each result with ``jfgpu_merged_image_coulomb_derivative`` at the
 tolerance of the other potential tests (1e-12 relative).  It lives in a file of its own that pytest collects last.
