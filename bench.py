@@ -408,6 +408,7 @@ def gpu_arm(args):
     candidates = int(state1["candidates"].sum() - state0["candidates"].sum())
     refined = int(state1["refined"].sum() - state0["refined"].sum())
     fallbacks = int(state1["refine_fallbacks"].sum() - state0["refine_fallbacks"].sum())
+    lookups = int(state1["far_lookups"].sum() - state0["far_lookups"].sum())
     # whole job: events of all ranks over the longest rank's timed region
     _, total_ms, value = replicas.timed_throughput(events_done, elapsed_ms, device)
     # the state the parity record replays to: every chain has run (warmup + steps) x events events
@@ -516,6 +517,7 @@ def gpu_arm(args):
                 "bytes_per_event": bytes_per_event, "events_per_launch": events_per_launch,
                 "ms_per_launch": dominant_s * 1000.0, "neighbours_per_event": nb,
                 "refined_per_event": refined / max(events_done, 1), "fallback_events": fallbacks,
+                "far_lookups_per_event": lookups / max(events_done, 1),
                 "kernels": kernels}
     if coulomb:
         roofline["fp64_pipe_active"] = COULOMB_NCU["fp64_pipe_active"]

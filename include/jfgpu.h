@@ -305,7 +305,8 @@ typedef struct {
                                      direction of motion (the excess displacement of the chains, whose ratio to the
                                      total displacement gives the pressure: beta P / rho = 1 + lift_sum / (v t)) */
     int64_t liftings;             /* accepted liftings (pair, bounded, cell-bounding and cell-veto events) */
-    int64_t staged_screens;       /* mixed mode: FP32 screens that read the role words from shared memory */
+    int64_t far_lookups;          /* mixed mode, cell-bounding far field: units whose keyed draw passed the rejection
+                                     by the largest far rate, whose role word the screen then read */
 } JfgpuChainState;
 
 /* one committed event (device log array [n_chains][log_capacity]) */
@@ -388,6 +389,9 @@ typedef struct {
                                      for surplus units bit 24 and the unit's index in the surplus list instead;
                                      bit 25 for the occupancy's active unit */
     JfgpuChainState *state;       /* [n_chains] */
+    float *cell_slots;            /* [occupancy_slots][4]: cell-ordered FP32 mirror of the occupancy, the occupant's
+                                     (x, y, z) and its identifier's bits as the fourth float (bits -1 when empty);
+                                     kept by the engine, rebuilt by jfgpu_chains_refresh_mirror */
 } JfgpuBuffers;
 
 typedef struct {
@@ -429,9 +433,10 @@ int jfgpu_chains_set_block_warps(JfgpuEngine *engine, int32_t warps_per_block);
 #define JFGPU_REFINE_LIST_MAX 28
 int jfgpu_chains_set_refine_limit(JfgpuEngine *engine, int32_t limit);
 
-/* Rewrite the FP32 mirror (buffers->positions32: x, y, z, charge) of chains [first_chain, first_chain + count) from
- * their FP64 positions (and charges): for hosts that upload positions between runs, instead of uploading the
- * mirror as well.  The mirror is otherwise kept by the engine (jfgpu_chains_init and every committed event). */
+/* Rewrite the FP32 mirrors of chains [first_chain, first_chain + count): buffers->positions32 (x, y, z, charge) from
+ * their FP64 positions (and charges), then buffers->cell_slots from the occupancy and that mirror.  For hosts that
+ * upload positions and occupancy between runs, instead of uploading the mirrors as well.  The mirrors are otherwise
+ * kept by the engine (jfgpu_chains_init and every committed event). */
 int jfgpu_chains_refresh_mirror(JfgpuEngine *engine, const JfgpuBuffers *buffers, int64_t first_chain, int64_t count,
                                 void *stream);
 

@@ -81,7 +81,7 @@ class ChainState(ctypes.Structure):
                 ("active", ctypes.c_int32), ("direction", ctypes.c_int32),
                 ("eoc_new_active", ctypes.c_int32), ("occ_active", ctypes.c_int32), ("occ_cell", ctypes.c_int32),
                 ("n_surplus", ctypes.c_int32), ("status", ctypes.c_int32), ("stopped", ctypes.c_int32),
-                ("lift_sum", ctypes.c_double), ("liftings", ctypes.c_int64), ("staged_screens", ctypes.c_int64)]
+                ("lift_sum", ctypes.c_double), ("liftings", ctypes.c_int64), ("far_lookups", ctypes.c_int64)]
 
 
 class Event(ctypes.Structure):
@@ -94,7 +94,7 @@ class Event(ctypes.Structure):
 class Buffers(ctypes.Structure):
     _fields_ = [("positions", ctypes.c_void_p), ("positions32", ctypes.c_void_p), ("charges", ctypes.c_void_p),
                 ("occupancy", ctypes.c_void_p), ("surplus", ctypes.c_void_p), ("roles", ctypes.c_void_p),
-                ("state", ctypes.c_void_p)]
+                ("state", ctypes.c_void_p), ("cell_slots", ctypes.c_void_p)]
 
 
 class Layout(ctypes.Structure):

@@ -49,7 +49,7 @@ STATE_DTYPE = np.dtype([("time_q", np.float64), ("time_r", np.float64), ("eoc_q"
                         ("active", np.int32), ("direction", np.int32),
                         ("eoc_new_active", np.int32), ("occ_active", np.int32), ("occ_cell", np.int32),
                         ("n_surplus", np.int32), ("status", np.int32), ("stopped", np.int32),
-                        ("lift_sum", np.float64), ("liftings", np.int64), ("staged_screens", np.int64)])
+                        ("lift_sum", np.float64), ("liftings", np.int64), ("far_lookups", np.int64)])
 assert EVENT_DTYPE.itemsize == ctypes.sizeof(_lib.Event)
 assert STATE_DTYPE.itemsize == ctypes.sizeof(_lib.ChainState)
 
@@ -176,11 +176,12 @@ class ChainBatch:
         self.occupancy_dev = t.full((O,), -1, dtype=t.int32, device=self.device)
         self.surplus_dev = t.zeros((P,), dtype=t.int32, device=self.device)
         self.roles_dev = t.zeros((P,), dtype=t.int32, device=self.device)
+        self.cell_slots_dev = t.zeros((O, 4), dtype=t.float32, device=self.device)
         self.state_dev = t.zeros((self.n_chains * STATE_DTYPE.itemsize,), dtype=t.uint8, device=self.device)
         self._buffers = _lib.Buffers(positions=_ptr(self.positions_dev), positions32=_ptr(self.positions32_dev),
                                      charges=_ptr(self.charges_dev), occupancy=_ptr(self.occupancy_dev),
                                      surplus=_ptr(self.surplus_dev), roles=_ptr(self.roles_dev),
-                                     state=_ptr(self.state_dev))
+                                     state=_ptr(self.state_dev), cell_slots=_ptr(self.cell_slots_dev))
         with torch.cuda.device(self.device):
             _lib.check(self.lib.jfgpu_chains_init(self._engine, ctypes.byref(self._buffers), self._stream()),
                        "jfgpu_chains_init")
@@ -218,7 +219,7 @@ class ChainBatch:
         self._torch.cuda.synchronize(self.device)
         specs = [dict(dataclasses.asdict(spec), rng_key=int(key)) for spec, key in zip(self.specs, self.keys)]
         arrays = {name: getattr(self, name + "_dev").cpu().numpy()
-                  for name in ("positions", "positions32", "occupancy", "surplus", "roles", "state")}
+                  for name in ("positions", "positions32", "occupancy", "surplus", "roles", "state", "cell_slots")}
         if self.charges_dev is not None:
             arrays["charges"] = self.charges_dev.cpu().numpy()
         np.savez(path, specs=json.dumps(specs), **arrays)
@@ -237,7 +238,7 @@ class ChainBatch:
         per_chain = [positions[offsets[c]:offsets[c + 1]] for c in range(len(specs))]
         per_charges = None if charges is None else [charges[offsets[c]:offsets[c + 1]] for c in range(len(specs))]
         batch.__init__(specs, per_chain, per_charges, device=device)
-        for name in ("positions", "positions32", "occupancy", "surplus", "roles", "state"):
+        for name in ("positions", "positions32", "occupancy", "surplus", "roles", "state", "cell_slots"):
             target = getattr(batch, name + "_dev")
             source = batch._torch.from_numpy(np.ascontiguousarray(data[name])).to(batch.device)
             if source.shape != target.shape or source.dtype != target.dtype:
@@ -247,8 +248,8 @@ class ChainBatch:
         return batch
 
     def refresh_mirror(self, first: int = 0, count: Optional[int] = None) -> None:
-        """Rewrite the FP32 mirror of chains [first, first + count) from their FP64 positions (after the host
-        has written positions_dev)."""
+        """Rewrite the FP32 mirrors of chains [first, first + count) (positions32 from the FP64 positions, the
+        cell slots from the occupancy and positions32), after the host has written positions_dev and occupancy_dev."""
         count = self.n_chains - first if count is None else count
         with self._torch.cuda.device(self.device):
             _lib.check(self.lib.jfgpu_chains_refresh_mirror(self._engine, ctypes.byref(self._buffers), int(first),
@@ -257,7 +258,7 @@ class ChainBatch:
 
     def input_tensors(self):
         """The device buffers a host uploads to set the batch's state: FP64 positions, occupancy, surplus lists,
-        role words and chain states (the FP32 mirror follows from the positions: ``refresh_mirror``)."""
+        role words and chain states (the FP32 mirrors follow from them: ``refresh_mirror``)."""
         return [self.positions_dev, self.occupancy_dev, self.surplus_dev, self.roles_dev, self.state_dev]
 
     def set_graphs(self, enable: bool) -> None:
@@ -372,5 +373,5 @@ class ChainBatch:
 
     # ---- host <-> device state transfer (the end-to-end path of a caller holding host buffers) ----
     def state_tensors(self):
-        return [self.positions_dev, self.positions32_dev, self.occupancy_dev, self.surplus_dev, self.roles_dev,
-                self.state_dev]
+        return [self.positions_dev, self.positions32_dev, self.cell_slots_dev, self.occupancy_dev, self.surplus_dev,
+                self.roles_dev, self.state_dev]

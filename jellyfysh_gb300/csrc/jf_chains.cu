@@ -31,6 +31,20 @@
 
 namespace jf {
 
+// The event-flow functions (candidate solves, single candidates, thinning, commit, occupancy update) are out of line
+// by default; JF_FLOW_INLINE inlines them into their kernels.
+#ifdef JF_FLOW_INLINE
+#define JF_FLOW __forceinline__
+#else
+#define JF_FLOW __noinline__
+#endif
+#ifndef JF_REFINE_THREADS
+#define JF_REFINE_THREADS 64   // threads per block of the FP64 re-solve kernel
+#endif
+#ifndef JF_RESOLVE_THREADS
+#define JF_RESOLVE_THREADS 32  // threads per block of the resolve kernel
+#endif
+
 constexpr unsigned kFull = 0xffffffffu;
 constexpr int kTopK = 4;
 
@@ -108,7 +122,7 @@ struct WarpState {
     double pa[3];
     double ts_q, ts_r, eoc_q, eoc_r;
     double lift_sum;
-    long long events, warnings, fallbacks, candidates, refined, liftings, staged;
+    long long events, warnings, fallbacks, candidates, refined, liftings, far_lookups;
     int active, direction, eoc_new, occ_active, occ_cell, n_surplus, status, stop;
     // the merged-image thinning derivative of the event against unit real_target, when the warp computed it
     double real_value = 0.0;
@@ -123,6 +137,7 @@ struct RunArgs {
     int32_t *occupancy;
     int32_t *surplus;
     int32_t *roles;
+    float4 *cell_slots;  // cell-ordered FP32 mirror of the occupancy (x, y, z, identifier bits; bits -1 empty)
     JfgpuChainState *state;
     JfgpuEvent *log;
     long long log_capacity;
@@ -223,7 +238,7 @@ __device__ inline uint64_t draw_at(uint64_t base, uint32_t target) {
 }
 
 // FP64 candidates of one (active, target) pair of the nearby / surplus taggers, one function per potential
-__device__ __noinline__ int exact_pair_hs(const RunArgs &A, const ChainDev &ch, const WarpState &w, int j,
+__device__ JF_FLOW int exact_pair_hs(const RunArgs &A, const ChainDev &ch, const WarpState &w, int j,
                                          Cand &best) {
     double pj[3], s[3], dt;
     load_pos(A, ch, j, pj);
@@ -233,7 +248,7 @@ __device__ __noinline__ int exact_pair_hs(const RunArgs &A, const ChainDev &ch, 
     return JFGPU_STATUS_OK;
 }
 
-__device__ __noinline__ int exact_pair_lj(const RunArgs &A, const ChainDev &ch, const SpeciesDev &sp,
+__device__ JF_FLOW int exact_pair_lj(const RunArgs &A, const ChainDev &ch, const SpeciesDev &sp,
                                          const WarpState &w, int j, long long ev, Cand &best) {
     double pj[3], s[3], disp;
     load_pos(A, ch, j, pj);
@@ -244,7 +259,7 @@ __device__ __noinline__ int exact_pair_lj(const RunArgs &A, const ChainDev &ch, 
     return JFGPU_STATUS_OK;
 }
 
-__device__ __noinline__ int exact_pair_coulomb(const RunArgs &A, const ChainDev &ch, const WarpState &w, int j,
+__device__ JF_FLOW int exact_pair_coulomb(const RunArgs &A, const ChainDev &ch, const WarpState &w, int j,
                                               long long ev, Cand &best) {
     double pj[3], s[3], dt;
     load_pos(A, ch, j, pj);
@@ -280,7 +295,7 @@ __device__ inline int exact_pair(const RunArgs &A, const ChainDev &ch, const Spe
 }
 
 // FP64 candidate of a far occupant under the cell-bounding potential (cells from the positions, as the handler)
-__device__ __noinline__ int exact_cell_bounding(const RunArgs &A, const ChainDev &ch, const SpeciesDev &sp,
+__device__ JF_FLOW int exact_cell_bounding(const RunArgs &A, const ChainDev &ch, const SpeciesDev &sp,
                                                const WarpState &w, int j, int active_cell, long long ev, Cand &best) {
     double pj[3];
     int target_cell;
@@ -295,7 +310,7 @@ __device__ __noinline__ int exact_cell_bounding(const RunArgs &A, const ChainDev
 }
 
 // cell veto, cell boundary and end of chain: the single candidates of lane 0
-__device__ __noinline__ int single_candidates(const RunArgs &A, const ChainDev &ch, const SpeciesDev &sp,
+__device__ JF_FLOW int single_candidates(const RunArgs &A, const ChainDev &ch, const SpeciesDev &sp,
                                              const WarpState &w, int active_cell, long long ev, Cand &best) {
     const int d = w.direction;
     if (ch.far == JFGPU_FAR_CELL_VETO) {
@@ -347,12 +362,18 @@ __device__ inline int32_t role_of_cell(const ChainDev &ch, int cell) {
     return a[0] | (a[1] << 8) | (a[2] << 16);
 }
 
+// the cell slot of occupancy entry `slot` holds the occupant's FP32 mirror position and identifier (or -1)
+__device__ inline void set_cell_slot(const RunArgs &A, long long slot, int id, const float4 &p) {
+    A.cell_slots[slot] = make_float4(p.x, p.y, p.z, __int_as_float(id));
+}
+
 __device__ inline void occ_insert(const RunArgs &A, const ChainDev &ch, WarpState &w, int cell, int id) {
     int32_t *slots = A.occupancy + ch.occ_off + (long long)cell * ch.max_occ;
     for (int k = 0; k < ch.max_occ; ++k)
         if (slots[k] < 0) {
             slots[k] = id;
             A.roles[ch.pos_off + id] = role_of_cell(ch, cell);
+            set_cell_slot(A, ch.occ_off + (long long)cell * ch.max_occ + k, id, A.positions32[ch.pos_off + id]);
             return;
         }
     A.surplus[ch.pos_off + w.n_surplus] = id;
@@ -360,7 +381,7 @@ __device__ inline void occ_insert(const RunArgs &A, const ChainDev &ch, WarpStat
     w.n_surplus += 1;
 }
 
-__device__ __noinline__ int occ_update(const RunArgs &A, const ChainDev &ch, WarpState &w) {
+__device__ JF_FLOW int occ_update(const RunArgs &A, const ChainDev &ch, WarpState &w) {
     if (w.active != w.occ_active) {
         if (w.occ_active >= 0) occ_insert(A, ch, w, w.occ_cell, w.occ_active);
         JF_TRY(cell_of(A.view, ch, w.pa, w.occ_cell));
@@ -371,6 +392,7 @@ __device__ __noinline__ int occ_update(const RunArgs &A, const ChainDev &ch, War
         for (int k = 0; k < ch.max_occ; ++k)
             if (slots[k] == w.active) {
                 slots[k] = -1;
+                set_cell_slot(A, ch.occ_off + (long long)w.occ_cell * ch.max_occ + k, -1, make_float4(0.f, 0.f, 0.f, 0.f));
                 return JFGPU_STATUS_OK;
             }
         // a surplus unit: its role word (read before it was overwritten above) holds its index in the list;
@@ -454,7 +476,7 @@ __device__ inline void warp_real_rate(const RunArgs &A, const ChainDev &ch, cons
 // Thinning: accept iff uniform(0, bound) < real rate (event_handler_with_bounding_potential.py:95-101).  For
 // Lennard-Jones the decision (and the bound-violation count) is first taken in FP32 from the FP32 mirror; only a
 // decision within the FP32 error margin is re-taken in FP64, so the outcome always equals the FP64 one.
-__device__ __noinline__ int thinning(const RunArgs &A, const ChainDev &ch, const SpeciesDev &sp, WarpState &w, int t,
+__device__ JF_FLOW int thinning(const RunArgs &A, const ChainDev &ch, const SpeciesDev &sp, WarpState &w, int t,
                                     double bounding_rate, long long ev, int &accepted) {
     const double u = uniform53(draw(ch.key, (uint64_t)ev, kRngThin, 0));
     if (ch.potential == JFGPU_POT_LENNARD_JONES) {
@@ -520,7 +542,7 @@ __device__ inline void time_slice(const ChainDev &ch, WarpState &w, double q, do
 }
 
 // commit the winner; returns a status
-__device__ __noinline__ int commit(const RunArgs &A, const ChainDev &ch, const SpeciesDev &sp, WarpState &w, const Cand &best,
+__device__ JF_FLOW int commit(const RunArgs &A, const ChainDev &ch, const SpeciesDev &sp, WarpState &w, const Cand &best,
                              int active_cell, long long chain_index, long long log_index) {
     const long long ev = w.events;
     int moved = w.active;
@@ -800,14 +822,9 @@ __device__ inline float lane_min_unflagged(const float (&key)[kTopK]) {
 // kernel carries a small instruction footprint.  The winner and its time are the FP64 ones: the mixed path equals
 // the FP64 path event for event.
 // ---------------------------------------------------------------------------------------------------------------
-constexpr int kRefineMax = 28;
-constexpr int kStagedRoles = 1024;  // units whose role words the screening kernel stages in shared memory
-// the screening kernels that may run the cell-bounding far field stage role words (dynamic shared memory)
-template <int FAR>
-__host__ __device__ constexpr bool stages_roles() { return FAR < 0 || FAR == JFGPU_FAR_CELL_BOUNDING; }
+constexpr int kRefineMax = JFGPU_REFINE_LIST_MAX;
 constexpr int32_t kListOverflow = 1;
 constexpr int32_t kListSkip = 2;
-constexpr int32_t kListStaged = 4;  // the screen read the role words from shared memory
 
 // list entry: target in bits 0-19, screening path in bits 20-23, bit 30 for a far (cell-bounding) candidate
 constexpr int32_t kCodeFar = 1 << 30;
@@ -819,7 +836,7 @@ __device__ inline int code_path(int32_t code) { return (code >> 20) & 0xF; }
 __device__ inline bool code_far(int32_t code) { return (code & kCodeFar) != 0; }
 
 struct RefineList {
-    int32_t count, flags, screened, pad;
+    int32_t count, flags, screened, far_lookups;
     int32_t code[kRefineMax];
 };
 
@@ -835,6 +852,19 @@ struct RefineQueue {
     int32_t *entries;  // [kPaths][stride], offset to the group's slice
     long long stride;  // n_chains * kRefineSlots
 };
+
+// keyed draw of a pair candidate: only its top 32 bits enter the FP32 screening (uniform within 2^-32)
+__device__ inline uint32_t draw_hi32(uint64_t base, uint32_t target) { return (uint32_t)(draw_at(base, target) >> 32); }
+
+// Nearby cells along one axis: the K cells starting at first = a - layers (wrapped), or the whole axis when the layers
+// cover it (K = m); the same set as the distinct residues of the layer offsets (cuboid_periodic_cells.py:74-100)
+__device__ inline int near_first(int a, int K, int m) {
+    if (K == m) return 0;
+    const int first = a - (K >> 1);
+    return first < 0 ? first + m : first;
+}
+
+constexpr int kNearBatch = 4;  // cell slots each lane loads before it screens them (loads in flight)
 
 template <int POT, int FAR>
 __global__ void __launch_bounds__(256, 4) screen_kernel(RunArgs A, RefineList *lists, RefineQueue queue,
@@ -853,6 +883,7 @@ __global__ void __launch_bounds__(256, 4) screen_kernel(RunArgs A, RefineList *l
             list.count = 0;
             list.flags = kListSkip;
             list.screened = 0;
+            list.far_lookups = 0;
         }
         return;
     }
@@ -862,43 +893,31 @@ __global__ void __launch_bounds__(256, 4) screen_kernel(RunArgs A, RefineList *l
             list.count = 0;
             list.flags = kListOverflow;
             list.screened = 0;
+            list.far_lookups = 0;
         }
         return;
     }
     const int active = g.active, d = g.direction, occ_cell = g.occ_cell, n_surplus = g.n_surplus;
-    // the role words of the chain's units, copied asynchronously into shared memory while the nearby candidates are
-    // screened (16-byte chunks; the far pass reads them from there)
-    extern __shared__ __align__(16) int32_t role_stage[];  // [warps][kStagedRoles] when the far field stages
-    int32_t *my_roles = role_stage + warp * kStagedRoles;
-    const bool staged = stages_roles<FAR>() && far_of<FAR>(ch) == JFGPU_FAR_CELL_BOUNDING && ch.n <= kStagedRoles &&
-                        ((uintptr_t)(A.roles + ch.pos_off) & 15) == 0;
-    if (staged) {
-        const int32_t *src = A.roles + ch.pos_off;
-        const int chunks = ch.n >> 2;
-        for (int k = lane; k < chunks; k += 32) {
-            const unsigned dst = (unsigned)__cvta_generic_to_shared(my_roles + 4 * k);
-            asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(dst), "l"(src + 4 * k) : "memory");
-        }
-        asm volatile("cp.async.commit_group;\n" ::: "memory");
-        for (int k = 4 * chunks + lane; k < ch.n; k += 32) my_roles[k] = src[k];
-    }
+    const int m = ch.m, K = ch.n_res, max_occ = ch.max_occ, n = ch.n;
+    const long long pos_off = ch.pos_off, occ_off = ch.occ_off;
     const uint64_t ev = (uint64_t)g.events;
     const float speed32 = ch.speed32;
     const float inv_beta32 = ch.inv_beta32;
     const float margin = ch.ulp_margin32;
+    const float L32 = ch.L32, half32 = ch.half32;
     const float rel = 1.0f + 1.0f / 1024.0f;
     const float abs_margin = ch.screen_abs32 / speed32;
-    const float4 pa32 = A.positions32[ch.pos_off + active];
+    const float4 pa32 = A.positions32[pos_off + active];
+    int ax[3];
+    cell_axes(ch, occ_cell, ax);
     // single candidates in FP32 bound the threshold: the cell boundary and the end of chain
     float t_single;
     {
-        int ax[3];
-        cell_axes(ch, occ_cell, ax);
-        const int next = ax[d] + 1 == ch.m ? 0 : ax[d] + 1;
+        const int next = ax[d] + 1 == m ? 0 : ax[d] + 1;
         const float boundary = (float)A.view.cell_min[ch.geom_offset + next];
         const float x = d == 0 ? pa32.x : (d == 1 ? pa32.y : pa32.z);
         float sep = boundary - x;
-        if (sep < 0.0f) sep += ch.L32;
+        if (sep < 0.0f) sep += L32;
         t_single = sep / speed32;
         t_single = fminf(t_single, (float)time_sub(g.eoc_q, g.eoc_r, g.time_q, g.time_r));
     }
@@ -917,17 +936,18 @@ __global__ void __launch_bounds__(256, 4) screen_kernel(RunArgs A, RefineList *l
     }
     const uint64_t pair_base = draw_base(ch.key, ev, kRngPair);
     int count = 0;
-    auto screen_pair = [&](int j) {
-        const float4 pj = A.positions32[ch.pos_off + j];
+    // the FP32 solve of a kept candidate (x, y, z, identifier bits)
+    auto screen_pair = [&](const float4 &pj) {
+        const int j = __float_as_int(pj.w);
         float sv[3];
         bool flag = false;
-        separation32(pa32, pj, ch.L32, ch.half32, margin, sv, flag);
+        separation32(pa32, pj, L32, half32, margin, sv, flag);
         float t;
         int path = kPathHardSphere;
         if (potential_of<POT>(ch) == JFGPU_POT_HARD_SPHERE) {
             t = hs_screen(ch.diameter_sq32, d, speed32, sv, margin, flag);
         } else {
-            const float du = expovariate32(draw_at(pair_base, (uint32_t)j), inv_beta32, flag);
+            const float du = expovariate32((uint64_t)draw_hi32(pair_base, (uint32_t)j) << 32, inv_beta32, flag);
             t = lj_screen(lj32, d, speed32, sv, du, margin, flag, path);
         }
         // a flagged candidate keeps the branch its FP32 solve took (the flag concerns the time, rarely the branch):
@@ -946,11 +966,10 @@ __global__ void __launch_bounds__(256, 4) screen_kernel(RunArgs A, RefineList *l
     const float horizon = (t_single * rel + abs_margin) * speed32;
     const float shell32 = potential_of<POT>(ch) == JFGPU_POT_HARD_SPHERE ? ch.diameter_sq32 : lj32.r0_sq;
     const float beta32 = 1.0f / inv_beta32;
-    auto keep = [&](int j) -> bool {
-        const float4 pj = A.positions32[ch.pos_off + j];
+    auto keep = [&](const float4 &pj) -> bool {
         float sv[3];
         bool flag = false;
-        separation32(pa32, pj, ch.L32, ch.half32, margin, sv, flag);
+        separation32(pa32, pj, L32, half32, margin, sv, flag);
         if (flag) return true;
         const float sd = sv[d];
         const float pa = d == 0 ? sv[1] : sv[0];
@@ -963,123 +982,154 @@ __global__ void __launch_bounds__(256, 4) screen_kernel(RunArgs A, RefineList *l
         const float ir2 = 1.0f / r_min_sq;
         const float ir6 = ir2 * ir2 * ir2;
         const float rise = -((lj32.a12 * ir6 + lj32.a6) * ir6);  // |U(r_min)|, U < 0 outside the shell
-        const uint64_t bits = draw_at(pair_base, (uint32_t)j);
-        const float u_low = (float)(uint32_t)(bits >> 40) * (1.0f / 16777216.0f);
+        const uint32_t hi = draw_hi32(pair_base, (uint32_t)__float_as_int(pj.w));
+        const float u_low = (float)(hi >> 8) * (1.0f / 16777216.0f);
         return !(u_low > beta32 * rise * (1.0f + 1.0f / 1024.0f));
     };
     {
-        __shared__ int32_t pending[8][64];  // per warp: kept candidates not yet solved (fewer than 32 + 32)
-        int32_t *buf = pending[warp];
+        // Nearby occupants from the cell-ordered mirror: one 16-byte load gives an occupant's FP32 position and
+        // identifier, the cells of a row along x are contiguous, and each lane keeps kNearBatch loads in flight.
+        // Kept candidates wait in a per-warp buffer until 32 of them fill a pass of FP32 solves.
+        __shared__ float4 pending[8][64];  // per warp: kept candidates not yet solved (fewer than 32 + 32)
+        float4 *buf = pending[warp];
         int buffered = 0;  // warp-uniform
-        int axes[3];
-        cell_axes(ch, occ_cell, axes);
-        const int K = ch.n_res, m = ch.m;
-        const int32_t *occ = A.occupancy + ch.occ_off;
-        const int cell_iters = (K * K * K + 31) / 32;
-        const int near_iters = cell_iters * ch.max_occ;
-        const int iters = near_iters + (n_surplus + 31) / 32;
-        Digits dg;
-        int batch = 0, slot = 0;
-        for (int it = 0; it < iters; ++it) {
-            int j = -1;
-            if (it < near_iters) {
-                if (batch == 0) dg.start(lane, K);
-                if (dg.z < K) {
-                    int cx = axes[0] + ch.res[dg.x], cy = axes[1] + ch.res[dg.y], cz = axes[2] + ch.res[dg.z];
-                    if (cx >= m) cx -= m;
-                    if (cy >= m) cy -= m;
-                    if (cz >= m) cz -= m;
-                    j = occ[(long long)(cx + m * (cy + m * cz)) * ch.max_occ + slot];
-                }
-                dg.advance();
-                if (++batch == cell_iters) {
-                    batch = 0;
-                    ++slot;
-                }
-            } else {
-                const int i = (it - near_iters) * 32 + lane;
-                if (i < n_surplus) j = A.surplus[ch.pos_off + i];
-            }
-            bool kept = false;
-            if (j >= 0) {
-                ++count;
-                kept = keep(j);
-            }
+        auto offer_kept = [&](bool kept, const float4 &pj) {
             const unsigned mask = __ballot_sync(kFull, kept);
-            if (kept) buf[buffered + __popc(mask & ((1u << lane) - 1u))] = j;
+            if (kept) buf[buffered + __popc(mask & ((1u << lane) - 1u))] = pj;
             buffered += __popc(mask);
             __syncwarp();
             if (buffered >= 32) {
                 buffered -= 32;
-                const int mine = buf[buffered + lane];
+                const float4 mine = buf[buffered + lane];
                 __syncwarp();
                 screen_pair(mine);
             }
+        };
+        const int first_x = near_first(ax[0], K, m), first_y = near_first(ax[1], K, m),
+                  first_z = near_first(ax[2], K, m);
+        const float4 *slots = A.cell_slots + occ_off;
+        const int cell_iters = (K * K * K + 31) / 32;
+        for (int slot = 0; slot < max_occ; ++slot) {
+            Digits dg;
+            dg.start(lane, K);
+            for (int it = 0; it < cell_iters; it += kNearBatch) {
+                float4 p[kNearBatch];
+#pragma unroll
+                for (int b = 0; b < kNearBatch; ++b) {
+                    p[b] = make_float4(0.0f, 0.0f, 0.0f, __int_as_float(-1));
+                    if (it + b < cell_iters && dg.z < K) {
+                        int cx = first_x + dg.x, cy = first_y + dg.y, cz = first_z + dg.z;
+                        if (cx >= m) cx -= m;
+                        if (cy >= m) cy -= m;
+                        if (cz >= m) cz -= m;
+                        p[b] = slots[(long long)(cx + m * (cy + m * cz)) * max_occ + slot];
+                    }
+                    dg.advance();
+                }
+#pragma unroll
+                for (int b = 0; b < kNearBatch; ++b) {
+                    if (it + b >= cell_iters) break;  // warp-uniform
+                    bool kept = false;
+                    if (__float_as_int(p[b].w) >= 0) {
+                        ++count;
+                        kept = keep(p[b]);
+                    }
+                    offer_kept(kept, p[b]);
+                }
+            }
         }
-        const int mine = lane < buffered ? buf[lane] : -1;
+        for (int base_i = 0; base_i < n_surplus; base_i += 32) {
+            const int i = base_i + lane;
+            bool kept = false;
+            float4 pj = make_float4(0.0f, 0.0f, 0.0f, __int_as_float(-1));
+            if (i < n_surplus) {
+                const int j = A.surplus[pos_off + i];
+                pj = A.positions32[pos_off + j];
+                pj.w = __int_as_float(j);
+                ++count;
+                kept = keep(pj);
+            }
+            offer_kept(kept, pj);
+        }
+        const bool mine = lane < buffered;
+        const float4 last = mine ? buf[lane] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         __syncwarp();
-        if (mine >= 0) screen_pair(mine);
+        if (mine) screen_pair(last);
     }
     float base = fminf(warp_min_float(lane_min_unflagged(key)), t_single);
+    int lookups = 0;
     if (far_of<FAR>(ch) == JFGPU_FAR_CELL_BOUNDING) {
-        // far units (one coalesced pass over the role words) with the rigorous early rejection
-        // -log(1 - u) >= u: a far time is at least u / (beta rate speed)
+        // Far units with the rigorous early rejection -log(1 - u) >= u: a far time is at least
+        // u / (beta rate speed), so a unit whose u exceeds reject * rate cannot come before the threshold.  Every far
+        // rate of the direction is at most the largest one, so most units are rejected from their keyed draw alone,
+        // before anything of theirs is read; only the others read their role word (occupancy cell, or surplus /
+        // active) to find their relative cell and rate.
         const float threshold0 = isinf(base) ? kInf32 : base * rel + abs_margin;
         const float reject = threshold0 * speed32 * (1.0f + 1.0f / 65536.0f) / inv_beta32;
-        const float *rates = sp.bound_upper32;
-        if (staged) {
-            asm volatile("cp.async.wait_all;\n" ::: "memory");
-            __syncwarp();
+        const float largest = sp.far_rate_max32[d];
+        if (largest > 0.0f) {
+            // u_low = u24 2^-24 > reject * largest  <=>  u24 > cut (u24 an integer; NaN or >= 1: nothing rejected)
+            const float scaled = (reject * largest) * 16777216.0f;
+            const uint32_t cut = scaled < 16777216.0f ? (uint32_t)scaled : (1u << 24);
+            const float *rates = sp.bound_upper32;
+            const int32_t *roles = A.roles + pos_off;
+            const int16_t *rel_table = A.view.rel + ch.table_offset;
+            for (int j = lane; j < n; j += 32) {
+                const uint32_t hi = draw_hi32(pair_base, (uint32_t)j);
+                if ((hi >> 8) > cut || j == active) continue;
+                ++lookups;
+                const int32_t role = roles[j];
+                if (role & (kRoleActive | kRoleSurplus)) continue;
+                const int cx = role & 0xFF, cy = (role >> 8) & 0xFF, cz = (role >> 16) & 0xFF;
+                int dx = cx - ax[0], dy = cy - ax[1], dz = cz - ax[2];
+                if (dx < 0) dx += m;
+                if (dy < 0) dy += m;
+                if (dz < 0) dz += m;
+                if (((ch.near_mask >> dx) & 1ull) && ((ch.near_mask >> dy) & 1ull) && ((ch.near_mask >> dz) & 1ull))
+                    continue;
+                const int rc = ch.rel_is_mod ? dx + m * (dy + m * dz)
+                                             : rel_table[cx * m + ax[0]] +
+                                                   m * (rel_table[cy * m + ax[1]] + m * rel_table[cz * m + ax[2]]);
+                const float rate = rates[rc * 3 + d];
+                if (!(rate > 0.0f)) continue;
+                const float u_low = (float)(hi >> 8) * (1.0f / 16777216.0f);
+                if (u_low > reject * rate) continue;
+                bool flag = false;
+                const float du = expovariate32((uint64_t)hi << 32, inv_beta32, flag);
+                float t = (du / rate) / speed32;
+                if (flag) t = -1.0f;
+                if (!isinf(t)) topk_insert(key, code, t, make_code(j, kPathFar, true));
+            }
         }
-        for_each_unit(staged ? my_roles : A.roles + ch.pos_off, A, ch, occ_cell, lane, [&](int j) {},
-                      [&](int j, int rc) {
-                          const float rate = rates[rc * 3 + d];
-                          if (!(rate > 0.0f)) return;
-                          const uint64_t bits = draw_at(pair_base, (uint32_t)j);
-                          const float u_low = (float)(uint32_t)(bits >> 40) * (1.0f / 16777216.0f);
-                          if (u_low > reject * rate) return;
-                          bool flag = false;
-                          const float du = expovariate32(bits, inv_beta32, flag);
-                          float t = (du / rate) / speed32;
-                          if (flag) t = -1.0f;
-                          if (!isinf(t)) topk_insert(key, code, t, make_code(j, kPathFar, true));
-                      });
         base = fminf(base, warp_min_float(lane_min_unflagged(key)));
     }
     const float threshold = isinf(base) ? kInf32 : base * rel + abs_margin;
     // compaction of the candidates inside the threshold into the chain's refine list
     int overflow = (code[kTopK - 1] >= 0 && key[kTopK - 1] <= threshold) ? 1 : 0;
     int total = 0;
-    int queued[kRefineSlots];  // the lane's entries at list offsets 0 .. kRefineSlots - 1, if any
-#pragma unroll
-    for (int q = 0; q < kRefineSlots; ++q) queued[q] = -1;
 #pragma unroll
     for (int i = 0; i < kTopK; ++i) {
         const bool take = code[i] >= 0 && key[i] <= threshold;
         const unsigned mask = __ballot_sync(kFull, take);
         const int offset = total + __popc(mask & ((1u << lane) - 1u));
         if (take && offset < kRefineMax) list.code[offset] = code[i];
-#pragma unroll
-        for (int q = 0; q < kRefineSlots; ++q)
-            if (take && offset == q) queued[q] = code[i];
         total += __popc(mask);
     }
     overflow = warp_max_int(overflow) || total > A.refine_limit;
     const int screened = warp_sum_int(count);
+    lookups = warp_sum_int(lookups);
     if (lane == 0) {
         list.count = total < kRefineMax ? total : kRefineMax;
-        list.flags = (overflow ? kListOverflow : 0) | (staged ? kListStaged : 0);
+        list.flags = overflow ? kListOverflow : 0;
         list.screened = screened;
+        list.far_lookups = lookups;
     }
-    // the entries at the first kRefineSlots offsets go to the queues of their paths
-    if (!overflow) {
-#pragma unroll
-        for (int q = 0; q < kRefineSlots; ++q) {
-            if (queued[q] < 0) continue;
-            const int path = code_path(queued[q]);
-            const int at = atomicAdd(queue.counts + path, 1);
-            queue.entries[path * queue.stride + at] = (int32_t)(local * kRefineSlots + q);
-        }
+    // the entries at the first kRefineSlots offsets go to the queues of their paths, lane q taking entry q
+    __syncwarp();
+    if (!overflow && lane < kRefineSlots && lane < total) {
+        const int path = code_path(list.code[lane]);
+        const int at = atomicAdd(queue.counts + path, 1);
+        queue.entries[path * queue.stride + at] = (int32_t)(local * kRefineSlots + lane);
     }
 }
 
@@ -1100,7 +1150,7 @@ __device__ inline void load_lifting(const JfgpuChainState &g, const RunArgs &A, 
     w.refined = g.refined;
     w.lift_sum = g.lift_sum;
     w.liftings = g.liftings;
-    w.staged = g.staged_screens;
+    w.far_lookups = g.far_lookups;
     w.active = g.active;
     w.direction = g.direction;
     w.eoc_new = g.eoc_new_active;
@@ -1115,7 +1165,7 @@ __device__ inline void load_lifting(const JfgpuChainState &g, const RunArgs &A, 
 // The queued entries by path: each path's range is padded to whole warps, so that the 32 threads of a warp re-solve
 // candidates that take the same branch of the case analysis (up to the rare FP32/FP64 disagreement).
 template <int POT, int FAR>
-__global__ void __launch_bounds__(64) refine_kernel(RunArgs A, const RefineList *lists, Refined *refined,
+__global__ void __launch_bounds__(JF_REFINE_THREADS) refine_kernel(RunArgs A, const RefineList *lists, Refined *refined,
                                                      RefineQueue queue, long long round, int first_round) {
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     long long start = 0;
@@ -1188,7 +1238,7 @@ __device__ __noinline__ int exact_serial(const RunArgs &A, const ChainDev &ch, c
 }
 
 template <int POT, int FAR>
-__global__ void __launch_bounds__(32) resolve_kernel(RunArgs A, const RefineList *lists, const Refined *refined,
+__global__ void __launch_bounds__(JF_RESOLVE_THREADS) resolve_kernel(RunArgs A, const RefineList *lists, const Refined *refined,
                                                      RefineQueue queue, long long round, int first_round) {
     const long long local = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (local < kPaths) queue.counts[local] = 0;  // the refine kernel of this round has consumed the queue
@@ -1204,7 +1254,7 @@ __global__ void __launch_bounds__(32) resolve_kernel(RunArgs A, const RefineList
     load_lifting(g, A, ch, w);
     w.candidates += list.screened;
     w.refined += list.count;
-    if (list.flags & kListStaged) w.staged += 1;
+    w.far_lookups += list.far_lookups;
 
     Cand best = cand_none();
     int st = single_candidates(A, ch, sp, w, w.occ_cell, w.events, best);
@@ -1260,7 +1310,7 @@ __global__ void __launch_bounds__(32) resolve_kernel(RunArgs A, const RefineList
     g.refined = w.refined;
     g.lift_sum = w.lift_sum;
     g.liftings = w.liftings;
-    g.staged_screens = w.staged;
+    g.far_lookups = w.far_lookups;
     g.active = w.active;
     g.direction = w.direction;
     g.eoc_new_active = w.eoc_new;
@@ -1385,9 +1435,13 @@ __global__ void __launch_bounds__(256, JF_CHAIN_MIN_BLOCKS) chains_kernel(RunArg
 // start of the chains: FP32 mirror, occupancy in particle order (single_active_cell_occupancy.py:95-121),
 // lifting state at time 0 (initial_chain_start_of_run_event_handler.py) and the first end-of-chain candidate
 // ---------------------------------------------------------------------------------------------------------------
+__device__ __noinline__ void init_chain(const EngineView &view, const ChainDev &ch, long long c, double *positions,
+                                        float4 *positions32, int32_t *occupancy, int32_t *surplus, int32_t *roles,
+                                        float4 *cell_slots, JfgpuChainState *state);
+
 __global__ void init_kernel(EngineView view, long long n_chains, double *positions, float4 *positions32,
                             const double *charges, int32_t *occupancy, int32_t *surplus, int32_t *roles,
-                            JfgpuChainState *state) {
+                            float4 *cell_slots, JfgpuChainState *state) {
     const int warp = threadIdx.x >> 5;
     const int lane = threadIdx.x & 31;
     const long long c = (long long)blockIdx.x * (blockDim.x >> 5) + warp;
@@ -1400,7 +1454,20 @@ __global__ void init_kernel(EngineView view, long long n_chains, double *positio
     }
     for (long long k = lane; k < (long long)ch.ncells * ch.max_occ; k += 32) occupancy[ch.occ_off + k] = -1;
     __syncwarp();
-    if (lane != 0) return;
+    if (lane == 0) init_chain(view, ch, c, positions, positions32, occupancy, surplus, roles, cell_slots, state);
+    __syncwarp();
+    // the cell-ordered FP32 mirror of the occupancy just built
+    for (long long k = lane; k < (long long)ch.ncells * ch.max_occ; k += 32) {
+        const int id = occupancy[ch.occ_off + k];
+        const float4 p = id >= 0 ? positions32[ch.pos_off + id] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        cell_slots[ch.occ_off + k] = make_float4(p.x, p.y, p.z, __int_as_float(id));
+    }
+}
+
+// lane 0 of init_kernel: occupancy in particle order, surplus lists, role words and the chain state
+__device__ __noinline__ void init_chain(const EngineView &view, const ChainDev &ch, long long c, double *positions,
+                                        float4 *positions32, int32_t *occupancy, int32_t *surplus, int32_t *roles,
+                                        float4 *cell_slots, JfgpuChainState *state) {
     int status = JFGPU_STATUS_OK;
     int n_surplus = 0;
     int32_t *occ = occupancy + ch.occ_off;
@@ -1440,16 +1507,18 @@ __global__ void init_kernel(EngineView view, long long n_chains, double *positio
     g.stopped = 0;
     g.lift_sum = 0.0;
     g.liftings = 0;
-    g.staged_screens = 0;
+    g.far_lookups = 0;
     if (status == JFGPU_STATUS_OK) {
         // the activator's first update after the start of the run: the initial active unit leaves the occupancy
         RunArgs A;
         memset(&A, 0, sizeof(A));
         A.view = view;
         A.positions = positions;
+        A.positions32 = positions32;
         A.occupancy = occupancy;
         A.surplus = surplus;
         A.roles = roles;
+        A.cell_slots = cell_slots;
         WarpState w;
         w.active = g.active;
         w.occ_active = -1;
@@ -1487,10 +1556,27 @@ __global__ void mirror_kernel(const double *positions, const double *charges, fl
     positions32[i] = make_float4((float)p[0], (float)p[1], (float)p[2], charges ? (float)charges[i] : 1.0f);
 }
 
-cudaError_t launch_mirror(const JfgpuBuffers &b, long long first_unit, long long units, cudaStream_t stream) {
+// the cell-ordered FP32 mirror of chains [first, first + count) from their occupancy and FP32 mirror, one warp a chain
+__global__ void slots_kernel(EngineView view, long long first, long long count, const int32_t *occupancy,
+                             const float4 *positions32, float4 *cell_slots) {
+    const long long c = first + (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (c >= first + count) return;
+    const ChainDev &ch = view.chains[c];
+    for (long long k = threadIdx.x & 31; k < (long long)ch.ncells * ch.max_occ; k += 32) {
+        const int id = occupancy[ch.occ_off + k];
+        const float4 p = id >= 0 ? positions32[ch.pos_off + id] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        cell_slots[ch.occ_off + k] = make_float4(p.x, p.y, p.z, __int_as_float(id));
+    }
+}
+
+cudaError_t launch_mirror(const EngineView &view, const JfgpuBuffers &b, long long first_chain, long long count,
+                          long long first_unit, long long units, cudaStream_t stream) {
     if (units <= 0) return cudaSuccess;
     mirror_kernel<<<(unsigned)((units + 255) / 256), 256, 0, stream>>>(
         b.positions, b.charges, reinterpret_cast<float4 *>(b.positions32), first_unit, units);
+    slots_kernel<<<(unsigned)((count + 7) / 8), 256, 0, stream>>>(view, first_chain, count, b.occupancy,
+                                                                  reinterpret_cast<const float4 *>(b.positions32),
+                                                                  reinterpret_cast<float4 *>(b.cell_slots));
     return cudaGetLastError();
 }
 
@@ -1498,10 +1584,9 @@ cudaError_t launch_init(const EngineView &view, long long n_chains, const JfgpuB
     const int warps = 4;
     long long blocks = (n_chains + warps - 1) / warps;
     if (plan.clock) plan.clock->begin(plan.stream);
-    init_kernel<<<(unsigned)blocks, warps * 32, 0, plan.stream>>>(view, n_chains, b.positions,
-                                                                   reinterpret_cast<float4 *>(b.positions32),
-                                                                   b.charges, b.occupancy, b.surplus, b.roles,
-                                                                   b.state);
+    init_kernel<<<(unsigned)blocks, warps * 32, 0, plan.stream>>>(
+        view, n_chains, b.positions, reinterpret_cast<float4 *>(b.positions32), b.charges, b.occupancy, b.surplus,
+        b.roles, reinterpret_cast<float4 *>(b.cell_slots), b.state);
     if (plan.clock) plan.clock->end(plan.stream, JFGPU_KERNEL_INIT);
     return cudaGetLastError();
 }
@@ -1532,16 +1617,16 @@ static long long issue_rounds(const GroupLaunch *groups, int n_groups, long long
             const long long count = G.args.count;
             const long long screen_blocks = (count + warps - 1) / warps;
             // every queued entry plus the padding of each path to whole warps
-            const long long refine_blocks = (count * kRefineSlots + kPaths * 31 + 63) / 64;
-            const long long resolve_blocks = (count + 31) / 32;  // one warp per block: resolve spreads over the SMs
-            const size_t stage = stages_roles<FAR>() ? (size_t)warps * kStagedRoles * sizeof(int32_t) : 0;
-            screen_kernel<POT, FAR><<<(unsigned)screen_blocks, warps * 32, stage, G.stream>>>(G.args, G.lists,
-                                                                                             G.queue, r, first_round);
+            const long long refine_blocks =
+                (count * kRefineSlots + kPaths * 31 + JF_REFINE_THREADS - 1) / JF_REFINE_THREADS;
+            const long long resolve_blocks = (count + JF_RESOLVE_THREADS - 1) / JF_RESOLVE_THREADS;
+            screen_kernel<POT, FAR><<<(unsigned)screen_blocks, warps * 32, 0, G.stream>>>(G.args, G.lists, G.queue,
+                                                                                         r, first_round);
             if (timed) timed->end(G.stream, JFGPU_KERNEL_SCREEN);
-            refine_kernel<POT, FAR><<<(unsigned)refine_blocks, 64, 0, G.stream>>>(G.args, G.lists, G.refined, G.queue,
+            refine_kernel<POT, FAR><<<(unsigned)refine_blocks, JF_REFINE_THREADS, 0, G.stream>>>(G.args, G.lists, G.refined, G.queue,
                                                                                  r, first_round);
             if (timed) timed->end(G.stream, JFGPU_KERNEL_REFINE);
-            resolve_kernel<POT, FAR><<<(unsigned)resolve_blocks, 32, 0, G.stream>>>(G.args, G.lists, G.refined,
+            resolve_kernel<POT, FAR><<<(unsigned)resolve_blocks, JF_RESOLVE_THREADS, 0, G.stream>>>(G.args, G.lists, G.refined,
                                                                                    G.queue, r, first_round);
             if (timed) timed->end(G.stream, JFGPU_KERNEL_RESOLVE);
             launches += 3;
@@ -1678,6 +1763,7 @@ cudaError_t launch_run(const EngineView &view, const JfgpuBuffers &b, long long 
     A.occupancy = b.occupancy;
     A.surplus = b.surplus;
     A.roles = b.roles;
+    A.cell_slots = reinterpret_cast<float4 *>(b.cell_slots);
     A.state = b.state;
     A.log = log;
     A.log_capacity = log_capacity;

@@ -19,6 +19,14 @@
 
 namespace jf {
 
+// The FP64 solve functions of the potentials are out of line by default (small code for kernels that call them from
+// many places); a translation unit that defines JF_SOLVE_INLINE inlines them into its callers.
+#ifdef JF_SOLVE_INLINE
+#define JF_SOLVE __forceinline__
+#else
+#define JF_SOLVE __noinline__
+#endif
+
 constexpr double kInf = __builtin_inf();
 
 __host__ __device__ inline uint64_t double_bits(double x) {
@@ -158,7 +166,7 @@ __host__ __device__ inline uint32_t randbelow(uint64_t bits, uint32_t n) {
 
 // Natural logarithm written out so that CPU and GPU give the same bits: x = 2^e m, m in [sqrt(1/2), sqrt(2)),
 // log m = 2 atanh((m - 1)/(m + 1)) by its Taylor series to the 23rd power (Abramowitz & Stegun 4.1.27).
-static __host__ __device__ __noinline__ double own_log(double x) {
+static __host__ __device__ JF_SOLVE double own_log(double x) {
     uint64_t bits = double_bits(x);
     int e = (int)((bits >> 52) & 0x7FF);
     if (e == 0) {
@@ -251,7 +259,7 @@ __device__ inline double pow15_cr(double x) {
 
 // x ** (1.0 / 6.0) for x > 0 (the exponent is the double nearest 1/6): Newton step on z^6 = x in double-double
 // from the CUDA pow, then the correction x^(e - 1/6) = 1 - c log x with c = 1/6 - double(1/6).
-static __device__ __noinline__ double sixth_root_cr(double x) {
+static __device__ JF_SOLVE double sixth_root_cr(double x) {
     if (!(x > 1e-30 && x < 1e30)) return pow(x, 1.0 / 6.0);
     // FP32 guess (relative error ~1e-7), one plain Newton step (~1e-14), then the double-double step
     double g = (double)exp2f(__log2f((float)x) * (1.0f / 6.0f));
@@ -455,7 +463,7 @@ struct MH {
 // Lennard-Jones potential six.potential(1, s) + twelve.potential(1, s) (lennard_jones_potential.py:83-98,
 // inverse_power_potential.py:127-143): k sigma^6 / |s|^6 terms from norm_sq ** 3.0 and norm_sq ** 6.0, both
 // correctly rounded from one double-double cube
-static __device__ __noinline__ int lj_potential(const MH &h, const double *s, double &out) {
+static __device__ JF_SOLVE int lj_potential(const MH &h, const double *s, double &out) {
     double ns = norm_sq3(s);
     if (!(ns > 0.0) || isinf(ns)) {
         double a, b;
@@ -483,7 +491,7 @@ __device__ inline int mh_potential(const MH &h, const double *s, double &out) {
     return JFGPU_STATUS_OK;
 }
 
-static __device__ __noinline__ int mh_invert_inside(const MH &h, double potential, double &out) {
+static __device__ JF_SOLVE int mh_invert_inside(const MH &h, double potential, double &out) {
     if (h.kind == 0) {  // lennard_jones_potential.py:100-115
         double root, denominator;
         JF_TRY(py_pow(1.0 + (4.0 * potential) / h.prefactor, 0.5, root));
@@ -497,7 +505,7 @@ static __device__ __noinline__ int mh_invert_inside(const MH &h, double potentia
     return JFGPU_STATUS_OK;
 }
 
-static __device__ __noinline__ int mh_invert_outside(const MH &h, double potential, double &out) {
+static __device__ JF_SOLVE int mh_invert_outside(const MH &h, double potential, double &out) {
     if (h.kind == 0) {  // lennard_jones_potential.py:117-135
         if (potential >= 0.0) {
             out = kInf;
@@ -515,13 +523,13 @@ static __device__ __noinline__ int mh_invert_outside(const MH &h, double potenti
     return JFGPU_STATUS_OK;
 }
 
-static __device__ __noinline__ int mh_front_outside(const MH &h, int d, double u, double du, double *s, double &out) {
+static __device__ JF_SOLVE int mh_front_outside(const MH &h, int d, double u, double du, double *s, double &out) {
     double norm_new;  // abstracts.py:384-408
     JF_TRY(mh_invert_outside(h, u + du, norm_new));
     return disp_until_negative(s, norm_new * norm_new, d, out);
 }
 
-static __device__ __noinline__ int mh_front_inside(const MH &h, int d, double du, double *s, double &out) {
+static __device__ JF_SOLVE int mh_front_inside(const MH &h, int d, double du, double *s, double &out) {
     double displacement, u, extra;  // abstracts.py:456-484
     JF_TRY(disp_until_negative(s, h.r0_squared, d, displacement));
     s[d] -= displacement;
@@ -531,7 +539,7 @@ static __device__ __noinline__ int mh_front_inside(const MH &h, int d, double du
     return JFGPU_STATUS_OK;
 }
 
-static __device__ __noinline__ int mh_behind_inside(const MH &h, int d, double u, double du, double *s, double &out) {
+static __device__ JF_SOLVE int mh_behind_inside(const MH &h, int d, double u, double du, double *s, double &out) {
     double s_max[3] = {s[0], s[1], s[2]};  // abstracts.py:486-530
     s_max[d] = 0.0;
     double u_max;
@@ -553,7 +561,7 @@ static __device__ __noinline__ int mh_behind_inside(const MH &h, int d, double u
 
 // abstracts.py:410-454: a ValueError anywhere in the try block switches to the fallback, which sees the
 // separation as mutated up to that point
-static __device__ __noinline__ int mh_behind_outside(const MH &h, int d, double du, double *s, double &out) {
+static __device__ JF_SOLVE int mh_behind_outside(const MH &h, int d, double du, double *s, double &out) {
     double displacement, u, extra;
     int st = disp_until_positive(s, h.r0_squared, d, displacement);
     if (st == JFGPU_STATUS_OK) {
@@ -595,7 +603,7 @@ __device__ inline int mh_std_displacement(const MH &h, int d, double *s, double 
 
 // Lennard-Jones space derivative (lennard_jones_potential.py:63-81 with inverse_power_potential.py:71-94):
 // norm ** 8 and norm ** 14 correctly rounded from shared double-double powers
-static __device__ __noinline__ int lj_std_derivative(const MH &h, int d, const double *s, double &out) {
+static __device__ JF_SOLVE int lj_std_derivative(const MH &h, int d, const double *s, double &out) {
     double n = norm3(s);
     if (!(n > 0.0) || isinf(n)) {
         double a, b;

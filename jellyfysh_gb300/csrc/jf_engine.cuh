@@ -5,6 +5,7 @@
 //   positions32 float4[P]      FP32 mirror (x, y, z, charge) read by the FP32 screening
 //   charges     double[P]
 //   occupancy   int32[O]       cells * max_occupants slots, -1 = empty (SingleActiveCellOccupancy._occupants)
+//   cell_slots  float4[O]      cell-ordered FP32 mirror of the occupancy: (x, y, z, identifier bits), bits -1 empty
 //   surplus     int32[P]       surplus identifiers of the chain, n_surplus of them (SingleActiveCellOccupancy._surplus)
 //   state       JfgpuChainState[C]
 // Engine tables (owned by the engine): per-chain ChainDev, per-geometry cell bounds and relative/translate
@@ -35,6 +36,7 @@ struct SpeciesDev {
     const double *bound_upper;   // [cells][3]
     const double *bound_lower;   // [cells][3] negated lower bounds
     const float *bound_upper32;  // [cells][3] FP32 copy for the screening
+    float far_rate_max32[3];     // largest FP32 far-field rate by direction (0 without a cell-bounding far field)
     WalkerDev walker[2][3];      // [upper/lower][direction]
     const int4 *mic_terms;       // merged-image sum: real-space images, then Fourier rows (mic_x_warp)
     int mic_images, mic_rows;

@@ -22,7 +22,8 @@
 
 namespace jf {
 cudaError_t launch_init(const EngineView &view, long long n_chains, const JfgpuBuffers &b, const LaunchPlan &plan);
-cudaError_t launch_mirror(const JfgpuBuffers &b, long long first_unit, long long units, cudaStream_t stream);
+cudaError_t launch_mirror(const EngineView &view, const JfgpuBuffers &b, long long first_chain, long long count,
+                          long long first_unit, long long units, cudaStream_t stream);
 cudaError_t launch_run(const EngineView &view, const JfgpuBuffers &b, long long first, long long count,
                        long long max_events, double stop_q, double stop_r, int mode, JfgpuEvent *log,
                        long long log_capacity, int uniform_potential, int uniform_far, void *lists, void *refined,
@@ -504,6 +505,14 @@ int build_species(JfgpuEngine *e, const JfgpuChainDesc &d, const std::vector<dou
     sp.bound_lower = device_copy(e, lower_host, stream, error);
     std::vector<float> upper32(upper_host.begin(), upper_host.end());
     sp.bound_upper32 = device_copy(e, upper32, stream, error);
+    // the largest FP32 rate of each direction over the far cells (nearby cells hold 0): a keyed draw above
+    // reject * this bound rejects its unit without reading where the unit is
+    for (int k = 0; k < 3; ++k) {
+        float largest = 0.0f;
+        for (int cell = 0; cell < ncells; ++cell)
+            if (upper32[cell * 3 + k] > largest) largest = upper32[cell * 3 + k];
+        sp.far_rate_max32[k] = largest;
+    }
     if (error) return error;
     if (d.far == JFGPU_FAR_CELL_VETO) {
         for (int which = 0; which < 2; ++which)
@@ -768,7 +777,8 @@ int jfgpu_chains_set_refine_limit(JfgpuEngine *e, int32_t limit) {
 }
 
 static bool buffers_ok(const JfgpuEngine *e, const JfgpuBuffers *b) {
-    return e && b && b->positions && b->positions32 && b->occupancy && b->surplus && b->roles && b->state;
+    return e && b && b->positions && b->positions32 && b->occupancy && b->surplus && b->roles && b->state &&
+           b->cell_slots;
 }
 
 int jfgpu_chains_set_groups(JfgpuEngine *e, int32_t groups) {
@@ -788,14 +798,15 @@ int jfgpu_chains_set_groups(JfgpuEngine *e, int32_t groups) {
 
 int jfgpu_chains_refresh_mirror(JfgpuEngine *e, const JfgpuBuffers *b, int64_t first, int64_t count,
                                 void *stream_ptr) {
-    if (!e || !b || !b->positions || !b->positions32 || first < 0 || count < 0 ||
+    if (!e || !b || !b->positions || !b->positions32 || !b->occupancy || !b->cell_slots || first < 0 || count < 0 ||
         first + count > (int64_t)e->chains.size())
         return JFGPU_ERROR_ARGUMENT;
     if (count == 0) return JFGPU_OK;
     const long long first_unit = e->chains[first].pos_off;
     const long long last_unit = e->chains[first + count - 1].pos_off + e->chains[first + count - 1].n;
-    cudaError_t err = launch_mirror(*b, first_unit, last_unit - first_unit, static_cast<cudaStream_t>(stream_ptr));
-    e->launches += 1;
+    cudaError_t err = launch_mirror(e->view, *b, first, count, first_unit, last_unit - first_unit,
+                                    static_cast<cudaStream_t>(stream_ptr));
+    e->launches += 2;
     return err == cudaSuccess ? JFGPU_OK : JFGPU_ERROR_CUDA;
 }
 
