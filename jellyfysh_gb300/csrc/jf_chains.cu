@@ -25,6 +25,14 @@
 
 #include <cuda_runtime.h>
 
+// The round kernels keep the FP64 solves and the event flow inline (no calls, no arrays in local memory): their
+// latency is the chain of dependent FP64 operations, which calls and stack traffic lengthen.  The warp-per-chain FP64
+// kernel calls the flow through out-of-line entry points (below).  JF_OUT_OF_LINE builds everything out of line.
+#ifndef JF_OUT_OF_LINE
+#define JF_SOLVE_INLINE
+#define JF_FLOW_INLINE
+#endif
+
 #include "jf_engine.cuh"
 #include "jf_composite.cuh"
 #include "jf_screen.cuh"
@@ -636,6 +644,30 @@ __device__ JF_FLOW int commit(const RunArgs &A, const ChainDev &ch, const Specie
     return JFGPU_STATUS_OK;
 }
 
+// out-of-line entry points of the event flow for the warp-per-chain FP64 kernel (chains_kernel) and the rare serial
+// re-solve of a whole event, which call it from several places
+template <int POT>
+__device__ __noinline__ int exact_pair_ool(const RunArgs &A, const ChainDev &ch, const SpeciesDev &sp,
+                                           const WarpState &w, int j, long long ev, Cand &best) {
+    return exact_pair<POT>(A, ch, sp, w, j, ev, best);
+}
+__device__ __noinline__ int exact_cell_bounding_ool(const RunArgs &A, const ChainDev &ch, const SpeciesDev &sp,
+                                                    const WarpState &w, int j, int active_cell, long long ev,
+                                                    Cand &best) {
+    return exact_cell_bounding(A, ch, sp, w, j, active_cell, ev, best);
+}
+__device__ __noinline__ int single_candidates_ool(const RunArgs &A, const ChainDev &ch, const SpeciesDev &sp,
+                                                  const WarpState &w, int active_cell, long long ev, Cand &best) {
+    return single_candidates(A, ch, sp, w, active_cell, ev, best);
+}
+__device__ __noinline__ int commit_ool(const RunArgs &A, const ChainDev &ch, const SpeciesDev &sp, WarpState &w,
+                                       const Cand &best, int active_cell, long long chain_index, long long log_index) {
+    return commit(A, ch, sp, w, best, active_cell, chain_index, log_index);
+}
+__device__ __noinline__ int occ_update_ool(const RunArgs &A, const ChainDev &ch, WarpState &w) {
+    return occ_update(A, ch, w);
+}
+
 // ---------------------------------------------------------------------------------------------------------------
 // candidate enumeration
 // ---------------------------------------------------------------------------------------------------------------
@@ -761,24 +793,24 @@ __device__ inline int exact_candidates(const RunArgs &A, const ChainDev &ch, con
     int count = 0;
     best = cand_none();
     for_each_near(A, ch, w.occ_cell, lane, [&](int j) {
-        int st = exact_pair<POT>(A, ch, sp, w, j, ev, best);
+        int st = exact_pair_ool<POT>(A, ch, sp, w, j, ev, best);
         if (st) status = st;
         ++count;
     });
     for (int i = lane; i < w.n_surplus; i += 32) {
-        int st = exact_pair<POT>(A, ch, sp, w, A.surplus[ch.pos_off + i], ev, best);
+        int st = exact_pair_ool<POT>(A, ch, sp, w, A.surplus[ch.pos_off + i], ev, best);
         if (st) status = st;
         ++count;
     }
     counted = warp_sum_int(count);
     if (far_of<FAR>(ch) == JFGPU_FAR_CELL_BOUNDING) {
         for_each_far(A, ch, w.occ_cell, lane, [&](int j, int cell, int rc) {
-            int st = exact_cell_bounding(A, ch, sp, w, j, active_cell, ev, best);
+            int st = exact_cell_bounding_ool(A, ch, sp, w, j, active_cell, ev, best);
             if (st) status = st;
         });
     }
     if (lane == 0) {
-        int st = single_candidates(A, ch, sp, w, active_cell, ev, best);
+        int st = single_candidates_ool(A, ch, sp, w, active_cell, ev, best);
         if (st) status = st;
     }
     best = warp_argmin(best);
@@ -1223,15 +1255,16 @@ __device__ __noinline__ int exact_serial(const RunArgs &A, const ChainDev &ch, c
                                  ch.m * ch.m * ((a[2] + ch.res[oz]) % ch.m);
                 for (int k = 0; k < ch.max_occ; ++k) {
                     const int j = occ[(long long)cell * ch.max_occ + k];
-                    if (j >= 0) JF_TRY(exact_pair<POT>(A, ch, sp, w, j, ev, best));
+                    if (j >= 0) JF_TRY(exact_pair_ool<POT>(A, ch, sp, w, j, ev, best));
                 }
             }
-    for (int i = 0; i < w.n_surplus; ++i) JF_TRY(exact_pair<POT>(A, ch, sp, w, A.surplus[ch.pos_off + i], ev, best));
+    for (int i = 0; i < w.n_surplus; ++i)
+        JF_TRY(exact_pair_ool<POT>(A, ch, sp, w, A.surplus[ch.pos_off + i], ev, best));
     if (far_of<FAR>(ch) == JFGPU_FAR_CELL_BOUNDING) {
         for (int cell = 0; cell < ch.ncells; ++cell) {
             const int j = occ[cell];
             if (j < 0 || is_nearby(ch, cell, w.occ_cell)) continue;
-            JF_TRY(exact_cell_bounding(A, ch, sp, w, j, w.occ_cell, ev, best));
+            JF_TRY(exact_cell_bounding_ool(A, ch, sp, w, j, w.occ_cell, ev, best));
         }
     }
     return JFGPU_STATUS_OK;
@@ -1281,8 +1314,8 @@ __global__ void __launch_bounds__(JF_RESOLVE_THREADS) resolve_kernel(RunArgs A, 
             for (int i = kRefineSlots; i < list.count && !st; ++i) {
                 const int code = list.code[i];
                 const int j = code_target(code);
-                st = code_far(code) ? exact_cell_bounding(A, ch, sp, w, j, w.occ_cell, w.events, best)
-                                    : exact_pair<POT>(A, ch, sp, w, j, w.events, best);
+                st = code_far(code) ? exact_cell_bounding_ool(A, ch, sp, w, j, w.occ_cell, w.events, best)
+                                    : exact_pair_ool<POT>(A, ch, sp, w, j, w.events, best);
             }
         }
     }
@@ -1366,7 +1399,7 @@ __global__ void __launch_bounds__(256, JF_CHAIN_MIN_BLOCKS) chains_kernel(RunArg
     for (long long e = 0; e < A.max_events; ++e) {
         if (w.status != JFGPU_STATUS_OK || w.stop) break;
         if (lane == 0 && w.active != w.occ_active) {
-            int st = occ_update(A, ch, w);
+            int st = occ_update_ool(A, ch, w);
             if (st) w.status = st;
         }
         __syncwarp();
@@ -1396,11 +1429,11 @@ __global__ void __launch_bounds__(256, JF_CHAIN_MIN_BLOCKS) chains_kernel(RunArg
                 time_slice(ch, w, A.stop_q, A.stop_r);
                 store_active(A, ch, w, w.active);
                 w.stop = 1;
-                int st = occ_update(A, ch, w);
+                int st = occ_update_ool(A, ch, w);
                 if (st) w.status = st;
             } else {
-                int st = commit(A, ch, sp, w, best, active_cell, c, w.events - start_events);
-                if (!st) st = occ_update(A, ch, w);  // the activator's update of the next event
+                int st = commit_ool(A, ch, sp, w, best, active_cell, c, w.events - start_events);
+                if (!st) st = occ_update_ool(A, ch, w);  // the activator's update of the next event
                 if (st) w.status = st;
             }
             w.real_target = -1;
@@ -1525,7 +1558,7 @@ __device__ __noinline__ void init_chain(const EngineView &view, const ChainDev &
         w.occ_cell = -1;
         w.n_surplus = n_surplus;
         load_pos(A, ch, w.active, w.pa);
-        g.status = occ_update(A, ch, w);
+        g.status = occ_update_ool(A, ch, w);
         g.occ_active = w.occ_active;
         g.occ_cell = w.occ_cell;
         g.n_surplus = w.n_surplus;
