@@ -67,14 +67,24 @@ def parse():
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     p.add_argument("--events", type=int, default=128, help="events per chain and step")
     p.add_argument("--chains", type=int, default=WORKLOAD["chains"])
-    p.add_argument("--block-warps", type=int, default=4, help="warps per screening block (0 = autotune)")
-    p.add_argument("--groups", type=int, default=1, help="chain groups on streams of their own (0 = autotune)")
+    p.add_argument("--block-warps", type=int, default=None, help="warps per screening block (0 = autotune)")
+    p.add_argument("--groups", type=int, default=None, help="chain groups on streams of their own (0 = autotune)")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-fp64", action="store_true")
     p.add_argument("--no-parity", action="store_true")
     p.add_argument("--fp64-events", type=int, default=16, help="events per chain of the batched FP64 comparison")
-    p.add_argument("--workload", default="lennard_jones", choices=["lennard_jones", "coulomb", "water"])
+    p.add_argument("--workload", default="lennard_jones",
+                   choices=["lennard_jones", "coulomb", "water", "hard_spheres", "hard_spheres_n64"])
     args = p.parse_args()
+    if args.workload in ("hard_spheres", "hard_spheres_n64") and "--chains" not in sys.argv:
+        args.chains = _workloads.BUILDERS[args.workload][0]["chains"]
+    # launch shape: the batched hard-sphere workloads are tuned by the package's autotuner, the others take the
+    # shape measured best for them (4 warps per block, one chain group)
+    tuned_default = 0 if args.workload in ("hard_spheres", "hard_spheres_n64") else None
+    if args.block_warps is None:
+        args.block_warps = 4 if tuned_default is None else tuned_default
+    if args.groups is None:
+        args.groups = 1 if tuned_default is None else tuned_default
     if args.workload == "water" and "--chains" not in sys.argv:
         args.chains = WATER_WORKLOAD["chains"]
     if args.workload == "water" and "--events" not in sys.argv:
@@ -85,17 +95,27 @@ def parse():
 
 
 def workload_of(args):
-    return COULOMB_WORKLOAD if args.workload == "coulomb" else WORKLOAD
+    return _workloads.BUILDERS[args.workload][0]
+
+
+METRICS = {"lennard_jones": METRIC, "coulomb": "events/s on 1 GB300, batched Coulomb replicas",
+           "hard_spheres": "events/s on 1 GB300, batched hard-sphere chains of uneven N and density",
+           "hard_spheres_n64": "events/s on 1 GB300, hard-sphere chains N=64"}
+DATA = {"lennard_jones": "synthetic: seeded simple-cubic lattice + uniform jitter",
+        "coulomb": "synthetic: seeded random sequential addition of +-1 charges with a hard core",
+        "hard_spheres": "synthetic: seeded random sequential addition below packing fraction 0.35, jittered fcc "
+                        "lattice above",
+        "hard_spheres_n64": "synthetic: seeded random sequential addition"}
+KERNELS = {"lennard_jones": "jf::screen_kernel<1, 2>", "hard_spheres": "jf::screen_kernel<0, 0>",
+           "hard_spheres_n64": "jf::screen_kernel<0, 0>", "coulomb": "jf::chains_kernel<-1, -1>"}
 
 
 def metric_of(args):
-    return "events/s on 1 GB300, batched Coulomb replicas" if args.workload == "coulomb" else METRIC
+    return METRICS[args.workload]
 
 
 def data_of(args):
-    if args.workload == "coulomb":
-        return "synthetic: seeded random sequential addition of +-1 charges with a hard core"
-    return "synthetic: seeded simple-cubic lattice + uniform jitter"
+    return DATA[args.workload]
 
 
 def build_workload(args, chains, seed_offset=0):
@@ -337,26 +357,6 @@ def reference_arm(args):
     print(json.dumps(line))
 
 
-def autotune(batch, events, warps_choices=(2, 4, 8), group_choices=(1, 2, 4)):
-    """Pick warps per block and chain groups of the mixed mode by a short timed sweep (the sweep's events also
-    warm the chains up)."""
-    import torch
-    best, best_time = (4, 1), math.inf
-    for warps in warps_choices:
-        for groups in group_choices:
-            batch.set_block_warps(warps)
-            batch.set_groups(groups)
-            torch.cuda.synchronize()
-            start = time.perf_counter()
-            batch.run(events, mode="mixed")
-            elapsed = time.perf_counter() - start
-            if elapsed < best_time:
-                best, best_time = (warps, groups), elapsed
-    batch.set_block_warps(best[0])
-    batch.set_groups(best[1])
-    return best
-
-
 def gpu_arm(args):
     import torch
     import torch.distributed as dist
@@ -371,11 +371,14 @@ def gpu_arm(args):
     specs, positions, charges, length = build_workload(args, args.chains, seed_offset=rank)
     batch = ChainBatch(specs, positions, charges, seed=1000 + rank, device="cuda:%d" % local)
     stream = torch.cuda.current_stream(device)
+    tuned = None
     if args.block_warps and args.groups:
         warps, groups = args.block_warps, args.groups
     else:
-        warps, groups = autotune(batch, 8, (args.block_warps,) if args.block_warps else (2, 4, 8),
-                                 (args.groups,) if args.groups else (1, 2, 4))
+        from jellyfysh_gb300 import autotune
+        (warps, groups), timings = autotune.tune(batch, 8, (args.block_warps,) if args.block_warps else autotune.WARPS,
+                                                 (args.groups,) if args.groups else autotune.GROUPS)
+        tuned = {"%dx%d" % shape: seconds * 1e6 for shape, seconds in timings.items()}
     batch.set_block_warps(warps)
     batch.set_groups(groups)
     # per-kernel CUDA events on the launching streams stay on through the warm-up and the timed region, around
@@ -501,19 +504,24 @@ def gpu_arm(args):
     # three kernels per event round and chain group (mixed rounds); one launch per step (FP64 kernel)
     events_per_launch = events_done / max(launches if coulomb else launches / 3, 1)
     nb = candidates / max(events_done, 1)
-    near_cells = (2 * specs[0].neighbor_layers + 1) ** 3
+    # nearby cells scanned per event, averaged over the chains (each chain commits one event per round)
+    near_cells = float(np.mean([_workloads.near_cells(spec) for spec in specs]))
     bytes_per_event = 4 * near_cells + (24 + 8 + 4) * nb + 32 if coulomb else 4 * near_cells + 12 * nb + 4 * nb + 32
     dominant_s = dominant["ms"] / dominant_launches / 1000.0
     achieved = bytes_per_event * events_per_launch / dominant_s / 1e9
     peak, peak_kind = measured_peaks()
-    traffic = (COULOMB_NCU["traffic_per_event"] if coulomb else NCU_TRAFFIC_PER_EVENT) * events_per_launch
+    traffic = None
+    if args.workload == "coulomb":
+        traffic = COULOMB_NCU["traffic_per_event"] * events_per_launch
+    elif args.workload == "lennard_jones":
+        traffic = NCU_TRAFFIC_PER_EVENT * events_per_launch
     total_kernel_ms = sum(v["ms"] for v in kernel_times.values()) or 1.0
     kernels = {name: {"launches": v["launches"], "ms_per_launch": v["ms"] / max(v["launches"], 1),
                       "share": v["ms"] / total_kernel_ms}
                for name, v in kernel_times.items() if v["launches"]}
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "traffic": traffic, "peak_source": peak_kind,
-                "kernel": "jf::chains_kernel<-1, -1>" if coulomb else "jf::screen_kernel<1, 2>",
+                "kernel": KERNELS[args.workload],
                 "bytes_per_event": bytes_per_event, "events_per_launch": events_per_launch,
                 "ms_per_launch": dominant_s * 1000.0, "neighbours_per_event": nb,
                 "refined_per_event": refined / max(events_done, 1), "fallback_events": fallbacks,
@@ -535,6 +543,7 @@ def gpu_arm(args):
                          % (threads, done, elapsed)}
     config = dict(workload_of(args))
     config.update(chains=args.chains, events_per_chain_per_step=args.events, block_warps=warps, chain_groups=groups,
+                  autotuned_us_per_round=tuned,
                   l2="inputs larger than L2 (working set %.0f MB)" % (sum(
                       t.numel() * t.element_size() for t in batch.state_tensors()) / 1e6),
                   parallelism="replicas" if world > 1 else "single GPU")

@@ -482,6 +482,17 @@ int64_t jfgpu_engine_launch_count(const JfgpuEngine *engine);
 int jfgpu_engine_set_timing(JfgpuEngine *engine, int32_t enable);
 int jfgpu_engine_kernel_times(JfgpuEngine *engine, double *milliseconds, int64_t *launches, int32_t reset);
 
+/* ======================================================================================================
+ * Initial states (host): random sequential addition of n hard spheres of the given radius in the periodic cube of
+ * side system_length, the trial points drawn from a SplitMix64 stream of `seed`; a trial closer than one diameter to
+ * a placed sphere (minimum image) is rejected.  positions [n][3] (host) receive the spheres in placement order.
+ * JFGPU_ERROR_TABLE after max_trials trials without n spheres.  The reference places atoms without overlap rejection
+ * (input_output_handler/input_handler/random_node_creator/atom_random_node_creator.py:56-67); its hard-sphere runs need
+ * non-overlapping starts, which this supplies for the batched hard-sphere workloads.
+ * ==================================================================================================== */
+int jfgpu_random_sequential_addition(int64_t n, double radius, double system_length, uint64_t seed,
+                                     int64_t max_trials, double *positions);
+
 const char *jfgpu_error_string(int code);
 int jfgpu_version(void);
 

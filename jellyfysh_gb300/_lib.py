@@ -156,6 +156,7 @@ SIGNATURES = {
     "jfgpu_engine_set_timing": (ctypes.c_int, [_P, _I32]),
     "jfgpu_engine_kernel_times": (ctypes.c_int, [_P, _P, _P, _I32]),
     "jfgpu_engine_launch_count": (ctypes.c_int64, [_P]),
+    "jfgpu_random_sequential_addition": (ctypes.c_int, [_I64, _D, _D, ctypes.c_uint64, _I64, _P]),
     "jfgpu_error_string": (ctypes.c_char_p, [ctypes.c_int]),
     "jfgpu_version": (ctypes.c_int, []),
 }

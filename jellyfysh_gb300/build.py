@@ -16,7 +16,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD_DIR = os.path.join(HERE, "_build")
 LIBRARY = os.path.join(BUILD_DIR, "libjfgpu.so")
 SOURCES = ["jf_chains.cu", "jf_engine_host.cu", "jf_potentials.cu", "jf_observe.cu", "jf_lifting.cu", "jf_composite.cu",
-           "jf_water.cu"]
+           "jf_water.cu", "jf_states.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-Xcompiler", "-fPIC", "-Xcompiler", "-fno-fast-math",
          "-I" + os.path.join(ROOT, "include"), "-I" + CSRC]

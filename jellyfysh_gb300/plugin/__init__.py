@@ -3,8 +3,9 @@
 The reference builds every object of a run from its configuration file with ``base/factory.py:22-135``: a class
 ``CamelName`` is found as ``jellyfysh.<package>.camel_name`` (``factory.py:111-122``) and constructed from the keys
 of its section, typed by the constructor's annotations (``factory.py:180-235``).  ``install()`` appends this
-package's directories to the search paths of ``jellyfysh.potential``, ``jellyfysh.lifting`` and
-``jellyfysh.mediator``, so that a configuration names the GPU classes exactly like the reference's own:
+package's directories to the search paths of ``jellyfysh.potential``, ``jellyfysh.lifting``, ``jellyfysh.mediator``,
+``jellyfysh.event_handler`` and ``jellyfysh.activator.tagger``, so that a configuration names the GPU classes exactly
+like the reference's own:
 
     [TwoLeafUnitEventHandler]
     potential = gpu_lennard_jones_potential          ; instead of lennard_jones_potential
@@ -15,9 +16,15 @@ package's directories to the search paths of ``jellyfysh.potential``, ``jellyfys
     [Run]
     mediator = gpu_chain_batch_mediator              ; instead of single_process_mediator
 
+    [TagActivator]
+    taggers = pair_neighbourhood (gpu_neighbourhood_tagger), ...   ; instead of the pairwise nearby/surplus taggers
+    [PairNeighbourhood]
+    event_handler = gpu_neighbourhood_event_handler  ; one GPU launch for all pairs of the neighbourhood
+
 The potentials evaluate the reference's displacement / derivative and the lifting schemes decide the new active
-unit on the GPU one call at a time (drop-ins for the reference's own event handlers); the mediator runs the whole
-configured system as a batch of chains on the GPU.
+unit on the GPU one call at a time (drop-ins for the reference's own event handlers); the neighbourhood event handler
+solves all pair candidates of the active unit in one launch inside the reference's own mediator loop; the mediator
+runs the whole configured system as a batch of chains on the GPU.
 Nothing here needs the reference to be importable except ``install()`` and the mediator's translation of a
 configured run.
 """
@@ -25,7 +32,8 @@ import os
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 PACKAGES = {"potential": os.path.join(HERE, "potential"), "mediator": os.path.join(HERE, "mediator"),
-            "lifting": os.path.join(HERE, "lifting")}
+            "lifting": os.path.join(HERE, "lifting"), "event_handler": os.path.join(HERE, "event_handler"),
+            "activator.tagger": os.path.join(HERE, "tagger")}
 
 
 def install() -> None:

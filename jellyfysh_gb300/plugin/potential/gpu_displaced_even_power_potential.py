@@ -23,6 +23,10 @@ class GpuDisplacedEvenPowerPotential(GpuPotential):
         return self._one(potentials.displaced_even_power_displacement(
             self._equilibrium_separation, self._power, self._prefactor, velocity, separation, potential_change))
 
+    def displacements(self, velocity, separations, charges, potential_changes):
+        return potentials.displaced_even_power_displacement(self._equilibrium_separation, self._power,
+                                                            self._prefactor, velocity, separations, potential_changes)
+
     def derivative(self, velocity: Sequence[float], separation: Sequence[float]) -> float:
         return self._one(potentials.displaced_even_power_derivative(
             self._equilibrium_separation, self._power, self._prefactor, velocity, separation))

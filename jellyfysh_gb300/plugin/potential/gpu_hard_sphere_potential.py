@@ -18,6 +18,9 @@ class GpuHardSpherePotential(GpuPotential):
     def displacement(self, velocity: Sequence[float], separation: Sequence[float]) -> float:
         return self._one(potentials.hard_sphere_displacement(self._radius, velocity, separation))
 
+    def displacements(self, velocity, separations, charges, potential_changes):
+        return potentials.hard_sphere_displacement(self._radius, velocity, separations)
+
     def derivative(self, velocity: Sequence[float], separation: Sequence[float]) -> float:
         raise NotImplementedError("The derivative method of the class {0} should not be used."
                                   .format(self.__class__.__name__))

@@ -27,6 +27,10 @@ class GpuInversePowerCoulombBoundingPotential(GpuPotential):
                                                                separation, [charge_one, charge_two],
                                                                potential_change))
 
+    def displacements(self, velocity, separations, charges, potential_changes):
+        return potentials.coulomb_bound_displacement(self._prefactor, self._length(), velocity, separations, charges,
+                                                     potential_changes)
+
     def derivative(self, velocity: Sequence[float], separation: Sequence[float], charge_one: float,
                    charge_two: float) -> float:
         return self._one(potentials.coulomb_bound_derivative(self._prefactor, velocity, separation,

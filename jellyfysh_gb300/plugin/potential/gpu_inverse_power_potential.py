@@ -24,6 +24,10 @@ class GpuInversePowerPotential(GpuPotential):
         return self._one(potentials.inverse_power_displacement(self._power, self._prefactor, velocity, separation,
                                                                [charge_one, charge_two], potential_change))
 
+    def displacements(self, velocity, separations, charges, potential_changes):
+        return potentials.inverse_power_displacement(self._power, self._prefactor, velocity, separations, charges,
+                                                     potential_changes)
+
     def derivative(self, velocity: Sequence[float], separation: Sequence[float], charge_one: float,
                    charge_two: float) -> float:
         return self._one(potentials.inverse_power_derivative(self._power, self._prefactor, velocity, separation,

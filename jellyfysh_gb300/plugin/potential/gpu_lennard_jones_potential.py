@@ -21,6 +21,10 @@ class GpuLennardJonesPotential(GpuPotential):
         return self._one(potentials.lennard_jones_displacement(self._prefactor, self._characteristic_length, velocity,
                                                                separation, potential_change))
 
+    def displacements(self, velocity, separations, charges, potential_changes):
+        return potentials.lennard_jones_displacement(self._prefactor, self._characteristic_length, velocity,
+                                                     separations, potential_changes)
+
     def derivative(self, velocity: Sequence[float], separation: Sequence[float]) -> float:
         return self._one(potentials.lennard_jones_derivative(self._prefactor, self._characteristic_length, velocity,
                                                              separation))

@@ -12,8 +12,8 @@ uncharged systems).  The parameters are those of the reference's vocabulary (INI
   merged-image Coulomb (alpha = 3.45, |n| <= 2, |k| <= 6) bounded by the inverse-power Coulomb bound, cell veto on
   8^3 cells, seeded random sequential addition.
 * ``hard_spheres``: independent hard-sphere chains of uneven size and density (N drawn from 32..2048, packing
-  fraction from [0.10, 0.45]; random sequential addition below 0.35, a jittered fcc lattice above), cells of at
-  least one diameter, chain time 0.3 L.
+  fraction from [0.10, 0.45]; random sequential addition below 0.35, a jittered fcc lattice above), cells whose
+  nearby cells reach one diameter and fit with one more cell in half the box, chain time 0.3 L.
 * ``hard_spheres_n64``: N = 64 spheres of radius 0.1 in the unit cube, 5^3 cells, chain time 0.3.
 """
 import numpy as np
@@ -70,13 +70,32 @@ def coulomb(chains, seed_offset=0):
     return specs, positions, charges, w["system_length"]
 
 
+def hard_sphere_cells(length, diameter):
+    """(cells per side, neighbour layers) of a hard-sphere chain in a periodic cube of side ``length``: the nearby
+    cells reach at least one diameter (layers x side >= diameter) and the nearby cells plus one cell fit in half the
+    box ((layers + 1) x side <= length / 2), so that the minimum image of every target that the active sphere can
+    reach before its next cell-boundary event is the one its candidate is solved for.  One layer where the box
+    allows it (length >= 4 diameters), else the fewest layers that fit; cells as many as the layers allow, at most
+    64 per side."""
+    for layers in (1, 2, 3, 4):
+        m = min(int(layers * length / diameter), 64)
+        if m >= 2 * (layers + 1):
+            return m, layers
+    raise ValueError("no cell system fits a periodic cube of side %r for spheres of diameter %r"
+                     % (length, diameter))
+
+
 def hard_sphere_chain(n, eta, rng, radius=0.5, lattice_above=0.35, chain_time_over_length=0.3):
-    """One hard-sphere chain of ``n`` spheres at packing fraction ``eta``: (spec, positions).  Cells are the most
-    that keep a side of at least one diameter (at most 64 per side); the nearby cells (one layer) then hold every
-    sphere that can touch the active one."""
-    state, length = systems.batched_hard_sphere_state(n, eta, radius, rng, rsa_limit=lattice_above)
-    m = max(3, min(int(length / (2.0 * radius)), 64))
-    spec = ChainSpec(n=n, system_length=length, cells_per_side=m, neighbor_layers=1, max_occupants=1,
+    """One hard-sphere chain of ``n`` spheres at packing fraction ``eta``: (spec, positions), cells from
+    ``hard_sphere_cells``."""
+    if eta < lattice_above:
+        # random sequential addition on a cell grid (thousands of spheres near the jamming density)
+        length = systems.hard_sphere_box(n, eta, radius)
+        state = systems.random_sequential_addition_grid(n, radius, length, seed=int(rng.integers(1 << 62)))
+    else:
+        state, length = systems.batched_hard_sphere_state(n, eta, radius, rng, rsa_limit=lattice_above)
+    m, layers = hard_sphere_cells(length, 2.0 * radius)
+    spec = ChainSpec(n=n, system_length=length, cells_per_side=m, neighbor_layers=layers, max_occupants=1,
                      hs_radius=radius, chain_time=chain_time_over_length * length,
                      initial_active=int(rng.integers(n)), initial_direction=int(rng.integers(3)))
     return spec, state

@@ -252,6 +252,19 @@ def initial_state(spec: dict):
 
 def run_one(tree: str, name: str) -> None:
     spec = SYSTEMS[name]
+    structured, positions, final, charges, length, key = record(tree, spec)
+    out = os.path.join(HERE, "trajectory_%s.npz" % name)
+    np.savez_compressed(out, events=structured, initial=positions, final=final,
+                        charges=np.zeros(0) if charges is None else charges,
+                        spec=json.dumps(dict(spec, system_length=length, rng_key=key)))
+    print("%s: %d events, kinds %s -> %s" % (name, len(structured), np.bincount(structured["kind"], minlength=8), out))
+
+
+def record(tree: str, spec: dict, transform=None, prepare=None):
+    """Run the reference's mediator on the system `spec` with the keyed random numbers and log every commit.
+    `transform` (optional) rewrites the configuration text; `prepare(context)` (optional) is called before the run
+    with the event-index function, the chain's key and beta, so that other event handlers draw the same numbers.
+    Returns (events, initial positions, final positions, charges, box length, key)."""
     sys.path.insert(0, tree)
     sys.path.insert(0, ROOT)
     import configparser
@@ -383,7 +396,10 @@ def run_one(tree: str, name: str) -> None:
             kind = kinds[name_of]
             target = -1
             accepted = 0
-            if kind in (oracle.EV_PAIR, oracle.EV_HARDCORE, oracle.EV_BOUNDED, oracle.EV_CELL_BOUNDING):
+            if hasattr(winner, "_target_index"):  # an event handler of a whole neighbourhood
+                target = winner._leaf_units[winner._target_index].identifier[0]
+                accepted = int(active_id != moved)
+            elif kind in (oracle.EV_PAIR, oracle.EV_HARDCORE, oracle.EV_BOUNDED, oracle.EV_CELL_BOUNDING):
                 target = winner._leaf_units[winner._active_leaf_unit_index ^ 1].identifier[0]
                 accepted = int(active_id != moved)
             elif kind == oracle.EV_CELL_VETO:
@@ -404,8 +420,11 @@ def run_one(tree: str, name: str) -> None:
         return result
     TreeStateHandler.insert_into_global_state = insert_into_global_state
 
+    if prepare is not None:
+        prepare({"event_index": event_index, "key": key, "beta": beta, "kinds": kinds})
+    text = config_text(spec, length)
     config = configparser.ConfigParser()
-    config.read_string(config_text(spec, length))
+    config.read_string(transform(text) if transform is not None else text)
     factory.build_from_config(config, to_camel_case(config.get("Run", "setting")), "jellyfysh.setting")
     mediator = factory.build_from_config(config, to_camel_case(config.get("Run", "mediator")), "jellyfysh.mediator")
     try:
@@ -419,11 +438,7 @@ def run_one(tree: str, name: str) -> None:
     structured = np.zeros(len(log), dtype=oracle.EVENT_DTYPE)
     for field_index, field in enumerate(oracle.EVENT_DTYPE.names):
         structured[field] = [row[field_index] for row in log]
-    out = os.path.join(HERE, "trajectory_%s.npz" % name)
-    np.savez_compressed(out, events=structured, initial=positions, final=final,
-                        charges=np.zeros(0) if charges is None else charges,
-                        spec=json.dumps(dict(spec, system_length=length, rng_key=key)))
-    print("%s: %d events, kinds %s -> %s" % (name, len(log), np.bincount(structured["kind"], minlength=8), out))
+    return structured, positions, final, charges, length, key
 
 
 def main(tree: str, names) -> None:

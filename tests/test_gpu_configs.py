@@ -1,9 +1,9 @@
 """The batched configurations of the path on the GPU against the oracle, event by event.
 
-* Batched hard spheres: per chain the packing fraction drawn from [0.10, 0.45] and N from {32 .. 640}, started by
-  random sequential addition below 0.35 and from a jittered face-centred cubic lattice (±2 % of the spacing)
-  above (N = 4 k^3 there, whole lattice cells), chain length 0.3 L, cells of at least one diameter: every event of the FP64 path equals the oracle's bit
-  for bit, and the mixed path equals the FP64 path.
+* Batched hard spheres (chains of the batched workload): per chain the packing fraction drawn from [0.10, 0.45] and
+  N from {32 .. 2048}, started by random sequential addition below 0.35 and from a jittered face-centred cubic
+  lattice (±2 % of the spacing) above (N = 4 k^3 there, whole lattice cells), chain length 0.3 L, cells of at least
+  one diameter: every event of the FP64 path equals the oracle's bit for bit, and the mixed path equals it too.
 * Batched Coulomb replicas: 32 point charges (16 of each sign) with a hard core of radius 0.05 in the unit cube,
   beta = 1, merged-image Coulomb (alpha = 3.45, real-space images to |n| <= 2, k-vectors to |k| <= 6) bounded by
   the inverse-power bound, cell veto on 8^3 cells: discrete outcomes equal the oracle's, event times to 1e-12
@@ -21,19 +21,14 @@ DISCRETE = ("kind", "moved", "target", "new_active", "new_direction", "accepted"
 
 
 def test_batched_hard_spheres_against_the_oracle():
-    from jellyfysh_gb300 import ChainBatch, ChainSpec, chain_key, systems
-    rng = np.random.default_rng(33)
-    specs, positions = [], []
-    for c in range(24):
-        eta = float(rng.uniform(0.10, 0.45))
-        # lattice starts fill whole fcc cells (n = 4 k^3): a partly filled lattice compressed into the box overlaps
-        n = int(rng.integers(32, 641)) if eta < 0.35 else 4 * int(rng.integers(2, 6)) ** 3
-        state, length = systems.batched_hard_sphere_state(n, eta, 0.5, rng)
-        m = max(3, min(int(length / 1.0), 24))
-        specs.append(ChainSpec(n=n, system_length=length, cells_per_side=m, neighbor_layers=1, max_occupants=1,
-                               hs_radius=0.5, chain_time=0.3 * length, initial_active=int(rng.integers(n)),
-                               initial_direction=int(rng.integers(3))))
-        positions.append(state)
+    from jellyfysh_gb300 import ChainBatch, chain_key, workloads
+    # the batched hard-sphere workload itself, 32 of its chains: N from 32 to 2048, packing fractions 0.10 - 0.45
+    specs, positions, _, _ = workloads.hard_spheres(32, seed_offset=7)
+    sizes = np.array([spec.n for spec in specs])
+    fractions = np.array([spec.n * (4.0 / 3.0) * np.pi * spec.hs_radius ** 3 / spec.system_length ** 3
+                          for spec in specs])
+    assert sizes.max() > 1500 and sizes.min() < 300
+    assert fractions.max() > 0.4 and fractions.min() < 0.15
     events = 300
     batch = ChainBatch(specs, positions, seed=8)
     logs = batch.run(events, mode="exact", log_capacity=events)
@@ -43,9 +38,10 @@ def test_batched_hard_spheres_against_the_oracle():
     mixed.check_status()
     for c, spec in enumerate(specs):
         system = oracle.make_system(n=spec.n, system_length=spec.system_length, cells_per_side=spec.cells_per_side,
-                                    neighbor_layers=1, max_occupants=1, chain_time=spec.chain_time,
+                                    neighbor_layers=spec.neighbor_layers, max_occupants=1, chain_time=spec.chain_time,
                                     initial_active=spec.initial_active, initial_direction=spec.initial_direction,
-                                    potential=oracle.POT_HARD_SPHERE, hs_radius=0.5, rng_key=chain_key(8, c))
+                                    potential=oracle.POT_HARD_SPHERE, hs_radius=spec.hs_radius,
+                                    rng_key=chain_key(8, c))
         chain = oracle.Chain(system, positions[c])
         expected = chain.run(events)
         for field in expected.dtype.names:

@@ -314,3 +314,106 @@ def test_separation_samples_equal_the_reference_output_handler(tmp_path):
     assert reference[0].startswith("# Run identification hash") and ours[0].startswith("# Run identification hash")
     assert reference[1:] == ours[1:]
 
+
+
+NEIGHBOURHOOD_SECTION = """
+[PairNeighbourhood]
+create = {create}
+trash = {create}
+internal_state_label = single_active_cell_occupancy
+event_handler = gpu_neighbourhood_event_handler
+number_event_handlers = 2
+
+[GpuNeighbourhoodEventHandler]
+potential = {potential}
+
+[{potential_section}]
+{parameters}
+"""
+
+
+def neighbourhood_configuration(text, spec):
+    """The trajectory configuration with the pairwise nearby and surplus taggers (one TwoLeafUnitEventHandler per
+    target) replaced by the GPU neighbourhood tagger and its event handler, which take the same targets as one
+    in-state.  Everything else of the configuration stays."""
+    import re
+    text = text.replace("pair_nearby (excluded_cells_tagger),\n    pair_surplus (surplus_cells_tagger)",
+                        "pair_neighbourhood (gpu_neighbourhood_tagger)")
+    text = text.replace("pair_nearby, pair_surplus", "pair_neighbourhood")
+    create = re.search(r"\[CellBoundary\]\ncreate = ([^\n]*)\n", text).group(1)
+    if spec["potential"] == "hard_sphere":
+        potential, section, parameters = "gpu_hard_sphere_potential", "GpuHardSpherePotential", "radius = %r" % (
+            spec["radius"],)
+    else:
+        potential, section, parameters = ("gpu_lennard_jones_potential", "GpuLennardJonesPotential",
+                                          "prefactor = 1.0\ncharacteristic_length = 1.0")
+    start = text.index("\n[PairNearby]")
+    end = text.index("\n[TwoLeafUnitEventHandler]")
+    end = text.index("\n[", end + 1)
+    return text[:start] + NEIGHBOURHOOD_SECTION.format(create=create, potential=potential,
+                                                       potential_section=section, parameters=parameters) + text[end:]
+
+
+def run_neighbourhood_handler(name):
+    """The reference's SingleProcessMediator on a trajectory configuration whose pair taggers are the GPU
+    neighbourhood tagger and event handler, built by the reference's factory (run in a child).  The random numbers are
+    the trajectory's keyed draws.  The batched solve of the handler (one GPU launch of the potential for all targets,
+    tested against the oracle on the GPU in tests/test_gpu_neighbourhood.py) is taken by a stand-in that solves the
+    same pairs with the oracle, so that this test runs the reference's CPU-only loop with the drop-in's tagger,
+    in-states, time slicing and out-states.  Returns the logged events and final positions."""
+    factory, camel = _reference()
+    sys.path.insert(0, os.path.join(ROOT, "tests", "golden"))
+    import make_reference_trajectories as trajectories
+    import oracle
+    spec = dict(trajectories.SYSTEMS[name])
+
+    def solve_with_oracle(potential, velocity, separations, charges, potential_changes):
+        if spec["potential"] == "hard_sphere":
+            times = [oracle.hs_displacement(spec["radius"], velocity, s) for s in separations]
+        else:
+            times = [oracle.lj_displacement(1.0, 1.0, velocity, s, du) for s, du in zip(separations, potential_changes)]
+        if not times:
+            return -1, float("inf")
+        index = int(np.argmin(times))
+        return (-1, float("inf")) if np.isinf(times[index]) else (index, float(times[index]))
+
+    calls = {"solves": 0, "targets": 0}
+
+    def counted_solve(potential, velocity, separations, charges, potential_changes):
+        calls["solves"] += 1
+        calls["targets"] += len(separations)
+        return solve_with_oracle(potential, velocity, separations, charges, potential_changes)
+
+    def prepare(context):
+        import jellyfysh.event_handler.gpu_neighbourhood_event_handler as handler_module
+        handler_module.earliest = counted_solve
+
+        def keyed_change(self, unit):
+            return oracle.expovariate(oracle.draw(context["key"], context["event_index"](), oracle.RNG_PAIR,
+                                                  unit.identifier[0]), context["beta"])
+        handler_module.GpuNeighbourhoodEventHandler._potential_change = keyed_change
+        context["kinds"]["GpuNeighbourhoodEventHandler"] = oracle.EV_PAIR
+
+    def transform(text):
+        text = neighbourhood_configuration(text, spec)
+        assert "[PairNearby]" not in text and "two_leaf_unit_event_handler" not in text
+        return text
+
+    events, _, final, _, _, _ = trajectories.record(TREE, spec, transform=transform, prepare=prepare)
+    return {"events": {field: events[field].tolist() for field in events.dtype.names}, "final": final.tolist(),
+            "calls": calls}
+
+
+@pytest.mark.parametrize("name", ["hard_spheres_n64", "lennard_jones_n64_cell_veto"])
+def test_neighbourhood_event_handler_reproduces_the_reference_trajectory(name):
+    """The GPU neighbourhood tagger and event handler, selected by name in the reference's configuration and run in
+    the reference's own mediator, reproduce the committed trajectory of the reference's pairwise handlers event for
+    event: the same events, targets, liftings and times, and the same final positions."""
+    result = _in_child("run_neighbourhood_handler", name)
+    spec, initial, charges, events, final = load_trajectory(name)
+    for field in events.dtype.names:
+        assert np.array_equal(np.array(result["events"][field]), events[field]), field
+    assert np.array_equal(np.array(result["final"]), final)
+    # one batched solve per event of the neighbourhood handler, over all targets of the neighbourhood
+    assert result["calls"]["solves"] >= len(events)
+    assert result["calls"]["targets"] > 3 * result["calls"]["solves"]
