@@ -318,6 +318,24 @@ __device__ JF_FLOW int exact_cell_bounding(const RunArgs &A, const ChainDev &ch,
 }
 
 // cell veto, cell boundary and end of chain: the single candidates of lane 0
+// the cell-boundary candidate (cell_boundary_event_handler.py:98-156) of the active unit at coordinate x along the
+// direction d in cell column a (along d), and the persistent end-of-chain candidate
+__device__ inline void boundary_and_end(const EngineView &view, const ChainDev &ch, int d, int a, double x, double ts_q,
+                                        double ts_r, double eoc_q, double eoc_r, int eoc_new, Cand &best) {
+    const double boundary = view.cell_min[ch.geom_offset + (a + 1 == ch.m ? 0 : a + 1)];
+    double sep = boundary - x;
+    if (sep < 0.0) sep = sep + ch.L;
+    offer(best, ts_q, ts_r, div_speed(ch, sep), JFGPU_EV_BOUNDARY, -1, -1, boundary);
+    Cand e;
+    e.q = eoc_q;
+    e.r = eoc_r;
+    e.kind = JFGPU_EV_END_OF_CHAIN;
+    e.target = eoc_new;
+    e.aux = -1;
+    e.rate = 0.0;
+    if (cand_better(e, best)) best = e;
+}
+
 __device__ JF_FLOW int single_candidates(const RunArgs &A, const ChainDev &ch, const SpeciesDev &sp,
                                              const WarpState &w, int active_cell, long long ev, Cand &best) {
     const int d = w.direction;
@@ -341,18 +359,7 @@ __device__ JF_FLOW int single_candidates(const RunArgs &A, const ChainDev &ch, c
     }
     int ax[3];
     cell_axes(ch, active_cell, ax);
-    double boundary = A.view.cell_min[ch.geom_offset + (ax[d] + 1 == ch.m ? 0 : ax[d] + 1)];
-    double sep = boundary - w.pa[d];
-    if (sep < 0.0) sep = sep + ch.L;
-    offer(best, w.ts_q, w.ts_r, div_speed(ch, sep), JFGPU_EV_BOUNDARY, -1, -1, boundary);
-    Cand e;
-    e.q = w.eoc_q;
-    e.r = w.eoc_r;
-    e.kind = JFGPU_EV_END_OF_CHAIN;
-    e.target = w.eoc_new;
-    e.aux = -1;
-    e.rate = 0.0;
-    if (cand_better(e, best)) best = e;
+    boundary_and_end(A.view, ch, d, ax[d], w.pa[d], w.ts_q, w.ts_r, w.eoc_q, w.eoc_r, w.eoc_new, best);
     return JFGPU_STATUS_OK;
 }
 
@@ -391,10 +398,16 @@ __device__ inline void occ_insert(const RunArgs &A, const ChainDev &ch, WarpStat
 
 __device__ JF_FLOW int occ_update(const RunArgs &A, const ChainDev &ch, WarpState &w) {
     if (w.active != w.occ_active) {
-        if (w.occ_active >= 0) occ_insert(A, ch, w, w.occ_cell, w.occ_active);
-        JF_TRY(cell_of(A.view, ch, w.pa, w.occ_cell));
-        w.occ_active = w.active;
         const int32_t role = A.roles[ch.pos_off + w.active];
+        if (w.occ_active >= 0) occ_insert(A, ch, w, w.occ_cell, w.occ_active);
+        if (role & (kRoleSurplus | kRoleActive)) {
+            JF_TRY(cell_of(A.view, ch, w.pa, w.occ_cell));
+        } else {
+            // an occupant has not moved since it entered its cell (only the active unit moves): the cell of its
+            // position is the one its role word names
+            w.occ_cell = (role & 0xFF) + ch.m * (((role >> 8) & 0xFF) + ch.m * ((role >> 16) & 0xFF));
+        }
+        w.occ_active = w.active;
         A.roles[ch.pos_off + w.active] = kRoleActive;
         int32_t *slots = A.occupancy + ch.occ_off + (long long)w.occ_cell * ch.max_occ;
         for (int k = 0; k < ch.max_occ; ++k)
@@ -1292,8 +1305,11 @@ __global__ void __launch_bounds__(JF_RESOLVE_THREADS) resolve_kernel(RunArgs A, 
     Cand best = cand_none();
     int st = single_candidates(A, ch, sp, w, w.occ_cell, w.events, best);
     if (!st) {
+        // the rare serial re-solves call out of line with a copy of the lifting state, so that the state itself is
+        // never addressed and stays in registers
         if (list.flags & kListOverflow) {
-            st = exact_serial<POT, FAR>(A, ch, sp, w, best);
+            const WarpState frozen = w;
+            st = exact_serial<POT, FAR>(A, ch, sp, frozen, best);
             if (potential_of<POT>(ch) != JFGPU_POT_COULOMB) w.fallbacks += 1;
         } else {
             for (int i = 0; i < list.count && i < kRefineSlots && !st; ++i) {
@@ -1311,11 +1327,15 @@ __global__ void __launch_bounds__(JF_RESOLVE_THREADS) resolve_kernel(RunArgs A, 
                     if (cand_better(cnd, best)) best = cnd;
                 }
             }
-            for (int i = kRefineSlots; i < list.count && !st; ++i) {
-                const int code = list.code[i];
-                const int j = code_target(code);
-                st = code_far(code) ? exact_cell_bounding_ool(A, ch, sp, w, j, w.occ_cell, w.events, best)
-                                    : exact_pair_ool<POT>(A, ch, sp, w, j, w.events, best);
+            if (list.count > kRefineSlots) {
+                const WarpState frozen = w;
+                for (int i = kRefineSlots; i < list.count && !st; ++i) {
+                    const int code = list.code[i];
+                    const int j = code_target(code);
+                    st = code_far(code)
+                             ? exact_cell_bounding_ool(A, ch, sp, frozen, j, frozen.occ_cell, frozen.events, best)
+                             : exact_pair_ool<POT>(A, ch, sp, frozen, j, frozen.events, best);
+                }
             }
         }
     }
