@@ -107,7 +107,7 @@ DATA = {"lennard_jones": "synthetic: seeded simple-cubic lattice + uniform jitte
                         "lattice above",
         "hard_spheres_n64": "synthetic: seeded random sequential addition"}
 KERNELS = {"lennard_jones": "jf::screen_kernel<1, 2>", "hard_spheres": "jf::screen_kernel<0, 0>",
-           "hard_spheres_n64": "jf::screen_kernel<0, 0>", "coulomb": "jf::chains_kernel<-1, -1>"}
+           "hard_spheres_n64": "jf::screen_kernel<0, 0>", "coulomb": "jf::coulomb_group_kernel<32>"}
 
 
 def metric_of(args):
@@ -549,7 +549,7 @@ def gpu_arm(args):
                   parallelism="replicas" if world > 1 else "single GPU")
     line = {"metric": metric_of(args), "value": value, "unit": "events/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64" if coulomb else "f32+f64",
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
             "data": data_of(args), "config": config,
             "e2e": {"value": e2e_value, "unit": "events/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "pipelining": "two batches take the steps in turn; each batch's copies overlap the other's run"},

@@ -685,17 +685,18 @@ __device__ __noinline__ int occ_update_ool(const RunArgs &A, const ChainDev &ch,
 // candidate enumeration
 // ---------------------------------------------------------------------------------------------------------------
 
-// base-K digits (x, y, z) of lane + 32 k, advanced by 32 without divisions (K >= 1; one carry per digit)
+// base-K digits (x, y, z) of lane + step k (step 32 by default), advanced without divisions (K >= 1, step <= 32; one
+// carry per digit)
 struct Digits {
     int x, y, z, sx, sy, sz, K;
-    __device__ inline void start(int lane, int base) {
+    __device__ inline void start(int lane, int base, int step = 32) {
         K = base;
         x = lane % K;
         y = (lane / K) % K;
         z = lane / (K * K);
-        sx = 32 % K;
-        sy = (32 / K) % K;
-        sz = 32 / (K * K);
+        sx = step % K;
+        sy = (step / K) % K;
+        sz = step / (K * K);
     }
     __device__ inline void advance() {
         x += sx;
@@ -712,15 +713,16 @@ struct Digits {
     }
 };
 
-// occupants of the nearby cells of the occupancy's active cell (ExcludedCellsTagger)
+// occupants of the nearby cells of the occupancy's active cell (ExcludedCellsTagger), lane `lane` of `step` lanes
 template <typename F>
-__device__ inline void for_each_near(const RunArgs &A, const ChainDev &ch, int occ_cell, int lane, F &&f) {
+__device__ inline void for_each_near(const RunArgs &A, const ChainDev &ch, int occ_cell, int lane, F &&f,
+                                     int step = 32) {
     int a[3];
     cell_axes(ch, occ_cell, a);
     const int K = ch.n_res;
     const int32_t *occ = A.occupancy + ch.occ_off;
     Digits g;
-    g.start(lane, K);
+    g.start(lane, K, step);
     for (; g.z < K; g.advance()) {
         int cx = a[0] + ch.res[g.x], cy = a[1] + ch.res[g.y], cz = a[2] + ch.res[g.z];
         if (cx >= ch.m) cx -= ch.m;
@@ -1485,6 +1487,254 @@ __global__ void __launch_bounds__(256, JF_CHAIN_MIN_BLOCKS) chains_kernel(RunArg
 }
 
 // ---------------------------------------------------------------------------------------------------------------
+// Merged-image Coulomb replicas in the mixed mode, several chains a warp.  Almost every event of these chains is a
+// cell-veto event whose work is serial (the alias sample, the potential change, the time arithmetic, the commit):
+// FP64 work of one lane, and an FP64 warp instruction occupies GB300's FP64 pipe for 16 cycles however few lanes it
+// has.  A group of GW lanes runs each chain, 32 / GW chains a warp, so that one FP64 instruction advances the serial
+// step of every chain of the warp.  The single candidates (cell veto, cell boundary, end of chain) come first, in
+// FP64 by the group's first lane; their earliest displacement bounds the pair candidates that can still win.  Every
+// nearby occupant and surplus unit is screened in FP32 over the group's lanes: the hard core by hs_screen (within
+// 2^-12 relative plus the chain's absolute margin unless flagged), the inverse-power Coulomb bound by
+// ipcb_x_displacement32 with its rigorous error bound, the potential change in FP32 from the same keyed draw (error
+// within 32 units of 2^-24).  A pair whose screened displacement, less its error, does not exceed the bound (or whose
+// screen cannot decide) is solved in FP64 with the reference's arithmetic, as the FP64 path solves it; the others
+// come after the single candidates and cannot win.  The thinning derivative is shared by the group (mic_x_group,
+// equal to the warp's sum bit for bit).
+// The events equal the FP64 path's bit for bit.  Groups whose chain has stopped skip the work of an event (their
+// lanes are left out of the group's shuffles by masks).
+// ---------------------------------------------------------------------------------------------------------------
+#ifndef JF_COULOMB_GROUP
+#define JF_COULOMB_GROUP 32  // lanes per chain of the grouped Coulomb kernel (8 and 16 measured slower)
+#endif
+
+template <int GW>
+__device__ inline int group_sum_int(int v, unsigned mask) {
+#pragma unroll
+    for (int offset = GW / 2; offset > 0; offset >>= 1) v += __shfl_xor_sync(mask, v, offset);
+    return v;
+}
+
+template <int GW>
+__device__ inline int group_max_int(int v, unsigned mask) {
+#pragma unroll
+    for (int offset = GW / 2; offset > 0; offset >>= 1) v = max(v, __shfl_xor_sync(mask, v, offset));
+    return v;
+}
+
+template <int GW>
+__device__ inline Cand group_argmin(Cand c, unsigned mask) {
+#pragma unroll
+    for (int offset = GW / 2; offset > 0; offset >>= 1) {
+        Cand o;
+        o.q = __shfl_xor_sync(mask, c.q, offset);
+        o.r = __shfl_xor_sync(mask, c.r, offset);
+        o.kind = __shfl_xor_sync(mask, c.kind, offset);
+        o.target = __shfl_xor_sync(mask, c.target, offset);
+        o.aux = __shfl_xor_sync(mask, c.aux, offset);
+        o.rate = __shfl_xor_sync(mask, c.rate, offset);
+        if (cand_better(o, c)) c = o;
+    }
+    return c;
+}
+
+// the candidates of a chain's event over the GW lanes of its group (mask: the lanes of every group that calls it)
+template <int GW>
+__device__ inline int group_screened_candidates(const RunArgs &A, const ChainDev &ch, const SpeciesDev &sp,
+                                                const WarpState &w, int glane, int leader, unsigned mask, Cand &best,
+                                                int &counted) {
+    const long long ev = w.events;
+    int status = JFGPU_STATUS_OK;
+    best = cand_none();
+    if (glane == 0) status = single_candidates_ool(A, ch, sp, w, w.occ_cell, ev, best);
+    double reach = glane == 0 ? time_sub(best.q, best.r, w.ts_q, w.ts_r) * ch.speed : 0.0;
+    reach = __shfl_sync(mask, reach, leader);
+    const float bound = (float)reach * (1.0f + 1.0f / 1024.0f) + ch.screen_abs32;
+    const int d = w.direction;
+    const float inv_beta32 = ch.inv_beta32;
+    const double charge_active = charge_of(A, ch, w.active);
+    int count = 0;
+    auto screen = [&](int j) {
+        ++count;
+        double pj[3], s[3];
+        load_pos(A, ch, j, pj);
+        separation64(ch, w.pa, pj, s);
+        bool solve = false;
+        if (ch.diameter_sq > 0.0) {
+            float sv[3] = {(float)s[0], (float)s[1], (float)s[2]};
+            bool flag = false;
+            const float x = hs_screen(ch.diameter_sq32, d, 1.0f, sv, ch.ulp_margin32, flag);
+            if (flag || x * (1.0f - 1.0f / 4096.0f) - ch.screen_abs32 <= bound) solve = true;
+        }
+        if (!solve) {
+            const uint64_t n = draw(ch.key, (uint64_t)ev, kRngPair, (uint32_t)j) >> 11;
+            const float du = n < (1ull << 52) ? -log1pf(-(float)n * 0x1p-53f) * inv_beta32
+                                              : -logf((float)((1ull << 53) - n) * 0x1p-53f) * inv_beta32;
+            const float du_error = 32.f * 0x1p-24f * du;
+            double p[3];
+            permute3(s, d, p);
+            float error;
+            bool unsafe = false;
+            const float x = ipcb_x_displacement32((float)(ch.bound_prefactor * charge_active * charge_of(A, ch, j)),
+                                                  (float)p[0], (float)p[1], (float)p[2], du, du_error, ch.L32, error,
+                                                  unsafe);
+            if (unsafe || !(x - error > bound)) solve = true;
+        }
+        if (solve) {
+            const int st = exact_pair_ool<JFGPU_POT_COULOMB>(A, ch, sp, w, j, ev, best);
+            if (st) status = st;
+        }
+    };
+    for_each_near(A, ch, w.occ_cell, glane, [&](int j) { screen(j); }, GW);
+    for (int i = glane; i < w.n_surplus; i += GW) screen(A.surplus[ch.pos_off + i]);
+    counted = group_sum_int<GW>(count, mask);
+    best = group_argmin<GW>(best, mask);
+    return group_max_int<GW>(status, mask);
+}
+
+// warp_real_rate for the group of a chain (mask: the lanes of every group that calls it)
+template <int GW>
+__device__ inline void group_real_rate(const RunArgs &A, const ChainDev &ch, const SpeciesDev &sp, WarpState &w,
+                                       const Cand &best, int glane, int leader, unsigned mask) {
+    int t = -1;
+    double pa[3] = {0.0, 0.0, 0.0};
+    if (glane == 0) {
+        w.real_target = -1;
+        if (best.kind == JFGPU_EV_BOUNDED)
+            t = best.target;
+        else if (best.kind == JFGPU_EV_CELL_VETO)
+            t = A.occupancy[ch.occ_off + (long long)best.aux * ch.max_occ];
+        if (t >= 0) {
+            const double dt = time_sub(best.q, best.r, w.ts_q, w.ts_r);  // as time_slice
+            for (int k = 0; k < 3; ++k) pa[k] = w.pa[k];
+            pa[w.direction] = py_mod_near(w.pa[w.direction] + ch.speed * dt, ch.L);
+        }
+    }
+    t = __shfl_sync(mask, t, leader);
+    const unsigned need = __ballot_sync(mask, t >= 0);
+    if (t < 0) return;
+    for (int k = 0; k < 3; ++k) pa[k] = __shfl_sync(need, pa[k], leader);
+    double pt[3], s[3], p[3];
+    load_pos(A, ch, t, pt);
+    separation64(ch, pa, pt, s);
+    permute3(s, w.direction, p);
+    CompositeModel model;
+    model.mic = sp.mic;
+    model.images = sp.mic_terms;
+    model.n_images = sp.mic_images;
+    model.rows = sp.mic_terms + sp.mic_images;
+    model.n_rows = sp.mic_rows;
+    const double value = mic_x_group<GW>(model, p[0], p[1], p[2], glane, need);
+    if (glane == 0) {
+        w.real_value = mul_speed(ch, ch.coulomb_prefactor * charge_of(A, ch, w.active) * charge_of(A, ch, t) * value);
+        w.real_target = t;
+    }
+}
+
+template <int GW>
+__global__ void __launch_bounds__(256, JF_CHAIN_MIN_BLOCKS) coulomb_group_kernel(RunArgs A) {
+    constexpr int G = 32 / GW;
+    extern __shared__ unsigned char smem_raw[];
+    WarpState *shared = reinterpret_cast<WarpState *>(smem_raw);
+    const int warp = threadIdx.x >> 5;
+    const int lane = threadIdx.x & 31;
+    const int group = lane / GW, glane = lane % GW, leader = group * GW;
+    const long long local = ((long long)blockIdx.x * (blockDim.x >> 5) + warp) * G + group;
+    const bool exists = local < A.count;
+    if (!__any_sync(kFull, exists)) return;
+    const long long c = A.first_chain + (exists ? local : 0);
+    const ChainDev &ch = A.view.chains[c];
+    const SpeciesDev &sp = A.view.species[ch.species];
+    WarpState &w = shared[warp * G + group];
+    if (glane == 0 && exists) {
+        const JfgpuChainState &g = A.state[c];
+        w.ts_q = g.time_q;
+        w.ts_r = g.time_r;
+        w.eoc_q = g.eoc_q;
+        w.eoc_r = g.eoc_r;
+        w.events = g.events;
+        w.warnings = g.bound_warnings;
+        w.fallbacks = g.refine_fallbacks;
+        w.candidates = g.candidates;
+        w.refined = g.refined;
+        w.lift_sum = g.lift_sum;
+        w.liftings = g.liftings;
+        w.far_lookups = g.far_lookups;
+        w.active = g.active;
+        w.direction = g.direction;
+        w.eoc_new = g.eoc_new_active;
+        w.occ_active = g.occ_active;
+        w.occ_cell = g.occ_cell;
+        w.n_surplus = g.n_surplus;
+        w.status = g.status;
+        w.stop = 0;
+        w.real_target = -1;
+        load_pos(A, ch, w.active, w.pa);
+    }
+    __syncwarp();
+    const long long start_events = exists ? w.events : 0;
+    for (long long e = 0; e < A.max_events; ++e) {
+        bool live = exists && w.status == JFGPU_STATUS_OK && !w.stop;
+        if (!__any_sync(kFull, live)) break;
+        if (live && glane == 0 && w.active != w.occ_active) {
+            const int st = occ_update_ool(A, ch, w);
+            if (st) w.status = st;
+        }
+        __syncwarp();
+        live = live && w.status == JFGPU_STATUS_OK;
+        const unsigned live_mask = __ballot_sync(kFull, live);
+        Cand best = cand_none();
+        int status = JFGPU_STATUS_OK, counted = 0;
+        if (live) status = group_screened_candidates<GW>(A, ch, sp, w, glane, leader, live_mask, best, counted);
+        __syncwarp();
+        if (live && glane == 0) w.candidates += counted;
+        const bool stop_here = A.has_stop && !time_lt(best.q, best.r, A.stop_q, A.stop_r);
+        const bool real = live && status == JFGPU_STATUS_OK && sp.mic_terms != nullptr && !stop_here;
+        const unsigned real_mask = __ballot_sync(kFull, real);
+        if (real) group_real_rate<GW>(A, ch, sp, w, best, glane, leader, real_mask);
+        __syncwarp();
+        if (live && glane == 0) {
+            if (status) {
+                w.status = status;
+            } else if (stop_here) {
+                time_slice(ch, w, A.stop_q, A.stop_r);
+                store_active(A, ch, w, w.active);
+                w.stop = 1;
+                const int st = occ_update_ool(A, ch, w);
+                if (st) w.status = st;
+            } else {
+                int st = commit_ool(A, ch, sp, w, best, w.occ_cell, c, w.events - start_events);
+                if (!st) st = occ_update_ool(A, ch, w);  // the activator's update of the next event
+                if (st) w.status = st;
+            }
+            w.real_target = -1;
+        }
+        __syncwarp();
+    }
+    if (exists && glane == 0) {
+        JfgpuChainState &g = A.state[c];
+        g.time_q = w.ts_q;
+        g.time_r = w.ts_r;
+        g.eoc_q = w.eoc_q;
+        g.eoc_r = w.eoc_r;
+        g.events = w.events;
+        g.bound_warnings = w.warnings;
+        g.refine_fallbacks = w.fallbacks;
+        g.candidates = w.candidates;
+        g.refined = w.refined;
+        g.lift_sum = w.lift_sum;
+        g.liftings = w.liftings;
+        g.active = w.active;
+        g.direction = w.direction;
+        g.eoc_new_active = w.eoc_new;
+        g.occ_active = w.occ_active;
+        g.occ_cell = w.occ_cell;
+        g.n_surplus = w.n_surplus;
+        g.status = w.status;
+        g.stopped = w.stop;
+    }
+}
+
+// ---------------------------------------------------------------------------------------------------------------
 // start of the chains: FP32 mirror, occupancy in particle order (single_active_cell_occupancy.py:95-121),
 // lifting state at time 0 (initial_chain_start_of_run_event_handler.py) and the first end-of-chain candidate
 // ---------------------------------------------------------------------------------------------------------------
@@ -1831,9 +2081,10 @@ cudaError_t launch_run(const EngineView &view, const JfgpuBuffers &b, long long 
     if (warps < 1) warps = 1;
     if (warps > 8) warps = 8;
     if (count < warps) warps = (int)count;
-    // merged-image Coulomb chains have no FP32 screen in the round kernels (their resolve thread would solve the
-    // whole event serially, 32 chains diverging in a warp): a batch of them runs the warp-per-chain FP64 kernel in
-    // either mode, with the same events
+    // merged-image Coulomb chains (a few dozen charges, almost every event a cell-veto event) run the warp-per-chain
+    // kernel in either mode: the mixed mode screens their pair candidates in FP32 (screened_candidates)
+    const bool coulomb_screen = mode == JFGPU_MODE_MIXED && uniform_potential == JFGPU_POT_COULOMB &&
+                                uniform_far == JFGPU_FAR_CELL_VETO;
     if (mode == JFGPU_MODE_MIXED && uniform_potential == JFGPU_POT_COULOMB) mode = JFGPU_MODE_EXACT;
     if (mode == JFGPU_MODE_MIXED) {
         // groups of at least one block of warps each; the event log stays on the caller's stream
@@ -1901,7 +2152,14 @@ cudaError_t launch_run(const EngineView &view, const JfgpuBuffers &b, long long 
         const long long blocks = (count + warps - 1) / warps;
         const size_t smem = sizeof(WarpState) * warps;
         if (plan.clock) plan.clock->begin(plan.stream);
-        chains_kernel<-1, -1><<<(unsigned)blocks, warps * 32, smem, plan.stream>>>(A);
+        if (coulomb_screen) {
+            constexpr int G = 32 / JF_COULOMB_GROUP;
+            const long long group_blocks = (count + (long long)warps * G - 1) / ((long long)warps * G);
+            coulomb_group_kernel<JF_COULOMB_GROUP>
+                <<<(unsigned)group_blocks, warps * 32, smem * G, plan.stream>>>(A);
+        } else {
+            chains_kernel<-1, -1><<<(unsigned)blocks, warps * 32, smem, plan.stream>>>(A);
+        }
         if (plan.clock) plan.clock->end(plan.stream, JFGPU_KERNEL_CHAINS);
         *launches += 1;
     }

@@ -153,6 +153,84 @@ static __device__ __noinline__ double mic_x_warp(const CompositeModel &c, double
     return derivative;
 }
 
+// mic_x_warp over a group of GW lanes (8 or 16) of a warp in which several chains each have a group: every lane takes
+// the terms of 32 / GW of mic_x_warp's lanes (lane l, l + GW, ...) into separate partial sums, and the partial sums
+// are combined in the order of mic_x_warp's butterfly (offsets 16, 8, ... 1; the offsets of at least GW between a
+// lane's own partial sums, the smaller ones by shuffles within the group), so that the value equals mic_x_warp's bit
+// for bit.  mask: the lanes of every group that calls it (whole groups).
+template <int GW>
+__device__ inline double mic_x_group(const CompositeModel &c, double sx, double sy, double sz, int glane,
+                                     unsigned mask) {
+    constexpr int V = 32 / GW;
+    const MIC &m = c.mic;
+    const int n = m.fourier_cutoff + 1;
+    double part[V];
+#pragma unroll
+    for (int k = 0; k < V; ++k) part[k] = 0.0;
+#pragma unroll
+    for (int k = 0; k < V; ++k) {
+        const int lane = glane + GW * k;
+        double derivative = 0.0;
+        for (int e = lane; e < c.n_images; e += 32) {
+            const int4 image = c.images[e];
+            const double vector_z_sq = (sz + image.z * m.system_length) * (sz + image.z * m.system_length);
+            const double vector_y_sq = (sy + image.y * m.system_length) * (sy + image.y * m.system_length);
+            const double vector_x = sx + image.x * m.system_length;
+            const double vector_sq = vector_x * vector_x + vector_y_sq + vector_z_sq;
+            const double vector_norm = sqrt(vector_sq);
+            derivative += vector_x *
+                          (m.two_alpha_over_length_root_pi * exp(-m.alpha_over_length_sq * vector_sq) +
+                           erfc(m.alpha_over_length * vector_norm) / vector_norm) /
+                          vector_sq;
+        }
+        if (c.n_rows > 0 && 31 - lane < c.n_rows) {
+            const double delta_cos_x = cos(m.two_pi_over_length * sx);
+            const double delta_sin_x = sin(m.two_pi_over_length * sx);
+            const double delta_cos_y = cos(m.two_pi_over_length * sy);
+            const double delta_sin_y = sin(m.two_pi_over_length * sy);
+            const double delta_cos_z = cos(m.two_pi_over_length * sz);
+            const double delta_sin_z = sin(m.two_pi_over_length * sz);
+            for (int e = 31 - lane; e < c.n_rows; e += 32) {
+                const int4 row = c.rows[e];
+                double cos_x = delta_cos_x, sin_x = delta_sin_x, store;
+                for (int i = 1; i < row.x; ++i) {
+                    store = cos_x;
+                    cos_x = store * delta_cos_x - sin_x * delta_sin_x;
+                    sin_x = sin_x * delta_cos_x + store * delta_sin_x;
+                }
+                double cos_y = 1.0, sin_y = 0.0;
+                for (int j = 0; j < row.y; ++j) {
+                    store = cos_y;
+                    cos_y = store * delta_cos_y - sin_y * delta_sin_y;
+                    sin_y = sin_y * delta_cos_y + store * delta_sin_y;
+                }
+                double cos_z = 1.0, sin_z = 0.0;
+                for (int kk = 0; kk < row.z + 1; ++kk) {
+                    derivative += m.fourier[(row.x * n + row.y) * n + kk] * sin_x * cos_y * cos_z;
+                    store = cos_z;
+                    cos_z = store * delta_cos_z - sin_z * delta_sin_z;
+                    sin_z = sin_z * delta_cos_z + store * delta_sin_z;
+                }
+            }
+        }
+        part[k] = derivative;
+    }
+    // the butterfly: lane v adds lane v ^ offset; v = glane + GW k, so an offset of at least GW pairs k with k ^ step
+#pragma unroll
+    for (int offset = 16; offset >= GW; offset >>= 1) {
+        const int step = offset / GW;
+        double next[V];
+#pragma unroll
+        for (int k = 0; k < V; ++k) next[k] = part[k] + part[k ^ step];
+#pragma unroll
+        for (int k = 0; k < V; ++k) part[k] = next[k];
+    }
+    double derivative = part[0];
+#pragma unroll
+    for (int offset = GW / 2; offset > 0; offset >>= 1) derivative += __shfl_xor_sync(mask, derivative, offset);
+    return derivative;
+}
+
 // HypercubicPeriodicBoundaries.separation_vector (setting/hypercubic_setting.py:120-140, :156-172)
 __device__ inline void periodic_separation(const double *from, const double *to, double length, double *s) {
     const double half = length / 2.0;
