@@ -49,11 +49,13 @@ SYSTEMS = {
                                                        cells_per_side=12, neighbor_layers=3, chain_time=2.0,
                                                        beta=1.0 / 1.2, far="cell_veto", seed=16, events=1000,
                                                        state="sc", estimator_prefactor=1.5, estimator_points=10),
-    "lennard_jones_n1024_three_layers_cell_bounding": dict(potential="lennard_jones", n=1024, density=0.8,
-                                                           cells_per_side=12, neighbor_layers=3, chain_time=2.0,
-                                                           beta=1.0 / 1.2, far="cell_bounding", seed=17,
-                                                           events=300, state="sc", estimator_prefactor=1.5,
-                                                           estimator_points=10),
+    # three neighbour layers with the cell-bounding far field at N = 512 (9^3 cells): the reference deep-copies one
+    # event handler per cell, and at N = 1024 (12^3 cells) its copies outgrow the memory of the recording machine
+    "lennard_jones_n512_three_layers_cell_bounding": dict(potential="lennard_jones", n=512, density=0.8,
+                                                          cells_per_side=9, neighbor_layers=3, chain_time=2.0,
+                                                          beta=1.0 / 1.2, far="cell_bounding", seed=17,
+                                                          events=400, state="sc", estimator_prefactor=1.5,
+                                                          estimator_points=10),
     "coulomb_n8_cell_veto": dict(potential="coulomb", n=8, radius=0.05, system_length=1.0, cells_per_side=4,
                                  neighbor_layers=1, chain_time=0.7, beta=1.0, far="cell_veto", seed=14, events=2500,
                                  state="rsa_charged", estimator_prefactor=1.0, estimator_points=10),
