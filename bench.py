@@ -48,15 +48,22 @@ WATER_WORKLOAD = dict(workload="water_chains_512x64_molecular_coulomb", chains=5
 NEAR_CELLS = (2 * WORKLOAD["neighbor_layers"] + 1) ** 3  # cells scanned for pair candidates per event
 CPU_SECONDS = 10.0  # wall time of the CPU baseline sample
 TIMING_STRIDE = 16  # event rounds between two rounds bracketed by per-kernel CUDA events
-# DRAM traffic of the screening kernel per event: ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch of
-# this workload (56.53 MB + 0.74 MB) divided by the 4096 events of that launch (the committed ncu summary of the
-# round kernels)
-NCU_TRAFFIC_PER_EVENT = (56.533504e6 + 0.742656e6) / 4096
-# the same for the water kernel (2.83 MB + 0.22 MB over 512 chains x 32 events) and the Coulomb chains kernel
-# (4.01 MB + 0.71 MB over 1024 chains x 128 events), with the FP64 pipe's busy fraction of active cycles
-# (sm__pipe_fp64_cycles_active) from the same captures: both kernels are bound by FP64 latency, not by HBM
+# DRAM traffic of the dominant kernel per event, from the ncu captures summarised under profiles/: the screening
+# kernel of the Lennard-Jones workload in steady state (one-pass metrics with the caches left warm, mean of 20
+# launches: 8.07 MB read + 3.97 MB written per launch of 4096 events), with the issue and pipe fractions of its full
+# capture; the hard-sphere screening kernel (a cold-cache capture: 33.78 MB + 0.03 MB per launch of 4096 events); the
+# Coulomb replica kernel (2.53 MB + 0.13 MB per launch of 1024 chains x 8 events) with its FP64 pipe's busy fraction
+NCU = {
+    "lennard_jones": {"traffic_per_event": (8.066662e6 + 3.968077e6) / 4096, "traffic_caches": "warm",
+                      "issue_active": 0.514, "fma_pipe_active": 0.174, "alu_pipe_active": 0.460,
+                      "fp64_pipe_active": 0.036},
+    "hard_spheres": {"traffic_per_event": (33.783296e6 + 0.034304e6) / 4096, "traffic_caches": "cold",
+                     "issue_active": 0.276, "fma_pipe_active": 0.077, "alu_pipe_active": 0.170},
+    "coulomb": {"traffic_per_event": (2.525440e6 + 0.129024e6) / (1024 * 8), "traffic_caches": "cold",
+                "issue_active": 0.096, "fp64_pipe_active": 0.458},
+}
+# the water kernel (2.83 MB + 0.22 MB over 512 chains x 32 events) with the FP64 pipe's busy fraction of its capture
 WATER_NCU = {"traffic_per_event": (2.830080e6 + 0.221952e6) / (512 * 32), "fp64_pipe_active": 0.501}
-COULOMB_NCU = {"traffic_per_event": (4.010496e6 + 0.713728e6) / (1024 * 128), "fp64_pipe_active": 0.598}
 
 
 def parse():
@@ -510,11 +517,8 @@ def gpu_arm(args):
     dominant_s = dominant["ms"] / dominant_launches / 1000.0
     achieved = bytes_per_event * events_per_launch / dominant_s / 1e9
     peak, peak_kind = measured_peaks()
-    traffic = None
-    if args.workload == "coulomb":
-        traffic = COULOMB_NCU["traffic_per_event"] * events_per_launch
-    elif args.workload == "lennard_jones":
-        traffic = NCU_TRAFFIC_PER_EVENT * events_per_launch
+    ncu = NCU.get(args.workload)
+    traffic = ncu["traffic_per_event"] * events_per_launch if ncu else None
     total_kernel_ms = sum(v["ms"] for v in kernel_times.values()) or 1.0
     kernels = {name: {"launches": v["launches"], "ms_per_launch": v["ms"] / max(v["launches"], 1),
                       "share": v["ms"] / total_kernel_ms}
@@ -527,8 +531,8 @@ def gpu_arm(args):
                 "refined_per_event": refined / max(events_done, 1), "fallback_events": fallbacks,
                 "far_lookups_per_event": lookups / max(events_done, 1),
                 "kernels": kernels}
-    if coulomb:
-        roofline["fp64_pipe_active"] = COULOMB_NCU["fp64_pipe_active"]
+    if ncu:
+        roofline["ncu"] = dict(ncu, source="profiles/ (committed ncu summaries of this kernel and workload)")
     cpu = None
     if not args.no_cpu_baseline and world == 1:
         import concurrent.futures
