@@ -378,6 +378,50 @@ int jfgpu_water_run(void *water, double *positions, const double *charges, Jfgpu
                     int64_t first_chain, int64_t events, double stop_q, double stop_r, JfgpuEvent *log,
                     int32_t warps_per_block, void *stream);
 
+/* Water with molecular cells.  Replaces the reference's SingleProcessMediator loop over its water cell-veto
+ * configuration (config_files/2018_JCP_149_064113/water/coulomb_cell_veto_lj_inverted.ini): the molecules' root
+ * units (barycentres) in SingleActiveCellOccupancy (activator/internal_state/single_active_cell_occupancy.py:95-203,
+ * cell_level 1, one occupant per cell), the summed-bounding Coulomb factor with the molecules of the nearby cells
+ * (ExcludedCellsTagger, activator/tagger/excluded_cells_tagger.py:107-132) and with the surplus molecules
+ * (SurplusCellsTagger, surplus_cells_tagger.py:107-131), the molecular cell veto
+ * (CompositeObjectCellVetoEventHandler, event_handler/composite_object_cell_veto_event_handler.py:110-162) and the
+ * cell-boundary event of the active root unit (CellBoundaryEventHandler, event_handler/cell_boundary_event_handler.py:
+ * 98-173), which keeps the bond and Lennard-Jones candidates alive. */
+typedef struct {
+    double pair_q, pair_r;        /* earliest bond / Lennard-Jones candidate (inf: none), kept across cell boundaries */
+    double snap_leaf[3], snap_root[3];  /* the active leaf and root unit as that candidate's in-state holds them */
+    double snap_q, snap_r;        /* ... at this time stamp */
+    int32_t pair_kind, pair_target;
+    int32_t pairs_valid;          /* the candidate above is alive (created, then only cell-boundary events) */
+    int32_t occ_active, occ_cell; /* the occupancy's active molecule (-1: none) and its cell */
+    int32_t reserved;
+    int64_t boundary_events, veto_events, veto_targets;
+} JfgpuWaterCellState;
+
+typedef struct {
+    double *roots;                /* [chains][molecules][3] root positions */
+    int32_t *occupancy;           /* [chains][cells]: the occupant molecule, -1 when empty */
+    int32_t *surplus;             /* [chains][molecules]: the cell of a surplus molecule, -1 otherwise */
+    JfgpuWaterCellState *cell_state;  /* [chains] */
+    double *root_log;             /* [chains][events][3] root of the moved unit's molecule after every event (may be
+                                     null) */
+} JfgpuWaterCellBuffers;
+
+/* attach the cell system to a water model: cells_per_side^3 cuboid periodic cells with neighbor_layers layers of
+ * nearby cells, and the molecular cell veto's bound tables (host arrays [cells][3]: the upper and the negated lower
+ * derivative bound of every relative cell and direction, as the estimator filled
+ * CellVetoEventHandler._derivative_bounds, abstracts/cell_veto_event_handler.py:134-160; NaN for the nearby cells),
+ * from which the Walker tables are built in the reference's order.  cells_per_side 1..32. */
+int jfgpu_water_set_cells(void *water, int32_t cells_per_side, int32_t neighbor_layers, const double *bounds_upper,
+                          const double *bounds_lower);
+/* the occupancy of chains first .. first + chains - 1 from their roots (root nodes in order, the first molecule of a
+ * cell its occupant, the others surplus) and a fresh cell state; with jfgpu_water_init for the rest of the state */
+int jfgpu_water_cells_init(void *water, const JfgpuWaterCellBuffers *buffers, int64_t chains, void *stream);
+/* jfgpu_water_run with the molecular cells (arguments as there) */
+int jfgpu_water_cells_run(void *water, double *positions, const double *charges, JfgpuWaterState *state,
+                          const JfgpuWaterCellBuffers *buffers, int64_t chains, int64_t first_chain, int64_t events,
+                          double stop_q, double stop_r, JfgpuEvent *log, int32_t warps_per_block, void *stream);
+
 /* device buffers of a chain batch, all owned by the caller; sizes from jfgpu_engine_layout */
 typedef struct {
     double *positions;            /* [particles][3], chain c at particle_offset[c] */

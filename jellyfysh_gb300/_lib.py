@@ -91,6 +91,12 @@ class Event(ctypes.Structure):
                 ("y", ctypes.c_double), ("z", ctypes.c_double)]
 
 
+class WaterCellBuffers(ctypes.Structure):
+    """JfgpuWaterCellBuffers."""
+    _fields_ = [("roots", ctypes.c_void_p), ("occupancy", ctypes.c_void_p), ("surplus", ctypes.c_void_p),
+                ("cell_state", ctypes.c_void_p), ("root_log", ctypes.c_void_p)]
+
+
 class Buffers(ctypes.Structure):
     _fields_ = [("positions", ctypes.c_void_p), ("positions32", ctypes.c_void_p), ("charges", ctypes.c_void_p),
                 ("occupancy", ctypes.c_void_p), ("surplus", ctypes.c_void_p), ("roles", ctypes.c_void_p),
@@ -139,6 +145,10 @@ SIGNATURES = {
     "jfgpu_water_destroy": (None, [_P]),
     "jfgpu_water_init": (ctypes.c_int, [_P, _P, _I64, _I64, _P]),
     "jfgpu_water_run": (ctypes.c_int, [_P, _P, _P, _P, _I64, _I64, _I64, _D, _D, _P, _I32, _P]),
+    "jfgpu_water_set_cells": (ctypes.c_int, [_P, _I32, _I32, _P, _P]),
+    "jfgpu_water_cells_init": (ctypes.c_int, [_P, ctypes.POINTER(WaterCellBuffers), _I64, _P]),
+    "jfgpu_water_cells_run": (ctypes.c_int, [_P, _P, _P, _P, ctypes.POINTER(WaterCellBuffers), _I64, _I64, _I64,
+                                             _D, _D, _P, _I32, _P]),
     "jfgpu_engine_create": (ctypes.c_int, [_P, _I64, _P, ctypes.POINTER(ctypes.c_void_p)]),
     "jfgpu_engine_destroy": (None, [_P]),
     "jfgpu_engine_layout": (ctypes.c_int, [_P, ctypes.POINTER(Layout)]),

@@ -381,6 +381,27 @@ __device__ inline bool composite_thinning(const CompositeModel &m, int draw_mode
     return !(event_rate <= thinning);
 }
 
+// The thinning against a given bounding event rate (the molecular cell-bounding handler,
+// two_composite_object_cell_bounding_potential_event_handler.py:231-253, and the molecular cell veto with a target,
+// composite_object_cell_veto_event_handler.py:131-153): the summed pair derivatives, event_rate = max(0, sum), and
+// event_rate <= uniform(0, given) rejects.  Fills target_factor as composite_thinning does.
+__device__ inline int composite_given_thinning(const CompositeModel &m, int draw_mode, double given,
+                                               const double *pair, const double *draws, double *target_factor,
+                                               double &bounding_rate, double &event_rate, bool &confirmed) {
+    // assert bounding_event_rate >= 0.0 (:243, composite_object_cell_veto_event_handler.py:150)
+    if (!(given >= 0.0)) return JFGPU_STATUS_ASSERTION;
+    double factor = 0.0;
+    for (int j = 0; j < m.units; ++j) {
+        factor += pair[j];
+        target_factor[j] = 0.0 - pair[j];
+    }
+    bounding_rate = given;
+    event_rate = factor > 0.0 ? factor : 0.0;
+    const double thinning = draw_mode == JFGPU_DRAW_UNIT ? 0.0 + (bounding_rate - 0.0) * draws[0] : draws[0];
+    confirmed = !(event_rate <= thinning);
+    return JFGPU_STATUS_OK;
+}
+
 // _fill_lifting (event_handler_with_bounding_potential.py:170-220) and the lifting scheme, from the potential
 // derivatives cross[i * units + j] of the non-active local units i against the target units j (the active
 // unit's velocity).  new_active as in composite_out_state.
@@ -451,17 +472,8 @@ __device__ inline int composite_out_state(const CompositeModel &m, int draw_mode
     }
     bool confirmed;
     if (given) {
-        // assert bounding_event_rate >= 0.0 (:243, composite_object_cell_veto_event_handler.py:150)
-        if (!(*given >= 0.0)) return JFGPU_STATUS_ASSERTION;
-        double factor = 0.0;
-        for (int j = 0; j < k; ++j) {
-            factor += pair[j];
-            target_factor[j] = 0.0 - pair[j];
-        }
-        bounding_rate = *given;
-        event_rate = factor > 0.0 ? factor : 0.0;
-        const double thinning = draw_mode == JFGPU_DRAW_UNIT ? 0.0 + (bounding_rate - 0.0) * draws[0] : draws[0];
-        confirmed = !(event_rate <= thinning);
+        JF_TRY(composite_given_thinning(m, draw_mode, *given, pair, draws, target_factor, bounding_rate, event_rate,
+                                        confirmed));
     } else {
         confirmed = composite_thinning(m, draw_mode, bound, pair, draws, target_factor, bounding_rate, event_rate);
     }

@@ -100,6 +100,15 @@ std::vector<double> fourier_table(int fc, double alpha, double length);
 MIC make_mic(int fc, int pc, double alpha, double length, const double *fourier);
 // the real-space images and Fourier rows of the merged-image sum, in the reference's order
 void merged_image_terms(int fc, int pc, std::vector<int4> &images, std::vector<int4> &rows);
+// exact float bounds of the cells along one axis (cuboid_cells.py:115-131)
+void cell_bounds(double length, int m, std::vector<double> &lo, std::vector<double> &hi);
+// Walker's alias table on the host in the reference's order (walker.py:53-103)
+struct HostWalker {
+    std::vector<int32_t> first_item, second_item;
+    std::vector<double> first_rate;
+    double total_rate = 0.0, mean_rate = 0.0;
+};
+int walker_build(const std::vector<int> &items, const std::vector<double> &rates, HostWalker &w);
 // Lennard-Jones and displaced-even-power parameters as the reference's constructors derive them
 MH make_lj(double prefactor, double sigma);
 MH make_displaced(double r0, int power, double prefactor);

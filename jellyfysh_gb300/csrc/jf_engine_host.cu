@@ -40,12 +40,6 @@ cudaError_t launch_observe(const EngineView &view, long long first, long long co
 
 using namespace jf;
 
-struct HostWalker {
-    std::vector<int32_t> first_item, second_item;
-    std::vector<double> first_rate;
-    double total_rate = 0.0, mean_rate = 0.0;
-};
-
 // CUDA events around the launches: one event before the first launch on a stream, one after every launch, so
 // that a launch's time is the interval between its stream's previous event and its own
 class EventClock : public KernelClock {
@@ -159,6 +153,10 @@ double next_up(double x) {
 
 double next_down(double x) { return -next_up(-x); }
 
+}  // namespace
+
+namespace jf {
+
 void cell_bounds(double length, int m, std::vector<double> &lo, std::vector<double> &hi) {
     double side = length / m;
     lo.resize(m);
@@ -222,6 +220,10 @@ int walker_build(const std::vector<int> &items, const std::vector<double> &rates
     }
     return JFGPU_OK;
 }
+
+}  // namespace jf
+
+namespace {
 
 template <typename T>
 T *device_copy(JfgpuEngine *e, const std::vector<T> &host, cudaStream_t stream, int &error) {

@@ -21,6 +21,19 @@
 
 namespace jf {
 
+// the molecular cells of a water model: cuboid periodic cells of the root units, the nearby cells of the neighbour
+// layers and the molecular cell veto's bound and Walker tables
+struct WaterCells {
+    int m, ncells, n_off;
+    int offsets[32];          // the distinct residues of -layers .. layers modulo m, ascending
+    double side;              // L / m: position_to_cell is int(x / side) along every axis
+    double root_speed;        // the active root unit's velocity component: the speed times the leaf's weight 1/3
+    const double *cell_min;   // [m] exact lower cell bounds along an axis
+    const int16_t *tra;       // [m * m] translate along one axis, [a * m + b]
+    const double *bound_upper, *bound_lower;  // [ncells][3] upper and negated lower bounds
+    WalkerDev walker[2][3];   // [upper / lower][direction]
+};
+
 struct WaterModel {
     CompositeModel coulomb;  // units 3
     MH oh, hh, lj;
@@ -30,6 +43,8 @@ struct WaterModel {
     float margin32;       // rounding scale of FP32 separations, 16 L 2^-24
     int molecules, initial_active, initial_direction, mode;
     uint64_t seed;
+    int cells_on;         // the molecular cells are attached (jfgpu_water_set_cells)
+    WaterCells cells;
 };
 
 struct WaterArgs {
@@ -40,6 +55,12 @@ struct WaterArgs {
     JfgpuEvent *log;
     int64_t chains, first_chain, events;
     double stop_q, stop_r;  // stop time (inf: none)
+    // molecular cells
+    double *roots;          // [chains][molecules][3]
+    int32_t *occ;           // [chains][cells]
+    int32_t *sur;           // [chains][molecules]
+    JfgpuWaterCellState *cell_state;
+    double *root_log;       // [chains][events][3] or null
 };
 
 struct WaterCand {
@@ -102,9 +123,52 @@ __host__ inline size_t water_shared_bytes(int molecules) {
            (size_t)water_chunks_max(molecules) * sizeof(int);
 }
 
-// one candidate item of the event: the bounded displacement of the active unit against one unit of another molecule
-// (the Coulomb factor of the two molecules takes the smallest over the three), Lennard-Jones against another oxygen,
-// or a bond within the molecule.  Returns a status; the candidate is offered to best.
+// the bounded displacement of the active unit against unit j of molecule `other`: the Coulomb factor of the two
+// molecules takes the smallest over the three; as time_add does not decrease with the displacement, the smallest of
+// the three times is the same time (two_composite_object_summed_bounding_potential_event_handler.py:119-150)
+__device__ inline void coulomb_unit_exact(const WaterModel &w, const double *pos, const double *charge, uint64_t key,
+                                          uint64_t ev, int other, int j, int d, const double *pa, double ca,
+                                          double ts_q, double ts_r, WaterCand &best) {
+    const int b = 3 * other + j;
+    const double du = expovariate(draw(key, ev, kRngComposite, (uint32_t)b), w.beta);
+    double sep[3], p[3];
+    periodic_separation(pa, pos + 3 * b, w.length, sep);
+    permute3(sep, d, p);
+    const double value = ipcb_x_displacement(w.coulomb.bound_prefactor * ca * charge[b], p[0], p[1], p[2], du,
+                                             w.length) / w.speed;
+    water_offer(best, ts_q, ts_r, value, JFGPU_EV_COMPOSITE, other);
+}
+
+// pair item k of the active unit 3 m + t: Lennard-Jones against the oxygen of another molecule for k < n_lj, else
+// one of the two bonds within the molecule (two_leaf_unit_event_handler.py:98-138)
+__device__ inline int pair_item_exact(const WaterModel &w, const double *pos, uint64_t key, uint64_t ev, int k,
+                                      int n_lj, int m, int t, int d, const double *pa, double ts_q, double ts_r,
+                                      WaterCand &best) {
+    int b, kind;
+    const MH *h;
+    if (k < n_lj) {
+        const int other = k + (k >= m);
+        b = 3 * other + 1;
+        h = &w.lj;
+        kind = JFGPU_EV_PAIR;
+    } else {
+        const int u = (k - n_lj) + ((k - n_lj) >= t);  // the two other units of the molecule
+        b = 3 * m + u;
+        h = (t == 1 || u == 1) ? &w.oh : &w.hh;
+        kind = JFGPU_EV_BOND;
+    }
+    double sep[3];
+    periodic_separation(pa, pos + 3 * b, w.length, sep);
+    const double du = expovariate(draw(key, ev, kRngPair, (uint32_t)b), w.beta);
+    double value;
+    JF_TRY(mh_std_displacement(*h, d, sep, du, value));
+    water_offer(best, ts_q, ts_r, value / w.speed, kind, b);
+    return JFGPU_STATUS_OK;
+}
+
+// one candidate item of the event: the bounded displacement of the active unit against one unit of another molecule,
+// Lennard-Jones against another oxygen, or a bond within the molecule.  Returns a status; the candidate is offered
+// to best.
 __device__ inline int water_item(const WaterModel &w, const double *pos, const double *charge, uint64_t key,
                                  uint64_t ev, int item, int m, int t, int d, const double *pa, double ca, double ts_q,
                                  double ts_r, WaterCand &best) {
@@ -113,45 +177,20 @@ __device__ inline int water_item(const WaterModel &w, const double *pos, const d
     // that a warp solves displacements of one charge sign (one branch of the inversion)
     const int group = ((M - 1) + 31) & ~31;
     const int n_coulomb = 3 * group, n_lj = t == 1 ? M - 1 : 0;
-    double sep[3];
     if (item < n_coulomb) {
         const int j = item / group;
         int other = item % group;
         if (other >= M - 1) return JFGPU_STATUS_OK;  // padding
         other += other >= m;
-        const int b = 3 * other + j;
-        const double du = expovariate(draw(key, ev, kRngComposite, (uint32_t)b), w.beta);
-        periodic_separation(pa, pos + 3 * b, w.length, sep);
-        double p[3];
-        permute3(sep, d, p);
-        const double value = ipcb_x_displacement(w.coulomb.bound_prefactor * ca * charge[b], p[0], p[1], p[2], du,
-                                                 w.length) / w.speed;
-        // the factor's candidate is the smallest of its three displacements; as time_add does not decrease with the
-        // displacement, the smallest of the three times is the same time
-        water_offer(best, ts_q, ts_r, value, JFGPU_EV_COMPOSITE, other);
+        coulomb_unit_exact(w, pos, charge, key, ev, other, j, d, pa, ca, ts_q, ts_r, best);
         return JFGPU_STATUS_OK;
     }
-    item -= n_coulomb;
-    int b, kind;
-    const MH *h;
-    if (item < n_lj) {
-        const int other = item + (item >= m);
-        b = 3 * other + 1;
-        h = &w.lj;
-        kind = JFGPU_EV_PAIR;
-    } else {
-        const int u = (item - n_lj) + ((item - n_lj) >= t);  // the two other units of the molecule
-        b = 3 * m + u;
-        h = (t == 1 || u == 1) ? &w.oh : &w.hh;
-        kind = JFGPU_EV_BOND;
-    }
-    periodic_separation(pa, pos + 3 * b, w.length, sep);
-    const double du = expovariate(draw(key, ev, kRngPair, (uint32_t)b), w.beta);
-    double value;
-    JF_TRY(mh_std_displacement(*h, d, sep, du, value));
-    water_offer(best, ts_q, ts_r, value / w.speed, kind, b);
-    return JFGPU_STATUS_OK;
+    return pair_item_exact(w, pos, key, ev, item - n_coulomb, n_lj, m, t, d, pa, ts_q, ts_r, best);
 }
+
+__device__ inline void coulomb_unit_screen(const WaterModel &w, const double *pos, const double *charge,
+                                           uint64_t key, uint64_t ev, int other, int j, int d, const double *pa,
+                                           double ca, float &time, float &error, bool &unsafe);
 
 // FP32 screen of a candidate item, in displacements over the speed: the Coulomb items solve the bound's inversion
 // in FP32 with an error bound (ipcb_x_displacement32), the Lennard-Jones items take the FP32 screen of the atomic
@@ -215,6 +254,14 @@ __device__ inline void water_screen(const WaterModel &w, const double *pos, cons
         return;
     }
     other += other >= m;
+    coulomb_unit_screen(w, pos, charge, key, ev, other, j, d, pa, ca, time, error, unsafe);
+}
+
+// FP32 screen of the bounded displacement of the active unit against unit j of molecule `other` (over the speed),
+// with its error bound; unsafe: the screen cannot decide
+__device__ inline void coulomb_unit_screen(const WaterModel &w, const double *pos, const double *charge,
+                                           uint64_t key, uint64_t ev, int other, int j, int d, const double *pa,
+                                           double ca, float &time, float &error, bool &unsafe) {
     const int b = 3 * other + j;
     // du = -log(1 - u) / beta of the FP64 draw u = n 2^-53 (uniform53): log1pf(-u) below u = 1/2 (u rounded to
     // FP32 moves -log(1 - u) by at most 2 units of 2^-24 relative there), logf of the exact 1 - u = (2^53 - n) 2^-53
@@ -536,12 +583,544 @@ __global__ void __launch_bounds__(256, 2) water_kernel(WaterArgs a) {
     if (threadIdx.x == 0) a.state[chain] = s;
 }
 
+// ---------------------------------------------------------------------------------------------------------------
+// Water with molecular cells
+// ---------------------------------------------------------------------------------------------------------------
+// position_to_cell of a root unit (cuboid_cells.py:190-211): int(x / side) along every axis
+__device__ inline int water_cell_of(const WaterCells &cl, const double *p, int &cell) {
+    const long long ix = (long long)(p[0] / cl.side), iy = (long long)(p[1] / cl.side),
+                    iz = (long long)(p[2] / cl.side);
+    const long long idx = ix + (long long)cl.m * iy + (long long)cl.m * cl.m * iz;
+    if (idx < 0 || idx >= cl.ncells) return JFGPU_STATUS_CELL_RANGE;
+    cell = (int)idx;
+    return JFGPU_STATUS_OK;
+}
+
+__device__ inline void water_cell_axes(const WaterCells &cl, int cell, int *a) {
+    a[0] = cell % cl.m;
+    a[1] = (cell / cl.m) % cl.m;
+    a[2] = cell / (cl.m * cl.m);
+}
+
+// SingleActiveCellOccupancy.update (single_active_cell_occupancy.py:149-203) with one occupant per cell: a new
+// active molecule returns the previous one to its cell (its occupant when the cell is empty, else a surplus
+// molecule of it) and leaves its own cell (as its occupant or as a surplus molecule of it); the same active molecule
+// only takes the cell of its root unit again
+__device__ inline int water_occupancy_update(const WaterCells &cl, JfgpuWaterCellState &cs, int32_t *occ,
+                                             int32_t *sur, const double *roots, int m) {
+    if (m != cs.occ_active) {
+        if (cs.occ_active >= 0) {
+            if (occ[cs.occ_cell] < 0)
+                occ[cs.occ_cell] = cs.occ_active;
+            else
+                sur[cs.occ_active] = cs.occ_cell;
+        }
+        JF_TRY(water_cell_of(cl, roots + 3 * m, cs.occ_cell));
+        cs.occ_active = m;
+        if (occ[cs.occ_cell] == m)
+            occ[cs.occ_cell] = -1;
+        else if (sur[m] == cs.occ_cell)
+            sur[m] = -1;
+        else
+            return JFGPU_STATUS_ASSERTION;  // list.remove of an identifier that is not there
+        return JFGPU_STATUS_OK;
+    }
+    return water_cell_of(cl, roots + 3 * m, cs.occ_cell);
+}
+
+// The single candidates of the active molecule in cell `cell`: the molecular cell veto
+// (abstracts/cell_veto_event_handler.py:200-238 with the charge factor of
+// DipoleMonteCarloEstimator.charge_correction_factor without target charges: the active unit's charge) and the
+// cell boundary of the active root unit at root (cell_boundary_event_handler.py:98-156).
+__device__ inline int water_single_candidates(const WaterModel &w, uint64_t key, uint64_t ev, int cell, int d,
+                                              double ca, const double *root, double ts_q, double ts_r,
+                                              WaterCand &single, int &veto_cell, double &veto_rate,
+                                              double &boundary) {
+    const WaterCells &cl = w.cells;
+    double charge_factor = ca;
+    int which = 0;
+    if (!(charge_factor > 0.0)) {
+        charge_factor *= -1.0;
+        which = 1;
+    }
+    const WalkerDev &wk = cl.walker[which][d];
+    const double total_rate = wk.total_rate * charge_factor;
+    const int k = (int)randbelow(draw(key, ev, kRngVetoChoice, 0), (uint32_t)wk.size);
+    const double u = wk.mean_rate * uniform53(draw(key, ev, kRngVetoUniform, 0));
+    const int rc = (u <= wk.first_rate[k]) ? wk.first_item[k] : wk.second_item[k];
+    veto_rate = (which == 0 ? cl.bound_upper[rc * 3 + d] : cl.bound_lower[rc * 3 + d]) * charge_factor;
+    if (!(veto_rate > 0.0)) return JFGPU_STATUS_ASSERTION;
+    int a[3], b[3];
+    water_cell_axes(cl, cell, a);
+    water_cell_axes(cl, rc, b);
+    veto_cell = cl.tra[a[0] * cl.m + b[0]] + cl.m * cl.tra[a[1] * cl.m + b[1]] +
+                cl.m * cl.m * cl.tra[a[2] * cl.m + b[2]];
+    const double dt = expovariate(draw(key, ev, kRngVetoTime, 0), w.beta) / (total_rate * w.speed);
+    single.q = INFINITY;
+    single.r = INFINITY;
+    single.kind = 1 << 30;
+    single.target = 1 << 30;
+    water_offer(single, ts_q, ts_r, dt, JFGPU_EV_CELL_VETO, -1);
+    boundary = cl.cell_min[a[d] + 1 == cl.m ? 0 : a[d] + 1];
+    double sep = boundary - root[d];
+    if (sep < 0.0) sep = sep + w.length;
+    water_offer(single, ts_q, ts_r, sep / cl.root_speed, JFGPU_EV_BOUNDARY, -1);
+    return JFGPU_STATUS_OK;
+}
+
+__device__ inline void block_reduce_cand(WaterCand &best, WaterCand *warp_slots, int lane, int warp, int warps) {
+    for (int offset = 16; offset > 0; offset >>= 1) shuffle_better(best, offset);
+    if (lane == 0) warp_slots[warp] = best;
+}
+
+// One block of `warps` warps advances one chain of water with molecular cells.  Per event: thread 0 updates the
+// occupancy and takes the single candidates (cell veto, cell boundary); the block lists the target molecules (the
+// occupants of the nearby cells and the surplus molecules) in shared memory; the candidate items are the three units
+// of every target (the summed-bounding Coulomb factor), and, unless the bond and Lennard-Jones candidates are still
+// alive from before a cell-boundary event, Lennard-Jones against every other oxygen and the two bonds.  The pair
+// items are always solved in FP64 (their earliest is kept for the events after a cell boundary); in the mixed mode
+// the Coulomb items are screened in FP32 against the smallest time some candidate surely reaches, and only the
+// listed ones are solved in FP64.  The out-state of a Coulomb factor or of a cell veto with a target shares the
+// merged-image sums among the warps as the all-pairs kernel does.  The committed active leaf and root unit are
+// time-sliced from the in-state of the winner: the current one, or for a bond or Lennard-Jones event the copies its
+// candidate took when it was created.
+__global__ void __launch_bounds__(256, 2) water_cells_kernel(WaterArgs a) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, warps = blockDim.x >> 5;
+    const int64_t chain = blockIdx.x;
+    if (chain >= a.chains) return;  // whole blocks
+    const WaterModel &w = a.w;
+    const WaterCells &cl = w.cells;
+    const int M = w.molecules;
+    const uint64_t key = chain_key(w.seed, (uint64_t)(a.first_chain + chain));
+    double *pos = a.positions + (size_t)chain * 9 * M;
+    double *roots = a.roots + (size_t)chain * 3 * M;
+    int32_t *occ = a.occ + (size_t)chain * cl.ncells;
+    int32_t *sur = a.sur + (size_t)chain * M;
+    const double *charge = a.charges;
+    __shared__ JfgpuWaterState s;
+    __shared__ JfgpuWaterCellState cs;
+    __shared__ WaterCand warp_best[kMaxWarps], warp_pair[kMaxWarps];
+    __shared__ float warp_upper[kMaxWarps];
+    extern __shared__ float dynamic[];
+    float *lower = dynamic;
+    int *list = reinterpret_cast<int *>(dynamic + water_items_max(M));
+    int *chunk_count = list + water_items_max(M);
+    int *targets = chunk_count + water_chunks_max(M);
+    __shared__ int status, n_targets, veto_cell;
+    __shared__ WaterCand single;
+    __shared__ double veto_rate, boundary;
+    __shared__ double bound[3], pair[3], cross[9];
+    __shared__ float pair32[3], error32[3];
+    if (threadIdx.x == 0) {
+        s = a.state[chain];
+        cs = a.cell_state[chain];
+        s.stopped = 0;
+        status = JFGPU_STATUS_OK;
+    }
+    __syncthreads();
+    for (int64_t step = 0; step < a.events && s.status == JFGPU_STATUS_OK; ++step) {
+        const int act = s.active, m = act / 3, t = act % 3, d = s.direction;
+        const uint64_t ev = (uint64_t)s.events;
+        const double ts_q = s.time_q, ts_r = s.time_r;
+        const double ca = charge[act];
+        if (threadIdx.x == 0) {
+            n_targets = 0;
+            int st = water_occupancy_update(cl, cs, occ, sur, roots, m);
+            if (!st)
+                st = water_single_candidates(w, key, ev, cs.occ_cell, d, ca, roots + 3 * m, ts_q, ts_r, single,
+                                             veto_cell, veto_rate, boundary);
+            status = st;
+        }
+        __syncthreads();
+        if (status != JFGPU_STATUS_OK) {
+            if (threadIdx.x == 0) s.status = status;
+            break;
+        }
+        // the target molecules: the occupants of the nearby cells (ExcludedCellsTagger), the surplus molecules
+        {
+            int ax[3];
+            water_cell_axes(cl, cs.occ_cell, ax);
+            const int n_near = cl.n_off * cl.n_off * cl.n_off;
+            for (int k = threadIdx.x; k < n_near + M; k += blockDim.x) {
+                int other = -1;
+                if (k < n_near) {
+                    const int ox = k % cl.n_off, oy = (k / cl.n_off) % cl.n_off, oz = k / (cl.n_off * cl.n_off);
+                    const int cell = (ax[0] + cl.offsets[ox]) % cl.m + cl.m * ((ax[1] + cl.offsets[oy]) % cl.m) +
+                                     cl.m * cl.m * ((ax[2] + cl.offsets[oz]) % cl.m);
+                    other = occ[cell];
+                } else if (sur[k - n_near] >= 0) {
+                    other = k - n_near;
+                }
+                if (other >= 0) targets[atomicAdd(&n_targets, 1)] = other;
+            }
+        }
+        __syncthreads();
+        const int nt = n_targets;
+        const bool new_pairs = !cs.pairs_valid;
+        double pa[3], pr[3], pa0[3], pr0[3];
+        for (int c = 0; c < 3; ++c) {
+            pa[c] = pa0[c] = pos[3 * act + c];
+            pr[c] = pr0[c] = roots[3 * m + c];
+        }
+        WaterCand eoc;
+        eoc.q = s.eoc_q;
+        eoc.r = s.eoc_r;
+        eoc.kind = JFGPU_EV_END_OF_CHAIN;
+        eoc.target = s.eoc_new_active;
+        WaterCand best, pbest;
+        best.q = pbest.q = INFINITY;
+        best.r = pbest.r = INFINITY;
+        best.kind = pbest.kind = 1 << 30;
+        best.target = pbest.target = 1 << 30;
+        const int group = (nt + 31) & ~31, n_coulomb = 3 * group;
+        const int n_lj = new_pairs && t == 1 ? M - 1 : 0, n_pairs = new_pairs ? n_lj + 2 : 0;
+        const int items = n_coulomb + n_pairs;
+        const bool mixed = w.mode == JFGPU_MODE_MIXED;
+        int st = JFGPU_STATUS_OK, refined = nt * 3 + n_pairs;
+        // phase A: the pair items in FP64; the Coulomb items in FP64 (exact mode) or screened in FP32 (mixed mode:
+        // lower[item] = the earliest time the item may reach, -inf where the screen cannot decide)
+        float mine = INFINITY;
+        for (int item = threadIdx.x; item < items && !st; item += blockDim.x) {
+            if (item >= n_coulomb) {
+                st = pair_item_exact(w, pos, key, ev, item - n_coulomb, n_lj, m, t, d, pa, ts_q, ts_r, pbest);
+                continue;
+            }
+            const int j = item / group, k = item % group;
+            if (k >= nt) {
+                lower[item] = INFINITY;  // padding
+                continue;
+            }
+            if (mixed) {
+                float t32, e32;
+                bool unsafe = false;
+                coulomb_unit_screen(w, pos, charge, key, ev, targets[k], j, d, pa, ca, t32, e32, unsafe);
+                lower[item] = unsafe ? -INFINITY : __fsub_rd(t32, e32);
+                if (!unsafe) mine = fminf(mine, __fadd_ru(t32, e32));
+            } else {
+                coulomb_unit_exact(w, pos, charge, key, ev, targets[k], j, d, pa, ca, ts_q, ts_r, best);
+            }
+        }
+        if (st) status = st;  // any failing thread; all stop after the barrier
+        block_reduce_cand(pbest, warp_pair, lane, warp, warps);
+        if (mixed) {
+            for (int offset = 16; offset > 0; offset >>= 1) mine = fminf(mine, __shfl_xor_sync(kFull, mine, offset));
+            if (lane == 0) warp_upper[warp] = mine;
+        }
+        __syncthreads();
+        if (status != JFGPU_STATUS_OK) {
+            if (threadIdx.x == 0) s.status = status;
+            break;
+        }
+        pbest = warp_pair[0];
+        for (int k = 1; k < warps; ++k)
+            if (water_better(warp_pair[k], pbest)) pbest = warp_pair[k];
+        WaterCand pcand = pbest;
+        if (!new_pairs) {
+            pcand.q = cs.pair_q;
+            pcand.r = cs.pair_r;
+            pcand.kind = cs.pair_kind;
+            pcand.target = cs.pair_target;
+        }
+        if (mixed) {
+            // the bound: the smallest time that some candidate surely reaches (a screened time plus its error bound,
+            // the pair candidate, the single candidates, the end of chain), rounded upwards
+            float bound_time = __double2float_ru(time_sub(eoc.q, eoc.r, ts_q, ts_r));
+            bound_time = fminf(bound_time, __double2float_ru(time_sub(pcand.q, pcand.r, ts_q, ts_r)));
+            bound_time = fminf(bound_time, __double2float_ru(time_sub(single.q, single.r, ts_q, ts_r)));
+            for (int k = 0; k < warps; ++k) bound_time = fminf(bound_time, warp_upper[k]);
+            // the Coulomb items that may come first, listed in item order (by unit type, so that a warp of the FP64
+            // pass follows one charge sign): the taken count of every chunk of 32 items, then every warp writes the
+            // items of its chunks at their offsets
+            const int chunks = n_coulomb >> 5;
+            for (int c = warp; c < chunks; c += warps) {
+                const unsigned votes = __ballot_sync(kFull, lower[32 * c + lane] <= bound_time);
+                if (lane == 0) chunk_count[c] = __popc(votes);
+            }
+            __syncthreads();
+            int taken = 0;
+            for (int c = 0; c < chunks; ++c) {
+                if (c % warps == warp) {
+                    const bool take = lower[32 * c + lane] <= bound_time;
+                    const unsigned votes = __ballot_sync(kFull, take);
+                    if (take) list[taken + __popc(votes & ((1u << lane) - 1u))] = 32 * c + lane;
+                }
+                taken += chunk_count[c];
+            }
+            __syncthreads();
+            // phase B: the FP64 solve of the listed items
+            for (int v = threadIdx.x; v < taken; v += blockDim.x) {
+                const int item = list[v];
+                if (item % group >= nt) continue;  // padding (listed only under an infinite bound)
+                coulomb_unit_exact(w, pos, charge, key, ev, targets[item % group], item / group, d, pa, ca, ts_q,
+                                   ts_r, best);
+            }
+            refined = taken + n_pairs;
+        }
+        block_reduce_cand(best, warp_best, lane, warp, warps);
+        __syncthreads();
+        // every thread takes the winner: the warps' best, the pair candidate, the single candidates, the end of
+        // chain, the stop time (which wins ties)
+        best = warp_best[0];
+        for (int k = 1; k < warps; ++k)
+            if (water_better(warp_best[k], best)) best = warp_best[k];
+        if (water_better(pcand, best)) best = pcand;
+        if (water_better(single, best)) best = single;
+        if (water_better(eoc, best)) best = eoc;
+        if (!isinf(a.stop_q) && !time_lt(best.q, best.r, a.stop_q, a.stop_r)) {
+            // the end of the run: the active leaf and root unit time-sliced to the stop time, no event; the pair
+            // candidates are created anew by the next call
+            if (threadIdx.x == 0) {
+                const double dt = time_sub(a.stop_q, a.stop_r, ts_q, ts_r);
+                for (int c = 0; c < 3; ++c) {
+                    pos[3 * act + c] = py_mod_near(pa[c] + (c == d ? w.speed : 0.0) * dt, w.length);
+                    roots[3 * m + c] = py_mod_near(pr[c] + (c == d ? cl.root_speed : 0.0) * dt, w.length);
+                }
+                s.time_q = a.stop_q;
+                s.time_r = a.stop_r;
+                s.stopped = 1;
+                cs.pairs_valid = 0;
+            }
+            break;
+        }
+        // commit: the active leaf and root unit time-sliced from the winner's in-state
+        {
+            const bool stale = (best.kind == JFGPU_EV_BOND || best.kind == JFGPU_EV_PAIR) && !new_pairs;
+            const double from_q = stale ? cs.snap_q : ts_q, from_r = stale ? cs.snap_r : ts_r;
+            const double dt = time_sub(best.q, best.r, from_q, from_r);
+            for (int c = 0; c < 3; ++c) {
+                const double leaf = stale ? cs.snap_leaf[c] : pa0[c], root = stale ? cs.snap_root[c] : pr0[c];
+                pa[c] = py_mod_near(leaf + (c == d ? w.speed : 0.0) * dt, w.length);
+                pr[c] = py_mod_near(root + (c == d ? cl.root_speed : 0.0) * dt, w.length);
+            }
+        }
+        int accepted = 1;
+        int other = -1;
+        if (best.kind == JFGPU_EV_COMPOSITE) other = best.target;
+        if (best.kind == JFGPU_EV_CELL_VETO) {
+            other = occ[veto_cell];  // the occupant of the sampled cell (Mediator.get_arguments_cell_veto_event_handler)
+            accepted = 0;
+        }
+        if (other >= 0) {
+            const bool veto = best.kind == JFGPU_EV_CELL_VETO;
+            const double *locals = pos + 9 * m, *targets_pos = pos + 9 * other;
+            double draws[3];
+            draws[0] = uniform53(draw(key, ev, kRngThin, 0));
+            draws[1] = uniform53(draw(key, ev, kRngLift, 0));
+            draws[2] = draws[1];
+            if (mixed) {
+                for (int j = warp; j < 3; j += warps) {
+                    double sep[3], p[3];
+                    periodic_separation(pa, targets_pos + 3 * j, w.length, sep);
+                    permute3(sep, d, p);
+                    float value, value_error;
+                    mic_x_warp32(w.coulomb, (float)p[0], (float)p[1], (float)p[2], lane, value, value_error);
+                    if (lane == 0) {
+                        const double scale = w.coulomb.coulomb_prefactor * ca * charge[3 * other + j] * w.speed;
+                        pair32[j] = (float)scale * value;
+                        error32[j] = fabsf((float)scale) * value_error + fabsf((float)scale * value) * 2.4e-7f;
+                        // the summed bound of a Coulomb factor: its bounding derivative pp s_x / |s|^3 times the
+                        // speed, within about 14 ulp, taken as 32 (a lower bound)
+                        const float x = (float)p[0], y = (float)p[1], z = (float)p[2];
+                        const float r2 = x * x + y * y + z * z;
+                        const float b = (float)(w.coulomb.bound_prefactor * ca * charge[3 * other + j]) * x /
+                                        (r2 * sqrtf(r2)) * w.speed32;
+                        bound[j] = (double)(b - fabsf(b) * 32.f * 0x1p-24f);
+                    }
+                }
+                __syncthreads();
+            }
+            // 0 rejected, 1 thinning in FP64, 2 accepted; every thread takes the same decision
+            int decision = 1;
+            if (mixed) {
+                // max(0, factor) <= uniform(0, bounding rate) is certain when the factor's upper bound stays below
+                // the draw times a lower bound of the bounding rate
+                double bounding = veto_rate;
+                if (!veto) {
+                    float sum = 0.f;
+                    for (int j = 0; j < 3; ++j) sum += fmaxf((float)bound[j], 0.f);
+                    bounding = (double)sum;
+                }
+                const double thinning_lower = bounding * draws[0] * (1.0 - 0x1p-20);
+                const float factor = pair32[0] + pair32[1] + pair32[2];
+                const float error = error32[0] + error32[1] + error32[2] + fabsf(factor) * 2.4e-7f;
+                if ((double)factor + (double)error < thinning_lower) decision = 0;  // rejection certain
+                __syncthreads();  // every thread has read the FP32 sums before bound[] is refilled
+            }
+            if (threadIdx.x == 0) {
+                if (!veto) ++s.composite_events;
+                if (decision) ++s.thinning_exact;
+            }
+            if (decision) {
+                if (!veto && threadIdx.x < 3) {
+                    double sep[3];
+                    periodic_separation(pa, targets_pos + 3 * threadIdx.x, w.length, sep);
+                    bound[threadIdx.x] =
+                        bound_derivative(w.coulomb, d, w.speed, sep, ca, charge[3 * other + threadIdx.x]);
+                }
+                for (int j = warp; j < 3; j += warps) {
+                    double sep[3];
+                    periodic_separation(pa, targets_pos + 3 * j, w.length, sep);
+                    const double value =
+                        coulomb_derivative_warp(w.coulomb, d, w.speed, sep, ca, charge[3 * other + j], lane);
+                    if (lane == 0) pair[j] = value;
+                }
+                __syncthreads();
+                double target_factor[3], bounding_rate, event_rate;
+                bool confirmed = false;
+                if (veto) {
+                    if (composite_given_thinning(w.coulomb, JFGPU_DRAW_UNIT, veto_rate, pair, draws, target_factor,
+                                                 bounding_rate, event_rate, confirmed))
+                        confirmed = false;  // the rate was checked positive when the candidate was made
+                } else {
+                    confirmed = composite_thinning(w.coulomb, JFGPU_DRAW_UNIT, bound, pair, draws, target_factor,
+                                                   bounding_rate, event_rate);
+                }
+                decision = confirmed ? 2 : 0;
+            }
+            if (decision == 2) {
+                // the derivatives of the two other local units against the three target units
+                for (int k = warp; k < 6; k += warps) {
+                    const int i = k / 3 < t ? k / 3 : k / 3 + 1, j = k % 3;
+                    double sep[3];
+                    periodic_separation(locals + 3 * i, targets_pos + 3 * j, w.length, sep);
+                    const double value = coulomb_derivative_warp(w.coulomb, d, w.speed, sep, charge[3 * m + i],
+                                                                 charge[3 * other + j], lane);
+                    if (lane == 0) cross[i * 3 + j] = value;
+                }
+                __syncthreads();
+                if (threadIdx.x == 0) {
+                    double target_factor[3], bounding_rate, event_rate, local_cross[9];
+                    bool confirmed = true;
+                    if (veto)
+                        composite_given_thinning(w.coulomb, JFGPU_DRAW_UNIT, veto_rate, pair, draws, target_factor,
+                                                 bounding_rate, event_rate, confirmed);
+                    else
+                        composite_thinning(w.coulomb, JFGPU_DRAW_UNIT, bound, pair, draws, target_factor,
+                                           bounding_rate, event_rate);
+                    for (int k = 0; k < 9; ++k) local_cross[k] = cross[k];
+                    int new_active = -1;
+                    const int lst = composite_lifting(w.coulomb, JFGPU_DRAW_UNIT, t, m < other, event_rate,
+                                                      target_factor, local_cross, draws, new_active);
+                    if (lst) {
+                        s.status = lst;
+                    } else {
+                        ++s.composite_accepted;
+                        s.active = new_active < 3 ? 3 * m + new_active : 3 * other + (new_active - 3);
+                    }
+                }
+            }
+            accepted = decision == 2;
+        } else if (threadIdx.x == 0) {
+            if (best.kind == JFGPU_EV_BOND || best.kind == JFGPU_EV_PAIR) {
+                s.active = best.target;
+                if (best.kind == JFGPU_EV_BOND) ++s.bond_events; else ++s.lj_events;
+            } else if (best.kind == JFGPU_EV_END_OF_CHAIN) {
+                s.direction = (s.direction + 1) % 3;
+                s.active = best.target;
+                time_add(best.q, best.r, time_sub(best.q, best.r, best.q, best.r) + w.chain_time, s.eoc_q, s.eoc_r);
+                s.eoc_new_active = water_new_active(w, key, ev + 1);
+                ++s.eoc_events;
+            } else if (best.kind == JFGPU_EV_BOUNDARY) {
+                accepted = 0;
+                ++cs.boundary_events;
+            } else if (best.kind != JFGPU_EV_CELL_VETO) {
+                s.status = JFGPU_STATUS_ASSERTION;
+            }
+        }
+        if (threadIdx.x == 0) {
+            if (best.kind == JFGPU_EV_BOUNDARY) pr[d] = boundary;
+            if (best.kind == JFGPU_EV_CELL_VETO) {
+                ++cs.veto_events;
+                if (other >= 0) ++cs.veto_targets;
+            }
+            if (new_pairs) {
+                // the pair candidates created with this event and the in-state copies they hold
+                cs.pair_q = pbest.q;
+                cs.pair_r = pbest.r;
+                cs.pair_kind = pbest.kind;
+                cs.pair_target = pbest.target;
+                for (int c = 0; c < 3; ++c) {
+                    cs.snap_leaf[c] = pa0[c];
+                    cs.snap_root[c] = pr0[c];
+                }
+                cs.snap_q = ts_q;
+                cs.snap_r = ts_r;
+            }
+            // the cell boundary trashes only the cell-based factors; every other event the pair candidates too
+            cs.pairs_valid = best.kind == JFGPU_EV_BOUNDARY;
+            for (int c = 0; c < 3; ++c) {
+                pos[3 * act + c] = pa[c];
+                roots[3 * m + c] = pr[c];
+            }
+            s.time_q = best.q;
+            s.time_r = best.r;
+            if (a.log) {
+                JfgpuEvent e;
+                e.kind = best.kind;
+                e.moved = act;
+                e.target = best.kind == JFGPU_EV_CELL_VETO ? other : (best.kind == JFGPU_EV_BOUNDARY ? -1 : best.target);
+                e.new_active = s.active;
+                e.new_direction = s.direction;
+                e.accepted = accepted;
+                e.time_q = best.q;
+                e.time_r = best.r;
+                e.x = pa[0];
+                e.y = pa[1];
+                e.z = pa[2];
+                a.log[chain * a.events + step] = e;
+            }
+            if (a.root_log)
+                for (int c = 0; c < 3; ++c) a.root_log[(chain * a.events + step) * 3 + c] = pr[c];
+            ++s.events;
+            s.refined_items += refined;
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        a.state[chain] = s;
+        a.cell_state[chain] = cs;
+    }
+}
+
+// the occupancy from the roots (SingleActiveCellOccupancy.initialize, single_active_cell_occupancy.py:95-121: the
+// root nodes in order, the first molecule of a cell its occupant, the others surplus), a fresh cell state
+__global__ void water_cells_init_kernel(WaterModel w, JfgpuWaterCellBuffers b, int64_t chains) {
+    const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= chains) return;
+    const WaterCells &cl = w.cells;
+    const int M = w.molecules;
+    int32_t *occ = b.occupancy + (size_t)c * cl.ncells;
+    int32_t *sur = b.surplus + (size_t)c * M;
+    const double *roots = b.roots + (size_t)c * 3 * M;
+    JfgpuWaterCellState cs;
+    memset(&cs, 0, sizeof(cs));
+    cs.pair_q = cs.pair_r = INFINITY;
+    cs.pair_kind = cs.pair_target = 1 << 30;
+    cs.occ_active = -1;
+    cs.occ_cell = -1;
+    for (int k = 0; k < cl.ncells; ++k) occ[k] = -1;
+    for (int i = 0; i < M; ++i) {
+        sur[i] = -1;
+        int cell;
+        if (water_cell_of(cl, roots + 3 * i, cell)) {
+            cs.reserved = JFGPU_STATUS_CELL_RANGE;
+            continue;
+        }
+        if (occ[cell] < 0)
+            occ[cell] = i;
+        else
+            sur[i] = cell;
+    }
+    b.cell_state[c] = cs;
+}
+
 struct WaterHandle {
     WaterModel model;
     double *fourier = nullptr;
     float *fourier32 = nullptr;
     int4 *terms = nullptr;  // real-space images, then Fourier rows
     int device = -1;
+    std::vector<void *> cell_tables;  // device tables of the molecular cells
 };
 
 }  // namespace jf
@@ -646,6 +1225,7 @@ extern "C" int jfgpu_water_create(const JfgpuWaterDesc *desc, void **water) {
 extern "C" void jfgpu_water_destroy(void *water) {
     WaterHandle *h = static_cast<WaterHandle *>(water);
     if (!h) return;
+    for (void *p : h->cell_tables) cudaFree(p);
     if (h->fourier) cudaFree(h->fourier);
     if (h->fourier32) cudaFree(h->fourier32);
     if (h->terms) cudaFree(h->terms);
@@ -674,6 +1254,7 @@ extern "C" int jfgpu_water_run(void *water, double *positions, const double *cha
     if (!positions || !charges || !state) return JFGPU_ERROR_ARGUMENT;
     const int warps = warps_per_block ? warps_per_block : 3;
     WaterArgs a;
+    memset(&a, 0, sizeof(a));
     a.w = h->model;
     a.positions = positions;
     a.charges = charges;
@@ -689,5 +1270,145 @@ extern "C" int jfgpu_water_run(void *water, double *positions, const double *cha
         cudaFuncSetAttribute(water_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shared) != cudaSuccess)
         return JFGPU_ERROR_CUDA;
     water_kernel<<<(unsigned)chains, 32 * warps, shared, static_cast<cudaStream_t>(stream)>>>(a);
+    return cudaGetLastError() == cudaSuccess ? JFGPU_OK : JFGPU_ERROR_CUDA;
+}
+
+namespace {
+
+template <typename T>
+const T *water_table(WaterHandle *h, const std::vector<T> &host, int &error) {
+    void *ptr = nullptr;
+    const size_t bytes = sizeof(T) * (host.empty() ? 1 : host.size());
+    if (cudaMalloc(&ptr, bytes) != cudaSuccess) {
+        error = JFGPU_ERROR_ALLOCATION;
+        return nullptr;
+    }
+    h->cell_tables.push_back(ptr);
+    if (!host.empty() && cudaMemcpy(ptr, host.data(), sizeof(T) * host.size(), cudaMemcpyHostToDevice) != cudaSuccess)
+        error = JFGPU_ERROR_CUDA;
+    return static_cast<const T *>(ptr);
+}
+
+}  // namespace
+
+extern "C" int jfgpu_water_set_cells(void *water, int32_t cells_per_side, int32_t neighbor_layers,
+                                     const double *bounds_upper, const double *bounds_lower) {
+    WaterHandle *h = static_cast<WaterHandle *>(water);
+    if (!h || cells_per_side < 1 || cells_per_side > 32 || neighbor_layers < 0 || !bounds_upper || !bounds_lower)
+        return JFGPU_ERROR_ARGUMENT;
+    WaterModel &w = h->model;
+    WaterCells cl;
+    memset(&cl, 0, sizeof(cl));
+    const int m = cells_per_side;
+    cl.m = m;
+    cl.ncells = m * m * m;
+    cl.side = w.length / m;
+    cl.root_speed = w.speed * (1.0 / 3.0);  // the leaf velocity times its weight 1 / len(children) in the molecule
+    // the residues of the neighbour-layer offsets (cuboid_periodic_cells.py:74-100), ascending
+    std::vector<char> near(m, 0);
+    for (int o = -neighbor_layers; o <= neighbor_layers; ++o) near[((o % m) + m) % m] = 1;
+    for (int r = 0; r < m; ++r)
+        if (near[r]) cl.offsets[cl.n_off++] = r;
+    std::vector<double> lo, hi;
+    cell_bounds(w.length, m, lo, hi);
+    std::vector<int16_t> tra((size_t)m * m);
+    for (int a = 0; a < m; ++a)
+        for (int b = 0; b < m; ++b) {
+            const double center = (hi[a] + lo[a]) / 2.0;
+            tra[(size_t)a * m + b] = (int16_t)(long long)(py_mod(center + lo[b], w.length) / cl.side);
+        }
+    auto nearby_zero = [&](int cell) {
+        return near[cell % m] && near[(cell / m) % m] && near[cell / (m * m)];
+    };
+    std::vector<double> upper(bounds_upper, bounds_upper + 3 * (size_t)cl.ncells);
+    std::vector<double> lower(bounds_lower, bounds_lower + 3 * (size_t)cl.ncells);
+    int error = JFGPU_OK;
+    HostWalker walkers[2][3];
+    for (int which = 0; which < 2; ++which)
+        for (int d = 0; d < 3; ++d) {
+            // the cells that are not nearby the zero cell, in the order of yield_cells, with max(bound, 0.0)
+            // (cell_veto_event_handler.py:149-160)
+            std::vector<int> items;
+            std::vector<double> rates;
+            for (int cell = 0; cell < cl.ncells; ++cell) {
+                if (nearby_zero(cell)) continue;
+                const double r = (which == 0 ? upper : lower)[3 * (size_t)cell + d];
+                if (std::isnan(r)) return JFGPU_ERROR_TABLE;  // a far cell without a bound
+                items.push_back(cell);
+                rates.push_back(r > 0.0 ? r : 0.0);
+            }
+            const int st = walker_build(items, rates, walkers[which][d]);
+            if (st) return st;
+        }
+    cl.cell_min = water_table(h, lo, error);
+    cl.tra = water_table(h, tra, error);
+    cl.bound_upper = water_table(h, upper, error);
+    cl.bound_lower = water_table(h, lower, error);
+    for (int which = 0; which < 2; ++which)
+        for (int d = 0; d < 3; ++d) {
+            const HostWalker &hw = walkers[which][d];
+            WalkerDev &wd = cl.walker[which][d];
+            wd.first_item = water_table(h, hw.first_item, error);
+            wd.second_item = water_table(h, hw.second_item, error);
+            wd.first_rate = water_table(h, hw.first_rate, error);
+            wd.size = (int32_t)hw.first_item.size();
+            wd.total_rate = hw.total_rate;
+            wd.mean_rate = hw.mean_rate;
+        }
+    if (error) return error;
+    w.cells = cl;
+    w.cells_on = 1;
+    return JFGPU_OK;
+}
+
+extern "C" int jfgpu_water_cells_init(void *water, const JfgpuWaterCellBuffers *buffers, int64_t chains,
+                                      void *stream) {
+    WaterHandle *h = static_cast<WaterHandle *>(water);
+    if (!h || !buffers || chains < 0 || !h->model.cells_on) return JFGPU_ERROR_ARGUMENT;
+    if (chains == 0) return JFGPU_OK;
+    if (!buffers->roots || !buffers->occupancy || !buffers->surplus || !buffers->cell_state)
+        return JFGPU_ERROR_ARGUMENT;
+    const int threads = 128;
+    water_cells_init_kernel<<<(unsigned)((chains + threads - 1) / threads), threads, 0,
+                              static_cast<cudaStream_t>(stream)>>>(h->model, *buffers, chains);
+    return cudaGetLastError() == cudaSuccess ? JFGPU_OK : JFGPU_ERROR_CUDA;
+}
+
+extern "C" int jfgpu_water_cells_run(void *water, double *positions, const double *charges, JfgpuWaterState *state,
+                                     const JfgpuWaterCellBuffers *buffers, int64_t chains, int64_t first_chain,
+                                     int64_t events, double stop_q, double stop_r, JfgpuEvent *log,
+                                     int32_t warps_per_block, void *stream) {
+    WaterHandle *h = static_cast<WaterHandle *>(water);
+    if (!h || !buffers || chains < 0 || first_chain < 0 || events < 0 || warps_per_block < 0 || warps_per_block > 8 ||
+        !h->model.cells_on)
+        return JFGPU_ERROR_ARGUMENT;
+    if (chains == 0 || events == 0) return JFGPU_OK;
+    if (!positions || !charges || !state || !buffers->roots || !buffers->occupancy || !buffers->surplus ||
+        !buffers->cell_state)
+        return JFGPU_ERROR_ARGUMENT;
+    const int warps = warps_per_block ? warps_per_block : 3;
+    WaterArgs a;
+    memset(&a, 0, sizeof(a));
+    a.w = h->model;
+    a.positions = positions;
+    a.charges = charges;
+    a.state = state;
+    a.log = log;
+    a.chains = chains;
+    a.first_chain = first_chain;
+    a.events = events;
+    a.stop_q = stop_q;
+    a.stop_r = stop_r;
+    a.roots = buffers->roots;
+    a.occ = buffers->occupancy;
+    a.sur = buffers->surplus;
+    a.cell_state = buffers->cell_state;
+    a.root_log = buffers->root_log;
+    const size_t shared = water_shared_bytes(h->model.molecules) + sizeof(int) * (size_t)h->model.molecules;
+    if (shared > 48 * 1024 &&
+        cudaFuncSetAttribute(water_cells_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shared) !=
+            cudaSuccess)
+        return JFGPU_ERROR_CUDA;
+    water_cells_kernel<<<(unsigned)chains, 32 * warps, shared, static_cast<cudaStream_t>(stream)>>>(a);
     return cudaGetLastError() == cudaSuccess ? JFGPU_OK : JFGPU_ERROR_CUDA;
 }

@@ -166,3 +166,23 @@ def water_lattice(molecules_per_side: int, system_length: float, oh_length: floa
     molecules = molecules_per_side ** 3
     charges = np.tile(np.array([charge_hydrogen, charge_oxygen, charge_hydrogen]), molecules)
     return _wrap(np.array(positions, dtype=np.float64), system_length), charges
+
+
+def water_roots(positions: np.ndarray, system_length: float) -> np.ndarray:
+    """The root unit of every water molecule (leaf units hydrogen, oxygen, hydrogen): the oxygen plus the mean of the
+    two O–H bond vectors taken in the minimum image, wrapped into [0, L).  Computed in Python floats component by
+    component, as the reference's water node creator places the barycentre
+    (``water_random_node_creator.py:83-99``: the oxygen is the centre minus the mean of the two bonds).
+    positions [3 M][3] -> roots [M][3]."""
+    length = float(system_length)
+    half = length / 2.0
+    atoms = np.asarray(positions, dtype=np.float64).reshape(-1, 3, 3).tolist()
+    roots = []
+    for hydrogen_one, oxygen, hydrogen_two in atoms:
+        centre = []
+        for d in range(3):
+            one = ((hydrogen_one[d] - oxygen[d]) + half) % length - half
+            two = ((hydrogen_two[d] - oxygen[d]) + half) % length - half
+            centre.append((oxygen[d] + (one + two) / 3.0) % length)
+        roots.append(centre)
+    return np.array(roots, dtype=np.float64).reshape(-1, 3)

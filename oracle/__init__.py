@@ -119,6 +119,13 @@ def lib() -> ctypes.CDLL:
         handle.jfo_water_run.restype = ctypes.c_int64
         handle.jfo_water_run.argtypes = [ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p, ctypes.POINTER(ctypes.c_int)]
         handle.jfo_water_positions.argtypes = [ctypes.c_void_p, _PD]
+        handle.jfo_water_run_roots.restype = ctypes.c_int64
+        handle.jfo_water_run_roots.argtypes = [ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p,
+                                               ctypes.POINTER(ctypes.c_int)]
+        handle.jfo_water_cells_create.restype = ctypes.c_void_p
+        handle.jfo_water_cells_create.argtypes = [ctypes.POINTER(JfoWaterSystem), ctypes.c_int, ctypes.c_int, _PD,
+                                                  _PD, _PD, _PD, _PD, ctypes.POINTER(ctypes.c_int)]
+        handle.jfo_water_roots.argtypes = [ctypes.c_void_p, _PD]
         handle.jfo_chain_create.restype = ctypes.c_void_p
         handle.jfo_chain_create.argtypes = [ctypes.POINTER(JfoSystem), _PD, _PD, ctypes.POINTER(ctypes.c_int)]
         handle.jfo_chain_destroy.argtypes = [ctypes.c_void_p]
@@ -483,16 +490,30 @@ def make_water_system(spec: dict, rng_key: int) -> JfoWaterSystem:
 
 
 class Water:
-    """One chain of flexible water molecules run by the oracle."""
+    """One chain of flexible water molecules run by the oracle.  With ``cells`` (cells_per_side, neighbor_layers,
+    roots [molecules][3], bounds_upper [cells][3], bounds_lower [cells][3]) the Coulomb interaction between molecules
+    goes through the molecular cells of the root units: nearby and surplus factors, the molecular cell veto with the
+    given bound tables and the cell-boundary events of the active root unit."""
 
-    def __init__(self, system: JfoWaterSystem, positions: np.ndarray, charges: np.ndarray):
+    def __init__(self, system: JfoWaterSystem, positions: np.ndarray, charges: np.ndarray, cells=None):
         self.system = system
         self._positions_in = np.ascontiguousarray(positions, dtype=np.float64).reshape(-1, 3)
         self._charges_in = np.ascontiguousarray(charges, dtype=np.float64)
         assert self._positions_in.shape[0] == 3 * system.molecules == len(self._charges_in)
         status = ctypes.c_int()
-        self._handle = lib().jfo_water_create(ctypes.byref(system), self._positions_in.ctypes.data_as(_PD),
-                                              self._charges_in.ctypes.data_as(_PD), ctypes.byref(status))
+        self.has_cells = cells is not None
+        if cells is None:
+            self._handle = lib().jfo_water_create(ctypes.byref(system), self._positions_in.ctypes.data_as(_PD),
+                                                  self._charges_in.ctypes.data_as(_PD), ctypes.byref(status))
+        else:
+            m, layers, roots, upper, lower = cells
+            self._cells_in = [np.ascontiguousarray(a, dtype=np.float64) for a in (roots, upper, lower)]
+            assert self._cells_in[0].shape == (system.molecules, 3)
+            assert self._cells_in[1].shape == self._cells_in[2].shape == (m ** 3, 3)
+            self._handle = lib().jfo_water_cells_create(
+                ctypes.byref(system), int(m), int(layers), self._positions_in.ctypes.data_as(_PD),
+                self._charges_in.ctypes.data_as(_PD), *[a.ctypes.data_as(_PD) for a in self._cells_in],
+                ctypes.byref(status))
         if not self._handle:
             raise OracleError("water creation failed: " + STATUS_NAMES.get(status.value, str(status.value)))
 
@@ -502,16 +523,25 @@ class Water:
             lib().jfo_water_destroy(handle)
             self._handle = None
 
-    def run(self, max_events: int, record: bool = True):
-        """Advance by ``max_events`` events; returns the event log (or the count without ``record``)."""
+    def run(self, max_events: int, record: bool = True, roots: bool = False):
+        """Advance by ``max_events`` events; returns the event log (or the count without ``record``); with ``roots``
+        also the root position of the moved unit's molecule after every event ([events][3], molecular cells)."""
         log_array = np.zeros(max_events if record else 0, dtype=EVENT_DTYPE)
+        root_array = np.zeros((max_events if roots else 0, 3), dtype=np.float64)
         status = ctypes.c_int()
-        done = lib().jfo_water_run(self._handle, max_events, log_array.ctypes.data if record else None,
-                                   ctypes.byref(status))
+        done = lib().jfo_water_run_roots(self._handle, max_events, log_array.ctypes.data if record else None,
+                                         root_array.ctypes.data if roots else None, ctypes.byref(status))
         if status.value != 0:
             raise OracleError("water run stopped after %d events: %s"
                               % (done, STATUS_NAMES.get(status.value, str(status.value))))
-        return log_array[:done] if record else done
+        result = log_array[:done] if record else done
+        return (result, root_array[:done]) if roots else result
+
+    def roots(self) -> np.ndarray:
+        """Root positions [molecules][3] (molecular cells)."""
+        out = np.zeros((self.system.molecules, 3), dtype=np.float64)
+        lib().jfo_water_roots(self._handle, out.ctypes.data_as(_PD))
+        return out
 
     def positions(self) -> np.ndarray:
         out = np.zeros((3 * self.system.molecules, 3), dtype=np.float64)

@@ -2031,6 +2031,16 @@ struct JfoWater {
     double eoc_q, eoc_r;    /* end-of-chain candidate */
     int eoc_new_active;
     int64_t event;
+    /* molecular cells (NULL: a Coulomb factor with every other molecule): the cell system, occupancy and cell-veto
+     * tables of the root units, whose positions the chain holds (cells->pos, [M][3]); cells->active is the active
+     * molecule */
+    JfoChain *cells;
+    double root_speed;      /* the active root unit's velocity component: the leaf's times its weight 1/3 */
+    /* the bond and Lennard-Jones candidates persist across molecular cell-boundary events: their earliest, and the
+     * active leaf and root unit as their in-state holds them (time stamp snap_q, snap_r) */
+    int pairs_valid;
+    Cand pair;
+    double snap_leaf[3], snap_root[3], snap_q, snap_r;
 };
 
 static int water_new_active(const JfoWater *w, uint64_t event) {
@@ -2077,6 +2087,7 @@ JfoWater *jfo_water_create(const JfoWaterSystem *system, const double *positions
 
 void jfo_water_destroy(JfoWater *w) {
     if (!w) return;
+    jfo_chain_destroy(w->cells);
     free(w->pos);
     free(w->charge);
     free(w);
@@ -2086,7 +2097,14 @@ static void water_separation(const JfoWater *w, int from, int to, double *s) {
     composite_separation(w->sys.system_length, &w->pos[3 * from], &w->pos[3 * to], s);
 }
 
+static int64_t water_cells_run(JfoWater *w, int64_t max_events, JfoEvent *log, double *root_log, int *status);
+
 int64_t jfo_water_run(JfoWater *w, int64_t max_events, JfoEvent *log, int *status) {
+    return jfo_water_run_roots(w, max_events, log, NULL, status);
+}
+
+int64_t jfo_water_run_roots(JfoWater *w, int64_t max_events, JfoEvent *log, double *root_log, int *status) {
+    if (w->cells) return water_cells_run(w, max_events, log, root_log, status);
     const JfoWaterSystem *s = &w->sys;
     const int M = s->molecules;
     int64_t done = 0;
@@ -2213,6 +2231,351 @@ int64_t jfo_water_run(JfoWater *w, int64_t max_events, JfoEvent *log, int *statu
         done++;
     }
     return done;
+}
+
+/* ======================================================================================
+ * Water with molecular cells: the Coulomb interaction of the active molecule by cells of root units
+ * (SingleActiveCellOccupancy with cell_level 1, single_active_cell_occupancy.py:95-203): the summed-bounding factor
+ * with the molecules of the nearby cells (ExcludedCellsTagger, excluded_cells_tagger.py:107-132) and with the
+ * surplus molecules (SurplusCellsTagger, surplus_cells_tagger.py:107-131), the molecular cell veto
+ * (CompositeObjectCellVetoEventHandler, composite_object_cell_veto_event_handler.py:110-162 with
+ * abstracts/cell_veto_event_handler.py:162-238) and the cell-boundary event of the active root unit
+ * (CellBoundaryEventHandler, cell_boundary_event_handler.py:98-173), whose tagger trashes and creates only the
+ * cell-based factors: the bond and Lennard-Jones candidates persist across it.
+ *
+ * The root unit of the active molecule moves with the active leaf unit's velocity times the leaf's weight 1/3
+ * (LeavesEventHandler._register_velocity_change_leaf_cnode / _commit_non_leaf_velocity_changes,
+ * event_handler/abstracts/abstracts.py:165-234) and carries the leaf's time stamp; every committed out-state holds
+ * it time-sliced to the event time (BasicEventHandler._time_slice_unit, abstracts.py:82-95).  A persistent bond or
+ * Lennard-Jones candidate commits the copies its in-state took when it was created (tree_state_handler.py:104-145),
+ * time-sliced from then to its event time, over the positions the cell-boundary events wrote meanwhile.
+ * ==================================================================================== */
+
+/* the bound tables of the molecular cell veto ([cells][3] upper, [cells][3] negated lower, as the estimator filled
+ * CellVetoEventHandler._derivative_bounds; NaN for the nearby cells) and their Walker tables
+ * (cell_veto_event_handler.py:134-160) */
+static int chain_install_bounds(JfoChain *c, const double *upper, const double *lower) {
+    int ncells = c->ncells;
+    c->bound_upper = (double *)calloc((size_t)ncells * 3, sizeof(double));
+    c->bound_lower = (double *)calloc((size_t)ncells * 3, sizeof(double));
+    int *items = (int *)malloc(sizeof(int) * ncells);
+    double *rates = (double *)malloc(sizeof(double) * ncells);
+    if (!c->bound_upper || !c->bound_lower || !items || !rates) {
+        free(items);
+        free(rates);
+        return JFO_ALLOC;
+    }
+    memcpy(c->bound_upper, upper, sizeof(double) * (size_t)ncells * 3);
+    memcpy(c->bound_lower, lower, sizeof(double) * (size_t)ncells * 3);
+    int st = JFO_OK;
+    for (int which = 0; which < 2 && !st; ++which)
+        for (int d = 0; d < 3 && !st; ++d) {
+            int n = 0;
+            for (int cell = 0; cell < ncells; ++cell) {
+                if (is_nearby(c, cell, 0)) continue;
+                double r = which == 0 ? c->bound_upper[cell * 3 + d] : c->bound_lower[cell * 3 + d];
+                if (isnan(r)) st = JFO_BAD_CONFIG;  /* a far cell without a bound */
+                items[n] = cell;
+                rates[n] = r > 0.0 ? r : 0.0;
+                ++n;
+            }
+            if (!st) st = walker_build(&c->walker[which][d], items, rates, n);
+            if (!st && which == 1 && d == 2) c->have_walker = 1;
+        }
+    free(items);
+    free(rates);
+    return st;
+}
+
+JfoWater *jfo_water_cells_create(const JfoWaterSystem *system, int cells_per_side, int neighbor_layers,
+                                 const double *positions, const double *charges, const double *roots,
+                                 const double *bounds_upper, const double *bounds_lower, int *status) {
+    JfoWater *w = jfo_water_create(system, positions, charges, status);
+    if (!w) return NULL;
+    JfoSystem cs;
+    memset(&cs, 0, sizeof(cs));
+    cs.n = system->molecules;
+    cs.system_length = system->system_length;
+    cs.cells_per_side = cells_per_side;
+    cs.neighbor_layers = neighbor_layers;
+    cs.max_occupants = 1;
+    cs.beta = system->beta;
+    cs.chain_time = system->chain_time;
+    cs.speed = system->speed;
+    cs.initial_direction = system->initial_direction;
+    cs.initial_active = system->initial_active / 3;
+    cs.potential = JFO_POT_HARD_SPHERE;
+    cs.far = JFO_FAR_NONE;
+    cs.rng_key = system->rng_key;
+    if (cells_per_side < 1 || neighbor_layers < 0) {
+        jfo_water_destroy(w);
+        *status = JFO_BAD_CONFIG;
+        return NULL;
+    }
+    /* the occupancy takes the root units in the order of the root nodes (initialize, :95-121) */
+    w->cells = jfo_chain_create(&cs, roots, NULL, status);
+    if (!w->cells) {
+        jfo_water_destroy(w);
+        return NULL;
+    }
+    *status = chain_install_bounds(w->cells, bounds_upper, bounds_lower);
+    if (*status) {
+        jfo_water_destroy(w);
+        return NULL;
+    }
+    w->root_speed = system->speed * (1.0 / 3.0);
+    w->pairs_valid = 0;
+    return w;
+}
+
+/* x_d <- (x_d + v_d (t - t_stamp)) % L along the direction of motion (the other components add 0.0) */
+static void water_slice(const JfoWater *w, double *p, double speed, double q, double r, double from_q, double from_r) {
+    double dt = jfo_time_sub(q, r, from_q, from_r);
+    for (int d = 0; d < 3; ++d) {
+        double v = d == w->direction ? speed : 0.0;
+        p[d] = jfo_py_mod(p[d] + v * dt, w->sys.system_length);
+    }
+}
+
+static int64_t water_cells_run(JfoWater *w, int64_t max_events, JfoEvent *log, double *root_log, int *status) {
+    const JfoWaterSystem *s = &w->sys;
+    JfoChain *c = w->cells;
+    const int M = s->molecules;
+    int64_t done = 0;
+    *status = JFO_OK;
+    while (done < max_events) {
+        const int a = w->active, m = a / 3, t = a % 3;
+        double *root = &c->pos[3 * m];
+        double velocity[3] = {0.0, 0.0, 0.0};
+        velocity[w->direction] = s->speed;
+        c->active = m;
+        c->direction = w->direction;
+        int st = occ_update(c);
+        if (st) {
+            *status = st;
+            return done;
+        }
+        Cand best;
+        best.q = INFINITY;
+        best.r = INFINITY;
+        best.kind = 1 << 30;
+        best.target = 1 << 30;
+        best.aux = -1;
+        best.rate = 0.0;
+        if (!w->pairs_valid) {
+            /* the bonds of the active unit's molecule and Lennard-Jones between oxygens (the factor-type-map taggers),
+             * created with the event: their in-state copies are the current active leaf and root unit */
+            Cand pair = best;
+            for (int u = 0; u < 3 && !st; ++u) {
+                if (u == t) continue;
+                const MH *bond = (t == 1 || u == 1) ? &w->oh : &w->hh;
+                int b = 3 * m + u;
+                double sep[3], dt;
+                water_separation(w, a, b, sep);
+                double du = jfo_expovariate(jfo_draw(s->rng_key, w->event, JFO_RNG_PAIR, b), s->beta);
+                st = mh_displacement(bond, velocity, sep, du, &dt);
+                if (!st) offer(&pair, w->ts_q, w->ts_r, dt, JFO_EV_BOND, b, -1, 0.0);
+            }
+            for (int other = 0; other < M && !st && t == 1; ++other) {
+                if (other == m) continue;
+                int b = 3 * other + 1;
+                double sep[3], dt;
+                water_separation(w, a, b, sep);
+                double du = jfo_expovariate(jfo_draw(s->rng_key, w->event, JFO_RNG_PAIR, b), s->beta);
+                st = mh_displacement(&w->lj, velocity, sep, du, &dt);
+                if (!st) offer(&pair, w->ts_q, w->ts_r, dt, JFO_EV_PAIR, b, -1, 0.0);
+            }
+            if (st) {
+                *status = st;
+                return done;
+            }
+            w->pair = pair;
+            w->pairs_valid = 1;
+            memcpy(w->snap_leaf, &w->pos[3 * a], sizeof(w->snap_leaf));
+            memcpy(w->snap_root, root, sizeof(w->snap_root));
+            w->snap_q = w->ts_q;
+            w->snap_r = w->ts_r;
+        }
+        if (cand_better(&w->pair, &best)) best = w->pair;
+        /* the summed-bounding Coulomb factor with the occupants of the nearby cells, then the surplus molecules */
+        int ax[3];
+        cell_axes(c, c->occ_cell, ax);
+        int n_off = 0, offsets[64];
+        for (int o = 0; o < c->m; ++o)
+            if (c->near_axis[o]) offsets[n_off++] = o;
+        for (int pass = 0; pass < 2 && !st; ++pass) {
+            int first = 0, last = pass == 0 ? n_off * n_off * n_off : c->ncells;
+            for (int k = first; k < last && !st; ++k) {
+                int cell, count, *list;
+                if (pass == 0) {
+                    int ox = k % n_off, oy = (k / n_off) % n_off, oz = k / (n_off * n_off);
+                    cell = (ax[0] + offsets[ox]) % c->m + c->m * ((ax[1] + offsets[oy]) % c->m) +
+                           c->m * c->m * ((ax[2] + offsets[oz]) % c->m);
+                    count = c->occ_count[cell];
+                    list = &c->occ[cell * c->cap];
+                } else {
+                    cell = k;
+                    count = c->sur_count[cell];
+                    list = &c->sur[(size_t)cell * c->sys.n];
+                }
+                for (int i = 0; i < count && !st; ++i) {
+                    int other = list[i];
+                    double du[3], dt;
+                    for (int j = 0; j < 3; ++j)
+                        du[j] = jfo_expovariate(
+                            jfo_draw(s->rng_key, w->event, JFO_RNG_COMPOSITE, (uint32_t)(3 * other + j)), s->beta);
+                    st = jfo_composite_event_time(3, s->ewald_alpha, s->fourier_cutoff, s->position_cutoff,
+                                                  s->coulomb_prefactor, s->bound_prefactor, s->system_length,
+                                                  velocity, &w->pos[3 * a], w->charge[a], &w->pos[9 * other],
+                                                  &w->charge[3 * other], du, &dt);
+                    if (!st) offer(&best, w->ts_q, w->ts_r, dt, JFO_EV_COMPOSITE, other, -1, 0.0);
+                }
+            }
+        }
+        if (st) {
+            *status = st;
+            return done;
+        }
+        int active_cell;
+        st = cell_of(c, root, &active_cell);
+        if (st) {
+            *status = st;
+            return done;
+        }
+        {
+            /* the molecular cell veto: the charge factor is the active unit's charge
+             * (DipoleMonteCarloEstimator.charge_correction_factor without target charges) */
+            double charge_factor = w->charge[a];
+            int which = 0;
+            if (!(charge_factor > 0.0)) {
+                charge_factor *= -1.0;
+                which = 1;
+            }
+            const Walker *wk = &c->walker[which][w->direction];
+            double total_rate = wk->total_rate * charge_factor;
+            int rc = walker_sample(wk, jfo_draw(s->rng_key, w->event, JFO_RNG_VETO_CHOICE, 0),
+                                   jfo_draw(s->rng_key, w->event, JFO_RNG_VETO_UNIFORM, 0));
+            double rate = (which == 0 ? c->bound_upper[rc * 3 + w->direction] : c->bound_lower[rc * 3 + w->direction]) *
+                          charge_factor;
+            if (!(rate > 0.0)) {
+                *status = JFO_ASSERT;
+                return done;
+            }
+            int target_cell = translate_cell(c, active_cell, rc);
+            double dt = jfo_expovariate(jfo_draw(s->rng_key, w->event, JFO_RNG_VETO_TIME, 0), s->beta) /
+                        (total_rate * s->speed);
+            offer(&best, w->ts_q, w->ts_r, dt, JFO_EV_CELL_VETO, -1, target_cell, rate);
+        }
+        {
+            /* the cell boundary of the active root unit */
+            int cax[3];
+            cell_axes(c, active_cell, cax);
+            int d = w->direction;
+            double boundary = c->cmin[(cax[d] + 1) % c->m];
+            double sep = boundary - root[d];
+            if (sep < 0.0) sep = sep + s->system_length;
+            offer(&best, w->ts_q, w->ts_r, sep / w->root_speed, JFO_EV_BOUNDARY, -1, -1, boundary);
+        }
+        {
+            Cand e;
+            e.q = w->eoc_q;
+            e.r = w->eoc_r;
+            e.kind = JFO_EV_END_OF_CHAIN;
+            e.target = w->eoc_new_active;
+            e.aux = -1;
+            e.rate = 0.0;
+            if (cand_better(&e, &best)) best = e;
+        }
+        /* commit: the active leaf and root unit time-sliced to the event time, from the in-state of the winner */
+        JfoEvent ev;
+        ev.kind = best.kind;
+        ev.moved = a;
+        ev.target = best.target;
+        ev.accepted = 1;
+        ev.time_q = best.q;
+        ev.time_r = best.r;
+        if (best.kind == JFO_EV_BOND || best.kind == JFO_EV_PAIR) {
+            memcpy(&w->pos[3 * a], w->snap_leaf, sizeof(w->snap_leaf));
+            memcpy(root, w->snap_root, sizeof(w->snap_root));
+            water_slice(w, &w->pos[3 * a], s->speed, best.q, best.r, w->snap_q, w->snap_r);
+            water_slice(w, root, w->root_speed, best.q, best.r, w->snap_q, w->snap_r);
+        } else {
+            water_slice(w, &w->pos[3 * a], s->speed, best.q, best.r, w->ts_q, w->ts_r);
+            water_slice(w, root, w->root_speed, best.q, best.r, w->ts_q, w->ts_r);
+        }
+        w->ts_q = best.q;
+        w->ts_r = best.r;
+        switch (best.kind) {
+        case JFO_EV_BOND:
+        case JFO_EV_PAIR:
+            w->active = best.target;
+            break;
+        case JFO_EV_COMPOSITE:
+        case JFO_EV_CELL_VETO: {
+            int other = best.target;
+            if (best.kind == JFO_EV_CELL_VETO) {
+                /* the occupant of the sampled cell, looked up at the commit (Mediator.get_arguments_cell_veto_event_handler) */
+                other = c->occ_count[best.aux] > 0 ? c->occ[best.aux * c->cap] : -1;
+                ev.target = other;
+                ev.accepted = 0;
+                if (other < 0) break;
+            }
+            int new_active;
+            double draws[3], bounding, rate;
+            draws[0] = jfo_uniform(jfo_draw(s->rng_key, w->event, JFO_RNG_THIN, 0));
+            draws[1] = jfo_uniform(jfo_draw(s->rng_key, w->event, JFO_RNG_LIFT, 0));
+            draws[2] = draws[1];
+            if (best.kind == JFO_EV_COMPOSITE)
+                st = jfo_composite_out_state(3, s->lifting, 1, s->ewald_alpha, s->fourier_cutoff, s->position_cutoff,
+                                             s->coulomb_prefactor, s->bound_prefactor, s->system_length, velocity,
+                                             &w->pos[9 * m], &w->charge[3 * m], t, &w->pos[9 * other],
+                                             &w->charge[3 * other], m < other, draws, &new_active, &bounding, &rate);
+            else
+                st = jfo_composite_bounded_out_state(3, s->lifting, 1, s->ewald_alpha, s->fourier_cutoff,
+                                                     s->position_cutoff, s->coulomb_prefactor, s->system_length,
+                                                     velocity, &w->pos[9 * m], &w->charge[3 * m], t,
+                                                     &w->pos[9 * other], &w->charge[3 * other], m < other, best.rate,
+                                                     draws, &new_active, &rate);
+            if (st) {
+                *status = st;
+                return done;
+            }
+            ev.accepted = new_active >= 0;
+            if (new_active >= 0) w->active = new_active < 3 ? 3 * m + new_active : 3 * other + (new_active - 3);
+            break;
+        }
+        case JFO_EV_BOUNDARY:
+            root[w->direction] = best.rate;
+            ev.accepted = 0;
+            break;
+        case JFO_EV_END_OF_CHAIN:
+            w->direction = (w->direction + 1) % 3;
+            w->active = best.target;
+            jfo_time_add(w->ts_q, w->ts_r, jfo_time_sub(w->ts_q, w->ts_r, w->ts_q, w->ts_r) + s->chain_time,
+                         &w->eoc_q, &w->eoc_r);
+            w->eoc_new_active = water_new_active(w, (uint64_t)(w->event + 1));
+            break;
+        default:
+            *status = JFO_ASSERT;
+            return done;
+        }
+        /* every event but the cell boundary trashes the bond and Lennard-Jones candidates */
+        if (best.kind != JFO_EV_BOUNDARY) w->pairs_valid = 0;
+        ev.new_active = w->active;
+        ev.new_direction = w->direction;
+        ev.x = w->pos[3 * a];
+        ev.y = w->pos[3 * a + 1];
+        ev.z = w->pos[3 * a + 2];
+        if (log) log[done] = ev;
+        if (root_log) memcpy(&root_log[3 * done], root, sizeof(double) * 3);
+        w->event++;
+        done++;
+    }
+    return done;
+}
+
+void jfo_water_roots(const JfoWater *w, double *roots) {
+    if (w->cells) memcpy(roots, w->cells->pos, sizeof(double) * 3 * (size_t)w->sys.molecules);
 }
 
 void jfo_water_positions(const JfoWater *w, double *positions) {

@@ -218,6 +218,17 @@ JfoWater *jfo_water_create(const JfoWaterSystem *system, const double *positions
 void jfo_water_destroy(JfoWater *water);
 /* runs up to max_events events; returns the number run; *status is JFO_OK or the first failure */
 int64_t jfo_water_run(JfoWater *water, int64_t max_events, JfoEvent *log, int *status);
+/* the same with the root position of the moved unit's molecule after every event (root_log [max_events][3], may be
+ * NULL; molecular cells only) */
+int64_t jfo_water_run_roots(JfoWater *water, int64_t max_events, JfoEvent *log, double *root_log, int *status);
+/* flexible water with molecular cells of root units (cells_per_side^3 cuboid periodic cells, neighbor_layers): the
+ * Coulomb factor with the molecules of the nearby cells and the surplus molecules, the molecular cell veto with the
+ * given bound tables ([cells][3] upper and negated lower bounds, NaN for the nearby cells) and the cell-boundary
+ * events of the active root unit; roots [molecules][3] are the initial root positions */
+JfoWater *jfo_water_cells_create(const JfoWaterSystem *system, int cells_per_side, int neighbor_layers,
+                                 const double *positions, const double *charges, const double *roots,
+                                 const double *bounds_upper, const double *bounds_lower, int *status);
+void jfo_water_roots(const JfoWater *water, double *roots);
 void jfo_water_positions(const JfoWater *water, double *positions);
 void jfo_water_state(const JfoWater *water, int64_t *event_count, int *active, int *direction, double *time_q,
                      double *time_r);
