@@ -17,9 +17,14 @@ Other workloads (parity configurations measured beside the headline, not the hea
     unit cube, beta = 1, merged-image Coulomb bounded by the inverse-power bound, cell veto on 8^3 cells.
     ``--workload water``:
     512 independent chains of 64 flexible water molecules (12.42 A box, 300 K, O-H and H-H harmonic bonds,
-    Lennard-Jones on oxygen, merged-image Coulomb between molecules with the summed inverse-power Coulomb bound and
-    inside-first lifting), FP64 (thinning screened in FP32 with an error bound), one block per chain; seeded lattices
+    Lennard-Jones on oxygen, merged-image Coulomb between molecules, inside-first lifting) with the molecular cells of
+    the reference's water cell-veto configuration: root units in 8^3 cells with two neighbour layers, the
+    summed-bounding Coulomb factor with the molecules of the nearby cells and the surplus molecules, the molecular
+    cell veto (the reference's dipole Monte Carlo bound tables of this geometry, recorded with the trajectory
+    tests/golden/water_n64_cell_veto.npz) and the cell-boundary events of the active root unit; mixed precision
+    (FP32 screen of the Coulomb candidates and of the thinning, FP64 re-solve), one block per chain; seeded lattices
     of molecules in random orientations.
+    ``--workload water_all_pairs``: the same water with a Coulomb factor for every pair of molecules.
 
 Multi-GPU: one process per GPU under torchrun; every rank runs its own 4096 chains (independent replicas, no
 collective on the data path), value = all ranks' events / max-over-ranks time.
@@ -43,8 +48,15 @@ from jellyfysh_gb300 import workloads as _workloads  # noqa: E402
 
 WORKLOAD = _workloads.LENNARD_JONES
 COULOMB_WORKLOAD = _workloads.COULOMB
-WATER_WORKLOAD = dict(workload="water_chains_512x64_molecular_coulomb", chains=512, molecules=64,
-                      system_length=12.42, temperature_kelvin=300.0, chain_time=2.0, lifting="inside_first")
+WATER_ALL_PAIRS_WORKLOAD = dict(workload="water_chains_512x64_molecular_coulomb", chains=512, molecules=64,
+                                system_length=12.42, temperature_kelvin=300.0, chain_time=2.0, lifting="inside_first",
+                                coulomb="a summed-bounding factor for every pair of molecules")
+WATER_WORKLOAD = dict(WATER_ALL_PAIRS_WORKLOAD, workload="water_chains_512x64_molecular_cell_veto", cells_per_side=8,
+                      neighbor_layers=2,
+                      coulomb="molecular cells: nearby and surplus factors, molecular cell veto, cell boundaries",
+                      bound_tables="the reference's DipoleMonteCarloEstimator tables of this geometry (dipole "
+                                   "separation 0.5, charge 0.82, prefactor 1.5, 1000 trials, empirical bound 30)")
+WATER_BOUNDS = os.path.join(ROOT, "tests", "golden", "water_n64_cell_veto.npz")
 NEAR_CELLS = (2 * WORKLOAD["neighbor_layers"] + 1) ** 3  # cells scanned for pair candidates per event
 CPU_SECONDS = 10.0  # wall time of the CPU baseline sample
 TIMING_STRIDE = 16  # event rounds between two rounds bracketed by per-kernel CUDA events
@@ -62,8 +74,13 @@ NCU = {
     "coulomb": {"traffic_per_event": (2.525440e6 + 0.129024e6) / (1024 * 8), "traffic_caches": "cold",
                 "issue_active": 0.096, "fp64_pipe_active": 0.458},
 }
-# the water kernel (2.83 MB + 0.22 MB over 512 chains x 32 events) with the FP64 pipe's busy fraction of its capture
-WATER_NCU = {"traffic_per_event": (2.830080e6 + 0.221952e6) / (512 * 32), "fp64_pipe_active": 0.501}
+# the all-pairs water kernel (2.83 MB + 0.22 MB over 512 chains x 32 events) with the FP64 pipe's busy fraction of
+# its capture
+WATER_NCU = {"water_all_pairs": {"traffic_per_event": (2.830080e6 + 0.221952e6) / (512 * 32),
+                                 "fp64_pipe_active": 0.501},
+             "water": {"traffic_per_event": (2.830080e6 + 0.221952e6) / (512 * 32), "fp64_pipe_active": 0.501}}
+WATER_METRICS = {"water": "events/s on 1 GB300, batched water chains with the molecular cell veto",
+                 "water_all_pairs": "events/s on 1 GB300, batched water chains, Coulomb factors of all pairs"}
 
 
 def parse():
@@ -81,7 +98,8 @@ def parse():
     p.add_argument("--no-parity", action="store_true")
     p.add_argument("--fp64-events", type=int, default=16, help="events per chain of the batched FP64 comparison")
     p.add_argument("--workload", default="lennard_jones",
-                   choices=["lennard_jones", "coulomb", "water", "hard_spheres", "hard_spheres_n64"])
+                   choices=["lennard_jones", "coulomb", "water", "water_all_pairs", "hard_spheres",
+                            "hard_spheres_n64"])
     args = p.parse_args()
     if args.workload in ("hard_spheres", "hard_spheres_n64") and "--chains" not in sys.argv:
         args.chains = _workloads.BUILDERS[args.workload][0]["chains"]
@@ -92,10 +110,12 @@ def parse():
         args.block_warps = 4 if tuned_default is None else tuned_default
     if args.groups is None:
         args.groups = 1 if tuned_default is None else tuned_default
-    if args.workload == "water" and "--chains" not in sys.argv:
+    if args.workload.startswith("water") and "--chains" not in sys.argv:
         args.chains = WATER_WORKLOAD["chains"]
-    if args.workload == "water" and "--events" not in sys.argv:
+    if args.workload == "water_all_pairs" and "--events" not in sys.argv:
         args.events = 32
+    if args.workload == "water" and "--events" not in sys.argv:
+        args.events = 128
     if args.workload == "coulomb" and "--chains" not in sys.argv:
         args.chains = COULOMB_WORKLOAD["chains"]
     return args
@@ -573,13 +593,41 @@ def water_model_and_positions(chains, seed):
     return model, water.lattice_positions(model, chains, seed)
 
 
-def water_cpu_chains(threads, pool, seed=99):
+def water_cells(args):
+    """The molecular cells of the water workload (None for the all-pairs water): 8^3 cells, two neighbour layers,
+    the reference estimator's bound tables of this geometry."""
+    if args.workload != "water":
+        return None
+    from jellyfysh_gb300 import water
+    data = np.load(WATER_BOUNDS)
+    return water.WaterCells(WATER_WORKLOAD["cells_per_side"], WATER_WORKLOAD["neighbor_layers"],
+                            data["bounds_upper"], data["bounds_lower"])
+
+
+def water_cpu_chains(threads, pool, cells, seed=99):
     """One oracle water chain of the water workload per host thread."""
     import oracle
+    from jellyfysh_gb300 import systems
     model, positions = water_model_and_positions(threads, seed)
     spec = dict(vars(model))
-    return list(pool.map(lambda c: oracle.Water(oracle.make_water_system(spec, oracle.chain_key(seed, c)),
-                                                positions[c], model.charges()), range(threads)))
+
+    def make(c):
+        extra = {}
+        if cells is not None:
+            roots = systems.water_roots(positions[c], model.system_length)
+            extra["cells"] = (cells.cells_per_side, cells.neighbor_layers, roots, cells.bounds_upper,
+                              cells.bounds_lower)
+        return oracle.Water(oracle.make_water_system(spec, oracle.chain_key(seed, c)), positions[c], model.charges(),
+                            **extra)
+    return list(pool.map(make, range(threads)))
+
+
+def water_state_tensors(batch):
+    """The device tensors that hold a water batch's chains (uploaded and read back by the end-to-end steps)."""
+    tensors = [batch.positions_dev, batch.state_dev]
+    if batch.cells is not None:
+        tensors += [batch.roots_dev, batch.occupancy_dev, batch.surplus_dev, batch.cell_state_dev]
+    return tensors
 
 
 def water_gpu_arm(args):
@@ -594,8 +642,10 @@ def water_gpu_arm(args):
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     device = torch.device("cuda", local)
+    cells = water_cells(args)
+    workload = WATER_WORKLOAD if cells is not None else WATER_ALL_PAIRS_WORKLOAD
     model, positions = water_model_and_positions(args.chains, 1000 + rank)
-    batch = water.WaterBatch(model, positions, seed=1000 + rank, first_chain=0)
+    batch = water.WaterBatch(model, positions, seed=1000 + rank, first_chain=0, cells=cells)
     stream = torch.cuda.current_stream(device)
     for _ in range(args.warmup):
         batch.run(args.events)
@@ -620,8 +670,8 @@ def water_gpu_arm(args):
     # end to end: every step uploads positions and chain states from pinned host memory, runs, and reads both back;
     # double-buffered as for the atomic chains (two batches take the steps in turn, each batch's copies on a stream of
     # its own, the runs one after the other on one stream)
-    pair = [batch, water.WaterBatch(model, positions, seed=1000 + rank, first_chain=0)]
-    host_in = [batch.positions_dev.cpu().pin_memory(), batch.state_dev.cpu().pin_memory()]
+    pair = [batch, water.WaterBatch(model, positions, seed=1000 + rank, first_chain=0, cells=cells)]
+    host_in = [t.cpu().pin_memory() for t in water_state_tensors(batch)]
     host_out = [[t.clone().pin_memory() for t in host_in] for _ in pair]
     h2d = sum(t.numel() * t.element_size() for t in host_in)
     e2e_steps = max(2, args.steps // 2)
@@ -636,8 +686,8 @@ def water_gpu_arm(args):
         x = step % 2
         b, copy = pair[x], copy_streams[x]
         with torch.cuda.stream(copy):  # after this batch's previous read-back, in stream order
-            b.positions_dev.copy_(host_in[0], non_blocking=True)
-            b.state_dev.copy_(host_in[1], non_blocking=True)
+            for target, source in zip(water_state_tensors(b), host_in):
+                target.copy_(source, non_blocking=True)
         uploaded = torch.cuda.Event()
         uploaded.record(copy)
         stream.wait_event(uploaded)
@@ -646,8 +696,8 @@ def water_gpu_arm(args):
         ran.record(stream)
         copy.wait_event(ran)
         with torch.cuda.stream(copy):
-            host_out[x][0].copy_(b.positions_dev, non_blocking=True)
-            host_out[x][1].copy_(b.state_dev, non_blocking=True)
+            for target, source in zip(host_out[x], water_state_tensors(b)):
+                target.copy_(source, non_blocking=True)
     for copy in copy_streams:
         done = torch.cuda.Event()
         done.record(copy)
@@ -667,10 +717,25 @@ def water_gpu_arm(args):
     counts = {key: int(after[key].sum() - before[key].sum())
               for key in ("composite_events", "composite_accepted", "bond_events", "lj_events", "eoc_events",
                           "thinning_exact", "refined_items")}
-    # algorithmic bytes per event: every unit's position and charge read once (the candidates of all molecule
-    # pairs), the active unit's position written, the chain state read and written
     units = 3 * model.molecules
-    bytes_per_event = units * (24 + 8) + 24 + 2 * 96
+    if cells is None:
+        # algorithmic bytes per event: every unit's position and charge read once (the candidates of all molecule
+        # pairs), the active unit's position written, the chain state read and written
+        bytes_per_event = units * (24 + 8) + 24 + 2 * 96
+    else:
+        cell_counts = batch.cell_states()
+        counts.update(boundary_events=int(cell_counts["boundary_events"].sum()),
+                      veto_events=int(cell_counts["veto_events"].sum()),
+                      veto_targets=int(cell_counts["veto_targets"].sum()))
+        # algorithmic bytes per event: the occupancy words of the nearby cells and the surplus words, the positions
+        # and charges of the target molecules' units (the nearby cells hold 125/512 of the other molecules on
+        # average), the oxygens and bond partners of the pair items (created at a third of the events: the active
+        # unit is an oxygen a third of the time), the active leaf and root written, the chain and cell states read
+        # and written
+        n_near = (2 * cells.neighbor_layers + 1) ** 3
+        targets = (model.molecules - 1) * n_near / cells.cells
+        bytes_per_event = (4 * (n_near + model.molecules) + 3 * targets * (24 + 8) +
+                           ((model.molecules - 1) / 3.0 + 2) * 24 + 2 * 24 + 2 * (96 + 128))
     step_s = elapsed_ms / args.steps / 1000.0
     achieved = bytes_per_event * args.chains * args.events / step_s / 1e9
     peak, peak_kind = measured_peaks()
@@ -679,28 +744,30 @@ def water_gpu_arm(args):
         import concurrent.futures
         threads = host_threads()
         with concurrent.futures.ThreadPoolExecutor(max_workers=threads) as pool:
-            chains = water_cpu_chains(threads, pool)
+            chains = water_cpu_chains(threads, pool, cells)
             cpu_run(pool, chains, 0.5)
             done, seconds = cpu_run(pool, chains, CPU_SECONDS)
         cpu = {"value": done / seconds, "unit": "events/s", "cores": threads, "kind": "port",
                "per_core": done / seconds / threads,
                "sample": "%d water chains (one per host thread), %d events in %.1f s" % (threads, done, seconds)}
-    config = dict(WATER_WORKLOAD)
-    config.update(chains=args.chains, events_per_chain_per_step=args.events,
+    config = dict(workload)
+    config.update(chains=args.chains, events_per_chain_per_step=args.events, mode=model.mode,
                   l2="working set %.1f MB (in L2): the step is FP64-latency-bound, not HBM-bound" % (
-                      (batch.positions_dev.numel() * 8 + batch.state_dev.numel()) / 1e6),
+                      sum(t.numel() * t.element_size() for t in water_state_tensors(batch)) / 1e6),
                   event_counts=counts, parallelism="replicas" if world > 1 else "single GPU")
-    line = {"metric": "events/s on 1 GB300, batched FP64 water chains", "value": value, "unit": "events/s",
+    line = {"metric": WATER_METRICS[args.workload], "value": value, "unit": "events/s",
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
             "data": "synthetic: seeded lattices of water molecules in random orientations", "config": config,
             "e2e": {"value": e2e_value, "unit": "events/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": h2d,
                     "pipelining": "two batches take the steps in turn; each batch's copies overlap the other's run"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak,
-                         "traffic": WATER_NCU["traffic_per_event"] * args.chains * args.events,
-                         "peak_source": peak_kind, "kernel": "jf::water_kernel", "bytes_per_event": bytes_per_event,
-                         "fp64_pipe_active": WATER_NCU["fp64_pipe_active"]},
+                         "traffic": WATER_NCU[args.workload]["traffic_per_event"] * args.chains * args.events,
+                         "peak_source": peak_kind,
+                         "kernel": "jf::water_cells_kernel" if cells is not None else "jf::water_kernel",
+                         "bytes_per_event": bytes_per_event,
+                         "fp64_pipe_active": WATER_NCU[args.workload]["fp64_pipe_active"]},
             "cpu_baseline": cpu, "gpu_launches": args.steps, "clocks": clocks.summary()}
     print(json.dumps(line))
     if world > 1:
@@ -716,8 +783,9 @@ def water_reference_arm(args):
         return
     threads = host_threads()
     seconds = max(0.2, min(3.0, 90.0 / max(args.steps, 1)))
+    cells = water_cells(args)
     with concurrent.futures.ThreadPoolExecutor(max_workers=threads) as pool:
-        chains = water_cpu_chains(threads, pool)
+        chains = water_cpu_chains(threads, pool, cells)
         for _ in range(args.warmup):
             cpu_run(pool, chains, 0.5)
         total_events, total_time = 0, 0.0
@@ -726,12 +794,12 @@ def water_reference_arm(args):
             total_events += done
             total_time += elapsed
     value = total_events / total_time
-    config = dict(WATER_WORKLOAD)
+    config = dict(WATER_WORKLOAD if cells is not None else WATER_ALL_PAIRS_WORKLOAD)
     config["sample"] = "%d water chains (one per host thread) x %.0f s of events per step" % (threads, seconds)
-    print(json.dumps({"impl": "reference", "metric": "events/s on 1 GB300, batched FP64 water chains",
+    print(json.dumps({"impl": "reference", "metric": WATER_METRICS[args.workload],
                       "value": value, "unit": "events/s", "n_gpus": args.gpus, "steps": args.steps,
                       "warmup": args.warmup, "ms_per_step": 1000.0 * total_time / args.steps,
-                      "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                      "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
                       "data": "synthetic: seeded lattices of water molecules in random orientations",
                       "config": config,
                       "cpu_baseline": {"value": value, "unit": "events/s", "cores": threads, "kind": "port",
@@ -742,7 +810,7 @@ def water_reference_arm(args):
 
 def main():
     args = parse()
-    if args.workload == "water":
+    if args.workload.startswith("water"):
         if args.impl == "reference":
             water_reference_arm(args)
         else:

@@ -27,8 +27,10 @@ struct WaterCells {
     int m, ncells, n_off;
     int offsets[32];          // the distinct residues of -layers .. layers modulo m, ascending
     double side;              // L / m: position_to_cell is int(x / side) along every axis
+    double inv_side;          // 1 / side, the first guess of int(x / side)
     double root_speed;        // the active root unit's velocity component: the speed times the leaf's weight 1/3
     const double *cell_min;   // [m] exact lower cell bounds along an axis
+    const double *cell_max;   // [m] exact upper cell bounds along an axis
     const int16_t *tra;       // [m * m] translate along one axis, [a * m + b]
     const double *bound_upper, *bound_lower;  // [ncells][3] upper and negated lower bounds
     WalkerDev walker[2][3];   // [upper / lower][direction]
@@ -190,7 +192,51 @@ __device__ inline int water_item(const WaterModel &w, const double *pos, const d
 
 __device__ inline void coulomb_unit_screen(const WaterModel &w, const double *pos, const double *charge,
                                            uint64_t key, uint64_t ev, int other, int j, int d, const double *pa,
-                                           double ca, float &time, float &error, bool &unsafe);
+                                           double ca, float &time, float &error, bool &unsafe,
+                                           const float *pp32 = nullptr);
+
+// FP32 lower bound of the time of bond k of the active unit 3 m + t (the k-th of the two other units of its
+// molecule): a bond k (|s| - r0)^2 along the motion has |d|s|/dx| <= 1, so the potential rises at most at
+// 2 k (a + x) with a = ||s| - r0| after a displacement x, and a rise du takes at least
+// (du / k) / (a + sqrt(a^2 + du / k)); computed with every rounding towards a smaller value.  It bounds the bond's
+// time from below only.
+__device__ inline void bond_unit_screen(const WaterModel &w, const double *pos, uint64_t key, uint64_t ev, int m,
+                                        int t, int k, const double *pa, float &time, bool &unsafe) {
+    const int u = k + (k >= t);
+    const int b = 3 * m + u;
+    const MH &bond = (t == 1 || u == 1) ? w.oh : w.hh;
+    bool flag = false;
+    const float du = expovariate32(draw(key, ev, kRngPair, (uint32_t)b), 1.0f / w.beta32, flag);
+    double sep[3];
+    periodic_separation(pa, pos + 3 * b, w.length, sep);
+    const float r = sqrtf((float)(sep[0] * sep[0] + sep[1] * sep[1] + sep[2] * sep[2]));
+    const float a = fabsf(r - (float)bond.r0) * (1.f + 0x1p-16f) + 0x1p-20f * (float)bond.r0;
+    const float ratio = du * (1.f - 0x1p-16f) / (float)(bond.prefactor * (1.0 + 0x1p-20));
+    time = ratio / (a + sqrtf(a * a + ratio)) * (1.f - 0x1p-16f) / w.speed32;
+    unsafe = flag || !(time >= 0.f);
+}
+
+// FP32 screen of Lennard-Jones against the oxygen of molecule `other` (over the speed): the FP32 screen of the
+// atomic engine, within 2^-13 relative plus its absolute margin unless flagged; a pair without an event (U + du
+// stays below zero) screens to an infinite time that is safe
+__device__ inline void lj_unit_screen(const WaterModel &w, const double *pos, uint64_t key, uint64_t ev, int other,
+                                      int d, const double *pa, float &time, float &error, bool &unsafe) {
+    const int b = 3 * other + 1;
+    bool flag = false;
+    const float du = expovariate32(draw(key, ev, kRngPair, (uint32_t)b), 1.0f / w.beta32, flag);
+    double sep64[3];
+    periodic_separation(pa, pos + 3 * b, w.length, sep64);
+    float sep[3] = {(float)sep64[0], (float)sep64[1], (float)sep64[2]};
+    int path;
+    time = lj_screen(w.lj32, d, w.speed32, sep, du, w.margin32, flag, path);
+    error = 0x1p-11f * fabsf(time) + w.length32 * 0x1p-17f / w.speed32;
+    unsafe = flag || isinf(time);
+    if (isinf(time) && !flag) {
+        unsafe = false;
+        time = INFINITY;
+        error = 0.f;
+    }
+}
 
 // FP32 screen of a candidate item, in displacements over the speed: the Coulomb items solve the bound's inversion
 // in FP32 with an error bound (ipcb_x_displacement32), the Lennard-Jones items take the FP32 screen of the atomic
@@ -206,45 +252,15 @@ __device__ inline void water_screen(const WaterModel &w, const double *pos, cons
     time = 0.f;
     error = 0.f;
     if (item >= 3 * group + (t == 1 ? M - 1 : 0)) {
-        // a bond k (|s| - r0)^2: along the motion |d|s|/dx| <= 1, so the potential rises at most at
-        // 2 k (a + x) with a = ||s| - r0| after a displacement x, and a rise du takes at least
-        // (du / k) / (a + sqrt(a^2 + du / k)); computed with every rounding towards a smaller value
-        const int k = item - 3 * group - (t == 1 ? M - 1 : 0);
-        const int u = k + (k >= t);
-        const int b = 3 * m + u;
-        const MH &bond = (t == 1 || u == 1) ? w.oh : w.hh;
-        bool flag = false;
-        const float du = expovariate32(draw(key, ev, kRngPair, (uint32_t)b), 1.0f / w.beta32, flag);
-        double sep[3];
-        periodic_separation(pa, pos + 3 * b, w.length, sep);
-        const float r = sqrtf((float)(sep[0] * sep[0] + sep[1] * sep[1] + sep[2] * sep[2]));
-        const float a = fabsf(r - (float)bond.r0) * (1.f + 0x1p-16f) + 0x1p-20f * (float)bond.r0;
-        const float ratio = du * (1.f - 0x1p-16f) / (float)(bond.prefactor * (1.0 + 0x1p-20));
-        time = ratio / (a + sqrtf(a * a + ratio)) * (1.f - 0x1p-16f) / w.speed32;
+        bond_unit_screen(w, pos, key, ev, m, t, item - 3 * group - (t == 1 ? M - 1 : 0), pa, time, unsafe);
         lower_only = true;
-        unsafe = flag || !(time >= 0.f);
         return;
     }
     if (item >= 3 * group) {
-        // Lennard-Jones against another oxygen (only listed when the active unit is an oxygen): the FP32 screen
-        // of the atomic engine, within 2^-13 relative plus its absolute margin unless flagged
+        // Lennard-Jones against another oxygen (only listed when the active unit is an oxygen)
         int other = item - 3 * group;
         other += other >= m;
-        const int b = 3 * other + 1;
-        bool flag = false;
-        const float du = expovariate32(draw(key, ev, kRngPair, (uint32_t)b), 1.0f / w.beta32, flag);
-        double sep64[3];
-        periodic_separation(pa, pos + 3 * b, w.length, sep64);
-        float sep[3] = {(float)sep64[0], (float)sep64[1], (float)sep64[2]};
-        int path;
-        time = lj_screen(w.lj32, d, w.speed32, sep, du, w.margin32, flag, path);
-        error = 0x1p-11f * fabsf(time) + w.length32 * 0x1p-17f / w.speed32;
-        unsafe = flag || isinf(time);
-        if (isinf(time) && !flag) {  // no event from this pair (U + du stays below zero): not a candidate
-            unsafe = false;
-            time = INFINITY;
-            error = 0.f;
-        }
+        lj_unit_screen(w, pos, key, ev, other, d, pa, time, error, unsafe);
         return;
     }
     const int j = item / group;
@@ -259,9 +275,11 @@ __device__ inline void water_screen(const WaterModel &w, const double *pos, cons
 
 // FP32 screen of the bounded displacement of the active unit against unit j of molecule `other` (over the speed),
 // with its error bound; unsafe: the screen cannot decide
+// pp32: the FP32 prefactors (float)(bound prefactor * active charge * charge[b]) of every unit b, or null to compute
+// the unit's here
 __device__ inline void coulomb_unit_screen(const WaterModel &w, const double *pos, const double *charge,
                                            uint64_t key, uint64_t ev, int other, int j, int d, const double *pa,
-                                           double ca, float &time, float &error, bool &unsafe) {
+                                           double ca, float &time, float &error, bool &unsafe, const float *pp32) {
     const int b = 3 * other + j;
     // du = -log(1 - u) / beta of the FP64 draw u = n 2^-53 (uniform53): log1pf(-u) below u = 1/2 (u rounded to
     // FP32 moves -log(1 - u) by at most 2 units of 2^-24 relative there), logf of the exact 1 - u = (2^53 - n) 2^-53
@@ -275,7 +293,8 @@ __device__ inline void coulomb_unit_screen(const WaterModel &w, const double *po
     periodic_separation(pa, pos + 3 * b, w.length, sep);
     permute3(sep, d, p);
     float value_error;
-    const float value = ipcb_x_displacement32((float)(w.coulomb.bound_prefactor * ca * charge[b]), (float)p[0],
+    const float pp = pp32 ? pp32[b] : (float)(w.coulomb.bound_prefactor * ca * charge[b]);
+    const float value = ipcb_x_displacement32(pp, (float)p[0],
                                               (float)p[1], (float)p[2], du, du_error, w.length32, value_error,
                                               unsafe);
     time = value / w.speed32;
@@ -586,10 +605,24 @@ __global__ void __launch_bounds__(256, 2) water_kernel(WaterArgs a) {
 // ---------------------------------------------------------------------------------------------------------------
 // Water with molecular cells
 // ---------------------------------------------------------------------------------------------------------------
+// int(x / side) along one axis: the exact cell bounds hold cell_min[i] <= x <= cell_max[i] if and only if
+// int(x / side) == i, so a multiply by 1 / side guesses the index and a step or two against the bounds corrects it
+__device__ inline long long water_axis_index(const WaterCells &cl, double x) {
+    if (!(x >= 0.0) || !(x < (double)cl.m * cl.side)) return (long long)(x / cl.side);
+    long long i = (long long)(x * cl.inv_side);
+    if (i > cl.m - 1) i = cl.m - 1;
+    if (i < 0) i = 0;
+    while (i > 0 && x < cl.cell_min[i]) --i;
+    while (x > cl.cell_max[i]) {
+        if (i == cl.m - 1) return cl.m;
+        ++i;
+    }
+    return i;
+}
+
 // position_to_cell of a root unit (cuboid_cells.py:190-211): int(x / side) along every axis
 __device__ inline int water_cell_of(const WaterCells &cl, const double *p, int &cell) {
-    const long long ix = (long long)(p[0] / cl.side), iy = (long long)(p[1] / cl.side),
-                    iz = (long long)(p[2] / cl.side);
+    const long long ix = water_axis_index(cl, p[0]), iy = water_axis_index(cl, p[1]), iz = water_axis_index(cl, p[2]);
     const long long idx = ix + (long long)cl.m * iy + (long long)cl.m * cl.m * iz;
     if (idx < 0 || idx >= cl.ncells) return JFGPU_STATUS_CELL_RANGE;
     cell = (int)idx;
@@ -700,13 +733,15 @@ __global__ void __launch_bounds__(256, 2) water_cells_kernel(WaterArgs a) {
     __shared__ JfgpuWaterState s;
     __shared__ JfgpuWaterCellState cs;
     __shared__ WaterCand warp_best[kMaxWarps], warp_pair[kMaxWarps];
-    __shared__ float warp_upper[kMaxWarps];
+    __shared__ float warp_upper[kMaxWarps], warp_pair_upper[kMaxWarps];
     extern __shared__ float dynamic[];
     float *lower = dynamic;
     int *list = reinterpret_cast<int *>(dynamic + water_items_max(M));
     int *chunk_count = list + water_items_max(M);
     int *targets = chunk_count + water_chunks_max(M);
-    __shared__ int status, n_targets, veto_cell;
+    __shared__ int status, single_status, n_targets, veto_cell, pp_active;
+    __shared__ float single_bound;
+    float *pp32 = reinterpret_cast<float *>(targets + M);  // [3 M]
     __shared__ WaterCand single;
     __shared__ double veto_rate, boundary;
     __shared__ double bound[3], pair[3], cross[9];
@@ -716,6 +751,8 @@ __global__ void __launch_bounds__(256, 2) water_cells_kernel(WaterArgs a) {
         cs = a.cell_state[chain];
         s.stopped = 0;
         status = JFGPU_STATUS_OK;
+        single_status = JFGPU_STATUS_OK;
+        pp_active = -1;
     }
     __syncthreads();
     for (int64_t step = 0; step < a.events && s.status == JFGPU_STATUS_OK; ++step) {
@@ -723,17 +760,34 @@ __global__ void __launch_bounds__(256, 2) water_cells_kernel(WaterArgs a) {
         const uint64_t ev = (uint64_t)s.events;
         const double ts_q = s.time_q, ts_r = s.time_r;
         const double ca = charge[act];
+        // the occupancy (thread 0) and, beside it, the single candidates from the cell of the active root unit
+        // (the first thread of the second warp, or thread 0 of a one-warp block)
         if (threadIdx.x == 0) {
             n_targets = 0;
-            int st = water_occupancy_update(cl, cs, occ, sur, roots, m);
+            status = water_occupancy_update(cl, cs, occ, sur, roots, m);
+        }
+        if (threadIdx.x == (warps > 1 ? 32 : 0)) {
+            int cell;
+            int st = water_cell_of(cl, roots + 3 * m, cell);
             if (!st)
-                st = water_single_candidates(w, key, ev, cs.occ_cell, d, ca, roots + 3 * m, ts_q, ts_r, single,
-                                             veto_cell, veto_rate, boundary);
-            status = st;
+                st = water_single_candidates(w, key, ev, cell, d, ca, roots + 3 * m, ts_q, ts_r, single, veto_cell,
+                                             veto_rate, boundary);
+            // the time since the time stamp that these candidates surely reach, rounded up (the screen's bound)
+            float sb = __double2float_ru(time_sub(single.q, single.r, ts_q, ts_r));
+            sb = fminf(sb, __double2float_ru(time_sub(s.eoc_q, s.eoc_r, ts_q, ts_r)));
+            if (cs.pairs_valid) sb = fminf(sb, __double2float_ru(time_sub(cs.pair_q, cs.pair_r, ts_q, ts_r)));
+            single_bound = sb;
+            single_status = st;
+        }
+        if (act != pp_active) {
+            // the FP32 prefactors of the Coulomb screen for a new active unit
+            for (int b = threadIdx.x; b < 3 * M; b += blockDim.x)
+                pp32[b] = (float)(w.coulomb.bound_prefactor * ca * charge[b]);
         }
         __syncthreads();
-        if (status != JFGPU_STATUS_OK) {
-            if (threadIdx.x == 0) s.status = status;
+        if (threadIdx.x == 0) pp_active = act;
+        if (status != JFGPU_STATUS_OK || single_status != JFGPU_STATUS_OK) {
+            if (threadIdx.x == 0) s.status = status != JFGPU_STATUS_OK ? status : single_status;
             break;
         }
         // the target molecules: the occupants of the nearby cells (ExcludedCellsTagger), the surplus molecules
@@ -779,10 +833,23 @@ __global__ void __launch_bounds__(256, 2) water_cells_kernel(WaterArgs a) {
         int st = JFGPU_STATUS_OK, refined = nt * 3 + n_pairs;
         // phase A: the pair items in FP64; the Coulomb items in FP64 (exact mode) or screened in FP32 (mixed mode:
         // lower[item] = the earliest time the item may reach, -inf where the screen cannot decide)
-        float mine = INFINITY;
+        float mine = INFINITY, pair_mine = INFINITY;
         for (int item = threadIdx.x; item < items && !st; item += blockDim.x) {
             if (item >= n_coulomb) {
-                st = pair_item_exact(w, pos, key, ev, item - n_coulomb, n_lj, m, t, d, pa, ts_q, ts_r, pbest);
+                const int k = item - n_coulomb;
+                if (mixed) {
+                    // Lennard-Jones screened in FP32 (a lower and an upper bound), a bond bounded from below
+                    float t32, e32 = 0.f;
+                    bool unsafe = false;
+                    if (k < n_lj)
+                        lj_unit_screen(w, pos, key, ev, k + (k >= m), d, pa, t32, e32, unsafe);
+                    else
+                        bond_unit_screen(w, pos, key, ev, m, t, k - n_lj, pa, t32, unsafe);
+                    lower[item] = unsafe ? -INFINITY : __fsub_rd(t32, e32);
+                    if (!unsafe && k < n_lj) pair_mine = fminf(pair_mine, __fadd_ru(t32, e32));
+                    continue;
+                }
+                st = pair_item_exact(w, pos, key, ev, k, n_lj, m, t, d, pa, ts_q, ts_r, pbest);
                 continue;
             }
             const int j = item / group, k = item % group;
@@ -793,7 +860,7 @@ __global__ void __launch_bounds__(256, 2) water_cells_kernel(WaterArgs a) {
             if (mixed) {
                 float t32, e32;
                 bool unsafe = false;
-                coulomb_unit_screen(w, pos, charge, key, ev, targets[k], j, d, pa, ca, t32, e32, unsafe);
+                coulomb_unit_screen(w, pos, charge, key, ev, targets[k], j, d, pa, ca, t32, e32, unsafe, pp32);
                 lower[item] = unsafe ? -INFINITY : __fsub_rd(t32, e32);
                 if (!unsafe) mine = fminf(mine, __fadd_ru(t32, e32));
             } else {
@@ -803,8 +870,14 @@ __global__ void __launch_bounds__(256, 2) water_cells_kernel(WaterArgs a) {
         if (st) status = st;  // any failing thread; all stop after the barrier
         block_reduce_cand(pbest, warp_pair, lane, warp, warps);
         if (mixed) {
-            for (int offset = 16; offset > 0; offset >>= 1) mine = fminf(mine, __shfl_xor_sync(kFull, mine, offset));
-            if (lane == 0) warp_upper[warp] = mine;
+            for (int offset = 16; offset > 0; offset >>= 1) {
+                mine = fminf(mine, __shfl_xor_sync(kFull, mine, offset));
+                pair_mine = fminf(pair_mine, __shfl_xor_sync(kFull, pair_mine, offset));
+            }
+            if (lane == 0) {
+                warp_upper[warp] = mine;
+                warp_pair_upper[warp] = pair_mine;
+            }
         }
         __syncthreads();
         if (status != JFGPU_STATUS_OK) {
@@ -822,39 +895,58 @@ __global__ void __launch_bounds__(256, 2) water_cells_kernel(WaterArgs a) {
             pcand.target = cs.pair_target;
         }
         if (mixed) {
-            // the bound: the smallest time that some candidate surely reaches (a screened time plus its error bound,
-            // the pair candidate, the single candidates, the end of chain), rounded upwards
-            float bound_time = __double2float_ru(time_sub(eoc.q, eoc.r, ts_q, ts_r));
-            bound_time = fminf(bound_time, __double2float_ru(time_sub(pcand.q, pcand.r, ts_q, ts_r)));
-            bound_time = fminf(bound_time, __double2float_ru(time_sub(single.q, single.r, ts_q, ts_r)));
-            for (int k = 0; k < warps; ++k) bound_time = fminf(bound_time, warp_upper[k]);
-            // the Coulomb items that may come first, listed in item order (by unit type, so that a warp of the FP64
-            // pass follows one charge sign): the taken count of every chunk of 32 items, then every warp writes the
-            // items of its chunks at their offsets
-            const int chunks = n_coulomb >> 5;
+            // the bound: the smallest time that some candidate surely reaches (a screened Coulomb or Lennard-Jones
+            // time plus its error bound, the pair candidate kept across a cell boundary, the single candidates, the
+            // end of chain), in time since the time stamp, rounded up
+            float bound_time = single_bound;
+            for (int k = 0; k < warps; ++k) bound_time = fminf(bound_time, fminf(warp_upper[k], warp_pair_upper[k]));
+            // the items that may come first, listed in item order (the Coulomb items by unit type, so that a warp of
+            // the FP64 pass follows one charge sign; then the pair items): the taken count of every chunk of 32
+            // items, then every warp writes the items of its chunks at their offsets
+            const int chunks = (items + 31) >> 5;
             for (int c = warp; c < chunks; c += warps) {
-                const unsigned votes = __ballot_sync(kFull, lower[32 * c + lane] <= bound_time);
+                const int item = 32 * c + lane;
+                const unsigned votes = __ballot_sync(kFull, item < items && lower[item] <= bound_time);
                 if (lane == 0) chunk_count[c] = __popc(votes);
             }
             __syncthreads();
             int taken = 0;
             for (int c = 0; c < chunks; ++c) {
                 if (c % warps == warp) {
-                    const bool take = lower[32 * c + lane] <= bound_time;
+                    const int item = 32 * c + lane;
+                    const bool take = item < items && lower[item] <= bound_time;
                     const unsigned votes = __ballot_sync(kFull, take);
-                    if (take) list[taken + __popc(votes & ((1u << lane) - 1u))] = 32 * c + lane;
+                    if (take) list[taken + __popc(votes & ((1u << lane) - 1u))] = item;
                 }
                 taken += chunk_count[c];
             }
             __syncthreads();
             // phase B: the FP64 solve of the listed items
-            for (int v = threadIdx.x; v < taken; v += blockDim.x) {
+            for (int v = threadIdx.x; v < taken && !st; v += blockDim.x) {
                 const int item = list[v];
+                if (item >= n_coulomb) {
+                    st = pair_item_exact(w, pos, key, ev, item - n_coulomb, n_lj, m, t, d, pa, ts_q, ts_r, pbest);
+                    continue;
+                }
                 if (item % group >= nt) continue;  // padding (listed only under an infinite bound)
                 coulomb_unit_exact(w, pos, charge, key, ev, targets[item % group], item / group, d, pa, ca, ts_q,
                                    ts_r, best);
             }
-            refined = taken + n_pairs;
+            if (st) status = st;
+            refined = taken;
+            if (new_pairs) {
+                // the earliest of the listed pair items: the winner when a pair item comes first
+                block_reduce_cand(pbest, warp_pair, lane, warp, warps);
+                __syncthreads();
+                if (status != JFGPU_STATUS_OK) {
+                    if (threadIdx.x == 0) s.status = status;
+                    break;
+                }
+                pbest = warp_pair[0];
+                for (int k = 1; k < warps; ++k)
+                    if (water_better(warp_pair[k], pbest)) pbest = warp_pair[k];
+                pcand = pbest;
+            }
         }
         block_reduce_cand(best, warp_best, lane, warp, warps);
         __syncthreads();
@@ -866,6 +958,28 @@ __global__ void __launch_bounds__(256, 2) water_cells_kernel(WaterArgs a) {
         if (water_better(pcand, best)) best = pcand;
         if (water_better(single, best)) best = single;
         if (water_better(eoc, best)) best = eoc;
+        if (mixed && new_pairs && best.kind == JFGPU_EV_BOUNDARY) {
+            // the pair candidates outlive a cell boundary: the earliest of all of them in FP64 (the screen listed only
+            // those that could come first at this event)
+            WaterCand all;
+            all.q = INFINITY;
+            all.r = INFINITY;
+            all.kind = 1 << 30;
+            all.target = 1 << 30;
+            for (int k = threadIdx.x; k < n_pairs && !st; k += blockDim.x)
+                st = pair_item_exact(w, pos, key, ev, k, n_lj, m, t, d, pa, ts_q, ts_r, all);
+            if (st) status = st;
+            block_reduce_cand(all, warp_pair, lane, warp, warps);
+            __syncthreads();
+            if (status != JFGPU_STATUS_OK) {
+                if (threadIdx.x == 0) s.status = status;
+                break;
+            }
+            pbest = warp_pair[0];
+            for (int k = 1; k < warps; ++k)
+                if (water_better(warp_pair[k], pbest)) pbest = warp_pair[k];
+            refined += n_pairs;
+        }
         if (!isinf(a.stop_q) && !time_lt(best.q, best.r, a.stop_q, a.stop_r)) {
             // the end of the run: the active leaf and root unit time-sliced to the stop time, no event; the pair
             // candidates are created anew by the next call
@@ -1303,6 +1417,7 @@ extern "C" int jfgpu_water_set_cells(void *water, int32_t cells_per_side, int32_
     cl.m = m;
     cl.ncells = m * m * m;
     cl.side = w.length / m;
+    cl.inv_side = 1.0 / cl.side;
     cl.root_speed = w.speed * (1.0 / 3.0);  // the leaf velocity times its weight 1 / len(children) in the molecule
     // the residues of the neighbour-layer offsets (cuboid_periodic_cells.py:74-100), ascending
     std::vector<char> near(m, 0);
@@ -1341,6 +1456,7 @@ extern "C" int jfgpu_water_set_cells(void *water, int32_t cells_per_side, int32_
             if (st) return st;
         }
     cl.cell_min = water_table(h, lo, error);
+    cl.cell_max = water_table(h, hi, error);
     cl.tra = water_table(h, tra, error);
     cl.bound_upper = water_table(h, upper, error);
     cl.bound_lower = water_table(h, lower, error);
@@ -1404,7 +1520,9 @@ extern "C" int jfgpu_water_cells_run(void *water, double *positions, const doubl
     a.sur = buffers->surplus;
     a.cell_state = buffers->cell_state;
     a.root_log = buffers->root_log;
-    const size_t shared = water_shared_bytes(h->model.molecules) + sizeof(int) * (size_t)h->model.molecules;
+    // the water kernel's arrays, the target list [molecules] and the screen's prefactors [3 molecules]
+    const size_t shared = water_shared_bytes(h->model.molecules) + sizeof(int) * (size_t)h->model.molecules +
+                          sizeof(float) * 3 * (size_t)h->model.molecules;
     if (shared > 48 * 1024 &&
         cudaFuncSetAttribute(water_cells_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shared) !=
             cudaSuccess)
