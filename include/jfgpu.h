@@ -27,6 +27,13 @@
  *       leaf_unit_cell_veto_event_handler.py:117-149, cell_boundary_event_handler.py:98-173,
  *       single_independent_active_periodic_direction_end_of_chain_event_handler.py:151-237,
  *       scheduler/heap_scheduler/heap.c:156-304, activator/internal_state/single_active_cell_occupancy.py:95-237
+ *   jfgpu_water_run / jfgpu_water_cells_run
+ *       SingleProcessMediator.run over flexible water: factor-type-map bonds and Lennard-Jones,
+ *       two_composite_object_summed_bounding_potential_event_handler.py:119-202, lifting/lifting.py:47-108;
+ *       with molecular cells the reference's water cell-veto configuration
+ *       (config_files/2018_JCP_149_064113/water/coulomb_cell_veto_lj_inverted.ini): root units in
+ *       single_active_cell_occupancy.py:95-203, composite_object_cell_veto_event_handler.py:110-162,
+ *       cell_boundary_event_handler.py:98-173, excluded_cells_tagger.py:107-132, surplus_cells_tagger.py:107-131
  */
 #ifndef JFGPU_H
 #define JFGPU_H
@@ -411,9 +418,11 @@ typedef struct {
  * nearby cells, and the molecular cell veto's bound tables (host arrays [cells][3]: the upper and the negated lower
  * derivative bound of every relative cell and direction, as the estimator filled
  * CellVetoEventHandler._derivative_bounds, abstracts/cell_veto_event_handler.py:134-160; NaN for the nearby cells),
- * from which the Walker tables are built in the reference's order.  cells_per_side 1..32. */
+ * from which the Walker tables are built in the reference's order.  cells_per_side 1..32.  keep_pairs: the cell
+ * boundary's tagger trashes only the cell-based factors, so the bond and Lennard-Jones candidates outlive it (the
+ * reference's water cell-veto configuration); 0: it trashes them too. */
 int jfgpu_water_set_cells(void *water, int32_t cells_per_side, int32_t neighbor_layers, const double *bounds_upper,
-                          const double *bounds_lower);
+                          const double *bounds_lower, int32_t keep_pairs);
 /* the occupancy of chains first .. first + chains - 1 from their roots (root nodes in order, the first molecule of a
  * cell its occupant, the others surplus) and a fresh cell state; with jfgpu_water_init for the rest of the state */
 int jfgpu_water_cells_init(void *water, const JfgpuWaterCellBuffers *buffers, int64_t chains, void *stream);

@@ -25,6 +25,7 @@ namespace jf {
 // layers and the molecular cell veto's bound and Walker tables
 struct WaterCells {
     int m, ncells, n_off;
+    int keep_pairs;           // the bond and Lennard-Jones candidates outlive a cell boundary
     int offsets[32];          // the distinct residues of -layers .. layers modulo m, ascending
     double side;              // L / m: position_to_cell is int(x / side) along every axis
     double inv_side;          // 1 / side, the first guess of int(x / side)
@@ -958,7 +959,7 @@ __global__ void __launch_bounds__(256, 2) water_cells_kernel(WaterArgs a) {
         if (water_better(pcand, best)) best = pcand;
         if (water_better(single, best)) best = single;
         if (water_better(eoc, best)) best = eoc;
-        if (mixed && new_pairs && best.kind == JFGPU_EV_BOUNDARY) {
+        if (mixed && new_pairs && best.kind == JFGPU_EV_BOUNDARY && cl.keep_pairs) {
             // the pair candidates outlive a cell boundary: the earliest of all of them in FP64 (the screen listed only
             // those that could come first at this event)
             WaterCand all;
@@ -1161,7 +1162,7 @@ __global__ void __launch_bounds__(256, 2) water_cells_kernel(WaterArgs a) {
                 cs.snap_r = ts_r;
             }
             // the cell boundary trashes only the cell-based factors; every other event the pair candidates too
-            cs.pairs_valid = best.kind == JFGPU_EV_BOUNDARY;
+            cs.pairs_valid = best.kind == JFGPU_EV_BOUNDARY && cl.keep_pairs;
             for (int c = 0; c < 3; ++c) {
                 pos[3 * act + c] = pa[c];
                 roots[3 * m + c] = pr[c];
@@ -1406,7 +1407,7 @@ const T *water_table(WaterHandle *h, const std::vector<T> &host, int &error) {
 }  // namespace
 
 extern "C" int jfgpu_water_set_cells(void *water, int32_t cells_per_side, int32_t neighbor_layers,
-                                     const double *bounds_upper, const double *bounds_lower) {
+                                     const double *bounds_upper, const double *bounds_lower, int32_t keep_pairs) {
     WaterHandle *h = static_cast<WaterHandle *>(water);
     if (!h || cells_per_side < 1 || cells_per_side > 32 || neighbor_layers < 0 || !bounds_upper || !bounds_lower)
         return JFGPU_ERROR_ARGUMENT;
@@ -1416,6 +1417,7 @@ extern "C" int jfgpu_water_set_cells(void *water, int32_t cells_per_side, int32_
     const int m = cells_per_side;
     cl.m = m;
     cl.ncells = m * m * m;
+    cl.keep_pairs = keep_pairs ? 1 : 0;
     cl.side = w.length / m;
     cl.inv_side = 1.0 / cl.side;
     cl.root_speed = w.speed * (1.0 / 3.0);  // the leaf velocity times its weight 1 / len(children) in the molecule

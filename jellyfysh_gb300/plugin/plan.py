@@ -65,7 +65,10 @@ def _lennard_jones(potential):
 
 @dataclasses.dataclass
 class WaterPlan:
-    """One configured water system run as `chains` independent chains on the GPU (``jellyfysh_gb300.water``)."""
+    """One configured water system run as `chains` independent chains on the GPU (``jellyfysh_gb300.water``).  With
+    molecular cells (the reference's water cell-veto configuration) ``roots`` holds the root units' positions and
+    ``cell_veto`` the cell system and the dipole estimator's parameters, from which ``run_plan`` builds the bound
+    tables on the GPU."""
     model: Any
     positions: np.ndarray
     charges: np.ndarray
@@ -74,6 +77,8 @@ class WaterPlan:
     mode: str = "mixed"
     seed: int = 0
     events_per_launch: int = 256
+    roots: Optional[np.ndarray] = None
+    cell_veto: Optional[dict] = None
 
 
 _LIFTINGS = {"InsideFirstLifting": "inside_first", "OutsideFirstLifting": "outside_first",
@@ -106,11 +111,53 @@ def _translate_water(state_handler, activator, setting, roots, chains, mode, see
                   mode=mode)
     bonds = {}
     end_of_run_time = math.inf
+    pair_tags, cell_tags, end_of_chain_tags, trash_lists = set(), set(), set(), {}
+    boundary_tag, veto, coulomb_taggers = None, None, set()
+
+    def coulomb_factor(handler):
+        """The parameters of a summed-bounding Coulomb factor: merged-image Coulomb with the inverse-power bound and
+        a lifting scheme."""
+        mic, bound = handler._potential, handler._bounding_potential
+        if _potential_kind(mic) != "MergedImageCoulomb" or _potential_kind(bound) != "InversePowerCoulombBounding":
+            raise ConfigurationError("the Coulomb factor runs merged-image Coulomb with its inverse-power bound")
+        fields.update(coulomb_prefactor=float(mic._prefactor), alpha=float(mic._alpha),
+                      fourier_cutoff=int(mic._fourier_cutoff), position_cutoff=int(mic._position_cutoff),
+                      bound_prefactor=float(bound._prefactor), lifting=lifting_of(handler))
+
+    def lifting_of(handler):
+        name = _name(handler._lifting)
+        lifting = name.replace("Gpu", "", 1) if name.startswith("Gpu") else name
+        if lifting not in _LIFTINGS:
+            raise ConfigurationError("lifting scheme %s is not on the water engine's path" % lifting)
+        return _LIFTINGS[lifting]
+
     for tagger in activator._taggers:
         tagger_name = _name(tagger)
         handler = tagger._event_handler_to_copy
         handler_name = _name(handler)
+        trash_lists[tagger.tag] = set(tagger.trashes)
+        if tagger_name == "CellBoundaryTagger" and handler_name == "CellBoundaryEventHandler":
+            boundary_tag = tagger.tag
+            cell_tags.add(tagger.tag)
+            continue
+        if tagger_name in ("ExcludedCellsTagger", "SurplusCellsTagger"):
+            if handler_name != "TwoCompositeObjectSummedBoundingPotentialEventHandler":
+                raise ConfigurationError("the molecular cells take the summed-bounding Coulomb factor")
+            coulomb_factor(handler)
+            coulomb_taggers.add(tagger_name)
+            cell_tags.add(tagger.tag)
+            continue
+        if tagger_name == "CellVetoTagger":
+            if handler_name != "CompositeObjectCellVetoEventHandler":
+                raise ConfigurationError("the water engine's cell veto is the molecular one")
+            estimator = handler._estimator
+            if _name(estimator) != "DipoleMonteCarloEstimator":
+                raise ConfigurationError("the molecular cell veto's bounds come from the dipole Monte Carlo estimator")
+            veto = dict(handler=handler, estimator=estimator, lifting=lifting_of(handler))
+            cell_tags.add(tagger.tag)
+            continue
         if tagger_name == "FactorTypeMapInStateTagger":
+            pair_tags.add(tagger.tag)
             groups = _factor_groups(tagger)
             if handler_name == "TwoLeafUnitEventHandler":
                 potential = handler._potential
@@ -130,21 +177,14 @@ def _translate_water(state_handler, activator, setting, roots, chains, mode, see
             elif handler_name == "TwoCompositeObjectSummedBoundingPotentialEventHandler":
                 if groups != {(0, 1, 2, 3, 4, 5)}:
                     raise ConfigurationError("the water engine's Coulomb factor takes both molecules whole")
-                mic, bound = handler._potential, handler._bounding_potential
-                if _potential_kind(mic) != "MergedImageCoulomb" or \
-                        _potential_kind(bound) != "InversePowerCoulombBounding":
-                    raise ConfigurationError("the Coulomb factor runs merged-image Coulomb with its inverse-power bound")
-                lifting = _name(handler._lifting).replace("Gpu", "", 1) if _name(handler._lifting).startswith(
-                    "Gpu") else _name(handler._lifting)
-                if lifting not in _LIFTINGS:
-                    raise ConfigurationError("lifting scheme %s is not on the water engine's path" % lifting)
-                fields.update(coulomb_prefactor=float(mic._prefactor), alpha=float(mic._alpha),
-                              fourier_cutoff=int(mic._fourier_cutoff), position_cutoff=int(mic._position_cutoff),
-                              bound_prefactor=float(bound._prefactor), lifting=_LIFTINGS[lifting])
+                coulomb_factor(handler)
+                pair_tags.discard(tagger.tag)
+                coulomb_taggers.add(tagger_name)
             else:
                 raise ConfigurationError("factor event handler %s is not on the water engine's path" % handler_name)
         elif handler_name == "SingleIndependentActivePeriodicDirectionEndOfChainEventHandler":
             fields["chain_time"] = float(handler._chain_time)
+            end_of_chain_tags.add(tagger.tag)
         elif handler_name == "InitialChainStartOfRunEventHandler":
             velocity = list(handler._initial_velocity)
             direction = [i for i, v in enumerate(velocity) if v != 0.0]
@@ -165,9 +205,57 @@ def _translate_water(state_handler, activator, setting, roots, chains, mode, see
     for key in ("chain_time", "initial_direction", "lj_prefactor", "coulomb_prefactor"):
         if key not in fields:
             raise ConfigurationError("the water system lacks %s" % key)
+    cell_veto, root_positions = None, None
+    if cell_tags:
+        cell_veto = _water_cells(activator, fields, coulomb_taggers, boundary_tag, veto, pair_tags, cell_tags,
+                                 end_of_chain_tags, trash_lists)
+        root_positions = np.array([node.value.position for node in roots], dtype=np.float64)
     return WaterPlan(model=WaterModel(**fields), positions=positions, charges=charges,
                      end_of_run_time=end_of_run_time, chains=int(chains), mode=mode, seed=int(seed),
-                     events_per_launch=int(events_per_launch))
+                     events_per_launch=int(events_per_launch), roots=root_positions, cell_veto=cell_veto)
+
+
+def _water_cells(activator, fields, coulomb_taggers, boundary_tag, veto, pair_tags, cell_tags, end_of_chain_tags,
+                 trash_lists) -> dict:
+    """The molecular cells of a water configuration as the reference's water cell-veto configuration sets them up
+    (``config_files/2018_JCP_149_064113/water/coulomb_cell_veto_lj_inverted.ini``): one single-active cell
+    occupancy of the root units on cubic periodic cells, the nearby and surplus Coulomb factors, the molecular cell
+    veto with the dipole Monte Carlo estimator, and the cell boundary; every other event recreates every factor."""
+    if coulomb_taggers != {"ExcludedCellsTagger", "SurplusCellsTagger"} or boundary_tag is None or veto is None:
+        raise ConfigurationError("the molecular cells need the nearby and surplus Coulomb factors, the cell veto and "
+                                 "the cell boundary")
+    occupancies = [s for s in activator._internal_states if _name(s) == "SingleActiveCellOccupancy"]
+    if len(occupancies) != 1 or int(occupancies[0]._cell_level) != 1:
+        raise ConfigurationError("the molecular cells need one single-active cell occupancy of the root units")
+    occupancy = occupancies[0]
+    cells = occupancy._cells
+    if _name(cells) != "CuboidPeriodicCells" or len(set(cells._cells_per_side)) != 1:
+        raise ConfigurationError("the water engine needs cubic periodic cells")
+    if int(occupancy._maximum_number_occupants) != 1:
+        raise ConfigurationError("the molecular cells hold one occupant per cell")
+    if veto["lifting"] != fields["lifting"]:
+        raise ConfigurationError("the cell veto and the Coulomb factors lift with the same scheme")
+    estimator = veto["estimator"]
+    mic = estimator._potential
+    if _potential_kind(mic) != "MergedImageCoulomb" or (
+            float(mic._prefactor), float(mic._alpha), int(mic._fourier_cutoff), int(mic._position_cutoff)) != (
+            fields["coulomb_prefactor"], fields["alpha"], fields["fourier_cutoff"], fields["position_cutoff"]):
+        raise ConfigurationError("the dipole estimator bounds the Coulomb factors' merged-image potential")
+    everything = pair_tags | cell_tags
+    for tag, trashed in trash_lists.items():
+        if tag != boundary_tag and tag in everything | end_of_chain_tags and not everything <= trashed:
+            raise ConfigurationError("tagger %s must trash every pair and cell factor" % tag)
+    boundary_trash = trash_lists[boundary_tag] & everything
+    if boundary_trash == everything:
+        keep_pairs = False
+    elif boundary_trash == cell_tags:
+        keep_pairs = True
+    else:
+        raise ConfigurationError("the cell boundary trashes the cell factors, with or without the pair factors")
+    return dict(cells_per_side=int(cells._cells_per_side[0]), neighbor_layers=int(cells._neighbor_layers),
+                dipole_separation=float(estimator._dipole_separation), dipole_charge=float(estimator._dipole_charge),
+                prefactor=float(estimator._prefactor), number_trials=int(estimator._number_trials),
+                empirical_bound=float(estimator._empirical_bound), keep_pairs=keep_pairs)
 
 
 def translate(state_handler, activator, setting, chains: int = 1, mode: str = "mixed", seed: int = 0,
@@ -293,8 +381,13 @@ def run_plan(plan, stop_time: Optional[float] = None, device: str = "cuda:0"):
         import torch
         from jellyfysh_gb300.water import WaterBatch
         with torch.cuda.device(torch.device(device)):
+            cells, roots = None, None
+            if plan.cell_veto is not None:
+                from jellyfysh_gb300.water import dipole_cell_veto_bounds
+                cells = dipole_cell_veto_bounds(plan.model, seed=plan.seed, **plan.cell_veto)
+                roots = np.repeat(plan.roots[None], plan.chains, axis=0)
             batch = WaterBatch(plan.model, np.repeat(plan.positions[None], plan.chains, axis=0), seed=plan.seed,
-                               charges=plan.charges)
+                               charges=plan.charges, cells=cells, roots=roots)
             while True:
                 batch.run(plan.events_per_launch, stop_time=t_stop)
                 batch.check_status()

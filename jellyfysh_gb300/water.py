@@ -45,12 +45,15 @@ class WaterCells:
     (``config_files/2018_JCP_149_064113/water/coulomb_cell_veto_lj_inverted.ini``): cells_per_side^3 cuboid periodic
     cells of the molecules' root units with neighbor_layers layers of nearby cells, one occupant per cell, and the
     molecular cell veto's bound tables [cells][3] (upper and negated lower derivative bound of every relative cell
-    and direction; NaN for the nearby cells)."""
+    and direction; NaN for the nearby cells).  keep_pairs: the cell boundary's tagger trashes only the cell-based
+    factors (the reference's configuration: the bond and Lennard-Jones candidates outlive it); False: it trashes them
+    too."""
 
     cells_per_side: int
     neighbor_layers: int
     bounds_upper: np.ndarray
     bounds_lower: np.ndarray
+    keep_pairs: bool = True
 
     @property
     def cells(self) -> int:
@@ -59,7 +62,8 @@ class WaterCells:
 
 def dipole_cell_veto_bounds(model: "WaterModel", cells_per_side: int, neighbor_layers: int,
                             dipole_separation: float = 0.5, dipole_charge: float = 0.82, prefactor: float = 1.5,
-                            number_trials: int = 1000, empirical_bound: float = 30.0, seed: int = 0) -> WaterCells:
+                            number_trials: int = 1000, empirical_bound: float = 30.0, seed: int = 0,
+                            keep_pairs: bool = True) -> WaterCells:
     """The bound tables of the molecular cell veto as the reference's ``CellVetoEventHandler.initialize``
     (``event_handler/abstracts/cell_veto_event_handler.py:93-160``) fills them with the
     ``DipoleMonteCarloEstimator`` (``estimator/dipole_monte_carlo_estimator.py:74-155``): for every relative cell
@@ -122,7 +126,7 @@ def dipole_cell_veto_bounds(model: "WaterModel", cells_per_side: int, neighbor_l
     bounds_lower = np.full((cells, 3), np.nan)
     bounds_upper[far] = upper
     bounds_lower[far] = -np.maximum(-empirical_bound, -upper)
-    return WaterCells(m, int(neighbor_layers), bounds_upper, bounds_lower)
+    return WaterCells(m, int(neighbor_layers), bounds_upper, bounds_lower, bool(keep_pairs))
 
 
 def _cell_bounds(length: float, m: int):
@@ -248,7 +252,8 @@ class WaterBatch:
         upper = np.ascontiguousarray(cells.bounds_upper, dtype=np.float64).reshape(cells.cells, 3)
         lower = np.ascontiguousarray(cells.bounds_lower, dtype=np.float64).reshape(cells.cells, 3)
         _lib.check(self.lib.jfgpu_water_set_cells(self._handle, int(cells.cells_per_side), int(cells.neighbor_layers),
-                                                  upper.ctypes.data, lower.ctypes.data), "jfgpu_water_set_cells")
+                                                  upper.ctypes.data, lower.ctypes.data, int(bool(cells.keep_pairs))),
+                   "jfgpu_water_set_cells")
         M = self.model.molecules
         if roots is None:
             host = self.positions_dev.cpu().numpy()
@@ -319,7 +324,8 @@ class WaterBatch:
         self._torch.cuda.synchronize(self.device)
         extra = {}
         if self.cells is not None:
-            extra = dict(cells=json.dumps([self.cells.cells_per_side, self.cells.neighbor_layers]),
+            extra = dict(cells=json.dumps([self.cells.cells_per_side, self.cells.neighbor_layers,
+                                           bool(self.cells.keep_pairs)]),
                          bounds_upper=self.cells.bounds_upper, bounds_lower=self.cells.bounds_lower,
                          roots=self.roots_dev.cpu().numpy(), occupancy=self.occupancy_dev.cpu().numpy(),
                          surplus=self.surplus_dev.cpu().numpy(), cell_state=self.cell_state_dev.cpu().numpy())
@@ -332,8 +338,9 @@ class WaterBatch:
         data = np.load(path)
         cells = None
         if "cells" in data.files:
-            m, layers = json.loads(str(data["cells"]))
-            cells = WaterCells(int(m), int(layers), np.asarray(data["bounds_upper"]), np.asarray(data["bounds_lower"]))
+            m, layers, keep_pairs = json.loads(str(data["cells"]))
+            cells = WaterCells(int(m), int(layers), np.asarray(data["bounds_upper"]), np.asarray(data["bounds_lower"]),
+                               bool(keep_pairs))
         batch = cls(WaterModel(**json.loads(str(data["model"]))), np.asarray(data["positions"]), seed=int(data["seed"]),
                     first_chain=int(data["first_chain"]), charges=np.asarray(data["charges"]),
                     warps_per_block=int(data["warps_per_block"]), cells=cells,

@@ -124,7 +124,7 @@ def lib() -> ctypes.CDLL:
                                                ctypes.POINTER(ctypes.c_int)]
         handle.jfo_water_cells_create.restype = ctypes.c_void_p
         handle.jfo_water_cells_create.argtypes = [ctypes.POINTER(JfoWaterSystem), ctypes.c_int, ctypes.c_int, _PD,
-                                                  _PD, _PD, _PD, _PD, ctypes.POINTER(ctypes.c_int)]
+                                                  _PD, _PD, _PD, _PD, ctypes.c_int, ctypes.POINTER(ctypes.c_int)]
         handle.jfo_water_roots.argtypes = [ctypes.c_void_p, _PD]
         handle.jfo_chain_create.restype = ctypes.c_void_p
         handle.jfo_chain_create.argtypes = [ctypes.POINTER(JfoSystem), _PD, _PD, ctypes.POINTER(ctypes.c_int)]
@@ -491,9 +491,10 @@ def make_water_system(spec: dict, rng_key: int) -> JfoWaterSystem:
 
 class Water:
     """One chain of flexible water molecules run by the oracle.  With ``cells`` (cells_per_side, neighbor_layers,
-    roots [molecules][3], bounds_upper [cells][3], bounds_lower [cells][3]) the Coulomb interaction between molecules
-    goes through the molecular cells of the root units: nearby and surplus factors, the molecular cell veto with the
-    given bound tables and the cell-boundary events of the active root unit."""
+    roots [molecules][3], bounds_upper [cells][3], bounds_lower [cells][3][, keep_pairs]) the Coulomb interaction
+    between molecules goes through the molecular cells of the root units: nearby and surplus factors, the molecular
+    cell veto with the given bound tables and the cell-boundary events of the active root unit (across which the
+    bond and Lennard-Jones candidates persist unless keep_pairs is False)."""
 
     def __init__(self, system: JfoWaterSystem, positions: np.ndarray, charges: np.ndarray, cells=None):
         self.system = system
@@ -506,14 +507,15 @@ class Water:
             self._handle = lib().jfo_water_create(ctypes.byref(system), self._positions_in.ctypes.data_as(_PD),
                                                   self._charges_in.ctypes.data_as(_PD), ctypes.byref(status))
         else:
-            m, layers, roots, upper, lower = cells
+            m, layers, roots, upper, lower = cells[:5]
+            keep_pairs = bool(cells[5]) if len(cells) > 5 else True
             self._cells_in = [np.ascontiguousarray(a, dtype=np.float64) for a in (roots, upper, lower)]
             assert self._cells_in[0].shape == (system.molecules, 3)
             assert self._cells_in[1].shape == self._cells_in[2].shape == (m ** 3, 3)
             self._handle = lib().jfo_water_cells_create(
                 ctypes.byref(system), int(m), int(layers), self._positions_in.ctypes.data_as(_PD),
                 self._charges_in.ctypes.data_as(_PD), *[a.ctypes.data_as(_PD) for a in self._cells_in],
-                ctypes.byref(status))
+                int(keep_pairs), ctypes.byref(status))
         if not self._handle:
             raise OracleError("water creation failed: " + STATUS_NAMES.get(status.value, str(status.value)))
 

@@ -2038,6 +2038,7 @@ struct JfoWater {
     double root_speed;      /* the active root unit's velocity component: the leaf's times its weight 1/3 */
     /* the bond and Lennard-Jones candidates persist across molecular cell-boundary events: their earliest, and the
      * active leaf and root unit as their in-state holds them (time stamp snap_q, snap_r) */
+    int keep_pairs;         /* the cell boundary trashes only the cell-based factors */
     int pairs_valid;
     Cand pair;
     double snap_leaf[3], snap_root[3], snap_q, snap_r;
@@ -2289,7 +2290,8 @@ static int chain_install_bounds(JfoChain *c, const double *upper, const double *
 
 JfoWater *jfo_water_cells_create(const JfoWaterSystem *system, int cells_per_side, int neighbor_layers,
                                  const double *positions, const double *charges, const double *roots,
-                                 const double *bounds_upper, const double *bounds_lower, int *status) {
+                                 const double *bounds_upper, const double *bounds_lower, int keep_pairs,
+                                 int *status) {
     JfoWater *w = jfo_water_create(system, positions, charges, status);
     if (!w) return NULL;
     JfoSystem cs;
@@ -2324,6 +2326,7 @@ JfoWater *jfo_water_cells_create(const JfoWaterSystem *system, int cells_per_sid
         return NULL;
     }
     w->root_speed = system->speed * (1.0 / 3.0);
+    w->keep_pairs = keep_pairs ? 1 : 0;
     w->pairs_valid = 0;
     return w;
 }
@@ -2560,7 +2563,7 @@ static int64_t water_cells_run(JfoWater *w, int64_t max_events, JfoEvent *log, d
             return done;
         }
         /* every event but the cell boundary trashes the bond and Lennard-Jones candidates */
-        if (best.kind != JFO_EV_BOUNDARY) w->pairs_valid = 0;
+        if (best.kind != JFO_EV_BOUNDARY || !w->keep_pairs) w->pairs_valid = 0;
         ev.new_active = w->active;
         ev.new_direction = w->direction;
         ev.x = w->pos[3 * a];

@@ -224,10 +224,12 @@ int64_t jfo_water_run_roots(JfoWater *water, int64_t max_events, JfoEvent *log, 
 /* flexible water with molecular cells of root units (cells_per_side^3 cuboid periodic cells, neighbor_layers): the
  * Coulomb factor with the molecules of the nearby cells and the surplus molecules, the molecular cell veto with the
  * given bound tables ([cells][3] upper and negated lower bounds, NaN for the nearby cells) and the cell-boundary
- * events of the active root unit; roots [molecules][3] are the initial root positions */
+ * events of the active root unit; roots [molecules][3] are the initial root positions; keep_pairs: the bond and
+ * Lennard-Jones candidates outlive a cell boundary (its tagger trashes only the cell-based factors) */
 JfoWater *jfo_water_cells_create(const JfoWaterSystem *system, int cells_per_side, int neighbor_layers,
                                  const double *positions, const double *charges, const double *roots,
-                                 const double *bounds_upper, const double *bounds_lower, int *status);
+                                 const double *bounds_upper, const double *bounds_lower, int keep_pairs,
+                                 int *status);
 void jfo_water_roots(const JfoWater *water, double *roots);
 void jfo_water_positions(const JfoWater *water, double *positions);
 void jfo_water_state(const JfoWater *water, int64_t *event_count, int *active, int *direction, double *time_q,

@@ -156,3 +156,43 @@ def test_device_dipole_estimator_agrees_with_the_reference_tables(water):
     assert abs(np.median(ratio) - 1.0) < 0.05
     assert np.mean((ratio > 0.8) & (ratio < 1.25)) > 0.9
     assert np.all((ratio > 0.5) & (ratio < 2.0)), (ratio.min(), ratio.max())
+
+
+def test_drop_in_plan_with_molecular_cells_runs_to_its_end_of_run_time(water):
+    """The drop-in mediator's water plan with molecular cells (as ``plugin.plan`` reads it from the reference's water
+    cell-veto configuration): the bound tables from the device dipole estimator, every chain stopped at the end-of-run
+    time, the same chains as a batch built directly; with keep_pairs off the pair candidates do not outlive a cell
+    boundary, as the oracle's loop with that setting."""
+    from jellyfysh_gb300.plugin.plan import WaterPlan, run_plan
+    spec, data = load_water_cells("water_n8_cell_boundaries")
+    model = water.WaterModel.from_spec(spec)
+    cell_veto = dict(cells_per_side=spec["cells_per_side"], neighbor_layers=spec["neighbor_layers"],
+                     dipole_separation=spec["dipole_separation"], dipole_charge=spec["dipole_charge"],
+                     prefactor=spec["estimator_prefactor"], number_trials=200, empirical_bound=spec["empirical_bound"],
+                     keep_pairs=True)
+    plan = WaterPlan(model=model, positions=data["initial"], charges=data["charges"], end_of_run_time=40.0, chains=3,
+                     seed=spec["seed"], events_per_launch=300, roots=data["initial_roots"], cell_veto=cell_veto)
+    batch = run_plan(plan)
+    states = batch.states()
+    assert (states["stopped"] == 1).all() and (states["time_q"] + states["time_r"] == 40.0).all()
+    assert batch.cell_states()["boundary_events"].sum() > 0
+    cells = water.dipole_cell_veto_bounds(model, seed=spec["seed"], **cell_veto)
+    direct = water.WaterBatch(model, np.repeat(data["initial"][None], 3, axis=0), seed=spec["seed"],
+                              charges=data["charges"], cells=cells, roots=np.repeat(data["initial_roots"][None], 3, 0))
+    direct.run(int(states["events"][0]) + 10, stop_time=40.0)
+    assert np.array_equal(direct.positions(), batch.positions())
+    assert np.array_equal(direct.roots(), batch.roots())
+    # keep_pairs off against the oracle's loop with the same setting
+    trashing = water.WaterCells(spec["cells_per_side"], spec["neighbor_layers"], data["bounds_upper"],
+                                data["bounds_lower"], keep_pairs=False)
+    events = 2000
+    gpu = water.WaterBatch(model, data["initial"][None], seed=spec["seed"], charges=data["charges"], cells=trashing,
+                           roots=data["initial_roots"][None])
+    log, roots = gpu.run(events, record=True, record_roots=True)
+    gpu.check_status()
+    chain = oracle.Water(oracle.make_water_system(spec, spec["rng_key"]), data["initial"], data["charges"],
+                         cells=(spec["cells_per_side"], spec["neighbor_layers"], data["initial_roots"],
+                                data["bounds_upper"], data["bounds_lower"], False))
+    expected, expected_roots = chain.run(events, roots=True)
+    compare_logs(log[0], expected, model.system_length, roots[0], expected_roots)
+    assert np.sum(expected["kind"] == oracle.EV_BOUNDARY) > 10

@@ -230,6 +230,75 @@ def test_mediator_translates_the_reference_water_configuration(name):
     assert plan["end_of_run_time"] == 1e9
 
 
+def translate_water_cell_configuration(name, boundary_trashes_pairs="0"):
+    """The reference's factory builds the drop-in mediator from the water cell-veto configuration of a recorded
+    trajectory (run in a child); with boundary_trashes_pairs the molecule cell boundary trashes the pair factors too.
+    Returns the water plan."""
+    factory, camel = _reference()
+    sys.path.insert(0, os.path.join(ROOT, "tests", "golden"))
+    import tempfile
+    import make_water_cell_trajectories as cells
+    from tests.water_cases import load_water_cells
+    spec, data = load_water_cells(name)
+    initial, charges, roots = data["initial"], data["charges"], data["initial_roots"]
+    scratch = tempfile.mkdtemp()
+    factor_file = os.path.join(scratch, "factors.txt")
+    with open(factor_file, "w") as handle:
+        handle.write(cells.FACTORS.replace("[0, 1, 2, 3, 4, 5], Coulomb\n", ""))
+    text = cells.config_text(spec, factor_file)
+    text = text.replace("mediator = single_process_mediator", "mediator = gpu_chain_batch_mediator")
+    text = text.replace("[SingleProcessMediator]", "[GpuChainBatchMediator]\nchains = 3\nmode = mixed\nseed = 5")
+    if boundary_trashes_pairs == "1":
+        every = ", ".join(cells.PAIR_TAGS + cells.CELL_TAGS)
+        text = text.replace("[MoleculeCellBoundary]\ntrash = %s" % ", ".join(cells.CELL_TAGS),
+                            "[MoleculeCellBoundary]\ntrash = %s" % every)
+    config = configparser.ConfigParser()
+    config.read_string(text)
+    from jellyfysh.base.node import Node
+    from jellyfysh.base.particle import Particle
+    from jellyfysh.input_output_handler.input_handler.random_node_creator import water_random_node_creator
+    queue = list(range(len(initial) // 3))
+
+    def fill_root_node(self, node):
+        m = queue.pop(0)
+        for t in range(3):
+            node.add_child(Node(Particle([float(v) for v in initial[3 * m + t]],
+                                         {"electric_charge": float(charges[3 * m + t])})))
+        node.value = Particle(position=[float(v) for v in roots[m]])
+    water_random_node_creator.WaterRandomNodeCreator.fill_root_node = fill_root_node
+    factory.build_from_config(config, camel(config.get("Run", "setting")), "jellyfysh.setting")
+    mediator = factory.build_from_config(config, camel(config.get("Run", "mediator")), "jellyfysh.mediator")
+    plan = mediator.plan
+    return {"type": type(plan).__name__, "model": dataclasses.asdict(plan.model), "positions": plan.positions.tolist(),
+            "roots": plan.roots.tolist(), "cell_veto": plan.cell_veto, "charges": plan.charges.tolist()}
+
+
+@pytest.mark.parametrize("name", ["water_n8_cell_veto", "water_n64_cell_veto"])
+def test_mediator_translates_the_reference_water_cell_veto_configuration(name):
+    """The reference's water cell-veto configuration (with this project's water model) becomes a water plan with
+    molecular cells: the cell system, the dipole estimator's parameters, the root units, and the pair candidates kept
+    across cell boundaries exactly when the boundary's tagger leaves them out of its trash list."""
+    from tests.water_cases import load_water_cells
+    spec, data = load_water_cells(name)
+    plan = _in_child("translate_water_cell_configuration", name)
+    assert plan["type"] == "WaterPlan"
+    for key in ("system_length", "beta", "chain_time", "oh_r0", "hh_prefactor", "lj_sigma", "coulomb_prefactor",
+                "bound_prefactor", "alpha", "fourier_cutoff", "position_cutoff", "initial_active", "lifting"):
+        assert plan["model"][key] == spec[key], key
+    cell_veto = plan["cell_veto"]
+    assert (cell_veto["cells_per_side"], cell_veto["neighbor_layers"]) == (spec["cells_per_side"],
+                                                                           spec["neighbor_layers"])
+    assert (cell_veto["dipole_separation"], cell_veto["dipole_charge"], cell_veto["prefactor"],
+            cell_veto["number_trials"], cell_veto["empirical_bound"]) == (
+        spec["dipole_separation"], spec["dipole_charge"], spec["estimator_prefactor"], spec["number_trials"],
+        spec["empirical_bound"])
+    assert cell_veto["keep_pairs"] is True
+    assert np.array_equal(np.array(plan["roots"]), data["initial_roots"])
+    assert np.array_equal(np.array(plan["positions"]), data["initial"])
+    trashing = _in_child("translate_water_cell_configuration", name, "1")
+    assert trashing["cell_veto"]["keep_pairs"] is False
+
+
 def reference_separation_file(path):
     """The reference's SeparationOutputHandler writing one sample of a fixed configuration (run in a child)."""
     if TREE not in sys.path:
