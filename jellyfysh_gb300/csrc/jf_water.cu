@@ -71,10 +71,16 @@ struct WaterCand {
     int kind, target;
 };
 
-// the earliest time; on equal times the lower kind, then the lower target (as the oracle orders candidates)
+// the earliest time; on equal times the lower kind, then the lower target (as the oracle orders candidates).  The
+// quotient and remainder of a time are non-negative (never -0.0, as Python's divmod gives) or +inf, so their IEEE
+// bit patterns order as the values do: the comparison runs on integers, off GB300's scarce FP64 pipe.
 __device__ inline bool water_better(const WaterCand &a, const WaterCand &b) {
-    if (time_lt(a.q, a.r, b.q, b.r)) return true;
-    if (time_lt(b.q, b.r, a.q, a.r)) return false;
+    const unsigned long long aq = (unsigned long long)__double_as_longlong(a.q);
+    const unsigned long long bq = (unsigned long long)__double_as_longlong(b.q);
+    if (aq != bq) return aq < bq;
+    const unsigned long long ar = (unsigned long long)__double_as_longlong(a.r);
+    const unsigned long long br = (unsigned long long)__double_as_longlong(b.r);
+    if (ar != br) return ar < br;
     if (a.kind != b.kind) return a.kind < b.kind;
     return a.target < b.target;
 }
@@ -662,14 +668,19 @@ __device__ inline int water_occupancy_update(const WaterCells &cl, JfgpuWaterCel
     return water_cell_of(cl, roots + 3 * m, cs.occ_cell);
 }
 
-// The single candidates of the active molecule in cell `cell`: the molecular cell veto
-// (abstracts/cell_veto_event_handler.py:200-238 with the charge factor of
-// DipoleMonteCarloEstimator.charge_correction_factor without target charges: the active unit's charge) and the
-// cell boundary of the active root unit at root (cell_boundary_event_handler.py:98-156).
-__device__ inline int water_single_candidates(const WaterModel &w, uint64_t key, uint64_t ev, int cell, int d,
-                                              double ca, const double *root, double ts_q, double ts_r,
-                                              WaterCand &single, int &veto_cell, double &veto_rate,
-                                              double &boundary) {
+__device__ inline void water_no_candidate(WaterCand &c) {
+    c.q = INFINITY;
+    c.r = INFINITY;
+    c.kind = 1 << 30;
+    c.target = 1 << 30;
+}
+
+// The molecular cell veto of the active molecule in cell `cell` (abstracts/cell_veto_event_handler.py:200-238 with
+// the charge factor of DipoleMonteCarloEstimator.charge_correction_factor without target charges: the active unit's
+// charge)
+__device__ inline int water_veto_candidate(const WaterModel &w, uint64_t key, uint64_t ev, int cell, int d, double ca,
+                                           double ts_q, double ts_r, WaterCand &veto, int &veto_cell,
+                                           double &veto_rate) {
     const WaterCells &cl = w.cells;
     double charge_factor = ca;
     int which = 0;
@@ -690,16 +701,22 @@ __device__ inline int water_single_candidates(const WaterModel &w, uint64_t key,
     veto_cell = cl.tra[a[0] * cl.m + b[0]] + cl.m * cl.tra[a[1] * cl.m + b[1]] +
                 cl.m * cl.m * cl.tra[a[2] * cl.m + b[2]];
     const double dt = expovariate(draw(key, ev, kRngVetoTime, 0), w.beta) / (total_rate * w.speed);
-    single.q = INFINITY;
-    single.r = INFINITY;
-    single.kind = 1 << 30;
-    single.target = 1 << 30;
-    water_offer(single, ts_q, ts_r, dt, JFGPU_EV_CELL_VETO, -1);
+    water_no_candidate(veto);
+    water_offer(veto, ts_q, ts_r, dt, JFGPU_EV_CELL_VETO, -1);
+    return JFGPU_STATUS_OK;
+}
+
+// The cell boundary of the active root unit at root in cell `cell` (cell_boundary_event_handler.py:98-156)
+__device__ inline void water_boundary_candidate(const WaterModel &w, int cell, int d, const double *root,
+                                                double ts_q, double ts_r, WaterCand &bnd, double &boundary) {
+    const WaterCells &cl = w.cells;
+    int a[3];
+    water_cell_axes(cl, cell, a);
     boundary = cl.cell_min[a[d] + 1 == cl.m ? 0 : a[d] + 1];
     double sep = boundary - root[d];
     if (sep < 0.0) sep = sep + w.length;
-    water_offer(single, ts_q, ts_r, sep / cl.root_speed, JFGPU_EV_BOUNDARY, -1);
-    return JFGPU_STATUS_OK;
+    water_no_candidate(bnd);
+    water_offer(bnd, ts_q, ts_r, sep / cl.root_speed, JFGPU_EV_BOUNDARY, -1);
 }
 
 __device__ inline void block_reduce_cand(WaterCand &best, WaterCand *warp_slots, int lane, int warp, int warps) {
@@ -741,9 +758,9 @@ __global__ void __launch_bounds__(256, 2) water_cells_kernel(WaterArgs a) {
     int *chunk_count = list + water_items_max(M);
     int *targets = chunk_count + water_chunks_max(M);
     __shared__ int status, single_status, n_targets, veto_cell, pp_active;
-    __shared__ float single_bound;
+    __shared__ float veto_bound, other_bound;
+    __shared__ WaterCand veto, bnd;
     float *pp32 = reinterpret_cast<float *>(targets + M);  // [3 M]
-    __shared__ WaterCand single;
     __shared__ double veto_rate, boundary;
     __shared__ double bound[3], pair[3], cross[9];
     __shared__ float pair32[3], error32[3];
@@ -767,18 +784,29 @@ __global__ void __launch_bounds__(256, 2) water_cells_kernel(WaterArgs a) {
             n_targets = 0;
             status = water_occupancy_update(cl, cs, occ, sur, roots, m);
         }
-        if (threadIdx.x == (warps > 1 ? 32 : 0)) {
+        // the cell veto (the first thread of the second warp) and the cell boundary with the bounds of the end of
+        // chain and of a kept pair candidate (the first thread of the third warp), each from the cell of the active
+        // root unit, beside the occupancy update; with fewer warps the same threads take more of them
+        const int veto_thread = warps > 1 ? 32 : 0, boundary_thread = warps > 2 ? 64 : veto_thread;
+        if (threadIdx.x == veto_thread) {
             int cell;
             int st = water_cell_of(cl, roots + 3 * m, cell);
-            if (!st)
-                st = water_single_candidates(w, key, ev, cell, d, ca, roots + 3 * m, ts_q, ts_r, single, veto_cell,
-                                             veto_rate, boundary);
+            if (!st) st = water_veto_candidate(w, key, ev, cell, d, ca, ts_q, ts_r, veto, veto_cell, veto_rate);
+            veto_bound = __double2float_ru(time_sub(veto.q, veto.r, ts_q, ts_r));
+            single_status = st;
+        }
+        if (threadIdx.x == boundary_thread) {
             // the time since the time stamp that these candidates surely reach, rounded up (the screen's bound)
-            float sb = __double2float_ru(time_sub(single.q, single.r, ts_q, ts_r));
+            int cell;
+            if (water_cell_of(cl, roots + 3 * m, cell) == JFGPU_STATUS_OK) {
+                water_boundary_candidate(w, cell, d, roots + 3 * m, ts_q, ts_r, bnd, boundary);
+            } else {
+                water_no_candidate(bnd);  // the veto thread reports the cell error
+            }
+            float sb = __double2float_ru(time_sub(bnd.q, bnd.r, ts_q, ts_r));
             sb = fminf(sb, __double2float_ru(time_sub(s.eoc_q, s.eoc_r, ts_q, ts_r)));
             if (cs.pairs_valid) sb = fminf(sb, __double2float_ru(time_sub(cs.pair_q, cs.pair_r, ts_q, ts_r)));
-            single_bound = sb;
-            single_status = st;
+            other_bound = sb;
         }
         if (act != pp_active) {
             // the FP32 prefactors of the Coulomb screen for a new active unit
@@ -787,6 +815,8 @@ __global__ void __launch_bounds__(256, 2) water_cells_kernel(WaterArgs a) {
         }
         __syncthreads();
         if (threadIdx.x == 0) pp_active = act;
+        const WaterCand single = water_better(bnd, veto) ? bnd : veto;
+        const float single_bound = fminf(veto_bound, other_bound);
         if (status != JFGPU_STATUS_OK || single_status != JFGPU_STATUS_OK) {
             if (threadIdx.x == 0) s.status = status != JFGPU_STATUS_OK ? status : single_status;
             break;
