@@ -384,6 +384,35 @@ def reference_arm(args):
     print(json.dumps(line))
 
 
+def drop_in_costs(args, calls=200, pairs=30):
+    """Wall time of one call of the drop-in layer from Python: a GpuLennardJonesPotential.displacement (one pair, one
+    launch with its copies, as the reference's TwoLeafUnitEventHandler makes it per pair and event) and a
+    GpuNeighbourhoodEventHandler solve of `pairs` pairs (one launch per event for the whole neighbourhood)."""
+    from jellyfysh_gb300.plugin.potential._common import earliest
+    from jellyfysh_gb300.plugin.potential.gpu_lennard_jones_potential import GpuLennardJonesPotential
+    potential = GpuLennardJonesPotential(1.0, 1.0)
+    rng = np.random.default_rng(5)
+    separations = rng.uniform(-2.5, 2.5, (pairs, 3))
+    separations = separations[np.linalg.norm(separations, axis=1) > 0.9]
+    changes = rng.exponential(1.2, len(separations))
+    for _ in range(10):
+        potential.displacement([1.0, 0.0, 0.0], list(separations[0]), float(changes[0]))
+        earliest(potential, [1.0, 0.0, 0.0], separations, None, changes)
+    start = time.perf_counter()
+    for k in range(calls):
+        potential.displacement([1.0, 0.0, 0.0], list(separations[k % len(separations)]),
+                               float(changes[k % len(separations)]))
+    single = (time.perf_counter() - start) / calls
+    start = time.perf_counter()
+    for _ in range(calls):
+        earliest(potential, [1.0, 0.0, 0.0], separations, None, changes)
+    batched = (time.perf_counter() - start) / calls
+    return {"potential_call_us": single * 1e6, "neighbourhood_call_us": batched * 1e6,
+            "neighbourhood_pairs": int(len(separations)),
+            "note": "wall time per call from Python, one GPU launch and its host copies each; the reference's "
+                    "CPython LennardJonesPotential.displacement takes about 7 us a pair"}
+
+
 def gpu_arm(args):
     import torch
     import torch.distributed as dist
@@ -509,6 +538,9 @@ def gpu_arm(args):
         fp64["speedup_of_batched_mixed"] = value / fp64["value"]
         fp64["sample"] = "64 chains x 16 events, one launch per chain"
 
+    # the drop-in layer's per-call cost, where the reference's own mediator calls it once per pair or per event
+    drop_in = drop_in_costs(args) if args.workload == "lennard_jones" and not args.no_fp64 else None
+
     # parity of the benchmarked run: chains of the batch replayed from their initial state in the FP64 path for the
     # events they ran in the mixed path, bit for bit, and the event log of their first events against the oracle
     parity = None
@@ -578,7 +610,8 @@ def gpu_arm(args):
             "e2e": {"value": e2e_value, "unit": "events/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "pipelining": "two batches take the steps in turn; each batch's copies overlap the other's run"},
             "roofline": roofline, "cpu_baseline": cpu, "gpu_launches": launches, "clocks": clocks.summary(),
-            "fp64_batched": fp64_batched, "fp64_one_chain_per_launch": fp64, "parity": parity}
+            "fp64_batched": fp64_batched, "fp64_one_chain_per_launch": fp64, "parity": parity,
+            "drop_in": drop_in}
     print(json.dumps(line))
     if world > 1:
         dist.barrier()

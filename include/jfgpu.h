@@ -402,7 +402,8 @@ typedef struct {
     int32_t pairs_valid;          /* the candidate above is alive (created, then only cell-boundary events) */
     int32_t occ_active, occ_cell; /* the occupancy's active molecule (-1: none) and its cell */
     int32_t reserved;
-    int64_t boundary_events, veto_events, veto_targets;
+    int64_t boundary_events;
+    int64_t veto_events, veto_targets;  /* far-field events (cell veto or cell bounding) and those with a target */
 } JfgpuWaterCellState;
 
 typedef struct {
@@ -420,9 +421,12 @@ typedef struct {
  * CellVetoEventHandler._derivative_bounds, abstracts/cell_veto_event_handler.py:134-160; NaN for the nearby cells),
  * from which the Walker tables are built in the reference's order.  cells_per_side 1..32.  keep_pairs: the cell
  * boundary's tagger trashes only the cell-based factors, so the bond and Lennard-Jones candidates outlive it (the
- * reference's water cell-veto configuration); 0: it trashes them too. */
+ * reference's water cell-veto configuration); 0: it trashes them too.  far: JFGPU_FAR_CELL_VETO (the molecular cell
+ * veto) or JFGPU_FAR_CELL_BOUNDING (CellBoundingPotentialTagger with TwoCompositeObjectCellBoundingPotentialEventHandler,
+ * two_composite_object_cell_bounding_potential_event_handler.py:153-265: a factor for every occupied far cell, the
+ * charge factor over dipole_charge as DipoleMonteCarloEstimator.charge_correction_factor forms it). */
 int jfgpu_water_set_cells(void *water, int32_t cells_per_side, int32_t neighbor_layers, const double *bounds_upper,
-                          const double *bounds_lower, int32_t keep_pairs);
+                          const double *bounds_lower, int32_t keep_pairs, int32_t far, double dipole_charge);
 /* the occupancy of chains first .. first + chains - 1 from their roots (root nodes in order, the first molecule of a
  * cell its occupant, the others surplus) and a fresh cell state; with jfgpu_water_init for the rest of the state */
 int jfgpu_water_cells_init(void *water, const JfgpuWaterCellBuffers *buffers, int64_t chains, void *stream);

@@ -145,7 +145,7 @@ SIGNATURES = {
     "jfgpu_water_destroy": (None, [_P]),
     "jfgpu_water_init": (ctypes.c_int, [_P, _P, _I64, _I64, _P]),
     "jfgpu_water_run": (ctypes.c_int, [_P, _P, _P, _P, _I64, _I64, _I64, _D, _D, _P, _I32, _P]),
-    "jfgpu_water_set_cells": (ctypes.c_int, [_P, _I32, _I32, _P, _P, _I32]),
+    "jfgpu_water_set_cells": (ctypes.c_int, [_P, _I32, _I32, _P, _P, _I32, _I32, _D]),
     "jfgpu_water_cells_init": (ctypes.c_int, [_P, ctypes.POINTER(WaterCellBuffers), _I64, _P]),
     "jfgpu_water_cells_run": (ctypes.c_int, [_P, _P, _P, _P, ctypes.POINTER(WaterCellBuffers), _I64, _I64, _I64,
                                              _D, _D, _P, _I32, _P]),

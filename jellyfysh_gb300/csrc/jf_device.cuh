@@ -156,7 +156,7 @@ __host__ __device__ inline uint64_t draw(uint64_t key, uint64_t event, uint32_t 
 }
 
 enum RngKind : uint32_t { kRngPair = 0, kRngThin = 1, kRngVetoTime = 2, kRngVetoChoice = 3, kRngVetoUniform = 4,
-                          kRngNewActive = 5, kRngComposite = 6, kRngLift = 7 };
+                          kRngNewActive = 5, kRngComposite = 6, kRngLift = 7, kRngCellBound = 8 };
 
 __host__ __device__ inline double uniform53(uint64_t bits) { return (double)(bits >> 11) * (1.0 / 9007199254740992.0); }
 

@@ -26,6 +26,8 @@ namespace jf {
 struct WaterCells {
     int m, ncells, n_off;
     int keep_pairs;           // the bond and Lennard-Jones candidates outlive a cell boundary
+    int far;                  // JFGPU_FAR_CELL_VETO, or JFGPU_FAR_CELL_BOUNDING (a factor for every occupied far cell)
+    double dipole_charge;     // the estimator's dipole charge (the cell-bounding charge factor)
     int offsets[32];          // the distinct residues of -layers .. layers modulo m, ascending
     double side;              // L / m: position_to_cell is int(x / side) along every axis
     double inv_side;          // 1 / side, the first guess of int(x / side)
@@ -33,6 +35,7 @@ struct WaterCells {
     const double *cell_min;   // [m] exact lower cell bounds along an axis
     const double *cell_max;   // [m] exact upper cell bounds along an axis
     const int16_t *tra;       // [m * m] translate along one axis, [a * m + b]
+    const int16_t *rel;       // [m * m] relative_cell along one axis, [a * m + b]
     const double *bound_upper, *bound_lower;  // [ncells][3] upper and negated lower bounds
     WalkerDev walker[2][3];   // [upper / lower][direction]
 };
@@ -124,6 +127,22 @@ __host__ __device__ inline int water_items_max(int molecules) {
 
 // chunks of 32 items (one warp's share of a round)
 __host__ __device__ inline int water_chunks_max(int molecules) { return (water_items_max(molecules) + 31) >> 5; }
+
+// candidate items of an event of the kernel with molecular cells at most: the Coulomb items of the nearby and
+// surplus molecules in three warp-padded groups, the far cell-bounding items padded to whole warps, Lennard-Jones, two
+// bonds (the target molecules of the two lists together are at most molecules - 1)
+__host__ __device__ inline int water_cells_items_max(int molecules) {
+    return 4 * (((molecules - 1) + 31) & ~31) + (molecules - 1) + 2;
+}
+
+// dynamic shared memory of the kernel with molecular cells: per-item lower bounds (float), the item list (int), the
+// taken count of every chunk of 32 items (int), the target list [molecules], the screen's prefactors [3 molecules] and
+// the far target list [molecules]
+__host__ inline size_t water_cells_shared_bytes(int molecules) {
+    const int items = water_cells_items_max(molecules);
+    return (size_t)items * (sizeof(float) + sizeof(int)) + (size_t)((items + 31) >> 5) * sizeof(int) +
+           sizeof(int) * 5 * (size_t)molecules;
+}
 
 // per-item lower bounds (float), the item list (int), the taken count of every chunk (int)
 __host__ inline size_t water_shared_bytes(int molecules) {
@@ -719,6 +738,39 @@ __device__ inline void water_boundary_candidate(const WaterModel &w, int cell, i
     water_offer(bnd, ts_q, ts_r, sep / cl.root_speed, JFGPU_EV_BOUNDARY, -1);
 }
 
+// The molecular cell-bounding factor of the active unit (charge ca, direction d) with molecule `other` in a far
+// cell (two_composite_object_cell_bounding_potential_event_handler.py:153-207): the relative cell of the target's root
+// cell to the active cell (asserted not nearby), the bound of that cell and direction times the charge factor
+// (CellBoundingPotential.standard_velocity_displacement, cell_bounding_potential.py:155-198, with
+// DipoleMonteCarloEstimator.charge_correction_factor); rate per unit length, time for the potential change du.
+__device__ inline int water_cell_bound(const WaterModel &w, const double *roots, const double *charge, int other,
+                                       int active_cell, int d, double ca, double du, double &rate, double &time) {
+    const WaterCells &cl = w.cells;
+    int target_cell;
+    JF_TRY(water_cell_of(cl, roots + 3 * other, target_cell));
+    int a[3], b[3];
+    water_cell_axes(cl, target_cell, a);
+    water_cell_axes(cl, active_cell, b);
+    int rc = 0;
+    bool near = true;
+    for (int k = 2; k >= 0; --k) {
+        const int r = cl.rel[a[k] * cl.m + b[k]];
+        rc = rc * cl.m + r;
+        bool in = false;
+        for (int o = 0; o < cl.n_off; ++o) in = in || cl.offsets[o] == r;
+        near = near && in;
+    }
+    if (near) return JFGPU_STATUS_ASSERTION;  // the tagger yields far cells only
+    double upper[3], lower[3], velocity[3] = {0.0, 0.0, 0.0};
+    for (int k = 0; k < 3; ++k) {
+        upper[k] = cl.bound_upper[rc * 3 + k];
+        lower[k] = -cl.bound_lower[rc * 3 + k];  // stored negated
+    }
+    velocity[d] = w.speed;
+    return composite_cell_bound_time(upper, lower, velocity, ca, charge + 3 * other, 3, cl.dipole_charge, du, rate,
+                                     time);
+}
+
 __device__ inline void block_reduce_cand(WaterCand &best, WaterCand *warp_slots, int lane, int warp, int warps) {
     for (int offset = 16; offset > 0; offset >>= 1) shuffle_better(best, offset);
     if (lane == 0) warp_slots[warp] = best;
@@ -753,11 +805,13 @@ __global__ void __launch_bounds__(256, 2) water_cells_kernel(WaterArgs a) {
     __shared__ WaterCand warp_best[kMaxWarps], warp_pair[kMaxWarps];
     __shared__ float warp_upper[kMaxWarps], warp_pair_upper[kMaxWarps];
     extern __shared__ float dynamic[];
+    const int items_cap = water_cells_items_max(M);
     float *lower = dynamic;
-    int *list = reinterpret_cast<int *>(dynamic + water_items_max(M));
-    int *chunk_count = list + water_items_max(M);
-    int *targets = chunk_count + water_chunks_max(M);
-    __shared__ int status, single_status, n_targets, veto_cell, pp_active;
+    int *list = reinterpret_cast<int *>(dynamic + items_cap);
+    int *chunk_count = list + items_cap;
+    int *targets = chunk_count + ((items_cap + 31) >> 5);
+    int *far_targets = targets + 4 * M;  // after the screen's prefactors [3 M]
+    __shared__ int status, single_status, n_targets, n_far, veto_cell, pp_active;
     __shared__ float veto_bound, other_bound;
     __shared__ WaterCand veto, bnd;
     float *pp32 = reinterpret_cast<float *>(targets + M);  // [3 M]
@@ -782,6 +836,7 @@ __global__ void __launch_bounds__(256, 2) water_cells_kernel(WaterArgs a) {
         // (the first thread of the second warp, or thread 0 of a one-warp block)
         if (threadIdx.x == 0) {
             n_targets = 0;
+            n_far = 0;
             status = water_occupancy_update(cl, cs, occ, sur, roots, m);
         }
         // the cell veto (the first thread of the second warp) and the cell boundary with the bounds of the end of
@@ -791,7 +846,11 @@ __global__ void __launch_bounds__(256, 2) water_cells_kernel(WaterArgs a) {
         if (threadIdx.x == veto_thread) {
             int cell;
             int st = water_cell_of(cl, roots + 3 * m, cell);
-            if (!st) st = water_veto_candidate(w, key, ev, cell, d, ca, ts_q, ts_r, veto, veto_cell, veto_rate);
+            if (cl.far == JFGPU_FAR_CELL_VETO) {
+                if (!st) st = water_veto_candidate(w, key, ev, cell, d, ca, ts_q, ts_r, veto, veto_cell, veto_rate);
+            } else {
+                water_no_candidate(veto);  // the cell-bounding factors are items of the block's screen
+            }
             veto_bound = __double2float_ru(time_sub(veto.q, veto.r, ts_q, ts_r));
             single_status = st;
         }
@@ -838,9 +897,26 @@ __global__ void __launch_bounds__(256, 2) water_cells_kernel(WaterArgs a) {
                 }
                 if (other >= 0) targets[atomicAdd(&n_targets, 1)] = other;
             }
+            if (cl.far == JFGPU_FAR_CELL_BOUNDING) {
+                // CellBoundingPotentialTagger: the occupant of every occupied cell that is not nearby
+                for (int k = threadIdx.x; k < cl.ncells; k += blockDim.x) {
+                    const int other = occ[k];
+                    if (other < 0) continue;
+                    int c[3];
+                    water_cell_axes(cl, k, c);
+                    bool near = true;
+                    for (int axis = 0; axis < 3; ++axis) {
+                        const int r = (c[axis] - ax[axis] + cl.m) % cl.m;
+                        bool in = false;
+                        for (int o = 0; o < cl.n_off; ++o) in = in || cl.offsets[o] == r;
+                        near = near && in;
+                    }
+                    if (!near) far_targets[atomicAdd(&n_far, 1)] = other;
+                }
+            }
         }
         __syncthreads();
-        const int nt = n_targets;
+        const int nt = n_targets, nf = n_far;
         const bool new_pairs = !cs.pairs_valid;
         double pa[3], pr[3], pa0[3], pr0[3];
         for (int c = 0; c < 3; ++c) {
@@ -857,11 +933,13 @@ __global__ void __launch_bounds__(256, 2) water_cells_kernel(WaterArgs a) {
         best.r = pbest.r = INFINITY;
         best.kind = pbest.kind = 1 << 30;
         best.target = pbest.target = 1 << 30;
-        const int group = (nt + 31) & ~31, n_coulomb = 3 * group;
+        // items: the Coulomb factors' units by unit type, the far cell-bounding factors, the pair items
+        const int group = (nt + 31) & ~31, n_near_items = 3 * group;
+        const int n_coulomb = n_near_items + ((nf + 31) & ~31);
         const int n_lj = new_pairs && t == 1 ? M - 1 : 0, n_pairs = new_pairs ? n_lj + 2 : 0;
         const int items = n_coulomb + n_pairs;
         const bool mixed = w.mode == JFGPU_MODE_MIXED;
-        int st = JFGPU_STATUS_OK, refined = nt * 3 + n_pairs;
+        int st = JFGPU_STATUS_OK, refined = nt * 3 + nf + n_pairs;
         // phase A: the pair items in FP64; the Coulomb items in FP64 (exact mode) or screened in FP32 (mixed mode:
         // lower[item] = the earliest time the item may reach, -inf where the screen cannot decide)
         float mine = INFINITY, pair_mine = INFINITY;
@@ -881,6 +959,35 @@ __global__ void __launch_bounds__(256, 2) water_cells_kernel(WaterArgs a) {
                     continue;
                 }
                 st = pair_item_exact(w, pos, key, ev, k, n_lj, m, t, d, pa, ts_q, ts_r, pbest);
+                continue;
+            }
+            if (item >= n_near_items) {
+                // a far cell-bounding factor: its bound times the charge factor, the potential change keyed by the
+                // target molecule; screened in FP32 with the potential change's FP32 error (24 units of 2^-24) and
+                // the roundings of the rate and the division, taken as 64 units
+                const int f = item - n_near_items;
+                if (f >= nf) {
+                    lower[item] = INFINITY;  // padding
+                    continue;
+                }
+                const int other = far_targets[f];
+                const uint64_t bits = draw(key, ev, kRngCellBound, (uint32_t)other);
+                if (mixed) {
+                    const uint64_t n = bits >> 11;
+                    const float du32 = n < (1ull << 52) ? -log1pf(-(float)n * 0x1p-53f) / w.beta32
+                                                        : -logf((float)((1ull << 53) - n) * 0x1p-53f) / w.beta32;
+                    double rate, time;
+                    st = water_cell_bound(w, roots, charge, other, cs.occ_cell, d, ca, 1.0, rate, time);
+                    if (st) continue;
+                    const float t32 = rate > 0.0 ? du32 / (float)rate / w.speed32 : INFINITY;
+                    lower[item] = t32 * (1.f - 64.f * 0x1p-24f);
+                    mine = fminf(mine, t32 * (1.f + 64.f * 0x1p-24f));
+                } else {
+                    double rate, time;
+                    st = water_cell_bound(w, roots, charge, other, cs.occ_cell, d, ca, expovariate(bits, w.beta),
+                                          rate, time);
+                    if (!st) water_offer(best, ts_q, ts_r, time, JFGPU_EV_CELL_BOUNDING, other);
+                }
                 continue;
             }
             const int j = item / group, k = item % group;
@@ -957,6 +1064,17 @@ __global__ void __launch_bounds__(256, 2) water_cells_kernel(WaterArgs a) {
                 const int item = list[v];
                 if (item >= n_coulomb) {
                     st = pair_item_exact(w, pos, key, ev, item - n_coulomb, n_lj, m, t, d, pa, ts_q, ts_r, pbest);
+                    continue;
+                }
+                if (item >= n_near_items) {
+                    const int f = item - n_near_items;
+                    if (f >= nf) continue;  // padding
+                    const int other = far_targets[f];
+                    double rate, time;
+                    st = water_cell_bound(w, roots, charge, other, cs.occ_cell, d, ca,
+                                          expovariate(draw(key, ev, kRngCellBound, (uint32_t)other), w.beta), rate,
+                                          time);
+                    if (!st) water_offer(best, ts_q, ts_r, time, JFGPU_EV_CELL_BOUNDING, other);
                     continue;
                 }
                 if (item % group >= nt) continue;  // padding (listed only under an infinite bound)
@@ -1040,13 +1158,29 @@ __global__ void __launch_bounds__(256, 2) water_cells_kernel(WaterArgs a) {
         }
         int accepted = 1;
         int other = -1;
+        double given_rate = veto_rate;
         if (best.kind == JFGPU_EV_COMPOSITE) other = best.target;
         if (best.kind == JFGPU_EV_CELL_VETO) {
             other = occ[veto_cell];  // the occupant of the sampled cell (Mediator.get_arguments_cell_veto_event_handler)
             accepted = 0;
         }
+        if (best.kind == JFGPU_EV_CELL_BOUNDING) {
+            // send_out_state (:209-265): the active root is still in the candidate's cell (the reference has no
+            // out-state otherwise), and the thinning draws against the bounding event rate times the speed
+            other = best.target;
+            int now_cell;
+            double rate, time;
+            int cst = water_cell_of(cl, pr, now_cell);
+            if (!cst && now_cell != cs.occ_cell) cst = JFGPU_STATUS_ASSERTION;
+            if (!cst) cst = water_cell_bound(w, roots, charge, other, cs.occ_cell, d, ca, 1.0, rate, time);
+            if (cst) {
+                if (threadIdx.x == 0) s.status = cst;
+                other = -1;
+            }
+            given_rate = rate * w.speed;
+        }
         if (other >= 0) {
-            const bool veto = best.kind == JFGPU_EV_CELL_VETO;
+            const bool veto = best.kind == JFGPU_EV_CELL_VETO || best.kind == JFGPU_EV_CELL_BOUNDING;
             const double *locals = pos + 9 * m, *targets_pos = pos + 9 * other;
             double draws[3];
             draws[0] = uniform53(draw(key, ev, kRngThin, 0));
@@ -1079,7 +1213,7 @@ __global__ void __launch_bounds__(256, 2) water_cells_kernel(WaterArgs a) {
             if (mixed) {
                 // max(0, factor) <= uniform(0, bounding rate) is certain when the factor's upper bound stays below
                 // the draw times a lower bound of the bounding rate
-                double bounding = veto_rate;
+                double bounding = given_rate;
                 if (!veto) {
                     float sum = 0.f;
                     for (int j = 0; j < 3; ++j) sum += fmaxf((float)bound[j], 0.f);
@@ -1113,9 +1247,9 @@ __global__ void __launch_bounds__(256, 2) water_cells_kernel(WaterArgs a) {
                 double target_factor[3], bounding_rate, event_rate;
                 bool confirmed = false;
                 if (veto) {
-                    if (composite_given_thinning(w.coulomb, JFGPU_DRAW_UNIT, veto_rate, pair, draws, target_factor,
+                    if (composite_given_thinning(w.coulomb, JFGPU_DRAW_UNIT, given_rate, pair, draws, target_factor,
                                                  bounding_rate, event_rate, confirmed))
-                        confirmed = false;  // the rate was checked positive when the candidate was made
+                        confirmed = false;  // the rate was checked when the candidate was made
                 } else {
                     confirmed = composite_thinning(w.coulomb, JFGPU_DRAW_UNIT, bound, pair, draws, target_factor,
                                                    bounding_rate, event_rate);
@@ -1137,7 +1271,7 @@ __global__ void __launch_bounds__(256, 2) water_cells_kernel(WaterArgs a) {
                     double target_factor[3], bounding_rate, event_rate, local_cross[9];
                     bool confirmed = true;
                     if (veto)
-                        composite_given_thinning(w.coulomb, JFGPU_DRAW_UNIT, veto_rate, pair, draws, target_factor,
+                        composite_given_thinning(w.coulomb, JFGPU_DRAW_UNIT, given_rate, pair, draws, target_factor,
                                                  bounding_rate, event_rate, confirmed);
                     else
                         composite_thinning(w.coulomb, JFGPU_DRAW_UNIT, bound, pair, draws, target_factor,
@@ -1168,13 +1302,13 @@ __global__ void __launch_bounds__(256, 2) water_cells_kernel(WaterArgs a) {
             } else if (best.kind == JFGPU_EV_BOUNDARY) {
                 accepted = 0;
                 ++cs.boundary_events;
-            } else if (best.kind != JFGPU_EV_CELL_VETO) {
+            } else if (best.kind != JFGPU_EV_CELL_VETO && best.kind != JFGPU_EV_CELL_BOUNDING) {
                 s.status = JFGPU_STATUS_ASSERTION;
             }
         }
         if (threadIdx.x == 0) {
             if (best.kind == JFGPU_EV_BOUNDARY) pr[d] = boundary;
-            if (best.kind == JFGPU_EV_CELL_VETO) {
+            if (best.kind == JFGPU_EV_CELL_VETO || best.kind == JFGPU_EV_CELL_BOUNDING) {
                 ++cs.veto_events;
                 if (other >= 0) ++cs.veto_targets;
             }
@@ -1437,9 +1571,11 @@ const T *water_table(WaterHandle *h, const std::vector<T> &host, int &error) {
 }  // namespace
 
 extern "C" int jfgpu_water_set_cells(void *water, int32_t cells_per_side, int32_t neighbor_layers,
-                                     const double *bounds_upper, const double *bounds_lower, int32_t keep_pairs) {
+                                     const double *bounds_upper, const double *bounds_lower, int32_t keep_pairs,
+                                     int32_t far, double dipole_charge) {
     WaterHandle *h = static_cast<WaterHandle *>(water);
-    if (!h || cells_per_side < 1 || cells_per_side > 32 || neighbor_layers < 0 || !bounds_upper || !bounds_lower)
+    if (!h || cells_per_side < 1 || cells_per_side > 32 || neighbor_layers < 0 || !bounds_upper || !bounds_lower ||
+        (far != JFGPU_FAR_CELL_VETO && far != JFGPU_FAR_CELL_BOUNDING) || !(dipole_charge != 0.0))
         return JFGPU_ERROR_ARGUMENT;
     WaterModel &w = h->model;
     WaterCells cl;
@@ -1448,6 +1584,8 @@ extern "C" int jfgpu_water_set_cells(void *water, int32_t cells_per_side, int32_
     cl.m = m;
     cl.ncells = m * m * m;
     cl.keep_pairs = keep_pairs ? 1 : 0;
+    cl.far = far;
+    cl.dipole_charge = dipole_charge;
     cl.side = w.length / m;
     cl.inv_side = 1.0 / cl.side;
     cl.root_speed = w.speed * (1.0 / 3.0);  // the leaf velocity times its weight 1 / len(children) in the molecule
@@ -1458,11 +1596,13 @@ extern "C" int jfgpu_water_set_cells(void *water, int32_t cells_per_side, int32_
         if (near[r]) cl.offsets[cl.n_off++] = r;
     std::vector<double> lo, hi;
     cell_bounds(w.length, m, lo, hi);
-    std::vector<int16_t> tra((size_t)m * m);
+    // relative_cell / translate along one axis (cuboid_periodic_cells.py:156-207)
+    std::vector<int16_t> tra((size_t)m * m), rel((size_t)m * m);
     for (int a = 0; a < m; ++a)
         for (int b = 0; b < m; ++b) {
             const double center = (hi[a] + lo[a]) / 2.0;
             tra[(size_t)a * m + b] = (int16_t)(long long)(py_mod(center + lo[b], w.length) / cl.side);
+            rel[(size_t)a * m + b] = (int16_t)(long long)(py_mod(center - lo[b], w.length) / cl.side);
         }
     auto nearby_zero = [&](int cell) {
         return near[cell % m] && near[(cell / m) % m] && near[cell / (m * m)];
@@ -1490,6 +1630,7 @@ extern "C" int jfgpu_water_set_cells(void *water, int32_t cells_per_side, int32_
     cl.cell_min = water_table(h, lo, error);
     cl.cell_max = water_table(h, hi, error);
     cl.tra = water_table(h, tra, error);
+    cl.rel = water_table(h, rel, error);
     cl.bound_upper = water_table(h, upper, error);
     cl.bound_lower = water_table(h, lower, error);
     for (int which = 0; which < 2; ++which)
@@ -1552,9 +1693,7 @@ extern "C" int jfgpu_water_cells_run(void *water, double *positions, const doubl
     a.sur = buffers->surplus;
     a.cell_state = buffers->cell_state;
     a.root_log = buffers->root_log;
-    // the water kernel's arrays, the target list [molecules] and the screen's prefactors [3 molecules]
-    const size_t shared = water_shared_bytes(h->model.molecules) + sizeof(int) * (size_t)h->model.molecules +
-                          sizeof(float) * 3 * (size_t)h->model.molecules;
+    const size_t shared = water_cells_shared_bytes(h->model.molecules);
     if (shared > 48 * 1024 &&
         cudaFuncSetAttribute(water_cells_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shared) !=
             cudaSuccess)

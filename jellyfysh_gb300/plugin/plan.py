@@ -153,7 +153,20 @@ def _translate_water(state_handler, activator, setting, roots, chains, mode, see
             estimator = handler._estimator
             if _name(estimator) != "DipoleMonteCarloEstimator":
                 raise ConfigurationError("the molecular cell veto's bounds come from the dipole Monte Carlo estimator")
-            veto = dict(handler=handler, estimator=estimator, lifting=lifting_of(handler))
+            veto = dict(estimator=estimator, lifting=lifting_of(handler), far="cell_veto")
+            cell_tags.add(tagger.tag)
+            continue
+        if tagger_name == "CellBoundingPotentialTagger":
+            if handler_name != "TwoCompositeObjectCellBoundingPotentialEventHandler":
+                raise ConfigurationError("the water engine's cell-bounding factor is the molecular one")
+            mic, bounding = handler._potential, handler._bounding_potential
+            estimator = getattr(bounding, "_estimator", None)
+            if _name(bounding) != "CellBoundingPotential" or _name(estimator) != "DipoleMonteCarloEstimator":
+                raise ConfigurationError("the molecular cell-bounding factor takes the cell-bounding potential of the "
+                                         "dipole Monte Carlo estimator")
+            if _potential_kind(mic) != "MergedImageCoulomb":
+                raise ConfigurationError("the molecular cell-bounding factor bounds merged-image Coulomb")
+            veto = dict(estimator=estimator, lifting=lifting_of(handler), far="cell_bounding")
             cell_tags.add(tagger.tag)
             continue
         if tagger_name == "FactorTypeMapInStateTagger":
@@ -220,10 +233,12 @@ def _water_cells(activator, fields, coulomb_taggers, boundary_tag, veto, pair_ta
     """The molecular cells of a water configuration as the reference's water cell-veto configuration sets them up
     (``config_files/2018_JCP_149_064113/water/coulomb_cell_veto_lj_inverted.ini``): one single-active cell
     occupancy of the root units on cubic periodic cells, the nearby and surplus Coulomb factors, the molecular cell
-    veto with the dipole Monte Carlo estimator, and the cell boundary; every other event recreates every factor."""
+    veto with the dipole Monte Carlo estimator (or the molecular cell-bounding factor on it, as
+    ``config_files/2018_JCP_149_064113/dipoles/cell_bounded.ini`` sets it up), and the cell boundary; every other event
+    recreates every factor."""
     if coulomb_taggers != {"ExcludedCellsTagger", "SurplusCellsTagger"} or boundary_tag is None or veto is None:
-        raise ConfigurationError("the molecular cells need the nearby and surplus Coulomb factors, the cell veto and "
-                                 "the cell boundary")
+        raise ConfigurationError("the molecular cells need the nearby and surplus Coulomb factors, the cell veto or "
+                                 "the cell-bounding factor, and the cell boundary")
     occupancies = [s for s in activator._internal_states if _name(s) == "SingleActiveCellOccupancy"]
     if len(occupancies) != 1 or int(occupancies[0]._cell_level) != 1:
         raise ConfigurationError("the molecular cells need one single-active cell occupancy of the root units")
@@ -234,7 +249,7 @@ def _water_cells(activator, fields, coulomb_taggers, boundary_tag, veto, pair_ta
     if int(occupancy._maximum_number_occupants) != 1:
         raise ConfigurationError("the molecular cells hold one occupant per cell")
     if veto["lifting"] != fields["lifting"]:
-        raise ConfigurationError("the cell veto and the Coulomb factors lift with the same scheme")
+        raise ConfigurationError("the far field and the Coulomb factors lift with the same scheme")
     estimator = veto["estimator"]
     mic = estimator._potential
     if _potential_kind(mic) != "MergedImageCoulomb" or (
@@ -255,7 +270,7 @@ def _water_cells(activator, fields, coulomb_taggers, boundary_tag, veto, pair_ta
     return dict(cells_per_side=int(cells._cells_per_side[0]), neighbor_layers=int(cells._neighbor_layers),
                 dipole_separation=float(estimator._dipole_separation), dipole_charge=float(estimator._dipole_charge),
                 prefactor=float(estimator._prefactor), number_trials=int(estimator._number_trials),
-                empirical_bound=float(estimator._empirical_bound), keep_pairs=keep_pairs)
+                empirical_bound=float(estimator._empirical_bound), keep_pairs=keep_pairs, far=veto["far"])
 
 
 def translate(state_handler, activator, setting, chains: int = 1, mode: str = "mixed", seed: int = 0,

@@ -47,13 +47,17 @@ class WaterCells:
     molecular cell veto's bound tables [cells][3] (upper and negated lower derivative bound of every relative cell
     and direction; NaN for the nearby cells).  keep_pairs: the cell boundary's tagger trashes only the cell-based
     factors (the reference's configuration: the bond and Lennard-Jones candidates outlive it); False: it trashes them
-    too."""
+    too.  far: "cell_veto", or "cell_bounding" (``TwoCompositeObjectCellBoundingPotentialEventHandler`` with its tagger:
+    a factor for every occupied far cell, as the reference's dipole configuration ``dipoles/cell_bounded.ini`` sets it
+    up; the charge factor divides by the estimator's ``dipole_charge``)."""
 
     cells_per_side: int
     neighbor_layers: int
     bounds_upper: np.ndarray
     bounds_lower: np.ndarray
     keep_pairs: bool = True
+    far: str = "cell_veto"
+    dipole_charge: float = 1.0
 
     @property
     def cells(self) -> int:
@@ -63,9 +67,10 @@ class WaterCells:
 def dipole_cell_veto_bounds(model: "WaterModel", cells_per_side: int, neighbor_layers: int,
                             dipole_separation: float = 0.5, dipole_charge: float = 0.82, prefactor: float = 1.5,
                             number_trials: int = 1000, empirical_bound: float = 30.0, seed: int = 0,
-                            keep_pairs: bool = True) -> WaterCells:
+                            keep_pairs: bool = True, far: str = "cell_veto") -> WaterCells:
     """The bound tables of the molecular cell veto as the reference's ``CellVetoEventHandler.initialize``
-    (``event_handler/abstracts/cell_veto_event_handler.py:93-160``) fills them with the
+    (``event_handler/abstracts/cell_veto_event_handler.py:93-160``), and of the molecular cell-bounding factor as
+    ``CellBoundingPotential.initialize`` (``potential/cell_bounding_potential.py:70-126``), fill them with the
     ``DipoleMonteCarloEstimator`` (``estimator/dipole_monte_carlo_estimator.py:74-155``): for every relative cell
     that is not nearby and every direction, ``number_trials`` dipoles of two charges ``±dipole_charge`` at distance
     ``dipole_separation`` (centre uniform in the cell separation's box widened by half the separation, direction
@@ -82,13 +87,13 @@ def dipole_cell_veto_bounds(model: "WaterModel", cells_per_side: int, neighbor_l
     for o in range(-neighbor_layers, neighbor_layers + 1):
         near[o % m] = True
     cells = m ** 3
-    far = [c for c in range(cells) if not (near[c % m] and near[(c // m) % m] and near[c // (m * m)])]
+    far_cells = [c for c in range(cells) if not (near[c % m] and near[(c // m) % m] and near[c // (m * m)])]
     rng = np.random.default_rng(seed)
     half = dipole_separation / 2.0
-    n_far = len(far)
+    n_far = len(far_cells)
     lower_corner = np.empty((n_far, 3))
     upper_corner = np.empty((n_far, 3))
-    for i, c in enumerate(far):
+    for i, c in enumerate(far_cells):
         axes = (c % m, (c // m) % m, c // (m * m))
         for d in range(3):
             lower_corner[i, d] = lo[axes[d]] - hi[0] - half
@@ -124,9 +129,10 @@ def dipole_cell_veto_bounds(model: "WaterModel", cells_per_side: int, neighbor_l
     upper = np.minimum(empirical_bound, upper)
     bounds_upper = np.full((cells, 3), np.nan)
     bounds_lower = np.full((cells, 3), np.nan)
-    bounds_upper[far] = upper
-    bounds_lower[far] = -np.maximum(-empirical_bound, -upper)
-    return WaterCells(m, int(neighbor_layers), bounds_upper, bounds_lower, bool(keep_pairs))
+    bounds_upper[far_cells] = upper
+    bounds_lower[far_cells] = -np.maximum(-empirical_bound, -upper)
+    return WaterCells(m, int(neighbor_layers), bounds_upper, bounds_lower, bool(keep_pairs), far,
+                      float(dipole_charge))
 
 
 def _cell_bounds(length: float, m: int):
@@ -251,9 +257,10 @@ class WaterBatch:
         from . import systems
         upper = np.ascontiguousarray(cells.bounds_upper, dtype=np.float64).reshape(cells.cells, 3)
         lower = np.ascontiguousarray(cells.bounds_lower, dtype=np.float64).reshape(cells.cells, 3)
+        far = {"cell_veto": _lib.FAR_CELL_VETO, "cell_bounding": _lib.FAR_CELL_BOUNDING}[cells.far]
         _lib.check(self.lib.jfgpu_water_set_cells(self._handle, int(cells.cells_per_side), int(cells.neighbor_layers),
-                                                  upper.ctypes.data, lower.ctypes.data, int(bool(cells.keep_pairs))),
-                   "jfgpu_water_set_cells")
+                                                  upper.ctypes.data, lower.ctypes.data, int(bool(cells.keep_pairs)),
+                                                  far, float(cells.dipole_charge)), "jfgpu_water_set_cells")
         M = self.model.molecules
         if roots is None:
             host = self.positions_dev.cpu().numpy()
@@ -325,7 +332,7 @@ class WaterBatch:
         extra = {}
         if self.cells is not None:
             extra = dict(cells=json.dumps([self.cells.cells_per_side, self.cells.neighbor_layers,
-                                           bool(self.cells.keep_pairs)]),
+                                           bool(self.cells.keep_pairs), self.cells.far, self.cells.dipole_charge]),
                          bounds_upper=self.cells.bounds_upper, bounds_lower=self.cells.bounds_lower,
                          roots=self.roots_dev.cpu().numpy(), occupancy=self.occupancy_dev.cpu().numpy(),
                          surplus=self.surplus_dev.cpu().numpy(), cell_state=self.cell_state_dev.cpu().numpy())
@@ -338,9 +345,9 @@ class WaterBatch:
         data = np.load(path)
         cells = None
         if "cells" in data.files:
-            m, layers, keep_pairs = json.loads(str(data["cells"]))
+            m, layers, keep_pairs, far, dipole_charge = json.loads(str(data["cells"]))
             cells = WaterCells(int(m), int(layers), np.asarray(data["bounds_upper"]), np.asarray(data["bounds_lower"]),
-                               bool(keep_pairs))
+                               bool(keep_pairs), far, float(dipole_charge))
         batch = cls(WaterModel(**json.loads(str(data["model"]))), np.asarray(data["positions"]), seed=int(data["seed"]),
                     first_chain=int(data["first_chain"]), charges=np.asarray(data["charges"]),
                     warps_per_block=int(data["warps_per_block"]), cells=cells,

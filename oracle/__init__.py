@@ -20,6 +20,7 @@ EV_BOND, EV_COMPOSITE = 8, 9
 POT_HARD_SPHERE, POT_LENNARD_JONES, POT_COULOMB = range(3)
 FAR_NONE, FAR_CELL_VETO, FAR_CELL_BOUNDING = range(3)
 RNG_PAIR, RNG_THIN, RNG_VETO_TIME, RNG_VETO_CHOICE, RNG_VETO_UNIFORM, RNG_NEW_ACTIVE, RNG_COMPOSITE, RNG_LIFT = range(8)
+RNG_CELL_BOUND = 8  # potential change of a molecular cell-bounding factor, by target molecule
 
 STATUS_NAMES = {0: "ok", 1: "ValueError", 2: "AssertionError", 3: "ZeroDivisionError", 4: "complex result",
                 5: "bad configuration", 6: "allocation failure", 7: "cell index out of range",
@@ -124,7 +125,8 @@ def lib() -> ctypes.CDLL:
                                                ctypes.POINTER(ctypes.c_int)]
         handle.jfo_water_cells_create.restype = ctypes.c_void_p
         handle.jfo_water_cells_create.argtypes = [ctypes.POINTER(JfoWaterSystem), ctypes.c_int, ctypes.c_int, _PD,
-                                                  _PD, _PD, _PD, _PD, ctypes.c_int, ctypes.POINTER(ctypes.c_int)]
+                                                  _PD, _PD, _PD, _PD, ctypes.c_int, ctypes.c_int, _D,
+                                                  ctypes.POINTER(ctypes.c_int)]
         handle.jfo_water_roots.argtypes = [ctypes.c_void_p, _PD]
         handle.jfo_chain_create.restype = ctypes.c_void_p
         handle.jfo_chain_create.argtypes = [ctypes.POINTER(JfoSystem), _PD, _PD, ctypes.POINTER(ctypes.c_int)]
@@ -491,10 +493,11 @@ def make_water_system(spec: dict, rng_key: int) -> JfoWaterSystem:
 
 class Water:
     """One chain of flexible water molecules run by the oracle.  With ``cells`` (cells_per_side, neighbor_layers,
-    roots [molecules][3], bounds_upper [cells][3], bounds_lower [cells][3][, keep_pairs]) the Coulomb interaction
-    between molecules goes through the molecular cells of the root units: nearby and surplus factors, the molecular
-    cell veto with the given bound tables and the cell-boundary events of the active root unit (across which the
-    bond and Lennard-Jones candidates persist unless keep_pairs is False)."""
+    roots [molecules][3], bounds_upper [cells][3], bounds_lower [cells][3][, keep_pairs[, far, dipole_charge]])
+    the Coulomb interaction between molecules goes through the molecular cells of the root units: nearby and surplus
+    factors, the far field ("cell_veto", the default, or "cell_bounding" with the estimator's dipole charge) with the
+    given bound tables and the cell-boundary events of the active root unit (across which the bond and Lennard-Jones
+    candidates persist unless keep_pairs is False)."""
 
     def __init__(self, system: JfoWaterSystem, positions: np.ndarray, charges: np.ndarray, cells=None):
         self.system = system
@@ -509,13 +512,15 @@ class Water:
         else:
             m, layers, roots, upper, lower = cells[:5]
             keep_pairs = bool(cells[5]) if len(cells) > 5 else True
+            far = {"cell_veto": 1, "cell_bounding": 2}[cells[6] if len(cells) > 6 else "cell_veto"]
+            dipole_charge = float(cells[7]) if len(cells) > 7 else 1.0
             self._cells_in = [np.ascontiguousarray(a, dtype=np.float64) for a in (roots, upper, lower)]
             assert self._cells_in[0].shape == (system.molecules, 3)
             assert self._cells_in[1].shape == self._cells_in[2].shape == (m ** 3, 3)
             self._handle = lib().jfo_water_cells_create(
                 ctypes.byref(system), int(m), int(layers), self._positions_in.ctypes.data_as(_PD),
                 self._charges_in.ctypes.data_as(_PD), *[a.ctypes.data_as(_PD) for a in self._cells_in],
-                int(keep_pairs), ctypes.byref(status))
+                int(keep_pairs), far, dipole_charge, ctypes.byref(status))
         if not self._handle:
             raise OracleError("water creation failed: " + STATUS_NAMES.get(status.value, str(status.value)))
 

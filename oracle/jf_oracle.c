@@ -2039,6 +2039,8 @@ struct JfoWater {
     /* the bond and Lennard-Jones candidates persist across molecular cell-boundary events: their earliest, and the
      * active leaf and root unit as their in-state holds them (time stamp snap_q, snap_r) */
     int keep_pairs;         /* the cell boundary trashes only the cell-based factors */
+    int far;                /* JFO_FAR_CELL_VETO or JFO_FAR_CELL_BOUNDING (one candidate per occupied far cell) */
+    double dipole_charge;   /* the dipole estimator's charge (the cell-bounding charge factor) */
     int pairs_valid;
     Cand pair;
     double snap_leaf[3], snap_root[3], snap_q, snap_r;
@@ -2290,8 +2292,8 @@ static int chain_install_bounds(JfoChain *c, const double *upper, const double *
 
 JfoWater *jfo_water_cells_create(const JfoWaterSystem *system, int cells_per_side, int neighbor_layers,
                                  const double *positions, const double *charges, const double *roots,
-                                 const double *bounds_upper, const double *bounds_lower, int keep_pairs,
-                                 int *status) {
+                                 const double *bounds_upper, const double *bounds_lower, int keep_pairs, int far,
+                                 double dipole_charge, int *status) {
     JfoWater *w = jfo_water_create(system, positions, charges, status);
     if (!w) return NULL;
     JfoSystem cs;
@@ -2309,7 +2311,7 @@ JfoWater *jfo_water_cells_create(const JfoWaterSystem *system, int cells_per_sid
     cs.potential = JFO_POT_HARD_SPHERE;
     cs.far = JFO_FAR_NONE;
     cs.rng_key = system->rng_key;
-    if (cells_per_side < 1 || neighbor_layers < 0) {
+    if (cells_per_side < 1 || neighbor_layers < 0 || (far != JFO_FAR_CELL_VETO && far != JFO_FAR_CELL_BOUNDING)) {
         jfo_water_destroy(w);
         *status = JFO_BAD_CONFIG;
         return NULL;
@@ -2327,6 +2329,8 @@ JfoWater *jfo_water_cells_create(const JfoWaterSystem *system, int cells_per_sid
     }
     w->root_speed = system->speed * (1.0 / 3.0);
     w->keep_pairs = keep_pairs ? 1 : 0;
+    w->far = far;
+    w->dipole_charge = dipole_charge;
     w->pairs_valid = 0;
     return w;
 }
@@ -2445,7 +2449,34 @@ static int64_t water_cells_run(JfoWater *w, int64_t max_events, JfoEvent *log, d
             *status = st;
             return done;
         }
-        {
+        if (w->far == JFO_FAR_CELL_BOUNDING) {
+            /* CellBoundingPotentialTagger (cell_bounding_potential_tagger.py:127-155): the occupant of every occupied
+             * cell that is not nearby; TwoCompositeObjectCellBoundingPotentialEventHandler.send_event_time
+             * (two_composite_object_cell_bounding_potential_event_handler.py:153-207): the relative cell of the target's
+             * root cell to the active root's, the bound of that cell times the charge factor
+             * (CellBoundingPotential.standard_velocity_displacement, cell_bounding_potential.py:155-198) */
+            for (int cell = 0; cell < c->ncells && !st; ++cell) {
+                if (c->occ_count[cell] == 0 || is_nearby(c, cell, active_cell)) continue;
+                int other = c->occ[cell * c->cap], target_cell;
+                st = cell_of(c, &c->pos[3 * other], &target_cell);
+                if (st) break;
+                int rc = relative_cell(c, target_cell, active_cell);
+                if (is_nearby(c, rc, 0)) {
+                    st = JFO_ASSERT;
+                    break;
+                }
+                double lower[3], rate, dt;
+                for (int d = 0; d < 3; ++d) lower[d] = -c->bound_lower[rc * 3 + d];
+                double du = jfo_expovariate(jfo_draw(s->rng_key, w->event, JFO_RNG_CELL_BOUND, (uint32_t)other), s->beta);
+                st = jfo_composite_cell_bound_time(&c->bound_upper[rc * 3], lower, velocity, w->charge[a],
+                                                   &w->charge[3 * other], 3, w->dipole_charge, du, &rate, &dt);
+                if (!st) offer(&best, w->ts_q, w->ts_r, dt, JFO_EV_CELL_BOUNDING, other, active_cell, rate);
+            }
+            if (st) {
+                *status = st;
+                return done;
+            }
+        } else {
             /* the molecular cell veto: the charge factor is the active unit's charge
              * (DipoleMonteCarloEstimator.charge_correction_factor without target charges) */
             double charge_factor = w->charge[a];
@@ -2514,8 +2545,21 @@ static int64_t water_cells_run(JfoWater *w, int64_t max_events, JfoEvent *log, d
             w->active = best.target;
             break;
         case JFO_EV_COMPOSITE:
+        case JFO_EV_CELL_BOUNDING:
         case JFO_EV_CELL_VETO: {
             int other = best.target;
+            if (best.kind == JFO_EV_CELL_BOUNDING) {
+                /* send_out_state (:209-265): the active root must still be in the cell of the event time's
+                 * candidate (the reference returns no out-state otherwise, which its mediator cannot insert); the
+                 * thinning draws against the bounding event rate times the speed */
+                int now_cell;
+                st = cell_of(c, root, &now_cell);
+                if (st || now_cell != best.aux) {
+                    *status = st ? st : JFO_ASSERT;
+                    return done;
+                }
+                best.rate *= s->speed;
+            }
             if (best.kind == JFO_EV_CELL_VETO) {
                 /* the occupant of the sampled cell, looked up at the commit (Mediator.get_arguments_cell_veto_event_handler) */
                 other = c->occ_count[best.aux] > 0 ? c->occ[best.aux * c->cap] : -1;

@@ -61,6 +61,7 @@ extern "C" {
 #define JFO_RNG_NEW_ACTIVE 5   /* end-of-chain randint (target 0: molecule or atom, 1: unit of the molecule) */
 #define JFO_RNG_COMPOSITE 6    /* potential change of a Coulomb factor of two molecules, per target unit */
 #define JFO_RNG_LIFT 7         /* uniform of the lifting scheme */
+#define JFO_RNG_CELL_BOUND 8   /* potential change of a molecular cell-bounding factor, by target molecule */
 
 /* primitives */
 double jfo_py_mod(double x, double y);
@@ -222,14 +223,16 @@ int64_t jfo_water_run(JfoWater *water, int64_t max_events, JfoEvent *log, int *s
  * NULL; molecular cells only) */
 int64_t jfo_water_run_roots(JfoWater *water, int64_t max_events, JfoEvent *log, double *root_log, int *status);
 /* flexible water with molecular cells of root units (cells_per_side^3 cuboid periodic cells, neighbor_layers): the
- * Coulomb factor with the molecules of the nearby cells and the surplus molecules, the molecular cell veto with the
- * given bound tables ([cells][3] upper and negated lower bounds, NaN for the nearby cells) and the cell-boundary
- * events of the active root unit; roots [molecules][3] are the initial root positions; keep_pairs: the bond and
- * Lennard-Jones candidates outlive a cell boundary (its tagger trashes only the cell-based factors) */
+ * Coulomb factor with the molecules of the nearby cells and the surplus molecules, the far field (far
+ * JFO_FAR_CELL_VETO: the molecular cell veto; JFO_FAR_CELL_BOUNDING: the molecular cell-bounding factor of every
+ * occupied far cell, charge factor over dipole_charge) with the given bound tables ([cells][3] upper and negated lower
+ * bounds, NaN for the nearby cells) and the cell-boundary events of the active root unit; roots [molecules][3] are
+ * the initial root positions; keep_pairs: the bond and Lennard-Jones candidates outlive a cell boundary (its tagger
+ * trashes only the cell-based factors) */
 JfoWater *jfo_water_cells_create(const JfoWaterSystem *system, int cells_per_side, int neighbor_layers,
                                  const double *positions, const double *charges, const double *roots,
-                                 const double *bounds_upper, const double *bounds_lower, int keep_pairs,
-                                 int *status);
+                                 const double *bounds_upper, const double *bounds_lower, int keep_pairs, int far,
+                                 double dipole_charge, int *status);
 void jfo_water_roots(const JfoWater *water, double *roots);
 void jfo_water_positions(const JfoWater *water, double *positions);
 void jfo_water_state(const JfoWater *water, int64_t *event_count, int *active, int *direction, double *time_q,

@@ -21,6 +21,12 @@ configuration (``config_files/2018_JCP_149_064113/water/coulomb_cell_veto_lj_inv
   ``DipoleMonteCarloEstimator`` of the reference configuration (dipole separation 0.5, dipole charge 0.82, prefactor
   1.5, 1000 trials, empirical bound 30).
 
+Two trajectories take the molecular cell-bounding far field instead of the cell veto
+(``CellBoundingPotentialTagger`` with ``TwoCompositeObjectCellBoundingPotentialEventHandler`` and a
+``CellBoundingPotential`` on the same estimator, as the reference's dipole configuration
+``config_files/2018_JCP_149_064113/dipoles/cell_bounded.ini`` sets it up): one candidate per occupied far cell, whose
+potential change is keyed by the target molecule (kind RNG_CELL_BOUND).
+
 The bending potential of the reference configuration is not part of the model (it is not one of the factors of the
 event-time path this project rebuilds).  As for the other trajectories, the initial state, the random numbers of the
 event loop (keyed draws of the oracle's generator: pair changes by target unit, Coulomb factor changes by target
@@ -61,16 +67,67 @@ SYSTEMS = {
     "water_n8_cell_boundaries": dict(WATER, **dict(CELL_VETO, cells_per_side=6, neighbor_layers=1,
                                                    empirical_bound=0.02),
                                      molecules_per_side=2, system_length=12.42 / 2.0, seed=26, events=5000),
+    # the molecular cell-bounding far field instead of the cell veto
+    # (TwoCompositeObjectCellBoundingPotentialEventHandler with CellBoundingPotentialTagger, as the reference's dipole
+    # configuration config_files/2018_JCP_149_064113/dipoles/cell_bounded.ini sets it up): one candidate per occupied
+    # far cell; 8 molecules on 4^3 cells with one neighbour layer, and 64 molecules on 6^3 cells with one layer
+    "water_n8_cell_bounding": dict(WATER, **dict(CELL_VETO, cells_per_side=4, neighbor_layers=1, empirical_bound=2.0),
+                                   far="cell_bounding", molecules_per_side=2, system_length=12.42 / 2.0, seed=27,
+                                   events=4000),
+    "water_n64_cell_bounding": dict(WATER, **dict(CELL_VETO, cells_per_side=6, neighbor_layers=1,
+                                                  empirical_bound=5.0),
+                                    far="cell_bounding", molecules_per_side=4, system_length=12.42, seed=28,
+                                    events=2500),
 }
 
 PAIR_TAGS = ["harmonic_oh", "harmonic_hh", "lennard_jones"]
 CELL_TAGS = ["molecule_cell_boundary", "coulomb_nearby", "coulomb_surplus", "coulomb_cell_veto"]
+FAR_TAGGERS = {"cell_veto": "coulomb_cell_veto (cell_veto_tagger)",
+               "cell_bounding": "coulomb_cell_bounding (cell_bounding_potential_tagger)"}
+
+
+def cell_tags(spec):
+    return [t if t != "coulomb_cell_veto" or spec.get("far", "cell_veto") == "cell_veto" else "coulomb_cell_bounding"
+            for t in CELL_TAGS]
+
+
+def far_sections(spec, every):
+    molecules = spec["molecules_per_side"] ** 3
+    if spec.get("far", "cell_veto") == "cell_veto":
+        return """[CoulombCellVeto]
+trash = {every}
+create = {every}
+event_handler = coulomb_cell_veto_event_handler (composite_object_cell_veto_event_handler)
+internal_state_label = single_active_cell_occupancy
+
+[CoulombCellVetoEventHandler]
+estimator = dipole_monte_carlo_estimator
+lifting = inside_first_lifting
+charge = electric_charge
+""".format(every=every)
+    return """[CoulombCellBounding]
+trash = {every}
+create = {every}
+event_handler = two_composite_object_cell_bounding_potential_event_handler
+internal_state_label = single_active_cell_occupancy
+number_event_handlers = {others}
+
+[TwoCompositeObjectCellBoundingPotentialEventHandler]
+potential = merged_image_coulomb_potential
+bounding_potential = cell_bounding_potential
+lifting = inside_first_lifting
+charge = electric_charge
+
+[CellBoundingPotential]
+estimator = dipole_monte_carlo_estimator
+""".format(every=every, others=molecules - 1)
 
 
 def config_text(spec, factor_file):
     molecules = spec["molecules_per_side"] ** 3
-    every = ", ".join(PAIR_TAGS + CELL_TAGS)
-    cells = ", ".join(CELL_TAGS)
+    tags = cell_tags(spec)
+    every = ", ".join(PAIR_TAGS + tags)
+    cells = ", ".join(tags)
     sections = []
     pair_handlers = {"harmonic_oh": ("harmonic_oh_event_handler (two_leaf_unit_event_handler)", 2),
                      "harmonic_hh": ("harmonic_hh_event_handler (two_leaf_unit_event_handler)", 1),
@@ -104,7 +161,7 @@ taggers =
     molecule_cell_boundary (cell_boundary_tagger),
     coulomb_nearby (excluded_cells_tagger),
     coulomb_surplus (surplus_cells_tagger),
-    coulomb_cell_veto (cell_veto_tagger),
+    {far_tagger},
     end_of_chain (active_global_state_in_state_tagger),
     end_of_run (no_in_state_tagger),
     start_of_run (no_in_state_tagger)
@@ -142,12 +199,7 @@ event_handler = coulomb_exception_event_handler (two_composite_object_summed_bou
 internal_state_label = single_active_cell_occupancy
 number_event_handlers = {others}
 
-[CoulombCellVeto]
-trash = {every}
-create = {every}
-event_handler = coulomb_cell_veto_event_handler (composite_object_cell_veto_event_handler)
-internal_state_label = single_active_cell_occupancy
-
+{far_sections}
 [CoulombExceptionEventHandler]
 potential = merged_image_coulomb_potential
 bounding_potential = inverse_power_coulomb_bounding_potential
@@ -162,11 +214,6 @@ position_cutoff = {position_cutoff}
 
 [InversePowerCoulombBoundingPotential]
 prefactor = {bound_prefactor!r}
-
-[CoulombCellVetoEventHandler]
-estimator = dipole_monte_carlo_estimator
-lifting = inside_first_lifting
-charge = electric_charge
 
 [DipoleMonteCarloEstimator]
 potential = merged_image_coulomb_potential
@@ -244,7 +291,8 @@ charge_name = electric_charge
 charge_values = {charge_hydrogen!r}, {charge_oxygen!r}, {charge_hydrogen!r}
 """.format(L=float(spec["system_length"]), factor_file=factor_file, sections="\n".join(sections), every=every,
            cells=cells, m=spec["cells_per_side"], layers=spec["neighbor_layers"], molecules=molecules,
-           others=molecules - 1, **{k: v for k, v in spec.items() if k not in ("lifting",)})
+           others=molecules - 1, far_tagger=FAR_TAGGERS[spec.get("far", "cell_veto")],
+           far_sections=far_sections(spec, every), **{k: v for k, v in spec.items() if k not in ("lifting", "far")})
 
 
 def barycentres(positions, length):
@@ -280,6 +328,8 @@ def run_one(tree, name):
     import jellyfysh.event_handler.two_leaf_unit_event_handler as m_pair
     import jellyfysh.event_handler.two_composite_object_summed_bounding_potential_event_handler as m_composite
     import jellyfysh.event_handler.composite_object_cell_veto_event_handler as m_composite_veto
+    import jellyfysh.event_handler.two_composite_object_cell_bounding_potential_event_handler as m_cell_bounding
+    from jellyfysh.potential.cell_bounding_potential import CellBoundingPotential
     import jellyfysh.event_handler.abstracts.cell_veto_event_handler as m_veto
     import jellyfysh.event_handler.cell_boundary_event_handler as m_boundary
     import jellyfysh.event_handler.walker as m_walker
@@ -353,9 +403,21 @@ def run_one(tree, name):
             yield from original_local(self, active_identifier)
     local_map._yield_factor_identifier_local = yield_factor_identifier_local
 
+    class CellBoundRandom:
+        @staticmethod
+        def expovariate(lambd):
+            assert lambd == beta
+            return oracle.expovariate(oracle.draw(key, event_index(), oracle.RNG_CELL_BOUND, ctx["cb_target"]),
+                                      lambd)
+
+        @staticmethod
+        def uniform(a, b):
+            return a + (b - a) * oracle.uniform(oracle.draw(key, event_index(), oracle.RNG_THIN, 0))
+
     m_pair.random = PairRandom
     m_composite.random = CompositeRandom
     m_composite_veto.random = CompositeRandom
+    m_cell_bounding.random = CellBoundRandom
     m_veto.random = VetoRandom
     m_walker.random = WalkerRandom
     m_lifting.random = LiftRandom
@@ -384,6 +446,29 @@ def run_one(tree, name):
         assert not ctx["composite_targets"]
         return result
     composite_class.send_event_time = composite_event_time
+
+    bounding_class = m_cell_bounding.TwoCompositeObjectCellBoundingPotentialEventHandler
+    original_bounding_time = bounding_class.send_event_time
+
+    def bounding_event_time(self, in_state):
+        ctx["cb_target"] = in_state[1].value.identifier[0]
+        return original_bounding_time(self, in_state)
+    bounding_class.send_event_time = bounding_event_time
+
+    original_cell_bounding_initialize = CellBoundingPotential.initialize
+
+    def cell_bounding_initialize(self, cells, calculate_lower_bound):
+        original_cell_bounding_initialize(self, cells, calculate_lower_bound)
+        if ctx["bounds"] is None:
+            ncells = m_cells ** 3
+            upper = np.full((ncells, 3), np.nan)
+            lower = np.full((ncells, 3), np.nan)
+            for cell, values in self._derivative_bounds[0].items():
+                upper[cell_index(cell)] = values
+            for cell, values in self._derivative_bounds[1].items():
+                lower[cell_index(cell)] = [-v for v in values]  # stored negated, as the cell veto stores it
+            ctx["bounds"] = (upper, lower)
+    CellBoundingPotential.initialize = cell_bounding_initialize
 
     veto_class = m_composite_veto.CompositeObjectCellVetoEventHandler
     original_initialize = veto_class.initialize
@@ -449,6 +534,10 @@ def run_one(tree, name):
             accepted = int(active != moved)
         elif isinstance(winner, composite_class):
             kind = oracle.EV_COMPOSITE
+            target = winner._target_leaf_units[0].identifier[0]
+            accepted = int(active != moved)
+        elif isinstance(winner, bounding_class):
+            kind = oracle.EV_CELL_BOUNDING
             target = winner._target_leaf_units[0].identifier[0]
             accepted = int(active != moved)
         elif isinstance(winner, veto_class):

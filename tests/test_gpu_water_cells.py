@@ -48,13 +48,15 @@ def compare_logs(log, events, length, roots=None, ref_roots=None):
 
 def cells_of(water, spec, data):
     return water.WaterCells(spec["cells_per_side"], spec["neighbor_layers"], data["bounds_upper"],
-                            data["bounds_lower"])
+                            data["bounds_lower"], far=spec.get("far", "cell_veto"),
+                            dipole_charge=spec["dipole_charge"])
 
 
 def oracle_chain(spec, data, positions, roots, key, charges):
     system = oracle.make_water_system(spec, key)
     return oracle.Water(system, positions, charges, cells=(spec["cells_per_side"], spec["neighbor_layers"], roots,
-                                                           data["bounds_upper"], data["bounds_lower"]))
+                                                           data["bounds_upper"], data["bounds_lower"], True,
+                                                           spec.get("far", "cell_veto"), spec["dipole_charge"]))
 
 
 @pytest.mark.parametrize("mode", ["exact", "mixed"])
@@ -72,8 +74,9 @@ def test_gpu_water_cells_reproduce_the_reference_trajectory(water, name, mode):
     assert np.all(wrapped(batch.roots()[0] - data["final_roots"], model.system_length) <= REL * model.system_length)
     cell_state = batch.cell_states()[0]
     assert cell_state["boundary_events"] == np.sum(events["kind"] == oracle.EV_BOUNDARY)
-    assert cell_state["veto_events"] == np.sum(events["kind"] == oracle.EV_CELL_VETO)
-    assert cell_state["veto_targets"] == np.sum((events["kind"] == oracle.EV_CELL_VETO) & (events["target"] >= 0))
+    far = (events["kind"] == oracle.EV_CELL_VETO) | (events["kind"] == oracle.EV_CELL_BOUNDING)
+    assert cell_state["veto_events"] == np.sum(far)
+    assert cell_state["veto_targets"] == np.sum(far & (events["target"] >= 0))
     state = batch.states()[0]
     assert state["events"] == len(events)
     assert state["bond_events"] == np.sum(events["kind"] == oracle.EV_BOND)
@@ -196,3 +199,31 @@ def test_drop_in_plan_with_molecular_cells_runs_to_its_end_of_run_time(water):
     expected, expected_roots = chain.run(events, roots=True)
     compare_logs(log[0], expected, model.system_length, roots[0], expected_roots)
     assert np.sum(expected["kind"] == oracle.EV_BOUNDARY) > 10
+
+
+def test_batched_chains_with_cell_bounding_match_the_oracle(water):
+    """16 chains of the 64-molecule box with the molecular cell-bounding far field (6^3 cells, one layer) from lattice
+    starts of their own against the oracle, and the mixed mode (the far factors screened in FP32) equal to the exact
+    mode bit for bit."""
+    spec, data = load_water_cells("water_n64_cell_bounding")
+    chains, events, seed = 16, 500, 2468
+    runs = {}
+    for mode in ("exact", "mixed"):
+        model = water.WaterModel.from_spec(dict(spec, mode=mode))
+        positions = water.lattice_positions(model, chains, seed)
+        batch = water.WaterBatch(model, positions, seed=seed, cells=cells_of(water, spec, data))
+        log, roots = batch.run(events, record=True, record_roots=True)
+        batch.check_status()
+        runs[mode] = (log, roots, batch.positions(), batch.states(), positions, model)
+    log, roots, final, states, positions, model = runs["exact"]
+    for field in log.dtype.names:
+        assert np.array_equal(log[field], runs["mixed"][0][field]), field
+    assert np.array_equal(roots, runs["mixed"][1]) and np.array_equal(final, runs["mixed"][2])
+    assert runs["mixed"][3]["refined_items"].sum() < 0.5 * states["refined_items"].sum()
+    from jellyfysh_gb300 import systems
+    for c in (0, 9, 15):
+        roots0 = systems.water_roots(positions[c], model.system_length)
+        chain = oracle_chain(spec, data, positions[c], roots0, oracle.chain_key(seed, c), model.charges())
+        expected, expected_roots = chain.run(events, roots=True)
+        compare_logs(log[c], expected, model.system_length, roots[c], expected_roots)
+    assert np.sum(log["kind"] == oracle.EV_CELL_BOUNDING) > 0

@@ -249,8 +249,9 @@ def translate_water_cell_configuration(name, boundary_trashes_pairs="0"):
     text = text.replace("mediator = single_process_mediator", "mediator = gpu_chain_batch_mediator")
     text = text.replace("[SingleProcessMediator]", "[GpuChainBatchMediator]\nchains = 3\nmode = mixed\nseed = 5")
     if boundary_trashes_pairs == "1":
-        every = ", ".join(cells.PAIR_TAGS + cells.CELL_TAGS)
-        text = text.replace("[MoleculeCellBoundary]\ntrash = %s" % ", ".join(cells.CELL_TAGS),
+        tags = cells.cell_tags(spec)
+        every = ", ".join(cells.PAIR_TAGS + tags)
+        text = text.replace("[MoleculeCellBoundary]\ntrash = %s" % ", ".join(tags),
                             "[MoleculeCellBoundary]\ntrash = %s" % every)
     config = configparser.ConfigParser()
     config.read_string(text)
@@ -273,7 +274,7 @@ def translate_water_cell_configuration(name, boundary_trashes_pairs="0"):
             "roots": plan.roots.tolist(), "cell_veto": plan.cell_veto, "charges": plan.charges.tolist()}
 
 
-@pytest.mark.parametrize("name", ["water_n8_cell_veto", "water_n64_cell_veto"])
+@pytest.mark.parametrize("name", ["water_n8_cell_veto", "water_n64_cell_veto", "water_n8_cell_bounding"])
 def test_mediator_translates_the_reference_water_cell_veto_configuration(name):
     """The reference's water cell-veto configuration (with this project's water model) becomes a water plan with
     molecular cells: the cell system, the dipole estimator's parameters, the root units, and the pair candidates kept
@@ -292,7 +293,7 @@ def test_mediator_translates_the_reference_water_cell_veto_configuration(name):
             cell_veto["number_trials"], cell_veto["empirical_bound"]) == (
         spec["dipole_separation"], spec["dipole_charge"], spec["estimator_prefactor"], spec["number_trials"],
         spec["empirical_bound"])
-    assert cell_veto["keep_pairs"] is True
+    assert cell_veto["keep_pairs"] is True and cell_veto["far"] == spec.get("far", "cell_veto")
     assert np.array_equal(np.array(plan["roots"]), data["initial_roots"])
     assert np.array_equal(np.array(plan["positions"]), data["initial"])
     trashing = _in_child("translate_water_cell_configuration", name, "1")

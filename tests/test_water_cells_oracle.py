@@ -8,9 +8,10 @@ the trajectory) and the cell-boundary events of the active root unit, which keep
 candidates alive.  The oracle (``oracle/jf_oracle.c``: ``jfo_water_cells_create``, ``water_cells_run``) replays every
 event from the same initial state and keyed random numbers.
 
-Two trajectories are reproduced bit for bit (every logged field, the root of the moved unit's molecule after every
-event, the final leaf and root positions).  The third, ``water_n8_cell_boundaries``, runs 5000 events with 81 cell
-boundaries, 63 of them followed by a bond or Lennard-Jones event that commits the in-state copies of its creation;
+Four trajectories are reproduced bit for bit (every logged field, the root of the moved unit's molecule after every
+event, the final leaf and root positions): two with the molecular cell veto and two with the molecular cell-bounding
+far field of the reference's dipole configuration (``TwoCompositeObjectCellBoundingPotentialEventHandler``, a factor
+for every occupied far cell).  ``water_n8_cell_boundaries`` runs 5000 events with 81 cell boundaries, 63 of them followed by a bond or Lennard-Jones event that commits the in-state copies of its creation;
 it is bit for bit up to event 3699, whose H-H bond solve squares 1.0750481431014438: CPython's ``**`` calls the C
 library's ``pow``, which returns 1.1557285099858623 there, one unit in the last place below the correctly rounded
 square 1.1557285099858625 that the oracle (and the GPU) compute.  From there on every discrete field still matches
@@ -37,12 +38,14 @@ def run_oracle(z, spec, events=None):
     system = oracle.make_water_system(spec, spec["rng_key"])
     water = oracle.Water(system, z["initial"], z["charges"],
                          cells=(spec["cells_per_side"], spec["neighbor_layers"], z["initial_roots"],
-                                z["bounds_upper"], z["bounds_lower"]))
+                                z["bounds_upper"], z["bounds_lower"], True, spec.get("far", "cell_veto"),
+                                spec["dipole_charge"]))
     log, roots = water.run(len(z["events"]) if events is None else events, roots=True)
     return water, log, roots
 
 
-@pytest.mark.parametrize("name", ["water_n8_cell_veto", "water_n64_cell_veto"])
+@pytest.mark.parametrize("name", ["water_n8_cell_veto", "water_n64_cell_veto", "water_n8_cell_bounding",
+                                  "water_n64_cell_bounding"])
 def test_trajectory_bit_for_bit(name):
     z, spec = load(name)
     water, log, roots = run_oracle(z, spec)
@@ -84,7 +87,8 @@ def test_square_of_the_divergence():
 
 
 def test_bounds_and_walker_inputs():
-    for name in ("water_n8_cell_veto", "water_n64_cell_veto", "water_n8_cell_boundaries"):
+    for name in ("water_n8_cell_veto", "water_n64_cell_veto", "water_n8_cell_boundaries", "water_n8_cell_bounding",
+                 "water_n64_cell_bounding"):
         z, spec = load(name)
         m, layers = spec["cells_per_side"], spec["neighbor_layers"]
         upper, lower = z["bounds_upper"], z["bounds_lower"]
