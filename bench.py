@@ -75,10 +75,12 @@ NCU = {
                 "issue_active": 0.096, "fp64_pipe_active": 0.458},
 }
 # the all-pairs water kernel (2.83 MB + 0.22 MB over 512 chains x 32 events) with the FP64 pipe's busy fraction of
-# its capture
+# its capture; the water kernel with molecular cells in steady state (one-pass metrics with the caches left warm, mean
+# of 3 launches of 512 chains x 32 events) with the FP64 pipe's busy fraction and the issue fraction of its full capture
 WATER_NCU = {"water_all_pairs": {"traffic_per_event": (2.830080e6 + 0.221952e6) / (512 * 32),
                                  "fp64_pipe_active": 0.501},
-             "water": {"traffic_per_event": (2.830080e6 + 0.221952e6) / (512 * 32), "fp64_pipe_active": 0.501}}
+             "water": {"traffic_per_event": (0.044373e6 + 0.055893e6) / (512 * 32), "traffic_caches": "warm",
+                       "fp64_pipe_active": 0.260, "issue_active": 0.078}}
 WATER_METRICS = {"water": "events/s on 1 GB300, batched water chains with the molecular cell veto",
                  "water_all_pairs": "events/s on 1 GB300, batched water chains, Coulomb factors of all pairs"}
 
@@ -800,7 +802,8 @@ def water_gpu_arm(args):
                          "peak_source": peak_kind,
                          "kernel": "jf::water_cells_kernel" if cells is not None else "jf::water_kernel",
                          "bytes_per_event": bytes_per_event,
-                         "fp64_pipe_active": WATER_NCU[args.workload]["fp64_pipe_active"]},
+                         "fp64_pipe_active": WATER_NCU[args.workload]["fp64_pipe_active"],
+                         "ncu": WATER_NCU[args.workload]},
             "cpu_baseline": cpu, "gpu_launches": args.steps, "clocks": clocks.summary()}
     print(json.dumps(line))
     if world > 1:
