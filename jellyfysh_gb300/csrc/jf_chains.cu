@@ -74,9 +74,16 @@ __device__ inline Cand cand_none() {
 }
 
 // earliest time first; equal times: lower kind, then lower target
+// the earliest time; on equal times the lower kind, then the lower target.  The quotient and remainder of a
+// candidate's time are non-negative (never -0.0, as Python's divmod gives) or +inf, so their IEEE bit patterns order
+// as the values do: the comparison runs on integers, off GB300's scarce FP64 pipe.
 __device__ inline bool cand_better(const Cand &a, const Cand &b) {
-    if (time_lt(a.q, a.r, b.q, b.r)) return true;
-    if (time_lt(b.q, b.r, a.q, a.r)) return false;
+    const unsigned long long aq = (unsigned long long)__double_as_longlong(a.q);
+    const unsigned long long bq = (unsigned long long)__double_as_longlong(b.q);
+    if (aq != bq) return aq < bq;
+    const unsigned long long ar = (unsigned long long)__double_as_longlong(a.r);
+    const unsigned long long br = (unsigned long long)__double_as_longlong(b.r);
+    if (ar != br) return ar < br;
     if (a.kind != b.kind) return a.kind < b.kind;
     return a.target < b.target;
 }
@@ -135,6 +142,11 @@ struct WarpState {
     // the merged-image thinning derivative of the event against unit real_target, when the warp computed it
     double real_value = 0.0;
     int real_target = -1;
+    // cell-veto draws solved ahead by the lanes of a chain's group (coulomb_group_kernel): the first event they
+    // cover (-1: none), and the direction and signed charge factor they assumed
+    long long spec_base = -1;
+    int spec_d = -1;
+    double spec_factor = 0.0;
 };
 
 struct RunArgs {
@@ -1537,15 +1549,81 @@ __device__ inline Cand group_argmin(Cand c, unsigned mask) {
     return c;
 }
 
+// The cell veto's draws of the next GW events of a chain, one event a lane (the Walker sample and the potential
+// change keyed by the event index, abstracts/cell_veto_event_handler.py:200-238): they depend on the event, the
+// direction and the active unit's charge factor only, so the group's lanes solve them ahead in one pass while
+// the chain keeps its direction and charge; the event then takes its lane's relative cell, bounding rate and time
+// displacement.  Lane glane holds event w.spec_base + glane.
+struct VetoAhead {
+    double dt = 0.0, rate = 0.0;
+    int rc = 0;
+};
+
+template <int GW>
+__device__ inline void group_veto_ahead(const ChainDev &ch, const SpeciesDev &sp, WarpState &w, int glane,
+                                        int leader, unsigned mask, long long ev, int d, double charge_factor, int which,
+                                        VetoAhead &ahead) {
+    // the signed factor decides the table (upper or lower bounds) as well as the magnitude
+    const double signed_factor = which == 0 ? charge_factor : -charge_factor;
+    const bool fresh = w.spec_base >= 0 && ev - w.spec_base < GW && w.spec_d == d && w.spec_factor == signed_factor;
+    if (fresh) return;  // uniform over the group: every lane reads the same shared state
+    __syncwarp(mask);
+    const long long e = ev + glane;
+    const WalkerDev &wk = sp.walker[which][d];
+    const double total_rate = wk.total_rate * charge_factor;
+    const int k = (int)randbelow(draw(ch.key, (uint64_t)e, kRngVetoChoice, 0), (uint32_t)wk.size);
+    const double u = wk.mean_rate * uniform53(draw(ch.key, (uint64_t)e, kRngVetoUniform, 0));
+    ahead.rc = (u <= wk.first_rate[k]) ? wk.first_item[k] : wk.second_item[k];
+    ahead.rate = (which == 0 ? sp.bound_upper[ahead.rc * 3 + d] : sp.bound_lower[ahead.rc * 3 + d]) * charge_factor;
+    ahead.dt = expovariate(draw(ch.key, (uint64_t)e, kRngVetoTime, 0), ch.beta) / mul_speed(ch, total_rate);
+    __syncwarp(mask);
+    if (glane == 0) {
+        w.spec_base = ev;
+        w.spec_d = d;
+        w.spec_factor = signed_factor;
+    }
+    __syncwarp(mask);
+}
+
+// the single candidates of the event (single_candidates with the cell veto solved ahead by the group)
+template <int GW>
+__device__ inline int group_single_candidates(const RunArgs &A, const ChainDev &ch, const SpeciesDev &sp,
+                                              WarpState &w, int glane, int leader, unsigned mask, long long ev,
+                                              VetoAhead &ahead, Cand &best) {
+    const int d = w.direction;
+    double charge_factor = (charge_of(A, ch, w.active) * 1.0) / 1.0;
+    int which = 0;
+    if (!(charge_factor > 0.0)) {
+        charge_factor *= -1.0;
+        which = 1;
+    }
+    group_veto_ahead<GW>(ch, sp, w, glane, leader, mask, ev, d, charge_factor, which, ahead);
+    const int k = (int)(ev - w.spec_base);
+    const double dt = __shfl_sync(mask, ahead.dt, leader + k);
+    const double rate = __shfl_sync(mask, ahead.rate, leader + k);
+    const int rc = __shfl_sync(mask, ahead.rc, leader + k);
+    if (glane != 0) return JFGPU_STATUS_OK;
+    if (!(rate > 0.0)) return JFGPU_STATUS_ASSERTION;
+    const int target_cell = translate_cell(A.view, ch, w.occ_cell, rc);
+    offer(best, w.ts_q, w.ts_r, dt, JFGPU_EV_CELL_VETO, -1, target_cell, rate);
+    int ax[3];
+    cell_axes(ch, w.occ_cell, ax);
+    boundary_and_end(A.view, ch, d, ax[d], w.pa[d], w.ts_q, w.ts_r, w.eoc_q, w.eoc_r, w.eoc_new, best);
+    return JFGPU_STATUS_OK;
+}
+
 // the candidates of a chain's event over the GW lanes of its group (mask: the lanes of every group that calls it)
 template <int GW>
 __device__ inline int group_screened_candidates(const RunArgs &A, const ChainDev &ch, const SpeciesDev &sp,
-                                                const WarpState &w, int glane, int leader, unsigned mask, Cand &best,
-                                                int &counted) {
+                                                WarpState &w, int glane, int leader, unsigned mask, Cand &best,
+                                                int &counted, VetoAhead &ahead) {
     const long long ev = w.events;
     int status = JFGPU_STATUS_OK;
     best = cand_none();
-    if (glane == 0) status = single_candidates_ool(A, ch, sp, w, w.occ_cell, ev, best);
+    if (ch.far == JFGPU_FAR_CELL_VETO)
+        status = group_single_candidates<GW>(A, ch, sp, w, glane, leader, mask, ev, ahead, best);
+    else if (glane == 0)
+        status = single_candidates_ool(A, ch, sp, w, w.occ_cell, ev, best);
     double reach = glane == 0 ? time_sub(best.q, best.r, w.ts_q, w.ts_r) * ch.speed : 0.0;
     reach = __shfl_sync(mask, reach, leader);
     const float bound = (float)reach * (1.0f + 1.0f / 1024.0f) + ch.screen_abs32;
@@ -1668,9 +1746,11 @@ __global__ void __launch_bounds__(256, JF_CHAIN_MIN_BLOCKS) coulomb_group_kernel
         w.status = g.status;
         w.stop = 0;
         w.real_target = -1;
+        w.spec_base = -1;
         load_pos(A, ch, w.active, w.pa);
     }
     __syncwarp();
+    VetoAhead ahead;
     const long long start_events = exists ? w.events : 0;
     for (long long e = 0; e < A.max_events; ++e) {
         bool live = exists && w.status == JFGPU_STATUS_OK && !w.stop;
@@ -1684,7 +1764,8 @@ __global__ void __launch_bounds__(256, JF_CHAIN_MIN_BLOCKS) coulomb_group_kernel
         const unsigned live_mask = __ballot_sync(kFull, live);
         Cand best = cand_none();
         int status = JFGPU_STATUS_OK, counted = 0;
-        if (live) status = group_screened_candidates<GW>(A, ch, sp, w, glane, leader, live_mask, best, counted);
+        if (live)
+            status = group_screened_candidates<GW>(A, ch, sp, w, glane, leader, live_mask, best, counted, ahead);
         __syncwarp();
         if (live && glane == 0) w.candidates += counted;
         const bool stop_here = A.has_stop && !time_lt(best.q, best.r, A.stop_q, A.stop_r);
