@@ -131,7 +131,7 @@ int jfgpu_merged_image_coulomb_derivative(double alpha, int32_t fourier_cutoff, 
  * the table in a fixed file-scope device array (32 KiB, held by every GPU that loads the library until the process
  * exits), fills it on the device from the parameters passed by value, and calls no allocation routine.  Limit:
  * fourier_cutoff <= 15, larger values return JFGPU_ERROR_ARGUMENT.  Its first call on a device looks up the array's
- * device address with that device current; make that first call before any stream capture.  Every call shares the
+ * device address with that device current.  Every call shares the
  * array and rewrites it: calls that overlap on the GPU (different streams without ordering) race. */
 int jfgpu_merged_image_coulomb_derivative_noalloc(double alpha, int32_t fourier_cutoff, int32_t position_cutoff,
                                                   double prefactor, double system_length, const double *velocity,
