@@ -1701,6 +1701,30 @@ __device__ inline void group_real_rate(const RunArgs &A, const ChainDev &ch, con
     model.n_images = sp.mic_images;
     model.rows = sp.mic_terms + sp.mic_images;
     model.n_rows = sp.mic_rows;
+    const double scale = mul_speed(ch, ch.coulomb_prefactor * charge_of(A, ch, w.active) * charge_of(A, ch, t));
+    if (GW == 32 && best.kind == JFGPU_EV_CELL_VETO && sp.mic_fourier32 != nullptr) {
+        // the cell veto's thinning first in FP32: the merged-image sum with its error bound (mic_x_warp32); a
+        // rejection (the rate surely below uniform(0, bounding rate), hence also below the bounding rate: no bound
+        // warning) is taken here, the real rate stored as 0.0 for the commit's thinning; otherwise the FP64 sum
+        model.fourier32 = sp.mic_fourier32;
+        model.alpha_over_length32 = (float)sp.mic.alpha_over_length;
+        model.alpha_over_length_sq32 = (float)sp.mic.alpha_over_length_sq;
+        model.two_alpha_over_length_root_pi32 = (float)sp.mic.two_alpha_over_length_root_pi;
+        model.system_length32 = (float)sp.mic.system_length;
+        model.two_pi_over_length32 = (float)sp.mic.two_pi_over_length;
+        float value32, error32;
+        mic_x_warp32(model, (float)p[0], (float)p[1], (float)p[2], glane, value32, error32);
+        const double threshold = best.rate * uniform53(draw(ch.key, (uint64_t)w.events, kRngThin, 0));
+        const double real_upper = scale * (double)value32 + fabs(scale) * (double)error32 +
+                                  fabs(scale * (double)value32) * 0x1p-20;
+        if (real_upper < threshold * (1.0 - 0x1p-20)) {
+            if (glane == 0) {
+                w.real_value = 0.0;
+                w.real_target = t;
+            }
+            return;
+        }
+    }
     const double value = mic_x_group<GW>(model, p[0], p[1], p[2], glane, need);
     if (glane == 0) {
         w.real_value = mul_speed(ch, ch.coulomb_prefactor * charge_of(A, ch, w.active) * charge_of(A, ch, t) * value);
@@ -1708,8 +1732,10 @@ __device__ inline void group_real_rate(const RunArgs &A, const ChainDev &ch, con
     }
 }
 
+// 128 registers a thread: the replicas are few warps an SM (1024 chains of a warp each on 152 SMs), so the kernel
+// trades occupancy it does not use for fewer spills on its serial FP64 path
 template <int GW>
-__global__ void __launch_bounds__(256, JF_CHAIN_MIN_BLOCKS) coulomb_group_kernel(RunArgs A) {
+__global__ void __launch_bounds__(256, 2) coulomb_group_kernel(RunArgs A) {
     constexpr int G = 32 / GW;
     extern __shared__ unsigned char smem_raw[];
     WarpState *shared = reinterpret_cast<WarpState *>(smem_raw);

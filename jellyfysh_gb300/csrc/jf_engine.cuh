@@ -40,6 +40,7 @@ struct SpeciesDev {
     WalkerDev walker[2][3];      // [upper/lower][direction]
     const int4 *mic_terms;       // merged-image sum: real-space images, then Fourier rows (mic_x_warp)
     int mic_images, mic_rows;
+    const float *mic_fourier32;  // FP32 copy of the Fourier table (mic_x_warp32)
 };
 
 struct ChainDev {

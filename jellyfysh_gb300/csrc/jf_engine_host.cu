@@ -442,6 +442,9 @@ int build_species(JfgpuEngine *e, const JfgpuChainDesc &d, const std::vector<dou
         sp.mic_terms = dev_terms;
         sp.mic_images = (int)images.size();
         sp.mic_rows = (int)rows.size();
+        std::vector<float> table32(table.begin(), table.end());
+        sp.mic_fourier32 = device_copy(e, table32, stream, error);
+        if (error) return error;
     }
     if (d.far == JFGPU_FAR_NONE) return JFGPU_OK;
     if (d.max_occupants != 1) return JFGPU_ERROR_ARGUMENT;
