@@ -165,6 +165,7 @@ struct RunArgs {
     double stop_q, stop_r;
     int has_stop;
     int refine_limit;  // refine lists longer than this re-solve their event in FP64 (1 .. kRefineMax)
+    struct FarAhead *ahead;  // [n_chains] the far units' smallest keyed draws of each chain's next event
 };
 
 // int(x / side) along one axis (cuboid_cells.py:190-211), evaluated exactly without a division: the exact float
@@ -924,10 +925,35 @@ __device__ inline int near_first(int a, int K, int m) {
 }
 
 constexpr int kNearBatch = 4;  // cell slots each lane loads before it screens them (loads in flight)
+constexpr int kKeptMax = 96;   // kept nearby and surplus candidates a warp solves in FP32 (more: FP64 path)
 
+// The far units whose keyed pair draws of an event are small, listed before the event: every unit j of the chain
+// with u24 = (draw >> 40) < bound, in increasing j, with the top 32 bits of its draw.  The list depends only on the
+// chain's key, the event number and the number of units, so a record whose key and event match the screened event
+// is that event's list whenever it was made.  The screening kernel of an event writes `next` (the event number
+// after it, -1 for a skipped chain); far_ahead_warp lists that event while the round's FP64 kernels run.
+constexpr int kAhead = 32;        // listed units at most (one a lane)
+constexpr int kAheadExpect = 16;  // expected listed units: bound = ceil(16 * 2^24 / n)
+struct FarAhead {
+    long long event;  // the listed event (the record is void unless key matches too)
+    long long next;   // the event the next far_ahead_warp lists (-1: none)
+    uint64_t key;
+    uint32_t bound;   // every unlisted unit has u24 >= bound (0: the list overflowed)
+    int32_t count;
+    int32_t unit[kAhead];
+    uint32_t hi[kAhead];
+};
+__device__ inline uint32_t ahead_bound(int n) {
+    const uint64_t b = ((uint64_t)kAheadExpect << 24) / (uint64_t)(n > 0 ? n : 1) + 1;
+    return b < (1ull << 24) ? (uint32_t)b : (1u << 24);
+}
+
+#ifndef JF_SCREEN_REGS
+#define JF_SCREEN_REGS 72
+#endif
 template <int POT, int FAR>
-__global__ void __launch_bounds__(256, 4) screen_kernel(RunArgs A, RefineList *lists, RefineQueue queue,
-                                                        long long round, int first_round) {
+__global__ void __maxnreg__(JF_SCREEN_REGS) screen_kernel(RunArgs A, RefineList *lists, RefineQueue queue,
+                                                         long long round, int first_round) {
     const int warp = threadIdx.x >> 5;
     const int lane = threadIdx.x & 31;
     const long long local = (long long)blockIdx.x * (blockDim.x >> 5) + warp;
@@ -943,6 +969,7 @@ __global__ void __launch_bounds__(256, 4) screen_kernel(RunArgs A, RefineList *l
             list.flags = kListSkip;
             list.screened = 0;
             list.far_lookups = 0;
+            A.ahead[c].next = -1;
         }
         return;
     }
@@ -1045,24 +1072,21 @@ __global__ void __launch_bounds__(256, 4) screen_kernel(RunArgs A, RefineList *l
         const float u_low = (float)(hi >> 8) * (1.0f / 16777216.0f);
         return !(u_low > beta32 * rise * (1.0f + 1.0f / 1024.0f));
     };
+    bool kept_over = false;  // warp-uniform
     {
         // Nearby occupants from the cell-ordered mirror: one 16-byte load gives an occupant's FP32 position and
         // identifier, the cells of a row along x are contiguous, and each lane keeps kNearBatch loads in flight.
-        // Kept candidates wait in a per-warp buffer until 32 of them fill a pass of FP32 solves.
-        __shared__ float4 pending[8][64];  // per warp: kept candidates not yet solved (fewer than 32 + 32)
-        float4 *buf = pending[warp];
+        // Kept candidates wait in a per-warp buffer (dynamic shared memory, kKeptMax a warp) and are solved in FP32
+        // after the scan, so that the scan's loop carries none of the solve's registers; more than kKeptMax of them
+        // send the event to the FP64 path (the refine list's overflow).
+        extern __shared__ float4 kept_smem[];
+        float4 *buf = kept_smem + warp * kKeptMax;
         int buffered = 0;  // warp-uniform
         auto offer_kept = [&](bool kept, const float4 &pj) {
             const unsigned mask = __ballot_sync(kFull, kept);
-            if (kept) buf[buffered + __popc(mask & ((1u << lane) - 1u))] = pj;
+            const int at = buffered + __popc(mask & ((1u << lane) - 1u));
+            if (kept && at < kKeptMax) buf[at] = pj;
             buffered += __popc(mask);
-            __syncwarp();
-            if (buffered >= 32) {
-                buffered -= 32;
-                const float4 mine = buf[buffered + lane];
-                __syncwarp();
-                screen_pair(mine);
-            }
         };
         const int first_x = near_first(ax[0], K, m), first_y = near_first(ax[1], K, m),
                   first_z = near_first(ax[2], K, m);
@@ -1110,10 +1134,10 @@ __global__ void __launch_bounds__(256, 4) screen_kernel(RunArgs A, RefineList *l
             }
             offer_kept(kept, pj);
         }
-        const bool mine = lane < buffered;
-        const float4 last = mine ? buf[lane] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         __syncwarp();
-        if (mine) screen_pair(last);
+        kept_over = buffered > kKeptMax;
+        const int solved = kept_over ? kKeptMax : buffered;
+        for (int i = lane; i < solved; i += 32) screen_pair(buf[i]);
     }
     float base = fminf(warp_min_float(lane_min_unflagged(key)), t_single);
     int lookups = 0;
@@ -1133,31 +1157,37 @@ __global__ void __launch_bounds__(256, 4) screen_kernel(RunArgs A, RefineList *l
             const float *rates = sp.bound_upper32;
             const int32_t *roles = A.roles + pos_off;
             const int16_t *rel_table = A.view.rel + ch.table_offset;
-            for (int j = lane; j < n; j += 32) {
-                const uint32_t hi = draw_hi32(pair_base, (uint32_t)j);
-                if ((hi >> 8) > cut || j == active) continue;
+            auto far_unit = [&](int j, uint32_t hi) {
+                if ((hi >> 8) > cut || j == active) return;
                 ++lookups;
                 const int32_t role = roles[j];
-                if (role & (kRoleActive | kRoleSurplus)) continue;
+                if (role & (kRoleActive | kRoleSurplus)) return;
                 const int cx = role & 0xFF, cy = (role >> 8) & 0xFF, cz = (role >> 16) & 0xFF;
                 int dx = cx - ax[0], dy = cy - ax[1], dz = cz - ax[2];
                 if (dx < 0) dx += m;
                 if (dy < 0) dy += m;
                 if (dz < 0) dz += m;
                 if (((ch.near_mask >> dx) & 1ull) && ((ch.near_mask >> dy) & 1ull) && ((ch.near_mask >> dz) & 1ull))
-                    continue;
+                    return;
                 const int rc = ch.rel_is_mod ? dx + m * (dy + m * dz)
                                              : rel_table[cx * m + ax[0]] +
                                                    m * (rel_table[cy * m + ax[1]] + m * rel_table[cz * m + ax[2]]);
                 const float rate = rates[rc * 3 + d];
-                if (!(rate > 0.0f)) continue;
+                if (!(rate > 0.0f)) return;
                 const float u_low = (float)(hi >> 8) * (1.0f / 16777216.0f);
-                if (u_low > reject * rate) continue;
+                if (u_low > reject * rate) return;
                 bool flag = false;
                 const float du = expovariate32((uint64_t)hi << 32, inv_beta32, flag);
                 float t = (du / rate) / speed32;
                 if (flag) t = -1.0f;
                 if (!isinf(t)) topk_insert(key, code, t, make_code(j, kPathFar, true));
+            };
+            // every unit with u24 <= cut is listed when cut < bound: the listed units replace the draws of all n
+            const FarAhead &fa = A.ahead[c];
+            if (fa.event == (long long)ev && fa.key == ch.key && cut < fa.bound) {
+                if (lane < fa.count) far_unit(fa.unit[lane], fa.hi[lane]);
+            } else {
+                for (int j = lane; j < n; j += 32) far_unit(j, draw_hi32(pair_base, (uint32_t)j));
             }
         }
         base = fminf(base, warp_min_float(lane_min_unflagged(key)));
@@ -1174,7 +1204,7 @@ __global__ void __launch_bounds__(256, 4) screen_kernel(RunArgs A, RefineList *l
         if (take && offset < kRefineMax) list.code[offset] = code[i];
         total += __popc(mask);
     }
-    overflow = warp_max_int(overflow) || total > A.refine_limit;
+    overflow = warp_max_int(overflow) || total > A.refine_limit || kept_over;
     const int screened = warp_sum_int(count);
     lookups = warp_sum_int(lookups);
     if (lane == 0) {
@@ -1182,6 +1212,7 @@ __global__ void __launch_bounds__(256, 4) screen_kernel(RunArgs A, RefineList *l
         list.flags = overflow ? kListOverflow : 0;
         list.screened = screened;
         list.far_lookups = lookups;
+        if (far_of<FAR>(ch) == JFGPU_FAR_CELL_BOUNDING) A.ahead[c].next = (long long)ev + 1;
     }
     // the entries at the first kRefineSlots offsets go to the queues of their paths, lane q taking entry q
     __syncwarp();
@@ -1189,6 +1220,40 @@ __global__ void __launch_bounds__(256, 4) screen_kernel(RunArgs A, RefineList *l
         const int path = code_path(list.code[lane]);
         const int at = atomicAdd(queue.counts + path, 1);
         queue.entries[path * queue.stride + at] = (int32_t)(local * kRefineSlots + lane);
+    }
+}
+
+// One warp per chain: the far units of the chain's next event whose keyed pair draws have u24 < bound (the keyed
+// draws of an event depend on nothing that the event before it changes).  Extra blocks of the refine kernel run it,
+// beside the round's FP64 re-solves.
+__device__ inline void far_ahead_warp(const RunArgs &A, long long local, int lane) {
+    if (local >= A.count) return;
+    const long long c = A.first_chain + local;
+    const ChainDev &ch = A.view.chains[c];
+    FarAhead &fa = A.ahead[c];
+    const long long next = fa.next;
+    if (next < 0 || ch.far != JFGPU_FAR_CELL_BOUNDING || (fa.event == next && fa.key == ch.key)) return;
+    const uint64_t base = draw_base(ch.key, (uint64_t)next, kRngPair);
+    const uint32_t bound = ahead_bound(ch.n);
+    int total = 0;
+    for (int j0 = 0; j0 < ch.n; j0 += 32) {
+        const int j = j0 + lane;
+        uint32_t hi = 0;
+        const bool take = j < ch.n && ((hi = draw_hi32(base, (uint32_t)j)) >> 8) < bound;
+        const unsigned mask = __ballot_sync(kFull, take);
+        const int at = total + __popc(mask & ((1u << lane) - 1u));
+        if (take && at < kAhead) {
+            fa.unit[at] = j;
+            fa.hi[at] = hi;
+        }
+        total += __popc(mask);
+    }
+    __syncwarp();
+    if (lane == 0) {
+        fa.count = total < kAhead ? total : kAhead;
+        fa.bound = total <= kAhead ? bound : 0u;
+        fa.key = ch.key;
+        fa.event = next;
     }
 }
 
@@ -1225,7 +1290,14 @@ __device__ inline void load_lifting(const JfgpuChainState &g, const RunArgs &A, 
 // candidates that take the same branch of the case analysis (up to the rare FP32/FP64 disagreement).
 template <int POT, int FAR>
 __global__ void __launch_bounds__(JF_REFINE_THREADS) refine_kernel(RunArgs A, const RefineList *lists, Refined *refined,
-                                                     RefineQueue queue, long long round, int first_round) {
+                                                     RefineQueue queue, long long round, int first_round,
+                                                     unsigned ahead_block) {
+    if (FAR == JFGPU_FAR_CELL_BOUNDING && blockIdx.x >= ahead_block) {
+        // blocks from ahead_block on: the far units' draws of every chain's next event, a warp per chain
+        const int warps = JF_REFINE_THREADS / 32;
+        far_ahead_warp(A, (long long)(blockIdx.x - ahead_block) * warps + (threadIdx.x >> 5), threadIdx.x & 31);
+        return;
+    }
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     long long start = 0;
     int path = -1;
@@ -1944,6 +2016,7 @@ __device__ __noinline__ void init_chain(const EngineView &view, const ChainDev &
 }
 
 size_t refine_list_bytes() { return sizeof(RefineList); }
+size_t far_ahead_bytes() { return sizeof(FarAhead); }
 size_t refined_bytes() { return sizeof(Refined) * kRefineSlots; }
 // refine queues of up to 8 chain groups: 32 counters per group, then kPaths slices of n_chains * kRefineSlots entries
 size_t refine_queue_bytes(long long n_chains) {
@@ -2030,11 +2103,14 @@ static long long issue_rounds(const GroupLaunch *groups, int n_groups, long long
             const long long refine_blocks =
                 (count * kRefineSlots + kPaths * 31 + JF_REFINE_THREADS - 1) / JF_REFINE_THREADS;
             const long long resolve_blocks = (count + JF_RESOLVE_THREADS - 1) / JF_RESOLVE_THREADS;
-            screen_kernel<POT, FAR><<<(unsigned)screen_blocks, warps * 32, 0, G.stream>>>(G.args, G.lists, G.queue,
-                                                                                         r, first_round);
+            screen_kernel<POT, FAR><<<(unsigned)screen_blocks, warps * 32, warps * kKeptMax * sizeof(float4),
+                                      G.stream>>>(G.args, G.lists, G.queue, r, first_round);
             if (timed) timed->end(G.stream, JFGPU_KERNEL_SCREEN);
-            refine_kernel<POT, FAR><<<(unsigned)refine_blocks, JF_REFINE_THREADS, 0, G.stream>>>(G.args, G.lists, G.refined, G.queue,
-                                                                                 r, first_round);
+            // with the cell-bounding far field, further blocks list the far units' draws of every chain's next event
+            const long long ahead_blocks =
+                FAR == JFGPU_FAR_CELL_BOUNDING ? (count + JF_REFINE_THREADS / 32 - 1) / (JF_REFINE_THREADS / 32) : 0;
+            refine_kernel<POT, FAR><<<(unsigned)(refine_blocks + ahead_blocks), JF_REFINE_THREADS, 0, G.stream>>>(
+                G.args, G.lists, G.refined, G.queue, r, first_round, (unsigned)refine_blocks);
             if (timed) timed->end(G.stream, JFGPU_KERNEL_REFINE);
             resolve_kernel<POT, FAR><<<(unsigned)resolve_blocks, JF_RESOLVE_THREADS, 0, G.stream>>>(G.args, G.lists, G.refined,
                                                                                    G.queue, r, first_round);
@@ -2163,7 +2239,7 @@ static long long launch_mixed_rounds(const GroupLaunch *groups, int n_groups, lo
 cudaError_t launch_run(const EngineView &view, const JfgpuBuffers &b, long long first, long long count,
                        long long max_events, double stop_q, double stop_r, int mode, JfgpuEvent *log,
                        long long log_capacity, int uniform_potential, int uniform_far, void *lists, void *refined,
-                       void *queue, long long n_chains, const LaunchPlan &plan, long long *launches) {
+                       void *queue, void *ahead, long long n_chains, const LaunchPlan &plan, long long *launches) {
     RunArgs A;
     memset(&A, 0, sizeof(A));  // padding included: the arguments key the graph cache bytewise
     A.view = view;
@@ -2184,6 +2260,7 @@ cudaError_t launch_run(const EngineView &view, const JfgpuBuffers &b, long long 
     A.stop_r = stop_r;
     A.has_stop = isinf(stop_q) ? 0 : 1;
     A.refine_limit = plan.refine_limit < 1 ? 1 : (plan.refine_limit > kRefineMax ? kRefineMax : plan.refine_limit);
+    A.ahead = static_cast<FarAhead *>(ahead);
     int warps = plan.warps;
     if (warps < 1) warps = 1;
     if (warps > 8) warps = 8;
