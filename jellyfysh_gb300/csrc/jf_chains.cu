@@ -49,9 +49,6 @@ namespace jf {
 #ifndef JF_REFINE_THREADS
 #define JF_REFINE_THREADS 64   // threads per block of the FP64 re-solve kernel
 #endif
-#ifndef JF_RESOLVE_THREADS
-#define JF_RESOLVE_THREADS 32  // threads per block of the resolve kernel
-#endif
 
 constexpr unsigned kFull = 0xffffffffu;
 constexpr int kTopK = 4;
@@ -166,6 +163,7 @@ struct RunArgs {
     int has_stop;
     int refine_limit;  // refine lists longer than this re-solve their event in FP64 (1 .. kRefineMax)
     struct FarAhead *ahead;  // [n_chains] the far units' smallest keyed draws of each chain's next event
+    int32_t *settle;         // [n_chains] inputs of the chain's settle that have arrived this round (0 between)
 };
 
 // int(x / side) along one axis (cuboid_cells.py:190-211), evaluated exactly without a division: the exact float
@@ -873,11 +871,12 @@ __device__ inline float lane_min_unflagged(const float (&key)[kTopK]) {
 
 // ---------------------------------------------------------------------------------------------------------------
 // Mixed precision as a two-phase event.
-//   screen_kernel  (one warp per chain, FP32 only): every candidate is screened in FP32; the candidates within
-//                  (1 + 2^-10) t_min + margin, and every flagged one, go to the chain's refine list.
-//   resolve_kernel (one thread per chain, FP64): the single candidates (cell veto, cell boundary, end of chain) and
-//                  the listed candidates are solved with the reference's arithmetic, the earliest is committed and
-//                  the occupancy is updated for the next event.
+//   screen_kernel (one warp per chain, FP32 only): every candidate is screened in FP32; the candidates within
+//                 (1 + 2^-10) t_min + margin, and every flagged one, go to the chain's refine list.
+//   settle_kernel (FP64): the listed candidates (one thread each) and the single candidates (cell veto, cell
+//                 boundary, end of chain; one thread per chain) are solved with the reference's arithmetic; the
+//                 thread that completes a chain's inputs commits the earliest and updates the occupancy for the
+//                 next event.
 // The FP64 work of 32 chains thus shares each warp instruction, instead of occupying lane 0 of 32 warps, and each
 // kernel carries a small instruction footprint.  The winner and its time are the FP64 ones: the mixed path equals
 // the FP64 path event for event.
@@ -900,15 +899,16 @@ struct RefineList {
     int32_t code[kRefineMax];
 };
 
-// FP64 re-solves of the first kRefineSlots entries of every refine list, one thread per entry; the resolve kernel
-// takes the earliest of them (and solves any further entry itself)
+// FP64 re-solves of the first kRefineSlots entries of every refine list, one thread per entry; the thread that
+// settles the chain takes the earliest of them (and solves any further entry itself)
 constexpr int kRefineSlots = 4;
+constexpr int kQueueHalf = 16;  // a group's 32 queue counters: kPaths of the even rounds, then of the odd ones
 
 // Refine queue of a chain group: per screening path, the entries (local chain * kRefineSlots + slot) to re-solve.
 // counts[kPaths] sit in the group's header; entries[path][...] use the slice [lo, hi) * kRefineSlots of the group's
 // chains, so that groups on different streams never share a word.
 struct RefineQueue {
-    int32_t *counts;   // [kPaths], zeroed by the resolve kernel of the round
+    int32_t *counts;   // [2][kQueueHalf]: round r fills half r & 1, which the settle kernel of round r - 1 zeroed
     int32_t *entries;  // [kPaths][stride], offset to the group's slice
     long long stride;  // n_chains * kRefineSlots
 };
@@ -1218,13 +1218,13 @@ __global__ void __maxnreg__(JF_SCREEN_REGS) screen_kernel(RunArgs A, RefineList 
     __syncwarp();
     if (!overflow && lane < kRefineSlots && lane < total) {
         const int path = code_path(list.code[lane]);
-        const int at = atomicAdd(queue.counts + path, 1);
+        const int at = atomicAdd(queue.counts + (round & 1) * kQueueHalf + path, 1);
         queue.entries[path * queue.stride + at] = (int32_t)(local * kRefineSlots + lane);
     }
 }
 
 // One warp per chain: the far units of the chain's next event whose keyed pair draws have u24 < bound (the keyed
-// draws of an event depend on nothing that the event before it changes).  Extra blocks of the refine kernel run it,
+// draws of an event depend on nothing that the event before it changes).  Extra blocks of the settle kernel run it,
 // beside the round's FP64 re-solves.
 __device__ inline void far_ahead_warp(const RunArgs &A, long long local, int lane) {
     if (local >= A.count) return;
@@ -1286,58 +1286,6 @@ __device__ inline void load_lifting(const JfgpuChainState &g, const RunArgs &A, 
     load_pos(A, ch, w.active, w.pa);
 }
 
-// The queued entries by path: each path's range is padded to whole warps, so that the 32 threads of a warp re-solve
-// candidates that take the same branch of the case analysis (up to the rare FP32/FP64 disagreement).
-template <int POT, int FAR>
-__global__ void __launch_bounds__(JF_REFINE_THREADS) refine_kernel(RunArgs A, const RefineList *lists, Refined *refined,
-                                                     RefineQueue queue, long long round, int first_round,
-                                                     unsigned ahead_block) {
-    if (FAR == JFGPU_FAR_CELL_BOUNDING && blockIdx.x >= ahead_block) {
-        // blocks from ahead_block on: the far units' draws of every chain's next event, a warp per chain
-        const int warps = JF_REFINE_THREADS / 32;
-        far_ahead_warp(A, (long long)(blockIdx.x - ahead_block) * warps + (threadIdx.x >> 5), threadIdx.x & 31);
-        return;
-    }
-    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    long long start = 0;
-    int path = -1;
-    long long index = 0;
-#pragma unroll
-    for (int k = 0; k < kPaths; ++k) {
-        const long long n = queue.counts[k];
-        const long long padded = (n + 31) & ~31LL;
-        if (path < 0 && t < start + padded) {
-            path = k;
-            index = t - start;
-            if (index >= n) return;
-        }
-        start += padded;
-    }
-    if (path < 0) return;
-    const int entry = queue.entries[path * queue.stride + index];
-    const long long local = entry / kRefineSlots;
-    const int slot = entry % kRefineSlots;
-    Refined &out = refined[local * kRefineSlots + slot];
-    const RefineList &list = lists[local];
-    const long long c = A.first_chain + local;
-    const ChainDev &ch = A.view.chains[c];
-    const SpeciesDev &sp = A.view.species[ch.species];
-    WarpState w;
-    load_lifting(A.state[c], A, ch, w);
-    Cand best = cand_none();
-    const int code = list.code[slot];
-    const int j = code_target(code);
-    const int st = code_far(code) ? exact_cell_bounding(A, ch, sp, w, j, w.occ_cell, w.events, best)
-                                  : exact_pair<POT>(A, ch, sp, w, j, w.events, best);
-    out.q = best.q;
-    out.r = best.r;
-    out.rate = best.rate;
-    out.kind = best.kind;
-    out.target = best.target;
-    out.aux = best.aux;
-    out.status = st;
-}
-
 // every candidate of the event in FP64 by one thread (the rare overflow of a refine list)
 template <int POT, int FAR>
 __device__ __noinline__ int exact_serial(const RunArgs &A, const ChainDev &ch, const SpeciesDev &sp,
@@ -1369,27 +1317,48 @@ __device__ __noinline__ int exact_serial(const RunArgs &A, const ChainDev &ch, c
     return JFGPU_STATUS_OK;
 }
 
+// A chain's entry in the settle kernel's slots of the round: kRefineSlots FP64 re-solves, then its single candidates
+__device__ inline Refined load_refined(const Refined *p) {
+    // written by other threads of this kernel: read past L1
+    Refined r;
+    r.q = __ldcg(&p->q);
+    r.r = __ldcg(&p->r);
+    r.rate = __ldcg(&p->rate);
+    r.kind = __ldcg(&p->kind);
+    r.target = __ldcg(&p->target);
+    r.aux = __ldcg(&p->aux);
+    r.status = __ldcg(&p->status);
+    return r;
+}
+
+__device__ inline Cand refined_cand(const Refined &rf) {
+    Cand cnd;
+    cnd.q = rf.q;
+    cnd.r = rf.r;
+    cnd.kind = rf.kind;
+    cnd.target = rf.target;
+    cnd.aux = rf.aux;
+    cnd.rate = rf.rate;
+    return cnd;
+}
+
+// The end of a chain's round, by the thread that completes its inputs: the earliest of the single candidates and the
+// listed candidates (the FP64 re-solves of the first kRefineSlots entries, the others solved here) is committed and
+// the occupancy is updated for the next event.
 template <int POT, int FAR>
-__global__ void __launch_bounds__(JF_RESOLVE_THREADS) resolve_kernel(RunArgs A, const RefineList *lists, const Refined *refined,
-                                                     RefineQueue queue, long long round, int first_round) {
-    const long long local = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (local < kPaths) queue.counts[local] = 0;  // the refine kernel of this round has consumed the queue
-    if (local >= A.count) return;
-    const long long c = A.first_chain + local;
+__device__ inline void settle_chain(const RunArgs &A, const RefineList &list, const Refined *slots, long long c,
+                                    long long round) {
     const ChainDev &ch = A.view.chains[c];
     const SpeciesDev &sp = A.view.species[ch.species];
     JfgpuChainState &g = A.state[c];
-    if (g.status != JFGPU_STATUS_OK || (!first_round && g.stopped)) return;
-    const RefineList &list = lists[local];
-    if (list.flags & kListSkip) return;
     WarpState w;
     load_lifting(g, A, ch, w);
     w.candidates += list.screened;
     w.refined += list.count;
     w.far_lookups += list.far_lookups;
-
-    Cand best = cand_none();
-    int st = single_candidates(A, ch, sp, w, w.occ_cell, w.events, best);
+    const Refined singles = load_refined(slots + kRefineSlots);
+    Cand best = refined_cand(singles);
+    int st = singles.status;
     if (!st) {
         // the rare serial re-solves call out of line with a copy of the lifting state, so that the state itself is
         // never addressed and stays in registers
@@ -1399,17 +1368,11 @@ __global__ void __launch_bounds__(JF_RESOLVE_THREADS) resolve_kernel(RunArgs A, 
             if (potential_of<POT>(ch) != JFGPU_POT_COULOMB) w.fallbacks += 1;
         } else {
             for (int i = 0; i < list.count && i < kRefineSlots && !st; ++i) {
-                const Refined &rf = refined[local * kRefineSlots + i];
+                const Refined rf = load_refined(slots + i);
                 if (rf.status) {
                     st = rf.status;
                 } else if (rf.kind != (1 << 30)) {
-                    Cand cnd;
-                    cnd.q = rf.q;
-                    cnd.r = rf.r;
-                    cnd.kind = rf.kind;
-                    cnd.target = rf.target;
-                    cnd.aux = rf.aux;
-                    cnd.rate = rf.rate;
+                    const Cand cnd = refined_cand(rf);
                     if (cand_better(cnd, best)) best = cnd;
                 }
             }
@@ -1458,6 +1421,111 @@ __global__ void __launch_bounds__(JF_RESOLVE_THREADS) resolve_kernel(RunArgs A, 
     g.n_surplus = w.n_surplus;
     g.status = w.status;
     g.stopped = w.stop;
+}
+
+// One of a chain's inputs is in its slot: true for the thread that brings the last one, which settles the chain.
+// The count of a chain's inputs is its queued re-solves plus its own thread's single candidates.  Every increment
+// releases its thread's slot and the one that completes the count acquires them all; that thread resets the counter
+// for the next round.
+__device__ inline bool arrive(const RunArgs &A, const RefineList &list, long long c) {
+    const int queued = (list.flags & kListOverflow) ? 0 : (list.count < kRefineSlots ? list.count : kRefineSlots);
+    int prior;
+    // release: this thread's slot is visible before its increment; acquire: the last increment sees every slot
+    asm volatile("atom.acq_rel.gpu.global.add.s32 %0, [%1], 1;" : "=r"(prior) : "l"(A.settle + c) : "memory");
+    if (prior != queued) return false;
+    A.settle[c] = 0;
+    return true;
+}
+
+// The settle kernel of a round, three kinds of blocks:
+//   [0, chain_block)            the FP64 re-solves of the queued entries, one thread each, by screening path: each
+//                               path's range is padded to whole warps, so that the 32 threads of a warp re-solve
+//                               candidates that take the same branch of the case analysis (up to the rare FP32/FP64
+//                               disagreement);
+//   [chain_block, ahead_block)  one thread per chain: its single candidates (cell veto, cell boundary, end of chain);
+//   [ahead_block, ...)          with the cell-bounding far field, a warp per chain lists the far units' draws of its
+//                               next event (far_ahead_warp).
+// Each chain settles (settle_chain) as soon as its own inputs are there, not after every chain's re-solves.  The
+// queue counters of the round are read here; the other half of the double-buffered counters, which the next
+// round's screening fills, is zeroed here.
+template <int POT, int FAR>
+__global__ void __maxnreg__(128) settle_kernel(RunArgs A, const RefineList *lists, Refined *refined,
+                                                                   RefineQueue queue, long long round,
+                                                                   int first_round, unsigned chain_block,
+                                                                   unsigned ahead_block) {
+    if (FAR == JFGPU_FAR_CELL_BOUNDING && blockIdx.x >= ahead_block) {
+        const int warps = JF_REFINE_THREADS / 32;
+        far_ahead_warp(A, (long long)(blockIdx.x - ahead_block) * warps + (threadIdx.x >> 5), threadIdx.x & 31);
+        return;
+    }
+    long long local;  // the chain of this thread's input
+    if (blockIdx.x >= chain_block) {
+        local = (long long)(blockIdx.x - chain_block) * blockDim.x + threadIdx.x;
+        if (local < kPaths) queue.counts[((round + 1) & 1) * kQueueHalf + local] = 0;
+        if (local >= A.count) return;
+        const long long c = A.first_chain + local;
+        const ChainDev &ch = A.view.chains[c];
+        const SpeciesDev &sp = A.view.species[ch.species];
+        const JfgpuChainState &g = A.state[c];
+        if (g.status != JFGPU_STATUS_OK || (!first_round && g.stopped)) return;
+        const RefineList &list = lists[local];
+        if (list.flags & kListSkip) return;
+        WarpState w;
+        load_lifting(g, A, ch, w);
+        Cand best = cand_none();
+        const int st = single_candidates(A, ch, sp, w, w.occ_cell, w.events, best);
+        Refined &out = refined[local * (kRefineSlots + 1) + kRefineSlots];
+        out.q = best.q;
+        out.r = best.r;
+        out.rate = best.rate;
+        out.kind = best.kind;
+        out.target = best.target;
+        out.aux = best.aux;
+        out.status = st;
+    } else {
+        const int32_t *counts = queue.counts + (round & 1) * kQueueHalf;
+        const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+        long long start = 0;
+        int path = -1;
+        long long index = 0;
+#pragma unroll
+        for (int k = 0; k < kPaths; ++k) {
+            const long long n = counts[k];
+            const long long padded = (n + 31) & ~31LL;
+            if (path < 0 && t < start + padded) {
+                path = k;
+                index = t - start;
+                if (index >= n) return;
+            }
+            start += padded;
+        }
+        if (path < 0) return;
+        const int entry = queue.entries[path * queue.stride + index];
+        local = entry / kRefineSlots;
+        const int slot = entry % kRefineSlots;
+        Refined &out = refined[local * (kRefineSlots + 1) + slot];
+        const RefineList &list = lists[local];
+        const long long c = A.first_chain + local;
+        const ChainDev &ch = A.view.chains[c];
+        const SpeciesDev &sp = A.view.species[ch.species];
+        WarpState w;
+        load_lifting(A.state[c], A, ch, w);
+        Cand best = cand_none();
+        const int code = list.code[slot];
+        const int j = code_target(code);
+        const int st = code_far(code) ? exact_cell_bounding(A, ch, sp, w, j, w.occ_cell, w.events, best)
+                                      : exact_pair<POT>(A, ch, sp, w, j, w.events, best);
+        out.q = best.q;
+        out.r = best.r;
+        out.rate = best.rate;
+        out.kind = best.kind;
+        out.target = best.target;
+        out.aux = best.aux;
+        out.status = st;
+    }
+    const long long c = A.first_chain + local;
+    if (arrive(A, lists[local], c))
+        settle_chain<POT, FAR>(A, lists[local], refined + local * (kRefineSlots + 1), c, round);
 }
 
 #ifndef JF_CHAIN_MIN_BLOCKS
@@ -2017,7 +2085,7 @@ __device__ __noinline__ void init_chain(const EngineView &view, const ChainDev &
 
 size_t refine_list_bytes() { return sizeof(RefineList); }
 size_t far_ahead_bytes() { return sizeof(FarAhead); }
-size_t refined_bytes() { return sizeof(Refined) * kRefineSlots; }
+size_t refined_bytes() { return sizeof(Refined) * (kRefineSlots + 1); }
 // refine queues of up to 8 chain groups: 32 counters per group, then kPaths slices of n_chains * kRefineSlots entries
 size_t refine_queue_bytes(long long n_chains) {
     return sizeof(int32_t) * (8 * 32 + (size_t)kPaths * (size_t)n_chains * kRefineSlots);
@@ -2083,10 +2151,10 @@ struct GroupLaunch {
     cudaStream_t stream;
 };
 
-// Rounds [r0, r0 + n) of the mixed mode: per round the screening, the FP64 re-solves and the resolve kernel of every
-// group, issued round by round so that the groups' streams advance together; `clock` (may be null) brackets the
-// rounds it samples.  The round index reaches the kernels for the event log only; `first_round` marks round 0 of a
-// run call, where chains stopped by an earlier call start again.
+// Rounds [r0, r0 + n) of the mixed mode: per round the screening and the settle kernel of every group, issued round
+// by round so that the groups' streams advance together; `clock` (may be null) brackets the rounds it samples.  The
+// round index reaches the kernels for the event log and the parity of the queue counters; `first_round` marks round
+// 0 of a run call, where chains stopped by an earlier call start again.
 template <int POT, int FAR>
 static long long issue_rounds(const GroupLaunch *groups, int n_groups, long long r0, long long n, int warps,
                               KernelClock *clock) {
@@ -2099,23 +2167,22 @@ static long long issue_rounds(const GroupLaunch *groups, int n_groups, long long
             if (timed) timed->begin(G.stream);
             const long long count = G.args.count;
             const long long screen_blocks = (count + warps - 1) / warps;
-            // every queued entry plus the padding of each path to whole warps
+            // settle blocks: every queued entry plus the padding of each path to whole warps, a thread per chain, and
+            // with the cell-bounding far field a warp per chain for the far units' draws of its next event
             const long long refine_blocks =
                 (count * kRefineSlots + kPaths * 31 + JF_REFINE_THREADS - 1) / JF_REFINE_THREADS;
-            const long long resolve_blocks = (count + JF_RESOLVE_THREADS - 1) / JF_RESOLVE_THREADS;
+            const long long chain_blocks = (count + JF_REFINE_THREADS - 1) / JF_REFINE_THREADS;
+            const long long ahead_blocks =
+                FAR == JFGPU_FAR_CELL_BOUNDING ? (count + JF_REFINE_THREADS / 32 - 1) / (JF_REFINE_THREADS / 32) : 0;
             screen_kernel<POT, FAR><<<(unsigned)screen_blocks, warps * 32, warps * kKeptMax * sizeof(float4),
                                       G.stream>>>(G.args, G.lists, G.queue, r, first_round);
             if (timed) timed->end(G.stream, JFGPU_KERNEL_SCREEN);
-            // with the cell-bounding far field, further blocks list the far units' draws of every chain's next event
-            const long long ahead_blocks =
-                FAR == JFGPU_FAR_CELL_BOUNDING ? (count + JF_REFINE_THREADS / 32 - 1) / (JF_REFINE_THREADS / 32) : 0;
-            refine_kernel<POT, FAR><<<(unsigned)(refine_blocks + ahead_blocks), JF_REFINE_THREADS, 0, G.stream>>>(
-                G.args, G.lists, G.refined, G.queue, r, first_round, (unsigned)refine_blocks);
-            if (timed) timed->end(G.stream, JFGPU_KERNEL_REFINE);
-            resolve_kernel<POT, FAR><<<(unsigned)resolve_blocks, JF_RESOLVE_THREADS, 0, G.stream>>>(G.args, G.lists, G.refined,
-                                                                                   G.queue, r, first_round);
+            settle_kernel<POT, FAR>
+                <<<(unsigned)(refine_blocks + chain_blocks + ahead_blocks), JF_REFINE_THREADS, 0, G.stream>>>(
+                    G.args, G.lists, G.refined, G.queue, r, first_round, (unsigned)refine_blocks,
+                    (unsigned)(refine_blocks + chain_blocks));
             if (timed) timed->end(G.stream, JFGPU_KERNEL_RESOLVE);
-            launches += 3;
+            launches += 2;
         }
     }
     return launches;
@@ -2179,7 +2246,7 @@ template <int POT, int FAR>
 static long long replay_rounds(const GroupLaunch &group, long long r0, long long n, int warps, const LaunchPlan &plan,
                                GraphCache *cache, SegmentKey key) {
     key.rounds = n;
-    key.first = r0 == 0 ? 1 : 0;
+    key.first = (r0 == 0 ? 1 : 0) | (int)((r0 & 1) << 1);  // the first round, and the parity of the queue counters
     GroupLaunch G = group;
     G.stream = cache->stream;
     cudaGraphExec_t exec = cache->find(key);
@@ -2207,7 +2274,7 @@ static long long replay_rounds(const GroupLaunch &group, long long r0, long long
     cudaGraphLaunch(exec, cache->stream);
     cudaEventRecord(cache->join, cache->stream);
     cudaStreamWaitEvent(group.stream, cache->join, 0);
-    return 3 * n;
+    return 2 * n;
 }
 
 // All rounds of a run call.  One chain group without an event log: graph segments (with timing on, every sampled
@@ -2239,7 +2306,8 @@ static long long launch_mixed_rounds(const GroupLaunch *groups, int n_groups, lo
 cudaError_t launch_run(const EngineView &view, const JfgpuBuffers &b, long long first, long long count,
                        long long max_events, double stop_q, double stop_r, int mode, JfgpuEvent *log,
                        long long log_capacity, int uniform_potential, int uniform_far, void *lists, void *refined,
-                       void *queue, void *ahead, long long n_chains, const LaunchPlan &plan, long long *launches) {
+                       void *queue, void *ahead, void *settle, long long n_chains, const LaunchPlan &plan,
+                       long long *launches) {
     RunArgs A;
     memset(&A, 0, sizeof(A));  // padding included: the arguments key the graph cache bytewise
     A.view = view;
@@ -2261,6 +2329,7 @@ cudaError_t launch_run(const EngineView &view, const JfgpuBuffers &b, long long 
     A.has_stop = isinf(stop_q) ? 0 : 1;
     A.refine_limit = plan.refine_limit < 1 ? 1 : (plan.refine_limit > kRefineMax ? kRefineMax : plan.refine_limit);
     A.ahead = static_cast<FarAhead *>(ahead);
+    A.settle = static_cast<int32_t *>(settle);
     int warps = plan.warps;
     if (warps < 1) warps = 1;
     if (warps > 8) warps = 8;
@@ -2288,7 +2357,7 @@ cudaError_t launch_run(const EngineView &view, const JfgpuBuffers &b, long long 
             G.args.count = hi - lo;
             G.args.log = nullptr;
             G.lists = static_cast<RefineList *>(lists) + lo;
-            G.refined = static_cast<Refined *>(refined) + lo * kRefineSlots;
+            G.refined = static_cast<Refined *>(refined) + lo * (kRefineSlots + 1);
             G.queue.counts = static_cast<int32_t *>(queue) + 32 * g;
             G.queue.entries = static_cast<int32_t *>(queue) + 8 * 32 + (first + lo) * kRefineSlots;
             G.queue.stride = n_chains * kRefineSlots;

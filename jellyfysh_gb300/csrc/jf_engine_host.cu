@@ -27,7 +27,8 @@ cudaError_t launch_mirror(const EngineView &view, const JfgpuBuffers &b, long lo
 cudaError_t launch_run(const EngineView &view, const JfgpuBuffers &b, long long first, long long count,
                        long long max_events, double stop_q, double stop_r, int mode, JfgpuEvent *log,
                        long long log_capacity, int uniform_potential, int uniform_far, void *lists, void *refined,
-                       void *queue, void *ahead, long long n_chains, const LaunchPlan &plan, long long *launches);
+                       void *queue, void *ahead, void *settle, long long n_chains, const LaunchPlan &plan,
+                       long long *launches);
 size_t refine_list_bytes();
 size_t far_ahead_bytes();
 size_t refined_bytes();
@@ -121,6 +122,7 @@ struct JfgpuEngine {
     void *refined = nullptr;       // per-chain FP64 re-solves of the first list entries
     void *refine_queue = nullptr;  // the re-solves queued by screening path
     void *far_ahead = nullptr;     // per chain: the far units' smallest keyed draws of its next event
+    void *settle = nullptr;        // per chain: inputs of its settle that have arrived in the running round
     int groups = 1;                // chain groups of the mixed mode, each on a stream of its own
     cudaStream_t group_streams[8] = {};
     cudaEvent_t fork = nullptr, join[8] = {};
@@ -732,6 +734,8 @@ int jfgpu_engine_create(const JfgpuChainDesc *chains, int64_t n_chains, void *st
         e->refine_queue = device_copy(e, queue, stream, error);
         std::vector<unsigned char> ahead(far_ahead_bytes() * (size_t)n_chains, 0);  // zero: no listed event
         e->far_ahead = device_copy(e, ahead, stream, error);
+        std::vector<int32_t> settle((size_t)n_chains, 0);
+        e->settle = device_copy(e, settle, stream, error);
         if (!error && cudaStreamSynchronize(stream) != cudaSuccess) error = JFGPU_ERROR_CUDA;
     }
     if (error) {
@@ -913,6 +917,7 @@ int jfgpu_chains_run(JfgpuEngine *e, const JfgpuBuffers *b, int64_t first, int64
     long long launches = 0;
     cudaError_t err = launch_run(e->view, *b, first, count, max_events, stop_q, stop_r, mode, log, log_capacity,
                                  potential, far, e->refine_lists, e->refined, e->refine_queue, e->far_ahead,
+                                 e->settle,
                                  (long long)e->chains.size(), make_plan(e, stream_ptr), &launches);
     e->launches += launches;
     return err == cudaSuccess ? JFGPU_OK : JFGPU_ERROR_CUDA;

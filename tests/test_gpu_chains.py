@@ -133,10 +133,10 @@ def test_chain_groups_and_kernel_timing_leave_results_unchanged():
         results[label] = (batch.positions(), batch.state())
         if label == "grouped":
             times = batch.kernel_times()
-            for kind in ("screen", "refine", "resolve"):
+            for kind in ("screen", "resolve"):  # the settle kernel is timed as "resolve"
                 assert times[kind]["launches"] == 4 * events, (kind, times[kind])
                 assert times[kind]["ms"] > 0.0
-            assert times["chains"]["launches"] == 0
+            assert times["refine"]["launches"] == 0 and times["chains"]["launches"] == 0
         if label == "sampled":  # rounds 0, 7, 14, ... of each call are timed, the others replayed from graphs
             times = batch.kernel_times()
             sampled = sum((part + 6) // 7 for part in (events // 3, events // 3, events - 2 * (events // 3)))
