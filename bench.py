@@ -62,13 +62,13 @@ CPU_SECONDS = 10.0  # wall time of the CPU baseline sample
 TIMING_STRIDE = 16  # event rounds between two rounds bracketed by per-kernel CUDA events
 # DRAM traffic of the dominant kernel per event, from the ncu captures summarised under profiles/: the screening
 # kernel of the Lennard-Jones workload in steady state (one-pass metrics with the caches left warm, mean of 20
-# launches: 8.07 MB read + 3.97 MB written per launch of 4096 events), with the issue and pipe fractions of its full
+# launches: 7.46 MB read + 3.26 MB written per launch of 4096 events), with the issue and pipe fractions of its full
 # capture; the hard-sphere screening kernel (a cold-cache capture: 33.78 MB + 0.03 MB per launch of 4096 events); the
 # Coulomb replica kernel (2.53 MB + 0.13 MB per launch of 1024 chains x 8 events) with its FP64 pipe's busy fraction
 NCU = {
-    "lennard_jones": {"traffic_per_event": (8.066662e6 + 3.968077e6) / 4096, "traffic_caches": "warm",
-                      "issue_active": 0.514, "fma_pipe_active": 0.174, "alu_pipe_active": 0.460,
-                      "fp64_pipe_active": 0.036},
+    "lennard_jones": {"traffic_per_event": (7.458240e6 + 3.261158e6) / 4096, "traffic_caches": "warm",
+                      "issue_active": 0.524, "fma_pipe_active": 0.199, "alu_pipe_active": 0.411,
+                      "fp64_pipe_active": 0.052},
     "hard_spheres": {"traffic_per_event": (33.783296e6 + 0.034304e6) / 4096, "traffic_caches": "cold",
                      "issue_active": 0.276, "fma_pipe_active": 0.077, "alu_pipe_active": 0.170},
     "coulomb": {"traffic_per_event": (2.525440e6 + 0.129024e6) / (1024 * 8), "traffic_caches": "cold",
@@ -562,8 +562,9 @@ def gpu_arm(args):
     coulomb = args.workload == "coulomb"
     dominant = kernel_times["chains" if coulomb else "screen"]
     dominant_launches = max(dominant["launches"], 1)  # the timed launches
-    # three kernels per event round and chain group (mixed rounds); one launch per step (FP64 kernel)
-    events_per_launch = events_done / max(launches if coulomb else launches / 3, 1)
+    # two kernels per event round and chain group (mixed rounds: screening and settle); one launch per step (FP64
+    # kernel)
+    events_per_launch = events_done / max(launches if coulomb else launches / 2, 1)
     nb = candidates / max(events_done, 1)
     # nearby cells scanned per event, averaged over the chains (each chain commits one event per round)
     near_cells = float(np.mean([_workloads.near_cells(spec) for spec in specs]))

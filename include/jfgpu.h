@@ -523,8 +523,9 @@ int64_t jfgpu_engine_launch_count(const JfgpuEngine *engine);
 
 /* kernel kinds of jfgpu_engine_kernel_times */
 #define JFGPU_KERNEL_SCREEN 0          /* FP32 screening of every candidate (one warp per chain) */
-#define JFGPU_KERNEL_REFINE 1          /* FP64 re-solve of the listed near-winners */
-#define JFGPU_KERNEL_RESOLVE 2         /* single candidates, argmin, commit and occupancy update */
+#define JFGPU_KERNEL_REFINE 1          /* not launched: the settle kernel runs the FP64 re-solves */
+#define JFGPU_KERNEL_RESOLVE 2         /* the settle kernel: FP64 re-solves of the listed near-winners, single
+                                          candidates, argmin, commit and occupancy update */
 #define JFGPU_KERNEL_CHAINS 3          /* the FP64 event loop of JFGPU_MODE_EXACT */
 #define JFGPU_KERNEL_INIT 4            /* chain start */
 #define JFGPU_KERNEL_OBSERVE 5         /* observables of jfgpu_chains_observe */

@@ -1,7 +1,7 @@
 """Launch-shape autotuner of the mixed-precision event rounds.
 
-A round is three launches (FP32 screen with one warp per chain, FP64 re-solves, resolve); their shape is the number
-of warps per screening block and the number of chain groups on streams of their own.  The best shape depends on the
+A round is two launches (FP32 screen with one warp per chain; the settle kernel's FP64 re-solves and commits); their
+shape is the number of warps per screening block and the number of chain groups on streams of their own.  The best shape depends on the
 batch (number of chains, their N and neighbourhood sizes, the far field): ``tune`` times every candidate shape on the
 batch itself for a few event rounds and keeps the fastest.  The batch's device state is saved before and restored
 after the timing, so tuning changes no chain: the results do not depend on the launch shape in any case (every shape
