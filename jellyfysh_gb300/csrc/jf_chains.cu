@@ -924,7 +924,10 @@ __device__ inline int near_first(int a, int K, int m) {
     return first < 0 ? first + m : first;
 }
 
-constexpr int kNearBatch = 4;  // cell slots each lane loads before it screens them (loads in flight)
+#ifndef JF_NEAR_BATCH
+#define JF_NEAR_BATCH 4
+#endif
+constexpr int kNearBatch = JF_NEAR_BATCH;  // cell slots each lane loads before it screens them (loads in flight)
 constexpr int kKeptMax = 96;   // kept nearby and surplus candidates a warp solves in FP32 (more: FP64 path)
 
 // The far units whose keyed pair draws of an event are small, listed before the event: every unit j of the chain
