@@ -63,16 +63,16 @@ TIMING_STRIDE = 16  # event rounds between two rounds bracketed by per-kernel CU
 # DRAM traffic of the dominant kernel per event, from the ncu captures summarised under profiles/: the screening
 # kernel of the Lennard-Jones workload in steady state (one-pass metrics with the caches left warm, mean of 20
 # launches: 7.46 MB read + 3.26 MB written per launch of 4096 events), with the issue and pipe fractions of its full
-# capture; the hard-sphere screening kernel (a cold-cache capture: 33.78 MB + 0.03 MB per launch of 4096 events); the
-# Coulomb replica kernel (2.53 MB + 0.13 MB per launch of 1024 chains x 8 events) with its FP64 pipe's busy fraction
+# capture; the hard-sphere screening kernel (a cold-cache capture: 34.03 MB + 0.01 MB per launch of 4096 events); the
+# Coulomb replica kernel (2.45 MB + 0.02 MB per launch of 1024 chains x 8 events) with its FP64 pipe's busy fraction
 NCU = {
     "lennard_jones": {"traffic_per_event": (7.458240e6 + 3.261158e6) / 4096, "traffic_caches": "warm",
                       "issue_active": 0.524, "fma_pipe_active": 0.199, "alu_pipe_active": 0.411,
                       "fp64_pipe_active": 0.052},
-    "hard_spheres": {"traffic_per_event": (33.783296e6 + 0.034304e6) / 4096, "traffic_caches": "cold",
-                     "issue_active": 0.276, "fma_pipe_active": 0.077, "alu_pipe_active": 0.170},
-    "coulomb": {"traffic_per_event": (2.525440e6 + 0.129024e6) / (1024 * 8), "traffic_caches": "cold",
-                "issue_active": 0.096, "fp64_pipe_active": 0.458},
+    "hard_spheres": {"traffic_per_event": (34.032640e6 + 0.005888e6) / 4096, "traffic_caches": "cold",
+                     "issue_active": 0.258, "fma_pipe_active": 0.076, "alu_pipe_active": 0.158},
+    "coulomb": {"traffic_per_event": (2.450944e6 + 0.024576e6) / (1024 * 8), "traffic_caches": "cold",
+                "issue_active": 0.102, "fp64_pipe_active": 0.356},
 }
 # the all-pairs water kernel (2.83 MB + 0.22 MB over 512 chains x 32 events) with the FP64 pipe's busy fraction of
 # its capture; the water kernel with molecular cells in steady state (one-pass metrics with the caches left warm, mean
