@@ -1065,12 +1065,14 @@ __global__ void __maxnreg__(JF_SCREEN_REGS) screen_kernel(RunArgs A, RefineList 
         const float pb = d == 2 ? sv[1] : sv[2];
         const float x = fminf(fmaxf(sd, 0.0f), horizon);
         const float gap = sd - x;
-        const float r_min_sq = (gap * gap + (pa * pa + pb * pb)) * (1.0f - 1.0f / 4096.0f);
+        const float r_min_sq = __fmaf_rn(gap, gap, __fmaf_rn(pa, pa, pb * pb)) * (1.0f - 1.0f / 4096.0f);
         if (!(r_min_sq > shell32 * (1.0f + 1.0f / 4096.0f))) return true;
         if (potential_of<POT>(ch) == JFGPU_POT_HARD_SPHERE) return false;
-        const float ir2 = 1.0f / r_min_sq;
+        // the approximate reciprocal (1 ulp) and the fused products stay far inside the bound's 2^-10 margin
+        float ir2;
+        asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(ir2) : "f"(r_min_sq));
         const float ir6 = ir2 * ir2 * ir2;
-        const float rise = -((lj32.a12 * ir6 + lj32.a6) * ir6);  // |U(r_min)|, U < 0 outside the shell
+        const float rise = -(__fmaf_rn(lj32.a12, ir6, lj32.a6) * ir6);  // |U(r_min)|, U < 0 outside the shell
         const uint32_t hi = draw_hi32(pair_base, (uint32_t)__float_as_int(pj.w));
         const float u_low = (float)(hi >> 8) * (1.0f / 16777216.0f);
         return !(u_low > beta32 * rise * (1.0f + 1.0f / 1024.0f));
@@ -1473,6 +1475,12 @@ __global__ void __maxnreg__(128) settle_kernel(RunArgs A, const RefineList *list
         if (g.status != JFGPU_STATUS_OK || (!first_round && g.stopped)) return;
         const RefineList &list = lists[local];
         if (list.flags & kListSkip) return;
+        // the listed targets' FP64 positions and role words into L2 for the commit that follows their re-solves
+        for (int i = 0; i < list.count && i < kRefineSlots; ++i) {
+            const int j = code_target(list.code[i]);
+            asm volatile("prefetch.global.L2 [%0];" ::"l"(A.positions + 3 * (ch.pos_off + j)));
+            asm volatile("prefetch.global.L2 [%0];" ::"l"(A.roles + ch.pos_off + j));
+        }
         WarpState w;
         load_lifting(g, A, ch, w);
         Cand best = cand_none();
