@@ -1763,6 +1763,33 @@ __device__ inline int group_single_candidates(const RunArgs &A, const ChainDev &
     return JFGPU_STATUS_OK;
 }
 
+// The FP32 screen of a Coulomb pair candidate (the active unit at pa, keyed draws of event ev): false when its event
+// provably comes after `bound` (the displacement of the single candidates), true when it must be solved in FP64.
+__device__ inline bool coulomb_pair_screen(const RunArgs &A, const ChainDev &ch, const double *pa, long long ev, int d,
+                                           double charge_active, float bound, int j) {
+    double pj[3], s[3];
+    load_pos(A, ch, j, pj);
+    separation64(ch, pa, pj, s);
+    if (ch.diameter_sq > 0.0) {
+        float sv[3] = {(float)s[0], (float)s[1], (float)s[2]};
+        bool flag = false;
+        const float x = hs_screen(ch.diameter_sq32, d, 1.0f, sv, ch.ulp_margin32, flag);
+        if (flag || x * (1.0f - 1.0f / 4096.0f) - ch.screen_abs32 <= bound) return true;
+    }
+    const uint64_t n = draw(ch.key, (uint64_t)ev, kRngPair, (uint32_t)j) >> 11;
+    const float du = n < (1ull << 52) ? -log1pf(-(float)n * 0x1p-53f) * ch.inv_beta32
+                                      : -logf((float)((1ull << 53) - n) * 0x1p-53f) * ch.inv_beta32;
+    const float du_error = 32.f * 0x1p-24f * du;
+    double p[3];
+    permute3(s, d, p);
+    float error;
+    bool unsafe = false;
+    const float x = ipcb_x_displacement32((float)(ch.bound_prefactor * charge_active * charge_of(A, ch, j)),
+                                          (float)p[0], (float)p[1], (float)p[2], du, du_error, ch.L32, error,
+                                          unsafe);
+    return unsafe || !(x - error > bound);
+}
+
 // the candidates of a chain's event over the GW lanes of its group (mask: the lanes of every group that calls it)
 template <int GW>
 __device__ inline int group_screened_candidates(const RunArgs &A, const ChainDev &ch, const SpeciesDev &sp,
@@ -1779,36 +1806,11 @@ __device__ inline int group_screened_candidates(const RunArgs &A, const ChainDev
     reach = __shfl_sync(mask, reach, leader);
     const float bound = (float)reach * (1.0f + 1.0f / 1024.0f) + ch.screen_abs32;
     const int d = w.direction;
-    const float inv_beta32 = ch.inv_beta32;
     const double charge_active = charge_of(A, ch, w.active);
     int count = 0;
     auto screen = [&](int j) {
         ++count;
-        double pj[3], s[3];
-        load_pos(A, ch, j, pj);
-        separation64(ch, w.pa, pj, s);
-        bool solve = false;
-        if (ch.diameter_sq > 0.0) {
-            float sv[3] = {(float)s[0], (float)s[1], (float)s[2]};
-            bool flag = false;
-            const float x = hs_screen(ch.diameter_sq32, d, 1.0f, sv, ch.ulp_margin32, flag);
-            if (flag || x * (1.0f - 1.0f / 4096.0f) - ch.screen_abs32 <= bound) solve = true;
-        }
-        if (!solve) {
-            const uint64_t n = draw(ch.key, (uint64_t)ev, kRngPair, (uint32_t)j) >> 11;
-            const float du = n < (1ull << 52) ? -log1pf(-(float)n * 0x1p-53f) * inv_beta32
-                                              : -logf((float)((1ull << 53) - n) * 0x1p-53f) * inv_beta32;
-            const float du_error = 32.f * 0x1p-24f * du;
-            double p[3];
-            permute3(s, d, p);
-            float error;
-            bool unsafe = false;
-            const float x = ipcb_x_displacement32((float)(ch.bound_prefactor * charge_active * charge_of(A, ch, j)),
-                                                  (float)p[0], (float)p[1], (float)p[2], du, du_error, ch.L32, error,
-                                                  unsafe);
-            if (unsafe || !(x - error > bound)) solve = true;
-        }
-        if (solve) {
+        if (coulomb_pair_screen(A, ch, w.pa, ev, d, charge_active, bound, j)) {
             const int st = exact_pair_ool<JFGPU_POT_COULOMB>(A, ch, sp, w, j, ev, best);
             if (st) status = st;
         }
@@ -1885,6 +1887,166 @@ __device__ inline void group_real_rate(const RunArgs &A, const ChainDev &ch, con
 
 // 128 registers a thread: the replicas are few warps an SM (1024 chains of a warp each on 152 SMs), so the kernel
 // trades occupancy it does not use for fewer spills on its serial FP64 path
+constexpr int kRunNear = 64;  // nearby occupants a run of null cell-veto events keeps (more: no run)
+
+// Runs of null cell-veto events (one warp per chain).  Most events of a Coulomb chain with the cell veto move the
+// active unit to its veto time and change nothing else: the vetoed cell is empty, the veto comes before the cell
+// boundary and the end of chain, and no pair candidate comes before it.  The lanes check the next events of the
+// speculation window at once, lane k event ev + k: every lane steps through the time slices of the events before its
+// own (the reference's arithmetic, in order), then takes its event's single candidates, its vetoed cell and the FP32
+// screen of its pair candidates (an FP64 solve where the screen cannot decide).  The leading events that are null
+// are committed together, each exactly as the event loop commits it (time slice, log record, candidate count); the
+// first event that is not null is left to the event loop.  Returns the events committed; `broke` tells whether an
+// event that is not null ended the run (rather than the window or the event budget).
+__device__ inline int warp_null_run(const RunArgs &A, const ChainDev &ch, const SpeciesDev &sp, WarpState &w, int lane,
+                                    long long budget, long long log_index, long long chain_index, VetoAhead &ahead,
+                                    bool &broke) {
+    const long long ev = w.events;
+    const int d = w.direction;
+    double charge_factor = (charge_of(A, ch, w.active) * 1.0) / 1.0;
+    int which = 0;
+    if (!(charge_factor > 0.0)) {
+        charge_factor *= -1.0;
+        which = 1;
+    }
+    group_veto_ahead<32>(ch, sp, w, lane, 0, kFull, ev, d, charge_factor, which, ahead);
+    const int k0 = (int)(ev - w.spec_base);  // lane of event ev in the speculation window
+    int n_try = 32 - k0;
+    if (budget < n_try) n_try = (int)budget;
+    broke = false;
+    if (n_try < 2) return 0;
+    // the vetoed cells do not depend on the time slices: the run ends at the first one that holds a unit (a thinning)
+    const int src = k0 + (lane < n_try ? lane : 0);
+    const double rate = __shfl_sync(kFull, ahead.rate, src);
+    const int rc = __shfl_sync(kFull, ahead.rc, src);
+    const int target_cell = translate_cell(A.view, ch, w.occ_cell, rc);
+    const bool thinning = lane < n_try && A.occupancy[ch.occ_off + (long long)target_cell * ch.max_occ] >= 0;
+    const unsigned thin_mask = __ballot_sync(kFull, thinning);
+    if (thin_mask) n_try = __ffs(thin_mask);  // up to and including the first thinning, which fails below
+    // the time slices of events ev .. ev + lane, in order (time_add of the veto candidate, then time_slice); every
+    // lane steps through all n_try events so that the shuffles stay warp-wide
+    double ts_q = w.ts_q, ts_r = w.ts_r, x = w.pa[d];
+    double pre_q = 0.0, pre_r = 0.0, pre_x = 0.0, post_q = 0.0, post_r = 0.0, post_x = 0.0, dt_mine = 0.0;
+    for (int i = 0; i < n_try; ++i) {
+        const double dt = __shfl_sync(kFull, ahead.dt, k0 + i);
+        double cq, cr;
+        time_add(ts_q, ts_r, dt, cq, cr);
+        const double x_next = py_mod_near(x + ch.speed * time_sub(cq, cr, ts_q, ts_r), ch.L);
+        if (i == lane) {
+            pre_q = ts_q;
+            pre_r = ts_r;
+            pre_x = x;
+            dt_mine = dt;
+            post_q = cq;
+            post_r = cr;
+            post_x = x_next;
+        }
+        x = x_next;
+        ts_q = cq;
+        ts_r = cr;
+    }
+    bool ok = lane < n_try && !thinning && rate > 0.0 && !isinf(dt_mine);
+    int count = 0;
+    Cand best = cand_none();
+    if (ok) {
+        int ax[3];
+        cell_axes(ch, w.occ_cell, ax);
+        // the events before this one left the active unit in its cell (else the occupancy update moves it)
+        if (axis_index(A.view, ch, pre_x) != ax[d]) ok = false;
+        offer(best, pre_q, pre_r, dt_mine, JFGPU_EV_CELL_VETO, -1, target_cell, rate);
+        boundary_and_end(A.view, ch, d, ax[d], pre_x, pre_q, pre_r, w.eoc_q, w.eoc_r, w.eoc_new, best);
+        if (best.kind != JFGPU_EV_CELL_VETO || best.q != post_q || best.r != post_r) ok = false;
+        if (A.has_stop && !time_lt(post_q, post_r, A.stop_q, A.stop_r)) ok = false;
+    }
+    // the pair candidates, the same units for every event of the run: the nearby occupants (gathered once by the
+    // warp, a cell a lane) and the surplus units
+    __shared__ int near_units[8][kRunNear];
+    int *units = near_units[threadIdx.x >> 5];
+    int n_units = 0;  // warp-uniform
+    {
+        int a[3];
+        cell_axes(ch, w.occ_cell, a);
+        const int K = ch.n_res, slots = K * K * K * ch.max_occ;
+        const int32_t *occ = A.occupancy + ch.occ_off;
+        for (int base = 0; base < slots; base += 32) {
+            const int slot = base + lane;
+            int j = -1;
+            if (slot < slots) {
+                const int k = slot / ch.max_occ, ox = k % K, oy = (k / K) % K, oz = k / (K * K);
+                int cx = a[0] + ch.res[ox], cy = a[1] + ch.res[oy], cz = a[2] + ch.res[oz];
+                if (cx >= ch.m) cx -= ch.m;
+                if (cy >= ch.m) cy -= ch.m;
+                if (cz >= ch.m) cz -= ch.m;
+                j = occ[(long long)(cx + ch.m * (cy + ch.m * cz)) * ch.max_occ + slot % ch.max_occ];
+            }
+            const unsigned found = __ballot_sync(kFull, j >= 0);
+            const int at = n_units + __popc(found & ((1u << lane) - 1u));
+            if (j >= 0 && at < kRunNear) units[at] = j;
+            n_units += __popc(found);
+        }
+        __syncwarp();
+    }
+    if (n_units > kRunNear) ok = false;  // too many to keep: the event loop takes the events one by one
+    if (ok) {
+        const float bound = (float)(time_sub(post_q, post_r, pre_q, pre_r) * ch.speed) * (1.0f + 1.0f / 1024.0f) +
+                            ch.screen_abs32;
+        double pa[3] = {w.pa[0], w.pa[1], w.pa[2]};
+        pa[d] = pre_x;
+        const double charge_active = charge_of(A, ch, w.active);
+        auto screen = [&](int j) {
+            ++count;
+            if (!ok || !coulomb_pair_screen(A, ch, pa, ev + lane, d, charge_active, bound, j)) return;
+            WarpState wk = w;  // the state before this lane's event
+            wk.pa[d] = pre_x;
+            wk.ts_q = pre_q;
+            wk.ts_r = pre_r;
+            Cand pair = cand_none();
+            if (exact_pair_ool<JFGPU_POT_COULOMB>(A, ch, sp, wk, j, ev + lane, pair) || cand_better(pair, best))
+                ok = false;
+        };
+        for (int i = 0; i < n_units; ++i) screen(units[i]);
+        for (int i = 0; i < w.n_surplus; ++i) screen(A.surplus[ch.pos_off + i]);
+    }
+    const unsigned okm = __ballot_sync(kFull, ok);
+    const int run = okm == kFull ? 32 : __ffs(~okm) - 1;
+    broke = run < n_try;
+    if (run == 0) return 0;
+    const int counted = warp_sum_int(lane < run ? count : 0);
+    if (A.log && lane < run && log_index + lane < A.log_capacity) {
+        JfgpuEvent rec;
+        rec.kind = JFGPU_EV_CELL_VETO;
+        rec.moved = w.active;
+        rec.target = -1;
+        rec.accepted = 0;
+        rec.time_q = post_q;
+        rec.time_r = post_r;
+        rec.new_active = w.active;
+        rec.new_direction = d;
+        double p[3] = {w.pa[0], w.pa[1], w.pa[2]};
+        p[d] = post_x;
+        rec.x = p[0];
+        rec.y = p[1];
+        rec.z = p[2];
+        A.log[(chain_index - A.first_chain) * A.log_capacity + log_index + lane] = rec;
+    }
+    const double last_q = __shfl_sync(kFull, post_q, run - 1);
+    const double last_r = __shfl_sync(kFull, post_r, run - 1);
+    const double last_x = __shfl_sync(kFull, post_x, run - 1);
+    __syncwarp();
+    if (lane == 0) {
+        w.ts_q = last_q;
+        w.ts_r = last_r;
+        w.pa[d] = last_x;
+        w.events = ev + run;
+        w.candidates += counted;
+        store_active(A, ch, w, w.active);
+        const int st = occ_update_ool(A, ch, w);  // the activator's update of the next event (the same cell)
+        if (st) w.status = st;
+    }
+    __syncwarp();
+    return run;
+}
+
 template <int GW>
 __global__ void __launch_bounds__(256, 2) coulomb_group_kernel(RunArgs A) {
     constexpr int G = 32 / GW;
@@ -1929,6 +2091,7 @@ __global__ void __launch_bounds__(256, 2) coulomb_group_kernel(RunArgs A) {
     __syncwarp();
     VetoAhead ahead;
     const long long start_events = exists ? w.events : 0;
+    long long no_run = -1;  // an event that ended a run of null cell-veto events
     for (long long e = 0; e < A.max_events; ++e) {
         bool live = exists && w.status == JFGPU_STATUS_OK && !w.stop;
         if (!__any_sync(kFull, live)) break;
@@ -1938,6 +2101,18 @@ __global__ void __launch_bounds__(256, 2) coulomb_group_kernel(RunArgs A) {
         }
         __syncwarp();
         live = live && w.status == JFGPU_STATUS_OK;
+        if (GW == 32 && ch.far == JFGPU_FAR_CELL_VETO && live && w.events != no_run) {
+            // a run of null cell-veto events, committed together (one chain per warp: live is warp-uniform); the
+            // event that ended a run goes through the event loop without a second attempt
+            bool broke = false;
+            const int run =
+                warp_null_run(A, ch, sp, w, lane, A.max_events - e, w.events - start_events, c, ahead, broke);
+            if (broke) no_run = w.events;
+            if (run > 0) {
+                e += run - 1;
+                continue;
+            }
+        }
         const unsigned live_mask = __ballot_sync(kFull, live);
         Cand best = cand_none();
         int status = JFGPU_STATUS_OK, counted = 0;

@@ -67,7 +67,9 @@ __host__ __device__ inline double py_mod(double x, double y) {
 // float.__mod__ for x in (-y, 2y), y > 0, without fmod: fmod(x, y) is x for |x| < y and the exact x - y for
 // y <= x < 2y; the sign correction of a negative remainder then adds y with one rounding, as CPython does.
 __host__ __device__ inline double py_mod_near(double x, double y) {
-    if (x > 0.0 && x < y) return x;
+    // 0 < x < y decided on the bit patterns (positive doubles order as integers; y > 0): no FP64 compare
+    const int64_t bx = (int64_t)double_bits(x);
+    if (bx > 0 && bx < (int64_t)double_bits(y)) return x;
     if (x == 0.0) return 0.0;
     if (x < 0.0 && x > -y) return x + y;
     if (x >= y && x < 2.0 * y) {
@@ -79,6 +81,13 @@ __host__ __device__ inline double py_mod_near(double x, double y) {
 
 // divmod(x, 1.0) (CPython float_divmod with the divisor 1.0); fmod(x, 1.0) is the exact x - trunc(x)
 __host__ __device__ inline void py_divmod1(double vx, double &quotient, double &remainder) {
+    // 0 < vx < 1, decided on the bit pattern: the steps below give (+0.0, vx)
+    const int64_t bits = (int64_t)double_bits(vx);
+    if (bits > 0 && bits < 0x3FF0000000000000LL) {
+        quotient = 0.0;
+        remainder = vx;
+        return;
+    }
     double mod = fabs(vx) < 4503599627370496.0 ? vx - trunc(vx) : fmod(vx, 1.0);
     double div = vx - mod;
     if (mod != 0.0) {
