@@ -169,15 +169,18 @@ struct RunArgs {
 // int(x / side) along one axis (cuboid_cells.py:190-211), evaluated exactly without a division: the exact float
 // bounds of the cells satisfy cell_min[i] <= x <= cell_max[i] if and only if int(x / side) == i, so a multiply by
 // 1 / side guesses the index and at most a step or two against the bounds corrects it.
+// The compares are taken on the bit patterns, which order the non-negative doubles as integers (no FP64 compare):
+// x < 0, -0.0, NaN and x >= L take the division, which gives the same index as before.
 __device__ inline long long axis_index(const EngineView &v, const ChainDev &ch, double x) {
-    if (!(x >= 0.0) || !(x < ch.L)) return (long long)(x / ch.side);
+    const long long bx = (long long)double_bits(x);
+    if (bx < 0 || bx >= (long long)double_bits(ch.L)) return (long long)(x / ch.side);
     const double *lo = v.cell_min + ch.geom_offset;
     const double *hi = v.cell_max + ch.geom_offset;
     long long i = (long long)(x * ch.inv_side);
     if (i > ch.m - 1) i = ch.m - 1;
     if (i < 0) i = 0;
-    while (i > 0 && x < lo[i]) --i;
-    while (x > hi[i]) {
+    while (i > 0 && bx < (long long)double_bits(lo[i])) --i;
+    while (bx > (long long)double_bits(hi[i])) {
         if (i == ch.m - 1) return ch.m;
         ++i;
     }
