@@ -91,3 +91,39 @@ def test_batched_coulomb_replicas_against_the_oracle():
             assert np.array_equal(mixed_logs[c][field], logs[c][field]), (c, field)
     batch.close()
     mixed.close()
+
+
+def test_coulomb_null_veto_runs_in_pieces_with_stop_times():
+    """The Coulomb kernel commits runs of null cell-veto events together.  Calls of a few events (runs cut by the
+    event budget), stop times inside runs and long calls (runs cut by thinnings and by the veto window) give the
+    events, the whole chain state and the positions of the FP64 path bit for bit."""
+    from jellyfysh_gb300 import ChainBatch, ChainSpec, systems
+    rng = np.random.default_rng(45)
+    n, replicas = 32, 8
+    charges = systems.alternating_charges(n)
+    specs, positions = [], []
+    for c in range(replicas):
+        specs.append(ChainSpec(n=n, system_length=1.0, cells_per_side=8, neighbor_layers=1, potential="coulomb",
+                               far="cell_veto", hs_radius=0.05, beta=1.0, chain_time=0.7, coulomb_prefactor=1.0,
+                               bound_prefactor=1.5837, ewald_alpha=3.45, fourier_cutoff=6, position_cutoff=2,
+                               estimator_points=4, estimator_prefactor=1.0, initial_active=int(rng.integers(n)),
+                               initial_direction=int(rng.integers(3))))
+        positions.append(systems.random_sequential_addition(n, 0.05, 1.0, rng))
+    calls = [(3, None), (7, None), (200, 0.37), (1, None), (40, 0.81), (300, None), (5, 1.9), (500, None)]
+    results = {}
+    for mode in ("exact", "mixed"):
+        batch = ChainBatch(specs, positions, [charges] * replicas, seed=12)
+        logs = [batch.run(events, stop_time=stop, mode=mode, log_capacity=events) for events, stop in calls]
+        batch.check_status()
+        results[mode] = (logs, batch.state(), batch.positions())
+        batch.close()
+    (exact_logs, exact_state, exact_pos), (mixed_logs, mixed_state, mixed_pos) = results["exact"], results["mixed"]
+    for a, b in zip(exact_logs, mixed_logs):
+        for field in a.dtype.names:
+            assert np.array_equal(a[field], b[field]), field
+    # the chain itself; the counters of screened and re-solved candidates count different work in the two paths
+    for field in ("time_q", "time_r", "eoc_q", "eoc_r", "events", "active", "direction", "eoc_new_active",
+                  "occ_active", "occ_cell", "n_surplus", "status", "stopped", "lift_sum", "liftings"):
+        assert np.array_equal(exact_state[field], mixed_state[field]), field
+    assert np.array_equal(exact_pos, mixed_pos)
+    assert (exact_state["events"] > 600).all()
