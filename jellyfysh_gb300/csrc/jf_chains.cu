@@ -904,7 +904,10 @@ struct RefineList {
 
 // FP64 re-solves of the first kRefineSlots entries of every refine list, one thread per entry; the thread that
 // settles the chain takes the earliest of them (and solves any further entry itself)
-constexpr int kRefineSlots = 4;
+#ifndef JF_REFINE_SLOTS
+#define JF_REFINE_SLOTS 4
+#endif
+constexpr int kRefineSlots = JF_REFINE_SLOTS;
 constexpr int kQueueHalf = 16;  // a group's 32 queue counters: kPaths of the even rounds, then of the odd ones
 
 // Refine queue of a chain group: per screening path, the entries (local chain * kRefineSlots + slot) to re-solve.
