@@ -559,11 +559,10 @@ __device__ inline void store_active(const RunArgs &A, const ChainDev &ch, const 
     q[0] = w.pa[0];
     q[1] = w.pa[1];
     q[2] = w.pa[2];
-    float4 m = A.positions32[ch.pos_off + id];
-    m.x = (float)w.pa[0];
-    m.y = (float)w.pa[1];
-    m.z = (float)w.pa[2];
-    A.positions32[ch.pos_off + id] = m;
+    float *m = reinterpret_cast<float *>(A.positions32 + ch.pos_off + id);  // x, y, z; the charge stays
+    m[0] = (float)w.pa[0];
+    m[1] = (float)w.pa[1];
+    m[2] = (float)w.pa[2];
 }
 
 // BasicEventHandler._time_slice_unit (abstracts.py:82-95): position[d] = (position[d] + v[d] * dt) % L.  For the
@@ -579,6 +578,13 @@ __device__ inline void time_slice(const ChainDev &ch, WarpState &w, double q, do
 // commit the winner; returns a status
 __device__ JF_FLOW int commit(const RunArgs &A, const ChainDev &ch, const SpeciesDev &sp, WarpState &w, const Cand &best,
                              int active_cell, long long chain_index, long long log_index) {
+    // the data of the commit and of the occupancy update after it, requested together so that their latencies
+    // overlap the time slice: the cell's slots, and the new active unit's position and role word
+    asm volatile("prefetch.global.L1 [%0];" ::"l"(A.occupancy + ch.occ_off + (long long)active_cell * ch.max_occ));
+    if (best.target >= 0 && best.target < ch.n) {
+        asm volatile("prefetch.global.L1 [%0];" ::"l"(A.positions + 3 * (ch.pos_off + best.target)));
+        asm volatile("prefetch.global.L1 [%0];" ::"l"(A.roles + ch.pos_off + best.target));
+    }
     const long long ev = w.events;
     int moved = w.active;
     JfgpuEvent rec;
