@@ -633,13 +633,16 @@ __global__ void __launch_bounds__(256, 2) water_kernel(WaterArgs a) {
 // ---------------------------------------------------------------------------------------------------------------
 // int(x / side) along one axis: the exact cell bounds hold cell_min[i] <= x <= cell_max[i] if and only if
 // int(x / side) == i, so a multiply by 1 / side guesses the index and a step or two against the bounds corrects it
+// The compares with the cell bounds are taken on the bit patterns, which order the non-negative doubles as integers
+// (no FP64 compare); x < 0, -0.0, NaN and x >= m side take the division as before.
 __device__ inline long long water_axis_index(const WaterCells &cl, double x) {
-    if (!(x >= 0.0) || !(x < (double)cl.m * cl.side)) return (long long)(x / cl.side);
+    const long long bx = (long long)double_bits(x);
+    if (bx < 0 || !(x < (double)cl.m * cl.side)) return (long long)(x / cl.side);
     long long i = (long long)(x * cl.inv_side);
     if (i > cl.m - 1) i = cl.m - 1;
     if (i < 0) i = 0;
-    while (i > 0 && x < cl.cell_min[i]) --i;
-    while (x > cl.cell_max[i]) {
+    while (i > 0 && bx < (long long)double_bits(cl.cell_min[i])) --i;
+    while (bx > (long long)double_bits(cl.cell_max[i])) {
         if (i == cl.m - 1) return cl.m;
         ++i;
     }
