@@ -79,8 +79,8 @@ NCU = {
 # of 3 launches of 512 chains x 32 events) with the FP64 pipe's busy fraction and the issue fraction of its full capture
 WATER_NCU = {"water_all_pairs": {"traffic_per_event": (2.830080e6 + 0.221952e6) / (512 * 32),
                                  "fp64_pipe_active": 0.501},
-             "water": {"traffic_per_event": (0.044373e6 + 0.055893e6) / (512 * 32), "traffic_caches": "warm",
-                       "fp64_pipe_active": 0.260, "issue_active": 0.078}}
+             "water": {"traffic_per_event": (0.044800e6 + 0.059819e6) / (512 * 32), "traffic_caches": "warm",
+                       "fp64_pipe_active": 0.223, "issue_active": 0.079}}
 WATER_METRICS = {"water": "events/s on 1 GB300, batched water chains with the molecular cell veto",
                  "water_all_pairs": "events/s on 1 GB300, batched water chains, Coulomb factors of all pairs"}
 
