@@ -1009,6 +1009,9 @@ __global__ void __maxnreg__(JF_SCREEN_REGS) screen_kernel(RunArgs A, RefineList 
     const float rel = 1.0f + 1.0f / 1024.0f;
     const float abs_margin = ch.screen_abs32 / speed32;
     const float4 pa32 = A.positions32[pos_off + active];
+    // the chain's far-ahead record (three 128-byte lines), read by the far pass after the nearby scan
+    if (far_of<FAR>(ch) == JFGPU_FAR_CELL_BOUNDING && lane < 3)
+        asm volatile("prefetch.global.L1 [%0];" ::"l"(reinterpret_cast<const char *>(A.ahead + c) + 128 * lane));
     int ax[3];
     cell_axes(ch, occ_cell, ax);
     // single candidates in FP32 bound the threshold: the cell boundary and the end of chain
