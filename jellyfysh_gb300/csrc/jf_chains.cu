@@ -1924,6 +1924,13 @@ __device__ inline int warp_null_run(const RunArgs &A, const ChainDev &ch, const 
         charge_factor *= -1.0;
         which = 1;
     }
+#ifndef JF_RUN_REFRESH
+#define JF_RUN_REFRESH 16
+#endif
+    // a window with fewer than 32 - JF_RUN_REFRESH events left is drawn anew from this event, so that a run is not
+    // cut short by its end (the draws are pure functions of the event: the same values either way)
+    if (lane == 0 && w.spec_base >= 0 && ev - w.spec_base > JF_RUN_REFRESH) w.spec_base = -1;
+    __syncwarp();
     group_veto_ahead<32>(ch, sp, w, lane, 0, kFull, ev, d, charge_factor, which, ahead);
     const int k0 = (int)(ev - w.spec_base);  // lane of event ev in the speculation window
     int n_try = 32 - k0;
